@@ -1,0 +1,368 @@
+"""Benchmark: dense CP-ALS sweeps/s at 512^3 rank 64 on one GB300.
+
+Workload (synthetic, seeded): float32 512x512x512 tensor from a rank-64 CP
+model with N(0,1) unit-norm factor columns plus 20 dB Gaussian noise
+(tensorly_gb300.workloads.dense_cp_large); rank 64; 50 ALS sweeps per step
+(tol=0, fixed count), init='random' with seed 0.  One step = one full
+``parafac`` call.  The tensor (512 MiB f32) is larger than L2 (129 MB), so no
+L2 flush is needed between steps.
+
+Arms:
+  default            tensorly_gb300 on the GPU (precision bf16 = tensor-core
+                     MTTKRP + 3 closing f32 sweeps, or --precision native)
+  --impl reference   the NumPy restatement of TensorLy's CPU path (oracle/)
+                     on the host cores, a bounded sample of sweeps per step
+
+One JSON line on rank 0.  Under torchrun each rank runs an independent
+replica (the path does not shard); value = all ranks' sweeps / max time.
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "CP-ALS sweeps/s at 512^3 R64"
+UNIT = "sweeps/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--precision", default=os.environ.get("TLGB_BENCH_PRECISION", "bf16"),
+                   choices=["bf16", "native"])
+    p.add_argument("--size", type=int, default=512)
+    p.add_argument("--rank", type=int, default=64)
+    p.add_argument("--sweeps", type=int, default=50)
+    p.add_argument("--refine", type=int, default=3)
+    p.add_argument("--cpu-sweeps", type=int, default=2)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# ----------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for name, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(self.rows)}
+
+
+def measured_peaks():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ----------------------------------------------------------------------------- CPU arm
+def cpu_sample(x, init, rank, sweeps):
+    """Times `sweeps` ALS sweeps of the NumPy restatement of TensorLy's parafac
+    on the host cores; returns (sweeps/s, seconds)."""
+    import oracle
+    w = np.ones(rank, dtype=x.dtype)
+    t0 = time.perf_counter()
+    oracle.parafac_sweeps(x, w, init, sweeps)
+    dt = time.perf_counter() - t0
+    return sweeps / dt, dt
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from tensorly_gb300 import workloads
+    x, _ = workloads.dense_cp_large(size=args.size, rank=args.rank)
+    rs = np.random.RandomState(0)
+    init = [rs.random_sample((args.size, args.rank)).astype(np.float32) for _ in range(3)]
+    cores = os.cpu_count()
+    for _ in range(args.warmup):
+        cpu_sample(x, init, args.rank, 1)
+    times = []
+    for _ in range(args.steps):
+        _, dt = cpu_sample(x, init, args.rank, 1)
+        times.append(dt)
+    value = args.steps / sum(times)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * sum(times) / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": f"dense CP-ALS {args.size}^3 f32 rank {args.rank}",
+                       "step": "1 ALS sweep (bounded sample of the 50-sweep run)",
+                       "l2": "input larger than L2"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{args.steps} sweeps of the NumPy restatement of "
+                                       "tensorly parafac (explicit KR + GEMM + LAPACK gesv)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------- GPU arm
+def launches_per_step(ndim, sweeps, refine, precision):
+    """Kernel launches of one parafac call (library structure):
+    set-up: sum-of-squares (2) + one Gram per mode (2 each) [+ bf16 casts 1 + ndim];
+    per sweep: per mode factorise + MTTKRP + solve + Gram reduce (4), + fit (1)."""
+    setup = 2 + 2 * ndim + (1 + ndim if precision == "bf16" else 0)
+    return setup + sweeps * (4 * ndim + 1)
+
+
+# DRAM bytes per launch of the dominant kernel from the committed ncu captures
+# (profiles/); None until a capture exists for that kernel.
+NCU_TRAFFIC = {"native": None, "bf16": None}
+KERNEL = {"native": "mttkrp_split_kernel<float,64> + reduce (SIMT f32)",
+          "bf16": "mttkrp_tc_kernel (tcgen05 bf16, TMA)"}
+
+
+def mttkrp_callable(x, factors, mode, precision):
+    """A closure that enqueues one MTTKRP of `mode` through the C ABI with
+    preallocated buffers (no allocation per call)."""
+    import ctypes
+    import torch
+    from tensorly_gb300 import _lib
+    lib = _lib.lib()
+    n = x.ndim
+    rank = factors[0].shape[1]
+    shape = _lib.i64_array(x.shape)
+    out = torch.empty((x.shape[mode], rank), dtype=torch.float32, device=x.device)
+    st = torch.cuda.current_stream().cuda_stream
+    if precision == "bf16":
+        xb = x.to(torch.bfloat16)
+        fbt = [f.t().contiguous().to(torch.bfloat16) for f in factors]
+        nbytes = ctypes.c_size_t(0)
+        _lib.check(lib.tlgb_mttkrp_bf16_workspace_size(n, shape, rank, mode, ctypes.byref(nbytes)))
+        ws = torch.empty(max(256, nbytes.value), dtype=torch.uint8, device=x.device)
+        fp = _lib.ptr_array([f.data_ptr() for f in factors])
+        bp = _lib.ptr_array([f.data_ptr() for f in fbt])
+
+        def fn():
+            _lib.check(lib.tlgb_mttkrp_bf16(xb.data_ptr(), n, shape, fp, bp, None, rank, mode,
+                                            out.data_ptr(), ws.data_ptr(), ws.numel(), st))
+        fn.keep = (xb, fbt, ws)
+        return fn
+    nbytes = ctypes.c_size_t(0)
+    _lib.check(lib.tlgb_mttkrp_workspace_size(_lib.TLGB_F32, n, shape, rank, mode,
+                                              ctypes.byref(nbytes)))
+    ws = torch.empty(max(256, nbytes.value), dtype=torch.uint8, device=x.device)
+    fp = _lib.ptr_array([f.data_ptr() for f in factors])
+
+    def fn():
+        _lib.check(lib.tlgb_mttkrp(_lib.TLGB_F32, x.data_ptr(), n, shape, fp, None, rank, mode,
+                                   out.data_ptr(), ws.data_ptr(), ws.numel(), st))
+    fn.keep = (ws,)
+    return fn
+
+
+def mttkrp_alone_ms(tg, x, factors, mode, precision, reps=10):
+    """Average duration of the dominant kernel (the MTTKRP of `mode`),
+    launched alone through the library on the current stream, CUDA events."""
+    import torch
+    st = torch.cuda.current_stream()
+    fn = mttkrp_callable(x, factors, mode, precision)
+    for _ in range(3):
+        fn()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(st)
+    for _ in range(reps):
+        fn()
+    b.record(st)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def run_gpu(args):
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    import tensorly_gb300 as tg
+    tg.build() if not os.path.exists(tg._lib.library_path()) else None
+    from tensorly_gb300 import workloads
+    dev = torch.device("cuda", torch.cuda.current_device())
+
+    x_np, _ = workloads.dense_cp_large(size=args.size, rank=args.rank)
+    rs = np.random.RandomState(0)
+    init_np = [rs.random_sample((args.size, args.rank)).astype(np.float32) for _ in range(3)]
+    x_host = torch.from_numpy(x_np).pin_memory()
+    x = x_host.to(dev)
+    init = [torch.from_numpy(f).to(dev) for f in init_np]
+
+    kw = dict(n_iter_max=args.sweeps, tol=0, precision=args.precision,
+              refine_sweeps=args.refine, check_every=args.sweeps, return_errors=True)
+
+    def step():
+        return tg.parafac(x, args.rank, init=tg.CPTensor((None, init)), **kw)
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        cp, errs = step()
+    barrier()
+    st = torch.cuda.current_stream()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    barrier()
+    ev0.record(st)
+    for _ in range(args.steps):
+        cp, errs = step()
+    ev1.record(st)
+    barrier()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    if ws > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    total_sweeps = args.sweeps * args.steps * ws
+    value = total_sweeps / (ms / 1000.0)
+    final_err = errs[-1]
+
+    # ---- end to end through the public API with host buffers (pinned input,
+    # results copied back each step)
+    init_host = [torch.from_numpy(f) for f in init_np]
+
+    def step_host():
+        cp_h, e_h = tg.parafac(x_host, args.rank, init=tg.CPTensor((None, init_host)), **kw)
+        return cp_h, e_h
+
+    step_host()
+    barrier()
+    e0 = time.perf_counter()
+    for _ in range(args.steps):
+        cp_h, _ = step_host()
+    barrier()
+    e_ms = (time.perf_counter() - e0) * 1000.0
+    e2e_value = args.sweeps * args.steps * ws / (e_ms / 1000.0)
+    h2d = x_np.nbytes + sum(f.nbytes for f in init_np)
+    d2h = sum(f.nbytes for f in init_np) + 4 * args.rank
+
+    # ---- the dominant kernel alone (CUDA events) for the roofline
+    mode = 1
+    k_ms = mttkrp_alone_ms(tg, x, init, mode, args.precision)
+    esz = 2 if args.precision == "bf16" else 4
+    nel = args.size ** 3
+    alg_bytes = nel * esz + 2 * args.size * args.rank * (esz + 4) + args.size * args.rank * 4
+    achieved = alg_bytes / (k_ms / 1000.0) / 1e9
+    peak, peak_kind = measured_peaks()
+
+    # ---- CPU baseline: bounded sample of the NumPy restatement (rank 0, N=1)
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        v, dt = cpu_sample(x_np, init_np, args.rank, args.cpu_sweeps)
+        cpu = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+               "sample": f"{args.cpu_sweeps} ALS sweeps ({dt:.1f} s) of the NumPy restatement of "
+                         "tensorly parafac on the same tensor and init"}
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16+f32" if args.precision == "bf16" else "f32",
+        "data": "synthetic",
+        "config": {"workload": f"dense CP-ALS {args.size}^3 f32 rank {args.rank}, "
+                               f"{args.sweeps} sweeps per step",
+                   "precision": args.precision,
+                   "refine_sweeps": args.refine if args.precision == "bf16" else 0,
+                   "parallelism": "replicas" if ws > 1 else "single GPU",
+                   "l2": "input 512 MiB > L2, no flush"},
+        "final_rel_error": final_err,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_kind,
+                     "kernel": KERNEL[args.precision],
+                     "kernel_ms": k_ms, "algorithmic_bytes": alg_bytes,
+                     "traffic": NCU_TRAFFIC[args.precision]},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "clocks": clk,
+        "gpu_launches": launches_per_step(3, args.sweeps, args.refine, args.precision) * args.steps,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

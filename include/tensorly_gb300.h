@@ -1,0 +1,150 @@
+/*
+ * tensorly_gb300 — C ABI of the GB300 (sm_103a) CP-ALS / Tucker-HOOI library.
+ *
+ * Every entry point takes plain device pointers, sizes and a CUDA stream
+ * (passed as void*, i.e. a cudaStream_t; NULL = legacy default stream).
+ * Tensors are dense, C-contiguous (row-major, last mode fastest) and live in
+ * device memory unless a parameter says "host".  Factor matrices are
+ * row-major (rows x rank).  Nothing here allocates device memory: entry points
+ * that need scratch space take a caller-provided workspace whose size comes
+ * from the matching *_workspace_size query.  Work is enqueued on `stream`;
+ * functions return before the GPU finishes unless documented otherwise.
+ *
+ * Return value: TLGB_OK (0) or an error code; tlgb_last_error() gives the
+ * message of the last failure on the calling thread.
+ *
+ * Each entry point names the TensorLy 0.9.0 function it replaces
+ * (file:line inside the TensorLy source tree).
+ */
+#ifndef TENSORLY_GB300_H
+#define TENSORLY_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TLGB_MAX_MODES 8
+
+/* status codes */
+#define TLGB_OK 0
+#define TLGB_EINVAL 1        /* bad argument (shape, dtype, size, mode) */
+#define TLGB_ECUDA 2         /* CUDA runtime or launch error */
+#define TLGB_ESINGULAR 3     /* normal equations singular (LAPACK gesv would fail too) */
+#define TLGB_EUNSUPPORTED 4  /* valid request this library does not implement */
+#define TLGB_ETIMEOUT 5      /* a bounded device-side wait gave up */
+#define TLGB_EWORKSPACE 6    /* workspace smaller than the size query returned */
+
+/* element types */
+#define TLGB_F32 0
+#define TLGB_F64 1
+#define TLGB_BF16 2
+
+/* CP-ALS precision modes */
+#define TLGB_PREC_NATIVE 0   /* every sweep in the tensor dtype (f32 or f64) */
+#define TLGB_PREC_BF16 1     /* bf16 tensor + tensor-core MTTKRP, then native refinement sweeps */
+
+/* Library version, e.g. 100 for 0.1.0. */
+int tlgb_version(void);
+
+/* Message of the last failure on this thread ("" if none). */
+const char* tlgb_last_error(void);
+
+/*
+ * Khatri-Rao product of `n_mats` matrices (rows[k] x rank each), first matrix
+ * varying slowest; optional `weights` (rank) scale the first matrix and the
+ * optional `mask` (prod(rows)) scales output rows.  out: prod(rows) x rank.
+ * Replaces tensorly/tenalg/core_tenalg/_khatri_rao.py:9-109 (khatri_rao).
+ * dtype: TLGB_F32 or TLGB_F64.  weights/mask may be NULL.
+ */
+int tlgb_khatri_rao(int dtype, int n_mats, const void* const* mats, const int64_t* rows,
+                    int64_t rank, const void* weights, const void* mask, void* out,
+                    void* stream);
+
+/*
+ * MTTKRP: out = unfold(X, mode) . khatri_rao(factors, weights, skip_matrix=mode)
+ * without forming the Khatri-Rao product or the unfolding.
+ * X: shape[0..ndim) dense; factors[k]: shape[k] x rank (factors[mode] unused,
+ * may be NULL); weights: rank or NULL; out: shape[mode] x rank.
+ * Replaces tensorly/tenalg/core_tenalg/mttkrp.py:9-50
+ * (unfolding_dot_khatri_rao).  dtype: TLGB_F32 or TLGB_F64 (SIMT kernels;
+ * f64 accumulation for f64, f32 accumulation with f64 split reduction for f32).
+ */
+int tlgb_mttkrp_workspace_size(int dtype, int ndim, const int64_t* shape, int64_t rank,
+                               int mode, size_t* bytes);
+int tlgb_mttkrp(int dtype, const void* X, int ndim, const int64_t* shape,
+                const void* const* factors, const void* weights, int64_t rank, int mode,
+                void* out, void* workspace, size_t workspace_bytes, void* stream);
+
+/*
+ * Tensor-times-matrix: out = X x_mode U, i.e. fold(U . unfold(X, mode)).
+ * U is J x shape[mode] (row-major); with transpose != 0, U is shape[mode] x J
+ * and U^T is applied.  out has shape[mode] replaced by J.
+ * Replaces tensorly/tenalg/core_tenalg/n_mode_product.py:5-76 (mode_dot,
+ * matrix case; the vector case is J = 1 with the mode squeezed by the caller).
+ */
+int tlgb_mode_dot(int dtype, const void* X, int ndim, const int64_t* shape, const void* U,
+                  int64_t J, int transpose, int mode, void* out, void* stream);
+
+/*
+ * Dense CP-ALS (the sweep loop of tensorly/decomposition/_cp.py:394-530,
+ * parafac).  On entry factors[k] (shape[k] x rank, tensor dtype) and weights
+ * (rank) hold the initial CP tensor; on exit the result.  Per sweep and mode:
+ * the Hadamard product of the other factors' Grams (+ l2_reg I, scaled by
+ * w w^T) is factorised in f64 (Cholesky, LU with partial pivoting if not
+ * positive definite), the MTTKRP is formed without the Khatri-Rao product,
+ * and the factor is the f64 solve.  The error uses the last mode's MTTKRP
+ * (tensorly/decomposition/_cp.py:217-225) in f64; the stop test mirrors
+ * _cp.py:505-524.  errors (host, n_iter_max entries) receive the relative
+ * errors, *n_errors their count.  The call returns after the GPU finished.
+ */
+typedef int (*tlgb_sweep_callback)(void* user, int iteration, double rec_error);
+
+typedef struct tlgb_cp_als_options {
+  int n_iter_max;          /* parafac n_iter_max */
+  double tol;              /* parafac tol (0 disables the stop test) */
+  double l2_reg;           /* parafac l2_reg */
+  int cvg_criterion;       /* 0 = 'abs_rec_error', 1 = 'rec_error' */
+  int normalize_factors;   /* parafac normalize_factors */
+  uint32_t fixed_modes;    /* bit k set: mode k is kept fixed (parafac fixed_modes) */
+  int precision;           /* TLGB_PREC_NATIVE or TLGB_PREC_BF16 (f32 tensors only) */
+  int refine_sweeps;       /* TLGB_PREC_BF16: closing sweeps in f32 */
+  int check_every;         /* sweeps between host reads of the device stop flag (>= 1) */
+  int use_graph;           /* replay one captured sweep as a CUDA graph */
+  tlgb_sweep_callback callback;  /* per-sweep hook (parafac callback) or NULL */
+  void* callback_user;
+} tlgb_cp_als_options;
+
+void tlgb_cp_als_default_options(tlgb_cp_als_options* opts);
+int tlgb_cp_als_workspace_size(int dtype, int ndim, const int64_t* shape, int64_t rank,
+                               const tlgb_cp_als_options* opts, size_t* bytes);
+int tlgb_cp_als(int dtype, const void* X, int ndim, const int64_t* shape, int64_t rank,
+                void* const* factors, void* weights, const tlgb_cp_als_options* opts,
+                double* errors, int* n_errors, void* workspace, size_t workspace_bytes,
+                void* stream);
+
+/*
+ * cp_normalize: unit-norm factor columns, norms multiplied into weights
+ * (factor 0 first absorbs the weights).  In place on factors and weights.
+ * Replaces tensorly/cp_tensor.py:278-321 (cp_normalize).
+ */
+int tlgb_cp_normalize(int dtype, int ndim, const int64_t* rows, int64_t rank,
+                      void* const* factors, void* weights, void* stream);
+
+/*
+ * cp_norm: ||[[weights; factors]]||_F from the Hadamard product of the factor
+ * Grams (f64).  out: one double in device memory.  weights may be NULL.
+ * Replaces tensorly/cp_tensor.py:614-644 (cp_norm).
+ */
+int tlgb_cp_norm_workspace_size(int ndim, const int64_t* rows, int64_t rank, size_t* bytes);
+int tlgb_cp_norm(int dtype, int ndim, const int64_t* rows, int64_t rank,
+                 const void* const* factors, const void* weights, double* out,
+                 void* workspace, size_t workspace_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TENSORLY_GB300_H */

@@ -1,0 +1,542 @@
+"""NumPy restatement of TensorLy 0.9.0's CP-ALS / Tucker-HOOI hot path.
+
+TEST INFRASTRUCTURE: this module is the oracle the CUDA library is checked
+against.  It is imported only by ``tests/``, ``__graft_entry__.smoke()`` and
+the CPU-baseline legs of ``bench.py``; the shipped package never calls it.
+
+Every function names the reference file:line whose behaviour it restates
+(paths are relative to the TensorLy source tree, ``tensorly/...``).  The
+arithmetic that TensorLy delegates to NumPy/LAPACK (``np.dot``,
+``np.linalg.solve`` = LAPACK gesv, ``np.linalg.svd`` = LAPACK gesdd) is called
+the same way here, so on identical inputs this module reproduces the
+reference's NumPy backend to rounding (pinned by ``tests/golden``).
+
+Only the dense, real, unmasked, non-sparse branches are restated: those are
+the branches the GB300 library implements.  Other branches raise
+``NotImplementedError``.
+"""
+
+import math
+import warnings
+
+import numpy as np
+
+__all__ = [
+    "check_random_state", "unfold", "fold", "khatri_rao",
+    "unfolding_dot_khatri_rao", "mode_dot", "multi_mode_dot", "svd_flip",
+    "truncated_svd", "svd_interface", "random_cp", "cp_to_tensor", "cp_norm",
+    "cp_normalize", "validate_cp_rank", "initialize_cp", "error_calc",
+    "parafac", "initialize_tucker", "partial_tucker", "tucker",
+    "tucker_to_tensor", "validate_tucker_rank", "parafac_sweeps",
+]
+
+
+# --------------------------------------------------------------------------
+# random state, norm, unfolding
+# --------------------------------------------------------------------------
+def norm(tensor, axis=None):
+    """tensorly/backend/core.py:714-739 (order 2): sqrt(sum(|x|**2))."""
+    return np.sqrt(np.sum(np.abs(tensor) ** 2, axis=axis))
+
+
+def check_random_state(seed):
+    """tensorly/backend/core.py:163-188: None -> global RandomState,
+    int -> RandomState(seed), RandomState -> itself."""
+    if seed is None:
+        return np.random.mtrand._rand
+    if isinstance(seed, (int, np.integer)):
+        return np.random.RandomState(int(seed))
+    if isinstance(seed, np.random.RandomState):
+        return seed
+    raise ValueError("Seed should be None, int or np.random.RandomState")
+
+
+def unfold(tensor, mode):
+    """tensorly/base.py:39-53: moveaxis(mode -> 0) then C-order reshape."""
+    return np.reshape(np.moveaxis(tensor, mode, 0), (tensor.shape[mode], -1))
+
+
+def fold(unfolded, mode, shape):
+    """tensorly/base.py:56-79: inverse of :func:`unfold`."""
+    full_shape = list(shape)
+    mode_dim = full_shape.pop(mode)
+    full_shape.insert(0, mode_dim)
+    return np.moveaxis(np.reshape(unfolded, full_shape), 0, mode)
+
+
+# --------------------------------------------------------------------------
+# tenalg primitives
+# --------------------------------------------------------------------------
+def khatri_rao(matrices, weights=None, skip_matrix=None, mask=None):
+    """tensorly/tenalg/core_tenalg/_khatri_rao.py:64-109.
+
+    Column-wise Kronecker product; the first matrix varies slowest.  Weights
+    multiply the first matrix (``:96-99``) before the pairwise products
+    (``:101-105``); the optional mask multiplies the rows (``:107-109``).
+    """
+    if skip_matrix is not None:
+        matrices = [matrices[i] for i in range(len(matrices)) if i != skip_matrix]
+    if len(matrices) == 1:
+        return matrices[0]
+    if np.ndim(matrices[0]) == 2:
+        n_columns = matrices[0].shape[1]
+    else:
+        n_columns = 1
+        matrices = [np.reshape(m, (-1, 1)) for m in matrices]
+    for i, matrix in enumerate(matrices):
+        if np.ndim(matrix) != 2:
+            raise ValueError(
+                "All the matrices must have exactly 2 dimensions!"
+                f"Matrix {i} has dimension {np.ndim(matrix)} != 2.")
+        if matrix.shape[1] != n_columns:
+            raise ValueError(
+                "All matrices must have same number of columns!"
+                f"Matrix {i} has {matrix.shape[1]} columns != {n_columns}.")
+    res = None
+    for i, e in enumerate(matrices[1:]):
+        if not i:
+            res = matrices[0] if weights is None else matrices[0] * np.reshape(weights, (1, -1))
+        s1, s2 = res.shape
+        s3, s4 = e.shape
+        res = np.reshape(np.reshape(res, (s1, 1, s2)) * np.reshape(e, (1, s3, s4)),
+                         (-1, n_columns))
+    m = np.reshape(mask, (-1, 1)) if mask is not None else 1
+    return res * m
+
+
+def unfolding_dot_khatri_rao(tensor, cp_tensor, mode):
+    """tensorly/tenalg/core_tenalg/mttkrp.py:9-50: explicit KR, then
+    ``dot(unfold(tensor, mode), conj(KR))``."""
+    weights, factors = cp_tensor
+    kr = khatri_rao(factors, weights=weights, skip_matrix=mode)
+    return np.dot(unfold(tensor, mode), np.conj(kr))
+
+
+def mode_dot(tensor, matrix_or_vector, mode, transpose=False):
+    """tensorly/tenalg/core_tenalg/n_mode_product.py:5-76."""
+    fold_mode = mode
+    new_shape = list(tensor.shape)
+    if np.ndim(matrix_or_vector) == 2:
+        dim = 0 if transpose else 1
+        if matrix_or_vector.shape[dim] != tensor.shape[mode]:
+            raise ValueError(
+                f"shapes {tensor.shape} and {matrix_or_vector.shape} not aligned in "
+                f"mode-{mode} multiplication: {tensor.shape[mode]} (mode {mode}) != "
+                f"{matrix_or_vector.shape[dim]} (dim 1 of matrix)")
+        if transpose:
+            matrix_or_vector = np.conj(np.transpose(matrix_or_vector))
+        new_shape[mode] = matrix_or_vector.shape[0]
+        vec = False
+    elif np.ndim(matrix_or_vector) == 1:
+        if matrix_or_vector.shape[0] != tensor.shape[mode]:
+            raise ValueError(
+                f"shapes {tensor.shape} and {matrix_or_vector.shape} not aligned for "
+                f"mode-{mode} multiplication: {tensor.shape[mode]} (mode {mode}) != "
+                f"{matrix_or_vector.shape[0]} (vector size)")
+        if len(new_shape) > 1:
+            new_shape.pop(mode)
+        else:
+            new_shape = ()
+        vec = True
+    else:
+        raise ValueError(
+            "Can only take n_mode_product with a vector or a matrix."
+            f"Provided array of dimension {np.ndim(matrix_or_vector)} not in [1, 2].")
+    res = np.dot(matrix_or_vector, unfold(tensor, mode))
+    if vec:
+        return np.reshape(res, new_shape)
+    return fold(res, fold_mode, new_shape)
+
+
+def multi_mode_dot(tensor, matrix_or_vec_list, modes=None, skip=None, transpose=False):
+    """tensorly/tenalg/core_tenalg/n_mode_product.py:79-135: modes applied in
+    sorted order, ``skip`` indexes the sorted list, vectors drop a mode."""
+    if modes is None:
+        modes = range(len(matrix_or_vec_list))
+    decrement = 0
+    res = tensor
+    factors_modes = sorted(zip(matrix_or_vec_list, modes), key=lambda x: x[1])
+    for i, (m, mode) in enumerate(factors_modes):
+        if skip is not None and i == skip:
+            continue
+        if transpose:
+            res = mode_dot(res, np.conj(np.transpose(m)), mode - decrement)
+        else:
+            res = mode_dot(res, m, mode - decrement)
+        if np.ndim(m) == 1:
+            decrement += 1
+    return res
+
+
+# --------------------------------------------------------------------------
+# SVD
+# --------------------------------------------------------------------------
+def svd_flip(U, V, u_based_decision=True):
+    """tensorly/tenalg/svd.py:13-65: make the max-|.| entry of each U column
+    positive (U-based rule) and flip the matching V rows."""
+    if u_based_decision:
+        max_abs_cols = np.argmax(np.abs(U), axis=0)
+        signs = np.sign(U[max_abs_cols, np.arange(U.shape[1])])
+        U = U * np.conj(signs)
+        if V.shape[0] > U.shape[1]:
+            signs = np.concatenate((signs, np.ones(V.shape[0] - U.shape[1])))
+        V = V * signs[: V.shape[0]][:, None]
+    else:
+        max_abs_rows = np.argmax(np.abs(V), axis=1)
+        signs = np.sign(V[np.arange(V.shape[0]), max_abs_rows])
+        V = V * np.conj(signs[:, None])
+        if U.shape[1] > V.shape[0]:
+            signs = np.concatenate((signs, np.ones(U.shape[1] - V.shape[0])))
+        U = U * signs[: U.shape[1]]
+    return U, V
+
+
+def _svd_checks(matrix, n_eigenvecs=None):
+    """tensorly/tenalg/svd.py:172-208 (shape checks of the SVD helpers)."""
+    if np.ndim(matrix) != 2:
+        raise ValueError(f"matrix be a matrix. matrix.ndim is {np.ndim(matrix)} != 2")
+    dim_1, dim_2 = matrix.shape
+    min_dim, max_dim = (dim_1, dim_2) if dim_1 <= dim_2 else (dim_2, dim_1)
+    if n_eigenvecs is None:
+        n_eigenvecs = max_dim
+    if n_eigenvecs > max_dim:
+        warnings.warn(
+            f"Trying to compute SVD with n_eigenvecs={n_eigenvecs}, which is larger "
+            f"than max(matrix.shape)={max_dim}. Setting n_eigenvecs to {max_dim}.")
+        n_eigenvecs = max_dim
+    return n_eigenvecs, min_dim, max_dim
+
+
+def truncated_svd(matrix, n_eigenvecs=None, **kwargs):
+    """tensorly/tenalg/svd.py:211-235: full ``np.linalg.svd`` then truncate."""
+    n_eigenvecs, min_dim, _ = _svd_checks(matrix, n_eigenvecs)
+    full_matrices = n_eigenvecs > min_dim
+    U, S, V = np.linalg.svd(matrix, full_matrices=full_matrices)
+    return U[:, :n_eigenvecs], S[:n_eigenvecs], V[:n_eigenvecs, :]
+
+
+def svd_interface(matrix, method="truncated_svd", n_eigenvecs=None, flip_sign=True,
+                  u_based_flip_sign=True, non_negative=None, mask=None,
+                  n_iter_mask_imputation=5, **kwargs):
+    """tensorly/tenalg/svd.py:366-447 (truncated_svd method, no mask, no NNDSVD)."""
+    if method != "truncated_svd":
+        raise NotImplementedError("oracle restates method='truncated_svd' only")
+    if mask is not None or (non_negative is not False and non_negative is not None):
+        raise NotImplementedError("oracle restates the unmasked, signed branch only")
+    U, S, V = truncated_svd(matrix, n_eigenvecs=n_eigenvecs)
+    if flip_sign:
+        U, V = svd_flip(U, V, u_based_decision=u_based_flip_sign)
+    return U, S, V
+
+
+# --------------------------------------------------------------------------
+# CP tensors
+# --------------------------------------------------------------------------
+def validate_cp_rank(tensor_shape, rank="same", rounding="round"):
+    """tensorly/cp_tensor.py:240-275."""
+    fun = {"ceil": np.ceil, "floor": np.floor, "round": np.round}.get(rounding)
+    if fun is None:
+        raise ValueError(f"Rounding should be of round, floor or ceil, but got {rounding}")
+    if rank == "same":
+        rank = float(1)
+    if isinstance(rank, float):
+        rank = int(fun(np.prod(tensor_shape) * rank / np.sum(tensor_shape)))
+    return rank
+
+
+def random_cp(shape, rank, random_state=None, dtype=np.float64):
+    """tensorly/random/base.py:64-114 with ``normalise_factors=False``:
+    one ``random_sample((s, rank))`` draw per mode, in mode order (``:104``),
+    float64 cast to the tensor dtype; weights are ones (``:105``)."""
+    rns = check_random_state(random_state)
+    factors = [rns.random_sample((s, rank)).astype(dtype) for s in shape]
+    return np.ones(rank, dtype=dtype), factors
+
+
+def cp_to_tensor(cp_tensor):
+    """tensorly/cp_tensor.py:433-485 (no mask): mode-0 unfolding
+    ``dot(factors[0]*weights, KR(factors[1:]).T)`` folded back."""
+    weights, factors = cp_tensor
+    shape = tuple(f.shape[0] for f in factors)
+    if len(shape) == 1:
+        return np.sum(weights * factors[0], axis=1)
+    w = 1 if weights is None else weights
+    full = np.dot(factors[0] * w, np.transpose(khatri_rao(factors, skip_matrix=0)))
+    return fold(full, 0, shape)
+
+
+def cp_norm(cp_tensor):
+    """tensorly/cp_tensor.py:614-644: sqrt(sum(Hadamard of Grams * w w^T))."""
+    weights, factors = cp_tensor
+    r = factors[0].shape[1]
+    norm = np.ones((r, r), dtype=factors[0].dtype)
+    for f in factors:
+        norm = norm * np.dot(np.transpose(f), np.conj(f))
+    if weights is not None:
+        norm = norm * (np.reshape(weights, (-1, 1)) * np.reshape(weights, (1, -1)))
+    return np.sqrt(np.sum(norm))
+
+
+def cp_normalize(cp_tensor):
+    """tensorly/cp_tensor.py:278-321: unit-norm columns, norms into weights
+    (weights are first folded into factor 0)."""
+    weights, factors = cp_tensor
+    rank = factors[0].shape[1]
+    if weights is None:
+        weights = np.ones(rank, dtype=factors[0].dtype)
+    out = []
+    for i, factor in enumerate(factors):
+        if i == 0:
+            factor = factor * weights
+            weights = np.ones(rank, dtype=factor.dtype)
+        scales = norm(factor, axis=0)
+        scales_nz = np.where(scales == 0, np.ones(scales.shape, dtype=factor.dtype), scales)
+        weights = weights * scales
+        out.append(factor / np.reshape(scales_nz, (1, -1)))
+    return weights, out
+
+
+def initialize_cp(tensor, rank, init="svd", svd="truncated_svd", random_state=None,
+                  normalize_factors=False):
+    """tensorly/decomposition/_cp.py:26-137 (non_negative=False, no mask)."""
+    rng = check_random_state(random_state)
+    if isinstance(init, str) and init == "random":
+        weights, factors = random_cp(tensor.shape, rank, random_state=rng, dtype=tensor.dtype)
+    elif isinstance(init, str) and init == "svd":
+        factors = []
+        for mode in range(tensor.ndim):
+            U, S, _ = svd_interface(unfold(tensor, mode), n_eigenvecs=rank, method=svd)
+            if mode == 0:
+                idx = min(rank, S.shape[0])
+                U = U.copy()
+                U[:, :idx] = U[:, :idx] * S[:idx]
+            if tensor.shape[mode] < rank:
+                random_part = rng.random_sample((U.shape[0], rank - tensor.shape[mode]))
+                U = np.concatenate([U, random_part.astype(tensor.dtype)], axis=1)
+            factors.append(U[:, :rank])
+        weights = None
+    elif isinstance(init, (tuple, list)):
+        weights, factors = init
+        factors = list(factors)
+        if weights is None or np.all(weights == 1):
+            return None, factors
+        avg = np.prod(weights) ** (1.0 / weights.shape[0])
+        return None, [f * avg for f in factors]
+    else:
+        raise ValueError(f'Initialization method "{init}" not recognized')
+    if normalize_factors:
+        weights, factors = cp_normalize((weights, factors))
+    return weights, factors
+
+
+def error_calc(tensor, norm_tensor, weights, factors, mttkrp):
+    """tensorly/decomposition/_cp.py:162-227, fast branch ``:217-225``:
+    ||X - rec||^2 = ||X||^2 + ||rec||^2 - 2 <X, rec>, with <X, rec> taken from
+    the last mode's MTTKRP."""
+    factors_norm = cp_norm((weights, factors))
+    iprod = np.sum(np.sum(mttkrp * np.conj(factors[-1]), axis=0))
+    return np.sqrt(np.abs(norm_tensor ** 2 + factors_norm ** 2 - 2 * iprod))
+
+
+def parafac(tensor, rank, n_iter_max=100, init="svd", svd="truncated_svd",
+            normalize_factors=False, orthogonalise=False, tol=1e-8, random_state=None,
+            verbose=0, return_errors=False, sparsity=None, l2_reg=0, mask=None,
+            cvg_criterion="abs_rec_error", fixed_modes=None, svd_mask_repeats=5,
+            linesearch=False, callback=None):
+    """tensorly/decomposition/_cp.py:230-543 (dense ALS; no sparsity, mask,
+    linesearch or orthogonalisation).
+
+    Per sweep and mode (``:407-428``): Hadamard of the other factors' Grams
+    plus ``l2_reg*I``, scaled by ``w w^T``; MTTKRP; ``solve(V^H, M^T)^T``
+    (LAPACK gesv).  Error from the last mode's MTTKRP (``:437-440``), stop on
+    ``|e[-2]-e[-1]| < tol`` (``:505-524``), then optional normalisation
+    (``:529-530``).  Returns ``((weights, factors), errors)`` or
+    ``(weights, factors)``.
+    """
+    if sparsity or mask is not None or linesearch or orthogonalise:
+        raise NotImplementedError("oracle restates the dense unmasked ALS only")
+    rank = validate_cp_rank(tensor.shape, rank=rank)
+    weights, factors = initialize_cp(tensor, rank, init=init, svd=svd,
+                                     random_state=random_state,
+                                     normalize_factors=normalize_factors)
+    factors = [np.array(f, copy=True) for f in factors]
+    if weights is None:
+        weights = np.ones(rank, dtype=tensor.dtype)
+    rec_errors = []
+    norm_tensor = norm(tensor)
+    Id = np.eye(rank, dtype=tensor.dtype) * l2_reg if l2_reg else 0
+    fixed_modes = [] if fixed_modes is None else list(fixed_modes)
+    if fixed_modes == list(range(tensor.ndim)):
+        return (weights, factors)
+    if tensor.ndim - 1 in fixed_modes:
+        warnings.warn("You asked for fixing the last mode, which is not supported.")
+        fixed_modes.remove(tensor.ndim - 1)
+    modes_list = [m for m in range(tensor.ndim) if m not in fixed_modes]
+    if callback is not None:
+        unnorm = error_calc_full(tensor, weights, factors)
+        callback((weights, factors), unnorm / norm_tensor)
+    mttkrp = None
+    for iteration in range(n_iter_max):
+        for mode in modes_list:
+            V = np.ones((rank, rank), dtype=tensor.dtype)
+            for i, f in enumerate(factors):
+                if i != mode:
+                    V = V * np.dot(np.conj(np.transpose(f)), f)
+            V = V + Id
+            V = np.reshape(weights, (-1, 1)) * V * np.reshape(weights, (1, -1))
+            mttkrp = unfolding_dot_khatri_rao(tensor, (weights, factors), mode)
+            factors[mode] = np.transpose(
+                np.linalg.solve(np.conj(np.transpose(V)), np.transpose(mttkrp)))
+        if tol or return_errors:
+            unnorm = error_calc(tensor, norm_tensor, weights, factors, mttkrp)
+            rec_errors.append(unnorm / norm_tensor)
+        if callback is not None:
+            if callback((weights, factors), rec_errors[-1]) is True:
+                break
+        if tol and iteration >= 1:
+            dec = rec_errors[-2] - rec_errors[-1]
+            if cvg_criterion == "abs_rec_error":
+                stop = abs(dec) < tol
+            elif cvg_criterion == "rec_error":
+                stop = dec < tol
+            else:
+                raise TypeError("Unknown convergence criterion")
+            if stop:
+                break
+        if normalize_factors:
+            weights, factors = cp_normalize((weights, factors))
+    if return_errors:
+        return (weights, factors), rec_errors
+    return (weights, factors)
+
+
+def error_calc_full(tensor, weights, factors):
+    """tensorly/decomposition/_cp.py:194-207 (``mttkrp=None`` branch, no mask):
+    norm of the explicit residual."""
+    return norm(tensor - cp_to_tensor((weights, factors)))
+
+
+def parafac_sweeps(tensor, weights, factors, n_sweeps, l2_reg=0.0):
+    """A bounded number of ALS sweeps from given factors (the body of
+    tensorly/decomposition/_cp.py:394-440), used to time a CPU sample of a
+    long run.  Returns (weights, factors, errors)."""
+    rank = factors[0].shape[1]
+    factors = [np.array(f, copy=True) for f in factors]
+    norm_tensor = norm(tensor)
+    Id = np.eye(rank, dtype=tensor.dtype) * l2_reg if l2_reg else 0
+    errors = []
+    for _ in range(n_sweeps):
+        for mode in range(tensor.ndim):
+            V = np.ones((rank, rank), dtype=tensor.dtype)
+            for i, f in enumerate(factors):
+                if i != mode:
+                    V = V * np.dot(np.conj(np.transpose(f)), f)
+            V = V + Id
+            V = np.reshape(weights, (-1, 1)) * V * np.reshape(weights, (1, -1))
+            mttkrp = unfolding_dot_khatri_rao(tensor, (weights, factors), mode)
+            factors[mode] = np.transpose(
+                np.linalg.solve(np.conj(np.transpose(V)), np.transpose(mttkrp)))
+        errors.append(error_calc(tensor, norm_tensor, weights, factors, mttkrp) / norm_tensor)
+    return weights, factors, errors
+
+
+# --------------------------------------------------------------------------
+# Tucker
+# --------------------------------------------------------------------------
+def validate_tucker_rank(tensor_shape, rank="same"):
+    """tensorly/tucker_tensor.py:344-447 (int and sequence ranks)."""
+    if isinstance(rank, int):
+        warnings.warn("Given only one int for 'rank'. Using this rank for all modes.")
+        return tuple([rank] * len(tensor_shape))
+    if rank == "same" or isinstance(rank, float):
+        raise NotImplementedError("oracle restates int / sequence ranks only")
+    return tuple(rank)
+
+
+def tucker_to_tensor(tucker_tensor, skip_factor=None, transpose_factors=False, modes=None):
+    """tensorly/tucker_tensor.py:50-75."""
+    core, factors = tucker_tensor
+    return multi_mode_dot(core, factors, skip=skip_factor,
+                          transpose=transpose_factors, modes=modes)
+
+
+def initialize_tucker(tensor, rank, modes, random_state, init="svd", svd="truncated_svd"):
+    """tensorly/decomposition/_tucker.py:25-102 (non_negative=False, no mask)."""
+    if isinstance(init, str) and init == "svd":
+        factors = []
+        for index, mode in enumerate(modes):
+            U, _, _ = svd_interface(unfold(tensor, mode), n_eigenvecs=rank[index], method=svd)
+            factors.append(U)
+        core = multi_mode_dot(tensor, factors, modes=modes, transpose=True)
+    elif isinstance(init, str) and init == "random":
+        rng = check_random_state(random_state)
+        core = (rng.random_sample([rank[i] for i in range(len(modes))]) + 0.01).astype(tensor.dtype)
+        factors = [rng.random_sample((tensor.shape[mode], rank[index])).astype(tensor.dtype)
+                   for index, mode in enumerate(modes)]
+    else:
+        core, factors = init
+    return core, list(factors)
+
+
+def partial_tucker(tensor, rank, modes=None, n_iter_max=100, init="svd", tol=10e-5,
+                   svd="truncated_svd", random_state=None, verbose=False, mask=None,
+                   svd_mask_repeats=5):
+    """tensorly/decomposition/_tucker.py:105-221 (HOOI, no mask)."""
+    if mask is not None:
+        raise NotImplementedError("oracle restates the unmasked HOOI only")
+    if modes is None:
+        modes = list(range(tensor.ndim))
+    if rank is None:
+        rank = [tensor.shape[m] for m in modes]
+    elif isinstance(rank, int):
+        rank = tuple(rank for _ in modes)
+    else:
+        rank = tuple(rank)
+    core, factors = initialize_tucker(tensor, rank, modes, init=init, svd=svd,
+                                      random_state=random_state)
+    rec_errors = []
+    norm_tensor = norm(tensor)
+    for iteration in range(n_iter_max):
+        for index, mode in enumerate(modes):
+            core_approximation = multi_mode_dot(tensor, factors, modes=modes, skip=index,
+                                                transpose=True)
+            eigenvecs, _, _ = svd_interface(unfold(core_approximation, mode),
+                                            n_eigenvecs=rank[index])
+            factors[index] = eigenvecs
+        core = multi_mode_dot(tensor, factors, modes=modes, transpose=True)
+        rec_error = math.sqrt(abs(norm_tensor ** 2 - norm(core) ** 2)) / norm_tensor
+        rec_errors.append(rec_error)
+        if iteration > 1:
+            if tol and abs(rec_errors[-2] - rec_errors[-1]) < tol:
+                break
+    return (core, factors), rec_errors
+
+
+def tucker(tensor, rank, fixed_factors=None, n_iter_max=100, init="svd",
+           return_errors=False, svd="truncated_svd", tol=10e-5, random_state=None,
+           mask=None, verbose=False):
+    """tensorly/decomposition/_tucker.py:224-345 (all modes; fixed_factors path
+    ``:288-322`` included)."""
+    if fixed_factors:
+        core, factors = init
+        fixed_factors = sorted(fixed_factors)
+        modes_fixed, factors_fixed = zip(*[(i, f) for i, f in enumerate(factors)
+                                           if i in fixed_factors])
+        core = multi_mode_dot(core, factors_fixed, modes=modes_fixed)
+        modes, factors = zip(*[(i, f) for i, f in enumerate(factors) if i not in fixed_factors])
+        (core, new_factors), rec_errors = partial_tucker(
+            tensor, rank=rank, modes=modes, n_iter_max=n_iter_max, init=(core, list(factors)),
+            svd=svd, tol=tol, random_state=random_state, mask=mask)
+        factors = list(new_factors)
+        for i, e in enumerate(fixed_factors):
+            factors.insert(e, factors_fixed[i])
+        core = multi_mode_dot(core, factors_fixed, modes=modes_fixed, transpose=True)
+        return (core, factors)
+    modes = list(range(tensor.ndim))
+    rank = validate_tucker_rank(tensor.shape, rank=rank)
+    (core, factors), rec_errors = partial_tucker(
+        tensor, rank=rank, modes=modes, n_iter_max=n_iter_max, init=init, svd=svd, tol=tol,
+        random_state=random_state, mask=mask)
+    if return_errors:
+        return (core, factors), rec_errors
+    return (core, factors)

@@ -1,0 +1,21 @@
+"""tensorly_gb300: TensorLy's CP-ALS / Tucker-HOOI hot path on GB300 (sm_103a).
+
+Public API mirrors ``tensorly.decomposition`` and ``tensorly.tenalg``:
+
+    parafac, CP, initialize_cp, tucker, partial_tucker, Tucker
+    khatri_rao, unfolding_dot_khatri_rao, mode_dot, multi_mode_dot
+    CPTensor, TuckerTensor, cp_norm, cp_normalize, cp_to_tensor, tucker_to_tensor
+
+All computation runs in ``libtensorly_gb300.so`` (CUDA, sm_103a) through its
+C ABI (``include/tensorly_gb300.h``); tensors are PyTorch CUDA tensors.
+``plugin.register()`` installs the primitives as a TensorLy tenalg backend.
+"""
+
+from ._lib import GB300Error, SingularMatrixError, build, lib
+from .cp_tensor import (CPTensor, TuckerTensor, cp_norm, cp_normalize, cp_to_tensor,
+                        tucker_to_tensor, validate_cp_rank, validate_tucker_rank)
+from .decomposition import CP, initialize_cp, parafac
+from .random import check_random_state, random_cp
+from .tenalg import khatri_rao, mode_dot, multi_mode_dot, unfolding_dot_khatri_rao
+
+__version__ = "0.1.0"

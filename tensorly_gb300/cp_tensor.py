@@ -1,0 +1,228 @@
+"""CP and Tucker containers and helpers (tensorly/cp_tensor.py, tensorly/tucker_tensor.py).
+
+The containers behave like the reference's: a CPTensor unpacks as
+``weights, factors = cp``; a TuckerTensor as ``core, factors = tt``.
+"""
+
+import warnings
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._tensor import dtype_code, ptr, stream_of, workspace
+
+
+class CPTensor:
+    """(weights, factors) pair; tensorly/cp_tensor.py:17-160.
+
+    ``weights`` default to ones (``:25-26``).
+    """
+
+    def __init__(self, cp_tensor):
+        weights, factors = cp_tensor
+        factors = list(factors)
+        if len(factors) == 0:
+            raise ValueError("A CP tensor needs at least one factor")
+        rank = factors[0].shape[1] if factors[0].ndim == 2 else 1
+        if weights is None:
+            f0 = factors[0]
+            if isinstance(f0, torch.Tensor):
+                weights = torch.ones(rank, dtype=f0.dtype, device=f0.device)
+            else:
+                weights = np.ones(rank, dtype=np.asarray(f0).dtype)
+        self.weights = weights
+        self.factors = factors
+        self.shape = tuple(int(f.shape[0]) for f in factors)
+        self.rank = int(rank)
+
+    def __getitem__(self, i):
+        if i == 0:
+            return self.weights
+        if i == 1:
+            return self.factors
+        raise IndexError(f"CPTensor index {i} out of range (0: weights, 1: factors)")
+
+    def __setitem__(self, i, value):
+        if i == 0:
+            self.weights = value
+        elif i == 1:
+            self.factors = list(value)
+        else:
+            raise IndexError(f"CPTensor index {i} out of range")
+
+    def __iter__(self):
+        yield self.weights
+        yield self.factors
+
+    def __len__(self):
+        return 2
+
+    def __repr__(self):
+        return f"(weights, factors) : rank-{self.rank} CPTensor of shape {self.shape}"
+
+    def to_tensor(self):
+        return cp_to_tensor(self)
+
+    def norm(self):
+        return cp_norm(self)
+
+    def normalize(self, inplace=True):
+        w, f = cp_normalize(self)
+        if inplace:
+            self.weights, self.factors = w, f
+            return self
+        return CPTensor((w, f))
+
+
+class TuckerTensor:
+    """(core, factors) pair; tensorly/tucker_tensor.py:227-320."""
+
+    def __init__(self, tucker_tensor):
+        core, factors = tucker_tensor
+        self.core = core
+        self.factors = list(factors)
+        self.shape = tuple(int(f.shape[0]) for f in self.factors)
+        self.rank = tuple(int(s) for s in core.shape)
+
+    def __getitem__(self, i):
+        if i == 0:
+            return self.core
+        if i == 1:
+            return self.factors
+        raise IndexError(f"TuckerTensor index {i} out of range (0: core, 1: factors)")
+
+    def __iter__(self):
+        yield self.core
+        yield self.factors
+
+    def __len__(self):
+        return 2
+
+    def __repr__(self):
+        return f"Decomposed Tucker tensor of shape {self.shape} with rank {self.rank}"
+
+    def to_tensor(self):
+        return tucker_to_tensor(self)
+
+
+def validate_cp_rank(tensor_shape, rank="same", rounding="round"):
+    """tensorly/cp_tensor.py:240-275."""
+    fun = {"ceil": np.ceil, "floor": np.floor, "round": np.round}.get(rounding)
+    if fun is None:
+        raise ValueError(f"Rounding should be of round, floor or ceil, but got {rounding}")
+    if rank == "same":
+        rank = float(1)
+    if isinstance(rank, float):
+        rank = int(fun(np.prod(tensor_shape) * rank / np.sum(tensor_shape)))
+    return rank
+
+
+def validate_tucker_rank(tensor_shape, rank="same", rounding="round", fixed_modes=None):
+    """tensorly/tucker_tensor.py:344-447 (int and sequence ranks; 'same' and
+    fractional ranks follow the reference's parameter-count rule)."""
+    if rank == "same":
+        rank = float(1)
+    if isinstance(rank, float):
+        from scipy.optimize import brentq
+        fun_r = {"ceil": np.ceil, "floor": np.floor, "round": np.round}[rounding]
+        n_modes = len(tensor_shape)
+        n_param = np.prod(tensor_shape)
+        shape = list(tensor_shape)
+        n_fixed = 0
+        fixed = None
+        if fixed_modes is not None:
+            fixed = [(m, shape.pop(m)) for m in sorted(fixed_modes, reverse=True)][::-1]
+            n_fixed = np.sum([s ** 2 for _, s in fixed])
+            n_modes -= len(fixed)
+        sq = np.sum([s ** 2 for s in shape])
+        f = lambda x: n_param * x ** n_modes + sq * x + n_fixed * x - rank * n_param  # noqa: E731
+        frac = brentq(f, 0.0, max(rank, 1.0))
+        out = [max(int(fun_r(s * frac)), 1) for s in shape]
+        if fixed is not None:
+            for m, s in fixed:
+                out.insert(m, s)
+        return tuple(out)
+    if isinstance(rank, int):
+        warnings.warn(
+            f"Given only one int for 'rank' for decomposition a tensor of order "
+            f"{len(tensor_shape)}. Using this rank for all modes.")
+        if fixed_modes is None:
+            return tuple([rank] * len(tensor_shape))
+        return tuple(rank if i not in fixed_modes else s for i, s in enumerate(tensor_shape))
+    return tuple(rank)
+
+
+def _factors_cuda(cp_tensor):
+    weights, factors = cp_tensor
+    ref = factors[0]
+    if not isinstance(ref, torch.Tensor) or not ref.is_cuda:
+        raise TypeError("tensorly_gb300 CP helpers take CUDA tensors")
+    return weights, factors
+
+
+def cp_normalize(cp_tensor):
+    """Unit-norm factor columns, norms into the weights
+    (tensorly/cp_tensor.py:278-321), by the library's normalisation kernel."""
+    weights, factors = _factors_cuda(cp_tensor)
+    factors = [f.contiguous().clone() for f in factors]
+    rank = factors[0].shape[1]
+    if weights is None:
+        weights = torch.ones(rank, dtype=factors[0].dtype, device=factors[0].device)
+    else:
+        weights = weights.to(factors[0].dtype).contiguous().clone()
+    lib = _lib.lib()
+    rows = _lib.i64_array([f.shape[0] for f in factors])
+    _lib.check(lib.tlgb_cp_normalize(dtype_code(factors[0]), len(factors), rows, rank,
+                                     _lib.ptr_array([ptr(f) for f in factors]), ptr(weights),
+                                     stream_of(factors[0])))
+    return CPTensor((weights, factors))
+
+
+def cp_norm(cp_tensor):
+    """||[[w; A]]||_F from the Hadamard product of the factor Grams
+    (tensorly/cp_tensor.py:614-644); f64 accumulation on the GPU."""
+    weights, factors = _factors_cuda(cp_tensor)
+    factors = [f.contiguous() for f in factors]
+    rank = factors[0].shape[1]
+    lib = _lib.lib()
+    out = torch.empty(1, dtype=torch.float64, device=factors[0].device)
+    rows = _lib.i64_array([f.shape[0] for f in factors])
+    w = None if weights is None else weights.to(factors[0].dtype).contiguous()
+    nbytes = _lib.ctypes.c_size_t(0)
+    _lib.check(lib.tlgb_cp_norm_workspace_size(len(factors), rows, rank, _lib.ctypes.byref(nbytes)))
+    ws = workspace(nbytes.value, factors[0].device)
+    _lib.check(lib.tlgb_cp_norm(dtype_code(factors[0]), len(factors), rows, rank,
+                                _lib.ptr_array([ptr(f) for f in factors]), ptr(w), ptr(out),
+                                ptr(ws), ws.numel(), stream_of(factors[0])))
+    return out[0].to(factors[0].dtype)
+
+
+def cp_to_tensor(cp_tensor, mask=None):
+    """Full tensor of a CP model (tensorly/cp_tensor.py:433-485): mode-0
+    unfolding ``(A_0 * w) . KR(A_1..A_{N-1})^T`` refolded, with the
+    Khatri-Rao product and the product computed by the library's kernels."""
+    from .tenalg import khatri_rao, mode_dot
+    if mask is not None:
+        raise NotImplementedError("cp_to_tensor with a mask is not supported")
+    weights, factors = _factors_cuda(cp_tensor)
+    shape = tuple(int(f.shape[0]) for f in factors)
+    if len(shape) == 1:
+        a0w = khatri_rao([factors[0]], weights=weights) if weights is not None else factors[0]
+        return a0w.sum(dim=1)
+    a0w = factors[0] if weights is None else _scaled(factors[0], weights)
+    kr = khatri_rao(factors, skip_matrix=0)
+    full = mode_dot(a0w, kr, 1)          # (I_0, prod others) = A0w . KR^T
+    return full.reshape(shape)
+
+
+def _scaled(matrix, weights):
+    from .tenalg import _khatri_rao_raw
+    return _khatri_rao_raw([matrix], weights)
+
+
+def tucker_to_tensor(tucker_tensor, skip_factor=None, transpose_factors=False, modes=None):
+    """tensorly/tucker_tensor.py:50-75: multi_mode_dot of the core."""
+    from .tenalg import multi_mode_dot
+    core, factors = tucker_tensor
+    return multi_mode_dot(core, factors, skip=skip_factor, transpose=transpose_factors, modes=modes)

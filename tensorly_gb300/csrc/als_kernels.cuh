@@ -1,0 +1,66 @@
+// f64 normal-equation, Gram, fit and normalisation kernels of the CP-ALS sweep.
+#pragma once
+#include "common.cuh"
+
+namespace tlgb {
+
+// Device-side state of one CP-ALS run (lives in the workspace).
+struct AlsCtrl {
+  int done;      // stop flag: every sweep kernel returns at once when set
+  int iter;      // sweeps whose error has been recorded
+  int status;    // TLGB_OK or TLGB_ESINGULAR
+  int fac_kind;  // 0: Cholesky factor, 1: LU factors with row permutation
+  double norm_x2;
+};
+
+constexpr int kMaxAlsRank = 160;     // f64 factorisation held in one CTA's shared memory
+constexpr int kSolveWarps = 4;       // rows solved per CTA (one warp each)
+
+int als_launch_sumsq(int dtype, const void* X, int64_t n, double* part, int nblocks,
+                     AlsCtrl* ctrl, cudaStream_t st);
+
+template <typename T>
+int als_launch_gram(const T* A, int64_t I, int R, double* gpart, int nparts_max, double* G,
+                    const int* done, cudaStream_t st);
+
+template <typename T>
+int als_launch_factorize(const double* G, int ndim, int mode, int R, const T* weights,
+                         double l2_reg, double* fac, int* perm, AlsCtrl* ctrl, cudaStream_t st);
+
+// Sums the MTTKRP partials of each row, solves with the factorisation, stores
+// the factor (and optionally its bf16 transpose), and writes per-CTA Gram and
+// <M, A> partial sums.  Returns the number of CTAs used via *nblocks.
+template <typename T>
+int als_launch_solve(const T* partial, int splits, int64_t I, int R, const double* fac,
+                     const int* perm, T* A, __nv_bfloat16* A_bf16_t, double* gpart,
+                     double* ipart, AlsCtrl* ctrl, int* nblocks, cudaStream_t st);
+
+int als_launch_gram_reduce(const double* gpart, int nparts, int R, double* G, const int* done,
+                           cudaStream_t st);
+
+template <typename T>
+int als_launch_fit(const double* G, int ndim, int R, const T* weights, const double* ipart,
+                   int nip, AlsCtrl* ctrl, double* errors, int n_iter_max, double tol,
+                   int cvg_criterion, cudaStream_t st);
+
+template <typename T>
+int als_launch_normalize(T* const* factors, const int64_t* rows, int ndim, int R, T* weights,
+                         const int* done, cudaStream_t st);
+
+template <typename T>
+int als_launch_cp_norm(const double* G, int ndim, int R, const T* weights, double* out,
+                       cudaStream_t st);
+
+// Relative error of the current model from an MTTKRP of the last mode
+// (split partials) and the Grams; result (f64) to *out on the device.
+template <typename T>
+int als_launch_probe_error(const T* partial, int splits, int64_t I, int R, const T* A,
+                           const double* G, int ndim, const T* weights, double* ipart,
+                           int nip_max, const AlsCtrl* ctrl, double* out, cudaStream_t st);
+
+int solve_blocks_for(int64_t I);
+
+// Sets kernel attributes once per device (call before stream capture).
+int als_prepare(int dtype);
+
+}  // namespace tlgb

@@ -1,0 +1,89 @@
+// Shared definitions for the tensorly_gb300 CUDA library (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+#include <stddef.h>
+#include <string>
+
+#include "../../include/tensorly_gb300.h"
+
+namespace tlgb {
+
+// Records a message for tlgb_last_error() and returns `code`.
+int set_error(int code, const std::string& msg);
+void clear_error();
+
+// Number of SMs of the current device (cached per device).
+int sm_count();
+int current_device();
+
+#define TLGB_CUDA_TRY(expr)                                                        \
+  do {                                                                             \
+    cudaError_t _e = (expr);                                                       \
+    if (_e != cudaSuccess)                                                         \
+      return ::tlgb::set_error(TLGB_ECUDA, std::string(#expr ": ") +               \
+                                               cudaGetErrorString(_e));            \
+  } while (0)
+
+#define TLGB_CHECK_ARG(cond, msg)                                                  \
+  do {                                                                             \
+    if (!(cond)) return ::tlgb::set_error(TLGB_EINVAL, msg);                       \
+  } while (0)
+
+#define TLGB_LAUNCH_CHECK()                                                        \
+  do {                                                                             \
+    cudaError_t _e = cudaGetLastError();                                           \
+    if (_e != cudaSuccess)                                                         \
+      return ::tlgb::set_error(TLGB_ECUDA, std::string("kernel launch: ") +        \
+                                               cudaGetErrorString(_e));            \
+  } while (0)
+
+constexpr int kMaxModes = TLGB_MAX_MODES;
+
+// Mode geometry of a dense C-order tensor, passed to kernels by value.
+struct Shape {
+  int ndim;
+  int64_t dim[kMaxModes];
+  int64_t stride[kMaxModes];  // element strides (C order)
+  int64_t numel;
+};
+
+inline Shape make_shape(int ndim, const int64_t* dims) {
+  Shape s{};
+  s.ndim = ndim;
+  int64_t st = 1;
+  for (int k = ndim - 1; k >= 0; --k) {
+    s.dim[k] = dims[k];
+    s.stride[k] = st;
+    st *= dims[k];
+  }
+  s.numel = st;
+  return s;
+}
+
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Carves aligned sub-buffers out of one caller-provided workspace.
+struct Carver {
+  char* base;
+  size_t off = 0;
+  explicit Carver(void* b) : base(static_cast<char*>(b)) {}
+  template <typename T>
+  T* take(size_t count) {
+    off = align_up(off, 256);
+    T* p = base ? reinterpret_cast<T*>(base + off) : nullptr;
+    off += count * sizeof(T);
+    return p;
+  }
+  size_t used() const { return align_up(off, 256); }
+};
+
+template <typename T> struct TypeCode;
+template <> struct TypeCode<float> { static constexpr int value = TLGB_F32; };
+template <> struct TypeCode<double> { static constexpr int value = TLGB_F64; };
+
+__host__ __device__ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+}  // namespace tlgb

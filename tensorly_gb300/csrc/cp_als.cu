@@ -1,0 +1,491 @@
+// Native CP-ALS driver: the sweep loop of tensorly/decomposition/_cp.py:394-530
+// (parafac) run entirely on the GPU.
+//
+// One sweep = for each non-fixed mode: f64 factorisation of the normal
+// equations (k_factorize), split MTTKRP, fused partial-sum + f64 solve + Gram
+// partials (k_solve), Gram reduction; then the fit (k_fit) and, if asked,
+// cp_normalize.  The stop test runs on the device: k_fit raises a `done`
+// flag that makes every later sweep kernel return at once, so the host can
+// enqueue several sweeps (one CUDA graph launch each) and read the flag only
+// every `check_every` sweeps.  With a callback the host syncs every sweep.
+#include <cstring>
+#include <vector>
+
+#include "als_kernels.cuh"
+#include "mttkrp_simt.cuh"
+#include "mttkrp_tc.cuh"
+
+namespace tlgb {
+namespace {
+
+struct AlsBuffers {
+  AlsCtrl* ctrl;
+  double* errors;
+  double* G;
+  double* fac;
+  int* perm;
+  void* partial;
+  double* gpart;
+  double* ipart;
+  double* sumsq_part;
+  __nv_bfloat16* xbf;                   // bf16 copy of X (mixed precision)
+  __nv_bfloat16* fbt[kMaxModes];        // bf16 transposed factors (rank x rows)
+  void* tc_partial;
+  double* probe;                        // one f64 result slot (initial error)
+  size_t bytes;
+};
+
+constexpr int kSumsqBlocks = 1024;
+
+int layout(int dtype, const Shape& sh, int64_t R, const tlgb_cp_als_options& o,
+           const MttkrpPlan* plans, const TcPlan* tcplans, void* base, AlsBuffers* B) {
+  Carver c(base);
+  const int64_t RR = R * R;
+  const int esz = dtype == TLGB_F64 ? 8 : 4;
+  B->ctrl = c.take<AlsCtrl>(1);
+  B->errors = c.take<double>(std::max(1, o.n_iter_max));
+  B->G = c.take<double>((size_t)sh.ndim * RR);
+  B->fac = c.take<double>((size_t)RR + R);
+  B->perm = c.take<int>(R);
+  size_t pmax = 0;
+  int64_t imax = 0;
+  for (int k = 0; k < sh.ndim; ++k) {
+    pmax = std::max(pmax, plans[k].partial_bytes);
+    imax = std::max(imax, sh.dim[k]);
+  }
+  B->partial = c.take<char>(pmax);
+  const int nparts = solve_blocks_for(imax);
+  B->gpart = c.take<double>((size_t)nparts * RR);
+  B->ipart = c.take<double>(nparts);
+  B->sumsq_part = c.take<double>(kSumsqBlocks);
+  B->probe = c.take<double>(1);
+  B->xbf = nullptr;
+  for (int k = 0; k < kMaxModes; ++k) B->fbt[k] = nullptr;
+  B->tc_partial = nullptr;
+  if (o.precision == TLGB_PREC_BF16) {
+    B->xbf = c.take<__nv_bfloat16>((size_t)sh.numel);
+    for (int k = 0; k < sh.ndim; ++k) B->fbt[k] = c.take<__nv_bfloat16>((size_t)R * sh.dim[k]);
+    size_t tmax = 0;
+    for (int k = 0; k < sh.ndim; ++k) tmax = std::max(tmax, tcplans[k].partial_bytes);
+    B->tc_partial = c.take<char>(tmax);
+  }
+  (void)esz;
+  B->bytes = c.used();
+  return TLGB_OK;
+}
+
+int validate(int dtype, int ndim, const int64_t* shape, int64_t rank,
+             const tlgb_cp_als_options* o) {
+  TLGB_CHECK_ARG(dtype == TLGB_F32 || dtype == TLGB_F64, "cp_als: dtype must be f32 or f64");
+  TLGB_CHECK_ARG(shape != nullptr && o != nullptr, "cp_als: null pointer");
+  TLGB_CHECK_ARG(ndim >= 2 && ndim <= kMaxModes, "cp_als: ndim must be in [2, 8]");
+  TLGB_CHECK_ARG(rank >= 1, "cp_als: rank must be >= 1");
+  if (rank > kMaxAlsRank)
+    return set_error(TLGB_EUNSUPPORTED, "cp_als: rank above 160 is not supported");
+  for (int k = 0; k < ndim; ++k) TLGB_CHECK_ARG(shape[k] >= 1, "cp_als: empty mode");
+  TLGB_CHECK_ARG(o->n_iter_max >= 0, "cp_als: n_iter_max must be >= 0");
+  TLGB_CHECK_ARG(o->cvg_criterion == 0 || o->cvg_criterion == 1, "cp_als: bad cvg_criterion");
+  if (o->precision == TLGB_PREC_BF16) {
+    if (dtype != TLGB_F32)
+      return set_error(TLGB_EUNSUPPORTED, "cp_als: bf16 precision needs an f32 tensor");
+    TLGB_CHECK_ARG(o->refine_sweeps >= 0, "cp_als: refine_sweeps must be >= 0");
+  } else {
+    TLGB_CHECK_ARG(o->precision == TLGB_PREC_NATIVE, "cp_als: unknown precision");
+  }
+  return TLGB_OK;
+}
+
+struct Plans {
+  MttkrpPlan simt[kMaxModes];
+  TcPlan tc[kMaxModes];
+};
+
+int make_plans(int dtype, const Shape& sh, int64_t R, const tlgb_cp_als_options& o, Plans* P) {
+  for (int k = 0; k < sh.ndim; ++k) {
+    int rc = mttkrp_make_plan(dtype, sh, R, k, &P->simt[k]);
+    if (rc) return rc;
+    P->tc[k] = TcPlan{};
+    if (o.precision == TLGB_PREC_BF16) {
+      rc = mttkrp_tc_make_plan(sh, R, k, &P->tc[k]);
+      if (rc) return rc;
+    }
+  }
+  return TLGB_OK;
+}
+
+template <typename T>
+struct Runner {
+  const T* X;
+  Shape sh;
+  int64_t R;
+  T* const* factors;
+  T* weights;
+  tlgb_cp_als_options o;
+  Plans* P;
+  AlsBuffers B;
+  std::vector<int> modes;
+  int last_nb = 1;
+
+  // Enqueues one sweep; `tc` selects the bf16 tensor-core MTTKRP.
+  int sweep(bool tc, cudaStream_t st) {
+    const int N = sh.ndim;
+    const int RR = (int)(R * R);
+    const int* done = &B.ctrl->done;
+    const T* cf[kMaxModes];
+    for (int k = 0; k < N; ++k) cf[k] = factors[k];
+    // The reference's Khatri-Rao of a single remaining factor drops the
+    // weights (tensorly/tenalg/core_tenalg/_khatri_rao.py:71-73), so a 2-way
+    // MTTKRP is unweighted there; kept for parity.
+    const T* mw = (N == 2) ? nullptr : weights;
+    for (size_t mi = 0; mi < modes.size(); ++mi) {
+      const int mode = modes[mi];
+      const bool last = (mi + 1 == modes.size());
+      int rc = als_launch_factorize<T>(B.G, N, mode, (int)R, weights, o.l2_reg, B.fac, B.perm,
+                                       B.ctrl, st);
+      if (rc) return rc;
+      int splits;
+      const void* partial;
+      if (tc) {
+        if constexpr (sizeof(T) == 4) {
+          rc = mttkrp_tc_launch(P->tc[mode], B.xbf, (const float* const*)cf, B.fbt,
+                                (const float*)mw, (float*)B.tc_partial, done, st);
+        }
+        if (rc) return rc;
+        splits = P->tc[mode].splits;
+        partial = B.tc_partial;
+      } else {
+        rc = mttkrp_launch_partials<T>(P->simt[mode], X, cf, mw, (T*)B.partial, done, st);
+        if (rc) return rc;
+        splits = P->simt[mode].splits;
+        partial = B.partial;
+      }
+      int nb = 0;
+      rc = als_launch_solve<T>((const T*)partial, splits, sh.dim[mode], (int)R, B.fac, B.perm,
+                               factors[mode], B.fbt[mode], B.gpart, last ? B.ipart : nullptr,
+                               B.ctrl, &nb, st);
+      if (rc) return rc;
+      if (last) last_nb = nb;
+      rc = als_launch_gram_reduce(B.gpart, nb, (int)R, B.G + (size_t)mode * RR, done, st);
+      if (rc) return rc;
+    }
+    int rc = als_launch_fit<T>(B.G, N, (int)R, weights, B.ipart, last_nb, B.ctrl, B.errors,
+                               o.n_iter_max, o.tol, o.cvg_criterion, st);
+    if (rc) return rc;
+    if (o.normalize_factors) {
+      rc = als_launch_normalize<T>(factors, sh.dim, N, (int)R, weights, done, st);
+      if (rc) return rc;
+      rc = grams(done, st);
+      if (rc) return rc;
+      if (tc) {
+        rc = bf16_factors(st);
+        if (rc) return rc;
+      }
+    }
+    return TLGB_OK;
+  }
+
+  int grams(const int* done, cudaStream_t st) {
+    const int RR = (int)(R * R);
+    int64_t imax = 0;
+    for (int k = 0; k < sh.ndim; ++k) imax = std::max(imax, sh.dim[k]);
+    for (int k = 0; k < sh.ndim; ++k) {
+      int rc = als_launch_gram<T>(factors[k], sh.dim[k], (int)R, B.gpart, solve_blocks_for(imax),
+                                  B.G + (size_t)k * RR, done, st);
+      if (rc) return rc;
+    }
+    return TLGB_OK;
+  }
+
+  // Relative error of the initial model (what the reference's callback gets
+  // before the first sweep, tensorly/decomposition/_cp.py:379-392).
+  int initial_error(cudaStream_t st, double* host_err) {
+    const int N = sh.ndim;
+    const int last = N - 1;
+    const T* cf[kMaxModes];
+    for (int k = 0; k < N; ++k) cf[k] = factors[k];
+    int rc = mttkrp_launch_partials<T>(P->simt[last], X, cf, weights, (T*)B.partial, nullptr, st);
+    if (rc) return rc;
+    int64_t imax = 0;
+    for (int k = 0; k < N; ++k) imax = std::max(imax, sh.dim[k]);
+    rc = als_launch_probe_error<T>((const T*)B.partial, P->simt[last].splits, sh.dim[last], (int)R,
+                                   factors[last], B.G, N, weights, B.ipart, solve_blocks_for(imax),
+                                   B.ctrl, B.probe, st);
+    if (rc) return rc;
+    TLGB_CUDA_TRY(cudaMemcpyAsync(host_err, B.probe, sizeof(double), cudaMemcpyDeviceToHost, st));
+    TLGB_CUDA_TRY(cudaStreamSynchronize(st));
+    return TLGB_OK;
+  }
+
+  // bf16 transposed copies of every factor (tensor-core operand B)
+  int bf16_factors(cudaStream_t st) {
+    for (int k = 0; k < sh.ndim; ++k) {
+      int rc = tc_launch_factor_bf16t((const float*)factors[k], sh.dim[k], R, B.fbt[k], st);
+      if (rc) return rc;
+    }
+    return TLGB_OK;
+  }
+};
+
+class StreamGuard {
+ public:
+  cudaStream_t s = nullptr;
+  ~StreamGuard() { if (s) cudaStreamDestroy(s); }
+};
+class GraphGuard {
+ public:
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t e = nullptr;
+  ~GraphGuard() {
+    if (e) cudaGraphExecDestroy(e);
+    if (g) cudaGraphDestroy(g);
+  }
+};
+
+template <typename T>
+int run(const T* X, const Shape& sh, int64_t R, T* const* factors, T* weights,
+        const tlgb_cp_als_options& o, double* errors_host, int* n_errors, void* ws,
+        size_t ws_bytes, cudaStream_t st) {
+  Plans P;
+  int rc = make_plans(TypeCode<T>::value, sh, R, o, &P);
+  if (rc) return rc;
+  Runner<T> run{};
+  run.X = X; run.sh = sh; run.R = R; run.factors = factors; run.weights = weights; run.o = o;
+  run.P = &P;
+  rc = layout(TypeCode<T>::value, sh, R, o, P.simt, P.tc, ws, &run.B);
+  if (rc) return rc;
+  if (ws_bytes < run.B.bytes) return set_error(TLGB_EWORKSPACE, "cp_als: workspace too small");
+  for (int k = 0; k < sh.ndim; ++k)
+    if (!((o.fixed_modes >> k) & 1u) || k == sh.ndim - 1) run.modes.push_back(k);
+  if (n_errors) *n_errors = 0;
+  rc = mttkrp_prepare(TypeCode<T>::value);
+  if (rc) return rc;
+  rc = als_prepare(TypeCode<T>::value);
+  if (rc) return rc;
+  const bool mixed = o.precision == TLGB_PREC_BF16;
+  if (mixed) {
+    rc = mttkrp_tc_prepare();
+    if (rc) return rc;
+  }
+
+  // ---- set-up: control block, ||X||^2, Grams, bf16 operands
+  TLGB_CUDA_TRY(cudaMemsetAsync(run.B.ctrl, 0, sizeof(AlsCtrl), st));
+  rc = als_launch_sumsq(TypeCode<T>::value, X, sh.numel, run.B.sumsq_part, kSumsqBlocks,
+                        run.B.ctrl, st);
+  if (rc) return rc;
+  rc = run.grams(nullptr, st);
+  if (rc) return rc;
+  if (mixed) {
+    rc = tc_launch_to_bf16((const float*)X, sh.numel, run.B.xbf, st);
+    if (rc) return rc;
+    rc = run.bf16_factors(st);
+    if (rc) return rc;
+  }
+  if (o.callback) {
+    double e0 = 0.0;
+    rc = run.initial_error(st, &e0);
+    if (rc) return rc;
+    if (o.callback(o.callback_user, -1, e0) != 0) {
+      // the reference ignores the return value of this first call
+    }
+  }
+  if (o.n_iter_max == 0) {
+    TLGB_CUDA_TRY(cudaStreamSynchronize(st));
+    return TLGB_OK;
+  }
+
+  // ---- phases: (bf16 sweeps, then native refinement) or native sweeps only
+  struct Phase { bool tc; int sweeps; };
+  std::vector<Phase> phases;
+  if (mixed) {
+    const int refine = std::min(o.refine_sweeps, o.n_iter_max);
+    if (o.n_iter_max - refine > 0) phases.push_back({true, o.n_iter_max - refine});
+    if (refine > 0) phases.push_back({false, refine});
+  } else {
+    phases.push_back({false, o.n_iter_max});
+  }
+  const int check_every = (o.callback != nullptr) ? 1 : std::max(1, o.check_every);
+
+  StreamGuard cap;
+  if (o.use_graph) TLGB_CUDA_TRY(cudaStreamCreateWithFlags(&cap.s, cudaStreamNonBlocking));
+
+  AlsCtrl hc{};
+  int launched = 0;
+  int reported = 0;
+  bool stopped = false;
+  for (size_t pi = 0; pi < phases.size() && !stopped; ++pi) {
+    const Phase ph = phases[pi];
+    if (pi > 0) {
+      // A converged bf16 phase still gets its refinement sweeps: clear the flag.
+      TLGB_CUDA_TRY(cudaMemsetAsync(&run.B.ctrl->done, 0, sizeof(int), st));
+    }
+    GraphGuard gg;
+    if (o.use_graph) {
+      TLGB_CUDA_TRY(cudaStreamBeginCapture(cap.s, cudaStreamCaptureModeThreadLocal));
+      int rc2 = run.sweep(ph.tc, cap.s);
+      cudaGraph_t g = nullptr;
+      cudaError_t ce = cudaStreamEndCapture(cap.s, &g);
+      gg.g = g;
+      if (rc2) return rc2;
+      if (ce != cudaSuccess)
+        return set_error(TLGB_ECUDA, std::string("cp_als: graph capture: ") + cudaGetErrorString(ce));
+      TLGB_CUDA_TRY(cudaGraphInstantiate(&gg.e, gg.g, 0));
+    }
+    for (int s = 0; s < ph.sweeps; ++s) {
+      if (o.use_graph) {
+        TLGB_CUDA_TRY(cudaGraphLaunch(gg.e, st));
+      } else {
+        rc = run.sweep(ph.tc, st);
+        if (rc) return rc;
+      }
+      ++launched;
+      const bool end_of_phase = (s + 1 == ph.sweeps);
+      if (((s + 1) % check_every) == 0 || end_of_phase) {
+        TLGB_CUDA_TRY(cudaMemcpyAsync(&hc, run.B.ctrl, sizeof(AlsCtrl), cudaMemcpyDeviceToHost, st));
+        TLGB_CUDA_TRY(cudaStreamSynchronize(st));
+        if (hc.status != TLGB_OK)
+          return set_error(hc.status, "cp_als: singular normal equations (LU found a zero pivot)");
+        if (o.callback) {
+          while (reported < hc.iter) {
+            double e = 0.0;
+            TLGB_CUDA_TRY(cudaMemcpy(&e, run.B.errors + reported, sizeof(double),
+                                     cudaMemcpyDeviceToHost));
+            const int ret = o.callback(o.callback_user, reported, e);
+            ++reported;
+            if (ret != 0) { stopped = true; break; }
+          }
+        }
+        if (stopped || hc.done) break;  // callback asked to stop, or converged
+      }
+    }
+  }
+  TLGB_CUDA_TRY(cudaMemcpyAsync(&hc, run.B.ctrl, sizeof(AlsCtrl), cudaMemcpyDeviceToHost, st));
+  TLGB_CUDA_TRY(cudaStreamSynchronize(st));
+  if (hc.status != TLGB_OK)
+    return set_error(hc.status, "cp_als: singular normal equations (LU found a zero pivot)");
+  const int n = std::min(hc.iter, o.n_iter_max);
+  if (errors_host && n > 0)
+    TLGB_CUDA_TRY(cudaMemcpy(errors_host, run.B.errors, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  if (n_errors) *n_errors = n;
+  (void)launched;
+  return TLGB_OK;
+}
+
+}  // namespace
+}  // namespace tlgb
+
+using namespace tlgb;
+
+extern "C" void tlgb_cp_als_default_options(tlgb_cp_als_options* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->n_iter_max = 100;
+  o->tol = 1e-8;
+  o->l2_reg = 0.0;
+  o->cvg_criterion = 0;
+  o->normalize_factors = 0;
+  o->fixed_modes = 0;
+  o->precision = TLGB_PREC_NATIVE;
+  o->refine_sweeps = 3;
+  o->check_every = 8;
+  o->use_graph = 1;
+  o->callback = nullptr;
+  o->callback_user = nullptr;
+}
+
+extern "C" int tlgb_cp_als_workspace_size(int dtype, int ndim, const int64_t* shape, int64_t rank,
+                                          const tlgb_cp_als_options* opts, size_t* bytes) {
+  clear_error();
+  int rc = validate(dtype, ndim, shape, rank, opts);
+  if (rc) return rc;
+  TLGB_CHECK_ARG(bytes != nullptr, "cp_als_workspace_size: null pointer");
+  Shape sh = make_shape(ndim, shape);
+  Plans P;
+  rc = make_plans(dtype, sh, rank, *opts, &P);
+  if (rc) return rc;
+  AlsBuffers B;
+  rc = layout(dtype, sh, rank, *opts, P.simt, P.tc, nullptr, &B);
+  if (rc) return rc;
+  *bytes = B.bytes;
+  return TLGB_OK;
+}
+
+extern "C" int tlgb_cp_als(int dtype, const void* X, int ndim, const int64_t* shape, int64_t rank,
+                           void* const* factors, void* weights, const tlgb_cp_als_options* opts,
+                           double* errors, int* n_errors, void* workspace, size_t workspace_bytes,
+                           void* stream) {
+  clear_error();
+  int rc = validate(dtype, ndim, shape, rank, opts);
+  if (rc) return rc;
+  TLGB_CHECK_ARG(X && factors && weights && workspace, "cp_als: null pointer");
+  for (int k = 0; k < ndim; ++k) TLGB_CHECK_ARG(factors[k] != nullptr, "cp_als: null factor");
+  Shape sh = make_shape(ndim, shape);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (dtype == TLGB_F32)
+    return run<float>((const float*)X, sh, rank, (float* const*)factors, (float*)weights, *opts,
+                      errors, n_errors, workspace, workspace_bytes, st);
+  return run<double>((const double*)X, sh, rank, (double* const*)factors, (double*)weights, *opts,
+                     errors, n_errors, workspace, workspace_bytes, st);
+}
+
+extern "C" int tlgb_cp_normalize(int dtype, int ndim, const int64_t* rows, int64_t rank,
+                                 void* const* factors, void* weights, void* stream) {
+  clear_error();
+  TLGB_CHECK_ARG(dtype == TLGB_F32 || dtype == TLGB_F64, "cp_normalize: dtype must be f32 or f64");
+  TLGB_CHECK_ARG(ndim >= 1 && ndim <= kMaxModes && rows && factors && weights,
+                 "cp_normalize: bad arguments");
+  TLGB_CHECK_ARG(rank >= 1, "cp_normalize: rank must be >= 1");
+  for (int k = 0; k < ndim; ++k) TLGB_CHECK_ARG(factors[k] != nullptr, "cp_normalize: null factor");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (dtype == TLGB_F32)
+    return als_launch_normalize<float>((float* const*)factors, rows, ndim, (int)rank,
+                                       (float*)weights, nullptr, st);
+  return als_launch_normalize<double>((double* const*)factors, rows, ndim, (int)rank,
+                                      (double*)weights, nullptr, st);
+}
+
+extern "C" int tlgb_cp_norm_workspace_size(int ndim, const int64_t* rows, int64_t rank,
+                                           size_t* bytes) {
+  clear_error();
+  TLGB_CHECK_ARG(ndim >= 1 && ndim <= kMaxModes && rows && bytes, "cp_norm: bad arguments");
+  TLGB_CHECK_ARG(rank >= 1 && rank <= kMaxAlsRank, "cp_norm: rank must be in [1, 160]");
+  int64_t imax = 0;
+  for (int k = 0; k < ndim; ++k) imax = std::max(imax, rows[k]);
+  Carver c(nullptr);
+  c.take<double>((size_t)ndim * rank * rank);
+  c.take<double>((size_t)solve_blocks_for(imax) * rank * rank);
+  *bytes = c.used();
+  return TLGB_OK;
+}
+
+extern "C" int tlgb_cp_norm(int dtype, int ndim, const int64_t* rows, int64_t rank,
+                            const void* const* factors, const void* weights, double* out,
+                            void* workspace, size_t workspace_bytes, void* stream) {
+  clear_error();
+  size_t need = 0;
+  int rc = tlgb_cp_norm_workspace_size(ndim, rows, rank, &need);
+  if (rc) return rc;
+  TLGB_CHECK_ARG(dtype == TLGB_F32 || dtype == TLGB_F64, "cp_norm: dtype must be f32 or f64");
+  TLGB_CHECK_ARG(factors && out, "cp_norm: null pointer");
+  if (!workspace || workspace_bytes < need)
+    return set_error(TLGB_EWORKSPACE, "cp_norm: workspace too small");
+  int64_t imax = 0;
+  for (int k = 0; k < ndim; ++k) imax = std::max(imax, rows[k]);
+  Carver c(workspace);
+  double* G = c.take<double>((size_t)ndim * rank * rank);
+  double* gpart = c.take<double>((size_t)solve_blocks_for(imax) * rank * rank);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  rc = als_prepare(dtype);
+  if (rc) return rc;
+  const int R = (int)rank;
+  for (int k = 0; k < ndim; ++k) {
+    TLGB_CHECK_ARG(factors[k] != nullptr, "cp_norm: null factor");
+    rc = (dtype == TLGB_F32)
+             ? als_launch_gram<float>((const float*)factors[k], rows[k], R, gpart,
+                                      solve_blocks_for(imax), G + (size_t)k * R * R, nullptr, st)
+             : als_launch_gram<double>((const double*)factors[k], rows[k], R, gpart,
+                                       solve_blocks_for(imax), G + (size_t)k * R * R, nullptr, st);
+    if (rc) return rc;
+  }
+  return (dtype == TLGB_F32) ? als_launch_cp_norm<float>(G, ndim, R, (const float*)weights, out, st)
+                             : als_launch_cp_norm<double>(G, ndim, R, (const double*)weights, out, st);
+}

@@ -1,0 +1,254 @@
+"""Drop-in ``parafac`` / ``CP`` (tensorly/decomposition/_cp.py) and
+``tucker`` / ``partial_tucker`` / ``Tucker`` (tensorly/decomposition/_tucker.py)
+running on the GB300 library.
+
+The whole ALS sweep loop runs in the library (``tlgb_cp_als``); Python only
+prepares the initial factors, the options and the workspace.  Unsupported
+options raise ``NotImplementedError``; there is no CPU fallback.
+"""
+
+import ctypes
+import warnings
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._tensor import MAX_MODES, dtype_code, like, ptr, stream_of, to_device, workspace
+from .cp_tensor import (CPTensor, TuckerTensor, cp_normalize, validate_cp_rank,
+                        validate_tucker_rank)
+from .random import check_random_state
+
+
+class DecompositionMixin:
+    """tensorly/decomposition/_base_decomposition.py:5-13."""
+
+    def fit(self, tensor, **kwargs):
+        _ = self.fit_transform(tensor, **kwargs)
+        return self
+
+    def __repr__(self):
+        return f"{self.__class__.__name__} decomposition of rank {self.rank}."
+
+
+# ----------------------------------------------------------------------------
+# CP
+# ----------------------------------------------------------------------------
+def initialize_cp(tensor, rank, init="svd", svd="truncated_svd", non_negative=False,
+                  random_state=None, normalize_factors=False, mask=None, svd_mask_repeats=5):
+    """Initial CP tensor (tensorly/decomposition/_cp.py:26-137) on the tensor's device.
+
+    ``'random'``: the reference's host draws (random/base.py:104), copied once.
+    ``'svd'``: leading left singular vectors of each unfolding from the
+    library's f64 Gram eigensolver, sign-fixed like svd_flip; mode 0 scaled
+    by the singular values; random columns appended when a mode is shorter
+    than the rank (``:90-96``).
+    A CPTensor / (weights, factors): weights folded in as their geometric
+    mean (``:102-126``).
+    """
+    x, _ = to_device(tensor)
+    if mask is not None:
+        raise NotImplementedError("masked initialisation is not supported")
+    rng = check_random_state(random_state)
+    if isinstance(init, str) and init == "random":
+        factors = [torch.from_numpy(rng.random_sample((int(s), int(rank)))).to(x.device, x.dtype)
+                   for s in x.shape]
+        kt = CPTensor((None, factors))
+    elif isinstance(init, str) and init == "svd":
+        from .svd import svd_interface_unfolding
+        factors = []
+        for mode in range(x.ndim):
+            U, S = svd_interface_unfolding(x, mode, n_eigenvecs=rank, method=svd,
+                                           non_negative=non_negative)
+            if mode == 0:
+                idx = min(rank, S.shape[0])
+                U = U.clone()
+                U[:, :idx] = _scale_columns(U[:, :idx], S[:idx])
+            if x.shape[mode] < rank:
+                rp = torch.from_numpy(rng.random_sample((U.shape[0], rank - x.shape[mode])))
+                U = torch.cat([U, rp.to(x.device, x.dtype)], dim=1)
+            factors.append(U[:, :rank].contiguous())
+        kt = CPTensor((None, factors))
+    elif isinstance(init, (tuple, list, CPTensor)):
+        try:
+            if normalize_factors is True:
+                warnings.warn("It is not recommended to initialize a tensor with normalizing. "
+                              "Consider normalizing the tensor before using this function")
+            weights, factors = init
+            factors = [like(f, x) for f in factors]
+            if weights is None:
+                return CPTensor((None, factors))
+            w = like(weights, x)
+            if bool((w == 1).all()):
+                return CPTensor((None, factors))
+            avg = float(torch.prod(w.double()) ** (1.0 / w.shape[0]))
+            return CPTensor((None, [_scale_all(f, avg) for f in factors]))
+        except ValueError:
+            raise ValueError("If initialization method is a mapping, then it must "
+                             "be possible to convert it to a CPTensor instance")
+    else:
+        raise ValueError(f'Initialization method "{init}" not recognized')
+    if non_negative:
+        kt.factors = [f.abs() for f in kt.factors]
+    if normalize_factors:
+        kt = cp_normalize(kt)
+    return kt
+
+
+def _scale_columns(m, s):
+    from .tenalg import _khatri_rao_raw
+    return _khatri_rao_raw([m.contiguous()], weights=s)
+
+
+def _scale_all(m, scalar):
+    from .tenalg import _khatri_rao_raw
+    w = torch.full((m.shape[1],), scalar, dtype=m.dtype, device=m.device)
+    return _khatri_rao_raw([m.contiguous()], weights=w)
+
+
+_PRECISIONS = {"native": _lib.TLGB_PREC_NATIVE, "bf16": _lib.TLGB_PREC_BF16}
+
+
+def parafac(tensor, rank, n_iter_max=100, init="svd", svd="truncated_svd",
+            normalize_factors=False, orthogonalise=False, tol=1e-8, random_state=None,
+            verbose=0, return_errors=False, sparsity=None, l2_reg=0, mask=None,
+            cvg_criterion="abs_rec_error", fixed_modes=None, svd_mask_repeats=5,
+            linesearch=False, callback=None, *, precision="native", refine_sweeps=3,
+            check_every=8, use_graph=True):
+    """CP decomposition by ALS (tensorly/decomposition/_cp.py:230-543).
+
+    Same signature, return types and stopping rule as the reference.  The
+    keyword-only arguments select the GB300 execution: ``precision='bf16'``
+    stores an f32 tensor in bf16 and runs the tensor-core MTTKRP for all but
+    the last ``refine_sweeps`` sweeps, which run in f32; ``check_every`` is the
+    number of sweeps between host reads of the device-side stop flag;
+    ``use_graph`` replays one captured sweep as a CUDA graph.
+    """
+    if sparsity:
+        raise NotImplementedError("parafac with sparsity is not supported by tensorly_gb300")
+    if mask is not None:
+        raise NotImplementedError("masked parafac is not supported by tensorly_gb300")
+    if linesearch:
+        raise NotImplementedError("parafac line search is not supported by tensorly_gb300")
+    if orthogonalise:
+        raise NotImplementedError("parafac orthogonalise is not supported by tensorly_gb300")
+    if precision not in _PRECISIONS:
+        raise ValueError(f"precision must be one of {sorted(_PRECISIONS)}")
+    x, pl = to_device(tensor)
+    if x.ndim < 2 or x.ndim > MAX_MODES:
+        raise NotImplementedError(f"parafac supports tensors of order 2..{MAX_MODES}")
+    rank = validate_cp_rank(tuple(x.shape), rank=rank)
+    if tol and cvg_criterion not in ("abs_rec_error", "rec_error"):
+        raise TypeError("Unknown convergence criterion")
+
+    weights, factors = initialize_cp(x, rank, init=init, svd=svd, random_state=random_state,
+                                     normalize_factors=normalize_factors, mask=mask,
+                                     svd_mask_repeats=svd_mask_repeats)
+    factors = [f.to(x.dtype).contiguous().clone() for f in factors]
+    if weights is None:
+        weights = torch.ones(rank, dtype=x.dtype, device=x.device)
+    else:
+        weights = weights.to(x.dtype).contiguous().clone()
+
+    fixed = [] if fixed_modes is None else list(fixed_modes)
+    if fixed == list(range(x.ndim)):
+        return _place_cp(weights, factors, pl)
+    if x.ndim - 1 in fixed:
+        warnings.warn("You asked for fixing the last mode, which is not supported.\n The last "
+                      "mode will not be fixed. Consider using tl.moveaxis()")
+        fixed.remove(x.ndim - 1)
+    fixed_mask = 0
+    for m in fixed:
+        fixed_mask |= 1 << int(m)
+
+    lib = _lib.lib()
+    opts = _lib.CpAlsOptions()
+    lib.tlgb_cp_als_default_options(ctypes.byref(opts))
+    opts.n_iter_max = int(n_iter_max)
+    opts.tol = float(tol) if tol else 0.0
+    opts.l2_reg = float(l2_reg) if l2_reg else 0.0
+    opts.cvg_criterion = 1 if cvg_criterion == "rec_error" else 0
+    opts.normalize_factors = 1 if normalize_factors else 0
+    opts.fixed_modes = fixed_mask
+    opts.precision = _PRECISIONS[precision]
+    opts.refine_sweeps = int(refine_sweeps)
+    opts.check_every = int(check_every)
+    opts.use_graph = 1 if use_graph else 0
+
+    failure = []
+    if callback is not None:
+        def _cb(_user, iteration, rec_error):
+            try:
+                cp = _place_cp(weights.clone(), [f.clone() for f in factors], pl)
+                ret = callback(cp, float(rec_error))
+                return 1 if (iteration >= 0 and ret is True) else 0
+            except BaseException as e:  # re-raised after the library returns
+                failure.append(e)
+                return 1
+        c_cb = _lib.SWEEP_CALLBACK(_cb)
+        opts.callback = c_cb
+    shape = _lib.i64_array(x.shape)
+    nbytes = ctypes.c_size_t(0)
+    _lib.check(lib.tlgb_cp_als_workspace_size(dtype_code(x), x.ndim, shape, rank,
+                                              ctypes.byref(opts), ctypes.byref(nbytes)))
+    ws = workspace(nbytes.value, x.device)
+    errs = (ctypes.c_double * max(1, int(n_iter_max)))()
+    n_err = ctypes.c_int(0)
+    rc = lib.tlgb_cp_als(dtype_code(x), ptr(x), x.ndim, shape, rank,
+                         _lib.ptr_array([ptr(f) for f in factors]), ptr(weights),
+                         ctypes.byref(opts), errs, ctypes.byref(n_err), ptr(ws), ws.numel(),
+                         stream_of(x))
+    if failure:
+        raise failure[0]
+    _lib.check(rc)
+    rec_errors = [float(errs[i]) for i in range(n_err.value)]
+    if verbose:
+        for i, e in enumerate(rec_errors):
+            print(f"iteration {i}, reconstruction error: {e}")
+    cp = _place_cp(weights, factors, pl)
+    if return_errors:
+        return cp, rec_errors
+    return cp
+
+
+def _place_cp(weights, factors, pl):
+    return CPTensor((pl.back(weights), [pl.back(f) for f in factors]))
+
+
+class CP(DecompositionMixin):
+    """Estimator wrapper of :func:`parafac` (tensorly/decomposition/_cp.py:765-916)."""
+
+    def __init__(self, rank, n_iter_max=100, init="svd", svd="truncated_svd",
+                 normalize_factors=False, orthogonalise=False, tol=1e-8, random_state=None,
+                 verbose=0, sparsity=None, l2_reg=0, mask=None, cvg_criterion="abs_rec_error",
+                 fixed_modes=None, svd_mask_repeats=5, linesearch=False, callback=None):
+        self.rank = rank
+        self.n_iter_max = n_iter_max
+        self.init = init
+        self.svd = svd
+        self.normalize_factors = normalize_factors
+        self.orthogonalise = orthogonalise
+        self.tol = tol
+        self.random_state = random_state
+        self.verbose = verbose
+        self.sparsity = sparsity
+        self.l2_reg = l2_reg
+        self.mask = mask
+        self.cvg_criterion = cvg_criterion
+        self.fixed_modes = fixed_modes
+        self.svd_mask_repeats = svd_mask_repeats
+        self.linesearch = linesearch
+        self.callback = callback
+
+    def fit_transform(self, tensor):
+        cp_tensor, errors = parafac(
+            tensor, rank=self.rank, n_iter_max=self.n_iter_max, init=self.init, svd=self.svd,
+            normalize_factors=self.normalize_factors, orthogonalise=self.orthogonalise,
+            tol=self.tol, random_state=self.random_state, verbose=self.verbose,
+            return_errors=True, sparsity=self.sparsity, l2_reg=self.l2_reg, mask=self.mask,
+            cvg_criterion=self.cvg_criterion, fixed_modes=self.fixed_modes,
+            svd_mask_repeats=self.svd_mask_repeats, linesearch=self.linesearch,
+            callback=self.callback)
+        self.decomposition_ = cp_tensor
+        self.errors_ = errors
+        return self.decomposition_

@@ -1,0 +1,206 @@
+"""Generate the golden fixtures of the CP-ALS / Tucker path by running TensorLy.
+
+Run where the reference source tree is available (it is pure Python):
+
+    TENSORLY_REFERENCE=/root/reference python tests/golden/make_golden.py
+
+Outputs (committed, small, platform independent):
+
+* ``tenalg_kats.pkl``: every call of khatri_rao / mode_dot / multi_mode_dot /
+  unfolding_dot_khatri_rao made by the reference's own unit tests
+  (tensorly/tenalg/tests/test_khatri_rao.py, test_n_mode_product.py,
+  test_unfolding_dot_khatri_rao.py), recorded with its inputs, its output or
+  the exception it raised.  The tests run unmodified against the NumPy
+  backend with ``np.random.seed(0)``; the recorders wrap the functions the
+  test modules call and the ``assert_*`` helpers they use (which additionally
+  records the known answers the tests compare against).
+* ``reference_runs.pkl``: reference ``parafac`` / ``tucker`` / ``svd_interface``
+  outputs on seeded inputs (the tensors are regenerated from their seeds by
+  ``tensorly_gb300.workloads`` or by the case's own RandomState; each record
+  stores a checksum of the input so a regeneration mismatch is caught).
+
+Versions of numpy/scipy/tensorly used are stored in both files.
+"""
+
+import copy
+import importlib
+import os
+import pickle
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+REF = os.environ.get("TENSORLY_REFERENCE", "/root/reference")
+
+
+def _versions():
+    import scipy
+    import tensorly
+    return {"numpy": np.__version__, "scipy": scipy.__version__,
+            "tensorly": getattr(tensorly, "__version__", "?")}
+
+
+def _np(x):
+    return np.array(x, copy=True) if isinstance(x, np.ndarray) else copy.deepcopy(x)
+
+
+def record_kats():
+    import tensorly as tl
+    tl.set_backend("numpy")
+    records = []
+
+    def wrap(name, fn):
+        def recorder(*args, **kwargs):
+            rec = {"fn": name, "args": _np(list(args)), "kwargs": _np(dict(kwargs))}
+            try:
+                out = fn(*args, **kwargs)
+            except Exception as e:  # the reference's expected failures
+                rec["raises"] = type(e).__name__
+                records.append(rec)
+                raise
+            rec["result"] = _np(out)
+            records.append(rec)
+            return out
+        return recorder
+
+    def wrap_assert(name, fn):
+        def recorder(*args, **kwargs):
+            records.append({"fn": name, "args": _np(list(args)), "kwargs": _np(dict(kwargs))})
+            return fn(*args, **kwargs)
+        return recorder
+
+    mods = ["tensorly.tenalg.tests.test_khatri_rao",
+            "tensorly.tenalg.tests.test_n_mode_product",
+            "tensorly.tenalg.tests.test_unfolding_dot_khatri_rao"]
+    for mname in mods:
+        mod = importlib.import_module(mname)
+        for fname in ("khatri_rao", "mode_dot", "multi_mode_dot", "unfolding_dot_khatri_rao"):
+            if hasattr(mod, fname):
+                setattr(mod, fname, wrap(fname, getattr(mod, fname)))
+        for aname in ("assert_array_equal", "assert_array_almost_equal"):
+            if hasattr(mod, aname):
+                setattr(mod, aname, wrap_assert(aname, getattr(mod, aname)))
+        for tname in sorted(n for n in dir(mod) if n.startswith("test_")):
+            np.random.seed(0)
+            records.append({"fn": "__test__", "name": f"{mname}.{tname}"})
+            getattr(mod, tname)()
+    return records
+
+
+def reference_runs():
+    import tensorly as tl
+    from tensorly.decomposition import parafac, tucker
+    from tensorly.decomposition._cp import initialize_cp
+    from tensorly.tenalg.svd import svd_interface
+    sys.path.insert(0, REPO)
+    from tensorly_gb300 import workloads
+    tl.set_backend("numpy")
+    runs = []
+
+    def cs(x):
+        x = np.asarray(x, dtype=np.float64)
+        return [float(x.sum()), float(np.linalg.norm(x))]
+
+    # dense 64^3 f64 rank-8 parity case (init 'random', seed 0, tol 1e-8)
+    x, _ = workloads.dense_cp_small()
+    init = initialize_cp(x, 8, init="random", random_state=0)
+    cp, errs = parafac(x, 8, init="random", random_state=0, n_iter_max=100, tol=1e-8,
+                       return_errors=True)
+    runs.append({"case": "dense_cp_small", "gen": {"fn": "dense_cp_small"}, "checksum": cs(x),
+                 "kwargs": {"rank": 8, "init": "random", "random_state": 0, "n_iter_max": 100,
+                            "tol": 1e-8},
+                 "init_factors": [np.array(f) for f in init.factors],
+                 "weights": np.array(cp.weights), "factors": [np.array(f) for f in cp.factors],
+                 "errors": [float(e) for e in errs]})
+
+    def small(seed, shape, rank, dtype=np.float64, noise=0.01):
+        rs = np.random.RandomState(seed)
+        fs = [rs.uniform(size=(s, rank)) for s in shape]
+        t = tl.cp_to_tensor((None, fs))
+        n = rs.randn(*shape)
+        t = t + noise * np.linalg.norm(t) * n / np.linalg.norm(n)
+        return t.astype(dtype)
+
+    variants = [
+        ("normalize", dict(shape=(9, 8, 7), rank=3, seed=11),
+         dict(init="random", random_state=3, n_iter_max=30, tol=1e-10, normalize_factors=True)),
+        ("l2_reg", dict(shape=(9, 8, 7), rank=3, seed=12),
+         dict(init="random", random_state=4, n_iter_max=25, tol=0, l2_reg=0.05)),
+        ("fixed_mode0", dict(shape=(10, 6, 5), rank=2, seed=13),
+         dict(init="random", random_state=5, n_iter_max=20, tol=0, fixed_modes=[0])),
+        ("rec_error_crit", dict(shape=(7, 9, 8), rank=4, seed=14),
+         dict(init="random", random_state=6, n_iter_max=200, tol=1e-7,
+              cvg_criterion="rec_error")),
+        ("svd_init", dict(shape=(12, 10, 9), rank=3, seed=15),
+         dict(init="svd", n_iter_max=30, tol=1e-9)),
+        ("svd_init_short_mode", dict(shape=(4, 10, 9), rank=6, seed=16),
+         dict(init="svd", random_state=7, n_iter_max=15, tol=0)),
+        ("fourway", dict(shape=(6, 5, 7, 4), rank=3, seed=17),
+         dict(init="random", random_state=8, n_iter_max=40, tol=1e-9)),
+        ("twoway", dict(shape=(11, 9), rank=3, seed=18),
+         dict(init="random", random_state=9, n_iter_max=20, tol=0)),
+        ("fiveway", dict(shape=(4, 5, 3, 6, 4), rank=2, seed=19),
+         dict(init="random", random_state=10, n_iter_max=12, tol=0)),
+        ("rank1", dict(shape=(6, 8, 7), rank=1, seed=20),
+         dict(init="random", random_state=11, n_iter_max=20, tol=1e-10)),
+        ("f32_small", dict(shape=(16, 12, 10), rank=4, seed=21, dtype=np.float32),
+         dict(init="random", random_state=12, n_iter_max=30, tol=0)),
+    ]
+    for name, g, kw in variants:
+        x = small(g["seed"], g["shape"], g["rank"], g.get("dtype", np.float64))
+        try:
+            cp, errs = parafac(x, g["rank"], return_errors=True, **copy.deepcopy(kw))
+        except Exception as e:
+            raise RuntimeError(f"reference parafac failed on case {name}") from e
+        runs.append({"case": name, "gen": {"fn": "small", **g}, "checksum": cs(x),
+                     "kwargs": {"rank": g["rank"], **kw},
+                     "weights": np.array(cp.weights),
+                     "factors": [np.array(f) for f in cp.factors],
+                     "errors": [float(e) for e in errs]})
+
+    # Tucker (HOOI) small cases
+    tcases = [
+        ("tucker_svd", dict(shape=(12, 10, 8), seed=31), dict(rank=[3, 4, 2], init="svd",
+                                                             n_iter_max=20, tol=1e-9)),
+        ("tucker_random", dict(shape=(9, 8, 10), seed=32), dict(rank=[2, 3, 3], init="random",
+                                                               random_state=1, n_iter_max=15,
+                                                               tol=0)),
+        ("tucker_4way", dict(shape=(6, 7, 5, 8), seed=33), dict(rank=[2, 3, 2, 3], init="svd",
+                                                               n_iter_max=10, tol=1e-10)),
+    ]
+    for name, g, kw in tcases:
+        rs = np.random.RandomState(g["seed"])
+        x = rs.randn(*g["shape"])
+        tt, errs = tucker(x, return_errors=True, **copy.deepcopy(kw))
+        runs.append({"case": name, "gen": {"fn": "randn", **g}, "checksum": cs(x),
+                     "kwargs": kw, "core": np.array(tt.core),
+                     "factors": [np.array(f) for f in tt.factors],
+                     "errors": [float(e) for e in errs]})
+
+    # svd_interface of a tall and a wide matrix
+    for name, shape, k in (("svd_wide", (7, 30), 4), ("svd_tall", (25, 6), 3)):
+        rs = np.random.RandomState(40 + shape[0])
+        m = rs.randn(*shape)
+        U, S, V = svd_interface(m, n_eigenvecs=k)
+        runs.append({"case": name, "gen": {"fn": "randn", "shape": shape, "seed": 40 + shape[0]},
+                     "checksum": cs(m), "kwargs": {"n_eigenvecs": k},
+                     "U": np.array(U), "S": np.array(S), "V": np.array(V)})
+    return runs
+
+
+def main():
+    sys.path.insert(0, REF)
+    import tensorly  # noqa: F401  (the reference)
+    kats = record_kats()
+    with open(os.path.join(HERE, "tenalg_kats.pkl"), "wb") as f:
+        pickle.dump({"versions": _versions(), "records": kats}, f, protocol=4)
+    runs = reference_runs()
+    with open(os.path.join(HERE, "reference_runs.pkl"), "wb") as f:
+        pickle.dump({"versions": _versions(), "runs": runs}, f, protocol=4)
+    print(f"{len(kats)} tenalg records, {len(runs)} reference runs")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,30 @@
+"""Regenerates the inputs of the golden reference runs from their seeds."""
+
+import numpy as np
+
+from oracle import cp_to_tensor
+from tensorly_gb300 import workloads
+
+
+def small_cp(seed, shape, rank, dtype=np.float64, noise=0.01):
+    rs = np.random.RandomState(seed)
+    fs = [rs.uniform(size=(s, rank)) for s in shape]
+    t = cp_to_tensor((None, fs))
+    n = rs.randn(*shape)
+    t = t + noise * np.linalg.norm(t) * n / np.linalg.norm(n)
+    return t.astype(dtype)
+
+
+def regenerate(run):
+    g = run["gen"]
+    if g["fn"] == "dense_cp_small":
+        x, _ = workloads.dense_cp_small()
+    elif g["fn"] == "small":
+        x = small_cp(g["seed"], g["shape"], g["rank"], g.get("dtype", np.float64))
+    elif g["fn"] == "randn":
+        x = np.random.RandomState(g["seed"]).randn(*g["shape"])
+    else:
+        raise KeyError(g["fn"])
+    cs = [float(np.asarray(x, np.float64).sum()), float(np.linalg.norm(np.asarray(x, np.float64)))]
+    np.testing.assert_allclose(cs, run["checksum"], rtol=1e-12, atol=1e-12)
+    return x

@@ -1,0 +1,82 @@
+"""The C ABI library builds, loads without a GPU and exports every entry
+point that include/tensorly_gb300.h declares (no compute calls here)."""
+
+import ctypes
+import os
+import re
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(REPO, "include", "tensorly_gb300.h")
+
+
+def declared_symbols():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = set(re.findall(r"\b(tlgb_[a-z0-9_]+)\s*\(", text))
+    names.discard("tlgb_sweep_callback")
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def library():
+    from tensorly_gb300 import _build
+    path = _build.build()
+    return ctypes.CDLL(path)
+
+
+def test_header_declares_entry_points():
+    syms = declared_symbols()
+    for s in ("tlgb_mttkrp", "tlgb_khatri_rao", "tlgb_mode_dot", "tlgb_cp_als",
+              "tlgb_cp_als_workspace_size", "tlgb_last_error"):
+        assert s in syms
+
+
+def test_every_declared_symbol_is_exported(library):
+    missing = [s for s in declared_symbols() if not hasattr(library, s)]
+    assert not missing, f"not exported: {missing}"
+
+
+def test_python_binding_covers_header():
+    from tensorly_gb300 import _lib
+    bound = {name for name, _, _ in _lib.SIGNATURES}
+    assert set(declared_symbols()) <= bound
+
+
+def test_header_has_no_torch_types():
+    text = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    for bad in ("torch", "at::", "Tensor", "c10", "cudaStream_t"):
+        assert bad not in text
+
+
+def test_version_and_error_string(library):
+    library.tlgb_version.restype = ctypes.c_int
+    assert library.tlgb_version() >= 100
+    library.tlgb_last_error.restype = ctypes.c_char_p
+    assert isinstance(library.tlgb_last_error(), bytes)
+
+
+def test_argument_validation_without_gpu(library):
+    """Host-side checks reject bad arguments before any CUDA call."""
+    from tensorly_gb300 import _lib
+    lib = _lib.lib()
+    nbytes = ctypes.c_size_t(0)
+    shape = _lib.i64_array([4, 5, 6])
+    assert lib.tlgb_mttkrp_workspace_size(_lib.TLGB_F32, 3, shape, 2, 3,
+                                          ctypes.byref(nbytes)) == _lib.TLGB_EINVAL
+    assert b"mode" in lib.tlgb_last_error()
+    assert lib.tlgb_mttkrp_workspace_size(7, 3, shape, 2, 0, ctypes.byref(nbytes)) == _lib.TLGB_EINVAL
+    assert lib.tlgb_mttkrp_workspace_size(_lib.TLGB_F64, 9, shape, 2, 0,
+                                          ctypes.byref(nbytes)) == _lib.TLGB_EINVAL
+    opts = _lib.CpAlsOptions()
+    lib.tlgb_cp_als_default_options(ctypes.byref(opts))
+    assert opts.n_iter_max == 100 and abs(opts.tol - 1e-8) < 1e-20 and opts.use_graph == 1
+    opts.precision = _lib.TLGB_PREC_BF16
+    rc = lib.tlgb_cp_als_workspace_size(_lib.TLGB_F64, 3, shape, 2, ctypes.byref(opts),
+                                        ctypes.byref(nbytes))
+    assert rc == _lib.TLGB_EUNSUPPORTED
+    opts.precision = _lib.TLGB_PREC_NATIVE
+    rc = lib.tlgb_cp_als_workspace_size(_lib.TLGB_F64, 3, shape, 500, ctypes.byref(opts),
+                                        ctypes.byref(nbytes))
+    assert rc == _lib.TLGB_EUNSUPPORTED
