@@ -79,6 +79,41 @@ int tlgb_mttkrp(int dtype, const void* X, int ndim, const int64_t* shape,
                 void* out, void* workspace, size_t workspace_bytes, void* stream);
 
 /*
+ * MTTKRP on the bf16 tensor cores (tcgen05, TMA): same contraction as
+ * tlgb_mttkrp with X stored in bf16 and f32 accumulation.
+ * X: bf16 tensor; factors[k]: f32 (shape[k] x rank) for the scaling modes;
+ * factors_bf16_t[k]: the contracted inner factor (mode ndim-1, or ndim-2 when
+ * mode == ndim-1) transposed and split into two bf16 planes, each rank x
+ * shape[k] row-major: hi = bf16(A^T), then lo = bf16(A^T - hi); the kernel
+ * contracts with hi + lo (about 16 significant bits).  Pointers of other
+ * modes may be NULL.  weights: f32 rank or NULL.
+ * out: f32 shape[mode] x rank.  Requirements (else TLGB_EUNSUPPORTED):
+ * rank <= 128, the inner mode a multiple of 8 (and shape[ndim-1] a multiple
+ * of 8 when mode == ndim-1), inner mode * padded rank * 2 bytes <= 96 KiB.
+ * The first int of the workspace receives TLGB_ETIMEOUT if the kernel's
+ * bounded pipeline waits expired (read it with tlgb_workspace_status).
+ * Replaces tensorly/tenalg/core_tenalg/mttkrp.py:9-50 for bf16 storage.
+ */
+int tlgb_mttkrp_bf16_workspace_size(int ndim, const int64_t* shape, int64_t rank, int mode,
+                                    size_t* bytes);
+int tlgb_mttkrp_bf16(const void* X, int ndim, const int64_t* shape, const void* const* factors,
+                     const void* const* factors_bf16_t, const void* weights, int64_t rank,
+                     int mode, void* out, void* workspace, size_t workspace_bytes, void* stream);
+
+/*
+ * Tile-plan knobs of the bf16 tensor-core MTTKRP (used by the autotuner;
+ * value 0 restores the default): "tc_group_kib" = bytes of the split inner
+ * factor kept resident per CTA (KiB; sets how the inner mode is partitioned
+ * across CTAs), "tc_stages" = cap on the tensor-tile ring depth,
+ * "tc_waves" = CTAs per SM in the grid.  Process-wide; no counterpart in
+ * TensorLy.
+ */
+int tlgb_set_tuning(const char* key, int value);
+
+/* Synchronises `stream` and reads the status int at the start of a workspace. */
+int tlgb_workspace_status(const void* workspace, void* stream, int* status);
+
+/*
  * Tensor-times-matrix: out = X x_mode U, i.e. fold(U . unfold(X, mode)).
  * U is J x shape[mode] (row-major); with transpose != 0, U is shape[mode] x J
  * and U^T is applied.  out has shape[mode] replaced by J.

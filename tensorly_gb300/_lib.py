@@ -64,6 +64,14 @@ SIGNATURES = [
      [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, _c_i64p, _c_vpp, ctypes.c_void_p,
       ctypes.c_int64, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
       ctypes.c_void_p]),
+    ("tlgb_mttkrp_bf16_workspace_size", ctypes.c_int,
+     [ctypes.c_int, _c_i64p, ctypes.c_int64, ctypes.c_int, ctypes.POINTER(ctypes.c_size_t)]),
+    ("tlgb_mttkrp_bf16", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_int, _c_i64p, _c_vpp, _c_vpp, ctypes.c_void_p, ctypes.c_int64,
+      ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    ("tlgb_set_tuning", ctypes.c_int, [ctypes.c_char_p, ctypes.c_int]),
+    ("tlgb_workspace_status", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
     ("tlgb_mode_dot", ctypes.c_int,
      [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, _c_i64p, ctypes.c_void_p, ctypes.c_int64,
       ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),

@@ -42,13 +42,22 @@ __device__ double block_sum(double v, double* scratch /* >= 32 */) {
 template <typename T>
 __global__ void k_sumsq(const T* __restrict__ X, int64_t n, double* part) {
   __shared__ double scratch[32];
-  double s = 0.0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const double x = (double)X[i];
-    s = fma(x, x, s);
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;  // independent f64 chains
+  const int64_t step = (int64_t)gridDim.x * blockDim.x;
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  for (; i + 3 * step < n; i += 4 * step) {
+    const double x0 = (double)X[i], x1 = (double)X[i + step];
+    const double x2 = (double)X[i + 2 * step], x3 = (double)X[i + 3 * step];
+    s0 = fma(x0, x0, s0);
+    s1 = fma(x1, x1, s1);
+    s2 = fma(x2, x2, s2);
+    s3 = fma(x3, x3, s3);
   }
-  s = block_sum(s, scratch);
+  for (; i < n; i += step) {
+    const double x = (double)X[i];
+    s0 = fma(x, x, s0);
+  }
+  double s = block_sum((s0 + s1) + (s2 + s3), scratch);
   if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 
@@ -99,13 +108,33 @@ __global__ void k_gram_partial(const T* __restrict__ A, int64_t I, int R, int64_
   }
 }
 
-__global__ void k_gram_reduce(const double* __restrict__ gpart, int nparts, int RR, double* G,
-                              const int* done) {
+// G[e] = sum_p gpart[p][e].  Block b owns 32 consecutive entries (one per
+// lane, coalesced); its 8 warps take every 8th partial with four loads in
+// flight each, then the warps' sums are combined in a fixed order.
+__global__ void __launch_bounds__(256)
+k_gram_reduce(const double* __restrict__ gpart, int nparts, int RR, double* G, const int* done) {
   if (done && *done) return;
-  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < RR; e += gridDim.x * blockDim.x) {
-    double s = 0.0;
-    for (int p = 0; p < nparts; ++p) s += gpart[(int64_t)p * RR + e];
-    G[e] = s;
+  __shared__ double red[8][33];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int e = blockIdx.x * 32 + lane;
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+  if (e < RR) {
+    int p = warp;
+    for (; p + 24 < nparts; p += 32) {
+      s0 += gpart[(int64_t)p * RR + e];
+      s1 += gpart[(int64_t)(p + 8) * RR + e];
+      s2 += gpart[(int64_t)(p + 16) * RR + e];
+      s3 += gpart[(int64_t)(p + 24) * RR + e];
+    }
+    for (; p < nparts; p += 8) s0 += gpart[(int64_t)p * RR + e];
+  }
+  red[warp][lane] = (s0 + s1) + (s2 + s3);
+  __syncthreads();
+  if (warp == 0 && e < RR) {
+    double t = 0.0;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) t += red[w][lane];
+    G[e] = t;
   }
 }
 
@@ -125,11 +154,101 @@ __device__ void build_v(double* V, const double* G, int ndim, int mode, int R, c
   }
 }
 
-// fac layout: [R*R] factor(s), then [R] reciprocal diagonal.
-template <typename T>
-__global__ void k_factorize(const double* G, int ndim, int mode, int R, const T* w, double l2,
-                            double* fac, int* perm, AlsCtrl* ctrl) {
+// ---- fast path: f32 Gauss-Jordan inverse of V, matrix held in registers.
+// Thread (ti, tj) of a TI x TJ grid owns rows ti + TI*u and columns tj + TJ*v;
+// per pivot only row k and column k pass through shared memory.  No dynamic
+// shared memory and few threads, so the kernel can share an SM with the
+// tensor-core MTTKRP it runs beside.  Pivots of Gauss-Jordan are the Schur
+// complement pivots, so their spread bounds cond(V) from below; a spread
+// above kIrMaxPivotRatio (or a non-positive pivot) hands V to the f64 kernel.
+constexpr float kIrMaxPivotRatio = 1e5f;
+
+template <typename T, int TI, int TJ, int NI, int NJ>
+__global__ void __launch_bounds__(TI * TJ)
+k_factorize_fast(const double* __restrict__ G, int ndim, int mode, int R, const T* w, double l2,
+                 double* vmat, float* w32, AlsCtrl* ctrl) {
   if (ctrl->done) return;
+  __shared__ float rowk[NJ * TJ], colk[NI * TI];
+  const int ti = threadIdx.x / TJ, tj = threadIdx.x - (threadIdx.x / TJ) * TJ;
+  const int RR = R * R;
+  float a[NI][NJ];
+#pragma unroll
+  for (int u = 0; u < NI; ++u)
+#pragma unroll
+    for (int v = 0; v < NJ; ++v) {
+      const int i = ti + TI * u, j = tj + TJ * v;
+      float val = 0.f;
+      if (i < R && j < R) {   // V = (prod_{k != mode} G_k + l2 I) * w w^T, in f64
+        const int e = i * R + j;
+        double g = 1.0;
+        for (int k = 0; k < ndim; ++k)
+          if (k != mode) g = g * G[(int64_t)k * RR + e];
+        if (i == j) g = g + l2;
+        if (w) g = ((double)w[i] * g) * (double)w[j];
+        vmat[e] = g;
+        val = (float)g;
+      }
+      a[u][v] = val;
+    }
+  float pmin = 3.0e38f, pmax = 0.f;
+  bool ok = true;
+  for (int k = 0; k < R; ++k) {
+    const int ku = k / TI, kv = k / TJ;
+    if (k - ku * TI == ti) {
+#pragma unroll
+      for (int u = 0; u < NI; ++u)
+        if (u == ku)
+#pragma unroll
+          for (int v = 0; v < NJ; ++v) rowk[tj + TJ * v] = a[u][v];
+    }
+    if (k - kv * TJ == tj) {
+#pragma unroll
+      for (int v = 0; v < NJ; ++v)
+        if (v == kv)
+#pragma unroll
+          for (int u = 0; u < NI; ++u) colk[ti + TI * u] = a[u][v];
+    }
+    __syncthreads();
+    const float p = rowk[k];
+    if (!(p > 0.f)) { ok = false; break; }  // uniform: every thread read the same p
+    pmin = fminf(pmin, p);
+    pmax = fmaxf(pmax, p);
+    const float inv = 1.0f / p;
+#pragma unroll
+    for (int u = 0; u < NI; ++u) {
+      const int i = ti + TI * u;
+      const float fi = colk[i] * inv;
+#pragma unroll
+      for (int v = 0; v < NJ; ++v) {
+        const int j = tj + TJ * v;
+        const float rj = rowk[j];
+        const float upd = fmaf(-fi, rj, a[u][v]);
+        a[u][v] = (i == k) ? ((j == k) ? inv : a[u][v] * inv) : ((j == k) ? -fi : upd);
+      }
+    }
+    __syncthreads();
+  }
+  if (ok && pmax > kIrMaxPivotRatio * pmin) ok = false;
+  if (ok) {
+#pragma unroll
+    for (int u = 0; u < NI; ++u)
+#pragma unroll
+      for (int v = 0; v < NJ; ++v) {
+        const int i = ti + TI * u, j = tj + TJ * v;
+        if (i < R && j < R) w32[i * R + j] = a[u][v];
+      }
+  }
+  if (threadIdx.x == 0) ctrl->fac_kind = ok ? 2 : 3;
+}
+
+// ---- fallback: f64 Cholesky (fac_kind 0) or LU with partial pivoting
+// (fac_kind 1) of V when the fast path reported fac_kind 3; fac layout
+// [R*R] factor(s) then [R] reciprocal diagonal.
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_factorize(const double* G, int ndim, int mode, int R, const T* w, double l2, double* fac,
+            int* perm, AlsCtrl* ctrl) {
+  if (ctrl->done || ctrl->fac_kind != 3) return;
   extern __shared__ double V[];  // R*R
   __shared__ int s_fail;
   __shared__ int s_piv;
@@ -232,117 +351,259 @@ __device__ __forceinline__ void put(double (&v)[kRQ], int q, double x) {
     if (q == i) v[i] = x;
 }
 
+constexpr int kSolveThreads = 32 * kSolveWarps;
+constexpr double kIrStop = 1e-12;   // stop refining once max|correction| <= kIrStop max|x|
+
+// Store one solved row: the factor (tensor dtype), its bf16 split transposed
+// copy for the tensor cores, the stored value (f64) for the Gram, and the
+// row's contribution to <M, A>.
 template <typename T>
-__global__ void __launch_bounds__(32 * kSolveWarps)
+__device__ __forceinline__ double store_entry(T* A, __nv_bfloat16* A_bt, int64_t I, int R,
+                                              int64_t row, int r, double x, double* rb) {
+  const T xv = (T)x;
+  A[row * R + r] = xv;
+  const double xd = (double)xv;
+  rb[r] = xd;
+  if (A_bt) {  // bf16 split transposed copy (hi, lo planes) for the tensor cores
+    const float xf = (float)xv;
+    const __nv_bfloat16 hi = __float2bfloat16_rn(xf);
+    A_bt[(int64_t)r * I + row] = hi;
+    A_bt[(int64_t)R * I + (int64_t)r * I + row] = __float2bfloat16_rn(xf - __bfloat162float(hi));
+  }
+  return xd;
+}
+
+// Sum of the MTTKRP split partials of one entry, four independent f64 chains.
+template <typename T>
+__device__ __forceinline__ double sum_splits(const T* __restrict__ partial, int splits,
+                                             int64_t stride, int64_t off) {
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+  int p = 0;
+  for (; p + 3 < splits; p += 4) {
+    s0 += (double)partial[(int64_t)p * stride + off];
+    s1 += (double)partial[(int64_t)(p + 1) * stride + off];
+    s2 += (double)partial[(int64_t)(p + 2) * stride + off];
+    s3 += (double)partial[(int64_t)(p + 3) * stride + off];
+  }
+  for (; p < splits; ++p) s0 += (double)partial[(int64_t)p * stride + off];
+  return (s0 + s1) + (s2 + s3);
+}
+
+// Solves A_mode = M V^-1 for a block of rows (V symmetric), writes the factor
+// and the block's Gram and <M, A> partial sums.
+//   fac_kind 2: x = M W32 (f32 inverse), then up to kIrMaxPasses passes of
+//     mixed-precision iterative refinement x += W32 (m - V x) with the
+//     residual in f64; every dot product is split into independent chains
+//     (f64 FMA latency is long on this GPU, so long chains would dominate).
+//   fac_kind 0/1: forward/back substitution with the f64 Cholesky or LU
+//     factors, one warp per row.
+template <typename T>
+__global__ void __launch_bounds__(kSolveThreads)
 k_solve(const T* __restrict__ partial, int splits, int64_t I, int R,
-        const double* __restrict__ fac, const int* __restrict__ perm, T* A,
+        const double* __restrict__ fac, const int* __restrict__ perm,
+        const double* __restrict__ vmat, const float* __restrict__ w32, T* A,
         __nv_bfloat16* A_bt, double* gpart, double* ipart, AlsCtrl* ctrl, int64_t rpb,
-        int fac_in_smem) {
+        int mats_in_smem, int max_passes) {
   if (ctrl->done) return;
   extern __shared__ double sm[];
   const int RR = R * R;
-  double* gacc = sm;                      // RR
-  double* rowbuf = gacc + RR;             // kSolveWarps * R
-  double* sfac = rowbuf + kSolveWarps * R;  // RR + R (optional)
-  __shared__ double s_ip[kSolveWarps];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int kind = ctrl->fac_kind;
+  __shared__ double s_ip[kSolveWarps];
+  __shared__ unsigned long long s_dmax, s_xmax;
+  double* gacc = sm;                          // RR
   for (int e = tid; e < RR; e += blockDim.x) gacc[e] = 0.0;
-  if (fac_in_smem)
-    for (int e = tid; e < RR + R; e += blockDim.x) sfac[e] = fac[e];
-  __syncthreads();
-  const double* F = fac_in_smem ? sfac : fac;
-  const double* invd = F + RR;
   const int64_t row0 = blockIdx.x * rpb;
   const int64_t row1 = min(row0 + rpb, I);
-  double ip = 0.0;
   const int64_t IR = I * R;
-  for (int64_t base = row0; base < row1; base += kSolveWarps) {
-    const int64_t row = base + warp;
-    double* rb = rowbuf + warp * R;
-    if (row < row1) {
-      double v[kRQ], mv[kRQ];
-#pragma unroll
-      for (int q = 0; q < kRQ; ++q) {
-        const int r = lane + 32 * q;
-        double s = 0.0;
-        if (r < R)
-          for (int p = 0; p < splits; ++p) s += (double)partial[(int64_t)p * IR + row * R + r];
-        mv[q] = s;
-        v[q] = s;
+  double ip = 0.0;
+
+  if (kind == 2) {
+    // ------------------------------------------------ refinement path
+    const int RB = max(1, kSolveThreads / R);   // rows per round
+    double* mb = gacc + RR;                     // [RB][R] right-hand sides
+    double* xb = mb + RB * R;                   // [RB][R] solution
+    double* rb = xb + RB * R;                   // [RB][R] residual, then stored values
+    float* mbf = reinterpret_cast<float*>(rb + RB * R);   // [RB][R] f32 copy of m
+    float* rbf = mbf + RB * R;                              // [RB][R] f32 copy of r
+    const double* Vm = vmat;
+    const float* Wm = w32;
+    if (mats_in_smem) {
+      double* Vs = rb + 2 * RB * R;
+      float* Ws = reinterpret_cast<float*>(Vs + RR);
+      for (int e = tid; e < RR; e += blockDim.x) { Vs[e] = vmat[e]; Ws[e] = w32[e]; }
+      Vm = Vs;
+      Wm = Ws;
+    }
+    __syncthreads();
+    const int rr = tid / R, c = tid - (tid / R) * R;
+    const bool act = tid < RB * R;
+    for (int64_t base = row0; base < row1; base += RB) {
+      const int64_t row = base + rr;
+      const bool live = act && row < row1;
+      if (act) {
+        const double mv = live ? sum_splits(partial, splits, IR, row * R + c) : 0.0;
+        mb[rr * R + c] = mv;
+        mbf[rr * R + c] = (float)mv;
       }
-      if (kind == 1) {  // b = P m
-#pragma unroll
-        for (int q = 0; q < kRQ; ++q) {
-          const int r = lane + 32 * q;
-          if (r < R) rb[r] = v[q];
+      __syncthreads();
+      if (act) {   // x0 = m W32 (f32)
+        const float* m = mbf + rr * R;
+        float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+        int k = 0;
+        for (; k + 3 < R; k += 4) {
+          a0 = fmaf(m[k], Wm[k * R + c], a0);
+          a1 = fmaf(m[k + 1], Wm[(k + 1) * R + c], a1);
+          a2 = fmaf(m[k + 2], Wm[(k + 2) * R + c], a2);
+          a3 = fmaf(m[k + 3], Wm[(k + 3) * R + c], a3);
         }
-        __syncwarp();
-#pragma unroll
-        for (int q = 0; q < kRQ; ++q) {
-          const int r = lane + 32 * q;
-          if (r < R) v[q] = rb[perm[r]];
-        }
-        __syncwarp();
+        for (; k < R; ++k) a0 = fmaf(m[k], Wm[k * R + c], a0);
+        xb[rr * R + c] = (double)((a0 + a1) + (a2 + a3));
       }
-      // forward substitution with the lower factor
-      for (int j = 0; j < R; ++j) {
-        const int qj = j >> 5;
-        double yj = __shfl_sync(0xffffffffu, pick(v, qj), j & 31);
-        if (kind == 0) yj *= invd[j];
-        if (lane == (j & 31)) put(v, qj, yj);
+      __syncthreads();
+      for (int pass = 0; pass < max_passes; ++pass) {
+        if (tid == 0) { s_dmax = 0ull; s_xmax = 0ull; }
+        if (act) {   // r = m - x V (f64, eight chains)
+          const double* x = xb + rr * R;
+          double q[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+          int k = 0;
+          for (; k + 7 < R; k += 8)
 #pragma unroll
-        for (int q = 0; q < kRQ; ++q) {
-          const int i = lane + 32 * q;
-          if (i > j && i < R) v[q] = fma(-F[i * R + j], yj, v[q]);
+            for (int u = 0; u < 8; ++u) q[u] = fma(x[k + u], Vm[(k + u) * R + c], q[u]);
+          for (; k < R; ++k) q[0] = fma(x[k], Vm[k * R + c], q[0]);
+          const double vx = ((q[0] + q[1]) + (q[2] + q[3])) + ((q[4] + q[5]) + (q[6] + q[7]));
+          rbf[rr * R + c] = (float)(mb[rr * R + c] - vx);
         }
-      }
-      // back substitution with the upper factor (L^T for Cholesky)
-      for (int j = R - 1; j >= 0; --j) {
-        const int qj = j >> 5;
-        const double xj = __shfl_sync(0xffffffffu, pick(v, qj), j & 31) * invd[j];
-        if (lane == (j & 31)) put(v, qj, xj);
-#pragma unroll
-        for (int q = 0; q < kRQ; ++q) {
-          const int i = lane + 32 * q;
-          if (i < j) {
-            const double u = (kind == 0) ? F[j * R + i] : F[i * R + j];
-            v[q] = fma(-u, xj, v[q]);
+        __syncthreads();
+        if (act) {   // x += r W32 (f32 product of the small residual)
+          const float* r = rbf + rr * R;
+          float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+          int k = 0;
+          for (; k + 3 < R; k += 4) {
+            a0 = fmaf(r[k], Wm[k * R + c], a0);
+            a1 = fmaf(r[k + 1], Wm[(k + 1) * R + c], a1);
+            a2 = fmaf(r[k + 2], Wm[(k + 2) * R + c], a2);
+            a3 = fmaf(r[k + 3], Wm[(k + 3) * R + c], a3);
+          }
+          for (; k < R; ++k) a0 = fmaf(r[k], Wm[k * R + c], a0);
+          const double d = (double)((a0 + a1) + (a2 + a3));
+          const double xn = xb[rr * R + c] + d;
+          xb[rr * R + c] = xn;
+          if (live) {  // non-negative doubles order like their bit patterns
+            atomicMax(&s_dmax, (unsigned long long)__double_as_longlong(fabs(d)));
+            atomicMax(&s_xmax, (unsigned long long)__double_as_longlong(fabs(xn)));
           }
         }
+        __syncthreads();
+        const bool stop = __longlong_as_double((long long)s_dmax) <=
+                          kIrStop * __longlong_as_double((long long)s_xmax);
+        __syncthreads();  // everyone has read the maxima before they are reset
+        if (stop) break;
       }
+      if (live) {
+        const double xd = store_entry(A, A_bt, I, R, row, c, xb[rr * R + c], rb + rr * R);
+        ip = fma(mb[rr * R + c], xd, ip);
+      } else if (act) {
+        rb[rr * R + c] = 0.0;
+      }
+      __syncthreads();
+      for (int e = tid; e < RR; e += blockDim.x) {   // Gram of the stored rows
+        const int r = e / R, s2 = e - (e / R) * R;
+        if (s2 > r) continue;
+        double g = gacc[e];
+        for (int w = 0; w < RB; ++w) g = fma(rb[w * R + r], rb[w * R + s2], g);
+        gacc[e] = g;
+      }
+      __syncthreads();
+    }
+  } else {
+    // ------------------------------------------------ substitution path
+    double* rowbuf = gacc + RR;                    // kSolveWarps * R
+    double* sfac = rowbuf + kSolveWarps * R;       // RR + R (optional)
+    if (mats_in_smem)
+      for (int e = tid; e < RR + R; e += blockDim.x) sfac[e] = fac[e];
+    __syncthreads();
+    const double* F = mats_in_smem ? sfac : fac;
+    const double* invd = F + RR;
+    for (int64_t base = row0; base < row1; base += kSolveWarps) {
+      const int64_t row = base + warp;
+      double* rb = rowbuf + warp * R;
+      if (row < row1) {
+        double v[kRQ], mv[kRQ];
 #pragma unroll
-      for (int q = 0; q < kRQ; ++q) {
-        const int r = lane + 32 * q;
-        if (r < R) {
-          const T x = (T)v[q];
-          A[row * R + r] = x;
-          const double xd = (double)x;
-          rb[r] = xd;
-          if (A_bt) A_bt[(int64_t)r * I + row] = __float2bfloat16_rn((float)x);
-          ip = fma(mv[q], xd, ip);
+        for (int q = 0; q < kRQ; ++q) {
+          const int r = lane + 32 * q;
+          const double s = (r < R) ? sum_splits(partial, splits, IR, row * R + r) : 0.0;
+          mv[q] = s;
+          v[q] = s;
         }
-      }
-    } else {
-      for (int r = lane; r < R; r += 32) rb[r] = 0.0;
-    }
-    __syncthreads();
-    for (int e = tid; e < RR; e += blockDim.x) {
-      const int r = e / R, s = e % R;
-      if (s > r) continue;
-      double g = gacc[e];
+        if (kind == 1) {  // b = P m
 #pragma unroll
-      for (int w = 0; w < kSolveWarps; ++w) g = fma(rowbuf[w * R + r], rowbuf[w * R + s], g);
-      gacc[e] = g;
+          for (int q = 0; q < kRQ; ++q) {
+            const int r = lane + 32 * q;
+            if (r < R) rb[r] = v[q];
+          }
+          __syncwarp();
+#pragma unroll
+          for (int q = 0; q < kRQ; ++q) {
+            const int r = lane + 32 * q;
+            if (r < R) v[q] = rb[perm[r]];
+          }
+          __syncwarp();
+        }
+        for (int j = 0; j < R; ++j) {   // forward substitution, lower factor
+          const int qj = j >> 5;
+          double yj = __shfl_sync(0xffffffffu, pick(v, qj), j & 31);
+          if (kind == 0) yj *= invd[j];
+          if (lane == (j & 31)) put(v, qj, yj);
+#pragma unroll
+          for (int q = 0; q < kRQ; ++q) {
+            const int i = lane + 32 * q;
+            if (i > j && i < R) v[q] = fma(-F[i * R + j], yj, v[q]);
+          }
+        }
+        for (int j = R - 1; j >= 0; --j) {   // back substitution, upper factor (L^T for Cholesky)
+          const int qj = j >> 5;
+          const double xj = __shfl_sync(0xffffffffu, pick(v, qj), j & 31) * invd[j];
+          if (lane == (j & 31)) put(v, qj, xj);
+#pragma unroll
+          for (int q = 0; q < kRQ; ++q) {
+            const int i = lane + 32 * q;
+            if (i < j) {
+              const double u = (kind == 0) ? F[j * R + i] : F[i * R + j];
+              v[q] = fma(-u, xj, v[q]);
+            }
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < kRQ; ++q) {
+          const int r = lane + 32 * q;
+          if (r < R) {
+            const double xd = store_entry(A, A_bt, I, R, row, r, v[q], rb);
+            ip = fma(mv[q], xd, ip);
+          }
+        }
+      } else {
+        for (int r = lane; r < R; r += 32) rb[r] = 0.0;
+      }
+      __syncthreads();
+      for (int e = tid; e < RR; e += blockDim.x) {
+        const int r = e / R, s2 = e - (e / R) * R;
+        if (s2 > r) continue;
+        double g = gacc[e];
+#pragma unroll
+        for (int w = 0; w < kSolveWarps; ++w) g = fma(rowbuf[w * R + r], rowbuf[w * R + s2], g);
+        gacc[e] = g;
+      }
+      __syncthreads();
     }
-    __syncthreads();
   }
   ip = warp_sum(ip);
   if (lane == 0) s_ip[warp] = ip;
   double* out = gpart + (int64_t)blockIdx.x * RR;
   for (int e = tid; e < RR; e += blockDim.x) {
-    const int r = e / R, s = e % R;
-    out[e] = (s <= r) ? gacc[r * R + s] : gacc[s * R + r];
+    const int r = e / R, s2 = e - (e / R) * R;
+    out[e] = (s2 <= r) ? gacc[r * R + s2] : gacc[s2 * R + r];
   }
   __syncthreads();
   if (ipart && tid == 0) {
@@ -353,21 +614,43 @@ k_solve(const T* __restrict__ partial, int splits, int64_t I, int R,
 }
 
 // ---------------------------------------------------------------- fit
+// Hadamard product of all Grams scaled by w w^T, summed (= cp_norm^2); four
+// entries per thread in flight so the f64 products do not form one chain.
+template <typename T>
+__device__ double sum_gram_product(const double* G, int ndim, int R, const T* w) {
+  const int RR = R * R;
+  double acc = 0.0;
+  for (int e0 = threadIdx.x; e0 < RR; e0 += 4 * blockDim.x) {
+    double v[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) v[j] = 0.0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int e = e0 + j * blockDim.x;
+      if (e < RR) v[j] = 1.0;
+    }
+    for (int k = 0; k < ndim; ++k)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int e = e0 + j * blockDim.x;
+        if (e < RR) v[j] = v[j] * G[(int64_t)k * RR + e];
+      }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int e = e0 + j * blockDim.x;
+      if (e < RR && w) v[j] = v[j] * ((double)w[e / R] * (double)w[e % R]);
+    }
+    acc += (v[0] + v[1]) + (v[2] + v[3]);
+  }
+  return acc;
+}
+
 template <typename T>
 __global__ void k_fit(const double* G, int ndim, int R, const T* w, const double* ipart, int nip,
                       AlsCtrl* ctrl, double* errors, int n_iter_max, double tol, int crit) {
   if (ctrl->done) return;
   __shared__ double scratch[32];
-  const int RR = R * R;
-  double c = 0.0;
-  for (int e = threadIdx.x; e < RR; e += blockDim.x) {
-    const int r = e / R, s = e % R;
-    double v = 1.0;
-    for (int k = 0; k < ndim; ++k) v = v * G[(int64_t)k * RR + e];
-    if (w) v = v * ((double)w[r] * (double)w[s]);
-    c += v;
-  }
-  c = block_sum(c, scratch);
+  double c = block_sum(sum_gram_product<T>(G, ndim, R, w), scratch);
   double ip = 0.0;
   for (int i = threadIdx.x; i < nip; i += blockDim.x) ip += ipart[i];
   ip = block_sum(ip, scratch);
@@ -483,7 +766,7 @@ __global__ void k_normalize(FactorPtrs<T> fp, int ndim, int R, T* weights, const
 
 // ====================================================================== launchers
 int solve_blocks_for(int64_t I) {
-  const int64_t want = ceil_div(I, kSolveWarps);
+  const int64_t want = ceil_div(I, 4);  // about four rows per CTA
   return (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sm_count() * 2));
 }
 
@@ -523,53 +806,62 @@ int als_launch_gram(const T* A, int64_t I, int R, double* gpart, int nparts_max,
 int als_launch_gram_reduce(const double* gpart, int nparts, int R, double* G, const int* done,
                            cudaStream_t st) {
   const int RR = R * R;
-  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(RR, 128), sm_count()));
-  k_gram_reduce<<<blocks, 128, 0, st>>>(gpart, nparts, RR, G, done);
+  k_gram_reduce<<<(int)ceil_div(RR, 32), 256, 0, st>>>(gpart, nparts, RR, G, done);
   TLGB_LAUNCH_CHECK();
   return TLGB_OK;
+}
+
+template <typename T, int TI, int TJ, int NI, int NJ>
+static void launch_fast(const double* G, int ndim, int mode, int R, const T* w, double l2,
+                        double* vmat, float* w32, AlsCtrl* ctrl, cudaStream_t st) {
+  k_factorize_fast<T, TI, TJ, NI, NJ><<<1, TI * TJ, 0, st>>>(G, ndim, mode, R, w, l2, vmat, w32,
+                                                             ctrl);
 }
 
 template <typename T>
 int als_launch_factorize(const double* G, int ndim, int mode, int R, const T* weights,
-                         double l2_reg, double* fac, int* perm, AlsCtrl* ctrl, cudaStream_t st) {
-  const size_t smem = (size_t)R * R * sizeof(double);
-  static bool attr[64] = {};
-  const int dev = current_device();
-  if (dev < 64 && !attr[dev]) {
-    TLGB_CUDA_TRY(cudaFuncSetAttribute(k_factorize<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)((size_t)kMaxAlsRank * kMaxAlsRank * sizeof(double))));
-    attr[dev] = true;
-  }
-  k_factorize<T><<<1, 256, smem, st>>>(G, ndim, mode, R, weights, l2_reg, fac, perm, ctrl);
+                         double l2_reg, double* fac, int* perm, double* vmat, float* w32,
+                         AlsCtrl* ctrl, cudaStream_t st) {
+  int rc = als_prepare(TypeCode<T>::value);
+  if (rc) return rc;
+  if (R <= 32)
+    launch_fast<T, 8, 16, 4, 2>(G, ndim, mode, R, weights, l2_reg, vmat, w32, ctrl, st);
+  else if (R <= 64)
+    launch_fast<T, 8, 16, 8, 4>(G, ndim, mode, R, weights, l2_reg, vmat, w32, ctrl, st);
+  else if (R <= 96)
+    launch_fast<T, 8, 16, 12, 6>(G, ndim, mode, R, weights, l2_reg, vmat, w32, ctrl, st);
+  else
+    launch_fast<T, 16, 16, 10, 10>(G, ndim, mode, R, weights, l2_reg, vmat, w32, ctrl, st);
+  TLGB_LAUNCH_CHECK();
+  k_factorize<T><<<1, 256, (size_t)R * R * sizeof(double), st>>>(G, ndim, mode, R, weights,
+                                                                 l2_reg, fac, perm, ctrl);
   TLGB_LAUNCH_CHECK();
   return TLGB_OK;
 }
 
+// Dynamic shared memory of k_solve for rank R (largest of its two paths).
+static size_t solve_smem(int R) {
+  const size_t RR = (size_t)R * R;
+  const bool mats = R <= 96;
+  const size_t rb = (size_t)std::max(1, kSolveThreads / R) * R;
+  const size_t ir = RR + 4 * rb + (mats ? RR + (RR + 1) / 2 : 0);
+  const size_t direct = RR + (size_t)kSolveWarps * R + (mats ? RR + R : 0);
+  return std::max(ir, direct) * sizeof(double);
+}
+
 template <typename T>
 int als_launch_solve(const T* partial, int splits, int64_t I, int R, const double* fac,
-                     const int* perm, T* A, __nv_bfloat16* A_bt, double* gpart, double* ipart,
-                     AlsCtrl* ctrl, int* nblocks, cudaStream_t st) {
+                     const int* perm, const double* vmat, const float* w32, T* A,
+                     __nv_bfloat16* A_bt, double* gpart, double* ipart, AlsCtrl* ctrl,
+                     int max_passes, int* nblocks, cudaStream_t st) {
   const int nb = solve_blocks_for(I);
   const int64_t rpb = ceil_div(I, nb);
   const int nbe = (int)ceil_div(I, rpb);
-  const int fac_in_smem = R <= 96 ? 1 : 0;
-  const size_t smem = ((size_t)R * R + (size_t)kSolveWarps * R +
-                       (fac_in_smem ? (size_t)R * R + R : 0)) * sizeof(double);
-  static bool attr[64] = {};
-  const int dev = current_device();
-  if (dev < 64 && !attr[dev]) {
-    // the larger of the two layouts: R <= 96 with the factor in shared memory,
-    // or R up to kMaxAlsRank without it
-    const size_t with_fac = ((size_t)2 * 96 * 96 + (size_t)kSolveWarps * 96 + 96) * sizeof(double);
-    const size_t without = ((size_t)kMaxAlsRank * kMaxAlsRank + (size_t)kSolveWarps * kMaxAlsRank) *
-                           sizeof(double);
-    const size_t maxs = with_fac > without ? with_fac : without;
-    TLGB_CUDA_TRY(cudaFuncSetAttribute(k_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)maxs));
-    attr[dev] = true;
-  }
-  k_solve<T><<<nbe, 32 * kSolveWarps, smem, st>>>(partial, splits, I, R, fac, perm, A, A_bt,
-                                                  gpart, ipart, ctrl, rpb, fac_in_smem);
+  int rc = als_prepare(TypeCode<T>::value);
+  if (rc) return rc;
+  k_solve<T><<<nbe, kSolveThreads, solve_smem(R), st>>>(partial, splits, I, R, fac, perm, vmat,
+                                                        w32, A, A_bt, gpart, ipart, ctrl, rpb,
+                                                        R <= 96 ? 1 : 0, max_passes);
   TLGB_LAUNCH_CHECK();
   *nblocks = nbe;
   return TLGB_OK;
@@ -636,11 +928,10 @@ static int als_prepare_typed() {
   TLGB_CUDA_TRY(cudaFuncSetAttribute(
       k_gram_partial<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
       (int)(((size_t)kMaxAlsRank * kMaxAlsRank + kGramRows * kMaxAlsRank) * sizeof(double))));
-  const size_t with_fac = ((size_t)2 * 96 * 96 + (size_t)kSolveWarps * 96 + 96) * sizeof(double);
-  const size_t without =
-      ((size_t)kMaxAlsRank * kMaxAlsRank + (size_t)kSolveWarps * kMaxAlsRank) * sizeof(double);
+  size_t smax = 0;
+  for (int r = 1; r <= kMaxAlsRank; ++r) smax = std::max(smax, solve_smem(r));
   TLGB_CUDA_TRY(cudaFuncSetAttribute(k_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)(with_fac > without ? with_fac : without)));
+                                     (int)smax));
   if (dev >= 0 && dev < 64) done[dev] = true;
   return TLGB_OK;
 }
@@ -653,10 +944,11 @@ int als_prepare(int dtype) {
   template int als_launch_gram<T>(const T*, int64_t, int, double*, int, double*, const int*,  \
                                   cudaStream_t);                                             \
   template int als_launch_factorize<T>(const double*, int, int, int, const T*, double,       \
-                                       double*, int*, AlsCtrl*, cudaStream_t);               \
+                                       double*, int*, double*, float*, AlsCtrl*,             \
+                                       cudaStream_t);                                        \
   template int als_launch_solve<T>(const T*, int, int64_t, int, const double*, const int*,   \
-                                   T*, __nv_bfloat16*, double*, double*, AlsCtrl*, int*,     \
-                                   cudaStream_t);                                            \
+                                   const double*, const float*, T*, __nv_bfloat16*, double*, \
+                                   double*, AlsCtrl*, int, int*, cudaStream_t);              \
   template int als_launch_fit<T>(const double*, int, int, const T*, const double*, int,      \
                                  AlsCtrl*, double*, int, double, int, cudaStream_t);         \
   template int als_launch_normalize<T>(T* const*, const int64_t*, int, int, T*, const int*,  \

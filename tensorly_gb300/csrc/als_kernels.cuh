@@ -11,10 +11,12 @@ struct AlsCtrl {
   int status;    // TLGB_OK or TLGB_ESINGULAR
   int fac_kind;  // 0: Cholesky factor, 1: LU factors with row permutation
   double norm_x2;
+  int tc_err;    // TLGB_ETIMEOUT if a tensor-core pipeline wait expired
+  int pad;
 };
 
 constexpr int kMaxAlsRank = 160;     // f64 factorisation held in one CTA's shared memory
-constexpr int kSolveWarps = 4;       // rows solved per CTA (one warp each)
+constexpr int kSolveWarps = 8;       // warps per solve CTA
 
 int als_launch_sumsq(int dtype, const void* X, int64_t n, double* part, int nblocks,
                      AlsCtrl* ctrl, cudaStream_t st);
@@ -23,17 +25,25 @@ template <typename T>
 int als_launch_gram(const T* A, int64_t I, int R, double* gpart, int nparts_max, double* G,
                     const int* done, cudaStream_t st);
 
+// vmat (R*R f64) and w32 (R*R f32) receive V and its f32 inverse for the
+// refinement path; fac/perm the f64 Cholesky or LU fallback.
 template <typename T>
 int als_launch_factorize(const double* G, int ndim, int mode, int R, const T* weights,
-                         double l2_reg, double* fac, int* perm, AlsCtrl* ctrl, cudaStream_t st);
+                         double l2_reg, double* fac, int* perm, double* vmat, float* w32,
+                         AlsCtrl* ctrl, cudaStream_t st);
 
 // Sums the MTTKRP partials of each row, solves with the factorisation, stores
 // the factor (and optionally its bf16 transpose), and writes per-CTA Gram and
 // <M, A> partial sums.  Returns the number of CTAs used via *nblocks.
 template <typename T>
+// max_passes: refinement passes allowed on the f32-inverse path (each pass
+// stops early once the correction is below 1e-12 of the solution).
 int als_launch_solve(const T* partial, int splits, int64_t I, int R, const double* fac,
-                     const int* perm, T* A, __nv_bfloat16* A_bf16_t, double* gpart,
-                     double* ipart, AlsCtrl* ctrl, int* nblocks, cudaStream_t st);
+                     const int* perm, const double* vmat, const float* w32, T* A,
+                     __nv_bfloat16* A_bf16_t, double* gpart, double* ipart, AlsCtrl* ctrl,
+                     int max_passes, int* nblocks, cudaStream_t st);
+
+constexpr int kIrMaxPasses = 4;
 
 int als_launch_gram_reduce(const double* gpart, int nparts, int R, double* G, const int* done,
                            cudaStream_t st);

@@ -24,12 +24,14 @@ struct AlsBuffers {
   double* G;
   double* fac;
   int* perm;
+  double* vmat;                         // V of the current mode (f64)
+  float* w32;                           // f32 inverse of V (refinement path)
   void* partial;
   double* gpart;
   double* ipart;
   double* sumsq_part;
   __nv_bfloat16* xbf;                   // bf16 copy of X (mixed precision)
-  __nv_bfloat16* fbt[kMaxModes];        // bf16 transposed factors (rank x rows)
+  __nv_bfloat16* fbt[kMaxModes];        // bf16 split transposed factors (2 x rank x rows)
   void* tc_partial;
   double* probe;                        // one f64 result slot (initial error)
   size_t bytes;
@@ -47,6 +49,8 @@ int layout(int dtype, const Shape& sh, int64_t R, const tlgb_cp_als_options& o,
   B->G = c.take<double>((size_t)sh.ndim * RR);
   B->fac = c.take<double>((size_t)RR + R);
   B->perm = c.take<int>(R);
+  B->vmat = c.take<double>((size_t)RR);
+  B->w32 = c.take<float>((size_t)RR);
   size_t pmax = 0;
   int64_t imax = 0;
   for (int k = 0; k < sh.ndim; ++k) {
@@ -64,9 +68,11 @@ int layout(int dtype, const Shape& sh, int64_t R, const tlgb_cp_als_options& o,
   B->tc_partial = nullptr;
   if (o.precision == TLGB_PREC_BF16) {
     B->xbf = c.take<__nv_bfloat16>((size_t)sh.numel);
-    for (int k = 0; k < sh.ndim; ++k) B->fbt[k] = c.take<__nv_bfloat16>((size_t)R * sh.dim[k]);
+    for (int k = 0; k < sh.ndim; ++k)
+      B->fbt[k] = c.take<__nv_bfloat16>((size_t)2 * R * sh.dim[k]);  // hi and lo planes
     size_t tmax = 0;
-    for (int k = 0; k < sh.ndim; ++k) tmax = std::max(tmax, tcplans[k].partial_bytes);
+    for (int k = 0; k < sh.ndim; ++k)
+      if (tcplans[k].valid) tmax = std::max(tmax, tcplans[k].partial_bytes);
     B->tc_partial = c.take<char>(tmax);
   }
   (void)esz;
@@ -125,6 +131,11 @@ struct Runner {
   AlsBuffers B;
   std::vector<int> modes;
   int last_nb = 1;
+  // The factorisation of mode n's normal equations needs only the Grams, so
+  // it runs on `aux` concurrently with mode n's MTTKRP (fork/join by events,
+  // captured into the graph as parallel branches).
+  cudaStream_t aux = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 
   // Enqueues one sweep; `tc` selects the bf16 tensor-core MTTKRP.
   int sweep(bool tc, cudaStream_t st) {
@@ -140,15 +151,19 @@ struct Runner {
     for (size_t mi = 0; mi < modes.size(); ++mi) {
       const int mode = modes[mi];
       const bool last = (mi + 1 == modes.size());
+      TLGB_CUDA_TRY(cudaEventRecord(ev_fork, st));
+      TLGB_CUDA_TRY(cudaStreamWaitEvent(aux, ev_fork, 0));
       int rc = als_launch_factorize<T>(B.G, N, mode, (int)R, weights, o.l2_reg, B.fac, B.perm,
-                                       B.ctrl, st);
+                                       B.vmat, B.w32, B.ctrl, aux);
       if (rc) return rc;
+      TLGB_CUDA_TRY(cudaEventRecord(ev_join, aux));
       int splits;
       const void* partial;
-      if (tc) {
+      if (tc && P->tc[mode].valid) {
         if constexpr (sizeof(T) == 4) {
           rc = mttkrp_tc_launch(P->tc[mode], B.xbf, (const float* const*)cf, B.fbt,
-                                (const float*)mw, (float*)B.tc_partial, done, st);
+                                (const float*)mw, (float*)B.tc_partial, done, &B.ctrl->tc_err,
+                                st);
         }
         if (rc) return rc;
         splits = P->tc[mode].splits;
@@ -159,10 +174,14 @@ struct Runner {
         splits = P->simt[mode].splits;
         partial = B.partial;
       }
+      TLGB_CUDA_TRY(cudaStreamWaitEvent(st, ev_join, 0));
       int nb = 0;
       rc = als_launch_solve<T>((const T*)partial, splits, sh.dim[mode], (int)R, B.fac, B.perm,
-                               factors[mode], B.fbt[mode], B.gpart, last ? B.ipart : nullptr,
-                               B.ctrl, &nb, st);
+                               B.vmat, B.w32, factors[mode], B.fbt[mode], B.gpart,
+                               last ? B.ipart : nullptr, B.ctrl,
+                               // the bf16 MTTKRP is accurate to ~1e-6, so one refinement
+                               // pass (solve error ~(cond * 6e-8)^2) is enough there
+                               (tc && P->tc[mode].valid) ? 1 : kIrMaxPasses, &nb, st);
       if (rc) return rc;
       if (last) last_nb = nb;
       rc = als_launch_gram_reduce(B.gpart, nb, (int)R, B.G + (size_t)mode * RR, done, st);
@@ -231,6 +250,11 @@ class StreamGuard {
   cudaStream_t s = nullptr;
   ~StreamGuard() { if (s) cudaStreamDestroy(s); }
 };
+class EventGuard {
+ public:
+  cudaEvent_t e = nullptr;
+  ~EventGuard() { if (e) cudaEventDestroy(e); }
+};
 class GraphGuard {
  public:
   cudaGraph_t g = nullptr;
@@ -266,6 +290,15 @@ int run(const T* X, const Shape& sh, int64_t R, T* const* factors, T* weights,
     rc = mttkrp_tc_prepare();
     if (rc) return rc;
   }
+
+  StreamGuard aux;
+  EventGuard ev_fork, ev_join;
+  TLGB_CUDA_TRY(cudaStreamCreateWithFlags(&aux.s, cudaStreamNonBlocking));
+  TLGB_CUDA_TRY(cudaEventCreateWithFlags(&ev_fork.e, cudaEventDisableTiming));
+  TLGB_CUDA_TRY(cudaEventCreateWithFlags(&ev_join.e, cudaEventDisableTiming));
+  run.aux = aux.s;
+  run.ev_fork = ev_fork.e;
+  run.ev_join = ev_join.e;
 
   // ---- set-up: control block, ||X||^2, Grams, bf16 operands
   TLGB_CUDA_TRY(cudaMemsetAsync(run.B.ctrl, 0, sizeof(AlsCtrl), st));
@@ -344,6 +377,8 @@ int run(const T* X, const Shape& sh, int64_t R, T* const* factors, T* weights,
         TLGB_CUDA_TRY(cudaStreamSynchronize(st));
         if (hc.status != TLGB_OK)
           return set_error(hc.status, "cp_als: singular normal equations (LU found a zero pivot)");
+        if (hc.tc_err != 0)
+          return set_error(TLGB_ETIMEOUT, "cp_als: tensor-core MTTKRP pipeline wait timed out");
         if (o.callback) {
           while (reported < hc.iter) {
             double e = 0.0;

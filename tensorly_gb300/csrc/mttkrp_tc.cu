@@ -1,42 +1,734 @@
-// BF16 tensor-core MTTKRP (tcgen05 + TMA, sm_103a).
+// BF16 tensor-core MTTKRP for sm_103a: TMA-staged tcgen05 GEMM of the tensor
+// against the inner factor, accumulated in TMEM, and an epilogue that scales
+// each outer slice's 128 x R tile by the Khatri-Rao row of the remaining
+// factors and sums it in registers.  The Khatri-Rao product is never formed.
+//
+// Formulation (same as the SIMT path, mttkrp_simt.cuh):
+//   M(i, r) = sum_o s(o, r) * sum_c X[o, i, c] * F(c, r)
+//   c = inner mode (N-1, or N-2 when the output mode is N-1), F its factor,
+//   s(o, r) = w_r * prod_{outer k} A_k(i_k, r)  (f32, from the f32 factors).
+//
+// One CTA owns one 128-row output tile and a contiguous range of the
+// flattened (o, 64-wide c chunk) steps of that tile.  Warp roles:
+//   warp 0      TMA producer: the inner factor (bf16 hi/lo split, K-major)
+//               once, then one 128 x 64 tensor tile per step into a ring of
+//               3-6 stages (as many as shared memory leaves room for)
+//   warp 1      TMEM allocation and the single-thread tcgen05.mma issue
+//               (M = 128, N = 2 x padded rank, K = 16, four per step) into one
+//               of two TMEM accumulators (double buffered across outer slices)
+//   warps 2-5   epilogue: tcgen05.ld of the finished slice, scale by s(o, :),
+//               accumulate one output row per thread in registers; finally
+//               write the CTA's partial tile (summed in a fixed order later)
+// Every mbarrier wait is bounded (about 2 s of wall time): on expiry the
+// kernel records TLGB_ETIMEOUT in *err, stops waiting, frees its TMEM and
+// returns, so a broken pipeline can never hang the GPU.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <mutex>
+
 #include "mttkrp_tc.cuh"
 
 namespace tlgb {
 namespace {
+
+constexpr int kMaxStages = 12;
+constexpr int kMinStages = 3;
+constexpr int kTileM = 128;
+constexpr int kChunk = 64;                       // bf16 elements per 128-byte swizzle row
+constexpr int kStageBytes = kTileM * kChunk * 2;  // 16 KiB
+constexpr int kSmemBudget = 225 * 1024;          // dynamic shared memory used at most
+constexpr int kThreads = 192;
+constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s
+
+struct TcArgs {
+  int stages;                 // depth of the tensor-tile ring
+  const float* outer_f[kMaxModes];
+  int64_t outer_dim[kMaxModes];
+  int n_outer;
+  int64_t g2;                 // size of TMA dim 2 (faster outer run)
+  const float* weights;
+  int R;
+  int64_t I_out;
+  int kc_total;               // 64-wide chunks of the inner mode
+  int kcg;                    // chunks per inner-mode group (blockIdx.y selects the group)
+  int64_t O;                  // outer slices
+  int64_t steps_per_split;    // (o, chunk) steps per CTA within a group
+  int gsplits;                // CTAs per (output tile, group)
+  float* partial;
+  int* err;
+  const int* skip;
+};
+
+// ------------------------------------------------------------ PTX helpers
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ unsigned long long now_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t addr, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(addr), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait; returns false (and records the timeout) if it gave up.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, bool& failed) {
+  if (failed) return false;
+  const uint32_t addr = smem_u32(bar);
+  if (mbar_try_wait(addr, parity)) return true;
+  const unsigned long long t0 = now_ns();
+  while (true) {
+    if (mbar_try_wait(addr, parity)) return true;
+    if (now_ns() - t0 > kWaitNs) {
+      atomicExch(err, TLGB_ETIMEOUT);
+      failed = true;
+      return false;
+    }
+  }
+}
+// Bounded wait used only to drain asynchronous work before the CTA exits.
+__device__ __forceinline__ void mbar_drain(uint64_t* bar, uint32_t parity) {
+  const uint32_t addr = smem_u32(bar);
+  const unsigned long long t0 = now_ns();
+  while (!mbar_try_wait(addr, parity))
+    if (now_ns() - t0 > kWaitNs) return;
+}
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar,
+                                            int c0, int c1, int c2) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, uint64_t* bar,
+                                            int c0, int c1, int c2, int c3) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3),
+      "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc,
+                                          uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate));
+}
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+      "%11, %12, %13, %14, %15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_ld32_nowait(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+      "%11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, "
+      "%28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+        "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+        "=r"(r[31])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// tcgen05 shared-memory descriptor, 128-byte swizzle (layout type 2),
+// version 1, base offset 0 (operand tiles are 1024-byte aligned).
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+
+// Instruction descriptor, kind::f16: f32 accumulate, bf16 A and B, B K-major,
+// A K-major (a_mn = 0) or MN-major (a_mn = 1), M = 128, N = n (<= 256).
+__host__ __device__ constexpr uint32_t make_idesc(int n, int a_mn) {
+  return (1u << 4)                      // D format f32
+         | (1u << 7)                    // A bf16
+         | (1u << 10)                   // B bf16
+         | ((uint32_t)a_mn << 15)       // A major
+         | (0u << 16)                   // B K-major
+         | ((uint32_t)(n >> 3) << 17)   // N / 8
+         | ((uint32_t)(kTileM >> 4) << 24);  // M / 16
+}
+
+// B operand = [F_hi ; F_lo]: the inner factor split into two bf16 terms
+// (F_lo = bf16(F - F_hi)), stacked as 2*RP rows, so one MMA with N = 2*RP
+// forms X.F_hi and X.F_lo side by side in TMEM and the epilogue adds them.
+// The factor then enters the contraction with ~16 mantissa bits: with a
+// single bf16 rounding of the factor, ALS stalls at a worse stationary point
+// in swamp phases (rounding only the tensor to bf16 does not).
+template <int RP, bool MN>
+__global__ void __launch_bounds__(kThreads, 1)
+mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmF,
+                 const TcArgs a) {
+  if (a.skip && *a.skip) return;
+  constexpr int NB = 2 * RP;               // MMA N (hi and lo halves)
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* base = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  const int S = a.stages;
+  unsigned char* sA = base;                                   // S x 16 KiB
+  unsigned char* sB = sA + S * kStageBytes;                   // KC x NB x 128 B
+  const int split = blockIdx.x;
+  const int cg = blockIdx.y;                                  // inner-mode group
+  const int64_t m0 = (int64_t)blockIdx.z * kTileM;
+  const int kc0 = cg * a.kcg;
+  const int KC = min(a.kcg, a.kc_total - kc0);                // chunks of this group
+  const int b_bytes = KC * NB * 128;
+  uint64_t* full = reinterpret_cast<uint64_t*>(sB + b_bytes); // [S]
+  uint64_t* empty = full + kMaxStages;                        // [S]
+  uint64_t* dfull = empty + kMaxStages;   // [2]
+  uint64_t* dempty = dfull + 2;           // [2]
+  uint64_t* bfull = dempty + 2;           // [1]
+  uint64_t* mdrain = bfull + 1;           // [1] MMA completion before teardown
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mdrain + 1);
+  int* ep_ok = reinterpret_cast<int*>(tmem_slot + 1);         // [2] epilogue wait outcome
+  float* s_sm = reinterpret_cast<float*>(tmem_slot + 4);      // [2][RP]
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t t_begin = (int64_t)split * a.steps_per_split;
+  const int64_t t_end = min(t_begin + a.steps_per_split, a.O * KC);
+  // partial tile index: every (group, split) CTA of an output tile writes its own
+  const int64_t pidx = (int64_t)cg * a.gsplits + split;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < S; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&dfull[b], 1);
+      mbar_init(&dempty[b], 128);
+    }
+    mbar_init(bfull, 1);
+    mbar_init(mdrain, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(2 * NB)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  bool failed = false;
+
+  if (t_begin < t_end) {
+    if (warp == 0) {
+      // ------------------------------------------------------------ producer
+      if (lane == 0) {
+        mbar_expect_tx(bfull, (uint32_t)b_bytes);
+        for (int kc = 0; kc < KC; ++kc) {
+          unsigned char* dst = sB + kc * NB * 128;
+          tma_load_3d(dst, &tmF, bfull, (kc0 + kc) * kChunk, 0, 0);             // F_hi rows
+          tma_load_3d(dst + RP * 128, &tmF, bfull, (kc0 + kc) * kChunk, 0, 1);  // F_lo rows
+        }
+        // Coordinates advance incrementally (no 64-bit division per step:
+        // this single thread's issue rate bounds the whole CTA's bandwidth).
+        const int64_t o0 = t_begin / KC;
+        int kc = (int)(t_begin - o0 * KC);
+        int c2 = (int)(o0 % a.g2), c3 = (int)(o0 / a.g2);
+        int stage = 0;
+        uint32_t phase = 0;
+        int64_t i = 0;
+        for (int64_t t = t_begin; t < t_end; ++t, ++i) {
+          if (!mbar_wait(&empty[stage], phase ^ 1u, a.err, failed)) break;
+          mbar_expect_tx(&full[stage], kStageBytes);
+          unsigned char* dst = sA + stage * kStageBytes;
+          const int cx = (kc0 + kc) * kChunk;
+          if (!MN) {
+            tma_load_4d(dst, &tmX, &full[stage], cx, (int)m0, c2, c3);
+          } else {
+            tma_load_4d(dst, &tmX, &full[stage], (int)m0, cx, c2, c3);
+            tma_load_4d(dst + kStageBytes / 2, &tmX, &full[stage], (int)m0 + 64, cx, c2, c3);
+          }
+          if (++kc == KC) {
+            kc = 0;
+            if (++c2 == a.g2) { c2 = 0; ++c3; }
+          }
+          if (++stage == S) { stage = 0; phase ^= 1u; }
+        }
+        // every issued copy has landed before the CTA may exit
+        mbar_drain(bfull, 0);
+        {
+          const int n = (int)(i < S ? i : S);
+          int st_j = stage, ph_j = (int)phase;   // walk back over the last n issued steps
+          for (int j = 0; j < n; ++j) {
+            if (--st_j < 0) { st_j = S - 1; ph_j ^= 1; }
+            mbar_drain(&full[st_j], (uint32_t)ph_j);
+          }
+        }
+      }
+    } else if (warp == 1) {
+      // ------------------------------------------------------------ MMA issue
+      if (lane == 0) {
+        constexpr uint32_t idesc = make_idesc(NB, MN ? 1 : 0);
+        mbar_wait(bfull, 0, a.err, failed);
+        int64_t oc = 0;
+        int kc = (int)(t_begin % KC);
+        int stage = 0;
+        uint32_t phase = 0;
+        for (int64_t t = t_begin; t < t_end && !failed; ++t) {
+          const bool first_of_o = (t == t_begin) || (kc == 0);
+          const bool last_of_o = (t + 1 == t_end) || (kc == KC - 1);
+          const int buf = (int)(oc & 1);
+          if (first_of_o) {
+            if (!mbar_wait(&dempty[buf], (uint32_t)(((oc >> 1) & 1) ^ 1), a.err, failed)) break;
+            tc_fence_after();
+          }
+          if (!mbar_wait(&full[stage], phase, a.err, failed)) break;
+          tc_fence_after();
+          const uint32_t a_base = smem_u32(sA + stage * kStageBytes);
+          const uint32_t b_base = smem_u32(sB + kc * NB * 128);
+          const uint32_t d = tmem + (uint32_t)(buf * NB);
+#pragma unroll
+          for (int k = 0; k < kChunk / 16; ++k) {
+            const uint64_t adesc = MN ? smem_desc(a_base + k * 2048, kStageBytes / 2, 1024)
+                                      : smem_desc(a_base + k * 32, 16, 1024);
+            const uint64_t bdesc = smem_desc(b_base + k * 32, 16, 1024);
+            umma_bf16(d, adesc, bdesc, idesc, (first_of_o && k == 0) ? 0u : 1u);
+          }
+          umma_commit(&empty[stage]);
+          if (last_of_o) {
+            umma_commit(&dfull[buf]);
+            ++oc;
+          }
+          if (++kc == KC) kc = 0;
+          if (++stage == S) { stage = 0; phase ^= 1u; }
+        }
+        // all issued MMAs have completed before TMEM is freed
+        umma_commit(mdrain);
+        mbar_drain(mdrain, 0);
+      }
+    } else {
+      // ------------------------------------------------------------ epilogue
+      const int e = threadIdx.x - 64;            // 0..127
+      const int q = warp & 3;                    // TMEM lane quarter of this warp
+      const int row = 32 * q + lane;
+      float acc[RP];
+#pragma unroll
+      for (int r = 0; r < RP; ++r) acc[r] = 0.f;
+      const int64_t o_first = t_begin / KC, o_last = (t_end - 1) / KC;
+      // s(o, r) = w_r * prod_{outer k} A_k(i_k, r) for r = e (one entry per thread)
+      // outer multi-index of the next slice, advanced with carries (no division)
+      int64_t nidx[kMaxModes];
+      {
+        int64_t rem = o_first;
+        for (int k = a.n_outer - 1; k >= 0; --k) {
+          nidx[k] = rem % a.outer_dim[k];
+          rem /= a.outer_dim[k];
+        }
+      }
+      auto scale_of = [&](int64_t) -> float {
+        float s = 0.f;
+        if (e < a.R) {
+          s = a.weights ? a.weights[e] : 1.f;
+          for (int k = 0; k < a.n_outer; ++k) s *= a.outer_f[k][nidx[k] * a.R + e];
+        }
+        for (int k = a.n_outer - 1; k >= 0; --k) {
+          if (++nidx[k] < a.outer_dim[k]) break;
+          nidx[k] = 0;
+        }
+        return s;
+      };
+      float s_next = (e < RP) ? scale_of(o_first) : 0.f;
+      int64_t oc = 0;
+      for (int64_t o = o_first; o <= o_last; ++o, ++oc) {
+        const int buf = (int)(oc & 1);
+        if (e < RP) s_sm[buf * RP + e] = s_next;
+        // the next slice's scale loads overlap this slice's TMEM traffic
+        if (e < RP && o < o_last) s_next = scale_of(o + 1);
+        if (e == 0) ep_ok[buf] = mbar_wait(&dfull[buf], (uint32_t)((oc >> 1) & 1), a.err, failed) ? 1 : 0;
+        asm volatile("bar.sync 1, 128;" ::: "memory");
+        if (!ep_ok[buf]) break;  // uniform across the four epilogue warps
+        __syncwarp();            // tcgen05.ld is warp-collective
+        tc_fence_after();
+        const uint32_t lane_addr = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(buf * NB);
+        if constexpr (RP >= 32) {
+#pragma unroll
+          for (int c = 0; c < RP / 32; ++c) {
+            uint32_t hi[32], lo[32];
+            tmem_ld32_nowait(lane_addr + (uint32_t)(c * 32), hi);
+            tmem_ld32_nowait(lane_addr + (uint32_t)(RP + c * 32), lo);
+            tmem_wait_ld();
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+              acc[c * 32 + j] = fmaf(s_sm[buf * RP + c * 32 + j],
+                                     __uint_as_float(hi[j]) + __uint_as_float(lo[j]),
+                                     acc[c * 32 + j]);
+          }
+        } else {
+          float hi[16], lo[16];
+          tmem_ld16(lane_addr, hi);
+          tmem_ld16(lane_addr + (uint32_t)RP, lo);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) acc[j] = fmaf(s_sm[buf * RP + j], hi[j] + lo[j], acc[j]);
+        }
+        tc_fence_before();
+        mbar_arrive(&dempty[buf]);
+      }
+      const int64_t m = m0 + row;
+      if (m < a.I_out) {
+        float* out = a.partial + (pidx * a.I_out + m) * a.R;
+#pragma unroll
+        for (int r = 0; r < RP; ++r)
+          if (r < a.R) out[r] = acc[r];
+      }
+    }
+  } else if (warp >= 2) {
+    // empty range: this split contributes zeros
+    const int q = warp & 3;
+    const int64_t m = m0 + 32 * q + lane;
+    if (m < a.I_out)
+      for (int r = 0; r < a.R; ++r) a.partial[(pidx * a.I_out + m) * a.R + r] = 0.f;
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    __syncwarp();
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * NB)
+                 : "memory");
+  }
+}
 
 __global__ void k_to_bf16(const float* __restrict__ X, int64_t n, __nv_bfloat16* __restrict__ Y) {
   const int64_t n4 = n / 4;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n4;
        i += (int64_t)gridDim.x * blockDim.x) {
     const float4 v = reinterpret_cast<const float4*>(X)[i];
-    __nv_bfloat162 a = __floats2bfloat162_rn(v.x, v.y);
-    __nv_bfloat162 b = __floats2bfloat162_rn(v.z, v.w);
-    reinterpret_cast<__nv_bfloat162*>(Y)[2 * i] = a;
-    reinterpret_cast<__nv_bfloat162*>(Y)[2 * i + 1] = b;
+    reinterpret_cast<__nv_bfloat162*>(Y)[2 * i] = __floats2bfloat162_rn(v.x, v.y);
+    reinterpret_cast<__nv_bfloat162*>(Y)[2 * i + 1] = __floats2bfloat162_rn(v.z, v.w);
   }
   for (int64_t i = n4 * 4 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
     Y[i] = __float2bfloat16_rn(X[i]);
 }
 
+// Transposed bf16 split of a factor: out[0][r][i] = bf16(A[i][r]) (hi),
+// out[1][r][i] = bf16(A[i][r] - hi) (lo).
 __global__ void k_factor_bf16t(const float* __restrict__ A, int64_t rows, int64_t R,
                                __nv_bfloat16* __restrict__ out) {
   const int64_t n = rows * R;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
        e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = e / R, r = e % R;
-    out[r * rows + i] = __float2bfloat16_rn(A[e]);
+    const __nv_bfloat16 hi = __float2bfloat16_rn(A[e]);
+    out[r * rows + i] = hi;
+    out[n + r * rows + i] = __float2bfloat16_rn(A[e] - __bfloat162float(hi));
   }
 }
 
+__global__ void k_sum_partials(const float* __restrict__ partial, int splits, int64_t n,
+                               float* __restrict__ out) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int k = 0; k < splits; ++k) s += (double)partial[(int64_t)k * n + e];
+    out[e] = (float)s;
+  }
+}
+
+// ------------------------------------------------------------ host side
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+// barriers, TMEM slot, flags and the per-slice scale rows after the operands
+size_t tail_bytes(int n_pad) {
+  return (2 * kMaxStages + 6) * sizeof(uint64_t) + 16 + 2 * (size_t)n_pad * sizeof(float);
+}
+size_t b_bytes_for(int64_t kc, int n_pad) { return (size_t)kc * 2 * n_pad * 128; }
+size_t smem_for(const TcPlan& p) {
+  return 1024 + (size_t)p.stages * kStageBytes + b_bytes_for(p.kcg, p.n_pad) + tail_bytes(p.n_pad);
+}
+
+template <int RP, bool MN>
+int set_attr_one() {
+  TLGB_CUDA_TRY(cudaFuncSetAttribute(mttkrp_tc_kernel<RP, MN>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBudget));
+  return TLGB_OK;
+}
+
+template <bool MN>
+int set_attrs_mn() {
+  int rc = set_attr_one<16, MN>();
+  if (!rc) rc = set_attr_one<32, MN>();
+  if (!rc) rc = set_attr_one<64, MN>();
+  if (!rc) rc = set_attr_one<128, MN>();
+  return rc;
+}
+
+template <int RP, bool MN>
+int launch_tc(const TcPlan& p, const CUtensorMap& tx, const CUtensorMap& tf, const TcArgs& a,
+              cudaStream_t st) {
+  dim3 grid((unsigned)p.gsplits, (unsigned)p.n_cg, (unsigned)p.m_tiles);
+  mttkrp_tc_kernel<RP, MN><<<grid, kThreads, smem_for(p), st>>>(tx, tf, a);
+  TLGB_LAUNCH_CHECK();
+  return TLGB_OK;
+}
+
 }  // namespace
+
+int mttkrp_tc_prepare() {
+  static bool done[64] = {};
+  const int dev = current_device();
+  if (dev >= 0 && dev < 64 && done[dev]) return TLGB_OK;
+  if (!encode_fn()) return set_error(TLGB_EUNSUPPORTED, "cuTensorMapEncodeTiled unavailable");
+  int rc = set_attrs_mn<false>();
+  if (!rc) rc = set_attrs_mn<true>();
+  if (!rc && dev >= 0 && dev < 64) done[dev] = true;
+  return rc;
+}
+
+TcTuning& tc_tuning() {
+  static TcTuning t;
+  return t;
+}
+
+int mttkrp_tc_make_plan(const Shape& sh, int64_t rank, int mode, TcPlan* plan) {
+  TcPlan p{};
+  const int N = sh.ndim;
+  if (N < 2 || N > kMaxModes || mode < 0 || mode >= N)
+    return set_error(TLGB_EINVAL, "mttkrp_bf16: bad mode");
+  p.ndim = N;
+  for (int k = 0; k < N; ++k) p.dim[k] = sh.dim[k];
+  p.R = rank;
+  p.I_out = sh.dim[mode];
+  p.out_contig = (mode == N - 1) ? 1 : 0;
+  p.out_mode = mode;
+  p.inner_mode = p.out_contig ? N - 2 : N - 1;
+  p.C = sh.dim[p.inner_mode];
+  p.n_outer = 0;
+  p.O = 1;
+  for (int k = 0; k < N; ++k) {
+    if (k == mode || k == p.inner_mode) continue;
+    p.outer_mode[p.n_outer] = k;
+    p.outer_dim[p.n_outer] = sh.dim[k];
+    p.outer_stride[p.n_outer] = sh.stride[k];
+    p.n_outer++;
+    p.O *= sh.dim[k];
+  }
+  p.n_pad = rank <= 16 ? 16 : rank <= 32 ? 32 : rank <= 64 ? 64 : 128;
+  p.kc = ceil_div(p.C, kChunk);
+  p.m_tiles = (int)ceil_div(p.I_out, kTileM);
+  // Inner-mode groups: a CTA keeps only its group's slice of the split factor
+  // resident (about 64 KiB), which leaves room for a deep tensor-tile ring.
+  const int per_chunk = 2 * p.n_pad * 128;
+  const int resident = tc_tuning().group_kib > 0 ? tc_tuning().group_kib : 64;
+  const int max_g = std::max(1, (resident * 1024) / per_chunk);
+  int kcg = 1;
+  for (int g = 1; g <= std::min<int64_t>(max_g, p.kc); ++g)
+    if (p.kc % g == 0) kcg = g;
+  p.kcg = kcg;
+  p.n_cg = (int)ceil_div(p.kc, kcg);
+  p.total_steps = p.O * p.kc;
+  const size_t bbytes = b_bytes_for(p.kcg, p.n_pad);
+  const int64_t room = (int64_t)kSmemBudget - 1024 - (int64_t)bbytes - (int64_t)tail_bytes(p.n_pad);
+  p.stages = (int)std::min<int64_t>(kMaxStages, room > 0 ? room / kStageBytes : 0);
+  if (tc_tuning().stages > 0) p.stages = std::min(p.stages, tc_tuning().stages);
+  bool ok = rank <= 128 && (p.C % 8 == 0) && (p.I_out % (p.out_contig ? 8 : 1) == 0) &&
+            p.stages >= kMinStages && p.I_out < (1ll << 31) && p.C < (1ll << 31) &&
+            p.O < (1ll << 31) && p.m_tiles <= 65535 && p.n_cg <= 65535;
+  if (!ok) {
+    p.valid = 0;
+    *plan = p;
+    return TLGB_OK;
+  }
+  // one wave: (output tiles x groups x splits) CTAs <= SM count when possible
+  const int64_t pairs = (int64_t)p.m_tiles * p.n_cg;
+  const int64_t ctas = (int64_t)sm_count() * (tc_tuning().waves > 0 ? tc_tuning().waves : 1);
+  int64_t gs = std::max<int64_t>(1, ctas / pairs);
+  const int64_t gsteps = p.O * p.kcg;
+  gs = std::max<int64_t>(1, std::min<int64_t>(gs, gsteps));
+  p.steps_per_split = ceil_div(gsteps, gs);
+  p.gsplits = (int)std::min<int64_t>(65535, ceil_div(gsteps, p.steps_per_split));
+  p.splits = p.n_cg * p.gsplits;   // partial tiles per output tile
+  p.partial_bytes = (size_t)p.splits * p.I_out * p.R * sizeof(float);
+  p.valid = 1;
+  *plan = p;
+  return TLGB_OK;
+}
+
+int mttkrp_tc_launch(const TcPlan& p, const __nv_bfloat16* Xbf, const float* const* factors,
+                     __nv_bfloat16* const* fbt, const float* weights, float* partial,
+                     const int* skip_flag, int* err, cudaStream_t st) {
+  if (!p.valid) return set_error(TLGB_EUNSUPPORTED, "mttkrp_bf16: shape not supported");
+  auto enc = encode_fn();
+  if (!enc) return set_error(TLGB_EUNSUPPORTED, "cuTensorMapEncodeTiled unavailable");
+  TLGB_CHECK_ARG((reinterpret_cast<uintptr_t>(Xbf) % 16) == 0, "mttkrp_bf16: X not 16-byte aligned");
+  const __nv_bfloat16* F = fbt[p.inner_mode];
+  TLGB_CHECK_ARG((reinterpret_cast<uintptr_t>(F) % 16) == 0, "mttkrp_bf16: factor not aligned");
+  Shape sh = make_shape(p.ndim, p.dim);
+  // outer runs: consecutive outer modes merge into one TMA dimension
+  int64_t run_size[2] = {1, 1}, run_stride[2] = {0, 0};
+  int nrun = 0, prev = -2;
+  for (int j = 0; j < p.n_outer; ++j) {
+    const int k = p.outer_mode[j];
+    if (k != prev + 1 || nrun == 0) {
+      if (nrun == 2) return set_error(TLGB_EUNSUPPORTED, "mttkrp_bf16: too many outer runs");
+      run_size[nrun] = 1;
+      ++nrun;
+    }
+    run_size[nrun - 1] *= sh.dim[k];
+    run_stride[nrun - 1] = sh.stride[k];
+    prev = k;
+  }
+  // TMA dim 2 = the faster run (the later one), dim 3 = the slower run
+  int64_t g2 = 1, g3 = 1, s2 = 0, s3 = 0;
+  if (nrun == 1) { g2 = run_size[0]; s2 = run_stride[0]; }
+  if (nrun == 2) { g2 = run_size[1]; s2 = run_stride[1]; g3 = run_size[0]; s3 = run_stride[0]; }
+  cuuint64_t gdim[4];
+  cuuint64_t gstride[3];
+  cuuint32_t box[4];
+  const cuuint32_t estride[4] = {1, 1, 1, 1};
+  if (!p.out_contig) {   // dim0 = inner mode (contiguous), dim1 = output mode
+    gdim[0] = (cuuint64_t)p.C;
+    gdim[1] = (cuuint64_t)p.I_out;
+    gstride[0] = (cuuint64_t)sh.stride[p.out_mode] * 2;
+    box[0] = kChunk;
+    box[1] = kTileM;
+  } else {               // dim0 = output mode (contiguous), dim1 = inner mode
+    gdim[0] = (cuuint64_t)p.I_out;
+    gdim[1] = (cuuint64_t)p.C;
+    gstride[0] = (cuuint64_t)sh.stride[p.inner_mode] * 2;
+    box[0] = 64;
+    box[1] = kChunk;
+  }
+  gdim[2] = (cuuint64_t)g2;
+  gdim[3] = (cuuint64_t)g3;
+  gstride[1] = (cuuint64_t)(s2 ? s2 : 1) * 2;
+  gstride[2] = (cuuint64_t)(s3 ? s3 : 1) * 2;
+  // unit dimensions still need a legal (16-byte multiple) stride
+  if (g2 == 1) gstride[1] = gstride[0] * (cuuint64_t)gdim[1];
+  if (g3 == 1) gstride[2] = gstride[1] * (cuuint64_t)gdim[2];
+  box[2] = 1;
+  box[3] = 1;
+  for (int j = 0; j < 3; ++j)
+    if (gstride[j] % 16 != 0) return set_error(TLGB_EUNSUPPORTED, "mttkrp_bf16: stride not 16-byte aligned");
+  CUtensorMap tx, tf;
+  CUresult cr = enc(&tx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<__nv_bfloat16*>(Xbf), gdim,
+                    gstride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (cr != CUDA_SUCCESS) return set_error(TLGB_ECUDA, "mttkrp_bf16: tensor map for X failed");
+  // inner factor as (C, R, 2): hi and lo planes of the transposed bf16 factor
+  cuuint64_t fdim[3] = {(cuuint64_t)p.C, (cuuint64_t)p.R, 2};
+  cuuint64_t fstride[2] = {(cuuint64_t)p.C * 2, (cuuint64_t)p.C * (cuuint64_t)p.R * 2};
+  cuuint32_t fbox[3] = {(cuuint32_t)kChunk, (cuuint32_t)p.n_pad, 1};
+  cr = enc(&tf, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<__nv_bfloat16*>(F), fdim, fstride,
+           fbox, estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (cr != CUDA_SUCCESS) return set_error(TLGB_ECUDA, "mttkrp_bf16: tensor map for F failed");
+
+  TcArgs a{};
+  a.stages = p.stages;
+  for (int j = 0; j < p.n_outer; ++j) {
+    a.outer_f[j] = factors[p.outer_mode[j]];
+    a.outer_dim[j] = p.outer_dim[j];
+  }
+  a.n_outer = p.n_outer;
+  a.g2 = g2;
+  a.weights = weights;
+  a.R = (int)p.R;
+  a.I_out = p.I_out;
+  a.kc_total = (int)p.kc;
+  a.kcg = p.kcg;
+  a.O = p.O;
+  a.steps_per_split = p.steps_per_split;
+  a.gsplits = p.gsplits;
+  a.partial = partial;
+  a.err = err;
+  a.skip = skip_flag;
+  const bool mn = p.out_contig != 0;
+  switch (p.n_pad) {
+    case 16: return mn ? launch_tc<16, true>(p, tx, tf, a, st) : launch_tc<16, false>(p, tx, tf, a, st);
+    case 32: return mn ? launch_tc<32, true>(p, tx, tf, a, st) : launch_tc<32, false>(p, tx, tf, a, st);
+    case 64: return mn ? launch_tc<64, true>(p, tx, tf, a, st) : launch_tc<64, false>(p, tx, tf, a, st);
+    default: return mn ? launch_tc<128, true>(p, tx, tf, a, st) : launch_tc<128, false>(p, tx, tf, a, st);
+  }
+}
+
+int tc_launch_sum_partials(const TcPlan& p, const float* partial, float* out, cudaStream_t st) {
+  const int64_t n = p.I_out * p.R;
+  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), sm_count() * 4));
+  k_sum_partials<<<blocks, 256, 0, st>>>(partial, p.splits, n, out);
+  TLGB_LAUNCH_CHECK();
+  return TLGB_OK;
+}
 
 int tc_launch_to_bf16(const float* X, int64_t n, __nv_bfloat16* out, cudaStream_t st) {
   TLGB_CHECK_ARG((reinterpret_cast<uintptr_t>(X) % 16) == 0 &&
                      (reinterpret_cast<uintptr_t>(out) % 8) == 0,
                  "to_bf16: misaligned buffers");
-  const int blocks = sm_count() * 8;
-  k_to_bf16<<<blocks, 256, 0, st>>>(X, n, out);
+  k_to_bf16<<<sm_count() * 8, 256, 0, st>>>(X, n, out);
   TLGB_LAUNCH_CHECK();
   return TLGB_OK;
 }
@@ -50,19 +742,86 @@ int tc_launch_factor_bf16t(const float* A, int64_t rows, int64_t R, __nv_bfloat1
   return TLGB_OK;
 }
 
-int mttkrp_tc_prepare() { return set_error(TLGB_EUNSUPPORTED, "bf16 tensor-core MTTKRP not built"); }
-
-int mttkrp_tc_make_plan(const Shape& sh, int64_t rank, int mode, TcPlan* plan) {
-  (void)sh; (void)rank; (void)mode; (void)plan;
-  return set_error(TLGB_EUNSUPPORTED, "bf16 tensor-core MTTKRP not built");
-}
-
-int mttkrp_tc_launch(const TcPlan& p, const __nv_bfloat16* Xbf, const float* const* factors,
-                     __nv_bfloat16* const* fbt, const float* weights, float* partial,
-                     const int* skip_flag, cudaStream_t st) {
-  (void)p; (void)Xbf; (void)factors; (void)fbt; (void)weights; (void)partial; (void)skip_flag;
-  (void)st;
-  return set_error(TLGB_EUNSUPPORTED, "bf16 tensor-core MTTKRP not built");
-}
-
 }  // namespace tlgb
+
+// ---------------------------------------------------------------------------
+// C ABI: standalone bf16 tensor-core MTTKRP
+// ---------------------------------------------------------------------------
+using namespace tlgb;
+
+namespace {
+int tc_plan_for(int ndim, const int64_t* shape, int64_t rank, int mode, TcPlan* p) {
+  TLGB_CHECK_ARG(shape != nullptr, "mttkrp_bf16: null shape");
+  TLGB_CHECK_ARG(ndim >= 2 && ndim <= kMaxModes, "mttkrp_bf16: ndim must be in [2, 8]");
+  TLGB_CHECK_ARG(mode >= 0 && mode < ndim, "mttkrp_bf16: mode out of range");
+  TLGB_CHECK_ARG(rank >= 1, "mttkrp_bf16: rank must be >= 1");
+  for (int k = 0; k < ndim; ++k) TLGB_CHECK_ARG(shape[k] >= 1, "mttkrp_bf16: empty mode");
+  Shape sh = make_shape(ndim, shape);
+  int rc = mttkrp_tc_make_plan(sh, rank, mode, p);
+  if (rc) return rc;
+  if (!p->valid)
+    return set_error(TLGB_EUNSUPPORTED,
+                     "mttkrp_bf16: needs rank <= 128, inner mode (and a last output mode) a "
+                     "multiple of 8, and the inner factor within 96 KiB of shared memory");
+  return TLGB_OK;
+}
+}  // namespace
+
+extern "C" int tlgb_mttkrp_bf16_workspace_size(int ndim, const int64_t* shape, int64_t rank,
+                                               int mode, size_t* bytes) {
+  clear_error();
+  TLGB_CHECK_ARG(bytes != nullptr, "mttkrp_bf16_workspace_size: null pointer");
+  TcPlan p;
+  int rc = tc_plan_for(ndim, shape, rank, mode, &p);
+  if (rc) return rc;
+  *bytes = 256 + align_up(p.partial_bytes, 256);
+  return TLGB_OK;
+}
+
+extern "C" int tlgb_mttkrp_bf16(const void* X, int ndim, const int64_t* shape,
+                                const void* const* factors, const void* const* factors_bf16_t,
+                                const void* weights, int64_t rank, int mode, void* out,
+                                void* workspace, size_t workspace_bytes, void* stream) {
+  clear_error();
+  TcPlan p;
+  int rc = tc_plan_for(ndim, shape, rank, mode, &p);
+  if (rc) return rc;
+  TLGB_CHECK_ARG(X && factors && factors_bf16_t && out, "mttkrp_bf16: null pointer");
+  TLGB_CHECK_ARG(factors_bf16_t[p.inner_mode] != nullptr, "mttkrp_bf16: missing inner factor");
+  for (int j = 0; j < p.n_outer; ++j)
+    TLGB_CHECK_ARG(factors[p.outer_mode[j]] != nullptr, "mttkrp_bf16: missing factor");
+  if (!workspace || workspace_bytes < 256 + p.partial_bytes)
+    return set_error(TLGB_EWORKSPACE, "mttkrp_bf16: workspace too small");
+  rc = mttkrp_tc_prepare();
+  if (rc) return rc;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int* err = static_cast<int*>(workspace);
+  float* partial = reinterpret_cast<float*>(static_cast<char*>(workspace) + 256);
+  TLGB_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), st));
+  rc = mttkrp_tc_launch(p, static_cast<const __nv_bfloat16*>(X), (const float* const*)factors,
+                        (__nv_bfloat16* const*)factors_bf16_t, static_cast<const float*>(weights),
+                        partial, nullptr, err, st);
+  if (rc) return rc;
+  return tc_launch_sum_partials(p, partial, static_cast<float*>(out), st);
+}
+
+extern "C" int tlgb_workspace_status(const void* workspace, void* stream, int* status) {
+  clear_error();
+  TLGB_CHECK_ARG(workspace && status, "workspace_status: null pointer");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  TLGB_CUDA_TRY(cudaMemcpyAsync(status, workspace, sizeof(int), cudaMemcpyDeviceToHost, st));
+  TLGB_CUDA_TRY(cudaStreamSynchronize(st));
+  return TLGB_OK;
+}
+
+// Tuning knobs of the tensor-core MTTKRP plan (0 restores the default).
+extern "C" int tlgb_set_tuning(const char* key, int value) {
+  clear_error();
+  TLGB_CHECK_ARG(key != nullptr && value >= 0, "set_tuning: bad argument");
+  const std::string k(key);
+  if (k == "tc_group_kib") tc_tuning().group_kib = value;
+  else if (k == "tc_stages") tc_tuning().stages = value;
+  else if (k == "tc_waves") tc_tuning().waves = value;
+  else return set_error(TLGB_EINVAL, "set_tuning: unknown key " + k);
+  return TLGB_OK;
+}

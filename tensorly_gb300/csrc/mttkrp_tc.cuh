@@ -8,31 +8,51 @@ struct TcPlan {
   int valid;
   int64_t I_out, C, O, R;
   int inner_mode;
+  int out_mode;
   int n_outer;
   int outer_mode[kMaxModes];
   int64_t outer_dim[kMaxModes], outer_stride[kMaxModes];
   int out_contig;
-  int n_pad;            // rank padded to the MMA N granularity
+  int n_pad;            // rank padded to 16/32/64/128 (MMA N = 2 * n_pad)
+  int stages;           // tensor-tile ring depth that fits next to the resident factor
   int m_tiles;
   int64_t kc;           // 64-element chunks of the inner mode
   int64_t total_steps;  // O * kc per output tile
+  int kcg;              // chunks per inner-mode group (resident factor slice)
+  int n_cg;             // inner-mode groups
+  int gsplits;          // CTAs per (output tile, group)
   int64_t steps_per_split;
-  int splits;           // splits per output tile
+  int splits;           // partial tiles per output tile (= n_cg * gsplits)
   size_t partial_bytes;
   int ndim;
   int64_t dim[kMaxModes];
 };
 
+// Plan knobs set by tlgb_set_tuning (0 = default): resident factor slice per
+// CTA in KiB, ring depth cap, CTAs per SM.
+struct TcTuning {
+  int group_kib = 0;
+  int stages = 0;
+  int waves = 0;
+};
+TcTuning& tc_tuning();
+
 int mttkrp_tc_prepare();
 int mttkrp_tc_make_plan(const Shape& sh, int64_t rank, int mode, TcPlan* plan);
 
 // partial[split][I_out][R] (f32) from the bf16 tensor, the f32 factors (outer
-// scales) and the bf16 transposed factors (inner operand, rank x rows).
+// scales) and the bf16 split transposed factors (inner operand: two planes,
+// hi then lo, each rank x rows).
+// err: device int that receives TLGB_ETIMEOUT if a bounded wait expired.
 int mttkrp_tc_launch(const TcPlan& p, const __nv_bfloat16* Xbf, const float* const* factors,
                      __nv_bfloat16* const* fbt, const float* weights, float* partial,
-                     const int* skip_flag, cudaStream_t st);
+                     const int* skip_flag, int* err, cudaStream_t st);
+
+// out = sum over splits of partial (I_out x R, f32).
+int tc_launch_sum_partials(const TcPlan& p, const float* partial, float* out, cudaStream_t st);
 
 int tc_launch_to_bf16(const float* X, int64_t n, __nv_bfloat16* out, cudaStream_t st);
+// out (2 x R x rows bf16): hi = bf16(A^T), lo = bf16(A^T - hi).
 int tc_launch_factor_bf16t(const float* A, int64_t rows, int64_t R, __nv_bfloat16* out,
                            cudaStream_t st);
 

@@ -171,3 +171,26 @@ def test_parafac_deterministic(gb300):
     assert ea == eb
     for u, v in zip(a.factors, b.factors):
         assert torch.equal(u, v)
+
+
+def test_ill_conditioned_normal_equations_use_f64_fallback(gb300):
+    """Nearly collinear initial components make V ill-conditioned (pivot
+    spread > 1e5): the library factorises in f64 (Cholesky, LU if needed)
+    instead of refining from an f32 inverse; the first sweeps still match the
+    NumPy reference (LAPACK gesv) to the accuracy the conditioning allows."""
+    rs = np.random.RandomState(11)
+    shape, rank = (20, 18, 16), 4
+    fs = [rs.uniform(size=(s, rank)) for s in shape]
+    x = oracle.cp_to_tensor((None, fs)) + 0.01 * rs.randn(*shape)
+    init = [rs.uniform(size=(s, rank)) for s in shape]
+    for f in init:
+        f[:, 1] = f[:, 0] * (1 + 1e-4 * rs.randn(f.shape[0]))
+    (ow, of), oe = oracle.parafac(x, rank, init=(None, [f.copy() for f in init]), n_iter_max=3,
+                                  tol=0, return_errors=True)
+    xt = torch.as_tensor(x, device="cuda")
+    cp, errs = gb300.parafac(xt, rank, init=gb300.CPTensor((None, [torch.as_tensor(f, device="cuda")
+                                                                  for f in init])),
+                             n_iter_max=3, tol=0, return_errors=True)
+    np.testing.assert_allclose(errs, oe, rtol=1e-6)
+    for a, b in zip(cp.factors, of):
+        assert rel(host(a), b) < 1e-4
