@@ -39,6 +39,25 @@ __device__ double block_sum(double v, double* scratch /* >= 32 */) {
 }
 
 // ---------------------------------------------------------------- sum of squares
+// f32 tensors: each square is split exactly into hi + lo (TwoProd by FMA) and
+// summed with Neumaier compensation in f32, so the thread total is accurate
+// to ~2^-40 relative without touching the (much slower) f64 pipe per element.
+__global__ void k_sumsq_f32(const float* __restrict__ X, int64_t n, double* part) {
+  __shared__ double scratch[32];
+  float s = 0.f, c = 0.f;
+  const int64_t step = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += step) {
+    const float x = X[i];
+    const float hi = x * x;
+    const float lo = fmaf(x, x, -hi);
+    const float t = s + hi;
+    c += ((fabsf(s) >= hi) ? ((s - t) + hi) : ((hi - t) + s)) + lo;
+    s = t;
+  }
+  const double tot = block_sum((double)s + (double)c, scratch);
+  if (threadIdx.x == 0) part[blockIdx.x] = tot;
+}
+
 template <typename T>
 __global__ void k_sumsq(const T* __restrict__ X, int64_t n, double* part) {
   __shared__ double scratch[32];
@@ -112,23 +131,24 @@ __global__ void k_gram_partial(const T* __restrict__ A, int64_t I, int R, int64_
 // lane, coalesced); its 8 warps take every 8th partial with four loads in
 // flight each, then the warps' sums are combined in a fixed order.
 __global__ void __launch_bounds__(256)
-k_gram_reduce(const double* __restrict__ gpart, int nparts, int RR, double* G, const int* done) {
+k_gram_reduce(const double* __restrict__ gpart, int nparts, int R, double* G, const int* done) {
   if (done && *done) return;
   __shared__ double red[8][33];
+  const int RR = R * R;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int e = blockIdx.x * 32 + lane;
-  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+  // the partials hold the lower triangle: entry (r, s) with s > r reads (s, r)
+  const int r = e / R, s = e - (e / R) * R;
+  const int src = (s > r) ? s * R + r : e;
+  double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   if (e < RR) {
     int p = warp;
-    for (; p + 24 < nparts; p += 32) {
-      s0 += gpart[(int64_t)p * RR + e];
-      s1 += gpart[(int64_t)(p + 8) * RR + e];
-      s2 += gpart[(int64_t)(p + 16) * RR + e];
-      s3 += gpart[(int64_t)(p + 24) * RR + e];
-    }
-    for (; p < nparts; p += 8) s0 += gpart[(int64_t)p * RR + e];
+    for (; p + 56 < nparts; p += 64)
+#pragma unroll
+      for (int u = 0; u < 8; ++u) acc[u] += gpart[(int64_t)(p + 8 * u) * RR + src];
+    for (; p < nparts; p += 8) acc[0] += gpart[(int64_t)p * RR + src];
   }
-  red[warp][lane] = (s0 + s1) + (s2 + s3);
+  red[warp][lane] = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7]));
   __syncthreads();
   if (warp == 0 && e < RR) {
     double t = 0.0;
@@ -165,31 +185,56 @@ constexpr float kIrMaxPivotRatio = 1e5f;
 
 template <typename T, int TI, int TJ, int NI, int NJ>
 __global__ void __launch_bounds__(TI * TJ)
-k_factorize_fast(const double* __restrict__ G, int ndim, int mode, int R, const T* w, double l2,
-                 double* vmat, float* w32, AlsCtrl* ctrl) {
+k_factorize_fast(const double* __restrict__ G, int ndim, int mode, int R,
+                 const T* __restrict__ w, double l2, double* __restrict__ vmat,
+                 float* __restrict__ w32, AlsCtrl* ctrl) {
   if (ctrl->done) return;
   __shared__ float rowk[NJ * TJ], colk[NI * TI];
+  __shared__ double wsh[NI * TI];
   const int ti = threadIdx.x / TJ, tj = threadIdx.x - (threadIdx.x / TJ) * TJ;
   const int RR = R * R;
+  for (int t = threadIdx.x; t < R; t += TI * TJ) wsh[t] = w ? (double)w[t] : 1.0;
+  __syncthreads();
+  // V = (prod_{k != mode} G_k + l2 I) * w w^T in f64, a chunk of rows at a
+  // time with every Gram load of the chunk issued before any use (they come
+  // from L2; issued one by one they would serialise on its latency).
+  constexpr int UB = (32 / NJ) > 0 ? (32 / NJ) : 1;
   float a[NI][NJ];
 #pragma unroll
-  for (int u = 0; u < NI; ++u)
+  for (int u0 = 0; u0 < NI; u0 += UB) {
+    double g[UB][NJ];
 #pragma unroll
-    for (int v = 0; v < NJ; ++v) {
-      const int i = ti + TI * u, j = tj + TJ * v;
-      float val = 0.f;
-      if (i < R && j < R) {   // V = (prod_{k != mode} G_k + l2 I) * w w^T, in f64
-        const int e = i * R + j;
-        double g = 1.0;
-        for (int k = 0; k < ndim; ++k)
-          if (k != mode) g = g * G[(int64_t)k * RR + e];
-        if (i == j) g = g + l2;
-        if (w) g = ((double)w[i] * g) * (double)w[j];
-        vmat[e] = g;
-        val = (float)g;
-      }
-      a[u][v] = val;
+    for (int u = 0; u < UB; ++u)
+#pragma unroll
+      for (int v = 0; v < NJ; ++v) g[u][v] = 1.0;
+    for (int k = 0; k < ndim; ++k) {
+      if (k == mode) continue;
+      const double* Gk = G + (int64_t)k * RR;
+#pragma unroll
+      for (int u = 0; u < UB; ++u)
+#pragma unroll
+        for (int v = 0; v < NJ; ++v) {
+          const int i = ti + TI * (u0 + u), j = tj + TJ * v;
+          if (u0 + u < NI && i < R && j < R) g[u][v] *= Gk[i * R + j];
+        }
     }
+#pragma unroll
+    for (int u = 0; u < UB; ++u)
+#pragma unroll
+      for (int v = 0; v < NJ; ++v) {
+        if (u0 + u >= NI) continue;
+        const int i = ti + TI * (u0 + u), j = tj + TJ * v;
+        float val = 0.f;
+        if (i < R && j < R) {
+          double gv = g[u][v];
+          if (i == j) gv = gv + l2;
+          gv = (wsh[i] * gv) * wsh[j];
+          vmat[i * R + j] = gv;
+          val = (float)gv;
+        }
+        a[u0 + u][v] = val;
+      }
+  }
   float pmin = 3.0e38f, pmax = 0.f;
   bool ok = true;
   for (int k = 0; k < R; ++k) {
@@ -213,7 +258,7 @@ k_factorize_fast(const double* __restrict__ G, int ndim, int mode, int R, const 
     if (!(p > 0.f)) { ok = false; break; }  // uniform: every thread read the same p
     pmin = fminf(pmin, p);
     pmax = fmaxf(pmax, p);
-    const float inv = 1.0f / p;
+    const float inv = __frcp_rn(p);
 #pragma unroll
     for (int u = 0; u < NI; ++u) {
       const int i = ti + TI * u;
@@ -373,9 +418,54 @@ __device__ __forceinline__ double store_entry(T* A, __nv_bfloat16* A_bt, int64_t
   return xd;
 }
 
-// Sum of the MTTKRP split partials of one entry, four independent f64 chains.
-template <typename T>
-__device__ __forceinline__ double sum_splits(const T* __restrict__ partial, int splits,
+// gacc += sum over `nrows` rows of a a^T, lower triangle only; the entry
+// index advances without integer division.
+__device__ __forceinline__ void gram_update(double* gacc, const double* rows, int nrows, int R) {
+  const int RR = R * R;
+  int e = threadIdx.x;
+  int r = e / R, s = e - (e / R) * R;
+  const int dr = blockDim.x / R, ds = blockDim.x - dr * R;
+  for (; e < RR; e += blockDim.x) {
+    if (s <= r) {
+      double g = gacc[e];
+      for (int w = 0; w < nrows; ++w) g = fma(rows[w * R + r], rows[w * R + s], g);
+      gacc[e] = g;
+    }
+    r += dr;
+    s += ds;
+    if (s >= R) { s -= R; ++r; }
+  }
+}
+
+// Sum of the MTTKRP split partials of one entry.  f32 partials: compensated
+// f32 summation (Neumaier), whose error (~splits * 2^-48) is far below the
+// partials' own rounding, on the f32 pipe (the f64 pipe is ~70x slower here).
+__device__ __forceinline__ double sum_splits(const float* __restrict__ partial, int splits,
+                                             int64_t stride, int64_t off) {
+  float s = 0.f, c = 0.f;
+  int p = 0;
+  for (; p + 3 < splits; p += 4) {
+    float v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) v[u] = partial[(int64_t)(p + u) * stride + off];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const float t = s + v[u];
+      c += (fabsf(s) >= fabsf(v[u])) ? ((s - t) + v[u]) : ((v[u] - t) + s);
+      s = t;
+    }
+  }
+  for (; p < splits; ++p) {
+    const float x = partial[(int64_t)p * stride + off];
+    const float t = s + x;
+    c += (fabsf(s) >= fabsf(x)) ? ((s - t) + x) : ((x - t) + s);
+    s = t;
+  }
+  return (double)s + (double)c;
+}
+
+// f64 partials: four independent f64 chains.
+__device__ __forceinline__ double sum_splits(const double* __restrict__ partial, int splits,
                                              int64_t stride, int64_t off) {
   double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
   int p = 0;
@@ -507,13 +597,7 @@ k_solve(const T* __restrict__ partial, int splits, int64_t I, int R,
         rb[rr * R + c] = 0.0;
       }
       __syncthreads();
-      for (int e = tid; e < RR; e += blockDim.x) {   // Gram of the stored rows
-        const int r = e / R, s2 = e - (e / R) * R;
-        if (s2 > r) continue;
-        double g = gacc[e];
-        for (int w = 0; w < RB; ++w) g = fma(rb[w * R + r], rb[w * R + s2], g);
-        gacc[e] = g;
-      }
+      gram_update(gacc, rb, RB, R);   // Gram of the stored rows
       __syncthreads();
     }
   } else {
@@ -587,24 +671,15 @@ k_solve(const T* __restrict__ partial, int splits, int64_t I, int R,
         for (int r = lane; r < R; r += 32) rb[r] = 0.0;
       }
       __syncthreads();
-      for (int e = tid; e < RR; e += blockDim.x) {
-        const int r = e / R, s2 = e - (e / R) * R;
-        if (s2 > r) continue;
-        double g = gacc[e];
-#pragma unroll
-        for (int w = 0; w < kSolveWarps; ++w) g = fma(rowbuf[w * R + r], rowbuf[w * R + s2], g);
-        gacc[e] = g;
-      }
+      gram_update(gacc, rowbuf, kSolveWarps, R);
       __syncthreads();
     }
   }
   ip = warp_sum(ip);
   if (lane == 0) s_ip[warp] = ip;
+  // lower triangle only (the upper one is not accumulated); the reducer mirrors
   double* out = gpart + (int64_t)blockIdx.x * RR;
-  for (int e = tid; e < RR; e += blockDim.x) {
-    const int r = e / R, s2 = e - (e / R) * R;
-    out[e] = (s2 <= r) ? gacc[r * R + s2] : gacc[s2 * R + r];
-  }
+  for (int e = tid; e < RR; e += blockDim.x) out[e] = gacc[e];
   __syncthreads();
   if (ipart && tid == 0) {
     double t = 0.0;
@@ -773,7 +848,7 @@ int solve_blocks_for(int64_t I) {
 int als_launch_sumsq(int dtype, const void* X, int64_t n, double* part, int nblocks,
                      AlsCtrl* ctrl, cudaStream_t st) {
   if (dtype == TLGB_F32)
-    k_sumsq<float><<<nblocks, 256, 0, st>>>((const float*)X, n, part);
+    k_sumsq_f32<<<nblocks, 256, 0, st>>>((const float*)X, n, part);
   else
     k_sumsq<double><<<nblocks, 256, 0, st>>>((const double*)X, n, part);
   TLGB_LAUNCH_CHECK();
@@ -806,7 +881,7 @@ int als_launch_gram(const T* A, int64_t I, int R, double* gpart, int nparts_max,
 int als_launch_gram_reduce(const double* gpart, int nparts, int R, double* G, const int* done,
                            cudaStream_t st) {
   const int RR = R * R;
-  k_gram_reduce<<<(int)ceil_div(RR, 32), 256, 0, st>>>(gpart, nparts, RR, G, done);
+  k_gram_reduce<<<(int)ceil_div(RR, 32), 256, 0, st>>>(gpart, nparts, R, G, done);
   TLGB_LAUNCH_CHECK();
   return TLGB_OK;
 }
@@ -827,9 +902,9 @@ int als_launch_factorize(const double* G, int ndim, int mode, int R, const T* we
   if (R <= 32)
     launch_fast<T, 8, 16, 4, 2>(G, ndim, mode, R, weights, l2_reg, vmat, w32, ctrl, st);
   else if (R <= 64)
-    launch_fast<T, 8, 16, 8, 4>(G, ndim, mode, R, weights, l2_reg, vmat, w32, ctrl, st);
+    launch_fast<T, 16, 16, 4, 4>(G, ndim, mode, R, weights, l2_reg, vmat, w32, ctrl, st);
   else if (R <= 96)
-    launch_fast<T, 8, 16, 12, 6>(G, ndim, mode, R, weights, l2_reg, vmat, w32, ctrl, st);
+    launch_fast<T, 16, 16, 6, 6>(G, ndim, mode, R, weights, l2_reg, vmat, w32, ctrl, st);
   else
     launch_fast<T, 16, 16, 10, 10>(G, ndim, mode, R, weights, l2_reg, vmat, w32, ctrl, st);
   TLGB_LAUNCH_CHECK();
@@ -871,7 +946,7 @@ template <typename T>
 int als_launch_fit(const double* G, int ndim, int R, const T* weights, const double* ipart,
                    int nip, AlsCtrl* ctrl, double* errors, int n_iter_max, double tol,
                    int cvg_criterion, cudaStream_t st) {
-  k_fit<T><<<1, 256, 0, st>>>(G, ndim, R, weights, ipart, nip, ctrl, errors, n_iter_max, tol,
+  k_fit<T><<<1, 512, 0, st>>>(G, ndim, R, weights, ipart, nip, ctrl, errors, n_iter_max, tol,
                               cvg_criterion);
   TLGB_LAUNCH_CHECK();
   return TLGB_OK;
