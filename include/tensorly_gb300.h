@@ -79,6 +79,24 @@ int tlgb_mttkrp(int dtype, const void* X, int ndim, const int64_t* shape,
                 void* out, void* workspace, size_t workspace_bytes, void* stream);
 
 /*
+ * tlgb_mttkrp without a workspace, for callers that own no device allocator
+ * (a plain C, cgo or ctypes binding): the partial tiles live in one fixed
+ * 16 MiB device array inside the library (TLGB_NOALLOC_SCRATCH_BYTES), and
+ * nothing is allocated.  Same plan and kernels as tlgb_mttkrp, so the result
+ * is bitwise identical.  Shapes whose partial tiles
+ * (tlgb_mttkrp_workspace_size) exceed the array return TLGB_EWORKSPACE.  The
+ * first call on a device performs that device's set-up: make it before any
+ * stream capture.  Nothing needs to start at zero.  The array is shared by
+ * all calls on a device: calls in flight at the same time (other streams or
+ * threads) race, so serialise them on one stream.
+ * No counterpart in TensorLy (its MTTKRP allocates through the backend).
+ */
+#define TLGB_NOALLOC_SCRATCH_BYTES (16u << 20)
+int tlgb_mttkrp_noalloc(int dtype, const void* X, int ndim, const int64_t* shape,
+                        const void* const* factors, const void* weights, int64_t rank,
+                        int mode, void* out, void* stream);
+
+/*
  * MTTKRP on the bf16 tensor cores (tcgen05, TMA): same contraction as
  * tlgb_mttkrp with X stored in bf16 and f32 accumulation.
  * X: bf16 tensor; factors[k]: f32 (shape[k] x rank) for the scaling modes;

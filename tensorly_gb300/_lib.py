@@ -64,6 +64,9 @@ SIGNATURES = [
      [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, _c_i64p, _c_vpp, ctypes.c_void_p,
       ctypes.c_int64, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
       ctypes.c_void_p]),
+    ("tlgb_mttkrp_noalloc", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, _c_i64p, _c_vpp, ctypes.c_void_p,
+      ctypes.c_int64, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),
     ("tlgb_mttkrp_bf16_workspace_size", ctypes.c_int,
      [ctypes.c_int, _c_i64p, ctypes.c_int64, ctypes.c_int, ctypes.POINTER(ctypes.c_size_t)]),
     ("tlgb_mttkrp_bf16", ctypes.c_int,
