@@ -47,8 +47,10 @@ def parse():
     p.add_argument("--rank", type=int, default=64)
     p.add_argument("--sweeps", type=int, default=50)
     p.add_argument("--refine", type=int, default=3)
-    p.add_argument("--cpu-sweeps", type=int, default=2)
+    p.add_argument("--cpu-sweeps", type=int, default=40)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--profile", action="store_true",
+                   help="run only the warm-up and timed steps (for ncu launch lists)")
     return p.parse_args()
 
 
@@ -168,14 +170,16 @@ def run_reference(args):
 def launches_per_step(ndim, sweeps, refine, precision):
     """Kernel launches of one parafac call (library structure):
     set-up: sum-of-squares (2) + one Gram per mode (2 each) [+ bf16 casts 1 + ndim];
-    per sweep: per mode factorise + MTTKRP + solve + Gram reduce (4), + fit (1)."""
+    per sweep: per mode fast + fallback factorisation (2), MTTKRP (1), solve (1),
+    Gram reduce (1); then the fit (1)."""
     setup = 2 + 2 * ndim + (1 + ndim if precision == "bf16" else 0)
-    return setup + sweeps * (4 * ndim + 1)
+    return setup + sweeps * (5 * ndim + 1)
 
 
-# DRAM bytes per launch of the dominant kernel from the committed ncu captures
-# (profiles/); None until a capture exists for that kernel.
-NCU_TRAFFIC = {"native": None, "bf16": None}
+# DRAM bytes (read + write) per launch of the dominant kernel, from the ncu
+# captures summarised in profiles/mttkrp_tc_kernel_512_r64.md and
+# profiles/mttkrp_split_kernel_f32_512_r64.md (512^3, rank 64).
+NCU_TRAFFIC = {"native": 537485312 + 13983488, "bf16": 268757504 + 3681536}
 KERNEL = {"native": "mttkrp_split_kernel<float,64> + reduce (SIMT f32)",
           "bf16": "mttkrp_tc_kernel (tcgen05 bf16, TMA)"}
 
@@ -302,6 +306,11 @@ def run_gpu(args):
     barrier()
     clk = clocks.stop()
     ms = ev0.elapsed_time(ev1)
+    if args.profile:
+        if rank == 0:
+            print(json.dumps({"profile": True, "ms_per_step": ms / args.steps,
+                              "final_rel_error": errs[-1]}), flush=True)
+        return
     if ws > 1:
         t = torch.tensor([ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
