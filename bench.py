@@ -167,13 +167,26 @@ def run_reference(args):
 
 
 # ----------------------------------------------------------------------------- GPU arm
-def launches_per_step(ndim, sweeps, refine, precision):
+def launches_per_step(ndim, sweeps, refine, precision, rank=64):
     """Kernel launches of one parafac call (library structure):
-    set-up: sum-of-squares (2) + one Gram per mode (2 each) [+ bf16 casts 1 + ndim];
-    per sweep: per mode fast + fallback factorisation (2), MTTKRP (1), solve (1),
-    Gram reduce (1); then the fit (1)."""
-    setup = 2 + 2 * ndim + (1 + ndim if precision == "bf16" else 0)
-    return setup + sweeps * (5 * ndim + 1)
+    set-up: sum-of-squares (2) + one Gram per mode (2 each) [+ tensor split or
+    cast (1) + factor planes (ndim)];
+    per sweep and mode: fast + fallback factorisation (2), MTTKRP (1, or 3 for
+    the three-plane f32 split), solve (1), Gram reduce (1); then the fit (1).
+    The closing sweep runs its last mode's MTTKRP on the SIMT kernel."""
+    mode_cost = 5
+    if precision != "bf16":
+        return 2 + 2 * ndim + sweeps * (mode_cost * ndim + 1)
+    setup = 2 + 2 * ndim + 1 + ndim
+    refine = min(refine, sweeps)
+    bf16 = sweeps - refine
+    if refine == 0:
+        return setup + bf16 * (mode_cost * ndim + 1)
+    split = 7 if rank <= 64 else mode_cost      # three MTTKRP launches per mode
+    n = setup + bf16 * (mode_cost * ndim + 1)
+    n += (refine - 1) * (split * ndim + 1)
+    n += split * (ndim - 1) + mode_cost + 1
+    return n
 
 
 # DRAM bytes (read + write) per launch of the dominant kernel, from the ncu
@@ -182,68 +195,6 @@ def launches_per_step(ndim, sweeps, refine, precision):
 NCU_TRAFFIC = {"native": 537485312 + 13983488, "bf16": 268757504 + 3681536}
 KERNEL = {"native": "mttkrp_split_kernel<float,64> + reduce (SIMT f32)",
           "bf16": "mttkrp_tc_kernel (tcgen05 bf16, TMA)"}
-
-
-def mttkrp_callable(x, factors, mode, precision):
-    """A closure that enqueues one MTTKRP of `mode` through the C ABI with
-    preallocated buffers (no allocation per call)."""
-    import ctypes
-    import torch
-    from tensorly_gb300 import _lib
-    lib = _lib.lib()
-    n = x.ndim
-    rank = factors[0].shape[1]
-    shape = _lib.i64_array(x.shape)
-    out = torch.empty((x.shape[mode], rank), dtype=torch.float32, device=x.device)
-    st = torch.cuda.current_stream().cuda_stream
-    if precision == "bf16":
-        xb = x.to(torch.bfloat16)
-        fbt = []
-        for f in factors:  # hi / lo planes of the transposed factor
-            ft = f.t().contiguous()
-            hi = ft.to(torch.bfloat16)
-            fbt.append(torch.stack([hi, (ft - hi.float()).to(torch.bfloat16)]).contiguous())
-        nbytes = ctypes.c_size_t(0)
-        _lib.check(lib.tlgb_mttkrp_bf16_workspace_size(n, shape, rank, mode, ctypes.byref(nbytes)))
-        ws = torch.empty(max(256, nbytes.value), dtype=torch.uint8, device=x.device)
-        fp = _lib.ptr_array([f.data_ptr() for f in factors])
-        bp = _lib.ptr_array([f.data_ptr() for f in fbt])
-
-        def fn():
-            _lib.check(lib.tlgb_mttkrp_bf16(xb.data_ptr(), n, shape, fp, bp, None, rank, mode,
-                                            out.data_ptr(), ws.data_ptr(), ws.numel(), st))
-        fn.keep = (xb, fbt, ws)
-        return fn
-    nbytes = ctypes.c_size_t(0)
-    _lib.check(lib.tlgb_mttkrp_workspace_size(_lib.TLGB_F32, n, shape, rank, mode,
-                                              ctypes.byref(nbytes)))
-    ws = torch.empty(max(256, nbytes.value), dtype=torch.uint8, device=x.device)
-    fp = _lib.ptr_array([f.data_ptr() for f in factors])
-
-    def fn():
-        _lib.check(lib.tlgb_mttkrp(_lib.TLGB_F32, x.data_ptr(), n, shape, fp, None, rank, mode,
-                                   out.data_ptr(), ws.data_ptr(), ws.numel(), st))
-    fn.keep = (ws,)
-    return fn
-
-
-def mttkrp_alone_ms(tg, x, factors, mode, precision, reps=10):
-    """Average duration of the dominant kernel (the MTTKRP of `mode`),
-    launched alone through the library on the current stream, CUDA events."""
-    import torch
-    st = torch.cuda.current_stream()
-    fn = mttkrp_callable(x, factors, mode, precision)
-    for _ in range(3):
-        fn()
-    a = torch.cuda.Event(enable_timing=True)
-    b = torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    a.record(st)
-    for _ in range(reps):
-        fn()
-    b.record(st)
-    torch.cuda.synchronize()
-    return a.elapsed_time(b) / reps
 
 
 def congruence(fa, fb):
@@ -282,8 +233,8 @@ def run_gpu(args):
     kw = dict(n_iter_max=args.sweeps, tol=0, precision=args.precision,
               refine_sweeps=args.refine, check_every=args.sweeps, return_errors=True)
 
-    def step():
-        return tg.parafac(x, args.rank, init=tg.CPTensor((None, init)), **kw)
+    def step(times=None):
+        return tg.parafac(x, args.rank, init=tg.CPTensor((None, init)), mttkrp_times=times, **kw)
 
     def barrier():
         if ws > 1:
@@ -352,13 +303,25 @@ def run_gpu(args):
     h2d = x_np.nbytes + sum(f.nbytes for f in init_np)
     d2h = sum(f.nbytes for f in init_np) + 4 * args.rank
 
-    # ---- the dominant kernel alone (CUDA events) for the roofline
-    mode = 1
-    k_ms = mttkrp_alone_ms(tg, x, init, mode, args.precision)
+    # ---- the dominant kernel: CUDA events around each mode's MTTKRP launch on
+    # its stream, in steps identical to the timed ones except that the sweeps
+    # are launched directly instead of replayed as graphs (events inside a
+    # graph cannot be timed); the last sweep of each kind per step
+    timings = []
+    for _ in range(args.steps):
+        t = {}
+        step(t)
+        timings.append(t)
+    kind = "bf16" if args.precision == "bf16" else "native"
+    samples = [v for t in timings for v in t.get(kind, []) if v > 0]
+    k_ms = float(np.mean(samples)) if samples else None
+    by_kind = {k: float(np.mean([v for t in timings for v in t.get(k, []) if v > 0]))
+               for k in ("native", "bf16", "f32_split", "closing")
+               if any(v > 0 for t in timings for v in t.get(k, []))}
     esz = 2 if args.precision == "bf16" else 4
     nel = args.size ** 3
     alg_bytes = nel * esz + 2 * args.size * args.rank * (esz + 4) + args.size * args.rank * 4
-    achieved = alg_bytes / (k_ms / 1000.0) / 1e9
+    achieved = alg_bytes / (k_ms / 1000.0) / 1e9 if k_ms else None
     peak, peak_kind = measured_peaks()
 
     # ---- CPU baseline: bounded sample of the NumPy restatement (rank 0, N=1)
@@ -384,15 +347,19 @@ def run_gpu(args):
                    "l2": "input 512 MiB > L2, no flush"},
         "accuracy_vs_f64": acc,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_source": peak_kind,
+                     "frac": achieved / peak if achieved else None, "peak_source": peak_kind,
                      "kernel": KERNEL[args.precision],
-                     "kernel_ms": k_ms, "algorithmic_bytes": alg_bytes,
-                     "traffic": NCU_TRAFFIC[args.precision]},
+                     "kernel_ms": k_ms, "kernel_samples": len(samples),
+                     "algorithmic_bytes": alg_bytes,
+                     "traffic": (NCU_TRAFFIC[args.precision]
+                                 if (args.size, args.rank) == (512, 64) else None),
+                     "mttkrp_ms_by_sweep_kind": by_kind},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "clocks": clk,
-        "gpu_launches": launches_per_step(3, args.sweeps, args.refine, args.precision) * args.steps,
+        "gpu_launches": launches_per_step(3, args.sweeps, args.refine, args.precision,
+                                          args.rank) * args.steps,
     }
     print(json.dumps(line), flush=True)
 

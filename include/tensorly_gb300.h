@@ -44,7 +44,7 @@ extern "C" {
 
 /* CP-ALS precision modes */
 #define TLGB_PREC_NATIVE 0   /* every sweep in the tensor dtype (f32 or f64) */
-#define TLGB_PREC_BF16 1     /* bf16 tensor + tensor-core MTTKRP, then native refinement sweeps */
+#define TLGB_PREC_BF16 1     /* bf16 tensor + tensor-core MTTKRP, then f32 refinement sweeps */
 
 /* Library version, e.g. 100 for 0.1.0. */
 int tlgb_version(void);
@@ -107,7 +107,7 @@ int tlgb_mttkrp_noalloc(int dtype, const void* X, int ndim, const int64_t* shape
  * modes may be NULL.  weights: f32 rank or NULL.
  * out: f32 shape[mode] x rank.  Requirements (else TLGB_EUNSUPPORTED):
  * rank <= 128, the inner mode a multiple of 8 (and shape[ndim-1] a multiple
- * of 8 when mode == ndim-1), inner mode * padded rank * 2 bytes <= 96 KiB.
+ * of 8 when mode == ndim-1).
  * The first int of the workspace receives TLGB_ETIMEOUT if the kernel's
  * bounded pipeline waits expired (read it with tlgb_workspace_status).
  * Replaces tensorly/tenalg/core_tenalg/mttkrp.py:9-50 for bf16 storage.
@@ -123,8 +123,12 @@ int tlgb_mttkrp_bf16(const void* X, int ndim, const int64_t* shape, const void* 
  * value 0 restores the default): "tc_group_kib" = bytes of the split inner
  * factor kept resident per CTA (KiB; sets how the inner mode is partitioned
  * across CTAs), "tc_stages" = cap on the tensor-tile ring depth,
- * "tc_waves" = CTAs per SM in the grid.  Process-wide; no counterpart in
- * TensorLy.
+ * "tc_waves" = CTAs per SM in the grid, "tc_reserve_sms" = SMs the grid
+ * leaves free (CP-ALS leaves 1 for its concurrent factorisation kernel),
+ * "refine_simt" = 1 makes the f32
+ * refinement sweeps of TLGB_PREC_BF16 use the SIMT f32 MTTKRP instead of the
+ * tensor-core one on the exact three-plane bf16 split of the f32 tensor.
+ * Process-wide; no counterpart in TensorLy.
  */
 int tlgb_set_tuning(const char* key, int value);
 
@@ -163,12 +167,24 @@ typedef struct tlgb_cp_als_options {
   int normalize_factors;   /* parafac normalize_factors */
   uint32_t fixed_modes;    /* bit k set: mode k is kept fixed (parafac fixed_modes) */
   int precision;           /* TLGB_PREC_NATIVE or TLGB_PREC_BF16 (f32 tensors only) */
-  int refine_sweeps;       /* TLGB_PREC_BF16: closing sweeps in f32 */
+  int refine_sweeps;       /* TLGB_PREC_BF16: closing sweeps with an f32-accurate MTTKRP
+                              (tensor cores on the exact 3-plane bf16 split of X and
+                              the factor when rank <= 64, else the SIMT f32 kernel) */
   int check_every;         /* sweeps between host reads of the device stop flag (>= 1) */
   int use_graph;           /* replay one captured sweep as a CUDA graph */
   tlgb_sweep_callback callback;  /* per-sweep hook (parafac callback) or NULL */
   void* callback_user;
+  /* Optional (NULL = off), host, TLGB_CP_ALS_SWEEP_KINDS x TLGB_MAX_MODES
+   * doubles: entry [kind * TLGB_MAX_MODES + mode] receives the duration (ms,
+   * CUDA events recorded around the MTTKRP launch on the stream) of that
+   * mode's MTTKRP in the last sweep of each kind that ran, 0 if none, -1 if
+   * the events could not be read.  Setting it disables use_graph (events
+   * recorded inside a graph cannot be timed).  Kinds: 0 native SIMT, 1 bf16 tensor-core,
+   * 2 three-plane f32 split on the tensor cores, 3 the closing sweep.  No
+   * counterpart in TensorLy. */
+  double* mttkrp_ms;
 } tlgb_cp_als_options;
+#define TLGB_CP_ALS_SWEEP_KINDS 4
 
 void tlgb_cp_als_default_options(tlgb_cp_als_options* opts);
 int tlgb_cp_als_workspace_size(int dtype, int ndim, const int64_t* shape, int64_t rank,

@@ -47,7 +47,12 @@ class CpAlsOptions(ctypes.Structure):
         ("use_graph", ctypes.c_int),
         ("callback", SWEEP_CALLBACK),
         ("callback_user", ctypes.c_void_p),
+        ("mttkrp_ms", ctypes.POINTER(ctypes.c_double)),
     ]
+
+
+CP_ALS_SWEEP_KINDS = 4
+SWEEP_KIND_NAMES = ("native", "bf16", "f32_split", "closing")
 
 
 # (name, restype, argtypes) for every entry point of include/tensorly_gb300.h

@@ -288,13 +288,16 @@ k_factorize_fast(const double* __restrict__ G, int ndim, int mode, int R,
 
 // ---- fallback: f64 Cholesky (fac_kind 0) or LU with partial pivoting
 // (fac_kind 1) of V when the fast path reported fac_kind 3; fac layout
-// [R*R] factor(s) then [R] reciprocal diagonal.
+// [R*R] factor(s) then [R] reciprocal diagonal.  V is factorised in place in
+// global memory (`vmat`, which only the refinement path of the solve reads):
+// this rare path then needs no dynamic shared memory, so it never keeps an SM
+// from hosting a tensor-core MTTKRP CTA that runs concurrently on another
+// stream.
 template <typename T>
 __global__ void __launch_bounds__(256)
 k_factorize(const double* G, int ndim, int mode, int R, const T* w, double l2, double* fac,
-            int* perm, AlsCtrl* ctrl) {
+            int* perm, double* V, AlsCtrl* ctrl) {
   if (ctrl->done || ctrl->fac_kind != 3) return;
-  extern __shared__ double V[];  // R*R
   __shared__ int s_fail;
   __shared__ int s_piv;
   const int RR = R * R;
@@ -409,11 +412,15 @@ __device__ __forceinline__ double store_entry(T* A, __nv_bfloat16* A_bt, int64_t
   A[row * R + r] = xv;
   const double xd = (double)xv;
   rb[r] = xd;
-  if (A_bt) {  // bf16 split transposed copy (hi, lo planes) for the tensor cores
+  if (A_bt) {  // three-plane bf16 split, transposed, for the tensor cores
     const float xf = (float)xv;
-    const __nv_bfloat16 hi = __float2bfloat16_rn(xf);
-    A_bt[(int64_t)r * I + row] = hi;
-    A_bt[(int64_t)R * I + (int64_t)r * I + row] = __float2bfloat16_rn(xf - __bfloat162float(hi));
+    const __nv_bfloat16 p0 = __float2bfloat16_rn(xf);
+    const float r1 = xf - __bfloat162float(p0);
+    const __nv_bfloat16 p1 = __float2bfloat16_rn(r1);
+    const int64_t plane = (int64_t)R * I, at = (int64_t)r * I + row;
+    A_bt[at] = p0;
+    A_bt[plane + at] = p1;
+    A_bt[2 * plane + at] = __float2bfloat16_rn(r1 - __bfloat162float(p1));
   }
   return xd;
 }
@@ -908,8 +915,7 @@ int als_launch_factorize(const double* G, int ndim, int mode, int R, const T* we
   else
     launch_fast<T, 16, 16, 10, 10>(G, ndim, mode, R, weights, l2_reg, vmat, w32, ctrl, st);
   TLGB_LAUNCH_CHECK();
-  k_factorize<T><<<1, 256, (size_t)R * R * sizeof(double), st>>>(G, ndim, mode, R, weights,
-                                                                 l2_reg, fac, perm, ctrl);
+  k_factorize<T><<<1, 256, 0, st>>>(G, ndim, mode, R, weights, l2_reg, fac, perm, vmat, ctrl);
   TLGB_LAUNCH_CHECK();
   return TLGB_OK;
 }
@@ -992,14 +998,29 @@ template int als_launch_probe_error<double>(const double*, int, int64_t, int, co
                                             const double*, int, const double*, double*, int,
                                             const AlsCtrl*, double*, cudaStream_t);
 
+template <typename T, int TI, int TJ, int NI, int NJ>
+static cudaError_t set_carveout_fast() {
+  return cudaFuncSetAttribute(k_factorize_fast<T, TI, TJ, NI, NJ>,
+                              cudaFuncAttributePreferredSharedMemoryCarveout,
+                              cudaSharedmemCarveoutMaxShared);
+}
+
 template <typename T>
 static int als_prepare_typed() {
   static bool done[64] = {};
   const int dev = current_device();
   if (dev >= 0 && dev < 64 && done[dev]) return TLGB_OK;
-  TLGB_CUDA_TRY(cudaFuncSetAttribute(
-      k_factorize<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-      (int)((size_t)kMaxAlsRank * kMaxAlsRank * sizeof(double))));
+  // The factorisation kernels run on a side stream next to the tensor-core
+  // MTTKRP, whose CTAs need nearly all of an SM's shared memory: keep the SMs
+  // they land on configured for the maximum shared-memory carveout, so a
+  // MTTKRP CTA can start beside them instead of waiting for them to finish.
+  TLGB_CUDA_TRY(cudaFuncSetAttribute(k_factorize<T>,
+                                     cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     cudaSharedmemCarveoutMaxShared));
+  TLGB_CUDA_TRY((set_carveout_fast<T, 8, 16, 4, 2>()));
+  TLGB_CUDA_TRY((set_carveout_fast<T, 16, 16, 4, 4>()));
+  TLGB_CUDA_TRY((set_carveout_fast<T, 16, 16, 6, 6>()));
+  TLGB_CUDA_TRY((set_carveout_fast<T, 16, 16, 10, 10>()));
   TLGB_CUDA_TRY(cudaFuncSetAttribute(
       k_gram_partial<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
       (int)(((size_t)kMaxAlsRank * kMaxAlsRank + kGramRows * kMaxAlsRank) * sizeof(double))));

@@ -30,8 +30,9 @@ struct AlsBuffers {
   double* gpart;
   double* ipart;
   double* sumsq_part;
-  __nv_bfloat16* xbf;                   // bf16 copy of X (mixed precision)
-  __nv_bfloat16* fbt[kMaxModes];        // bf16 split transposed factors (2 x rank x rows)
+  __nv_bfloat16* xbf;                   // bf16 copy of X (mixed precision) = split plane x0
+  __nv_bfloat16* xsplit[2];             // planes x1, x2 of the exact split (f32 refinement)
+  __nv_bfloat16* fbt[kMaxModes];        // bf16 split transposed factors (3 x rank x rows)
   void* tc_partial;
   double* probe;                        // one f64 result slot (initial error)
   size_t bytes;
@@ -39,8 +40,22 @@ struct AlsBuffers {
 
 constexpr int kSumsqBlocks = 1024;
 
+constexpr int kFactorPlanes = 3;
+// The factorisation of the next normal equations runs on a side stream during
+// each MTTKRP (one CTA): the tensor-core MTTKRP grid leaves this many SMs free
+// for it (measured at 512^3: 86 us -> 55 us per MTTKRP).
+constexpr int kAuxSms = 1;
+
+struct Plans {
+  MttkrpPlan simt[kMaxModes];
+  TcPlan tc[kMaxModes];          // bf16 sweeps (2 factor planes)
+  TcPlan tcr[kMaxModes][3];      // f32-faithful refinement: x0, x1, x2 with 3, 2, 1 planes
+  bool refine_tc = false;        // refinement sweeps run on the tensor cores
+};
+
 int layout(int dtype, const Shape& sh, int64_t R, const tlgb_cp_als_options& o,
-           const MttkrpPlan* plans, const TcPlan* tcplans, void* base, AlsBuffers* B) {
+           const Plans& P, void* base, AlsBuffers* B) {
+  const MttkrpPlan* plans = P.simt;
   Carver c(base);
   const int64_t RR = R * R;
   const int esz = dtype == TLGB_F64 ? 8 : 4;
@@ -64,15 +79,24 @@ int layout(int dtype, const Shape& sh, int64_t R, const tlgb_cp_als_options& o,
   B->sumsq_part = c.take<double>(kSumsqBlocks);
   B->probe = c.take<double>(1);
   B->xbf = nullptr;
+  B->xsplit[0] = B->xsplit[1] = nullptr;
   for (int k = 0; k < kMaxModes; ++k) B->fbt[k] = nullptr;
   B->tc_partial = nullptr;
   if (o.precision == TLGB_PREC_BF16) {
     B->xbf = c.take<__nv_bfloat16>((size_t)sh.numel);
+    if (P.refine_tc) {
+      B->xsplit[0] = c.take<__nv_bfloat16>((size_t)sh.numel);
+      B->xsplit[1] = c.take<__nv_bfloat16>((size_t)sh.numel);
+    }
     for (int k = 0; k < sh.ndim; ++k)
-      B->fbt[k] = c.take<__nv_bfloat16>((size_t)2 * R * sh.dim[k]);  // hi and lo planes
+      B->fbt[k] = c.take<__nv_bfloat16>((size_t)kFactorPlanes * R * sh.dim[k]);
     size_t tmax = 0;
-    for (int k = 0; k < sh.ndim; ++k)
-      if (tcplans[k].valid) tmax = std::max(tmax, tcplans[k].partial_bytes);
+    for (int k = 0; k < sh.ndim; ++k) {
+      if (P.tc[k].valid) tmax = std::max(tmax, P.tc[k].partial_bytes);
+      if (P.refine_tc)
+        tmax = std::max(tmax, P.tcr[k][0].partial_bytes + P.tcr[k][1].partial_bytes +
+                                  P.tcr[k][2].partial_bytes);
+    }
     B->tc_partial = c.take<char>(tmax);
   }
   (void)esz;
@@ -101,23 +125,34 @@ int validate(int dtype, int ndim, const int64_t* shape, int64_t rank,
   return TLGB_OK;
 }
 
-struct Plans {
-  MttkrpPlan simt[kMaxModes];
-  TcPlan tc[kMaxModes];
-};
-
 int make_plans(int dtype, const Shape& sh, int64_t R, const tlgb_cp_als_options& o, Plans* P) {
+  const bool mixed = o.precision == TLGB_PREC_BF16;
+  P->refine_tc = mixed && o.refine_sweeps > 0 && !tc_tuning().refine_simt;
   for (int k = 0; k < sh.ndim; ++k) {
     int rc = mttkrp_make_plan(dtype, sh, R, k, &P->simt[k]);
     if (rc) return rc;
     P->tc[k] = TcPlan{};
-    if (o.precision == TLGB_PREC_BF16) {
-      rc = mttkrp_tc_make_plan(sh, R, k, &P->tc[k]);
+    for (int j = 0; j < 3; ++j) P->tcr[k][j] = TcPlan{};
+    if (mixed) {
+      rc = mttkrp_tc_make_plan(sh, R, k, 2, kAuxSms, &P->tc[k]);
       if (rc) return rc;
+    }
+    if (P->refine_tc) {
+      for (int j = 0; j < 3; ++j) {
+        rc = mttkrp_tc_make_plan(sh, R, k, 3 - j, kAuxSms, &P->tcr[k][j]);
+        if (rc) return rc;
+        if (!P->tcr[k][j].valid) P->refine_tc = false;
+      }
     }
   }
   return TLGB_OK;
 }
+
+constexpr int kSweepNative = 0;
+constexpr int kSweepBf16 = 1;
+constexpr int kSweepF32Tc = 2;
+constexpr int kSweepF32TcFinal = 3;
+constexpr int kCpAlsSweepKinds = TLGB_CP_ALS_SWEEP_KINDS;
 
 template <typename T>
 struct Runner {
@@ -136,9 +171,20 @@ struct Runner {
   // captured into the graph as parallel branches).
   cudaStream_t aux = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // optional timing events around each mode's MTTKRP (recorded into the graph)
+  cudaEvent_t ev_mt[2][kMaxModes] = {};
 
-  // Enqueues one sweep; `tc` selects the bf16 tensor-core MTTKRP.
-  int sweep(bool tc, cudaStream_t st) {
+  // Enqueues one sweep.  kind: kSweepNative (SIMT MTTKRP in the tensor dtype),
+  // kSweepBf16 (bf16 tensor, two-plane factor, tensor cores), kSweepF32Tc
+  // (three-plane split of the f32 tensor and factor on the tensor cores) or
+  // kSweepF32TcFinal (the same, but the last mode's MTTKRP on the SIMT f32
+  // kernel).  The tensor cores' f32 accumulation rounds toward zero (measured
+  // bias about -2e-7 of |M| at 512^3, against ~1e-10 for the SIMT kernel) and
+  // the fit's cancellation amplifies an error in <M_last, A_last> by about
+  // ||X||^2 / rec_error^2; the closing sweep's last MTTKRP feeds the reported
+  // error, so it runs unbiased.
+  int sweep(int kind, cudaStream_t st) {
+    const bool tc = kind == kSweepBf16;
     const int N = sh.ndim;
     const int RR = (int)(R * R);
     const int* done = &B.ctrl->done;
@@ -157,16 +203,34 @@ struct Runner {
                                        B.vmat, B.w32, B.ctrl, aux);
       if (rc) return rc;
       TLGB_CUDA_TRY(cudaEventRecord(ev_join, aux));
+      if (ev_mt[0][mode]) TLGB_CUDA_TRY(cudaEventRecord(ev_mt[0][mode], st));
       int splits;
       const void* partial;
       if (tc && P->tc[mode].valid) {
         if constexpr (sizeof(T) == 4) {
           rc = mttkrp_tc_launch(P->tc[mode], B.xbf, (const float* const*)cf, B.fbt,
-                                (const float*)mw, (float*)B.tc_partial, done, &B.ctrl->tc_err,
-                                st);
+                                kFactorPlanes, (const float*)mw, (float*)B.tc_partial, done,
+                                &B.ctrl->tc_err, st);
         }
         if (rc) return rc;
         splits = P->tc[mode].splits;
+        partial = B.tc_partial;
+      } else if (kind == kSweepF32Tc || (kind == kSweepF32TcFinal && !last)) {
+        // x0 . (f0 + f1 + f2) + x1 . (f0 + f1) + x2 . f0, each launch writing
+        // its own run of partial tiles; the solve sums all of them
+        splits = 0;
+        if constexpr (sizeof(T) == 4) {
+          const __nv_bfloat16* planes[3] = {B.xbf, B.xsplit[0], B.xsplit[1]};
+          for (int j = 0; j < 3 && !rc; ++j) {
+            const TcPlan& tp = P->tcr[mode][j];
+            rc = mttkrp_tc_launch(tp, planes[j], (const float* const*)cf, B.fbt, kFactorPlanes,
+                                  (const float*)mw,
+                                  (float*)B.tc_partial + (size_t)splits * tp.I_out * tp.R, done,
+                                  &B.ctrl->tc_err, st);
+            splits += tp.splits;
+          }
+        }
+        if (rc) return rc;
         partial = B.tc_partial;
       } else {
         rc = mttkrp_launch_partials<T>(P->simt[mode], X, cf, mw, (T*)B.partial, done, st);
@@ -174,6 +238,7 @@ struct Runner {
         splits = P->simt[mode].splits;
         partial = B.partial;
       }
+      if (ev_mt[1][mode]) TLGB_CUDA_TRY(cudaEventRecord(ev_mt[1][mode], st));
       TLGB_CUDA_TRY(cudaStreamWaitEvent(st, ev_join, 0));
       int nb = 0;
       rc = als_launch_solve<T>((const T*)partial, splits, sh.dim[mode], (int)R, B.fac, B.perm,
@@ -195,7 +260,7 @@ struct Runner {
       if (rc) return rc;
       rc = grams(done, st);
       if (rc) return rc;
-      if (tc) {
+      if (kind != kSweepNative) {
         rc = bf16_factors(st);
         if (rc) return rc;
       }
@@ -238,7 +303,8 @@ struct Runner {
   // bf16 transposed copies of every factor (tensor-core operand B)
   int bf16_factors(cudaStream_t st) {
     for (int k = 0; k < sh.ndim; ++k) {
-      int rc = tc_launch_factor_bf16t((const float*)factors[k], sh.dim[k], R, B.fbt[k], st);
+      int rc = tc_launch_factor_bf16t((const float*)factors[k], sh.dim[k], R, kFactorPlanes,
+                                      B.fbt[k], st);
       if (rc) return rc;
     }
     return TLGB_OK;
@@ -275,7 +341,7 @@ int run(const T* X, const Shape& sh, int64_t R, T* const* factors, T* weights,
   Runner<T> run{};
   run.X = X; run.sh = sh; run.R = R; run.factors = factors; run.weights = weights; run.o = o;
   run.P = &P;
-  rc = layout(TypeCode<T>::value, sh, R, o, P.simt, P.tc, ws, &run.B);
+  rc = layout(TypeCode<T>::value, sh, R, o, P, ws, &run.B);
   if (rc) return rc;
   if (ws_bytes < run.B.bytes) return set_error(TLGB_EWORKSPACE, "cp_als: workspace too small");
   for (int k = 0; k < sh.ndim; ++k)
@@ -299,6 +365,15 @@ int run(const T* X, const Shape& sh, int64_t R, T* const* factors, T* weights,
   run.aux = aux.s;
   run.ev_fork = ev_fork.e;
   run.ev_join = ev_join.e;
+  EventGuard ev_mt[2][kMaxModes];
+  if (o.mttkrp_ms) {
+    for (int i = 0; i < kCpAlsSweepKinds * kMaxModes; ++i) o.mttkrp_ms[i] = 0.0;
+    for (int j = 0; j < 2; ++j)
+      for (int k = 0; k < sh.ndim; ++k) {
+        TLGB_CUDA_TRY(cudaEventCreate(&ev_mt[j][k].e));
+        run.ev_mt[j][k] = ev_mt[j][k].e;
+      }
+  }
 
   // ---- set-up: control block, ||X||^2, Grams, bf16 operands
   TLGB_CUDA_TRY(cudaMemsetAsync(run.B.ctrl, 0, sizeof(AlsCtrl), st));
@@ -308,7 +383,9 @@ int run(const T* X, const Shape& sh, int64_t R, T* const* factors, T* weights,
   rc = run.grams(nullptr, st);
   if (rc) return rc;
   if (mixed) {
-    rc = tc_launch_to_bf16((const float*)X, sh.numel, run.B.xbf, st);
+    rc = P.refine_tc ? tc_launch_split3((const float*)X, sh.numel, run.B.xbf, run.B.xsplit[0],
+                                        run.B.xsplit[1], st)
+                     : tc_launch_to_bf16((const float*)X, sh.numel, run.B.xbf, st);
     if (rc) return rc;
     rc = run.bf16_factors(st);
     if (rc) return rc;
@@ -327,19 +404,24 @@ int run(const T* X, const Shape& sh, int64_t R, T* const* factors, T* weights,
   }
 
   // ---- phases: (bf16 sweeps, then native refinement) or native sweeps only
-  struct Phase { bool tc; int sweeps; };
+  struct Phase { int kind; int sweeps; };
   std::vector<Phase> phases;
   if (mixed) {
     const int refine = std::min(o.refine_sweeps, o.n_iter_max);
-    if (o.n_iter_max - refine > 0) phases.push_back({true, o.n_iter_max - refine});
-    if (refine > 0) phases.push_back({false, refine});
+    if (o.n_iter_max - refine > 0) phases.push_back({kSweepBf16, o.n_iter_max - refine});
+    if (refine > 0 && !P.refine_tc) phases.push_back({kSweepNative, refine});
+    if (refine > 1 && P.refine_tc) phases.push_back({kSweepF32Tc, refine - 1});
+    if (refine > 0 && P.refine_tc) phases.push_back({kSweepF32TcFinal, 1});
   } else {
-    phases.push_back({false, o.n_iter_max});
+    phases.push_back({kSweepNative, o.n_iter_max});
   }
   const int check_every = (o.callback != nullptr) ? 1 : std::max(1, o.check_every);
 
   StreamGuard cap;
-  if (o.use_graph) TLGB_CUDA_TRY(cudaStreamCreateWithFlags(&cap.s, cudaStreamNonBlocking));
+  // Timing events recorded inside a graph cannot be read back, so timed runs
+  // launch the sweeps directly (kernel durations are the same).
+  const bool use_graph = o.use_graph && !o.mttkrp_ms;
+  if (use_graph) TLGB_CUDA_TRY(cudaStreamCreateWithFlags(&cap.s, cudaStreamNonBlocking));
 
   AlsCtrl hc{};
   int launched = 0;
@@ -347,14 +429,14 @@ int run(const T* X, const Shape& sh, int64_t R, T* const* factors, T* weights,
   bool stopped = false;
   for (size_t pi = 0; pi < phases.size() && !stopped; ++pi) {
     const Phase ph = phases[pi];
-    if (pi > 0) {
+    if (pi > 0 && phases[pi - 1].kind == kSweepBf16) {
       // A converged bf16 phase still gets its refinement sweeps: clear the flag.
       TLGB_CUDA_TRY(cudaMemsetAsync(&run.B.ctrl->done, 0, sizeof(int), st));
     }
     GraphGuard gg;
-    if (o.use_graph) {
+    if (use_graph) {
       TLGB_CUDA_TRY(cudaStreamBeginCapture(cap.s, cudaStreamCaptureModeThreadLocal));
-      int rc2 = run.sweep(ph.tc, cap.s);
+      int rc2 = run.sweep(ph.kind, cap.s);
       cudaGraph_t g = nullptr;
       cudaError_t ce = cudaStreamEndCapture(cap.s, &g);
       gg.g = g;
@@ -364,10 +446,10 @@ int run(const T* X, const Shape& sh, int64_t R, T* const* factors, T* weights,
       TLGB_CUDA_TRY(cudaGraphInstantiate(&gg.e, gg.g, 0));
     }
     for (int s = 0; s < ph.sweeps; ++s) {
-      if (o.use_graph) {
+      if (use_graph) {
         TLGB_CUDA_TRY(cudaGraphLaunch(gg.e, st));
       } else {
-        rc = run.sweep(ph.tc, st);
+        rc = run.sweep(ph.kind, st);
         if (rc) return rc;
       }
       ++launched;
@@ -392,6 +474,16 @@ int run(const T* X, const Shape& sh, int64_t R, T* const* factors, T* weights,
         if (stopped || hc.done) break;  // callback asked to stop, or converged
       }
     }
+    if (o.mttkrp_ms) {  // durations of this phase's last sweep (the host synced above)
+      for (int k : run.modes) {
+        float ms = 0.f;
+        const cudaError_t e = cudaEventElapsedTime(&ms, run.ev_mt[0][k], run.ev_mt[1][k]);
+        if (e != cudaSuccess) cudaGetLastError();
+        o.mttkrp_ms[ph.kind * kMaxModes + k] = (e == cudaSuccess) ? (double)ms : -1.0;
+      }
+    }
+    // only the bf16 phase hands a converged run on to further sweeps
+    if (hc.done && ph.kind != kSweepBf16) break;
   }
   TLGB_CUDA_TRY(cudaMemcpyAsync(&hc, run.B.ctrl, sizeof(AlsCtrl), cudaMemcpyDeviceToHost, st));
   TLGB_CUDA_TRY(cudaStreamSynchronize(st));
@@ -438,7 +530,7 @@ extern "C" int tlgb_cp_als_workspace_size(int dtype, int ndim, const int64_t* sh
   rc = make_plans(dtype, sh, rank, *opts, &P);
   if (rc) return rc;
   AlsBuffers B;
-  rc = layout(dtype, sh, rank, *opts, P.simt, P.tc, nullptr, &B);
+  rc = layout(dtype, sh, rank, *opts, P, nullptr, &B);
   if (rc) return rc;
   *bytes = B.bytes;
   return TLGB_OK;

@@ -12,7 +12,7 @@
 // flattened (o, 64-wide c chunk) steps of that tile.  Warp roles:
 //   warp 0      TMA producer: the inner factor (bf16 hi/lo split, K-major)
 //               once, then one 128 x 64 tensor tile per step into a ring of
-//               3-6 stages (as many as shared memory leaves room for)
+//               3-12 stages (as many as shared memory leaves room for)
 //   warp 1      TMEM allocation and the single-thread tcgen05.mma issue
 //               (M = 128, N = 2 x padded rank, K = 16, four per step) into one
 //               of two TMEM accumulators (double buffered across outer slices)
@@ -203,18 +203,30 @@ __host__ __device__ constexpr uint32_t make_idesc(int n, int a_mn) {
          | ((uint32_t)(kTileM >> 4) << 24);  // M / 16
 }
 
-// B operand = [F_hi ; F_lo]: the inner factor split into two bf16 terms
-// (F_lo = bf16(F - F_hi)), stacked as 2*RP rows, so one MMA with N = 2*RP
-// forms X.F_hi and X.F_lo side by side in TMEM and the epilogue adds them.
-// The factor then enters the contraction with ~16 mantissa bits: with a
-// single bf16 rounding of the factor, ALS stalls at a worse stationary point
-// in swamp phases (rounding only the tensor to bf16 does not).
-template <int RP, bool MN>
+// TMEM columns of one accumulator buffer (a power of two >= the MMA N).
+__host__ __device__ constexpr int tmem_stride(int nb) {
+  return nb <= 32 ? 32 : nb <= 64 ? 64 : nb <= 128 ? 128 : nb <= 256 ? 256 : 512;
+}
+
+// B operand = the first NPL bf16 planes of the inner factor, F = f0 + f1 + f2
+// with f0 = bf16(F), f1 = bf16(F - f0), f2 = bf16(F - f0 - f1), stacked as
+// NPL*RP rows, so one MMA with N = NPL*RP forms X.f0, X.f1, ... side by side
+// in TMEM and the epilogue adds them.
+//  * bf16 sweeps: NPL = 2, the factor enters with ~16 mantissa bits (with a
+//    single bf16 rounding of the factor, ALS stalls at a worse stationary
+//    point in swamp phases; rounding only the tensor to bf16 does not).
+//  * f32-faithful MTTKRP: the f32 tensor is split exactly into x0 + x1 + x2
+//    (same construction) and contracted in three launches, x0 with NPL = 3,
+//    x1 with NPL = 2, x2 with NPL = 1: every product x_i f_j with i + j <= 2.
+//    The dropped terms are below 2^-26 of |x||f|, under one f32 rounding.
+template <int RP, bool MN, int NPL>
 __global__ void __launch_bounds__(kThreads, 1)
 mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmF,
                  const TcArgs a) {
   if (a.skip && *a.skip) return;
-  constexpr int NB = 2 * RP;               // MMA N (hi and lo halves)
+  constexpr int NB = NPL * RP;             // MMA N (one RP-wide block per factor plane)
+  constexpr int TS = tmem_stride(NB);      // TMEM columns per accumulator buffer
+  static_assert(NB <= 256 && 2 * TS <= 512, "accumulators exceed one MMA or TMEM");
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* base = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
@@ -259,7 +271,7 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant_
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(tmem_slot)),
-                 "r"(2 * NB)
+                 "r"(2 * TS)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -276,8 +288,9 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant_
         mbar_expect_tx(bfull, (uint32_t)b_bytes);
         for (int kc = 0; kc < KC; ++kc) {
           unsigned char* dst = sB + kc * NB * 128;
-          tma_load_3d(dst, &tmF, bfull, (kc0 + kc) * kChunk, 0, 0);             // F_hi rows
-          tma_load_3d(dst + RP * 128, &tmF, bfull, (kc0 + kc) * kChunk, 0, 1);  // F_lo rows
+#pragma unroll
+          for (int pl = 0; pl < NPL; ++pl)   // rows of factor plane pl
+            tma_load_3d(dst + pl * RP * 128, &tmF, bfull, (kc0 + kc) * kChunk, 0, pl);
         }
         // Coordinates advance incrementally (no 64-bit division per step:
         // this single thread's issue rate bounds the whole CTA's bandwidth).
@@ -336,7 +349,7 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant_
           tc_fence_after();
           const uint32_t a_base = smem_u32(sA + stage * kStageBytes);
           const uint32_t b_base = smem_u32(sB + kc * NB * 128);
-          const uint32_t d = tmem + (uint32_t)(buf * NB);
+          const uint32_t d = tmem + (uint32_t)(buf * TS);
 #pragma unroll
           for (int k = 0; k < kChunk / 16; ++k) {
             const uint64_t adesc = MN ? smem_desc(a_base + k * 2048, kStageBytes / 2, 1024)
@@ -399,26 +412,34 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant_
         if (!ep_ok[buf]) break;  // uniform across the four epilogue warps
         __syncwarp();            // tcgen05.ld is warp-collective
         tc_fence_after();
-        const uint32_t lane_addr = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(buf * NB);
+        const uint32_t lane_addr = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(buf * TS);
         if constexpr (RP >= 32) {
 #pragma unroll
           for (int c = 0; c < RP / 32; ++c) {
-            uint32_t hi[32], lo[32];
-            tmem_ld32_nowait(lane_addr + (uint32_t)(c * 32), hi);
-            tmem_ld32_nowait(lane_addr + (uint32_t)(RP + c * 32), lo);
+            uint32_t pv[NPL][32];
+#pragma unroll
+            for (int pl = 0; pl < NPL; ++pl)
+              tmem_ld32_nowait(lane_addr + (uint32_t)(pl * RP + c * 32), pv[pl]);
             tmem_wait_ld();
 #pragma unroll
-            for (int j = 0; j < 32; ++j)
-              acc[c * 32 + j] = fmaf(s_sm[buf * RP + c * 32 + j],
-                                     __uint_as_float(hi[j]) + __uint_as_float(lo[j]),
-                                     acc[c * 32 + j]);
+            for (int j = 0; j < 32; ++j) {
+              float v = __uint_as_float(pv[NPL - 1][j]);   // smallest plane first
+#pragma unroll
+              for (int pl = NPL - 2; pl >= 0; --pl) v += __uint_as_float(pv[pl][j]);
+              acc[c * 32 + j] = fmaf(s_sm[buf * RP + c * 32 + j], v, acc[c * 32 + j]);
+            }
           }
         } else {
-          float hi[16], lo[16];
-          tmem_ld16(lane_addr, hi);
-          tmem_ld16(lane_addr + (uint32_t)RP, lo);
+          float pv[NPL][16];
 #pragma unroll
-          for (int j = 0; j < 16; ++j) acc[j] = fmaf(s_sm[buf * RP + j], hi[j] + lo[j], acc[j]);
+          for (int pl = 0; pl < NPL; ++pl) tmem_ld16(lane_addr + (uint32_t)(pl * RP), pv[pl]);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            float v = pv[NPL - 1][j];
+#pragma unroll
+            for (int pl = NPL - 2; pl >= 0; --pl) v += pv[pl][j];
+            acc[j] = fmaf(s_sm[buf * RP + j], v, acc[j]);
+          }
         }
         tc_fence_before();
         mbar_arrive(&dempty[buf]);
@@ -444,7 +465,7 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant_
   if (warp == 1) {
     __syncwarp();
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * NB)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TS)
                  : "memory");
   }
 }
@@ -462,17 +483,51 @@ __global__ void k_to_bf16(const float* __restrict__ X, int64_t n, __nv_bfloat16*
     Y[i] = __float2bfloat16_rn(X[i]);
 }
 
-// Transposed bf16 split of a factor: out[0][r][i] = bf16(A[i][r]) (hi),
-// out[1][r][i] = bf16(A[i][r] - hi) (lo).
-__global__ void k_factor_bf16t(const float* __restrict__ A, int64_t rows, int64_t R,
+// Exact three-term bf16 split of an f32 tensor: x = x0 + x1 + x2 with
+// x0 = bf16(x), x1 = bf16(x - x0), x2 = bf16(x - x0 - x1).  The residuals are
+// exact in f32 and x2 holds the last <= 8 significant bits, so the sum is x
+// (for normal numbers).
+__global__ void k_split3_bf16(const float* __restrict__ X, int64_t n, __nv_bfloat16* __restrict__ y0,
+                              __nv_bfloat16* __restrict__ y1, __nv_bfloat16* __restrict__ y2) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n / 2;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 v = reinterpret_cast<const float2*>(X)[i];
+    const __nv_bfloat162 a0 = __floats2bfloat162_rn(v.x, v.y);
+    const float2 r1 = make_float2(v.x - __low2float(a0), v.y - __high2float(a0));
+    const __nv_bfloat162 a1 = __floats2bfloat162_rn(r1.x, r1.y);
+    const __nv_bfloat162 a2 =
+        __floats2bfloat162_rn(r1.x - __low2float(a1), r1.y - __high2float(a1));
+    reinterpret_cast<__nv_bfloat162*>(y0)[i] = a0;
+    reinterpret_cast<__nv_bfloat162*>(y1)[i] = a1;
+    reinterpret_cast<__nv_bfloat162*>(y2)[i] = a2;
+  }
+  if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+    const float x = X[n - 1];
+    const __nv_bfloat16 a0 = __float2bfloat16_rn(x);
+    const float r1 = x - __bfloat162float(a0);
+    const __nv_bfloat16 a1 = __float2bfloat16_rn(r1);
+    y0[n - 1] = a0;
+    y1[n - 1] = a1;
+    y2[n - 1] = __float2bfloat16_rn(r1 - __bfloat162float(a1));
+  }
+}
+
+// Transposed bf16 split of a factor into `planes` (2 or 3) planes, each
+// R x rows: out[0] = bf16(A^T), out[1] = bf16(A^T - out[0]),
+// out[2] = bf16(A^T - out[0] - out[1]).
+__global__ void k_factor_bf16t(const float* __restrict__ A, int64_t rows, int64_t R, int planes,
                                __nv_bfloat16* __restrict__ out) {
   const int64_t n = rows * R;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
        e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = e / R, r = e % R;
-    const __nv_bfloat16 hi = __float2bfloat16_rn(A[e]);
-    out[r * rows + i] = hi;
-    out[n + r * rows + i] = __float2bfloat16_rn(A[e] - __bfloat162float(hi));
+    const float x = A[e];
+    const __nv_bfloat16 p0 = __float2bfloat16_rn(x);
+    const float r1 = x - __bfloat162float(p0);
+    const __nv_bfloat16 p1 = __float2bfloat16_rn(r1);
+    out[r * rows + i] = p0;
+    out[n + r * rows + i] = p1;
+    if (planes > 2) out[2 * n + r * rows + i] = __float2bfloat16_rn(r1 - __bfloat162float(p1));
   }
 }
 
@@ -505,34 +560,50 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 size_t tail_bytes(int n_pad) {
   return (2 * kMaxStages + 6) * sizeof(uint64_t) + 16 + 2 * (size_t)n_pad * sizeof(float);
 }
-size_t b_bytes_for(int64_t kc, int n_pad) { return (size_t)kc * 2 * n_pad * 128; }
+size_t b_bytes_for(int64_t kc, int npl, int n_pad) { return (size_t)kc * npl * n_pad * 128; }
 size_t smem_for(const TcPlan& p) {
-  return 1024 + (size_t)p.stages * kStageBytes + b_bytes_for(p.kcg, p.n_pad) + tail_bytes(p.n_pad);
+  return 1024 + (size_t)p.stages * kStageBytes + b_bytes_for(p.kcg, p.npl, p.n_pad) +
+         tail_bytes(p.n_pad);
 }
 
-template <int RP, bool MN>
+template <int RP, bool MN, int NPL>
 int set_attr_one() {
-  TLGB_CUDA_TRY(cudaFuncSetAttribute(mttkrp_tc_kernel<RP, MN>,
+  TLGB_CUDA_TRY(cudaFuncSetAttribute(mttkrp_tc_kernel<RP, MN, NPL>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBudget));
   return TLGB_OK;
 }
 
+// Instantiated kernels: NPL = 2 for every padded rank; NPL = 1 and 3 (the
+// f32-faithful split) for padded ranks <= 64, where 3 planes fit one MMA.
 template <bool MN>
 int set_attrs_mn() {
-  int rc = set_attr_one<16, MN>();
-  if (!rc) rc = set_attr_one<32, MN>();
-  if (!rc) rc = set_attr_one<64, MN>();
-  if (!rc) rc = set_attr_one<128, MN>();
+  int rc = set_attr_one<16, MN, 2>();
+  if (!rc) rc = set_attr_one<32, MN, 2>();
+  if (!rc) rc = set_attr_one<64, MN, 2>();
+  if (!rc) rc = set_attr_one<128, MN, 2>();
+  if (!rc) rc = set_attr_one<16, MN, 1>();
+  if (!rc) rc = set_attr_one<32, MN, 1>();
+  if (!rc) rc = set_attr_one<64, MN, 1>();
+  if (!rc) rc = set_attr_one<16, MN, 3>();
+  if (!rc) rc = set_attr_one<32, MN, 3>();
+  if (!rc) rc = set_attr_one<64, MN, 3>();
   return rc;
 }
 
-template <int RP, bool MN>
+template <int RP, bool MN, int NPL>
 int launch_tc(const TcPlan& p, const CUtensorMap& tx, const CUtensorMap& tf, const TcArgs& a,
               cudaStream_t st) {
   dim3 grid((unsigned)p.gsplits, (unsigned)p.n_cg, (unsigned)p.m_tiles);
-  mttkrp_tc_kernel<RP, MN><<<grid, kThreads, smem_for(p), st>>>(tx, tf, a);
+  mttkrp_tc_kernel<RP, MN, NPL><<<grid, kThreads, smem_for(p), st>>>(tx, tf, a);
   TLGB_LAUNCH_CHECK();
   return TLGB_OK;
+}
+
+template <int RP, int NPL>
+int launch_mn(const TcPlan& p, const CUtensorMap& tx, const CUtensorMap& tf, const TcArgs& a,
+              cudaStream_t st) {
+  return p.out_contig ? launch_tc<RP, true, NPL>(p, tx, tf, a, st)
+                      : launch_tc<RP, false, NPL>(p, tx, tf, a, st);
 }
 
 }  // namespace
@@ -553,8 +624,10 @@ TcTuning& tc_tuning() {
   return t;
 }
 
-int mttkrp_tc_make_plan(const Shape& sh, int64_t rank, int mode, TcPlan* plan) {
+int mttkrp_tc_make_plan(const Shape& sh, int64_t rank, int mode, int npl, int free_sms,
+                        TcPlan* plan) {
   TcPlan p{};
+  p.npl = npl;
   const int N = sh.ndim;
   if (N < 2 || N > kMaxModes || mode < 0 || mode >= N)
     return set_error(TLGB_EINVAL, "mttkrp_bf16: bad mode");
@@ -581,7 +654,7 @@ int mttkrp_tc_make_plan(const Shape& sh, int64_t rank, int mode, TcPlan* plan) {
   p.m_tiles = (int)ceil_div(p.I_out, kTileM);
   // Inner-mode groups: a CTA keeps only its group's slice of the split factor
   // resident (about 64 KiB), which leaves room for a deep tensor-tile ring.
-  const int per_chunk = 2 * p.n_pad * 128;
+  const int per_chunk = npl * p.n_pad * 128;
   const int resident = tc_tuning().group_kib > 0 ? tc_tuning().group_kib : 64;
   const int max_g = std::max(1, (resident * 1024) / per_chunk);
   int kcg = 1;
@@ -590,11 +663,11 @@ int mttkrp_tc_make_plan(const Shape& sh, int64_t rank, int mode, TcPlan* plan) {
   p.kcg = kcg;
   p.n_cg = (int)ceil_div(p.kc, kcg);
   p.total_steps = p.O * p.kc;
-  const size_t bbytes = b_bytes_for(p.kcg, p.n_pad);
+  const size_t bbytes = b_bytes_for(p.kcg, p.npl, p.n_pad);
   const int64_t room = (int64_t)kSmemBudget - 1024 - (int64_t)bbytes - (int64_t)tail_bytes(p.n_pad);
   p.stages = (int)std::min<int64_t>(kMaxStages, room > 0 ? room / kStageBytes : 0);
   if (tc_tuning().stages > 0) p.stages = std::min(p.stages, tc_tuning().stages);
-  bool ok = rank <= 128 && (p.C % 8 == 0) && (p.I_out % (p.out_contig ? 8 : 1) == 0) &&
+  bool ok = rank <= 128 && npl >= 1 && npl <= 3 && (npl == 2 || p.n_pad <= 64) && (p.C % 8 == 0) && (p.I_out % (p.out_contig ? 8 : 1) == 0) &&
             p.stages >= kMinStages && p.I_out < (1ll << 31) && p.C < (1ll << 31) &&
             p.O < (1ll << 31) && p.m_tiles <= 65535 && p.n_cg <= 65535;
   if (!ok) {
@@ -604,7 +677,11 @@ int mttkrp_tc_make_plan(const Shape& sh, int64_t rank, int mode, TcPlan* plan) {
   }
   // one wave: (output tiles x groups x splits) CTAs <= SM count when possible
   const int64_t pairs = (int64_t)p.m_tiles * p.n_cg;
-  const int64_t ctas = (int64_t)sm_count() * (tc_tuning().waves > 0 ? tc_tuning().waves : 1);
+  const int64_t ctas =
+      std::max<int64_t>(1, (int64_t)(sm_count() - (tc_tuning().reserve_sms > 0
+                                                        ? tc_tuning().reserve_sms
+                                                        : free_sms)) *
+                               (tc_tuning().waves > 0 ? tc_tuning().waves : 1));
   int64_t gs = std::max<int64_t>(1, ctas / pairs);
   const int64_t gsteps = p.O * p.kcg;
   gs = std::max<int64_t>(1, std::min<int64_t>(gs, gsteps));
@@ -618,8 +695,8 @@ int mttkrp_tc_make_plan(const Shape& sh, int64_t rank, int mode, TcPlan* plan) {
 }
 
 int mttkrp_tc_launch(const TcPlan& p, const __nv_bfloat16* Xbf, const float* const* factors,
-                     __nv_bfloat16* const* fbt, const float* weights, float* partial,
-                     const int* skip_flag, int* err, cudaStream_t st) {
+                     __nv_bfloat16* const* fbt, int fplanes, const float* weights,
+                     float* partial, const int* skip_flag, int* err, cudaStream_t st) {
   if (!p.valid) return set_error(TLGB_EUNSUPPORTED, "mttkrp_bf16: shape not supported");
   auto enc = encode_fn();
   if (!enc) return set_error(TLGB_EUNSUPPORTED, "cuTensorMapEncodeTiled unavailable");
@@ -679,8 +756,9 @@ int mttkrp_tc_launch(const TcPlan& p, const __nv_bfloat16* Xbf, const float* con
                     CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (cr != CUDA_SUCCESS) return set_error(TLGB_ECUDA, "mttkrp_bf16: tensor map for X failed");
-  // inner factor as (C, R, 2): hi and lo planes of the transposed bf16 factor
-  cuuint64_t fdim[3] = {(cuuint64_t)p.C, (cuuint64_t)p.R, 2};
+  TLGB_CHECK_ARG(fplanes >= p.npl && fplanes <= 3, "mttkrp_bf16: too few factor planes");
+  // inner factor as (C, R, planes): the planes of the transposed bf16 split
+  cuuint64_t fdim[3] = {(cuuint64_t)p.C, (cuuint64_t)p.R, (cuuint64_t)fplanes};
   cuuint64_t fstride[2] = {(cuuint64_t)p.C * 2, (cuuint64_t)p.C * (cuuint64_t)p.R * 2};
   cuuint32_t fbox[3] = {(cuuint32_t)kChunk, (cuuint32_t)p.n_pad, 1};
   cr = enc(&tf, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<__nv_bfloat16*>(F), fdim, fstride,
@@ -707,12 +785,26 @@ int mttkrp_tc_launch(const TcPlan& p, const __nv_bfloat16* Xbf, const float* con
   a.partial = partial;
   a.err = err;
   a.skip = skip_flag;
-  const bool mn = p.out_contig != 0;
+  if (p.npl == 2) {
+    switch (p.n_pad) {
+      case 16: return launch_mn<16, 2>(p, tx, tf, a, st);
+      case 32: return launch_mn<32, 2>(p, tx, tf, a, st);
+      case 64: return launch_mn<64, 2>(p, tx, tf, a, st);
+      default: return launch_mn<128, 2>(p, tx, tf, a, st);
+    }
+  }
+  if (p.n_pad > 64) return set_error(TLGB_EUNSUPPORTED, "mttkrp_tc: 1 or 3 planes need rank <= 64");
+  if (p.npl == 1) {
+    switch (p.n_pad) {
+      case 16: return launch_mn<16, 1>(p, tx, tf, a, st);
+      case 32: return launch_mn<32, 1>(p, tx, tf, a, st);
+      default: return launch_mn<64, 1>(p, tx, tf, a, st);
+    }
+  }
   switch (p.n_pad) {
-    case 16: return mn ? launch_tc<16, true>(p, tx, tf, a, st) : launch_tc<16, false>(p, tx, tf, a, st);
-    case 32: return mn ? launch_tc<32, true>(p, tx, tf, a, st) : launch_tc<32, false>(p, tx, tf, a, st);
-    case 64: return mn ? launch_tc<64, true>(p, tx, tf, a, st) : launch_tc<64, false>(p, tx, tf, a, st);
-    default: return mn ? launch_tc<128, true>(p, tx, tf, a, st) : launch_tc<128, false>(p, tx, tf, a, st);
+    case 16: return launch_mn<16, 3>(p, tx, tf, a, st);
+    case 32: return launch_mn<32, 3>(p, tx, tf, a, st);
+    default: return launch_mn<64, 3>(p, tx, tf, a, st);
   }
 }
 
@@ -733,11 +825,23 @@ int tc_launch_to_bf16(const float* X, int64_t n, __nv_bfloat16* out, cudaStream_
   return TLGB_OK;
 }
 
-int tc_launch_factor_bf16t(const float* A, int64_t rows, int64_t R, __nv_bfloat16* out,
-                           cudaStream_t st) {
+int tc_launch_split3(const float* X, int64_t n, __nv_bfloat16* x0, __nv_bfloat16* x1,
+                     __nv_bfloat16* x2, cudaStream_t st) {
+  TLGB_CHECK_ARG((reinterpret_cast<uintptr_t>(X) % 8) == 0 &&
+                     (reinterpret_cast<uintptr_t>(x0) % 4) == 0 &&
+                     (reinterpret_cast<uintptr_t>(x1) % 4) == 0 &&
+                     (reinterpret_cast<uintptr_t>(x2) % 4) == 0,
+                 "split3: misaligned buffers");
+  k_split3_bf16<<<sm_count() * 8, 256, 0, st>>>(X, n, x0, x1, x2);
+  TLGB_LAUNCH_CHECK();
+  return TLGB_OK;
+}
+
+int tc_launch_factor_bf16t(const float* A, int64_t rows, int64_t R, int planes,
+                           __nv_bfloat16* out, cudaStream_t st) {
   const int64_t n = rows * R;
   const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), sm_count() * 4));
-  k_factor_bf16t<<<blocks, 256, 0, st>>>(A, rows, R, out);
+  k_factor_bf16t<<<blocks, 256, 0, st>>>(A, rows, R, planes, out);
   TLGB_LAUNCH_CHECK();
   return TLGB_OK;
 }
@@ -757,12 +861,12 @@ int tc_plan_for(int ndim, const int64_t* shape, int64_t rank, int mode, TcPlan* 
   TLGB_CHECK_ARG(rank >= 1, "mttkrp_bf16: rank must be >= 1");
   for (int k = 0; k < ndim; ++k) TLGB_CHECK_ARG(shape[k] >= 1, "mttkrp_bf16: empty mode");
   Shape sh = make_shape(ndim, shape);
-  int rc = mttkrp_tc_make_plan(sh, rank, mode, p);
+  int rc = mttkrp_tc_make_plan(sh, rank, mode, 2, 0, p);
   if (rc) return rc;
   if (!p->valid)
     return set_error(TLGB_EUNSUPPORTED,
-                     "mttkrp_bf16: needs rank <= 128, inner mode (and a last output mode) a "
-                     "multiple of 8, and the inner factor within 96 KiB of shared memory");
+                     "mttkrp_bf16: needs rank <= 128 and the inner mode (and a last output "
+                     "mode) a multiple of 8");
   return TLGB_OK;
 }
 }  // namespace
@@ -799,8 +903,8 @@ extern "C" int tlgb_mttkrp_bf16(const void* X, int ndim, const int64_t* shape,
   float* partial = reinterpret_cast<float*>(static_cast<char*>(workspace) + 256);
   TLGB_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), st));
   rc = mttkrp_tc_launch(p, static_cast<const __nv_bfloat16*>(X), (const float* const*)factors,
-                        (__nv_bfloat16* const*)factors_bf16_t, static_cast<const float*>(weights),
-                        partial, nullptr, err, st);
+                        (__nv_bfloat16* const*)factors_bf16_t, 2,
+                        static_cast<const float*>(weights), partial, nullptr, err, st);
   if (rc) return rc;
   return tc_launch_sum_partials(p, partial, static_cast<float*>(out), st);
 }
@@ -822,6 +926,8 @@ extern "C" int tlgb_set_tuning(const char* key, int value) {
   if (k == "tc_group_kib") tc_tuning().group_kib = value;
   else if (k == "tc_stages") tc_tuning().stages = value;
   else if (k == "tc_waves") tc_tuning().waves = value;
+  else if (k == "refine_simt") tc_tuning().refine_simt = value;
+  else if (k == "tc_reserve_sms") tc_tuning().reserve_sms = value;
   else return set_error(TLGB_EINVAL, "set_tuning: unknown key " + k);
   return TLGB_OK;
 }

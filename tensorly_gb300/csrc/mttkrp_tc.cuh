@@ -13,7 +13,8 @@ struct TcPlan {
   int outer_mode[kMaxModes];
   int64_t outer_dim[kMaxModes], outer_stride[kMaxModes];
   int out_contig;
-  int n_pad;            // rank padded to 16/32/64/128 (MMA N = 2 * n_pad)
+  int n_pad;            // rank padded to 16/32/64/128 (MMA N = npl * n_pad)
+  int npl;              // factor planes in the B operand (2: bf16 sweeps; 3, 2, 1: f32 split)
   int stages;           // tensor-tile ring depth that fits next to the resident factor
   int m_tiles;
   int64_t kc;           // 64-element chunks of the inner mode
@@ -34,26 +35,37 @@ struct TcTuning {
   int group_kib = 0;
   int stages = 0;
   int waves = 0;
+  int refine_simt = 0;  // 1: CP-ALS refinement sweeps use the SIMT f32 MTTKRP
+  int reserve_sms = 0;  // overrides the SMs a plan leaves free (0 = the plan's own)
 };
 TcTuning& tc_tuning();
 
 int mttkrp_tc_prepare();
-int mttkrp_tc_make_plan(const Shape& sh, int64_t rank, int mode, TcPlan* plan);
+// npl: factor planes contracted with the tensor (1..3; 1 and 3 need rank <= 64).
+// free_sms: SMs the one-wave grid leaves free for kernels that run concurrently
+// on another stream (a CTA of this kernel needs nearly a whole SM, so one busy
+// SM would otherwise delay the whole launch by that kernel's duration).
+int mttkrp_tc_make_plan(const Shape& sh, int64_t rank, int mode, int npl, int free_sms,
+                        TcPlan* plan);
 
-// partial[split][I_out][R] (f32) from the bf16 tensor, the f32 factors (outer
-// scales) and the bf16 split transposed factors (inner operand: two planes,
-// hi then lo, each rank x rows).
+// partial[split][I_out][R] (f32) from a bf16 tensor, the f32 factors (outer
+// scales) and the bf16 split transposed factors (inner operand: `fplanes`
+// planes of rank x rows each, the first p.npl of which are contracted).
 // err: device int that receives TLGB_ETIMEOUT if a bounded wait expired.
 int mttkrp_tc_launch(const TcPlan& p, const __nv_bfloat16* Xbf, const float* const* factors,
-                     __nv_bfloat16* const* fbt, const float* weights, float* partial,
-                     const int* skip_flag, int* err, cudaStream_t st);
+                     __nv_bfloat16* const* fbt, int fplanes, const float* weights,
+                     float* partial, const int* skip_flag, int* err, cudaStream_t st);
 
 // out = sum over splits of partial (I_out x R, f32).
 int tc_launch_sum_partials(const TcPlan& p, const float* partial, float* out, cudaStream_t st);
 
 int tc_launch_to_bf16(const float* X, int64_t n, __nv_bfloat16* out, cudaStream_t st);
-// out (2 x R x rows bf16): hi = bf16(A^T), lo = bf16(A^T - hi).
-int tc_launch_factor_bf16t(const float* A, int64_t rows, int64_t R, __nv_bfloat16* out,
-                           cudaStream_t st);
+// Exact split X = x0 + x1 + x2 into three bf16 tensors.
+int tc_launch_split3(const float* X, int64_t n, __nv_bfloat16* x0, __nv_bfloat16* x1,
+                     __nv_bfloat16* x2, cudaStream_t st);
+// out (planes x R x rows bf16, planes 2 or 3): the bf16 split of A^T,
+// plane 0 = bf16(A^T), plane k = bf16(A^T - planes before k).
+int tc_launch_factor_bf16t(const float* A, int64_t rows, int64_t R, int planes,
+                           __nv_bfloat16* out, cudaStream_t st);
 
 }  // namespace tlgb

@@ -114,7 +114,7 @@ def parafac(tensor, rank, n_iter_max=100, init="svd", svd="truncated_svd",
             verbose=0, return_errors=False, sparsity=None, l2_reg=0, mask=None,
             cvg_criterion="abs_rec_error", fixed_modes=None, svd_mask_repeats=5,
             linesearch=False, callback=None, *, precision="native", refine_sweeps=3,
-            check_every=8, use_graph=True):
+            check_every=8, use_graph=True, mttkrp_times=None):
     """CP decomposition by ALS (tensorly/decomposition/_cp.py:230-543).
 
     Same signature, return types and stopping rule as the reference.  The
@@ -122,7 +122,11 @@ def parafac(tensor, rank, n_iter_max=100, init="svd", svd="truncated_svd",
     stores an f32 tensor in bf16 and runs the tensor-core MTTKRP for all but
     the last ``refine_sweeps`` sweeps, which run in f32; ``check_every`` is the
     number of sweeps between host reads of the device-side stop flag;
-    ``use_graph`` replays one captured sweep as a CUDA graph.
+    ``use_graph`` replays one captured sweep as a CUDA graph.  If
+    ``mttkrp_times`` is a dict, it receives, per sweep kind that ran
+    (``'native'``, ``'bf16'``, ``'f32_split'``, ``'closing'``), the list of
+    per-mode MTTKRP durations (ms, CUDA events inside the sweep) of the last
+    sweep of that kind.
     """
     if sparsity:
         raise NotImplementedError("parafac with sparsity is not supported by tensorly_gb300")
@@ -174,6 +178,10 @@ def parafac(tensor, rank, n_iter_max=100, init="svd", svd="truncated_svd",
     opts.refine_sweeps = int(refine_sweeps)
     opts.check_every = int(check_every)
     opts.use_graph = 1 if use_graph else 0
+    times = None
+    if mttkrp_times is not None:
+        times = (ctypes.c_double * (_lib.CP_ALS_SWEEP_KINDS * MAX_MODES))()
+        opts.mttkrp_ms = ctypes.cast(times, ctypes.POINTER(ctypes.c_double))
 
     failure = []
     if callback is not None:
@@ -201,6 +209,11 @@ def parafac(tensor, rank, n_iter_max=100, init="svd", svd="truncated_svd",
     if failure:
         raise failure[0]
     _lib.check(rc)
+    if times is not None:
+        for kind, name in enumerate(_lib.SWEEP_KIND_NAMES):
+            row = [float(times[kind * MAX_MODES + m]) for m in range(x.ndim)]
+            if any(v != 0.0 for v in row):
+                mttkrp_times[name] = row
     rec_errors = [float(errs[i]) for i in range(n_err.value)]
     if verbose:
         for i, e in enumerate(rec_errors):

@@ -135,3 +135,61 @@ def test_parafac_bf16_reaches_f64_fit(gb300):
                              refine_sweeps=3)
     assert len(errs) == 25
     assert abs(errs[-1] - oerr[-1]) <= 1e-4 * oerr[-1], (errs[-1], oerr[-1])
+
+
+@pytest.mark.parametrize("shape,rank", [((64, 48, 40), 24), ((40, 24, 16, 32), 8),
+                                        ((128, 96, 80), 64), ((32, 40, 48), 5)])
+def test_f32_split_sweep_matches_simt_f32(gb300, shape, rank):
+    """A sweep whose MTTKRPs run on the tensor cores with the exact three-plane
+    bf16 split of the f32 tensor (x0 . (f0+f1+f2) + x1 . (f0+f1) + x2 . f0)
+    matches the same sweep with the SIMT f32 MTTKRP to f32 accuracy, and both
+    match the f64 oracle sweep on the same f32 bytes."""
+    import oracle
+    from tensorly_gb300 import _lib
+    lib = _lib.lib()
+    rs = np.random.RandomState(sum(shape) + rank)
+    x = rs.randn(*shape).astype(np.float32)
+    init = [rs.randn(s, rank).astype(np.float32) for s in shape]
+    xt = torch.as_tensor(x, device="cuda")
+
+    def one_sweep(refine_simt):
+        lib.tlgb_set_tuning(b"refine_simt", refine_simt)
+        try:
+            # n_iter_max == refine_sweeps: the only sweep is the f32 refinement sweep
+            cp, errs = gb300.parafac(
+                xt, rank, init=gb300.CPTensor((None, [torch.as_tensor(f, device="cuda")
+                                                      for f in init])),
+                n_iter_max=1, tol=0, return_errors=True, precision="bf16", refine_sweeps=1)
+        finally:
+            lib.tlgb_set_tuning(b"refine_simt", 0)
+        return [f.double().cpu().numpy() for f in cp.factors], errs[-1]
+
+    f_tc, e_tc = one_sweep(0)
+    f_simt, e_simt = one_sweep(1)
+    _, f_o, e_list = oracle.parafac_sweeps(x.astype(np.float64), np.ones(rank),
+                                           [f.astype(np.float64) for f in init], 1)
+    e_o = e_list[-1]
+    for a, b, c in zip(f_tc, f_simt, f_o):
+        scale = np.abs(c).max()
+        assert np.abs(a - c).max() <= 2e-4 * scale
+        assert np.abs(b - c).max() <= 2e-4 * scale
+        # the split path is at least as close to f64 as the SIMT f32 path (x4 slack)
+        assert np.abs(a - c).max() <= 4 * np.abs(b - c).max() + 1e-6 * scale
+    assert abs(e_tc - e_o) <= 1e-5 * e_o and abs(e_simt - e_o) <= 1e-5 * e_o
+
+
+def test_parafac_reports_mttkrp_times(gb300):
+    """The per-sweep-kind MTTKRP durations come back for every kind that ran."""
+    rs = np.random.RandomState(3)
+    x = torch.as_tensor(rs.randn(64, 48, 40).astype(np.float32), device="cuda")
+    init = [torch.as_tensor(rs.randn(s, 8).astype(np.float32), device="cuda") for s in x.shape]
+    times = {}
+    gb300.parafac(x, 8, init=gb300.CPTensor((None, init)), n_iter_max=6, tol=0,
+                  precision="bf16", refine_sweeps=3, mttkrp_times=times)
+    assert set(times) == {"bf16", "f32_split", "closing"}
+    for name, row in times.items():
+        assert len(row) == 3 and all(0 < v < 1000 for v in row), (name, row)
+    native = {}
+    gb300.parafac(x, 8, init=gb300.CPTensor((None, init)), n_iter_max=2, tol=0,
+                  mttkrp_times=native, use_graph=False)
+    assert set(native) == {"native"} and all(v > 0 for v in native["native"])
