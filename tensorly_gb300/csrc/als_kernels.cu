@@ -127,35 +127,64 @@ __global__ void k_gram_partial(const T* __restrict__ A, int64_t I, int R, int64_
   }
 }
 
-// G[e] = sum_p gpart[p][e].  Block b owns 32 consecutive entries (one per
-// lane, coalesced); its 8 warps take every 8th partial with four loads in
-// flight each, then the warps' sums are combined in a fixed order.
-__global__ void __launch_bounds__(256)
-k_gram_reduce(const double* __restrict__ gpart, int nparts, int R, double* G, const int* done) {
-  if (done && *done) return;
+// G[e] = sum_p gpart[p][e] over the lower triangle, mirrored into the upper
+// one.  Block b owns 32 consecutive row-major entries (one per lane) and
+// reduces those on or below the diagonal, so every load is coalesced; its 8
+// warps take every 8th partial, then the warps' sums are combined in a fixed
+// order.  df: the partials are (hi, lo) f32 planes, summed on the f32 pipe
+// (Neumaier for hi, plain for lo) with one conversion at the end.
+// Returns the reduced entry in warp 0's lanes that own one (0 elsewhere).
+__device__ __forceinline__ double gram_reduce_block(const double* __restrict__ gpart, int nparts,
+                                                   int R, double* G, int df) {
   __shared__ double red[8][33];
   const int RR = R * R;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int e = blockIdx.x * 32 + lane;
-  // the partials hold the lower triangle: entry (r, s) with s > r reads (s, r)
   const int r = e / R, s = e - (e / R) * R;
-  const int src = (s > r) ? s * R + r : e;
-  double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  if (e < RR) {
-    int p = warp;
-    for (; p + 56 < nparts; p += 64)
+  const bool mine = e < RR && s <= r;
+  double part = 0.0;
+  if (df) {
+    float h = 0.f, c = 0.f, l = 0.f;
+    if (mine) {
+      const float* gp = reinterpret_cast<const float*>(gpart);
+#pragma unroll 4
+      for (int p = warp; p < nparts; p += 8) {
+        const float v = gp[(int64_t)p * 2 * RR + e];
+        l += gp[(int64_t)p * 2 * RR + RR + e];
+        const float t = h + v;
+        c += (fabsf(h) >= fabsf(v)) ? ((h - t) + v) : ((v - t) + h);
+        h = t;
+      }
+    }
+    part = (double)h + (double)(c + l);
+  } else {
+    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (mine) {
+      int p = warp;
+      for (; p + 56 < nparts; p += 64)
 #pragma unroll
-      for (int u = 0; u < 8; ++u) acc[u] += gpart[(int64_t)(p + 8 * u) * RR + src];
-    for (; p < nparts; p += 8) acc[0] += gpart[(int64_t)p * RR + src];
+        for (int u = 0; u < 8; ++u) acc[u] += gpart[(int64_t)(p + 8 * u) * RR + e];
+      for (; p < nparts; p += 8) acc[0] += gpart[(int64_t)p * RR + e];
+    }
+    part = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7]));
   }
-  red[warp][lane] = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7]));
+  red[warp][lane] = part;
   __syncthreads();
-  if (warp == 0 && e < RR) {
-    double t = 0.0;
+  double t = 0.0;
+  if (warp == 0 && mine) {
 #pragma unroll
     for (int w = 0; w < 8; ++w) t += red[w][lane];
     G[e] = t;
+    if (s < r) G[s * R + r] = t;
   }
+  return t;
+}
+
+__global__ void __launch_bounds__(256)
+k_gram_reduce(const double* __restrict__ gpart, int nparts, int R, double* G, const int* done,
+              int df) {
+  if (done && *done) return;
+  gram_reduce_block(gpart, nparts, R, G, df);
 }
 
 // ---------------------------------------------------------------- factorisation
@@ -231,6 +260,9 @@ k_factorize_fast(const double* __restrict__ G, int ndim, int mode, int R,
           gv = (wsh[i] * gv) * wsh[j];
           vmat[i * R + j] = gv;
           val = (float)gv;
+          // f32 (hi, lo) planes of V after W in w32, for the double-float solve
+          w32[R * R + i * R + j] = val;
+          w32[2 * R * R + i * R + j] = (float)(gv - (double)val);
         }
         a[u0 + u][v] = val;
       }
@@ -444,6 +476,35 @@ __device__ __forceinline__ void gram_update(double* gacc, const double* rows, in
   }
 }
 
+// Double-float variant for f32 factor values: g = (gh, gl) f32 pairs; each
+// product a*b is split exactly (p + fma(a, b, -p)) and added with a Neumaier
+// step, so the block's Gram is accurate to ~2^-48 without the f64 pipe.
+__device__ __forceinline__ void gram_update_df(float* g, const float* rows, int nrows, int R) {
+  const int RR = R * R;
+  float* gh = g;
+  float* gl = g + RR;
+  int e = threadIdx.x;
+  int r = e / R, s = e - (e / R) * R;
+  const int dr = blockDim.x / R, ds = blockDim.x - dr * R;
+  for (; e < RR; e += blockDim.x) {
+    if (s <= r) {
+      float h = gh[e], l = gl[e];
+      for (int w = 0; w < nrows; ++w) {
+        const float a = rows[w * R + r], b = rows[w * R + s];
+        const float p = a * b;
+        const float t = h + p;
+        l += ((fabsf(h) >= fabsf(p)) ? ((h - t) + p) : ((p - t) + h)) + fmaf(a, b, -p);
+        h = t;
+      }
+      gh[e] = h;
+      gl[e] = l;
+    }
+    r += dr;
+    s += ds;
+    if (s >= R) { s -= R; ++r; }
+  }
+}
+
 // Sum of the MTTKRP split partials of one entry.  f32 partials: compensated
 // f32 summation (Neumaier), whose error (~splits * 2^-48) is far below the
 // partials' own rounding, on the f32 pipe (the f64 pipe is ~70x slower here).
@@ -451,6 +512,19 @@ __device__ __forceinline__ double sum_splits(const float* __restrict__ partial, 
                                              int64_t stride, int64_t off) {
   float s = 0.f, c = 0.f;
   int p = 0;
+  // twelve loads in flight per batch: the partials come from L2 and a batch
+  // costs one round trip
+  for (; p + 11 < splits; p += 12) {
+    float v[12];
+#pragma unroll
+    for (int u = 0; u < 12; ++u) v[u] = partial[(int64_t)(p + u) * stride + off];
+#pragma unroll
+    for (int u = 0; u < 12; ++u) {
+      const float t = s + v[u];
+      c += (fabsf(s) >= fabsf(v[u])) ? ((s - t) + v[u]) : ((v[u] - t) + s);
+      s = t;
+    }
+  }
   for (; p + 3 < splits; p += 4) {
     float v[4];
 #pragma unroll
@@ -515,22 +589,60 @@ k_solve(const T* __restrict__ partial, int splits, int64_t I, int R,
   const int64_t IR = I * R;
   double ip = 0.0;
 
+  // f32 tensors with V in shared memory: the residual and the Gram run in
+  // double-float arithmetic on the f32 pipe (exact products by FMA, Neumaier
+  // sums; ~2^-48 relative), since this GPU's f64 pipe is ~70x slower.  The
+  // block's Gram is then kept as f32 (hi, lo) pairs.
+  const bool df = (sizeof(T) == 4) && mats_in_smem;
   if (kind == 2) {
     // ------------------------------------------------ refinement path
     const int RB = max(1, kSolveThreads / R);   // rows per round
+    const int RBR = RB * R;
     double* mb = gacc + RR;                     // [RB][R] right-hand sides
-    double* xb = mb + RB * R;                   // [RB][R] solution
-    double* rb = xb + RB * R;                   // [RB][R] residual, then stored values
-    float* mbf = reinterpret_cast<float*>(rb + RB * R);   // [RB][R] f32 copy of m
-    float* rbf = mbf + RB * R;                              // [RB][R] f32 copy of r
+    double* xb = mb + RBR;                      // [RB][R] solution
+    double* rb = xb + RBR;                      // [RB][R] residual, then stored values
+    float* mbf = reinterpret_cast<float*>(rb + RBR);   // [RB][R] f32 copy of m
+    float* rbf = mbf + RBR;                              // [RB][R] f32 copy of r
+    float* xbh = rbf + RBR;                              // [RB][R] x = xbh + xbl (df)
+    float* xbl = xbh + RBR;
+    float* gbf = xbl + RBR;                              // [RB][R] stored values, f32 (df)
     const double* Vm = vmat;
     const float* Wm = w32;
+    const float* VmH = nullptr;                          // V = VmH + VmL (df)
+    const float* VmL = nullptr;
     if (mats_in_smem) {
-      double* Vs = rb + 2 * RB * R;
-      float* Ws = reinterpret_cast<float*>(Vs + RR);
-      for (int e = tid; e < RR; e += blockDim.x) { Vs[e] = vmat[e]; Ws[e] = w32[e]; }
-      Vm = Vs;
-      Wm = Ws;
+      double* Vs = rb + RBR + ((5 * RBR + 3) / 4) * 2;   // 16-byte aligned
+      if (df) {
+        // [W | V hi | V lo] as written by the factorisation, copied with
+        // 16-byte loads that are all issued before the first store
+        float* Ws = reinterpret_cast<float*>(Vs);
+        const int n = 3 * RR;
+        const int n4 = ((reinterpret_cast<uintptr_t>(w32) & 15) == 0) ? n / 4 : 0;
+        const float4* src = reinterpret_cast<const float4*>(w32);
+        float4* dst = reinterpret_cast<float4*>(Ws);
+        int e = tid;
+        for (; e + 3 * (int)blockDim.x < n4; e += 4 * blockDim.x) {
+          float4 v[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) v[u] = src[e + u * blockDim.x];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) dst[e + u * blockDim.x] = v[u];
+        }
+        for (; e < n4; e += blockDim.x) dst[e] = src[e];
+        for (int f = 4 * n4 + tid; f < n; f += blockDim.x) Ws[f] = w32[f];
+        VmH = Ws + RR;
+        VmL = Ws + 2 * RR;
+        Wm = Ws;
+      } else {
+        float* Ws = reinterpret_cast<float*>(Vs + RR);
+        for (int e = tid; e < RR; e += blockDim.x) { Vs[e] = vmat[e]; Ws[e] = w32[e]; }
+        Vm = Vs;
+        Wm = Ws;
+      }
+    }
+    if (df) {
+      float* gh = reinterpret_cast<float*>(gacc);
+      for (int e = tid; e < 2 * RR; e += blockDim.x) gh[e] = 0.f;
     }
     __syncthreads();
     const int rr = tid / R, c = tid - (tid / R) * R;
@@ -555,12 +667,36 @@ k_solve(const T* __restrict__ partial, int splits, int64_t I, int R,
           a3 = fmaf(m[k + 3], Wm[(k + 3) * R + c], a3);
         }
         for (; k < R; ++k) a0 = fmaf(m[k], Wm[k * R + c], a0);
-        xb[rr * R + c] = (double)((a0 + a1) + (a2 + a3));
+        const float x0 = (a0 + a1) + (a2 + a3);
+        xb[rr * R + c] = (double)x0;
+        if (df) { xbh[rr * R + c] = x0; xbl[rr * R + c] = 0.f; }
       }
       __syncthreads();
       for (int pass = 0; pass < max_passes; ++pass) {
         if (tid == 0) { s_dmax = 0ull; s_xmax = 0ull; }
-        if (act) {   // r = m - x V (f64, eight chains)
+        if (act && df) {   // r = m - x V in double-float (four Neumaier chains)
+          const float* xh = xbh + rr * R;
+          const float* xl = xbl + rr * R;
+          float s[4] = {0.f, 0.f, 0.f, 0.f}, cp[4] = {0.f, 0.f, 0.f, 0.f};
+          float low = 0.f;   // exact product errors and the cross terms
+          for (int k = 0; k < R; k += 4) {   // R <= 96 here; tail guarded per term
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              if (k + u < R) {
+                const float a = xh[k + u], al = xl[k + u];
+                const float b = VmH[(k + u) * R + c], bl = VmL[(k + u) * R + c];
+                const float p = a * b;
+                low += fmaf(a, b, -p) + fmaf(a, bl, al * b);
+                const float t = s[u] + p;
+                cp[u] += (fabsf(s[u]) >= fabsf(p)) ? ((s[u] - t) + p) : ((p - t) + s[u]);
+                s[u] = t;
+              }
+            }
+          }
+          const double vx = (((double)s[0] + (double)s[1]) + ((double)s[2] + (double)s[3])) +
+                            (double)(((cp[0] + cp[1]) + (cp[2] + cp[3])) + low);
+          rbf[rr * R + c] = (float)(mb[rr * R + c] - vx);
+        } else if (act) {   // r = m - x V (f64, eight chains)
           const double* x = xb + rr * R;
           double q[8] = {0, 0, 0, 0, 0, 0, 0, 0};
           int k = 0;
@@ -586,6 +722,11 @@ k_solve(const T* __restrict__ partial, int splits, int64_t I, int R,
           const double d = (double)((a0 + a1) + (a2 + a3));
           const double xn = xb[rr * R + c] + d;
           xb[rr * R + c] = xn;
+          if (df) {
+            const float h = (float)xn;
+            xbh[rr * R + c] = h;
+            xbl[rr * R + c] = (float)(xn - (double)h);
+          }
           if (live) {  // non-negative doubles order like their bit patterns
             atomicMax(&s_dmax, (unsigned long long)__double_as_longlong(fabs(d)));
             atomicMax(&s_xmax, (unsigned long long)__double_as_longlong(fabs(xn)));
@@ -600,11 +741,14 @@ k_solve(const T* __restrict__ partial, int splits, int64_t I, int R,
       if (live) {
         const double xd = store_entry(A, A_bt, I, R, row, c, xb[rr * R + c], rb + rr * R);
         ip = fma(mb[rr * R + c], xd, ip);
+        if (df) gbf[rr * R + c] = (float)xd;   // exact: xd is an f32 value
       } else if (act) {
         rb[rr * R + c] = 0.0;
+        if (df) gbf[rr * R + c] = 0.f;
       }
       __syncthreads();
-      gram_update(gacc, rb, RB, R);   // Gram of the stored rows
+      if (df) gram_update_df(reinterpret_cast<float*>(gacc), gbf, RB, R);
+      else gram_update(gacc, rb, RB, R);   // Gram of the stored rows
       __syncthreads();
     }
   } else {
@@ -684,9 +828,27 @@ k_solve(const T* __restrict__ partial, int splits, int64_t I, int R,
   }
   ip = warp_sum(ip);
   if (lane == 0) s_ip[warp] = ip;
-  // lower triangle only (the upper one is not accumulated); the reducer mirrors
+  // lower triangle only (the upper one is not accumulated); the reducer mirrors.
+  // With df the partial is written as (hi, lo) f32 planes into the same slot
+  // (the substitution path splits its f64 sums), which the reducer sums on
+  // the f32 pipe.
   double* out = gpart + (int64_t)blockIdx.x * RR;
-  for (int e = tid; e < RR; e += blockDim.x) out[e] = gacc[e];
+  if (df) {
+    float* o = reinterpret_cast<float*>(out);
+    if (kind == 2) {
+      const float* g = reinterpret_cast<const float*>(gacc);
+      for (int e = tid; e < 2 * RR; e += blockDim.x) o[e] = g[e];
+    } else {
+      for (int e = tid; e < RR; e += blockDim.x) {
+        const double g = gacc[e];
+        const float h = (float)g;
+        o[e] = h;
+        o[RR + e] = (float)(g - (double)h);
+      }
+    }
+  } else {
+    for (int e = tid; e < RR; e += blockDim.x) out[e] = gacc[e];
+  }
   __syncthreads();
   if (ipart && tid == 0) {
     double t = 0.0;
@@ -737,6 +899,63 @@ __global__ void k_fit(const double* G, int ndim, int R, const T* w, const double
   for (int i = threadIdx.x; i < nip; i += blockDim.x) ip += ipart[i];
   ip = block_sum(ip, scratch);
   if (threadIdx.x == 0) {
+    const double nx2 = ctrl->norm_x2;
+    const double err = sqrt(fabs(nx2 + c - 2.0 * ip)) / sqrt(nx2);
+    const int it = ctrl->iter;
+    if (it < n_iter_max) errors[it] = err;
+    if (tol > 0.0 && it >= 1) {
+      const double dec = errors[it - 1] - err;
+      const bool stop = (crit == 0) ? (fabs(dec) < tol) : (dec < tol);
+      if (stop) ctrl->done = 1;
+    }
+    ctrl->iter = it + 1;
+  }
+}
+
+// The last mode's Gram reduction fused with the fit.  Every block reduces its
+// 32 Gram entries and adds their terms of cp_norm^2 = sum_e prod_k G_k[e]
+// w_r w_s (an entry below the diagonal counts twice, for its mirror) into
+// fpart[block]; the block that finishes last (a device-scope counter in the
+// control block, which it resets) sums fpart and the <M, A> partials in a
+// fixed order and records the error.  Deterministic whichever block is last.
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_gram_reduce_fit(const double* __restrict__ gpart, int nparts, int R, double* G_all, int mode,
+                  int ndim, int df, const T* w, const double* ipart, int nip, double* fpart,
+                  AlsCtrl* ctrl, double* errors, int n_iter_max, double tol, int crit) {
+  if (ctrl->done) return;
+  const int RR = R * R;
+  const double t = gram_reduce_block(gpart, nparts, R, G_all + (int64_t)mode * RR, df);
+  __shared__ int s_last;
+  __shared__ double scratch[32];
+  if (threadIdx.x < 32) {
+    const int e = blockIdx.x * 32 + threadIdx.x;
+    const int r = e / R, s = e - (e / R) * R;
+    double v = 0.0;
+    if (e < RR && s <= r) {
+      v = t;
+      for (int k = 0; k < ndim; ++k)
+        if (k != mode) v = v * G_all[(int64_t)k * RR + e];
+      if (w) v = v * ((double)w[r] * (double)w[s]);
+      if (s < r) v = 2.0 * v;
+    }
+    v = warp_sum(v);
+    if (threadIdx.x == 0) fpart[blockIdx.x] = v;
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = (atomicAdd(&ctrl->red_count, 1) == (int)gridDim.x - 1) ? 1 : 0;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  double acc = 0.0;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) acc += __ldcg(&fpart[b]);
+  const double c = block_sum(acc, scratch);
+  double ip = 0.0;
+  for (int i = threadIdx.x; i < nip; i += blockDim.x) ip += ipart[i];
+  ip = block_sum(ip, scratch);
+  if (threadIdx.x == 0) {
+    ctrl->red_count = 0;
     const double nx2 = ctrl->norm_x2;
     const double err = sqrt(fabs(nx2 + c - 2.0 * ip)) / sqrt(nx2);
     const int it = ctrl->iter;
@@ -882,13 +1101,13 @@ int als_launch_gram(const T* A, int64_t I, int R, double* gpart, int nparts_max,
   }
   k_gram_partial<T><<<nparts, threads, smem, st>>>(A, I, R, rpb, gpart, done);
   TLGB_LAUNCH_CHECK();
-  return als_launch_gram_reduce(gpart, nparts, R, G, done, st);
+  return als_launch_gram_reduce(gpart, nparts, R, G, done, 0, st);
 }
 
 int als_launch_gram_reduce(const double* gpart, int nparts, int R, double* G, const int* done,
-                           cudaStream_t st) {
+                           int df, cudaStream_t st) {
   const int RR = R * R;
-  k_gram_reduce<<<(int)ceil_div(RR, 32), 256, 0, st>>>(gpart, nparts, R, G, done);
+  k_gram_reduce<<<(int)ceil_div(RR, 32), 256, 0, st>>>(gpart, nparts, R, G, done, df);
   TLGB_LAUNCH_CHECK();
   return TLGB_OK;
 }
@@ -923,9 +1142,10 @@ int als_launch_factorize(const double* G, int ndim, int mode, int R, const T* we
 // Dynamic shared memory of k_solve for rank R (largest of its two paths).
 static size_t solve_smem(int R) {
   const size_t RR = (size_t)R * R;
-  const bool mats = R <= 96;
+  const bool mats = R <= kSolveDfMaxRank;
   const size_t rb = (size_t)std::max(1, kSolveThreads / R) * R;
-  const size_t ir = RR + 4 * rb + (mats ? RR + (RR + 1) / 2 : 0);
+  // gacc, mb, xb, rb (f64) + five f32 arrays + V (f64, or two f32 planes) and W (f32)
+  const size_t ir = RR + 3 * rb + ((5 * rb + 3) / 4) * 2 + (mats ? RR + (RR + 1) / 2 : 0);
   const size_t direct = RR + (size_t)kSolveWarps * R + (mats ? RR + R : 0);
   return std::max(ir, direct) * sizeof(double);
 }
@@ -942,7 +1162,8 @@ int als_launch_solve(const T* partial, int splits, int64_t I, int R, const doubl
   if (rc) return rc;
   k_solve<T><<<nbe, kSolveThreads, solve_smem(R), st>>>(partial, splits, I, R, fac, perm, vmat,
                                                         w32, A, A_bt, gpart, ipart, ctrl, rpb,
-                                                        R <= 96 ? 1 : 0, max_passes);
+                                                        R <= kSolveDfMaxRank ? 1 : 0,
+                                                        max_passes);
   TLGB_LAUNCH_CHECK();
   *nblocks = nbe;
   return TLGB_OK;
@@ -954,6 +1175,19 @@ int als_launch_fit(const double* G, int ndim, int R, const T* weights, const dou
                    int cvg_criterion, cudaStream_t st) {
   k_fit<T><<<1, 512, 0, st>>>(G, ndim, R, weights, ipart, nip, ctrl, errors, n_iter_max, tol,
                               cvg_criterion);
+  TLGB_LAUNCH_CHECK();
+  return TLGB_OK;
+}
+
+template <typename T>
+int als_launch_gram_reduce_fit(const double* gpart, int nparts, int R, double* G_all, int mode,
+                               int ndim, int df, const T* weights, const double* ipart, int nip,
+                               double* fpart, AlsCtrl* ctrl, double* errors, int n_iter_max,
+                               double tol, int cvg_criterion, cudaStream_t st) {
+  const int RR = R * R;
+  k_gram_reduce_fit<T><<<(int)ceil_div(RR, 32), 256, 0, st>>>(
+      gpart, nparts, R, G_all, mode, ndim, df, weights, ipart, nip, fpart, ctrl, errors,
+      n_iter_max, tol, cvg_criterion);
   TLGB_LAUNCH_CHECK();
   return TLGB_OK;
 }
@@ -1047,6 +1281,9 @@ int als_prepare(int dtype) {
                                    double*, AlsCtrl*, int, int*, cudaStream_t);              \
   template int als_launch_fit<T>(const double*, int, int, const T*, const double*, int,      \
                                  AlsCtrl*, double*, int, double, int, cudaStream_t);         \
+  template int als_launch_gram_reduce_fit<T>(const double*, int, int, double*, int, int, int,  \
+                                             const T*, const double*, int, double*, AlsCtrl*, \
+                                             double*, int, double, int, cudaStream_t);       \
   template int als_launch_normalize<T>(T* const*, const int64_t*, int, int, T*, const int*,  \
                                        cudaStream_t);
 TLGB_INST(float)

@@ -12,7 +12,7 @@ struct AlsCtrl {
   int fac_kind;  // 0: Cholesky factor, 1: LU factors with row permutation
   double norm_x2;
   int tc_err;    // TLGB_ETIMEOUT if a tensor-core pipeline wait expired
-  int pad;
+  int red_count; // blocks of the fused Gram reduction + fit that finished (reset by the last)
 };
 
 constexpr int kMaxAlsRank = 160;     // f64 factorisation held in one CTA's shared memory
@@ -29,7 +29,8 @@ int als_launch_gram(const T* A, int64_t I, int R, double* gpart, int nparts_max,
 // refinement path; fac/perm the f64 Cholesky or LU fallback.
 template <typename T>
 int als_launch_factorize(const double* G, int ndim, int mode, int R, const T* weights,
-                         double l2_reg, double* fac, int* perm, double* vmat, float* w32,
+                         double l2_reg, double* fac, int* perm, double* vmat,
+                         float* w32 /* 3 R^2: W, then V's f32 hi and lo planes */,
                          AlsCtrl* ctrl, cudaStream_t st);
 
 // Sums the MTTKRP partials of each row, solves with the factorisation, stores
@@ -45,13 +46,25 @@ int als_launch_solve(const T* partial, int splits, int64_t I, int R, const doubl
 
 constexpr int kIrMaxPasses = 4;
 
+// df: the partials are (hi, lo) f32 planes (written by k_solve for f32 factors
+// with rank <= kSolveDfMaxRank), else f64.
 int als_launch_gram_reduce(const double* gpart, int nparts, int R, double* G, const int* done,
-                           cudaStream_t st);
+                           int df, cudaStream_t st);
+constexpr int kSolveDfMaxRank = 96;
 
 template <typename T>
 int als_launch_fit(const double* G, int ndim, int R, const T* weights, const double* ipart,
                    int nip, AlsCtrl* ctrl, double* errors, int n_iter_max, double tol,
                    int cvg_criterion, cudaStream_t st);
+
+// Gram reduction of `mode` (into G_all + mode * R^2) fused with the fit of
+// als_launch_fit: one launch instead of two at the end of a sweep.  fpart:
+// scratch of ceil(R^2 / 32) doubles.
+template <typename T>
+int als_launch_gram_reduce_fit(const double* gpart, int nparts, int R, double* G_all, int mode,
+                               int ndim, int df, const T* weights, const double* ipart, int nip,
+                               double* fpart, AlsCtrl* ctrl, double* errors, int n_iter_max,
+                               double tol, int cvg_criterion, cudaStream_t st);
 
 template <typename T>
 int als_launch_normalize(T* const* factors, const int64_t* rows, int ndim, int R, T* weights,

@@ -35,6 +35,7 @@ struct AlsBuffers {
   __nv_bfloat16* fbt[kMaxModes];        // bf16 split transposed factors (3 x rank x rows)
   void* tc_partial;
   double* probe;                        // one f64 result slot (initial error)
+  double* fpart;                        // per-block cp_norm^2 terms of the fused fit
   size_t bytes;
 };
 
@@ -65,7 +66,7 @@ int layout(int dtype, const Shape& sh, int64_t R, const tlgb_cp_als_options& o,
   B->fac = c.take<double>((size_t)RR + R);
   B->perm = c.take<int>(R);
   B->vmat = c.take<double>((size_t)RR);
-  B->w32 = c.take<float>((size_t)RR);
+  B->w32 = c.take<float>((size_t)3 * RR);   // W = V^-1 (f32), then V's f32 hi and lo planes
   size_t pmax = 0;
   int64_t imax = 0;
   for (int k = 0; k < sh.ndim; ++k) {
@@ -78,6 +79,7 @@ int layout(int dtype, const Shape& sh, int64_t R, const tlgb_cp_als_options& o,
   B->ipart = c.take<double>(nparts);
   B->sumsq_part = c.take<double>(kSumsqBlocks);
   B->probe = c.take<double>(1);
+  B->fpart = c.take<double>((size_t)ceil_div(RR, 32));
   B->xbf = nullptr;
   B->xsplit[0] = B->xsplit[1] = nullptr;
   for (int k = 0; k < kMaxModes; ++k) B->fbt[k] = nullptr;
@@ -249,12 +251,17 @@ struct Runner {
                                (tc && P->tc[mode].valid) ? 1 : kIrMaxPasses, &nb, st);
       if (rc) return rc;
       if (last) last_nb = nb;
-      rc = als_launch_gram_reduce(B.gpart, nb, (int)R, B.G + (size_t)mode * RR, done, st);
+      const int df = (sizeof(T) == 4 && R <= kSolveDfMaxRank) ? 1 : 0;
+      if (last)   // the last mode's Gram reduction also computes the fit
+        rc = als_launch_gram_reduce_fit<T>(B.gpart, nb, (int)R, B.G, mode, N, df, weights,
+                                           B.ipart, nb, B.fpart, B.ctrl, B.errors, o.n_iter_max,
+                                           o.tol,
+                                           o.cvg_criterion, st);
+      else
+        rc = als_launch_gram_reduce(B.gpart, nb, (int)R, B.G + (size_t)mode * RR, done, df, st);
       if (rc) return rc;
     }
-    int rc = als_launch_fit<T>(B.G, N, (int)R, weights, B.ipart, last_nb, B.ctrl, B.errors,
-                               o.n_iter_max, o.tol, o.cvg_criterion, st);
-    if (rc) return rc;
+    int rc = TLGB_OK;
     if (o.normalize_factors) {
       rc = als_launch_normalize<T>(factors, sh.dim, N, (int)R, weights, done, st);
       if (rc) return rc;
