@@ -146,6 +146,47 @@ int tlgb_mode_dot(int dtype, const void* X, int ndim, const int64_t* shape, cons
                   int64_t J, int transpose, int mode, void* out, void* stream);
 
 /*
+ * The k largest eigenpairs of a symmetric n x n matrix A (row-major, both
+ * triangles), eigenvalues descending in `evals` (k), eigenvectors as the
+ * columns of U (n x k, row-major).  With flip_sign != 0 every column's
+ * largest-magnitude entry (first one on ties) is made positive, the sign rule
+ * of tensorly/tenalg/svd.py:13-65 (svd_flip, u_based_decision).  One CTA:
+ * Householder tridiagonalisation, multisection, inverse iteration.
+ * dtype TLGB_F64 (n <= 160) or TLGB_F32 (n <= 224), else TLGB_EUNSUPPORTED.
+ * Stands in for the LAPACK eigen/SVD drivers behind
+ * tensorly/tenalg/svd.py:211-235 (truncated_svd).
+ */
+int tlgb_sym_eig_workspace_size(int dtype, int64_t n, int64_t k, size_t* bytes);
+int tlgb_sym_eig(int dtype, const void* A, int64_t n, int64_t k, void* U, void* evals,
+                 int flip_sign, void* workspace, size_t workspace_bytes, void* stream);
+
+/*
+ * Gram matrix of the mode-`mode` unfolding M = unfold(X, mode) without
+ * forming it: side 0 -> G = M M^T (shape[mode] x shape[mode]), side 1 ->
+ * G = M^T M (J x J, J = numel / shape[mode]).  f32 tensors: compensated f32
+ * sums with an f64 split reduction; f64 tensors: f64.  Deterministic.
+ * No direct counterpart in TensorLy (it is the first half of the SVD below).
+ */
+int tlgb_gram_unfolding_workspace_size(int ndim, const int64_t* shape, int mode, int side,
+                                       size_t* bytes);
+int tlgb_gram_unfolding(int dtype, const void* X, int ndim, const int64_t* shape, int mode,
+                        int side, void* G, void* workspace, size_t workspace_bytes, void* stream);
+
+/*
+ * svd_interface(unfold(X, mode), n_eigenvecs=k) for method 'truncated_svd'
+ * (tensorly/tenalg/svd.py:366-447, :211-235): the leading k left singular
+ * vectors U (shape[mode] x k, row-major) and singular values S (k,
+ * descending) of the unfolding, from the eigenpairs of its smaller Gram
+ * matrix; flip_sign applies svd_flip to U.  Requires k <= min(shape[mode], J)
+ * and that order of the Gram matrix within tlgb_sym_eig's limit.
+ */
+int tlgb_svd_unfolding_workspace_size(int dtype, int ndim, const int64_t* shape, int mode,
+                                      int64_t k, size_t* bytes);
+int tlgb_svd_unfolding(int dtype, const void* X, int ndim, const int64_t* shape, int mode,
+                       int64_t k, void* U, void* S, int flip_sign, void* workspace,
+                       size_t workspace_bytes, void* stream);
+
+/*
  * Dense CP-ALS (the sweep loop of tensorly/decomposition/_cp.py:394-530,
  * parafac).  On entry factors[k] (shape[k] x rank, tensor dtype) and weights
  * (rank) hold the initial CP tensor; on exit the result.  Per sweep and mode:
@@ -193,6 +234,36 @@ int tlgb_cp_als(int dtype, const void* X, int ndim, const int64_t* shape, int64_
                 void* const* factors, void* weights, const tlgb_cp_als_options* opts,
                 double* errors, int* n_errors, void* workspace, size_t workspace_bytes,
                 void* stream);
+
+/*
+ * Tucker decomposition by HOOI: the loop of
+ * tensorly/decomposition/_tucker.py:105-221 (partial_tucker) after
+ * initialize_tucker (:25-102).  modes[i] (n_modes ascending modes, NULL =
+ * 0..n_modes-1) is decomposed with rank ranks[i]; factors[i]
+ * (shape[modes[i]] x ranks[i], tensor dtype) receives the factor (and holds
+ * the initial one on entry when init_svd == 0); core receives the core
+ * (shape with modes[i] replaced by ranks[i]).  Per iteration and mode: the
+ * factors of the other modes applied transposed (ascending mode order, the
+ * skipped position counted in that order as the reference does), then the
+ * leading ranks[i] left singular vectors of that unfolding (svd_flip signs);
+ * the error is sqrt(|norm(X)^2 - norm(core)^2|) / norm(X) and the run stops
+ * after iteration index > 1 when it changed by less than tol.  errors (host,
+ * n_iter_max) and *n_errors receive the errors.  Returns after the GPU
+ * finished.  Each unfolding's Gram matrix must be within tlgb_sym_eig's size.
+ */
+typedef struct tlgb_tucker_options {
+  int n_iter_max;   /* partial_tucker n_iter_max */
+  double tol;       /* partial_tucker tol (0 disables the stop test) */
+  int init_svd;     /* 1: factors from the SVD of the unfoldings of X ('svd') */
+} tlgb_tucker_options;
+
+void tlgb_tucker_default_options(tlgb_tucker_options* opts);
+int tlgb_tucker_workspace_size(int dtype, int ndim, const int64_t* shape, int n_modes,
+                               const int* modes, const int64_t* ranks, size_t* bytes);
+int tlgb_tucker_hooi(int dtype, const void* X, int ndim, const int64_t* shape, int n_modes,
+                     const int* modes, const int64_t* ranks, void* const* factors, void* core,
+                     const tlgb_tucker_options* opts, double* errors, int* n_errors,
+                     void* workspace, size_t workspace_bytes, void* stream);
 
 /*
  * cp_normalize: unit-norm factor columns, norms multiplied into weights

@@ -51,6 +51,15 @@ class CpAlsOptions(ctypes.Structure):
     ]
 
 
+class TuckerOptions(ctypes.Structure):
+    """Mirror of ``tlgb_tucker_options``."""
+    _fields_ = [
+        ("n_iter_max", ctypes.c_int),
+        ("tol", ctypes.c_double),
+        ("init_svd", ctypes.c_int),
+    ]
+
+
 CP_ALS_SWEEP_KINDS = 4
 SWEEP_KIND_NAMES = ("native", "bf16", "f32_split", "closing")
 
@@ -83,6 +92,32 @@ SIGNATURES = [
     ("tlgb_mode_dot", ctypes.c_int,
      [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, _c_i64p, ctypes.c_void_p, ctypes.c_int64,
       ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),
+    ("tlgb_sym_eig_workspace_size", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_int64, ctypes.c_int64, ctypes.POINTER(ctypes.c_size_t)]),
+    ("tlgb_sym_eig", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p,
+      ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    ("tlgb_gram_unfolding_workspace_size", ctypes.c_int,
+     [ctypes.c_int, _c_i64p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_size_t)]),
+    ("tlgb_gram_unfolding", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, _c_i64p, ctypes.c_int, ctypes.c_int,
+      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    ("tlgb_svd_unfolding_workspace_size", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_int, _c_i64p, ctypes.c_int, ctypes.c_int64,
+      ctypes.POINTER(ctypes.c_size_t)]),
+    ("tlgb_svd_unfolding", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, _c_i64p, ctypes.c_int, ctypes.c_int64,
+      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t,
+      ctypes.c_void_p]),
+    ("tlgb_tucker_default_options", None, [ctypes.POINTER(TuckerOptions)]),
+    ("tlgb_tucker_workspace_size", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_int, _c_i64p, ctypes.c_int, ctypes.POINTER(ctypes.c_int), _c_i64p,
+      ctypes.POINTER(ctypes.c_size_t)]),
+    ("tlgb_tucker_hooi", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, _c_i64p, ctypes.c_int,
+      ctypes.POINTER(ctypes.c_int), _c_i64p, _c_vpp, ctypes.c_void_p,
+      ctypes.POINTER(TuckerOptions), ctypes.POINTER(ctypes.c_double),
+      ctypes.POINTER(ctypes.c_int), ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     ("tlgb_cp_als_default_options", None, [ctypes.POINTER(CpAlsOptions)]),
     ("tlgb_cp_als_workspace_size", ctypes.c_int,
      [ctypes.c_int, ctypes.c_int, _c_i64p, ctypes.c_int64, ctypes.POINTER(CpAlsOptions),

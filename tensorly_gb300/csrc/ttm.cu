@@ -7,7 +7,7 @@
 // contiguous one) and l is the batch; when T == 1 (last mode) M is l and the
 // contraction runs along the contiguous dimension.  SIMT f32 / f64 tiles,
 // 16-byte vector loads along whichever dimension is contiguous.
-#include "common.cuh"
+#include "linalg.cuh"
 
 namespace tlgb {
 namespace {
@@ -234,6 +234,18 @@ int ttm_typed(const T* X, const Shape& sh, const T* U, int64_t J, int transpose,
 }
 
 }  // namespace
+
+template <typename T>
+int ttm_launch(const T* X, const Shape& sh, const T* U, int64_t J, int transpose, int mode, T* Y,
+               cudaStream_t st) {
+  if (sh.numel == 0) return TLGB_OK;
+  return ttm_typed<T>(X, sh, U, J, transpose, mode, Y, st);
+}
+template int ttm_launch<float>(const float*, const Shape&, const float*, int64_t, int, int, float*,
+                               cudaStream_t);
+template int ttm_launch<double>(const double*, const Shape&, const double*, int64_t, int, int,
+                                double*, cudaStream_t);
+
 }  // namespace tlgb
 
 using namespace tlgb;

@@ -265,3 +265,207 @@ class CP(DecompositionMixin):
         self.decomposition_ = cp_tensor
         self.errors_ = errors
         return self.decomposition_
+
+
+# ----------------------------------------------------------------------------
+# Tucker
+# ----------------------------------------------------------------------------
+def initialize_tucker(tensor, rank, modes, random_state, init="svd", svd="truncated_svd",
+                      non_negative=False, mask=None, svd_mask_repeats=5):
+    """Initial core and factors (tensorly/decomposition/_tucker.py:25-102).
+
+    ``'svd'``: the leading left singular vectors of each unfolding from the
+    library (Gram eigensolver, svd_flip signs), core = X x_n U_n^T.
+    ``'random'``: the reference's host draws (core + 0.01), copied once.
+    A (core, factors) pair is used as given.
+    """
+    x, _ = to_device(tensor)
+    if mask is not None:
+        raise NotImplementedError("masked Tucker is not supported by tensorly_gb300")
+    if isinstance(init, str) and init == "svd":
+        from .svd import svd_interface_unfolding
+        from .tenalg import multi_mode_dot
+        factors = []
+        for index, mode in enumerate(modes):
+            U, _ = svd_interface_unfolding(x, mode, n_eigenvecs=rank[index], method=svd,
+                                           non_negative=non_negative)
+            factors.append(U)
+        core = multi_mode_dot(x, factors, modes=modes, transpose=True)
+    elif isinstance(init, str) and init == "random":
+        rng = check_random_state(random_state)
+        core = torch.from_numpy(rng.random_sample([rank[i] for i in range(len(modes))]) + 0.01)
+        core = core.to(x.device, x.dtype)
+        factors = [torch.from_numpy(rng.random_sample((x.shape[mode], rank[i]))).to(x.device,
+                                                                                    x.dtype)
+                   for i, mode in enumerate(modes)]
+    else:
+        core, factors = init
+        core = like(core, x)
+        factors = [like(f, x) for f in factors]
+    if non_negative is True:
+        factors = [f.abs() for f in factors]
+        core = core.abs()
+    return core, list(factors)
+
+
+def _hooi(x, rank, modes, factors, n_iter_max, tol, init_svd):
+    """Runs tlgb_tucker_hooi; returns (core, factors, errors)."""
+    lib = _lib.lib()
+    n_modes = len(modes)
+    for i, (m, f) in enumerate(zip(modes, factors)):
+        if f is not None and tuple(f.shape) != (x.shape[m], int(rank[i])):
+            raise ValueError(f"initial factor {i} has shape {tuple(f.shape)}, expected "
+                             f"{(x.shape[m], int(rank[i]))} (mode {m}, rank {rank[i]})")
+    factors = [f.to(x.dtype).contiguous().clone() if f is not None else
+               torch.empty((x.shape[m], rank[i]), dtype=x.dtype, device=x.device)
+               for i, (m, f) in enumerate(zip(modes, factors))]
+    core_shape = list(x.shape)
+    for i, m in enumerate(modes):
+        core_shape[m] = int(rank[i])
+    core = torch.empty(core_shape, dtype=x.dtype, device=x.device)
+    shape = _lib.i64_array(x.shape)
+    cmodes = (ctypes.c_int * n_modes)(*[int(m) for m in modes])
+    cranks = _lib.i64_array(rank)
+    opts = _lib.TuckerOptions()
+    lib.tlgb_tucker_default_options(ctypes.byref(opts))
+    opts.n_iter_max = int(n_iter_max)
+    opts.tol = float(tol) if tol else 0.0
+    opts.init_svd = 1 if init_svd else 0
+    nbytes = ctypes.c_size_t(0)
+    _lib.check(lib.tlgb_tucker_workspace_size(dtype_code(x), x.ndim, shape, n_modes, cmodes,
+                                              cranks, ctypes.byref(nbytes)))
+    ws = workspace(nbytes.value, x.device)
+    errs = (ctypes.c_double * max(1, int(n_iter_max)))()
+    n_err = ctypes.c_int(0)
+    _lib.check(lib.tlgb_tucker_hooi(dtype_code(x), ptr(x), x.ndim, shape, n_modes, cmodes,
+                                    cranks, _lib.ptr_array([ptr(f) for f in factors]), ptr(core),
+                                    ctypes.byref(opts), errs, ctypes.byref(n_err), ptr(ws),
+                                    ws.numel(), stream_of(x)))
+    return core, factors, [float(errs[i]) for i in range(n_err.value)]
+
+
+def partial_tucker(tensor, rank, modes=None, n_iter_max=100, init="svd", tol=10e-5,
+                   svd="truncated_svd", random_state=None, verbose=False, mask=None,
+                   svd_mask_repeats=5):
+    """Partial Tucker decomposition by HOOI (tensorly/decomposition/_tucker.py:105-221).
+
+    Same signature and return value, ``((core, factors), rec_errors)``; the
+    iteration runs in the library (``tlgb_tucker_hooi``).
+    """
+    if mask is not None:
+        raise NotImplementedError("masked Tucker is not supported by tensorly_gb300")
+    x, pl = to_device(tensor)
+    x = x.contiguous()
+    if modes is None:
+        modes = list(range(x.ndim))
+    if rank is None:
+        warnings.warn("No value given for 'rank'. The decomposition will preserve the original "
+                      "size.", Warning)
+        rank = [x.shape[mode] for mode in modes]
+    elif isinstance(rank, int):
+        warnings.warn(f"Given only one int for 'rank' instead of a list of {len(modes)} modes. "
+                      "Using this rank for all modes.", Warning)
+        rank = tuple(rank for _ in modes)
+    else:
+        rank = tuple(rank)
+    modes = [int(m) for m in modes]
+    if modes != sorted(modes):
+        # the reference applies `skip=index` as a position in the mode-sorted
+        # factor list (core_tenalg/n_mode_product.py:117-124), so unsorted
+        # modes feed it mismatched factors and end in a shape error
+        raise ValueError(f"partial_tucker: modes {modes} are not in ascending order")
+    if isinstance(init, str) and init == "svd" and svd not in ("truncated_svd", "symeig_svd"):
+        raise NotImplementedError(f"svd method {svd!r} is not supported by tensorly_gb300")
+    if isinstance(init, str) and init == "svd":
+        init_factors = [None] * len(modes)
+        core0 = None
+        init_svd = True
+    else:
+        core0, init_factors = initialize_tucker(x, rank, modes, random_state, init=init, svd=svd)
+        init_svd = False
+    if int(n_iter_max) <= 0:
+        if init_svd:
+            core0, init_factors = initialize_tucker(x, rank, modes, random_state, init=init,
+                                                    svd=svd)
+        return (pl.back(core0), [pl.back(f) for f in init_factors]), []
+    core, factors, rec_errors = _hooi(x, rank, modes, init_factors, n_iter_max, tol, init_svd)
+    if verbose:
+        for i in range(2, len(rec_errors)):
+            print(f"reconstruction error={rec_errors[i]}, "
+                  f"variation={rec_errors[i - 1] - rec_errors[i]}.")
+    return (pl.back(core), [pl.back(f) for f in factors]), rec_errors
+
+
+def tucker(tensor, rank, fixed_factors=None, n_iter_max=100, init="svd", return_errors=False,
+           svd="truncated_svd", tol=10e-5, random_state=None, mask=None, verbose=False):
+    """Tucker decomposition by HOOI (tensorly/decomposition/_tucker.py:224-345).
+
+    Same signature and return types: a ``TuckerTensor``, or
+    ``(TuckerTensor, rec_errors)`` with ``return_errors`` (without
+    ``fixed_factors``, as in the reference).
+    """
+    from .tenalg import multi_mode_dot
+    if fixed_factors:
+        try:
+            (core, factors) = init
+        except Exception:
+            raise ValueError(f"Got fixed_factor={fixed_factors} but no appropriate Tucker tensor "
+                             'was passed for "init".')
+        x, pl = to_device(tensor)
+        core = like(core, x)
+        factors = [like(f, x) for f in factors]
+        fixed_factors = sorted(fixed_factors)
+        modes_fixed, factors_fixed = zip(*[(i, f) for (i, f) in enumerate(factors)
+                                           if i in fixed_factors])
+        core = multi_mode_dot(core, list(factors_fixed), modes=list(modes_fixed))
+        modes, factors = zip(*[(i, f) for (i, f) in enumerate(factors)
+                               if i not in fixed_factors])
+        init = (core, list(factors))
+        (core, new_factors), rec_errors = partial_tucker(
+            x, rank=rank, modes=list(modes), n_iter_max=n_iter_max, init=init, svd=svd, tol=tol,
+            random_state=random_state, mask=mask, verbose=verbose)
+        factors = list(new_factors)
+        for i, e in enumerate(fixed_factors):
+            factors.insert(e, factors_fixed[i])
+        core = multi_mode_dot(core, list(factors_fixed), modes=list(modes_fixed),
+                              transpose=True)
+        return TuckerTensor((pl.back(core), [pl.back(f) for f in factors]))
+    x, pl = to_device(tensor)
+    modes = list(range(x.ndim))
+    rank = validate_tucker_rank(tuple(x.shape), rank=rank)
+    (core, factors), rec_errors = partial_tucker(
+        x, rank=rank, modes=modes, n_iter_max=n_iter_max, init=init, svd=svd, tol=tol,
+        random_state=random_state, mask=mask, verbose=verbose)
+    tt = TuckerTensor((pl.back(core), [pl.back(f) for f in factors]))
+    if return_errors:
+        return tt, rec_errors
+    return tt
+
+
+class Tucker(DecompositionMixin):
+    """Estimator wrapper of :func:`tucker` (tensorly/decomposition/_tucker.py:697-797)."""
+
+    def __init__(self, rank=None, n_iter_max=100, init="svd", return_errors=False,
+                 svd="truncated_svd", tol=10e-5, fixed_factors=None, random_state=None,
+                 mask=None, verbose=False):
+        self.rank = rank
+        self.fixed_factors = fixed_factors
+        self.n_iter_max = n_iter_max
+        self.init = init
+        self.return_errors = return_errors
+        self.svd = svd
+        self.tol = tol
+        self.random_state = random_state
+        self.mask = mask
+        self.verbose = verbose
+
+    def fit_transform(self, tensor):
+        tucker_tensor = tucker(
+            tensor, rank=self.rank, fixed_factors=self.fixed_factors, n_iter_max=self.n_iter_max,
+            init=self.init, return_errors=self.return_errors, svd=self.svd, tol=self.tol,
+            random_state=self.random_state, mask=self.mask, verbose=self.verbose)
+        self.decomposition_ = tucker_tensor
+        return self.decomposition_
+
+    def __repr__(self):
+        return f"Rank-{self.rank} Tucker decomposition via HOOI."
