@@ -127,7 +127,10 @@ int tlgb_mttkrp_bf16(const void* X, int ndim, const int64_t* shape, const void* 
  * leaves free (CP-ALS leaves 1 for its concurrent factorisation kernel),
  * "refine_simt" = 1 makes the f32
  * refinement sweeps of TLGB_PREC_BF16 use the SIMT f32 MTTKRP instead of the
- * tensor-core one on the exact three-plane bf16 split of the f32 tensor.
+ * tensor-core one on the exact three-plane bf16 split of the f32 tensor;
+ * "batched_threads_small" / "_medium" / "_large" = threads per CTA (128, 256
+ * or 512; 4, 2 or 1 CTAs per SM) of tlgb_cp_als_batched for the tensors
+ * whose padded size fits 128-, 256-thread CTAs' shared memory, or neither.
  * Process-wide; no counterpart in TensorLy.
  */
 int tlgb_set_tuning(const char* key, int value);
@@ -264,6 +267,34 @@ int tlgb_tucker_hooi(int dtype, const void* X, int ndim, const int64_t* shape, i
                      const int* modes, const int64_t* ranks, void* const* factors, void* core,
                      const tlgb_tucker_options* opts, double* errors, int* n_errors,
                      void* workspace, size_t workspace_bytes, void* stream);
+
+/*
+ * Batched CP-ALS of many small 3-way f32 tensors of uneven shape and rank:
+ * for every item, the sweep loop of tensorly/decomposition/_cp.py:394-440
+ * (parafac with normalize_factors=False, no stop test: exactly n_iter_max
+ * sweeps), weights all one.  items (host array): device pointers to the
+ * tensor (C order) and to the three factors (dims[k] x rank, row-major; the
+ * initial factors on entry, the result on exit).  Mode sizes 1..64, rank
+ * 1..16.  One persistent kernel per `sweeps_per_launch` sweeps (<= 0: all in
+ * one launch); each CTA takes the next tensor from a work queue ordered by
+ * decreasing work and keeps it in shared memory when it fits.
+ * final_errors (device, n_tensors doubles): relative error of the final
+ * model from the residual; sweep_errors (device, n_tensors x n_iter_max, or
+ * NULL): per-sweep errors from the reference's expansion (_cp.py:217-225).
+ * The call returns after the GPU finished.  No direct counterpart in TensorLy
+ * (its users loop over parafac).
+ */
+typedef struct tlgb_batch_item {
+  const void* X;
+  void* factors[3];
+  int64_t dims[3];
+  int64_t rank;
+} tlgb_batch_item;
+
+int tlgb_cp_als_batched_workspace_size(int n_tensors, size_t* bytes);
+int tlgb_cp_als_batched(int n_tensors, const tlgb_batch_item* items, int n_iter_max,
+                        int sweeps_per_launch, double* final_errors, double* sweep_errors,
+                        void* workspace, size_t workspace_bytes, void* stream);
 
 /*
  * cp_normalize: unit-norm factor columns, norms multiplied into weights

@@ -15,7 +15,7 @@ from ._lib import GB300Error, SingularMatrixError, build, lib
 from .cp_tensor import (CPTensor, TuckerTensor, cp_norm, cp_normalize, cp_to_tensor,
                         tucker_to_tensor, validate_cp_rank, validate_tucker_rank)
 from .decomposition import (CP, Tucker, initialize_cp, initialize_tucker, parafac,
-                            partial_tucker, tucker)
+                            parafac_batched, partial_tucker, tucker)
 from .svd import svd_flip, svd_interface, truncated_svd
 from .random import check_random_state, random_cp
 from .tenalg import khatri_rao, mode_dot, multi_mode_dot, unfolding_dot_khatri_rao

@@ -60,6 +60,16 @@ class TuckerOptions(ctypes.Structure):
     ]
 
 
+class BatchItem(ctypes.Structure):
+    """Mirror of ``tlgb_batch_item``."""
+    _fields_ = [
+        ("X", ctypes.c_void_p),
+        ("factors", ctypes.c_void_p * 3),
+        ("dims", ctypes.c_int64 * 3),
+        ("rank", ctypes.c_int64),
+    ]
+
+
 CP_ALS_SWEEP_KINDS = 4
 SWEEP_KIND_NAMES = ("native", "bf16", "f32_split", "closing")
 
@@ -118,6 +128,11 @@ SIGNATURES = [
       ctypes.POINTER(ctypes.c_int), _c_i64p, _c_vpp, ctypes.c_void_p,
       ctypes.POINTER(TuckerOptions), ctypes.POINTER(ctypes.c_double),
       ctypes.POINTER(ctypes.c_int), ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    ("tlgb_cp_als_batched_workspace_size", ctypes.c_int,
+     [ctypes.c_int, ctypes.POINTER(ctypes.c_size_t)]),
+    ("tlgb_cp_als_batched", ctypes.c_int,
+     [ctypes.c_int, ctypes.POINTER(BatchItem), ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     ("tlgb_cp_als_default_options", None, [ctypes.POINTER(CpAlsOptions)]),
     ("tlgb_cp_als_workspace_size", ctypes.c_int,
      [ctypes.c_int, ctypes.c_int, _c_i64p, ctypes.c_int64, ctypes.POINTER(CpAlsOptions),

@@ -15,6 +15,9 @@ namespace tlgb {
 int set_error(int code, const std::string& msg);
 void clear_error();
 
+// Tuning keys of the batched CP-ALS kernel variants (batched.cu).
+int batched_set_tuning(const std::string& key, int value);
+
 // Number of SMs of the current device (cached per device).
 int sm_count();
 int current_device();

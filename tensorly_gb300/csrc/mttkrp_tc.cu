@@ -928,6 +928,6 @@ extern "C" int tlgb_set_tuning(const char* key, int value) {
   else if (k == "tc_waves") tc_tuning().waves = value;
   else if (k == "refine_simt") tc_tuning().refine_simt = value;
   else if (k == "tc_reserve_sms") tc_tuning().reserve_sms = value;
-  else return set_error(TLGB_EINVAL, "set_tuning: unknown key " + k);
+  else return batched_set_tuning(k, value);   // the batched CP-ALS variants
   return TLGB_OK;
 }

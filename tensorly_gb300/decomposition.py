@@ -469,3 +469,144 @@ class Tucker(DecompositionMixin):
 
     def __repr__(self):
         return f"Rank-{self.rank} Tucker decomposition via HOOI."
+
+
+# ----------------------------------------------------------------------------
+# Batched CP-ALS
+# ----------------------------------------------------------------------------
+class BatchedProblem:
+    """Many small 3-way f32 tensors packed for ``tlgb_cp_als_batched``.
+
+    The tensors go into one device buffer and the initial factors into
+    another (``init='random'``: the reference's per-tensor draws,
+    random/base.py:104, with ``random_state`` None, one int, or one seed per
+    tensor; or a list of factor lists / CPTensors).  ``run`` restarts from
+    the initial factors every time, so it can be timed repeatedly.
+    """
+
+    def __init__(self, tensors, ranks, init="random", random_state=None):
+        tensors = list(tensors)
+        n = len(tensors)
+        if isinstance(ranks, int):
+            ranks = [ranks] * n
+        self.ranks = [int(r) for r in ranks]
+        if len(self.ranks) != n:
+            raise ValueError("one rank per tensor is needed")
+        if n == 0:
+            raise ValueError("empty batch")
+        placed = [to_device(t) for t in tensors]
+        self.placement = placed[0][1]
+        dev = placed[0][0].device
+        self.device = dev
+        xs = []
+        for x, _ in placed:
+            if x.ndim != 3:
+                raise NotImplementedError("parafac_batched takes 3-way tensors")
+            xs.append(x.to(dev, torch.float32).contiguous().reshape(-1))
+        self.shapes = [tuple(int(s) for s in x.shape) for x, _ in placed]
+        xoff = np.cumsum([0] + [int(x.numel()) for x in xs])
+        self.xbuf = torch.cat(xs) if n > 1 else xs[0].clone()
+        foff = [0]
+        for sh, r in zip(self.shapes, self.ranks):
+            for d in sh:
+                foff.append(foff[-1] + d * r)
+        self.foff = foff
+        self.finit = torch.empty(foff[-1], dtype=torch.float32, device=dev)
+        if isinstance(init, str) and init == "random":
+            if random_state is None or isinstance(random_state, (int, np.integer)):
+                seeds = [random_state] * n
+            else:
+                seeds = list(random_state)
+            host = np.empty(foff[-1], dtype=np.float32)
+            q = 0
+            for t, (sh, r) in enumerate(zip(self.shapes, self.ranks)):
+                rng = check_random_state(seeds[t])
+                for d in sh:
+                    host[foff[q]:foff[q + 1]] = rng.random_sample((d, r)).astype(np.float32).ravel()
+                    q += 1
+            self.finit.copy_(torch.from_numpy(host))
+        elif isinstance(init, (list, tuple)):
+            q = 0
+            for t, (sh, r) in enumerate(zip(self.shapes, self.ranks)):
+                f_init = init[t].factors if isinstance(init[t], CPTensor) else init[t]
+                for k, d in enumerate(sh):
+                    f = like(f_init[k], self.xbuf).to(torch.float32).reshape(-1)
+                    if f.numel() != d * r:
+                        raise ValueError(f"initial factor {k} of tensor {t} has the wrong size")
+                    self.finit[foff[q]:foff[q + 1]].copy_(f)
+                    q += 1
+        else:
+            raise ValueError(f'Initialization method "{init}" not recognized')
+        self.fbuf = torch.empty_like(self.finit)
+        self.items = (_lib.BatchItem * n)()
+        q = 0
+        for t, (sh, r) in enumerate(zip(self.shapes, self.ranks)):
+            self.items[t].X = self.xbuf.data_ptr() + 4 * int(xoff[t])
+            for k in range(3):
+                self.items[t].factors[k] = self.fbuf.data_ptr() + 4 * foff[q]
+                self.items[t].dims[k] = sh[k]
+                q += 1
+            self.items[t].rank = r
+        self.final = torch.empty(n, dtype=torch.float64, device=dev)
+        nbytes = ctypes.c_size_t(0)
+        _lib.check(_lib.lib().tlgb_cp_als_batched_workspace_size(n, ctypes.byref(nbytes)))
+        self.ws = workspace(nbytes.value, dev)
+        self.sweeps = None
+
+    def __len__(self):
+        return len(self.ranks)
+
+    def run(self, n_iter_max, sweeps_per_launch=0, sweep_errors=False):
+        """Restart from the initial factors and run ``n_iter_max`` sweeps."""
+        n = len(self)
+        self.fbuf.copy_(self.finit)
+        self.sweeps = (torch.empty((n, max(1, int(n_iter_max))), dtype=torch.float64,
+                                   device=self.device) if sweep_errors else None)
+        _lib.check(_lib.lib().tlgb_cp_als_batched(
+            n, self.items, int(n_iter_max), int(sweeps_per_launch), ptr(self.final),
+            ptr(self.sweeps) if self.sweeps is not None else None, ptr(self.ws),
+            self.ws.numel(), stream_of(self.xbuf)))
+        return self
+
+    def results(self):
+        out = []
+        q = 0
+        for sh, r in zip(self.shapes, self.ranks):
+            fs = []
+            for k in range(3):
+                fs.append(self.placement.back(self.fbuf[self.foff[q]:self.foff[q + 1]]
+                                              .view(sh[k], r).clone()))
+                q += 1
+            w = self.placement.back(torch.ones(r, dtype=torch.float32, device=self.device))
+            out.append(CPTensor((w, fs)))
+        return out
+
+
+def parafac_batched(tensors, ranks, n_iter_max=100, init="random", random_state=None,
+                    return_errors=False, sweep_errors=False, sweeps_per_launch=0):
+    """CP-ALS of many small 3-way f32 tensors at once (one persistent kernel
+    per size class of tensors).
+
+    Per tensor this is ``parafac(tensor, rank, n_iter_max=n_iter_max, tol=0,
+    init=..., normalize_factors=False)`` (tensorly/decomposition/_cp.py:230-543):
+    exactly ``n_iter_max`` sweeps, weights all one.  ``init``: ``'random'``
+    (``random_state``: None, an int applied to every tensor, or one seed per
+    tensor; the reference's draws, random/base.py:104) or a list of factor
+    lists.  Mode sizes 1..64, ranks 1..16.
+
+    Returns the list of ``CPTensor``; with ``return_errors`` also the final
+    relative errors (from the residual, as a NumPy array), and with
+    ``sweep_errors`` the per-sweep errors (n_tensors x n_iter_max).
+    """
+    tensors = list(tensors)
+    if len(tensors) == 0:
+        return ([], np.zeros(0)) if return_errors else []
+    prob = BatchedProblem(tensors, ranks, init=init, random_state=random_state)
+    prob.run(n_iter_max, sweeps_per_launch=sweeps_per_launch, sweep_errors=sweep_errors)
+    out = prob.results()
+    res = [out]
+    if return_errors:
+        res.append(prob.final.cpu().numpy())
+    if sweep_errors:
+        res.append(prob.sweeps[:, : int(n_iter_max)].cpu().numpy())
+    return out if len(res) == 1 else tuple(res)
