@@ -49,9 +49,12 @@ def parse():
     p.add_argument("--refine", type=int, default=3)
     p.add_argument("--cpu-sweeps", type=int, default=40)
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--workload", default="dense", choices=["dense", "batched"],
+    p.add_argument("--workload", default="dense", choices=["dense", "batched", "learned"],
                    help="dense: 512^3 rank-64 CP-ALS (the headline); batched: 4096 uneven "
-                        "3-way tensors, 100 sweeps each")
+                        "3-way tensors, 100 sweeps each; learned: time to fit 4096 32^3 "
+                        "rank-8 tensors from the learned warm start vs init='svd'")
+    p.add_argument("--train-samples", type=int, default=1_000_000,
+                   help="learned: tensors the network is trained on (before the timed steps)")
     p.add_argument("--count", type=int, default=4096, help="batched: number of tensors")
     p.add_argument("--profile", action="store_true",
                    help="run only the warm-up and timed steps (for ncu launch lists)")
@@ -463,6 +466,18 @@ def run_batched(args):
         v, dt = _batched_cpu_sample(xs, ranks, seeds, sweeps, 16)
         cpu = {"value": v, "unit": "decomps/s", "cores": os.cpu_count(), "kind": "port",
                "sample": f"16 tensors x {sweeps} sweeps ({dt:.1f} s) of the NumPy restatement"}
+    # plain per-tensor ALS on the same GPU: the single-tensor parafac, one call per tensor
+    n_pt = min(n, 64)
+    for t in range(2):
+        tg.parafac(torch.from_numpy(xs[t]).to(dev), ranks[t], n_iter_max=sweeps, init="random",
+                   random_state=seeds[t], tol=0)
+    torch.cuda.synchronize()
+    p0 = time.perf_counter()
+    for t in range(n_pt):
+        tg.parafac(torch.from_numpy(xs[t]).to(dev), ranks[t], n_iter_max=sweeps, init="random",
+                   random_state=seeds[t], tol=0)
+    torch.cuda.synchronize()
+    per_tensor = n_pt / (time.perf_counter() - p0)
     flops = sum(3 * 2 * x.size * r * sweeps for x, r in zip(xs, ranks))
     line = {"metric": BATCH_METRIC, "value": value, "unit": "decomps/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
@@ -474,6 +489,8 @@ def run_batched(args):
             "accuracy_vs_f64": {"max_rel_diff_final_error_8": float(max(rel)),
                                 "median": float(np.median(rel))},
             "mttkrp_tflops": flops / (ms / 1000.0) / 1e12,
+            "per_tensor_gpu": {"value": per_tensor, "unit": "decomps/s",
+                               "sample": f"{n_pt} tensors, one parafac call each (f32)"},
             "cpu_baseline": cpu,
             "e2e": {"value": n / e_s, "unit": "decomps/s",
                     "h2d_bytes_per_step": int(sum(x.nbytes for x in xs)),
@@ -482,10 +499,144 @@ def run_batched(args):
     print(json.dumps(line), flush=True)
 
 
+LEARNED_METRIC = ("time-to-fit decompositions/s, 4096 32^3 rank-8 f32 tensors, "
+                  "ALS to tol 1e-8 from the learned warm start")
+
+
+def _learned_cpu_sample(seeds, n_sample, tol, max_sweeps):
+    """The reference's per-tensor parafac (NumPy restatement) from init='svd'
+    to the same stop test, on the first `n_sample` tensors: decompositions/s."""
+    import oracle
+    from oracle import warm_start_oracle as wo
+    X, _, _ = wo.generate(seeds[:n_sample], wo.omega())
+    t0 = time.perf_counter()
+    for x in X:
+        oracle.parafac(x.reshape(32, 32, 32).astype(np.float32), 8, n_iter_max=max_sweeps,
+                       init="svd", tol=tol)
+    dt = time.perf_counter() - t0
+    return n_sample / dt, dt
+
+
+def run_learned(args):
+    import torch
+    import tensorly_gb300 as tg
+    from tensorly_gb300 import _lib, learned
+    ws_n, rank, _ = dist_env()
+    if rank != 0:
+        return
+    n = args.count
+    tol, max_sweeps, probe = 1e-8, 300, 5
+    seeds = np.arange(10 ** 6, 10 ** 6 + n)
+    workload = (f"{n} tensors 32^3 f32, rank-8 CP with column congruence U(0, 0.9) + 1 % "
+                f"noise; ALS to tol {tol} (abs_rec_error), at most {max_sweeps} sweeps")
+    if args.impl == "reference":
+        v, dt = _learned_cpu_sample(seeds, 8, tol, max_sweeps)
+        line = {"metric": LEARNED_METRIC, "value": v, "unit": "decomps/s", "n_gpus": args.gpus,
+                "steps": 1, "warmup": 0, "ms_per_step": 1000.0 * dt, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "impl": "reference",
+                "config": {"workload": workload, "step": "8 tensors (bounded sample), init='svd'"},
+                "cpu_baseline": {"value": v, "unit": "decomps/s", "cores": os.cpu_count(),
+                                 "kind": "port", "sample": "8 tensors, parafac(init='svd', tol)"},
+                "e2e": {"value": v, "unit": "decomps/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+    tg.build() if not os.path.exists(_lib.library_path()) else None
+    dev = torch.device("cuda", torch.cuda.current_device())
+    gen = learned.Generator(dev)
+    net = learned.WarmStartNet(seed=0, device=dev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    losses = net.train(n_samples=args.train_samples, batch=512, lr=1e-3, lr_final=1e-4,
+                       generator=gen)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    X, _, _ = gen(seeds)
+    torch.cuda.synchronize()
+    st = torch.cuda.current_stream()
+
+    def step():   # the learned path: sketch, inference, ALS to tol
+        feats, xnorm = learned.sketch(X, gen.omega)
+        return learned._als(X, net.predict(X, feats, xnorm), max_sweeps, tol=tol)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    ev0.record(st)
+    for _ in range(args.steps):
+        prob = step()
+    ev1.record(st)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    # inference alone: sketch + network + lift for the whole batch
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(5):
+        feats, xnorm = learned.sketch(X, gen.omega)
+        net.predict(X, feats, xnorm)
+    e1.record(st)
+    torch.cuda.synchronize()
+    infer_ms = e0.elapsed_time(e1) / 5
+    res = learned.evaluate(net, seeds, max_sweeps=max_sweeps, tol=tol, probe=probe, generator=gen)
+    # end to end: host tensors in, factors and errors back
+    Xh = X.cpu().numpy().reshape(n, 32, 32, 32)
+    torch.cuda.synchronize()
+    h0 = time.perf_counter()
+    Xd = torch.from_numpy(Xh).to(dev).reshape(n, -1)
+    feats, xnorm = learned.sketch(Xd, gen.omega)
+    pe = learned._als(Xd, net.predict(Xd, feats, xnorm), max_sweeps, tol=tol)
+    fb = pe.fbuf.cpu()
+    fe = pe.final.cpu()
+    e2e_s = time.perf_counter() - h0
+    cpu = None
+    if not args.no_cpu_baseline:
+        v, dt = _learned_cpu_sample(seeds, 8, tol, max_sweeps)
+        cpu = {"value": v, "unit": "decomps/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"8 tensors, parafac(init='svd', tol) of the NumPy restatement ({dt:.1f} s)"}
+
+    def stats(k):
+        v = res["sweeps_" + k]
+        return {"sweeps_mean": float(v.mean()), "sweeps_median": float(np.median(v)),
+                "sweeps_p90": float(np.percentile(v, 90)), "ms": res["ms_" + k],
+                "decomps_per_s": n / (res["ms_" + k] / 1000.0),
+                "median_final_err": float(np.median(res["err_" + k]))}
+
+    line = {"metric": LEARNED_METRIC, "value": n / (ms / 1000.0), "unit": "decomps/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": workload, "l2": "0.54 GB of tensors > L2",
+                       "network": "1536-1024-512-768 MLP + sketch skip, "
+                                  f"{net.n_params} parameters"},
+            "training": {"samples": args.train_samples, "seconds": train_s,
+                         "samples_per_s": args.train_samples / train_s,
+                         "loss_first_20": float(losses[:20].mean()),
+                         "loss_last_20": float(losses[-20:].mean())},
+            "inference": {"ms": infer_ms, "tensors_per_s": n / (infer_ms / 1000.0)},
+            "starts": {"svd": stats("svd"), "learned": stats("learned"), "warm": stats("warm"),
+                       "warm_kept_network_frac": float(1 - res["used_svd"].mean())},
+            "cpu_baseline": cpu,
+            "e2e": {"value": n / e2e_s, "unit": "decomps/s",
+                    "h2d_bytes_per_step": int(Xh.nbytes),
+                    "d2h_bytes_per_step": int(fb.numel() * 4 + fe.numel() * 8)},
+            # per step: sketch, 3 GEMMs + skip, loss/scale, lift, the batched ALS kernel
+            "clocks": clk, "gpu_launches": 8 * args.steps}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.workload == "batched":
         run_batched(args)
+    elif args.workload == "learned":
+        run_learned(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -271,8 +271,10 @@ int tlgb_tucker_hooi(int dtype, const void* X, int ndim, const int64_t* shape, i
 /*
  * Batched CP-ALS of many small 3-way f32 tensors of uneven shape and rank:
  * for every item, the sweep loop of tensorly/decomposition/_cp.py:394-440
- * (parafac with normalize_factors=False, no stop test: exactly n_iter_max
- * sweeps), weights all one.  items (host array): device pointers to the
+ * (parafac with normalize_factors=False), weights all one: exactly
+ * n_iter_max sweeps when tol is 0, else each tensor stops after the first
+ * sweep s >= 1 with |e_{s-1} - e_s| < tol (_cp.py:505-522, cvg_criterion
+ * 'abs_rec_error'), e_s the relative error from the residual.  items (host array): device pointers to the
  * tensor (C order) and to the three factors (dims[k] x rank, row-major; the
  * initial factors on entry, the result on exit).  Mode sizes 1..64, rank
  * 1..16.  One persistent kernel per `sweeps_per_launch` sweeps (<= 0: all in
@@ -280,7 +282,10 @@ int tlgb_tucker_hooi(int dtype, const void* X, int ndim, const int64_t* shape, i
  * decreasing work and keeps it in shared memory when it fits.
  * final_errors (device, n_tensors doubles): relative error of the final
  * model from the residual; sweep_errors (device, n_tensors x n_iter_max, or
- * NULL): per-sweep errors from the reference's expansion (_cp.py:217-225).
+ * NULL): per-sweep errors from the reference's expansion (_cp.py:217-225),
+ * or from the residual when flags has TLGB_BATCH_EXACT_SWEEP_ERRORS or tol
+ * is positive (rows are left unwritten past a tensor's stop); sweeps_done
+ * (device, n_tensors ints, or NULL): the sweeps each tensor ran.
  * The call returns after the GPU finished.  No direct counterpart in TensorLy
  * (its users loop over parafac).
  */
@@ -292,9 +297,57 @@ typedef struct tlgb_batch_item {
 } tlgb_batch_item;
 
 int tlgb_cp_als_batched_workspace_size(int n_tensors, size_t* bytes);
+#define TLGB_BATCH_EXACT_SWEEP_ERRORS 1
 int tlgb_cp_als_batched(int n_tensors, const tlgb_batch_item* items, int n_iter_max,
-                        int sweeps_per_launch, double* final_errors, double* sweep_errors,
-                        void* workspace, size_t workspace_bytes, void* stream);
+                        int sweeps_per_launch, int flags, double tol, double* final_errors,
+                        double* sweep_errors, int* sweeps_done, void* workspace,
+                        size_t workspace_bytes, void* stream);
+
+/*
+ * Learned warm start for CP-ALS (no counterpart in TensorLy; its fallback is
+ * TensorLy's init='svd', tensorly/decomposition/_cp.py:70-96).  Fixed problem
+ * family: 32 x 32 x 32 f32 tensors of rank 8 (factor columns with pairwise
+ * congruence c ~ U(0, 0.9) per mode, 1 % noise), generated from a seed by a
+ * counter-based SplitMix64 generator; the network maps the three sketches
+ * unfold(X, n) Omega_n (Omega_n: 1024 x 16 Gaussian, fixed) divided by ||X||
+ * to the three 32 x 8 factors divided by ||X||^(1/3).
+ *   tlgb_ws_omega      Omega (3 x 1024 x 16 f32)
+ *   tlgb_ws_generate   tensors (batch x 32768), sketch features (batch x 1536)
+ *                      and ||X|| (batch) of the tensors with the given seeds
+ *   tlgb_ws_sketch     sketch features and ||X|| of tensors given in memory
+ *   tlgb_ws_gemm       C(m, n) = epi(sum_k A[m sam + k sak] B[k sbk + n sbn])
+ *                      (+ bias[n], ReLU if relu, zeroed where mask(m, n) <= 0)
+ *   tlgb_ws_colsum     out[n] = sum_m Y[m ld + n]
+ *   tlgb_ws_cp_loss    loss (batch) = min_a ||X - a [[A]]||^2 / ||X||^2 with
+ *                      A = out * ||X||^(1/3) (= 1 - <X,[[A]]>^2 / (||X||^2 ||[[A]]||^2)),
+ *                      its gradient with respect to out divided by batch (dout
+ *                      may be NULL) and the best scale a (alpha, may be NULL)
+ *   tlgb_ws_lift       initial factors = out * (||X|| alpha)^(1/3)
+ *   tlgb_ws_sketch_skip out (batch x 3 x 32 x 8) += the first 8 columns of each
+ *                      32 x 16 sketch block of feats (the network's fixed skip)
+ *   tlgb_ws_adam       one Adam step on a flat parameter buffer
+ *   tlgb_ws_svd_init   init='svd' factors (batch x 3 x 32 x 8) of the tensors
+ * All pointers are device memory; all f32.
+ */
+int tlgb_ws_omega(void* omega, void* stream);
+int tlgb_ws_generate(const int64_t* seeds, int batch, void* X, void* feats, void* xnorm,
+                     const void* omega, void* stream);
+int tlgb_ws_sketch(const void* X, int batch, void* feats, void* xnorm, const void* omega,
+                   void* stream);
+int tlgb_ws_gemm(int M, int N, int K, const void* A, int64_t sam, int64_t sak, const void* B,
+                 int64_t sbk, int64_t sbn, void* C, int64_t ldc, const void* bias, int relu,
+                 const void* mask, void* stream);
+int tlgb_ws_colsum(const void* Y, int M, int N, int64_t ld, void* out, void* stream);
+int tlgb_ws_cp_loss(const void* X, const void* out, const void* xnorm, int batch, void* loss,
+                    void* dout, void* alpha, void* stream);
+int tlgb_ws_sketch_skip(const void* feats, int batch, void* out, void* stream);
+int tlgb_ws_lift(const void* out, const void* xnorm, const void* alpha, int batch, void* factors,
+                 void* stream);
+int tlgb_ws_adam(void* params, const void* grads, void* m, void* v, int64_t n, float lr,
+                 float beta1, float beta2, float eps, int step, void* stream);
+int tlgb_ws_svd_init_workspace_size(int batch, size_t* bytes);
+int tlgb_ws_svd_init(const void* X, int batch, void* factors, void* workspace,
+                     size_t workspace_bytes, void* stream);
 
 /*
  * cp_normalize: unit-norm factor columns, norms multiplied into weights

@@ -131,8 +131,40 @@ SIGNATURES = [
     ("tlgb_cp_als_batched_workspace_size", ctypes.c_int,
      [ctypes.c_int, ctypes.POINTER(ctypes.c_size_t)]),
     ("tlgb_cp_als_batched", ctypes.c_int,
-     [ctypes.c_int, ctypes.POINTER(BatchItem), ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
-      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+     [ctypes.c_int, ctypes.POINTER(BatchItem), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+      ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+      ctypes.c_size_t, ctypes.c_void_p]),
+    ("tlgb_ws_omega", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    ("tlgb_ws_generate", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+      ctypes.c_void_p, ctypes.c_void_p]),
+    ("tlgb_ws_sketch", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+      ctypes.c_void_p]),
+    ("tlgb_ws_gemm", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
+      ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
+      ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),
+    ("tlgb_ws_colsum", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_void_p,
+      ctypes.c_void_p]),
+    ("tlgb_ws_cp_loss", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    ("tlgb_ws_sketch_skip", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),
+    ("tlgb_ws_lift", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+      ctypes.c_void_p]),
+    ("tlgb_ws_adam", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+      ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_int,
+      ctypes.c_void_p]),
+    ("tlgb_ws_svd_init_workspace_size", ctypes.c_int,
+     [ctypes.c_int, ctypes.POINTER(ctypes.c_size_t)]),
+    ("tlgb_ws_svd_init", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+      ctypes.c_void_p]),
     ("tlgb_cp_als_default_options", None, [ctypes.POINTER(CpAlsOptions)]),
     ("tlgb_cp_als_workspace_size", ctypes.c_int,
      [ctypes.c_int, ctypes.c_int, _c_i64p, ctypes.c_int64, ctypes.POINTER(CpAlsOptions),

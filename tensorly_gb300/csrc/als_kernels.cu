@@ -611,7 +611,10 @@ k_solve(const T* __restrict__ partial, int splits, int64_t I, int R,
     const float* VmH = nullptr;                          // V = VmH + VmL (df)
     const float* VmL = nullptr;
     if (mats_in_smem) {
-      double* Vs = rb + RBR + ((5 * RBR + 3) / 4) * 2;   // 16-byte aligned
+      // 16-byte aligned for the float4 copies below: R * R (the offset of mb
+      // in doubles) is odd for odd R, so round up by one double
+      double* Vs = rb + RBR + ((5 * RBR + 3) / 4) * 2;
+      if (reinterpret_cast<uintptr_t>(Vs) & 15) Vs += 1;
       if (df) {
         // [W | V hi | V lo] as written by the factorisation, copied with
         // 16-byte loads that are all issued before the first store
@@ -1144,8 +1147,9 @@ static size_t solve_smem(int R) {
   const size_t RR = (size_t)R * R;
   const bool mats = R <= kSolveDfMaxRank;
   const size_t rb = (size_t)std::max(1, kSolveThreads / R) * R;
-  // gacc, mb, xb, rb (f64) + five f32 arrays + V (f64, or two f32 planes) and W (f32)
-  const size_t ir = RR + 3 * rb + ((5 * rb + 3) / 4) * 2 + (mats ? RR + (RR + 1) / 2 : 0);
+  // gacc, mb, xb, rb (f64) + five f32 arrays + V (f64, or two f32 planes) and W (f32),
+  // whose start is rounded up to 16 bytes (one more double)
+  const size_t ir = RR + 3 * rb + ((5 * rb + 3) / 4) * 2 + (mats ? RR + (RR + 1) / 2 + 1 : 0);
   const size_t direct = RR + (size_t)kSolveWarps * R + (mats ? RR + R : 0);
   return std::max(ir, direct) * sizeof(double);
 }

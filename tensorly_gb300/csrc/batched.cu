@@ -69,6 +69,10 @@ struct BArgs {
   int x_cap;           // floats of shared memory available for the tensor
   double* final_err;   // [n] (item order)
   double* sweep_err;   // [n][n_iter] or null
+  int exact_sweep_err; // per-sweep errors from the residual instead of the expansion
+  double tol;          // > 0: stop a tensor once |e_{s-1} - e_s| < tol (s >= 1)
+  int* sweeps_done;    // [n] sweeps run per tensor, or null
+  int* conv;           // [n] converged in an earlier launch (workspace, zeroed per run)
 };
 
 __device__ __forceinline__ double warp_sum_d(double v) {
@@ -228,6 +232,32 @@ __device__ __forceinline__ float4 mttkrp_rows(const float* __restrict__ X, Idx r
   return make_float4(a0, a1, a2, a3);
 }
 
+// sum over the tensor of (x - [[A0, A1, A2]])^2, compensated f32 per thread
+// then f64 across the block; one warp per (i, j) row of X (global memory).
+template <int NT>
+__device__ double residual2(const float* __restrict__ X, const float* Fs, int I0, int I1, int I2,
+                            int R, int RP, double* scratch) {
+  const float* A0 = Fs;
+  const float* A1 = Fs + kBMaxDim * kBMaxRank;
+  const float* A2 = Fs + 2 * kBMaxDim * kBMaxRank;
+  float s = 0.f, c = 0.f;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int row = warp; row < I0 * I1; row += NT / 32) {
+    const int i = row / I1, j = row - (row / I1) * I1;
+    const float* xr = X + (int64_t)row * I2;
+    for (int k = lane; k < I2; k += 32) {
+      float rec = 0.f;
+      for (int r = 0; r < R; ++r) rec = fmaf(A0[i * RP + r] * A1[j * RP + r], A2[k * RP + r], rec);
+      const float d = __ldg(&xr[k]) - rec;
+      const float h = d * d, l = fmaf(d, d, -h);
+      const float u = s + h;
+      c += ((fabsf(s) >= h) ? ((s - u) + h) : ((h - u) + s)) + l;
+      s = u;
+    }
+  }
+  return block_sum_d<NT>((double)s + (double)c, scratch);
+}
+
 template <int NT>
 __global__ void __launch_bounds__(NT, kBThreads / NT) k_cp_als_batched(const BArgs a) {
   extern __shared__ __align__(16) float sm[];
@@ -249,6 +279,7 @@ __global__ void __launch_bounds__(NT, kBThreads / NT) k_cp_als_batched(const BAr
     const int t = s_t;
     if (t >= a.n) break;
     const int idx = a.order[t];
+    if (a.tol > 0.0 && a.sweep0 > 0 && a.conv[idx]) continue;   // stopped in an earlier launch
     const BItem it = a.items[idx];
     const int I0 = it.I[0], I1 = it.I[1], I2 = it.I[2], R = it.R;
     const int RP = (R + 3) & ~3, NQ = RP / 4;
@@ -308,6 +339,11 @@ __global__ void __launch_bounds__(NT, kBThreads / NT) k_cp_als_batched(const BAr
     }
     __syncthreads();
 
+    // tol: the error of the previous sweep is carried between launches in final_err
+    double prev = (a.tol > 0.0 && a.sweep0 > 0) ? a.final_err[idx] : -1.0;
+    double e_last = -1.0;
+    int n_done = a.n_sweeps;
+    bool stopped = false;
     for (int sw = 0; sw < a.n_sweeps; ++sw) {
       for (int n = 0; n < 3; ++n) {
         // V = Hadamard product of the other Grams (identity on the padding)
@@ -425,7 +461,21 @@ __global__ void __launch_bounds__(NT, kBThreads / NT) k_cp_als_batched(const BAr
         }
         __syncthreads();
       }
-      if (a.sweep_err) {   // expansion of _cp.py:217-225 in f64 from the f32 pieces
+      if (a.tol > 0.0 || (a.sweep_err && a.exact_sweep_err)) {
+        const double res2 = residual2<NT>(it.X, Fs, I0, I1, I2, R, RP, scratch);
+        const double e = sqrt(res2) / sqrt(nx2);
+        e_last = e;
+        if (a.sweep_err && tid == 0) a.sweep_err[(int64_t)idx * a.n_iter + a.sweep0 + sw] = e;
+        // _cp.py:505-522 (cvg_criterion 'abs_rec_error'); e is uniform over the block
+        if (a.tol > 0.0) {
+          if (a.sweep0 + sw >= 1 && fabs(prev - e) < a.tol) {
+            n_done = sw + 1;
+            stopped = true;
+            break;
+          }
+          prev = e;
+        }
+      } else if (a.sweep_err) {   // expansion of _cp.py:217-225 in f64 from the f32 pieces
         double rec = 0.0, ip = 0.0;
         for (int e = tid; e < RP * RP; e += NT) {
           const int r = e / RP, c = e - (e / RP) * RP;
@@ -450,28 +500,16 @@ __global__ void __launch_bounds__(NT, kBThreads / NT) k_cp_als_batched(const BAr
         const int i = e / R, r = e - (e / R) * R;
         it.F[k][e] = Fs[k * kBMaxDim * kBMaxRank + i * RP + r];
       }
-    if (a.last) {   // relative error of the final model from the residual
-      const float* A0 = Fs;
-      const float* A1 = Fs + kBMaxDim * kBMaxRank;
-      const float* A2 = Fs + 2 * kBMaxDim * kBMaxRank;
-      float s = 0.f, c = 0.f;
-      const int lane = tid & 31, warp = tid >> 5;
-      for (int row = warp; row < I0 * I1; row += NT / 32) {   // one warp per (i, j) row
-        const int i = row / I1, j = row - (row / I1) * I1;
-        const float* xr = it.X + (int64_t)row * I2;
-        for (int k = lane; k < I2; k += 32) {
-          float rec = 0.f;
-          for (int r = 0; r < R; ++r)
-            rec = fmaf(A0[i * RP + r] * A1[j * RP + r], A2[k * RP + r], rec);
-          const float d = __ldg(&xr[k]) - rec;
-          const float h = d * d, l = fmaf(d, d, -h);
-          const float u = s + h;
-          c += ((fabsf(s) >= h) ? ((s - u) + h) : ((h - u) + s)) + l;
-          s = u;
-        }
+    if (a.last || a.tol > 0.0) {   // relative error of the current model from the residual
+      if (e_last < 0.0) {
+        const double res2 = residual2<NT>(it.X, Fs, I0, I1, I2, R, RP, scratch);
+        e_last = sqrt(res2) / sqrt(nx2);
       }
-      const double res2 = block_sum_d<NT>((double)s + (double)c, scratch);
-      if (tid == 0) a.final_err[idx] = sqrt(res2) / sqrt(nx2);
+      if (tid == 0) a.final_err[idx] = e_last;
+    }
+    if (tid == 0) {
+      if (a.sweeps_done) a.sweeps_done[idx] = a.sweep0 + n_done;
+      if (a.tol > 0.0 && stopped) a.conv[idx] = 1;
     }
   }
 }
@@ -483,7 +521,7 @@ using namespace tlgb;
 
 namespace {
 struct BatchLayout {
-  size_t items_off, order_off, counter_off, bytes;
+  size_t items_off, order_off, counter_off, conv_off, bytes;
 };
 BatchLayout batch_layout(int n) {
   BatchLayout L{};
@@ -492,6 +530,7 @@ BatchLayout batch_layout(int n) {
   L.items_off = take((size_t)n * sizeof(BItem));
   L.order_off = take((size_t)n * sizeof(int));
   L.counter_off = take(256);
+  L.conv_off = take((size_t)n * sizeof(int));
   L.bytes = align_up(off, 256);
   return L;
 }
@@ -551,13 +590,14 @@ int batched_set_tuning(const std::string& key, int value) {
 }  // namespace tlgb
 
 extern "C" int tlgb_cp_als_batched(int n_tensors, const tlgb_batch_item* items, int n_iter_max,
-                                   int sweeps_per_launch, double* final_errors,
-                                   double* sweep_errors, void* workspace, size_t workspace_bytes,
-                                   void* stream) {
+                                   int sweeps_per_launch, int flags, double tol,
+                                   double* final_errors, double* sweep_errors, int* sweeps_done,
+                                   void* workspace, size_t workspace_bytes, void* stream) {
   clear_error();
   TLGB_CHECK_ARG(n_tensors >= 0 && (n_tensors == 0 || items), "cp_als_batched: bad items");
   TLGB_CHECK_ARG(n_iter_max >= 0, "cp_als_batched: n_iter_max must be >= 0");
   TLGB_CHECK_ARG(final_errors != nullptr || n_tensors == 0, "cp_als_batched: null final_errors");
+  TLGB_CHECK_ARG(tol >= 0.0, "cp_als_batched: tol must be >= 0");
   if (n_tensors == 0) return TLGB_OK;
   const BatchLayout L = batch_layout(n_tensors);
   if (!workspace || workspace_bytes < L.bytes)
@@ -600,6 +640,7 @@ extern "C" int tlgb_cp_als_batched(int n_tensors, const tlgb_batch_item* items, 
   BItem* d_items = reinterpret_cast<BItem*>(base + L.items_off);
   int* d_order = reinterpret_cast<int*>(base + L.order_off);
   int* d_counter = reinterpret_cast<int*>(base + L.counter_off);
+  int* d_conv = reinterpret_cast<int*>(base + L.conv_off);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   TLGB_CUDA_TRY(cudaMemcpyAsync(d_items, hv.data(), hv.size() * sizeof(BItem),
                                 cudaMemcpyHostToDevice, st));
@@ -610,6 +651,12 @@ extern "C" int tlgb_cp_als_batched(int n_tensors, const tlgb_batch_item* items, 
   a.n_iter = std::max(1, n_iter_max);
   a.final_err = final_errors;
   a.sweep_err = sweep_errors;
+  a.exact_sweep_err = (flags & TLGB_BATCH_EXACT_SWEEP_ERRORS) ? 1 : 0;
+  a.tol = tol;
+  a.sweeps_done = sweeps_done;
+  a.conv = d_conv;
+  if (tol > 0.0)
+    TLGB_CUDA_TRY(cudaMemsetAsync(d_conv, 0, (size_t)n_tensors * sizeof(int), st));
   const int spl = sweeps_per_launch > 0 ? sweeps_per_launch : std::max(1, n_iter_max);
   const int sms = sm_count();
   int done = 0;

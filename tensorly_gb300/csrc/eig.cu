@@ -84,6 +84,12 @@ __device__ int sturm_count(const T* d, const T* e2, int n, T x) {
 template <typename T>
 __global__ void __launch_bounds__(kEigThreads)
 k_sym_eig(const T* __restrict__ A, int n, int k, T* U, T* lam, int flip, T* Z, T* W) {
+  // batched launches: CTA b solves matrix b (every operand advanced by its size)
+  A += (int64_t)blockIdx.x * n * n;
+  U += (int64_t)blockIdx.x * n * k;
+  lam += (int64_t)blockIdx.x * k;
+  Z += (int64_t)blockIdx.x * 6 * k * n;
+  W = Z + (int64_t)k * n;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* As = reinterpret_cast<T*>(smem_raw);   // n * n
   T* d = As + n * n;                         // n
@@ -331,6 +337,13 @@ size_t sym_eig_workspace(int dtype, int64_t n, int64_t k) {
 
 template <typename T>
 int sym_eig_launch(const T* A, int n, int k, T* U, T* lam, int flip, void* ws, cudaStream_t st) {
+  return sym_eig_batched_launch<T>(A, n, k, 1, U, lam, flip, ws, st);
+}
+
+template <typename T>
+int sym_eig_batched_launch(const T* A, int n, int k, int batch, T* U, T* lam, int flip, void* ws,
+                           cudaStream_t st) {
+  TLGB_CHECK_ARG(batch >= 1 && batch <= 2147483647, "sym_eig: bad batch");
   TLGB_CHECK_ARG(n >= 1 && k >= 1 && k <= n, "sym_eig: need 1 <= k <= n");
   if (n > EigLimits<T>::max_n)
     return set_error(TLGB_EUNSUPPORTED, "sym_eig: matrix order above " +
@@ -344,14 +357,17 @@ int sym_eig_launch(const T* A, int n, int k, T* U, T* lam, int flip, void* ws, c
     attr[dev] = true;
   }
   T* Z = static_cast<T*>(ws);
-  T* W = Z + (size_t)k * n;
-  k_sym_eig<T><<<1, kEigThreads, eig_smem<T>(n), st>>>(A, n, k, U, lam, flip, Z, W);
+  k_sym_eig<T><<<batch, kEigThreads, eig_smem<T>(n), st>>>(A, n, k, U, lam, flip, Z, Z);
   TLGB_LAUNCH_CHECK();
   return TLGB_OK;
 }
 
 template int sym_eig_launch<float>(const float*, int, int, float*, float*, int, void*,
                                    cudaStream_t);
+template int sym_eig_batched_launch<float>(const float*, int, int, int, float*, float*, int,
+                                           void*, cudaStream_t);
+template int sym_eig_batched_launch<double>(const double*, int, int, int, double*, double*, int,
+                                            void*, cudaStream_t);
 template int sym_eig_launch<double>(const double*, int, int, double*, double*, int, void*,
                                     cudaStream_t);
 

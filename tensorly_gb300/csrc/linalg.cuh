@@ -10,6 +10,11 @@ int sym_eig_max_n(int dtype);
 size_t sym_eig_workspace(int dtype, int64_t n, int64_t k);
 template <typename T>
 int sym_eig_launch(const T* A, int n, int k, T* U, T* lam, int flip, void* ws, cudaStream_t st);
+// `batch` independent matrices, consecutive in A (n x n each), U (n x k), lam
+// (k); the workspace is `batch` times sym_eig_workspace (6 k n elements each).
+template <typename T>
+int sym_eig_batched_launch(const T* A, int n, int k, int batch, T* U, T* lam, int flip, void* ws,
+                           cudaStream_t st);
 
 // ---- Gram matrix of a tensor unfolding (svd.cu).  side 0: M M^T
 // (shape[mode] x shape[mode]); side 1: M^T M (J x J, J = numel / shape[mode]),

@@ -485,7 +485,12 @@ class BatchedProblem:
     """
 
     def __init__(self, tensors, ranks, init="random", random_state=None):
-        tensors = list(tensors)
+        stacked = isinstance(tensors, torch.Tensor) and tensors.ndim == 4
+        if stacked:   # one tensor of shape (n, I0, I1, I2): used in place when on the GPU
+            x4, x4_placement = to_device(tensors)
+            tensors = list(x4)
+        else:
+            tensors = list(tensors)
         n = len(tensors)
         if isinstance(ranks, int):
             ranks = [ranks] * n
@@ -494,18 +499,25 @@ class BatchedProblem:
             raise ValueError("one rank per tensor is needed")
         if n == 0:
             raise ValueError("empty batch")
-        placed = [to_device(t) for t in tensors]
-        self.placement = placed[0][1]
-        dev = placed[0][0].device
+        if stacked:
+            self.placement = x4_placement
+            dev = x4.device
+            self.shapes = [tuple(int(d) for d in x4.shape[1:])] * n
+            self.xbuf = x4.to(torch.float32).contiguous().reshape(-1)
+            xoff = np.arange(n + 1, dtype=np.int64) * int(np.prod(self.shapes[0]))
+        else:
+            placed = [to_device(t) for t in tensors]
+            self.placement = placed[0][1]
+            dev = placed[0][0].device
+            xs = []
+            for x, _ in placed:
+                if x.ndim != 3:
+                    raise NotImplementedError("parafac_batched takes 3-way tensors")
+                xs.append(x.to(dev, torch.float32).contiguous().reshape(-1))
+            self.shapes = [tuple(int(s) for s in x.shape) for x, _ in placed]
+            xoff = np.cumsum([0] + [int(x.numel()) for x in xs])
+            self.xbuf = torch.cat(xs) if n > 1 else xs[0].clone()
         self.device = dev
-        xs = []
-        for x, _ in placed:
-            if x.ndim != 3:
-                raise NotImplementedError("parafac_batched takes 3-way tensors")
-            xs.append(x.to(dev, torch.float32).contiguous().reshape(-1))
-        self.shapes = [tuple(int(s) for s in x.shape) for x, _ in placed]
-        xoff = np.cumsum([0] + [int(x.numel()) for x in xs])
-        self.xbuf = torch.cat(xs) if n > 1 else xs[0].clone()
         foff = [0]
         for sh, r in zip(self.shapes, self.ranks):
             for d in sh:
@@ -525,6 +537,11 @@ class BatchedProblem:
                     host[foff[q]:foff[q + 1]] = rng.random_sample((d, r)).astype(np.float32).ravel()
                     q += 1
             self.finit.copy_(torch.from_numpy(host))
+        elif isinstance(init, torch.Tensor):   # packed: (n, ...) in the layout of self.finit
+            f = like(init, self.xbuf).to(torch.float32).reshape(-1)
+            if f.numel() != foff[-1]:
+                raise ValueError("packed initial factors have the wrong size")
+            self.finit.copy_(f)
         elif isinstance(init, (list, tuple)):
             q = 0
             for t, (sh, r) in enumerate(zip(self.shapes, self.ranks)):
@@ -548,6 +565,7 @@ class BatchedProblem:
                 q += 1
             self.items[t].rank = r
         self.final = torch.empty(n, dtype=torch.float64, device=dev)
+        self.n_sweeps = torch.zeros(n, dtype=torch.int32, device=dev)
         nbytes = ctypes.c_size_t(0)
         _lib.check(_lib.lib().tlgb_cp_als_batched_workspace_size(n, ctypes.byref(nbytes)))
         self.ws = workspace(nbytes.value, dev)
@@ -556,16 +574,22 @@ class BatchedProblem:
     def __len__(self):
         return len(self.ranks)
 
-    def run(self, n_iter_max, sweeps_per_launch=0, sweep_errors=False):
-        """Restart from the initial factors and run ``n_iter_max`` sweeps."""
+    def run(self, n_iter_max, sweeps_per_launch=0, sweep_errors=False, exact_sweep_errors=False,
+            tol=0.0):
+        """Restart from the initial factors and run ``n_iter_max`` sweeps, or
+        with ``tol`` > 0 stop each tensor at the reference's 'abs_rec_error'
+        test; ``exact_sweep_errors`` computes the per-sweep errors from the
+        residual (always so with ``tol``).  ``n_sweeps`` holds the sweeps
+        each tensor ran; per-sweep errors past a tensor's stop are NaN."""
         n = len(self)
         self.fbuf.copy_(self.finit)
-        self.sweeps = (torch.empty((n, max(1, int(n_iter_max))), dtype=torch.float64,
-                                   device=self.device) if sweep_errors else None)
+        self.sweeps = (torch.full((n, max(1, int(n_iter_max))), float("nan"), dtype=torch.float64,
+                                  device=self.device) if sweep_errors else None)
         _lib.check(_lib.lib().tlgb_cp_als_batched(
-            n, self.items, int(n_iter_max), int(sweeps_per_launch), ptr(self.final),
-            ptr(self.sweeps) if self.sweeps is not None else None, ptr(self.ws),
-            self.ws.numel(), stream_of(self.xbuf)))
+            n, self.items, int(n_iter_max), int(sweeps_per_launch),
+            1 if exact_sweep_errors else 0, float(tol), ptr(self.final),
+            ptr(self.sweeps) if self.sweeps is not None else None, ptr(self.n_sweeps),
+            ptr(self.ws), self.ws.numel(), stream_of(self.xbuf)))
         return self
 
     def results(self):
@@ -583,13 +607,15 @@ class BatchedProblem:
 
 
 def parafac_batched(tensors, ranks, n_iter_max=100, init="random", random_state=None,
-                    return_errors=False, sweep_errors=False, sweeps_per_launch=0):
+                    return_errors=False, sweep_errors=False, sweeps_per_launch=0, tol=0.0):
     """CP-ALS of many small 3-way f32 tensors at once (one persistent kernel
     per size class of tensors).
 
-    Per tensor this is ``parafac(tensor, rank, n_iter_max=n_iter_max, tol=0,
-    init=..., normalize_factors=False)`` (tensorly/decomposition/_cp.py:230-543):
-    exactly ``n_iter_max`` sweeps, weights all one.  ``init``: ``'random'``
+    Per tensor this is ``parafac(tensor, rank, n_iter_max=n_iter_max, tol=tol,
+    init=..., normalize_factors=False)`` (tensorly/decomposition/_cp.py:230-543),
+    weights all one: exactly ``n_iter_max`` sweeps with ``tol=0``, else each
+    tensor stops at the reference's 'abs_rec_error' test on its relative
+    error (computed from the residual).  ``init``: ``'random'``
     (``random_state``: None, an int applied to every tensor, or one seed per
     tensor; the reference's draws, random/base.py:104) or a list of factor
     lists.  Mode sizes 1..64, ranks 1..16.
@@ -602,7 +628,7 @@ def parafac_batched(tensors, ranks, n_iter_max=100, init="random", random_state=
     if len(tensors) == 0:
         return ([], np.zeros(0)) if return_errors else []
     prob = BatchedProblem(tensors, ranks, init=init, random_state=random_state)
-    prob.run(n_iter_max, sweeps_per_launch=sweeps_per_launch, sweep_errors=sweep_errors)
+    prob.run(n_iter_max, sweeps_per_launch=sweeps_per_launch, sweep_errors=sweep_errors, tol=tol)
     out = prob.results()
     res = [out]
     if return_errors:

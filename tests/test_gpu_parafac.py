@@ -194,3 +194,27 @@ def test_ill_conditioned_normal_equations_use_f64_fallback(gb300):
     np.testing.assert_allclose(errs, oe, rtol=1e-6)
     for a, b in zip(cp.factors, of):
         assert rel(host(a), b) < 1e-4
+
+
+@pytest.mark.parametrize("shape,rank,precision", [
+    ((53, 59, 22), 9, "native"), ((12, 45, 43), 5, "native"), ((30, 31, 29), 7, "native"),
+    ((40, 33, 35), 1, "native"), ((48, 40, 36), 11, "bf16"), ((64, 48, 40), 3, "bf16")])
+def test_parafac_f32_odd_ranks_match_f64_oracle(gb300, shape, rank, precision):
+    """Odd ranks (R * R odd) through the f32 normal-equation solve: same final
+    error as the f64 oracle from the same random initial factors."""
+    rs = np.random.RandomState(rank)
+    A = [rs.rand(d, rank) for d in shape]
+    x = (oracle.cp_to_tensor((None, A)) + 0.01 * rs.randn(*shape)).astype(np.float32)
+    init = oracle.random_cp(shape, rank, random_state=7, dtype=np.float64)[1]
+    # bf16 sweeps take a different path to the optimum: compare once converged
+    n_iter = 25 if precision == "native" else 120
+    (_, f), errs = gb300.parafac(torch.as_tensor(x, device="cuda"), rank, n_iter_max=n_iter,
+                                 init=(None, [torch.as_tensor(a.astype(np.float32), device="cuda")
+                                              for a in init]),
+                                 tol=0, return_errors=True, precision=precision)
+    x64 = x.astype(np.float64)
+    _, f64, _ = oracle.parafac_sweeps(x64, np.ones(rank), init, n_iter)
+    e64 = np.linalg.norm(x64 - oracle.cp_to_tensor((None, f64))) / np.linalg.norm(x64)
+    e = np.linalg.norm(x64 - oracle.cp_to_tensor((None, [host(t).astype(np.float64) for t in f]))) \
+        / np.linalg.norm(x64)
+    assert abs(e - e64) / e64 < 1e-3, (e, e64)
