@@ -53,7 +53,7 @@ def parse():
                    help="dense: 512^3 rank-64 CP-ALS (the headline); batched: 4096 uneven "
                         "3-way tensors, 100 sweeps each; learned: time to fit 4096 32^3 "
                         "rank-8 tensors from the learned warm start vs init='svd'")
-    p.add_argument("--train-samples", type=int, default=1_000_000,
+    p.add_argument("--train-samples", type=int, default=200_000,
                    help="learned: tensors the network is trained on (before the timed steps)")
     p.add_argument("--count", type=int, default=4096, help="batched: number of tensors")
     p.add_argument("--profile", action="store_true",
@@ -499,8 +499,8 @@ def run_batched(args):
     print(json.dumps(line), flush=True)
 
 
-LEARNED_METRIC = ("time-to-fit decompositions/s, 4096 32^3 rank-8 f32 tensors, "
-                  "ALS to tol 1e-8 from the learned warm start")
+LEARNED_METRIC = ("time-to-fit decompositions/s, 10000 held-out 32^3 rank-8 f32 tensors, "
+                  "ALS to a 1e-6 error change from the learned warm start")
 
 
 def _learned_cpu_sample(seeds, n_sample, tol, max_sweeps):
@@ -524,11 +524,13 @@ def run_learned(args):
     ws_n, rank, _ = dist_env()
     if rank != 0:
         return
-    n = args.count
-    tol, max_sweeps, probe = 1e-8, 300, 5
+    n = 10000
+    tol, max_sweeps = 1e-6, 300
     seeds = np.arange(10 ** 6, 10 ** 6 + n)
-    workload = (f"{n} tensors 32^3 f32, rank-8 CP with column congruence U(0, 0.9) + 1 % "
-                f"noise; ALS to tol {tol} (abs_rec_error), at most {max_sweeps} sweeps")
+    workload = (f"{n} held-out tensors 32^3 f32 (seeds 1e6..), rank-8 CP with column "
+                f"congruence U(0, 0.9) + 1 % noise; network trained on {args.train_samples} "
+                f"generated tensors; ALS to |e_(s-1) - e_s| < {tol} (abs_rec_error), "
+                f"at most {max_sweeps} sweeps")
     if args.impl == "reference":
         v, dt = _learned_cpu_sample(seeds, 8, tol, max_sweeps)
         line = {"metric": LEARNED_METRIC, "value": v, "unit": "decomps/s", "n_gpus": args.gpus,
@@ -556,12 +558,13 @@ def run_learned(args):
     torch.cuda.synchronize()
     st = torch.cuda.current_stream()
 
-    def step():   # the learned path: sketch, inference, ALS to tol
-        feats, xnorm = learned.sketch(X, gen.omega)
-        return learned._als(X, net.predict(X, feats, xnorm), max_sweeps, tol=tol)
+    def step():   # the learned path: sketch, inference, SVD fallback, ALS to tol
+        F, _, _ = learned.warm_start(net, X, gen.omega)
+        return learned._als(X, F, max_sweeps, tol=tol)
 
     for _ in range(args.warmup):
         step()
+    fallback_any = bool(learned.warm_start(net, X, gen.omega)[1].any().item())
     torch.cuda.synchronize()
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
@@ -584,14 +587,13 @@ def run_learned(args):
     e1.record(st)
     torch.cuda.synchronize()
     infer_ms = e0.elapsed_time(e1) / 5
-    res = learned.evaluate(net, seeds, max_sweeps=max_sweeps, tol=tol, probe=probe, generator=gen)
+    res = learned.evaluate(net, seeds, max_sweeps=max_sweeps, tol=tol, generator=gen)
     # end to end: host tensors in, factors and errors back
     Xh = X.cpu().numpy().reshape(n, 32, 32, 32)
     torch.cuda.synchronize()
     h0 = time.perf_counter()
     Xd = torch.from_numpy(Xh).to(dev).reshape(n, -1)
-    feats, xnorm = learned.sketch(Xd, gen.omega)
-    pe = learned._als(Xd, net.predict(Xd, feats, xnorm), max_sweeps, tol=tol)
+    pe = learned._als(Xd, learned.warm_start(net, Xd, gen.omega)[0], max_sweeps, tol=tol)
     fb = pe.fbuf.cpu()
     fe = pe.final.cpu()
     e2e_s = time.perf_counter() - h0
@@ -606,13 +608,14 @@ def run_learned(args):
         return {"sweeps_mean": float(v.mean()), "sweeps_median": float(np.median(v)),
                 "sweeps_p90": float(np.percentile(v, 90)), "ms": res["ms_" + k],
                 "decomps_per_s": n / (res["ms_" + k] / 1000.0),
+                "frac_at_cap": float((v >= max_sweeps).mean()),
                 "median_final_err": float(np.median(res["err_" + k]))}
 
     line = {"metric": LEARNED_METRIC, "value": n / (ms / 1000.0), "unit": "decomps/s",
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": workload, "l2": "0.54 GB of tensors > L2",
+            "config": {"workload": workload, "l2": "1.3 GB of tensors > L2",
                        "network": "1536-1024-512-768 MLP + sketch skip, "
                                   f"{net.n_params} parameters"},
             "training": {"samples": args.train_samples, "seconds": train_s,
@@ -626,8 +629,9 @@ def run_learned(args):
             "e2e": {"value": n / e2e_s, "unit": "decomps/s",
                     "h2d_bytes_per_step": int(Xh.nbytes),
                     "d2h_bytes_per_step": int(fb.numel() * 4 + fe.numel() * 8)},
-            # per step: sketch, 3 GEMMs + skip, loss/scale, lift, the batched ALS kernel
-            "clocks": clk, "gpu_launches": 8 * args.steps}
+            # per step: sketch, 3 GEMMs + skip, loss/scale, lift, the batched ALS
+            # kernel (+ gram3, eig and scale when a tensor falls back to the SVD start)
+            "clocks": clk, "gpu_launches": (8 + (3 if fallback_any else 0)) * args.steps}
     print(json.dumps(line), flush=True)
 
 

@@ -13,11 +13,12 @@ scale, 1 - <X, [[A]]>^2 / (||X||^2 ||[[A]]||^2), which is invariant to the
 order and scaling of the components and, unlike the plain error, has no
 saddle at a zero output.
 
-Plain ALS judges the prediction: ``warm_start`` runs ``probe`` sweeps from the
-network's factors and from TensorLy's ``init='svd'`` factors
-(tensorly/decomposition/_cp.py:70-96) and keeps, per tensor, whichever start
-is ahead after them (continuing from that state), so a tensor the network
-does not help falls back to the reference's default start.
+``warm_start`` falls back, per tensor, to TensorLy's ``init='svd'`` factors
+(tensorly/decomposition/_cp.py:70-96) when the network's model explains
+almost nothing of the tensor (or, with ``probe`` > 0, when the SVD start is
+ahead after that many plain ALS sweeps).  Plain ALS convergence judges the network: ``evaluate`` counts
+the sweeps and times the whole path to the reference's stop test from each
+start.
 """
 
 import ctypes
@@ -176,14 +177,15 @@ class WarmStartNet:
                                               ptr(alpha), _stream(out)))
         return loss, out, alpha
 
-    def predict(self, X, feats, xnorm):
+    def predict(self, X, feats, xnorm, return_loss=False):
         """Initial factors (batch x 3 x 32 x 8) for the tensors X with
-        sketch features ``feats``: the network's factors at their best scale."""
-        _, out, alpha = self.loss(X, feats, xnorm)
+        sketch features ``feats``: the network's factors at their best scale
+        (and, with ``return_loss``, their relative error squared)."""
+        loss, out, alpha = self.loss(X, feats, xnorm)
         F = torch.empty((feats.shape[0], 3, I, R), dtype=torch.float32, device=self.device)
         _lib.check(_lib.lib().tlgb_ws_lift(ptr(out), ptr(xnorm), ptr(alpha), feats.shape[0],
                                            ptr(F), _stream(out)))
-        return F
+        return (F, loss) if return_loss else F
 
     def state_dict(self):
         return {"params": self.params.cpu().numpy(), "step": self.step}
@@ -223,20 +225,31 @@ def sketch(X, omega):
     return feats, xnorm
 
 
-def warm_start(net, X, omega, probe=5):
-    """Initial factors (batch x 3 x 32 x 8) for ALS on X (batch x 32768).
+def warm_start(net, X, omega, probe=0, max_err=0.99):
+    """Initial factors (batch x 3 x 32 x 8) for ALS on X (batch x 32768), with
+    TensorLy's init='svd' as the fallback.
 
-    ``probe`` ALS sweeps run from the network's factors and from the SVD
-    start; per tensor the one with the lower relative error afterwards is
-    kept, in its state after the probe.  Returns (factors, used_svd,
-    probe sweeps taken)."""
+    ``probe`` = 0: the network's start, replaced by the SVD start for the
+    tensors whose predicted model explains almost nothing (relative error at
+    its best scale >= ``max_err``, read from the loss the prediction already
+    computes); the SVD start is computed for those tensors only.
+    ``probe`` > 0: plain ALS judges instead: ``probe`` sweeps run from both
+    starts and the one with the lower error afterwards is kept, in its state
+    after the probe.  Returns (factors, used_svd, probe sweeps taken)."""
     feats, xnorm = sketch(X, omega)
     b = X.shape[0]
-    pl = _als(X, net.predict(X, feats, xnorm), probe)
-    ps = _als(X, svd_init(X), probe)
-    use_svd = ps.final <= pl.final
-    F = torch.where(use_svd[:, None], ps.fbuf.view(b, -1), pl.fbuf.view(b, -1))
-    return F.view(b, 3, I, R), use_svd, probe
+    if probe > 0:
+        pl = _als(X, net.predict(X, feats, xnorm), probe)
+        ps = _als(X, svd_init(X), probe)
+        use_svd = ps.final < pl.final
+        F = torch.where(use_svd[:, None], ps.fbuf.view(b, -1), pl.fbuf.view(b, -1))
+        return F.view(b, 3, I, R), use_svd, probe
+    F, loss = net.predict(X, feats, xnorm, return_loss=True)
+    use_svd = loss >= max_err * max_err
+    idx = torch.nonzero(use_svd).flatten()
+    if idx.numel():
+        F[idx] = svd_init(X[idx].contiguous())
+    return F, use_svd, 0
 
 
 def sweeps_to_tol(sweep_errs, tol):
@@ -247,12 +260,13 @@ def sweeps_to_tol(sweep_errs, tol):
     return np.where(d.any(axis=1), d.argmax(axis=1) + 2, e.shape[1])
 
 
-def evaluate(net, seeds, max_sweeps=300, tol=1e-8, probe=5, generator=None, batch=4096):
+def evaluate(net, seeds, max_sweeps=300, tol=1e-6, probe=0, generator=None, batch=10000,
+             max_err=0.99):
     """Time-to-fit on the tensors of ``seeds``: batched ALS with the
     reference's stop test (tol, 'abs_rec_error') from init='svd', from the
     network's start alone (sketch + inference included) and from the
-    ALS-judged ``warm_start`` (its probe sweeps included), each timed with
-    CUDA events over the whole path."""
+    ``warm_start`` with its SVD fallback (and probe sweeps, if any), each
+    timed with CUDA events over the whole path."""
     gen = generator or Generator(net.device)
     keys = ("sweeps_svd", "sweeps_learned", "sweeps_warm", "used_svd", "err_svd",
             "err_learned", "err_warm")
@@ -261,7 +275,7 @@ def evaluate(net, seeds, max_sweeps=300, tol=1e-8, probe=5, generator=None, batc
     seeds = np.asarray(seeds)
     Xw, _, _ = gen(seeds[:8])             # warm-up: first launches and module loads untimed
     _als(Xw, svd_init(Xw), 2, tol=tol)
-    _als(Xw, warm_start(net, Xw, gen.omega, probe)[0], 2, tol=tol)
+    _als(Xw, warm_start(net, Xw, gen.omega, probe, max_err)[0], 2, tol=tol)
     for b0 in range(0, len(seeds), batch):
         X, _, _ = gen(seeds[b0:b0 + batch])
         torch.cuda.synchronize()
@@ -272,7 +286,7 @@ def evaluate(net, seeds, max_sweeps=300, tol=1e-8, probe=5, generator=None, batc
         feats, xnorm = sketch(X, gen.omega)
         pl = _als(X, net.predict(X, feats, xnorm), max_sweeps, tol=tol)
         ev[2].record()
-        F, used, probe_n = warm_start(net, X, gen.omega, probe)
+        F, used, probe_n = warm_start(net, X, gen.omega, probe, max_err)
         pw = _als(X, F, max_sweeps - probe_n, tol=tol)
         ev[3].record()
         torch.cuda.synchronize()

@@ -172,12 +172,13 @@ def test_training_reduces_loss(trained):
 
 def test_warm_start_gain_over_svd_start(ws, gen, trained):
     """What the trained network gains: sweeps and time to the reference's stop
-    test (tol 1e-8) on held-out tensors, from init='svd', from the network's
-    start and from the ALS-judged warm start; the fit must match."""
+    test (tol 1e-6) on held-out tensors, from init='svd', from the network's
+    start and from the warm start with its SVD fallback; the fit must match."""
     net, _ = trained
     untrained = ws.WarmStartNet(seed=0)
     seeds = np.arange(10 ** 6, 10 ** 6 + 1024)
-    res = ws.evaluate(net, seeds, max_sweeps=300, tol=1e-8, probe=5, generator=gen)
+    res = ws.evaluate(net, seeds, max_sweeps=300, tol=1e-6, generator=gen)
+    res5 = ws.evaluate(net, seeds[:256], max_sweeps=300, tol=1e-6, probe=5, generator=gen)
     X, feats, nrm = gen(seeds)
     loss_tr = net.loss(X, feats, nrm)[0].mean().item()
     loss_un = untrained.loss(X, feats, nrm)[0].mean().item()
@@ -187,12 +188,24 @@ def test_warm_start_gain_over_svd_start(ws, gen, trained):
         v = res["sweeps_" + k]
         print("start %-8s sweeps to tol mean %.1f median %.0f p90 %.0f; time to fit %.2f ms"
               % (k, v.mean(), np.median(v), np.percentile(v, 90), res["ms_" + k]))
-    print("network start kept by the judge for %.1f %% of tensors" % (100 * (1 - res["used_svd"].mean())))
+    print("network start kept by the fallback test for %.1f %% of tensors"
+          % (100 * (1 - res["used_svd"].mean())))
+    resu = ws.evaluate(untrained, seeds, max_sweeps=300, tol=1e-6, generator=gen)
+    print("untrained network (the sketch skip alone): %.1f mean sweeps from its start"
+          % resu["sweeps_learned"].mean())
+    resc = ws.evaluate(net, seeds[:256], max_sweeps=300, tol=1e-6, generator=gen, max_err=0.0)
+    print("falling back for every tensor (256 tensors): svd %.1f, warm %.1f mean sweeps"
+          % (resc["sweeps_svd"].mean(), resc["sweeps_warm"].mean()))
+    np.testing.assert_array_equal(resc["sweeps_warm"], resc["sweeps_svd"])
+    print("with 5 ALS probe sweeps as the judge (256 tensors): svd %.1f, warm %.1f mean sweeps, "
+          "network kept for %.1f %%" % (res5["sweeps_svd"].mean(), res5["sweeps_warm"].mean(),
+                                         100 * (1 - res5["used_svd"].mean())))
+    assert (res5["sweeps_warm"] >= 5).all()
     assert loss_tr < loss_un
     for k in ("learned", "warm"):   # same fit as from the SVD start
         rel = (res["err_" + k] - res["err_svd"]) / res["err_svd"]
         assert abs(np.median(rel)) < 1e-4, (k, np.median(rel))
-    assert (res["sweeps_warm"] >= 5).all()
-    # measured on 4096 held-out tensors: 57.5 (judged) and 56.8 (network) mean
-    # sweeps against 60.4 from the SVD start
+    # measured at tol 1e-8 on 4096 held-out tensors: 56.8 mean sweeps from the
+    # network's start against 60.4 from the SVD start
     assert res["sweeps_learned"].mean() <= 1.02 * res["sweeps_svd"].mean()
+    assert res["sweeps_warm"].mean() <= 1.02 * res["sweeps_svd"].mean()
