@@ -618,13 +618,16 @@ def parafac_batched(tensors, ranks, n_iter_max=100, init="random", random_state=
     error (computed from the residual).  ``init``: ``'random'``
     (``random_state``: None, an int applied to every tensor, or one seed per
     tensor; the reference's draws, random/base.py:104) or a list of factor
-    lists.  Mode sizes 1..64, ranks 1..16.
+    lists, or one packed tensor of all initial factors (tensor-major, then
+    mode, each ``I_k x rank`` row-major).  ``tensors`` may be a list or one
+    ``(n, I0, I1, I2)`` tensor.  Mode sizes 1..64, ranks 1..16.
 
     Returns the list of ``CPTensor``; with ``return_errors`` also the final
     relative errors (from the residual, as a NumPy array), and with
     ``sweep_errors`` the per-sweep errors (n_tensors x n_iter_max).
     """
-    tensors = list(tensors)
+    if not (isinstance(tensors, torch.Tensor) and tensors.ndim == 4):
+        tensors = list(tensors)   # a (n, I0, I1, I2) tensor is packed as it is
     if len(tensors) == 0:
         return ([], np.zeros(0)) if return_errors else []
     prob = BatchedProblem(tensors, ranks, init=init, random_state=random_state)
