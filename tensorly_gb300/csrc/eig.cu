@@ -14,7 +14,7 @@
 //      round by a group of threads, so ~log_33 instead of log_2 rounds);
 //   3. eigenvectors of the tridiagonal matrix by inverse iteration (one
 //      thread per eigenvalue, LU with partial pivoting), re-orthogonalised
-//      within clusters of close eigenvalues;
+//      within clusters of close eigenvalues, in shared memory when they fit;
 //   4. back-transformation by the reflectors, then the sign convention of
 //      svd_flip (the largest-magnitude entry of every column is positive).
 // The eigenvalues come out in descending order, as LAPACK's singular values.
@@ -65,6 +65,21 @@ __device__ T block_sum_t(T v, T* red) {
   return r;
 }
 
+// Block-wide sum with a single barrier: warp partials go to `red` (kEigWarps
+// slots) and every thread adds them up.  `red` must not be written again
+// before a later barrier, so consecutive calls alternate between two buffers.
+template <typename T>
+__device__ __forceinline__ T block_sum_1(T v, T* red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  v = warp_sum_t(v);
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  T t = T(0);
+#pragma unroll
+  for (int w = 0; w < kEigWarps; ++w) t += red[w];
+  return t;
+}
+
 // Number of eigenvalues of tridiag(d, e) below x (Sturm count); e2 = e^2.
 template <typename T>
 __device__ int sturm_count(const T* d, const T* e2, int n, T x) {
@@ -80,38 +95,43 @@ __device__ int sturm_count(const T* d, const T* e2, int n, T x) {
 }
 
 // A: n x n symmetric (row-major, both triangles).  Outputs: U (n x k,
-// row-major), lam (k), descending.  Z: workspace k x n; W: workspace k x 5n.
+// row-major), lam (k), descending.  Zg: global workspace of 6 k n elements per
+// matrix; with zsm the k eigenvectors and the three diagonals of their
+// triangular factors live in shared memory instead (4 k n elements).
 template <typename T>
 __global__ void __launch_bounds__(kEigThreads)
-k_sym_eig(const T* __restrict__ A, int n, int k, T* U, T* lam, int flip, T* Z, T* W) {
+k_sym_eig(const T* __restrict__ A, int n, int k, T* U, T* lam, int flip, T* Zg, int zsm) {
   // batched launches: CTA b solves matrix b (every operand advanced by its size)
   A += (int64_t)blockIdx.x * n * n;
   U += (int64_t)blockIdx.x * n * k;
   lam += (int64_t)blockIdx.x * k;
-  Z += (int64_t)blockIdx.x * 6 * k * n;
-  W = Z + (int64_t)k * n;
+  Zg += (int64_t)blockIdx.x * 6 * k * n;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* As = reinterpret_cast<T*>(smem_raw);   // n * n
   T* d = As + n * n;                         // n
   T* e = d + n;                              // n
   T* e2 = e + n;                             // n
   T* tau = e2 + n;                           // n
-  T* red = tau + n;                          // 32
-  T* bnd = red + 32;                         // 2 * kEigThreads (multisection bounds)
+  T* red = tau + n;                          // 32 (two halves for block_sum_1)
+  T* bnd = red + 32;                         // 2 * kEigThreads (multisection bounds, scratch)
+  T* Zb = zsm ? bnd + 2 * kEigThreads : Zg;  // k * n eigenvectors, then 3 * k * n
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
   for (int i = tid; i < n * n; i += kEigThreads) As[i] = A[i];
   for (int i = tid; i < n; i += kEigThreads) { e[i] = T(0); tau[i] = T(0); }
   __syncthreads();
 
-  // ---- 1. tridiagonalisation (reflector j zeroes column j below the subdiagonal)
+  // ---- 1. tridiagonalisation.  Reflector j zeroes column j below the
+  // subdiagonal; it is read from, and stored in, row j right of the diagonal
+  // (the same values by symmetry, contiguous, and no longer needed by the
+  // updates, which touch rows and columns > j only).
   for (int j = 0; j + 2 < n; ++j) {
     const int m = n - j - 1;               // length of the reflected part
-    T* col = As + (j + 1) * n + j;         // stride n
+    T* x = As + j * n + j + 1;
     T s2 = T(0);
-    for (int i = 1 + tid; i < m; i += kEigThreads) s2 += col[i * n] * col[i * n];
-    s2 = block_sum_t(s2, red);
-    const T alpha = col[0];
+    for (int i = 1 + tid; i < m; i += kEigThreads) s2 += x[i] * x[i];
+    s2 = block_sum_1(s2, red);
+    const T alpha = x[0];
     T t = T(0), beta = alpha, scale = T(0);
     if (s2 > T(0)) {
       const T mu = sqrt(alpha * alpha + s2);
@@ -119,31 +139,41 @@ k_sym_eig(const T* __restrict__ A, int n, int k, T* U, T* lam, int flip, T* Z, T
       t = (beta - alpha) / beta;
       scale = T(1) / (alpha - beta);
     }
-    __syncthreads();   // all threads have read col[0] before it is overwritten
-    if (tid == 0) { e[j] = beta; tau[j] = t; d[j] = As[j * n + j]; col[0] = T(1); }
+    __syncthreads();   // all threads have read x[0] before it is overwritten
+    if (tid == 0) { e[j] = beta; tau[j] = t; d[j] = As[j * n + j]; x[0] = T(1); }
     if (t != T(0))
-      for (int i = 1 + tid; i < m; i += kEigThreads) col[i * n] *= scale;
+      for (int i = 1 + tid; i < m; i += kEigThreads) x[i] *= scale;
     __syncthreads();
     if (t == T(0)) continue;
-    // p = t * A22 v (one warp per row, lanes across the row)
+    // p = t * A22 v: row r of A22 read as its column r (symmetric), so
+    // consecutive threads read consecutive addresses; H groups split the sum
     T* A22 = As + (j + 1) * n + (j + 1);
-    for (int r = warp; r < m; r += kEigWarps) {
-      T acc = T(0);
-      for (int c = lane; c < m; c += 32) acc += A22[r * n + c] * col[c * n];
-      acc = warp_sum_t(acc);
-      if (lane == 0) e2[r] = t * acc;      // e2 holds p until the loop ends
+    const int H = kEigThreads / m;         // >= 2 (m < n <= 224)
+    {
+      const int r = tid % m, h = tid / m;
+      if (h < H) {
+        T acc = T(0);
+        for (int c = h; c < m; c += H) acc += A22[c * n + r] * x[c];
+        bnd[h * m + r] = acc;
+      }
     }
     __syncthreads();
     T pv = T(0);
-    for (int i = tid; i < m; i += kEigThreads) pv += e2[i] * col[i * n];
-    pv = block_sum_t(pv, red);
+    for (int r = tid; r < m; r += kEigThreads) {
+      T acc = T(0);
+      for (int h = 0; h < H; ++h) acc += bnd[h * m + r];
+      e2[r] = t * acc;                     // e2 holds p, then w, until the loop ends
+      pv += e2[r] * x[r];
+    }
+    pv = block_sum_1(pv, red + kEigWarps);
     const T K = T(0.5) * t * pv;
-    for (int i = tid; i < m; i += kEigThreads) e2[i] -= K * col[i * n];   // w
+    for (int r = tid; r < m; r += kEigThreads) e2[r] -= K * x[r];   // w
     __syncthreads();
-    // A22 -= v w^T + w v^T
-    for (int idx = tid; idx < m * m; idx += kEigThreads) {
-      const int r = idx / m, c = idx - (idx / m) * m;
-      A22[r * n + c] -= col[r * n] * e2[c] + e2[r] * col[c * n];
+    // A22 -= v w^T + w v^T (warp per row, lanes along it)
+    for (int r = warp; r < m; r += kEigWarps) {
+      const T vr = x[r], wr = e2[r];
+      T* row = A22 + r * n;
+      for (int c = lane; c < m; c += 32) row[c] -= vr * e2[c] + wr * x[c];
     }
     __syncthreads();
   }
@@ -213,50 +243,48 @@ k_sym_eig(const T* __restrict__ A, int n, int k, T* U, T* lam, int flip, T* Z, T
   // ---- 3. eigenvectors of the tridiagonal matrix by inverse iteration
   const T pert = T(10) * EigLimits<T>::eps * tnorm + EigLimits<T>::tiny;
   for (int c = tid; c < k; c += kEigThreads) {
-    T* z = Z + (int64_t)c * n;
-    T* la = W + (int64_t)c * 5 * n;   // LU of (T - mu I): diag, super, second super, sub multipliers
-    T* lb = la + n;
-    T* lc = lb + n;
-    T* lm = lc + n;
-    T* piv = lm + n;                  // 1 if rows i, i+1 were swapped
+    T* z = Zb + (int64_t)c * n;
+    T* ua = Zb + (int64_t)k * n + (int64_t)c * 3 * n;   // U of the LU of (T - mu I):
+    T* ub = ua + n;                                      // diagonal and two superdiagonals
+    T* uc = ub + n;
     // nudge mu off the eigenvalue (alternating direction per index) so the
     // LU is non-singular; the shift is far below the eigenvalue's accuracy
     const T mu = lam[c] + ((c & 1) ? pert : -pert);
-    // factor T - mu I with partial pivoting (tridiagonal, fill in one super)
-    T a_i = d[0] - mu, b_i = (n > 1) ? e[0] : T(0);
-    for (int i = 0; i < n; ++i) {
-      if (i + 1 < n) {
-        const T sub = e[i];
-        const T a_n = d[i + 1] - mu;
-        const T b_n = (i + 2 < n) ? e[i + 1] : T(0);
-        if (fabs(sub) > fabs(a_i)) {   // swap rows i and i+1
-          const T mult = a_i / sub;
-          la[i] = sub; lb[i] = a_n; lc[i] = b_n; lm[i] = mult; piv[i] = T(1);
-          a_i = b_i - mult * a_n;
-          b_i = -mult * b_n;
-        } else {
-          const T div = (a_i == T(0)) ? pert : a_i;
-          const T mult = sub / div;
-          la[i] = div; lb[i] = b_i; lc[i] = T(0); lm[i] = mult; piv[i] = T(0);
-          a_i = a_n - mult * b_i;
-          b_i = b_n;
-        }
-      } else {
-        la[i] = (a_i == T(0)) ? pert : a_i;
-        lb[i] = T(0); lc[i] = T(0); lm[i] = T(0); piv[i] = T(0);
-      }
-    }
     // start vector: deterministic, no special alignment with any eigenvector
     for (int i = 0; i < n; ++i) z[i] = T(1) + T(0.01) * (T)((i * 7 + c * 3) % 11);
     for (int iter = 0; iter < 3; ++iter) {
-      for (int i = 0; i + 1 < n; ++i) {   // forward: apply row swaps and multipliers
-        if (piv[i] != T(0)) { const T tmp = z[i]; z[i] = z[i + 1]; z[i + 1] = tmp; }
-        z[i + 1] -= lm[i] * z[i];
+      // LU with partial pivoting (tridiagonal, fill in one super), its row
+      // swaps and multipliers applied to z on the way (only U is kept)
+      T a_i = d[0] - mu, b_i = (n > 1) ? e[0] : T(0);
+      T zi = z[0];
+      for (int i = 0; i + 1 < n; ++i) {
+        const T sub = e[i];
+        const T a_n = d[i + 1] - mu;
+        const T b_n = (i + 2 < n) ? e[i + 1] : T(0);
+        const T zn = z[i + 1];
+        if (fabs(sub) > fabs(a_i)) {   // swap rows i and i+1
+          const T mult = a_i / sub;
+          ua[i] = sub; ub[i] = a_n; uc[i] = b_n;
+          a_i = b_i - mult * a_n;
+          b_i = -mult * b_n;
+          z[i] = zn;
+          zi = zi - mult * zn;
+        } else {
+          const T div = (a_i == T(0)) ? pert : a_i;
+          const T mult = sub / div;
+          ua[i] = div; ub[i] = b_i; uc[i] = T(0);
+          a_i = a_n - mult * b_i;
+          b_i = b_n;
+          z[i] = zi;
+          zi = zn - mult * zi;
+        }
       }
-      z[n - 1] = z[n - 1] / la[n - 1];   // back substitution with U (diag, two supers)
-      if (n >= 2) z[n - 2] = (z[n - 2] - lb[n - 2] * z[n - 1]) / la[n - 2];
+      ua[n - 1] = (a_i == T(0)) ? pert : a_i;
+      z[n - 1] = zi;
+      z[n - 1] = z[n - 1] / ua[n - 1];   // back substitution with U (diag, two supers)
+      if (n >= 2) z[n - 2] = (z[n - 2] - ub[n - 2] * z[n - 1]) / ua[n - 2];
       for (int i = n - 3; i >= 0; --i)
-        z[i] = (z[i] - lb[i] * z[i + 1] - lc[i] * z[i + 2]) / la[i];
+        z[i] = (z[i] - ub[i] * z[i + 1] - uc[i] * z[i + 2]) / ua[i];
       T nrm = T(0);
       for (int i = 0; i < n; ++i) nrm += z[i] * z[i];
       nrm = T(1) / sqrt(nrm);
@@ -270,9 +298,9 @@ k_sym_eig(const T* __restrict__ A, int n, int k, T* U, T* lam, int flip, T* Z, T
     if (fabs(lam[c - 1] - lam[c]) > clus) continue;
     int c0 = c - 1;
     while (c0 > 0 && fabs(lam[c0 - 1] - lam[c0]) <= clus) --c0;
-    T* zc = Z + (int64_t)c * n;
+    T* zc = Zb + (int64_t)c * n;
     for (int q = c0; q < c; ++q) {
-      const T* zq = Z + (int64_t)q * n;
+      const T* zq = Zb + (int64_t)q * n;
       T dot = T(0);
       for (int i = tid; i < n; i += kEigThreads) dot += zq[i] * zc[i];
       dot = block_sum_t(dot, red);
@@ -289,16 +317,16 @@ k_sym_eig(const T* __restrict__ A, int n, int k, T* U, T* lam, int flip, T* Z, T
 
   // ---- 4. back-transformation (one warp per vector) and svd_flip signs
   for (int c = warp; c < k; c += kEigWarps) {
-    T* z = Z + (int64_t)c * n;
+    T* z = Zb + (int64_t)c * n;
     for (int j = n - 3; j >= 0; --j) {
       const T tj = tau[j];
       if (tj == T(0)) continue;
       const int m = n - j - 1;
-      const T* v = As + (j + 1) * n + j;    // v[0] = 1 stored explicitly
+      const T* v = As + j * n + j + 1;      // row j, v[0] = 1 stored explicitly
       T s = T(0);
-      for (int i = lane; i < m; i += 32) s += v[i * n] * z[j + 1 + i];
+      for (int i = lane; i < m; i += 32) s += v[i] * z[j + 1 + i];
       s = tj * warp_sum_t(s);
-      for (int i = lane; i < m; i += 32) z[j + 1 + i] -= s * v[i * n];
+      for (int i = lane; i < m; i += 32) z[j + 1 + i] -= s * v[i];
       __syncwarp();
     }
     // first index of the largest |z| (ties resolved to the lowest index)
@@ -319,9 +347,16 @@ k_sym_eig(const T* __restrict__ A, int n, int k, T* U, T* lam, int flip, T* Z, T
   }
 }
 
+constexpr size_t kEigSmemLimit = 227 * 1024;
+
 template <typename T>
 size_t eig_smem(int n) {
   return ((size_t)n * n + 4 * (size_t)n + 32 + 2 * kEigThreads) * sizeof(T);
+}
+// with the eigenvectors and triangular factors in shared memory as well
+template <typename T>
+size_t eig_smem_z(int n, int k) {
+  return eig_smem<T>(n) + 4 * (size_t)k * n * sizeof(T);
 }
 
 }  // namespace
@@ -353,11 +388,13 @@ int sym_eig_batched_launch(const T* A, int n, int k, int batch, T* U, T* lam, in
   const int dev = current_device();
   if (dev >= 0 && dev < 64 && !attr[dev]) {
     TLGB_CUDA_TRY(cudaFuncSetAttribute(k_sym_eig<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)eig_smem<T>(EigLimits<T>::max_n)));
+                                       (int)kEigSmemLimit));
     attr[dev] = true;
   }
   T* Z = static_cast<T*>(ws);
-  k_sym_eig<T><<<batch, kEigThreads, eig_smem<T>(n), st>>>(A, n, k, U, lam, flip, Z, Z);
+  const int zsm = eig_smem_z<T>(n, k) <= kEigSmemLimit ? 1 : 0;
+  k_sym_eig<T><<<batch, kEigThreads, zsm ? eig_smem_z<T>(n, k) : eig_smem<T>(n), st>>>(
+      A, n, k, U, lam, flip, Z, zsm);
   TLGB_LAUNCH_CHECK();
   return TLGB_OK;
 }

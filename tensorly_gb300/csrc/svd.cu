@@ -132,19 +132,29 @@ __global__ void __launch_bounds__(kGThreads) k_gram_tiles(const T* __restrict__ 
 template <typename T>
 __global__ void k_gram_finish(const double* __restrict__ partial, int64_t Na, int nt, int npairs,
                               int splits, T* G) {
-  const int p0 = blockIdx.x;
+  // one thread per tile element: grid (elements / blockDim, tile pairs)
+  const int p0 = blockIdx.y;
   int p = p0, ta = 0;
   while (p >= nt - ta) { p -= nt - ta; ++ta; }
   const int tb = ta + p;
-  for (int e = threadIdx.x; e < kGT * kGT; e += blockDim.x) {
-    const int i = e / kGT, j = e % kGT;
-    const int64_t a = (int64_t)ta * kGT + i, b = (int64_t)tb * kGT + j;
-    if (a >= Na || b >= Na) continue;
-    double s = 0.0;
-    for (int q = 0; q < splits; ++q) s += partial[((int64_t)q * npairs + p0) * (kGT * kGT) + e];
-    G[a * Na + b] = (T)s;
-    G[b * Na + a] = (T)s;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= kGT * kGT) return;
+  const int i = e / kGT, j = e % kGT;
+  const int64_t a = (int64_t)ta * kGT + i, b = (int64_t)tb * kGT + j;
+  if (a >= Na || b >= Na) return;
+  // the split order of the sum is fixed, so the result is deterministic
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+  int q = 0;
+  for (; q + 3 < splits; q += 4) {
+    s0 += partial[((int64_t)q * npairs + p0) * (kGT * kGT) + e];
+    s1 += partial[((int64_t)(q + 1) * npairs + p0) * (kGT * kGT) + e];
+    s2 += partial[((int64_t)(q + 2) * npairs + p0) * (kGT * kGT) + e];
+    s3 += partial[((int64_t)(q + 3) * npairs + p0) * (kGT * kGT) + e];
   }
+  for (; q < splits; ++q) s0 += partial[((int64_t)q * npairs + p0) * (kGT * kGT) + e];
+  const double s = (s0 + s1) + (s2 + s3);
+  G[a * Na + b] = (T)s;
+  G[b * Na + a] = (T)s;
 }
 
 // U[i][c] = (sum_j M[i][j] V[j][c]) / S[c]  (M = unfold(X, mode), tall case)
@@ -213,7 +223,7 @@ int gram_make_plan(const Shape& sh, int mode, int side, GramPlan* out) {
   p.npairs = p.nt * (p.nt + 1) / 2;
   p.chunks = ceil_div(p.Nk, kGK);
   int64_t splits = std::max<int64_t>(1, ceil_div(2 * (int64_t)sm_count(), p.npairs));
-  splits = std::min<int64_t>(splits, std::max<int64_t>(1, p.chunks / 8));
+  splits = std::min<int64_t>(splits, std::max<int64_t>(1, p.chunks / 2));
   splits = std::min<int64_t>(splits, 65535);
   p.cps = ceil_div(p.chunks, splits);
   p.splits = (int)ceil_div(p.chunks, p.cps);
@@ -233,7 +243,9 @@ int gram_launch(const GramPlan& p, const T* X, T* G, double* partial, cudaStream
   TLGB_CHECK_ARG(p.npairs <= 2147483647, "gram: too many tiles");
   k_gram_tiles<T><<<dim3((unsigned)p.npairs, (unsigned)p.splits), kGThreads, 0, st>>>(X, g);
   TLGB_LAUNCH_CHECK();
-  k_gram_finish<T><<<(unsigned)p.npairs, 256, 0, st>>>(partial, p.Na, p.nt, p.npairs, p.splits, G);
+  TLGB_CHECK_ARG(p.npairs <= 65535, "gram: too many tile pairs for the finish grid");
+  k_gram_finish<T><<<dim3((kGT * kGT + 255) / 256, (unsigned)p.npairs), 256, 0, st>>>(
+      partial, p.Na, p.nt, p.npairs, p.splits, G);
   TLGB_LAUNCH_CHECK();
   return TLGB_OK;
 }

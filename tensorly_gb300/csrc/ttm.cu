@@ -7,6 +7,8 @@
 // contiguous one) and l is the batch; when T == 1 (last mode) M is l and the
 // contraction runs along the contiguous dimension.  SIMT f32 / f64 tiles,
 // 16-byte vector loads along whichever dimension is contiguous.
+#include <type_traits>
+
 #include "linalg.cuh"
 
 namespace tlgb {
@@ -177,6 +179,105 @@ __global__ void __launch_bounds__(kThreads) ttm_kernel(const TtmArgs<T> a) {
   }
 }
 
+// Small J (<= 32), contracted mode not the last: Y[l, j, t] = sum_i W(i, j)
+// X[l, i, t] streamed once.  A thread owns V consecutive t for one l and keeps
+// all JP (J padded) outputs for them in registers; X rows come straight from
+// global memory as V-wide vectors, kRowBatch rows in flight; W sits in shared
+// memory, padded to JP columns, and is read as broadcast vectors.  Per row a
+// thread issues one X load, JP/4 (f32) or JP/2 (f64) shared loads and JP * V
+// FMAs, so the kernel streams at the HBM rate instead of being issue-bound.
+constexpr int kStreamThreads = 128;
+constexpr int kRowBatch = 8;
+constexpr size_t kStreamSmemMax = 96 * 1024;   // W in shared memory: I * JP elements
+
+template <typename T, int JP, int V>
+__global__ void __launch_bounds__(kStreamThreads)
+ttm_stream_kernel(const T* __restrict__ X, const T* __restrict__ U, T* __restrict__ Y, int64_t L,
+                  int I, int64_t Tt, int J, int transpose) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* Ws = reinterpret_cast<T*>(smem_raw);   // [I][JP]
+  const int tid = threadIdx.x;
+  for (int e = tid; e < I * JP; e += kStreamThreads) {
+    const int i = e / JP, j = e - (e / JP) * JP;
+    Ws[e] = (j < J) ? (transpose ? U[(int64_t)i * J + j] : U[(int64_t)j * I + i]) : T(0);
+  }
+  __syncthreads();
+  using Vec = typename std::conditional<sizeof(T) == 4,
+      typename std::conditional<V == 4, float4, typename std::conditional<V == 2, float2, float>::type>::type,
+      typename std::conditional<V == 2, double2, double>::type>::type;
+  // threads over (l, t / V) jointly, so a short t range does not idle lanes
+  const int64_t tv = Tt / V;
+  const int64_t total = L * tv;
+  for (int64_t g = (int64_t)blockIdx.x * kStreamThreads + tid; g < total;
+       g += (int64_t)gridDim.x * kStreamThreads) {
+    const int64_t l = g / tv;
+    const int64_t t0 = (g - l * tv) * V;
+    const T* xp = X + (l * I) * Tt + t0;
+    T acc[JP][V];
+#pragma unroll
+    for (int j = 0; j < JP; ++j)
+#pragma unroll
+      for (int v = 0; v < V; ++v) acc[j][v] = T(0);
+    for (int i0 = 0; i0 < I; i0 += kRowBatch) {
+      T xs[kRowBatch][V];
+#pragma unroll
+      for (int u = 0; u < kRowBatch; ++u) {
+        if (i0 + u < I) {
+          const Vec x = __ldg(reinterpret_cast<const Vec*>(xp + (int64_t)(i0 + u) * Tt));
+          const T* xv = reinterpret_cast<const T*>(&x);
+#pragma unroll
+          for (int v = 0; v < V; ++v) xs[u][v] = xv[v];
+        } else {
+#pragma unroll
+          for (int v = 0; v < V; ++v) xs[u][v] = T(0);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kRowBatch; ++u) {
+        if (i0 + u < I) {
+          const T* w = Ws + (i0 + u) * JP;
+#pragma unroll
+          for (int j = 0; j < JP; ++j) {
+            const T wj = w[j];
+#pragma unroll
+            for (int v = 0; v < V; ++v) acc[j][v] = fma(wj, xs[u][v], acc[j][v]);
+          }
+        }
+      }
+    }
+    T* yp = Y + (l * J) * Tt + t0;
+#pragma unroll
+    for (int j = 0; j < JP; ++j) {
+      if (j < J) {
+        Vec o;
+        T* ov = reinterpret_cast<T*>(&o);
+#pragma unroll
+        for (int v = 0; v < V; ++v) ov[v] = acc[j][v];
+        *reinterpret_cast<Vec*>(yp + (int64_t)j * Tt) = o;
+      }
+    }
+  }
+}
+
+template <typename T, int JP, int V>
+int launch_stream(const T* X, const T* U, T* Y, int64_t L, int I, int64_t Tt, int J,
+                  int transpose, cudaStream_t st) {
+  const size_t smem = (size_t)I * JP * sizeof(T);
+  static bool attr[64] = {};
+  const int dev = current_device();
+  if (dev >= 0 && dev < 64 && !attr[dev]) {
+    TLGB_CUDA_TRY(cudaFuncSetAttribute(ttm_stream_kernel<T, JP, V>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)kStreamSmemMax));
+    attr[dev] = true;
+  }
+  const int64_t tb = std::min<int64_t>(ceil_div(L * (Tt / V), kStreamThreads), 1ll << 30);
+  dim3 grid((unsigned)tb);
+  ttm_stream_kernel<T, JP, V><<<grid, kStreamThreads, smem, st>>>(X, U, Y, L, I, Tt, J, transpose);
+  TLGB_LAUNCH_CHECK();
+  return TLGB_OK;
+}
+
 template <typename T, int BN>
 int launch(const TtmArgs<T>& a, cudaStream_t st) {
   constexpr int VEC = TVec<T>::n;
@@ -228,6 +329,26 @@ int ttm_typed(const T* X, const Shape& sh, const T* U, int64_t J, int transpose,
     a.vec_a = al && (I % VEC == 0);
   }
   if (a.M == 0 || a.N == 0 || a.B == 0) return TLGB_OK;
+  // streaming kernel: small J, contracted mode not last, vector-aligned rows
+  const bool yal = (reinterpret_cast<uintptr_t>(Y) % 16) == 0;
+  const int jp = J <= 4 ? 4 : J <= 8 ? 8 : J <= 16 ? 16 : 32;
+  if (Tt > 1 && J <= 32 && (size_t)I * jp * sizeof(T) <= kStreamSmemMax && al && yal) {
+    if constexpr (sizeof(T) == 4) {
+      if (Tt % 4 == 0) {
+        if (J <= 4) return launch_stream<T, 4, 4>(X, U, Y, L, (int)I, Tt, (int)J, transpose, st);
+        if (J <= 8) return launch_stream<T, 8, 4>(X, U, Y, L, (int)I, Tt, (int)J, transpose, st);
+        if (J <= 16) return launch_stream<T, 16, 4>(X, U, Y, L, (int)I, Tt, (int)J, transpose, st);
+        return launch_stream<T, 32, 2>(X, U, Y, L, (int)I, Tt, (int)J, transpose, st);
+      }
+    } else {
+      if (Tt % 2 == 0) {
+        if (J <= 4) return launch_stream<T, 4, 2>(X, U, Y, L, (int)I, Tt, (int)J, transpose, st);
+        if (J <= 8) return launch_stream<T, 8, 2>(X, U, Y, L, (int)I, Tt, (int)J, transpose, st);
+        if (J <= 16) return launch_stream<T, 16, 2>(X, U, Y, L, (int)I, Tt, (int)J, transpose, st);
+        return launch_stream<T, 32, 1>(X, U, Y, L, (int)I, Tt, (int)J, transpose, st);
+      }
+    }
+  }
   if (J <= 16) return launch<T, 16>(a, st);
   if (J <= 32) return launch<T, 32>(a, st);
   return launch<T, 64>(a, st);
