@@ -36,10 +36,12 @@ template <typename T>
 int ttm_launch(const T* X, const Shape& sh, const T* U, int64_t J, int transpose, int mode, T* Y,
                cudaStream_t st);
 
-// ---- left singular vectors of an unfolding (svd.cu): U (I x k), S (k)
+// ---- left singular vectors of an unfolding (svd.cu): U (I x k), S (k).
+// `input_done` (optional) is recorded on st once X is no longer read.
 size_t svd_unfolding_workspace(int dtype, const Shape& sh, int mode, int64_t k);
 template <typename T>
 int svd_unfolding_launch(const T* X, const Shape& sh, int mode, int k, T* U, T* S, int flip,
-                         void* ws, size_t ws_bytes, cudaStream_t st);
+                         void* ws, size_t ws_bytes, cudaStream_t st,
+                         cudaEvent_t input_done = nullptr);
 
 }  // namespace tlgb

@@ -298,7 +298,7 @@ size_t svd_unfolding_workspace(int dtype, const Shape& sh, int mode, int64_t k) 
 
 template <typename T>
 int svd_unfolding_launch(const T* X, const Shape& sh, int mode, int k, T* U, T* S, int flip,
-                         void* ws, size_t ws_bytes, cudaStream_t st) {
+                         void* ws, size_t ws_bytes, cudaStream_t st, cudaEvent_t input_done) {
   SvdLayout L;
   int rc = svd_layout(TypeCode<T>::value, sh, mode, k, &L);
   if (rc) return rc;
@@ -311,6 +311,7 @@ int svd_unfolding_launch(const T* X, const Shape& sh, int mode, int k, T* U, T* 
   rc = gram_launch<T>(L.gp, X, G, part, st);
   if (rc) return rc;
   if (!L.tall) {
+    if (input_done) TLGB_CUDA_TRY(cudaEventRecord(input_done, st));   // X is not read again
     rc = sym_eig_launch<T>(G, (int)L.n, k, U, S, flip, eigws, st);
     if (rc) return rc;
     k_sqrt_clamp<T><<<(k + 255) / 256, 256, 0, st>>>(S, k);
@@ -327,6 +328,7 @@ int svd_unfolding_launch(const T* X, const Shape& sh, int mode, int k, T* U, T* 
   const int64_t tot = L.I * k;
   k_unfold_times<T><<<(unsigned)ceil_div(tot, 256), 256, 0, st>>>(X, L.I, L.J, Lb, Tt, V, S, k, U);
   TLGB_LAUNCH_CHECK();
+  if (input_done) TLGB_CUDA_TRY(cudaEventRecord(input_done, st));
   if (flip) {
     k_flip_columns<T><<<(unsigned)ceil_div(k, 8), 256, 0, st>>>(U, L.I, k);
     TLGB_LAUNCH_CHECK();
@@ -335,9 +337,9 @@ int svd_unfolding_launch(const T* X, const Shape& sh, int mode, int k, T* U, T* 
 }
 
 template int svd_unfolding_launch<float>(const float*, const Shape&, int, int, float*, float*, int,
-                                         void*, size_t, cudaStream_t);
+                                         void*, size_t, cudaStream_t, cudaEvent_t);
 template int svd_unfolding_launch<double>(const double*, const Shape&, int, int, double*, double*,
-                                          int, void*, size_t, cudaStream_t);
+                                          int, void*, size_t, cudaStream_t, cudaEvent_t);
 
 }  // namespace tlgb
 

@@ -15,6 +15,12 @@
 // The chain intermediates ping-pong between two workspace buffers; the SVDs
 // come from the Gram eigensolver (svd.cu, eig.cu); one host sync per
 // iteration reads norm(core)^2 for the stop test, like the reference's.
+//
+// Overlap: a chain applies the factor updated just before it last.  Its other
+// products do not depend on that update, so they run on a second stream as
+// soon as the previous SVD has read its input (its Gram is done), underneath
+// the previous SVD's eigensolver, which occupies one SM.  The products are
+// the same; only their order differs from the reference's ascending order.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -35,15 +41,30 @@ struct TuckerGeom {
   int order[kMaxModes];
 };
 
-// Shapes along a chain: applying factors (sorted order, skipping position
-// `skip`, -1 for none) to X; returns the largest intermediate element count.
-int64_t chain_max(const TuckerGeom& g, int skip, int64_t* final_dims) {
-  int64_t cur[kMaxModes];
-  for (int k = 0; k < g.ndim; ++k) cur[k] = g.dim[k];
-  int64_t best = 0;
+// The factor indices a chain applies: ascending mode order without position
+// `skip` (-1: none), with index `last` (-1: none) moved to the end.
+int chain_list(const TuckerGeom& g, int skip, int last, int* list) {
+  int cnt = 0;
+  bool has_last = false;
   for (int q = 0; q < g.n_modes; ++q) {
     if (q == skip) continue;
     const int idx = g.order[q];
+    if (idx == last) { has_last = true; continue; }
+    list[cnt++] = idx;
+  }
+  if (has_last) list[cnt++] = last;
+  return cnt;
+}
+
+// Shapes along a chain; returns the largest intermediate element count.
+int64_t chain_max(const TuckerGeom& g, int skip, int last, int64_t* final_dims) {
+  int list[kMaxModes];
+  const int cnt = chain_list(g, skip, last, list);
+  int64_t cur[kMaxModes];
+  for (int k = 0; k < g.ndim; ++k) cur[k] = g.dim[k];
+  int64_t best = 0;
+  for (int q = 0; q < cnt; ++q) {
+    const int idx = list[q];
     cur[g.modes[idx]] = g.ranks[idx];
     int64_t n = 1;
     for (int k = 0; k < g.ndim; ++k) n *= cur[k];
@@ -53,6 +74,9 @@ int64_t chain_max(const TuckerGeom& g, int skip, int64_t* final_dims) {
     for (int k = 0; k < g.ndim; ++k) final_dims[k] = cur[k];
   return best;
 }
+
+// The factor updated just before position i's chain (-1: none pending).
+int prev_index(const TuckerGeom& g, int i) { return (i == 0) ? -1 : i - 1; }
 
 struct TuckerLayout {
   size_t buf_elems;      // each ping-pong buffer
@@ -67,7 +91,14 @@ template <typename T>
 int layout(const TuckerGeom& g, TuckerLayout* L) {
   const int dtype = TypeCode<T>::value;
   int64_t mx = 1;
-  for (int i = -1; i < g.n_modes; ++i) mx = std::max(mx, chain_max(g, i, nullptr));
+  for (int i = 0; i < g.n_modes; ++i) {   // the chains as run: mode i's, and the core's
+    int pos = 0;
+    while (g.order[pos] != i) ++pos;
+    mx = std::max(mx, chain_max(g, pos, prev_index(g, i), nullptr));
+    mx = std::max(mx, chain_max(g, pos, -1, nullptr));
+  }
+  mx = std::max(mx, chain_max(g, -1, g.n_modes - 1, nullptr));
+  mx = std::max(mx, chain_max(g, -1, -1, nullptr));
   L->buf_elems = (size_t)mx;
   size_t svdb = 0;
   int64_t kmax = 1;
@@ -133,6 +164,17 @@ int make_geom(int ndim, const int64_t* shape, int n_modes, const int* modes, con
   return TLGB_OK;
 }
 
+class StreamGuard {
+ public:
+  cudaStream_t s = nullptr;
+  ~StreamGuard() { if (s) cudaStreamDestroy(s); }
+};
+class EventGuard {
+ public:
+  cudaEvent_t e = nullptr;
+  ~EventGuard() { if (e) cudaEventDestroy(e); }
+};
+
 template <typename T>
 struct Hooi {
   const TuckerGeom& g;
@@ -143,26 +185,41 @@ struct Hooi {
   size_t svd_bytes;
   T* S;
   cudaStream_t st;
+  cudaStream_t aux;          // independent products of a chain
+  cudaEvent_t ev_in_free;    // the last SVD has read its input
+  cudaEvent_t ev_part;       // the aux part of a chain is done
+  bool pending = false;      // ev_in_free was recorded by the last SVD
 
-  // Applies the factors (transposed) in sorted order skipping position
-  // `skip` (-1: none); returns the result pointer and its dims.
-  int chain(int skip, const T** out, int64_t* dims) {
+  // Applies the factors (transposed), ascending mode order without position
+  // `skip` (-1: none), factor index `last` at the end; the products before it
+  // run on the aux stream when an SVD is pending.  Returns the result and dims.
+  int chain(int skip, int last, const T** out, int64_t* dims) {
+    int list[kMaxModes];
+    const int cnt = chain_list(g, skip, last, list);
+    const bool split = pending && cnt >= 2 && list[cnt - 1] == last;
     int64_t cur[kMaxModes];
     for (int k = 0; k < g.ndim; ++k) cur[k] = g.dim[k];
     const T* src = X;
     int which = 0;
-    for (int q = 0; q < g.n_modes; ++q) {
-      if (q == skip) continue;
-      const int idx = g.order[q];
+    if (split) TLGB_CUDA_TRY(cudaStreamWaitEvent(aux, ev_in_free, 0));
+    for (int q = 0; q < cnt; ++q) {
+      const int idx = list[q];
       const int mode = g.modes[idx];
+      const bool on_aux = split && q + 1 < cnt;
+      if (split && q + 1 == cnt) {
+        TLGB_CUDA_TRY(cudaEventRecord(ev_part, aux));
+        TLGB_CUDA_TRY(cudaStreamWaitEvent(st, ev_part, 0));
+      }
       Shape sh = make_shape(g.ndim, cur);
       T* dst = buf[which];
-      int rc = ttm_launch<T>(src, sh, factors[idx], g.ranks[idx], /*transpose=*/1, mode, dst, st);
+      int rc = ttm_launch<T>(src, sh, factors[idx], g.ranks[idx], /*transpose=*/1, mode, dst,
+                             on_aux ? aux : st);
       if (rc) return rc;
       cur[mode] = g.ranks[idx];
       src = dst;
       which ^= 1;
     }
+    pending = false;
     *out = src;
     for (int k = 0; k < g.ndim; ++k) dims[k] = cur[k];
     return TLGB_OK;
@@ -170,8 +227,10 @@ struct Hooi {
 
   int svd_into(const T* Y, const int64_t* dims, int idx) {
     Shape sh = make_shape(g.ndim, dims);
-    return svd_unfolding_launch<T>(Y, sh, g.modes[idx], (int)g.ranks[idx], factors[idx], S, 1,
-                                   svdws, svd_bytes, st);
+    int rc = svd_unfolding_launch<T>(Y, sh, g.modes[idx], (int)g.ranks[idx], factors[idx], S, 1,
+                                     svdws, svd_bytes, st, ev_in_free);
+    pending = (rc == TLGB_OK);
+    return rc;
   }
 };
 
@@ -189,9 +248,15 @@ int run(const T* X, const TuckerGeom& g, T* const* factors, T* core,
     TLGB_CHECK_ARG(factors[i] != nullptr, "tucker: missing factor pointer");
   TLGB_CHECK_ARG(core != nullptr, "tucker: null core");
   char* base = static_cast<char*>(ws);
+  StreamGuard aux;
+  EventGuard ev_in_free, ev_part;
+  TLGB_CUDA_TRY(cudaStreamCreateWithFlags(&aux.s, cudaStreamNonBlocking));
+  TLGB_CUDA_TRY(cudaEventCreateWithFlags(&ev_in_free.e, cudaEventDisableTiming));
+  TLGB_CUDA_TRY(cudaEventCreateWithFlags(&ev_part.e, cudaEventDisableTiming));
   Hooi<T> h{g, X, factors, {reinterpret_cast<T*>(base + L.off_buf0),
                             reinterpret_cast<T*>(base + L.off_buf1)},
-            base + L.off_svd, L.svd_bytes, reinterpret_cast<T*>(base + L.off_s), st};
+            base + L.off_svd, L.svd_bytes, reinterpret_cast<T*>(base + L.off_s), st,
+            aux.s, ev_in_free.e, ev_part.e};
   AlsCtrl* ctrl = reinterpret_cast<AlsCtrl*>(base + L.off_ctrl);
   double* part = reinterpret_cast<double*>(base + L.off_part);
   const int dtype = TypeCode<T>::value;
@@ -223,13 +288,13 @@ int run(const T* X, const TuckerGeom& g, T* const* factors, T* core,
       while (g.order[pos] != i) ++pos;
       const T* Y;
       int64_t dims[kMaxModes];
-      rc = h.chain(pos, &Y, dims);
+      rc = h.chain(pos, prev_index(g, i), &Y, dims);
       if (rc) return rc;
       rc = h.svd_into(Y, dims, i);
       if (rc) return rc;
     }
     const T* C;
-    rc = h.chain(-1, &C, cdims);
+    rc = h.chain(-1, g.n_modes - 1, &C, cdims);
     if (rc) return rc;
     int64_t cn = 1;
     for (int k = 0; k < g.ndim; ++k) cn *= cdims[k];
@@ -248,7 +313,8 @@ int run(const T* X, const TuckerGeom& g, T* const* factors, T* core,
   }
   if (o.n_iter_max <= 0) {   // no iteration: the core of the initial factors
     const T* C;
-    rc = h.chain(-1, &C, cdims);
+    h.pending = false;
+    rc = h.chain(-1, -1, &C, cdims);
     if (rc) return rc;
     int64_t cn = 1;
     for (int k = 0; k < g.ndim; ++k) cn *= cdims[k];
