@@ -49,10 +49,12 @@ def parse():
     p.add_argument("--refine", type=int, default=3)
     p.add_argument("--cpu-sweeps", type=int, default=40)
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--workload", default="dense", choices=["dense", "batched", "learned"],
+    p.add_argument("--workload", default="dense",
+                   choices=["dense", "batched", "learned", "tucker"],
                    help="dense: 512^3 rank-64 CP-ALS (the headline); batched: 4096 uneven "
-                        "3-way tensors, 100 sweeps each; learned: time to fit 4096 32^3 "
-                        "rank-8 tensors from the learned warm start vs init='svd'")
+                        "3-way tensors, 100 sweeps each; learned: time to fit 10000 32^3 "
+                        "rank-8 tensors from the learned warm start vs init='svd'; tucker: "
+                        "128^4 Tucker-HOOI rank 16^4 (20 iterations) and CP rank 32")
     p.add_argument("--train-samples", type=int, default=200_000,
                    help="learned: tensors the network is trained on (before the timed steps)")
     p.add_argument("--count", type=int, default=4096, help="batched: number of tensors")
@@ -635,12 +637,142 @@ def run_learned(args):
     print(json.dumps(line), flush=True)
 
 
+TUCKER_METRIC = "Tucker-HOOI iterations/s at 128^4 f32 rank 16^4 (init='svd' included)"
+
+
+def _tucker_cpu_sample(x, n_iter):
+    """The NumPy restatement of tucker (init='random', the SVD init alone takes
+    minutes on the host) for `n_iter` iterations: iterations/s."""
+    import oracle
+    t0 = time.perf_counter()
+    oracle.tucker(x, rank=[16] * 4, n_iter_max=n_iter, init="random", tol=0, random_state=0)
+    dt = time.perf_counter() - t0
+    return n_iter / dt, dt
+
+
+def run_tucker(args):
+    import torch
+    import tensorly_gb300 as tg
+    from tensorly_gb300 import _lib, workloads
+    ws_n, rank, _ = dist_env()
+    if rank != 0:
+        return
+    n_iter = 20
+    x_np = workloads.cp_tucker_4way()
+    workload = ("128^4 f32: rank-32 CP + 16^4 Tucker (orthonormal factors) + 1 % noise; "
+                f"tucker(rank=[16]*4, n_iter_max={n_iter}, tol=0, init='svd')")
+    if args.impl == "reference":
+        v, dt = _tucker_cpu_sample(x_np, 1)
+        line = {"metric": TUCKER_METRIC, "value": v, "unit": "iterations/s", "n_gpus": args.gpus,
+                "steps": 1, "warmup": 0, "ms_per_step": 1000.0 * dt, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "impl": "reference",
+                "config": {"workload": workload,
+                           "step": "1 HOOI iteration from init='random' (bounded sample)"},
+                "cpu_baseline": {"value": v, "unit": "iterations/s", "cores": os.cpu_count(),
+                                 "kind": "port", "sample": "1 HOOI iteration, NumPy restatement"},
+                "e2e": {"value": v, "unit": "iterations/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+    tg.build() if not os.path.exists(_lib.library_path()) else None
+    dev = torch.device("cuda", torch.cuda.current_device())
+    x = torch.from_numpy(x_np).to(dev)
+    st = torch.cuda.current_stream()
+
+    def step(it=n_iter):
+        return tg.tucker(x, rank=[16] * 4, n_iter_max=it, tol=0, init="svd")
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    ev[0].record(st)
+    for _ in range(args.steps):
+        core, factors = step()
+    ev[1].record(st)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = ev[0].elapsed_time(ev[1]) / args.steps
+    ev[2].record(st)
+    step(1)
+    ev[3].record(st)
+    torch.cuda.synchronize()
+    ms1 = ev[2].elapsed_time(ev[3])
+    rec = tg.tenalg.multi_mode_dot(core, factors)
+    rel_err = float(((x - rec).double().norm() / x.double().norm()).item())
+    # the first (largest) TTM of a chain alone: 1 GiB in, 128 MiB out
+    U = factors[1].t().contiguous()
+    tg.tenalg.mode_dot(x, U, 1)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(10):
+        tg.tenalg.mode_dot(x, U, 1)
+    e1.record(st)
+    torch.cuda.synchronize()
+    ttm_ms = e0.elapsed_time(e1) / 10
+    ttm_bytes = x.numel() * 4 + x.numel() // 8 * 4 + 16 * 128 * 4
+    peak, peak_kind = measured_peaks()
+    # CP at the same shape: rank 32, 30 sweeps, bf16 and native f32
+    init = tg.initialize_cp(x, 32, init="random", random_state=0)
+    cp = {}
+    for prec in ("bf16", "native"):
+        tg.parafac(x, 32, n_iter_max=2, tol=0, init=init, precision=prec)
+        torch.cuda.synchronize()
+        c0 = torch.cuda.Event(enable_timing=True)
+        c1 = torch.cuda.Event(enable_timing=True)
+        c0.record(st)
+        _, errs = tg.parafac(x, 32, n_iter_max=30, tol=0, init=init, precision=prec,
+                             return_errors=True)
+        c1.record(st)
+        torch.cuda.synchronize()
+        cp[prec] = {"sweeps_per_s": 30 / (c0.elapsed_time(c1) / 1000.0),
+                    "final_rel_err": float(errs[-1])}
+    # end to end: host tensor in, core and factors back
+    torch.cuda.synchronize()
+    h0 = time.perf_counter()
+    core_h, factors_h = tg.tucker(x_np, rank=[16] * 4, n_iter_max=n_iter, tol=0, init="svd")
+    e2e_s = time.perf_counter() - h0
+    cpu = None
+    if not args.no_cpu_baseline:
+        v, dt = _tucker_cpu_sample(x_np, 1)
+        cpu = {"value": v, "unit": "iterations/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"1 HOOI iteration from init='random' of the NumPy restatement ({dt:.1f} s)"}
+    line = {"metric": TUCKER_METRIC, "value": n_iter / (ms / 1000.0), "unit": "iterations/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": workload, "l2": "1 GiB input > L2"},
+            "ms_per_iteration_after_init": (ms - ms1) / (n_iter - 1),
+            "ms_init_plus_one_iteration": ms1,
+            "rel_err": rel_err,
+            "roofline": {"bound": "hbm", "kernel": "ttm_stream_kernel (first TTM of a chain)",
+                         "achieved": ttm_bytes / (ttm_ms / 1000.0) / 1e9, "peak": peak,
+                         "unit": "GB/s", "frac": ttm_bytes / (ttm_ms / 1000.0) / 1e9 / peak,
+                         "peak_source": peak_kind, "traffic": None, "ms": ttm_ms},
+            "cp_rank32_30_sweeps": cp,
+            "cpu_baseline": cpu,
+            "e2e": {"value": n_iter / e2e_s, "unit": "iterations/s",
+                    "h2d_bytes_per_step": int(x_np.nbytes),
+                    "d2h_bytes_per_step": int(np.prod(np.shape(core_h))) * 4 + 4 * 128 * 16 * 4},
+            # per call: norm (2), init 4 x (Gram tiles, finish, eig, sqrt), per iteration
+            # 4 x (3 TTMs + the 4 SVD kernels) + the core's 4 TTMs + its norm (2)
+            "clocks": clk, "gpu_launches": (18 + 34 * n_iter) * args.steps}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.workload == "batched":
         run_batched(args)
     elif args.workload == "learned":
         run_learned(args)
+    elif args.workload == "tucker":
+        run_tucker(args)
     elif args.impl == "reference":
         run_reference(args)
     else:
