@@ -568,13 +568,16 @@ __device__ __forceinline__ double sum_splits(const double* __restrict__ partial,
 //     (f64 FMA latency is long on this GPU, so long chains would dominate).
 //   fac_kind 0/1: forward/back substitution with the f64 Cholesky or LU
 //     factors, one warp per row.
-template <typename T>
+// RT > 0: the rank is the compile-time constant RT (R_in == RT), so the
+// rank loops unroll and the index arithmetic folds; RT == 0: runtime rank.
+template <typename T, int RT>
 __global__ void __launch_bounds__(kSolveThreads)
-k_solve(const T* __restrict__ partial, int splits, int64_t I, int R,
+k_solve(const T* __restrict__ partial, int splits, int64_t I, int R_in,
         const double* __restrict__ fac, const int* __restrict__ perm,
         const double* __restrict__ vmat, const float* __restrict__ w32, T* A,
         __nv_bfloat16* A_bt, double* gpart, double* ipart, AlsCtrl* ctrl, int64_t rpb,
         int mats_in_smem, int max_passes) {
+  const int R = (RT > 0) ? RT : R_in;
   if (ctrl->done) return;
   extern __shared__ double sm[];
   const int RR = R * R;
@@ -1164,10 +1167,19 @@ int als_launch_solve(const T* partial, int splits, int64_t I, int R, const doubl
   const int nbe = (int)ceil_div(I, rpb);
   int rc = als_prepare(TypeCode<T>::value);
   if (rc) return rc;
-  k_solve<T><<<nbe, kSolveThreads, solve_smem(R), st>>>(partial, splits, I, R, fac, perm, vmat,
-                                                        w32, A, A_bt, gpart, ipart, ctrl, rpb,
-                                                        R <= kSolveDfMaxRank ? 1 : 0,
-                                                        max_passes);
+  const int mats = R <= kSolveDfMaxRank ? 1 : 0;
+  if (R == 64)
+    k_solve<T, 64><<<nbe, kSolveThreads, solve_smem(R), st>>>(
+        partial, splits, I, R, fac, perm, vmat, w32, A, A_bt, gpart, ipart, ctrl, rpb, mats,
+        max_passes);
+  else if (R == 32)
+    k_solve<T, 32><<<nbe, kSolveThreads, solve_smem(R), st>>>(
+        partial, splits, I, R, fac, perm, vmat, w32, A, A_bt, gpart, ipart, ctrl, rpb, mats,
+        max_passes);
+  else
+    k_solve<T, 0><<<nbe, kSolveThreads, solve_smem(R), st>>>(
+        partial, splits, I, R, fac, perm, vmat, w32, A, A_bt, gpart, ipart, ctrl, rpb, mats,
+        max_passes);
   TLGB_LAUNCH_CHECK();
   *nblocks = nbe;
   return TLGB_OK;
@@ -1264,8 +1276,14 @@ static int als_prepare_typed() {
       (int)(((size_t)kMaxAlsRank * kMaxAlsRank + kGramRows * kMaxAlsRank) * sizeof(double))));
   size_t smax = 0;
   for (int r = 1; r <= kMaxAlsRank; ++r) smax = std::max(smax, solve_smem(r));
-  TLGB_CUDA_TRY(cudaFuncSetAttribute(k_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  TLGB_CUDA_TRY(cudaFuncSetAttribute(k_solve<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)smax));
+  TLGB_CUDA_TRY((cudaFuncSetAttribute(k_solve<T, 32>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)solve_smem(32))));
+  TLGB_CUDA_TRY((cudaFuncSetAttribute(k_solve<T, 64>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)solve_smem(64))));
   if (dev >= 0 && dev < 64) done[dev] = true;
   return TLGB_OK;
 }
