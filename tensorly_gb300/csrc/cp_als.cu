@@ -196,13 +196,25 @@ struct Runner {
     // weights (tensorly/tenalg/core_tenalg/_khatri_rao.py:71-73), so a 2-way
     // MTTKRP is unweighted there; kept for parity.
     const T* mw = (N == 2) ? nullptr : weights;
+    const int df = (sizeof(T) == 4 && R <= kSolveDfMaxRank) ? 1 : 0;
+    // The Gram reduction of a mode other than the last runs on the aux
+    // stream in front of the next mode's factorisation (the only consumer of
+    // that Gram), so the next MTTKRP does not wait for it.
+    int pending_mode = -1, pending_nb = 0;
     for (size_t mi = 0; mi < modes.size(); ++mi) {
       const int mode = modes[mi];
       const bool last = (mi + 1 == modes.size());
       TLGB_CUDA_TRY(cudaEventRecord(ev_fork, st));
       TLGB_CUDA_TRY(cudaStreamWaitEvent(aux, ev_fork, 0));
-      int rc = als_launch_factorize<T>(B.G, N, mode, (int)R, weights, o.l2_reg, B.fac, B.perm,
-                                       B.vmat, B.w32, B.ctrl, aux);
+      int rc;
+      if (pending_mode >= 0) {
+        rc = als_launch_gram_reduce(B.gpart, pending_nb, (int)R,
+                                    B.G + (size_t)pending_mode * RR, done, df, aux);
+        if (rc) return rc;
+        pending_mode = -1;
+      }
+      rc = als_launch_factorize<T>(B.G, N, mode, (int)R, weights, o.l2_reg, B.fac, B.perm,
+                                   B.vmat, B.w32, B.ctrl, aux);
       if (rc) return rc;
       TLGB_CUDA_TRY(cudaEventRecord(ev_join, aux));
       if (ev_mt[0][mode]) TLGB_CUDA_TRY(cudaEventRecord(ev_mt[0][mode], st));
@@ -251,15 +263,16 @@ struct Runner {
                                (tc && P->tc[mode].valid) ? 1 : kIrMaxPasses, &nb, st);
       if (rc) return rc;
       if (last) last_nb = nb;
-      const int df = (sizeof(T) == 4 && R <= kSolveDfMaxRank) ? 1 : 0;
-      if (last)   // the last mode's Gram reduction also computes the fit
+      if (last) {   // the last mode's Gram reduction also computes the fit (in order)
         rc = als_launch_gram_reduce_fit<T>(B.gpart, nb, (int)R, B.G, mode, N, df, weights,
                                            B.ipart, nb, B.fpart, B.ctrl, B.errors, o.n_iter_max,
                                            o.tol,
                                            o.cvg_criterion, st);
-      else
-        rc = als_launch_gram_reduce(B.gpart, nb, (int)R, B.G + (size_t)mode * RR, done, df, st);
-      if (rc) return rc;
+        if (rc) return rc;
+      } else {      // reduced on the aux stream before the next factorisation
+        pending_mode = mode;
+        pending_nb = nb;
+      }
     }
     int rc = TLGB_OK;
     if (o.normalize_factors) {
