@@ -107,29 +107,35 @@ k_sym_eig(const T* __restrict__ A, int n, int k, T* U, T* lam, int flip, T* Zg, 
   lam += (int64_t)blockIdx.x * k;
   Zg += (int64_t)blockIdx.x * 6 * k * n;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* As = reinterpret_cast<T*>(smem_raw);   // n * n
-  T* d = As + n * n;                         // n
+  const int ld = n | 1;                      // odd: rows and columns are both conflict-free
+  T* As = reinterpret_cast<T*>(smem_raw);   // n * ld
+  T* d = As + (size_t)n * ld;                // n
   T* e = d + n;                              // n
   T* e2 = e + n;                             // n
   T* tau = e2 + n;                           // n
-  T* red = tau + n;                          // 32 (two halves for block_sum_1)
+  T* vv = tau + n;                           // n (the current reflector, contiguous)
+  T* red = vv + n;                           // 32 (two halves for block_sum_1)
   T* bnd = red + 32;                         // 2 * kEigThreads (multisection bounds, scratch)
   T* Zb = zsm ? bnd + 2 * kEigThreads : Zg;  // k * n eigenvectors, then 3 * k * n
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
-  for (int i = tid; i < n * n; i += kEigThreads) As[i] = A[i];
+  for (int i = tid; i < n * n; i += kEigThreads) {
+    const int r = i / n, c = i - (i / n) * n;
+    As[r * ld + c] = A[i];
+  }
   for (int i = tid; i < n; i += kEigThreads) { e[i] = T(0); tau[i] = T(0); }
   __syncthreads();
 
-  // ---- 1. tridiagonalisation.  Reflector j zeroes column j below the
-  // subdiagonal; it is read from, and stored in, row j right of the diagonal
-  // (the same values by symmetry, contiguous, and no longer needed by the
-  // updates, which touch rows and columns > j only).
+  // ---- 1. tridiagonalisation on the lower triangle.  Reflector j zeroes
+  // column j below the subdiagonal and is stored there (v[0] = 1); a
+  // contiguous copy serves the step.  Only the lower triangle (diagonal
+  // included) of the trailing block is updated; the matrix-vector product
+  // reads each element from whichever triangle holds it.
   for (int j = 0; j + 2 < n; ++j) {
     const int m = n - j - 1;               // length of the reflected part
-    T* x = As + j * n + j + 1;
+    T* x = As + (j + 1) * ld + j;          // x[i] at x[i * ld]
     T s2 = T(0);
-    for (int i = 1 + tid; i < m; i += kEigThreads) s2 += x[i] * x[i];
+    for (int i = 1 + tid; i < m; i += kEigThreads) s2 += x[i * ld] * x[i * ld];
     s2 = block_sum_1(s2, red);
     const T alpha = x[0];
     T t = T(0), beta = alpha, scale = T(0);
@@ -140,20 +146,24 @@ k_sym_eig(const T* __restrict__ A, int n, int k, T* U, T* lam, int flip, T* Zg, 
       scale = T(1) / (alpha - beta);
     }
     __syncthreads();   // all threads have read x[0] before it is overwritten
-    if (tid == 0) { e[j] = beta; tau[j] = t; d[j] = As[j * n + j]; x[0] = T(1); }
+    if (tid == 0) { e[j] = beta; tau[j] = t; d[j] = As[j * ld + j]; x[0] = T(1); vv[0] = T(1); }
     if (t != T(0))
-      for (int i = 1 + tid; i < m; i += kEigThreads) x[i] *= scale;
+      for (int i = 1 + tid; i < m; i += kEigThreads) {
+        const T v = x[i * ld] * scale;
+        x[i * ld] = v;
+        vv[i] = v;
+      }
     __syncthreads();
     if (t == T(0)) continue;
-    // p = t * A22 v: row r of A22 read as its column r (symmetric), so
-    // consecutive threads read consecutive addresses; H groups split the sum
-    T* A22 = As + (j + 1) * n + (j + 1);
+    // p = t * A22 v, thread r summing over c (H groups split the sum)
+    T* A22 = As + (j + 1) * ld + (j + 1);
     const int H = kEigThreads / m;         // >= 2 (m < n <= 224)
     {
       const int r = tid % m, h = tid / m;
       if (h < H) {
         T acc = T(0);
-        for (int c = h; c < m; c += H) acc += A22[c * n + r] * x[c];
+        for (int c = h; c < m; c += H)
+          acc += ((c <= r) ? A22[r * ld + c] : A22[c * ld + r]) * vv[c];
         bnd[h * m + r] = acc;
       }
     }
@@ -163,26 +173,26 @@ k_sym_eig(const T* __restrict__ A, int n, int k, T* U, T* lam, int flip, T* Zg, 
       T acc = T(0);
       for (int h = 0; h < H; ++h) acc += bnd[h * m + r];
       e2[r] = t * acc;                     // e2 holds p, then w, until the loop ends
-      pv += e2[r] * x[r];
+      pv += e2[r] * vv[r];
     }
     pv = block_sum_1(pv, red + kEigWarps);
     const T K = T(0.5) * t * pv;
-    for (int r = tid; r < m; r += kEigThreads) e2[r] -= K * x[r];   // w
+    for (int r = tid; r < m; r += kEigThreads) e2[r] -= K * vv[r];   // w
     __syncthreads();
-    // A22 -= v w^T + w v^T (warp per row, lanes along it)
+    // lower triangle of A22 -= v w^T + w v^T (warp per row, lanes along it)
     for (int r = warp; r < m; r += kEigWarps) {
-      const T vr = x[r], wr = e2[r];
-      T* row = A22 + r * n;
-      for (int c = lane; c < m; c += 32) row[c] -= vr * e2[c] + wr * x[c];
+      const T vr = vv[r], wr = e2[r];
+      T* row = A22 + r * ld;
+      for (int c = lane; c <= r; c += 32) row[c] -= vr * e2[c] + wr * vv[c];
     }
     __syncthreads();
   }
   if (tid == 0) {
     if (n >= 2) {
-      d[n - 2] = As[(n - 2) * n + (n - 2)];
-      e[n - 2] = As[(n - 1) * n + (n - 2)];
+      d[n - 2] = As[(n - 2) * ld + (n - 2)];
+      e[n - 2] = As[(n - 1) * ld + (n - 2)];
     }
-    d[n - 1] = As[(n - 1) * n + (n - 1)];
+    d[n - 1] = As[(n - 1) * ld + (n - 1)];
   }
   __syncthreads();
   for (int i = tid; i < n; i += kEigThreads) e2[i] = (i + 1 < n) ? e[i] * e[i] : T(0);
@@ -322,11 +332,11 @@ k_sym_eig(const T* __restrict__ A, int n, int k, T* U, T* lam, int flip, T* Zg, 
       const T tj = tau[j];
       if (tj == T(0)) continue;
       const int m = n - j - 1;
-      const T* v = As + j * n + j + 1;      // row j, v[0] = 1 stored explicitly
+      const T* v = As + (j + 1) * ld + j;   // column j, v[0] = 1 stored explicitly
       T s = T(0);
-      for (int i = lane; i < m; i += 32) s += v[i] * z[j + 1 + i];
+      for (int i = lane; i < m; i += 32) s += v[i * ld] * z[j + 1 + i];
       s = tj * warp_sum_t(s);
-      for (int i = lane; i < m; i += 32) z[j + 1 + i] -= s * v[i];
+      for (int i = lane; i < m; i += 32) z[j + 1 + i] -= s * v[i * ld];
       __syncwarp();
     }
     // first index of the largest |z| (ties resolved to the lowest index)
@@ -351,7 +361,7 @@ constexpr size_t kEigSmemLimit = 227 * 1024;
 
 template <typename T>
 size_t eig_smem(int n) {
-  return ((size_t)n * n + 4 * (size_t)n + 32 + 2 * kEigThreads) * sizeof(T);
+  return ((size_t)n * (n | 1) + 5 * (size_t)n + 32 + 2 * kEigThreads) * sizeof(T);
 }
 // with the eigenvectors and triangular factors in shared memory as well
 template <typename T>

@@ -214,3 +214,20 @@ def test_tucker_estimator(gb300, golden):
     tt = est.fit_transform(cuda(x))
     np.testing.assert_allclose(host(tt.core), run["core"], rtol=1e-9, atol=1e-10)
     assert repr(est).startswith("Rank-")
+
+
+@pytest.mark.parametrize("shape,rank", [((40, 6, 5, 7), [3, 2, 3, 2]),
+                                        ((12, 14, 16, 10), [4, 5, 3, 4])])
+def test_tucker_4way_uneven_matches_oracle(gb300, shape, rank):
+    """Four modes: every chain has two products on the second stream and the
+    factor updated last applied last; (40, 6, 5, 7) makes mode 0's unfolding
+    tall after the chain (the SVD's input is read again after the eigensolver)."""
+    rs = np.random.RandomState(sum(shape))
+    x = rs.randn(*shape)
+    (core, factors), errs = gb300.partial_tucker(cuda(x), rank, modes=[0, 1, 2, 3],
+                                                 n_iter_max=6, tol=0)
+    (co, fo), eo = oracle.partial_tucker(x, rank, modes=[0, 1, 2, 3], n_iter_max=6, tol=0)
+    np.testing.assert_allclose(errs, eo, rtol=1e-10, atol=1e-12)
+    np.testing.assert_allclose(host(core), co, rtol=1e-9, atol=1e-10)
+    for a, b in zip(factors, fo):
+        np.testing.assert_allclose(host(a), b, rtol=1e-9, atol=1e-10)
