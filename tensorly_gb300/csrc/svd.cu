@@ -128,6 +128,102 @@ __global__ void __launch_bounds__(kGThreads) k_gram_tiles(const T* __restrict__ 
     }
 }
 
+// f32 Gram tiles, tuned: 128 threads, each owning an 8 x 4 block of the
+// 64 x 64 tile (rows 8 ty.., columns 4 tx..), read from shared memory as
+// 16-byte vectors (three loads per 32 FMAs); the next chunk's tensor elements
+// are fetched into registers while the current chunk is multiplied.  Same
+// chunking and Neumaier compensation as k_gram_tiles, so the same accuracy.
+constexpr int kGT2Threads = 128;
+constexpr int kGPad4 = kGT + 4;   // 16-byte aligned rows of the k-major tiles
+constexpr int kGLoads = kGK * kGT / kGT2Threads;   // 16 elements per thread per operand
+
+__global__ void __launch_bounds__(kGT2Threads)
+k_gram_tiles_f32(const float* __restrict__ X, const GramArgs g) {
+  __shared__ __align__(16) float As[kGK * kGPad4];
+  __shared__ __align__(16) float Bs[kGK * kGPad4];
+  __shared__ int64_t offa[kGT], offb[kGT];
+  const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;   // ty 0..7, tx 0..15
+  int p = blockIdx.x, ta = 0;
+  while (p >= g.nt - ta) { p -= g.nt - ta; ++ta; }
+  const int tb = ta + p;
+  const bool diag = ta == tb;
+  const int64_t a0 = (int64_t)ta * kGT, b0 = (int64_t)tb * kGT;
+  if (tid < kGT) {
+    const int64_t a = a0 + tid, b = b0 + tid;
+    offa[tid] = (a < g.Na) ? off2(a, g.aD, g.aS1, g.aS0) : -1;
+    offb[tid] = (b < g.Na) ? off2(b, g.aD, g.aS1, g.aS0) : -1;
+  }
+  __syncthreads();
+  const int64_t c_begin = (int64_t)blockIdx.y * g.cps;
+  const int64_t c_end = min(c_begin + g.cps, g.chunks);
+  // loader: k = tid & 31 (fastest, coalesced), rows (tid >> 5) + 4 q
+  const int kk = tid & 31, rr = tid >> 5;
+  float ra[kGLoads], rb[kGLoads];
+  auto fetch = [&](int64_t c) {
+    const int64_t k = c * kGK + kk;
+    const int64_t ok = (k < g.Nk) ? off2(k, g.kD, g.kS1, g.kS0) : -1;
+#pragma unroll
+    for (int q = 0; q < kGLoads; ++q) {
+      const int r = rr + 4 * q;
+      const int64_t oa = offa[r];
+      ra[q] = (oa >= 0 && ok >= 0) ? __ldg(X + oa + ok) : 0.f;
+      if (!diag) {
+        const int64_t ob = offb[r];
+        rb[q] = (ob >= 0 && ok >= 0) ? __ldg(X + ob + ok) : 0.f;
+      }
+    }
+  };
+  float fh[8][4], fc[8][4];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) { fh[i][j] = 0.f; fc[i][j] = 0.f; }
+  if (c_begin < c_end) fetch(c_begin);
+  for (int64_t c = c_begin; c < c_end; ++c) {
+    __syncthreads();   // the previous chunk's tiles have been read
+#pragma unroll
+    for (int q = 0; q < kGLoads; ++q) {
+      As[kk * kGPad4 + rr + 4 * q] = ra[q];
+      if (!diag) Bs[kk * kGPad4 + rr + 4 * q] = rb[q];
+    }
+    __syncthreads();
+    if (c + 1 < c_end) fetch(c + 1);
+    const float* Bsrc = diag ? As : Bs;
+    float acc[8][4];
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+#pragma unroll 4
+    for (int k = 0; k < kGK; ++k) {
+      const float4 a_lo = *reinterpret_cast<const float4*>(As + k * kGPad4 + 8 * ty);
+      const float4 a_hi = *reinterpret_cast<const float4*>(As + k * kGPad4 + 8 * ty + 4);
+      const float4 bq = *reinterpret_cast<const float4*>(Bsrc + k * kGPad4 + 4 * tx);
+      const float av[8] = {a_lo.x, a_lo.y, a_lo.z, a_lo.w, a_hi.x, a_hi.y, a_hi.z, a_hi.w};
+      const float bv[4] = {bq.x, bq.y, bq.z, bq.w};
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const float v = acc[i][j];
+        const float t = fh[i][j] + v;
+        fc[i][j] += (fabsf(fh[i][j]) >= fabsf(v)) ? ((fh[i][j] - t) + v) : ((v - t) + fh[i][j]);
+        fh[i][j] = t;
+      }
+  }
+  double* out = g.partial + ((int64_t)blockIdx.y * g.npairs + blockIdx.x) * (kGT * kGT);
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      out[(8 * ty + i) * kGT + 4 * tx + j] = (double)fh[i][j] + (double)fc[i][j];
+}
+
 // G[a][b] = G[b][a] = sum over splits of the partial tiles, in split order.
 template <typename T>
 __global__ void k_gram_finish(const double* __restrict__ partial, int64_t Na, int nt, int npairs,
@@ -241,7 +337,11 @@ int gram_launch(const GramPlan& p, const T* X, T* G, double* partial, cudaStream
   g.nt = p.nt; g.npairs = p.npairs; g.chunks = p.chunks; g.cps = p.cps;
   g.partial = partial;
   TLGB_CHECK_ARG(p.npairs <= 2147483647, "gram: too many tiles");
-  k_gram_tiles<T><<<dim3((unsigned)p.npairs, (unsigned)p.splits), kGThreads, 0, st>>>(X, g);
+  if constexpr (sizeof(T) == 4)
+    k_gram_tiles_f32<<<dim3((unsigned)p.npairs, (unsigned)p.splits), kGT2Threads, 0, st>>>(
+        reinterpret_cast<const float*>(X), g);
+  else
+    k_gram_tiles<T><<<dim3((unsigned)p.npairs, (unsigned)p.splits), kGThreads, 0, st>>>(X, g);
   TLGB_LAUNCH_CHECK();
   TLGB_CHECK_ARG(p.npairs <= 65535, "gram: too many tile pairs for the finish grid");
   k_gram_finish<T><<<dim3((kGT * kGT + 255) / 256, (unsigned)p.npairs), 256, 0, st>>>(

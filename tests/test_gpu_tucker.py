@@ -231,3 +231,33 @@ def test_tucker_4way_uneven_matches_oracle(gb300, shape, rank):
     np.testing.assert_allclose(host(core), co, rtol=1e-9, atol=1e-10)
     for a, b in zip(factors, fo):
         np.testing.assert_allclose(host(a), b, rtol=1e-9, atol=1e-10)
+
+
+@pytest.mark.parametrize("shape,mode,side", [((70, 33, 50), 0, 0), ((70, 33, 50), 1, 0),
+                                             ((70, 33, 50), 2, 0), ((9, 200, 7), 0, 1),
+                                             ((20, 30, 3), 2, 1), ((130, 64, 3), 2, 0),
+                                             ((64, 64, 64), 1, 0)])
+def test_gram_unfolding_f32_matches_f64(gb300, shape, mode, side):
+    """Gram of an f32 unfolding (M M^T, or M^T M for side 1) against f64 NumPy."""
+    import ctypes
+    from tensorly_gb300 import _lib
+    from tensorly_gb300._tensor import workspace
+    rs = np.random.RandomState(sum(shape) + mode)
+    x = rs.randn(*shape).astype(np.float32)
+    M = np.moveaxis(x.astype(np.float64), mode, 0).reshape(shape[mode], -1)
+    want = M @ M.T if side == 0 else M.T @ M
+    xt = cuda(x, torch.float32)
+    n = want.shape[0]
+    G = torch.empty((n, n), dtype=torch.float32, device="cuda")
+    shp = (ctypes.c_int64 * 3)(*shape)
+    nb = ctypes.c_size_t(0)
+    lib = _lib.lib()
+    _lib.check(lib.tlgb_gram_unfolding_workspace_size(3, shp, mode, side, ctypes.byref(nb)))
+    ws = workspace(nb.value, xt.device)
+    _lib.check(lib.tlgb_gram_unfolding(_lib.TLGB_F32, xt.data_ptr(), 3, shp, mode, side,
+                                       G.data_ptr(), ws.data_ptr(), ws.numel(),
+                                       torch.cuda.current_stream().cuda_stream))
+    got = G.cpu().numpy().astype(np.float64)
+    scale = np.sqrt(np.outer(np.diag(want), np.diag(want)))
+    assert np.abs(got - want).max() / scale.max() < 2e-6
+    np.testing.assert_array_equal(got, got.T)
