@@ -73,15 +73,20 @@ __device__ float block_sum_f(float v, float* red) {
 
 // ||X|| from the sum of squares and the three sketches S_n = unfold(X, n) Omega_n
 // (32 x 16 each) divided by ||X||, of the tensor in shared memory; thread ->
-// (two rows, one column) of each sketch.
+// (two rows, one column) of each sketch.  Omega_n (64 KiB) is staged in shared
+// memory (Os) per mode, so the inner loop reads only shared memory.
 __device__ void sketch_block(const float* Xs, float sumsq, const float* __restrict__ omega,
-                             float* fo_base, float* xnorm_out) {
+                             float* Os, float* fo_base, float* xnorm_out) {
   const int tid = threadIdx.x;
   const float nrm = sqrtf(sumsq);
   if (tid == 0) *xnorm_out = nrm;
   const int s = tid & 15, rp = tid >> 4;   // rp: 0..15 -> rows 2 rp, 2 rp + 1
   for (int n = 0; n < 3; ++n) {
-    const float* Om = omega + (int64_t)n * kI * kI * kS;
+    __syncthreads();   // the previous mode's reads of Os are done
+    const float4* src = reinterpret_cast<const float4*>(omega + (int64_t)n * kI * kI * kS);
+    float4* dst = reinterpret_cast<float4*>(Os);
+    for (int i = tid; i < kI * kI * kS / 4; i += kLThreads) dst[i] = __ldg(src + i);
+    __syncthreads();
     float acc0 = 0.f, acc1 = 0.f;
     const int r0 = 2 * rp, r1 = 2 * rp + 1;
     for (int col = 0; col < kI * kI; ++col) {
@@ -90,7 +95,7 @@ __device__ void sketch_block(const float* Xs, float sumsq, const float* __restri
       if (n == 0) { e0 = r0 * 1024 + col; e1 = r1 * 1024 + col; }
       else if (n == 1) { e0 = hi * 1024 + r0 * 32 + lo; e1 = hi * 1024 + r1 * 32 + lo; }
       else { e0 = hi * 1024 + lo * 32 + r0; e1 = hi * 1024 + lo * 32 + r1; }
-      const float w = __ldg(&Om[col * kS + s]);
+      const float w = Os[col * kS + s];
       acc0 = fmaf(Xs[e0], w, acc0);
       acc1 = fmaf(Xs[e1], w, acc1);
     }
@@ -98,6 +103,17 @@ __device__ void sketch_block(const float* Xs, float sumsq, const float* __restri
     fo[r0 * kS + s] = acc0 / nrm;
     fo[r1 * kS + s] = acc1 / nrm;
   }
+}
+
+// Copy one 32^3 tensor into shared memory with 16-byte loads, eight in flight
+// per thread (one CTA per SM holds a 128 KiB tensor, so each thread must keep
+// many loads outstanding to stream at the memory's rate).
+__device__ __forceinline__ void load_tensor_smem(const float* __restrict__ Xg, float* Xs) {
+  const float4* src = reinterpret_cast<const float4*>(Xg);
+  float4* dst = reinterpret_cast<float4*>(Xs);
+  constexpr int n4 = kN3 / 4, per = n4 / kLThreads;   // 32 per thread
+#pragma unroll 8
+  for (int k = 0; k < per; ++k) dst[threadIdx.x + k * kLThreads] = __ldg(src + threadIdx.x + k * kLThreads);
 }
 
 __global__ void k_omega(float* omega) {   // 3 x 1024 x 16
@@ -115,6 +131,7 @@ k_generate(const int64_t* seeds, int batch, float* X, float* feats, float* xnorm
   float* Xs = lsm;                     // 32768
   float* F = Xs + kN3;                 // [3][32][8]
   float* red = F + 3 * kI * kR;        // 32
+  float* Os = red + 32;                // 16384 (Omega of one mode)
   const int b = blockIdx.x;
   const uint64_t t = (uint64_t)seeds[b];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -190,7 +207,7 @@ k_generate(const int64_t* seeds, int batch, float* X, float* feats, float* xnorm
     sf += v * v;
   }
   sf = block_sum_f(sf, red);
-  sketch_block(Xs, sf, omega, feats + (int64_t)b * kFeat, xnorm + b);
+  sketch_block(Xs, sf, omega, Os, feats + (int64_t)b * kFeat, xnorm + b);
 }
 
 // Sketch features and norm of tensors already in memory (batch x 32768).
@@ -199,16 +216,17 @@ k_sketch(const float* __restrict__ X, float* feats, float* xnorm, const float* _
   extern __shared__ __align__(16) float lsm[];
   float* Xs = lsm;
   float* red = Xs + kN3;
+  float* Os = red + 32;                // 16384 (Omega of one mode)
   const int b = blockIdx.x, tid = threadIdx.x;
-  const float* Xg = X + (int64_t)b * kN3;
-  float sf = 0.f;
+  load_tensor_smem(X + (int64_t)b * kN3, Xs);
+  __syncthreads();
+  float sf = 0.f;   // the same per-thread order as the generator's, so ||X|| agrees bitwise
   for (int e = tid; e < kN3; e += kLThreads) {
-    const float v = Xg[e];
-    Xs[e] = v;
+    const float v = Xs[e];
     sf += v * v;
   }
   sf = block_sum_f(sf, red);
-  sketch_block(Xs, sf, omega, feats + (int64_t)b * kFeat, xnorm + b);
+  sketch_block(Xs, sf, omega, Os, feats + (int64_t)b * kFeat, xnorm + b);
 }
 
 // C(m, n) = epi(sum_k A(m, k) B(k, n)), A(m, k) = A[m sam + k sak],
@@ -298,8 +316,7 @@ k_cp_loss(const float* __restrict__ X, const float* __restrict__ out,
   const int b = blockIdx.x, tid = threadIdx.x;
   const float nx = xnorm[b];
   const float sc = cbrtf(nx);
-  const float* Xg = X + (int64_t)b * kN3;
-  for (int e = tid; e < kN3; e += kLThreads) Xs[e] = Xg[e];
+  load_tensor_smem(X + (int64_t)b * kN3, Xs);
   for (int e = tid; e < kOut; e += kLThreads) Ah[e] = out[(int64_t)b * kOut + e] * sc;
   __syncthreads();
   for (int e = tid; e < 3 * kR * kR; e += kLThreads) {
@@ -315,7 +332,8 @@ k_cp_loss(const float* __restrict__ X, const float* __restrict__ out,
     float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
     for (int u = 0; u < kI; ++u) {
       float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f;
-      for (int v = 0; v < kI; ++v) {
+      for (int v0 = 0; v0 < kI; ++v0) {
+        const int v = (v0 + row) & (kI - 1);   // rotated per row: no bank conflicts
         int e;
         if (n == 0) e = row * 1024 + u * 32 + v;
         else if (n == 1) e = u * 1024 + row * 32 + v;
@@ -399,8 +417,7 @@ k_gram3(const float* __restrict__ X, float* G) {
   extern __shared__ __align__(16) float lsm[];
   float* Xs = lsm;
   const int b = blockIdx.x, tid = threadIdx.x;
-  const float* Xg = X + (int64_t)b * kN3;
-  for (int e = tid; e < kN3; e += kLThreads) Xs[e] = Xg[e];
+  load_tensor_smem(X + (int64_t)b * kN3, Xs);
   __syncthreads();
   for (int w = tid; w < 3 * kI * kI; w += kLThreads) {
     const int n = w / (kI * kI), rem = w - n * kI * kI, r = rem / kI, c = rem - (rem / kI) * kI;
@@ -444,7 +461,7 @@ extern "C" int tlgb_ws_generate(const int64_t* seeds, int batch, void* X, void* 
                                 const void* omega, void* stream) {
   clear_error();
   TLGB_CHECK_ARG(seeds && X && feats && xnorm && omega && batch >= 1, "ws_generate: bad argument");
-  const size_t smem = (size_t)(kN3 + 3 * kI * kR + 32) * sizeof(float);
+  const size_t smem = (size_t)(kN3 + 3 * kI * kR + 32 + kI * kI * kS) * sizeof(float);
   static bool attr[64] = {};
   const int dev = current_device();
   if (dev >= 0 && dev < 64 && !attr[dev]) {
@@ -462,7 +479,7 @@ extern "C" int tlgb_ws_sketch(const void* X, int batch, void* feats, void* xnorm
                               const void* omega, void* stream) {
   clear_error();
   TLGB_CHECK_ARG(X && feats && xnorm && omega && batch >= 1, "ws_sketch: bad argument");
-  const size_t smem = (size_t)(kN3 + 32) * sizeof(float);
+  const size_t smem = (size_t)(kN3 + 32 + kI * kI * kS) * sizeof(float);
   static bool attr[64] = {};
   const int dev = current_device();
   if (dev >= 0 && dev < 64 && !attr[dev]) {
