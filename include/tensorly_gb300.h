@@ -304,6 +304,40 @@ int tlgb_cp_als_batched(int n_tensors, const tlgb_batch_item* items, int n_iter_
                         size_t workspace_bytes, void* stream);
 
 /*
+ * Non-negative CP by multiplicative updates: the loop of
+ * tensorly/decomposition/_nn_cp.py:26-183 (non_negative_parafac) with weights
+ * all one, normalize_factors=False and no mask.  factors: the initial
+ * non-negative factors on entry, the result on exit (dtype of X, row-major
+ * shape[k] x rank).  free_modes: ascending, ending with ndim - 1 (the
+ * reference frees the last mode).  With tol > 0 the relative error of every
+ * iteration goes to errors (host, n_iter_max doubles) and the run stops at
+ * the reference's test (cvg_criterion 0 'abs_rec_error', 1 'rec_error');
+ * *n_errors receives how many were recorded (0 when tol is 0, as the
+ * reference records none then).
+ */
+int tlgb_cp_nn_mu_workspace_size(int dtype, int ndim, const int64_t* shape, int64_t rank,
+                                 int n_iter_max, size_t* bytes);
+int tlgb_cp_nn_mu(int dtype, const void* X, int ndim, const int64_t* shape, void* const* factors,
+                  int64_t rank, const int* free_modes, int n_free, int n_iter_max, double tol,
+                  int cvg_criterion, double* errors, int* n_errors, void* workspace,
+                  size_t workspace_bytes, void* stream);
+
+/*
+ * Pieces of the non-negative SVD (NNDSVD, tensorly/tenalg/svd.py:68-134):
+ *   tlgb_sum             sum of n elements into *out (device f64); workspace
+ *                        >= 256 doubles
+ *   tlgb_nndsvd_columns  W (I x k) from U (I x k), S (k) and Y = U^T M viewed as
+ *                        (L, k, Tt) (the mode-n product of the tensor with U^T);
+ *                        fill 1: 'nndsvda' (entries below eps become avg),
+ *                        0: 'nndsvd' (soft threshold); workspace >= 2 k elements
+ */
+int tlgb_sum(int dtype, const void* X, int64_t n, double* out, void* workspace,
+             size_t workspace_bytes, void* stream);
+int tlgb_nndsvd_columns(int dtype, const void* U, const void* S, const void* Y, int64_t I,
+                        int64_t k, int64_t L, int64_t Tt, int fill, double avg, void* W,
+                        void* workspace, size_t workspace_bytes, void* stream);
+
+/*
  * Learned warm start for CP-ALS (no counterpart in TensorLy; its fallback is
  * TensorLy's init='svd', tensorly/decomposition/_cp.py:70-96).  Fixed problem
  * family: 32 x 32 x 32 f32 tensors of rank 8 (factor columns with pairwise

@@ -26,7 +26,8 @@ __all__ = [
     "unfolding_dot_khatri_rao", "mode_dot", "multi_mode_dot", "svd_flip",
     "truncated_svd", "svd_interface", "random_cp", "cp_to_tensor", "cp_norm",
     "cp_normalize", "validate_cp_rank", "initialize_cp", "error_calc",
-    "parafac", "initialize_tucker", "partial_tucker", "tucker",
+    "parafac", "initialize_tucker", "partial_tucker", "tucker", "non_negative_parafac",
+    "make_svd_non_negative",
     "tucker_to_tensor", "validate_tucker_rank", "parafac_sweeps",
 ]
 
@@ -218,15 +219,58 @@ def truncated_svd(matrix, n_eigenvecs=None, **kwargs):
 def svd_interface(matrix, method="truncated_svd", n_eigenvecs=None, flip_sign=True,
                   u_based_flip_sign=True, non_negative=None, mask=None,
                   n_iter_mask_imputation=5, **kwargs):
-    """tensorly/tenalg/svd.py:366-447 (truncated_svd method, no mask, no NNDSVD)."""
+    """tensorly/tenalg/svd.py:366-447 (truncated_svd method, no mask); the
+    non-negative branch (``:443-444``) applies ``make_svd_non_negative``."""
     if method != "truncated_svd":
         raise NotImplementedError("oracle restates method='truncated_svd' only")
-    if mask is not None or (non_negative is not False and non_negative is not None):
-        raise NotImplementedError("oracle restates the unmasked, signed branch only")
+    if mask is not None:
+        raise NotImplementedError("oracle restates the unmasked branch only")
     U, S, V = truncated_svd(matrix, n_eigenvecs=n_eigenvecs)
     if flip_sign:
         U, V = svd_flip(U, V, u_based_decision=u_based_flip_sign)
+    if non_negative is not False and non_negative is not None:
+        U, V = make_svd_non_negative(matrix, U, S, V, non_negative)
     return U, S, V
+
+
+def make_svd_non_negative(tensor, U, S, V, nntype=True):
+    """tensorly/tenalg/svd.py:68-134: NNDSVD (Boutsidis & Gallopoulos 2008).
+    Column 0 is sqrt(S_0) |U_0|; column j >= 1 takes the positive or the
+    negative parts of (U_j, V_j), whichever has the larger product of norms,
+    scaled by sqrt(S_j * that product).  'nndsvda' (the default for True)
+    then replaces entries below eps by the tensor's mean."""
+    if nntype is True:
+        nntype = "nndsvda"
+    W = np.zeros_like(U)
+    H = np.zeros_like(V)
+    W[:, 0] = np.sqrt(S[0]) * np.abs(U[:, 0])
+    H[0, :] = np.sqrt(S[0]) * np.abs(V[0, :])
+    for j in range(1, min(U.shape[1], V.shape[0])):
+        x, y = U[:, j], V[j, :]
+        x_p, y_p = np.clip(x, 0.0, None), np.clip(y, 0.0, None)
+        x_n, y_n = np.abs(np.clip(x, None, 0.0)), np.abs(np.clip(y, None, 0.0))
+        x_p_nrm, y_p_nrm = np.linalg.norm(x_p), np.linalg.norm(y_p)
+        x_n_nrm, y_n_nrm = np.linalg.norm(x_n), np.linalg.norm(y_n)
+        m_p, m_n = x_p_nrm * y_p_nrm, x_n_nrm * y_n_nrm
+        if m_p > m_n:
+            u, v, sigma = x_p / x_p_nrm, y_p / y_p_nrm, m_p
+        else:
+            u, v, sigma = x_n / x_n_nrm, y_n / y_n_nrm, m_n
+        lbd = np.sqrt(S[j] * sigma)
+        W[:, j] = lbd * u
+        H[j, :] = lbd * v
+    eps = np.finfo(np.asarray(tensor).dtype).eps
+    if nntype == "nndsvd":
+        W = np.where(W > eps, W - eps, np.where(W < -eps, W + eps, 0.0))
+        H = np.where(H > eps, H - eps, np.where(H < -eps, H + eps, 0.0))
+    elif nntype == "nndsvda":
+        avg = np.mean(tensor)
+        W = np.where(W < eps, np.ones(W.shape, dtype=W.dtype) * avg, W)
+        H = np.where(H < eps, np.ones(H.shape, dtype=H.dtype) * avg, H)
+    else:
+        raise ValueError(f'Invalid nntype parameter: got {nntype} instead of one of '
+                         '("nndsvd", "nndsvda")')
+    return W, H
 
 
 # --------------------------------------------------------------------------
@@ -297,15 +341,17 @@ def cp_normalize(cp_tensor):
 
 
 def initialize_cp(tensor, rank, init="svd", svd="truncated_svd", random_state=None,
-                  normalize_factors=False):
-    """tensorly/decomposition/_cp.py:26-137 (non_negative=False, no mask)."""
+                  normalize_factors=False, non_negative=False):
+    """tensorly/decomposition/_cp.py:26-137 (no mask); ``non_negative`` makes
+    the SVD non-negative (NNDSVDA) and takes absolute values (``:129-131``)."""
     rng = check_random_state(random_state)
     if isinstance(init, str) and init == "random":
         weights, factors = random_cp(tensor.shape, rank, random_state=rng, dtype=tensor.dtype)
     elif isinstance(init, str) and init == "svd":
         factors = []
         for mode in range(tensor.ndim):
-            U, S, _ = svd_interface(unfold(tensor, mode), n_eigenvecs=rank, method=svd)
+            U, S, _ = svd_interface(unfold(tensor, mode), n_eigenvecs=rank, method=svd,
+                                    non_negative=non_negative)
             if mode == 0:
                 idx = min(rank, S.shape[0])
                 U = U.copy()
@@ -324,9 +370,73 @@ def initialize_cp(tensor, rank, init="svd", svd="truncated_svd", random_state=No
         return None, [f * avg for f in factors]
     else:
         raise ValueError(f'Initialization method "{init}" not recognized')
+    if non_negative:
+        factors = [np.abs(f) for f in factors]
     if normalize_factors:
         weights, factors = cp_normalize((weights, factors))
     return weights, factors
+
+
+def non_negative_parafac(tensor, rank, n_iter_max=100, init="svd", svd="truncated_svd",
+                         tol=10e-7, random_state=None, verbose=0, normalize_factors=False,
+                         return_errors=False, mask=None, cvg_criterion="abs_rec_error",
+                         fixed_modes=None):
+    """tensorly/decomposition/_nn_cp.py:26-183: non-negative CP by the
+    multiplicative updates of Shashua & Hazan (ICML 2005).  Per mode
+    (``:116-138``): accum = Hadamard of the other Grams scaled by w w^T;
+    A <- A * clip(MTTKRP, eps) / clip(A accum, eps).  The error (``:140-152``,
+    only when ``tol``) uses the last mode's MTTKRP; stop on the 'abs_rec_error'
+    or 'rec_error' test from the second iteration on."""
+    if mask is not None:
+        raise NotImplementedError("oracle restates the unmasked branch only")
+    tensor = np.asarray(tensor)
+    epsilon = np.finfo(tensor.dtype).eps
+    rank = validate_cp_rank(tensor.shape, rank=rank)
+    weights, factors = initialize_cp(tensor, rank, init=init, svd=svd,
+                                     random_state=random_state,
+                                     normalize_factors=normalize_factors, non_negative=True)
+    if weights is None:
+        weights = np.ones(rank, dtype=tensor.dtype)
+    factors = list(factors)
+    rec_errors = []
+    norm_tensor = norm(tensor)
+    fixed_modes = [] if fixed_modes is None else list(fixed_modes)
+    if tensor.ndim - 1 in fixed_modes:
+        warnings.warn("You asked for fixing the last mode, which is not supported while tol "
+                      "is fixed.\n The last mode will not be fixed. Consider using tl.moveaxis()")
+        fixed_modes.remove(tensor.ndim - 1)
+    modes_list = [m for m in range(tensor.ndim) if m not in fixed_modes]
+    mttkrp = None
+    for iteration in range(n_iter_max):
+        for mode in modes_list:
+            accum = None
+            for i, e in enumerate([k for k in range(len(factors)) if k != mode]):
+                g = factors[e].T @ factors[e]
+                accum = g if i == 0 else accum * g
+            accum = weights.reshape(-1, 1) * accum * weights.reshape(1, -1)
+            mttkrp = unfolding_dot_khatri_rao(tensor, (weights, factors), mode)
+            numerator = np.clip(mttkrp, epsilon, None)
+            denominator = np.clip(factors[mode] @ accum, epsilon, None)
+            factors[mode] = factors[mode] * numerator / denominator
+            if normalize_factors and mode != modes_list[-1]:
+                weights, factors = cp_normalize((weights, factors))
+        if tol:
+            rec_error = error_calc(tensor, norm_tensor, weights, factors, mttkrp) / norm_tensor
+            rec_errors.append(rec_error)
+            if iteration >= 1:
+                dec = rec_errors[-2] - rec_errors[-1]
+                if cvg_criterion == "abs_rec_error":
+                    stop = abs(dec) < tol
+                elif cvg_criterion == "rec_error":
+                    stop = dec < tol
+                else:
+                    raise TypeError("Unknown convergence criterion")
+                if stop:
+                    break
+        if normalize_factors:
+            weights, factors = cp_normalize((weights, factors))
+    cp = (weights, factors)
+    return (cp, rec_errors) if return_errors else cp
 
 
 def error_calc(tensor, norm_tensor, weights, factors, mttkrp):

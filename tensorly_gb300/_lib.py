@@ -134,6 +134,21 @@ SIGNATURES = [
      [ctypes.c_int, ctypes.POINTER(BatchItem), ctypes.c_int, ctypes.c_int, ctypes.c_int,
       ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
       ctypes.c_size_t, ctypes.c_void_p]),
+    ("tlgb_cp_nn_mu_workspace_size", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_int, _c_i64p, ctypes.c_int64, ctypes.c_int,
+      ctypes.POINTER(ctypes.c_size_t)]),
+    ("tlgb_cp_nn_mu", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, _c_i64p, _c_vpp, ctypes.c_int64,
+      ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+      ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int), ctypes.c_void_p,
+      ctypes.c_size_t, ctypes.c_void_p]),
+    ("tlgb_sum", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
+      ctypes.c_size_t, ctypes.c_void_p]),
+    ("tlgb_nndsvd_columns", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+      ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int, ctypes.c_double,
+      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     ("tlgb_ws_omega", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     ("tlgb_ws_generate", ctypes.c_int,
      [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,

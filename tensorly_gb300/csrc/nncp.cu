@@ -1,0 +1,441 @@
+// Non-negative CP by multiplicative updates on the GPU: the loop of
+// tensorly/decomposition/_nn_cp.py:26-183 (non_negative_parafac, weights all
+// one, normalize_factors=False, no mask).  Per iteration and free mode:
+//   accum = Hadamard product of the other factors' Grams        (:116-125)
+//   M     = MTTKRP of the mode                                   (:129)
+//   A    <- A * clip(M, eps) / clip(A accum, eps)                (:131-134)
+// and, when tol > 0, the relative error from the last mode's MTTKRP and the
+// Grams with the reference's stop test (:140-170).  The MTTKRP is the SIMT
+// split kernel of CP-ALS; the Grams are kept in f64 and refreshed after every
+// update; the stop flag lives on the device, so kernels after convergence
+// return at once and the host reads the flag every few iterations.
+//
+// The NNDSVD helpers of the non-negative SVD initialisation
+// (tensorly/tenalg/svd.py:68-134) are here too: the norms of the positive and
+// negative parts of rows, and the column update that follows.
+#include <algorithm>
+#include <cmath>
+#include <limits>
+#include <vector>
+
+#include "als_kernels.cuh"
+#include "mttkrp_simt.cuh"
+
+namespace tlgb {
+namespace {
+
+constexpr int kMuThreads = 256;
+constexpr int kMuSumsqBlocks = 256;
+constexpr int kMuCheckEvery = 8;
+
+// V = Hadamard product of the Grams of every mode but `mode`.
+__global__ void k_mu_accum(const double* __restrict__ G, int ndim, int mode, int R, double* V,
+                           const int* done) {
+  if (*done) return;
+  const int RR = R * R;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < RR; e += gridDim.x * blockDim.x) {
+    double v = 0.0;
+    bool first = true;
+    for (int k = 0; k < ndim; ++k) {
+      if (k == mode) continue;
+      v = first ? G[(int64_t)k * RR + e] : v * G[(int64_t)k * RR + e];
+      first = false;
+    }
+    V[e] = first ? 1.0 : v;
+  }
+}
+
+// A <- A * max(M, eps) / max(A V, eps) for a block of rows; M is the sum of
+// the MTTKRP's split partials.  The block's rows are staged in shared memory
+// before any is overwritten.  With ipart, the block's sum of M * A_new (the
+// <X, [[A]]> term of the error, from the MTTKRP taken before the update as
+// in the reference).
+template <typename T>
+__global__ void __launch_bounds__(kMuThreads)
+k_mu_update(const T* __restrict__ partial, int splits, int64_t I, int R,
+            const double* __restrict__ V, T eps, T* A, double* ipart, const int* done,
+            int64_t rpb) {
+  if (*done) return;
+  extern __shared__ double smu[];   // [rows of the block][R]
+  __shared__ double red[kMuThreads / 32];
+  const int tid = threadIdx.x;
+  const int64_t row0 = blockIdx.x * rpb;
+  const int64_t row1 = min(row0 + rpb, I);
+  const int n = (int)(row1 - row0) * R;
+  const int64_t IR = I * R;
+  for (int e = tid; e < n; e += kMuThreads) smu[e] = (double)A[row0 * R + e];
+  __syncthreads();
+  double ip = 0.0;
+  for (int e = tid; e < n; e += kMuThreads) {
+    const int i = e / R, c = e - (e / R) * R;
+    const int64_t off = (row0 + i) * R + c;
+    double m0 = 0.0, m1 = 0.0;
+    int p = 0;
+    for (; p + 1 < splits; p += 2) {
+      m0 += (double)partial[(int64_t)p * IR + off];
+      m1 += (double)partial[(int64_t)(p + 1) * IR + off];
+    }
+    if (p < splits) m0 += (double)partial[(int64_t)p * IR + off];
+    const double m = m0 + m1;
+    double den = 0.0;
+    for (int s = 0; s < R; ++s) den = fma(smu[i * R + s], V[(int64_t)s * R + c], den);
+    const T mt = (T)m;
+    const T num = mt > eps ? mt : eps;
+    const T dt = (T)den;
+    const T dn = dt > eps ? dt : eps;
+    const T a = (T)smu[i * R + c] * num / dn;
+    A[off] = a;
+    if (ipart) ip += (double)mt * (double)a;
+  }
+  if (ipart) {
+    for (int o = 16; o > 0; o >>= 1) ip += __shfl_xor_sync(0xffffffffu, ip, o);
+    if ((tid & 31) == 0) red[tid >> 5] = ip;
+    __syncthreads();
+    if (tid == 0) {
+      double t = 0.0;
+      for (int w = 0; w < kMuThreads / 32; ++w) t += red[w];
+      ipart[blockIdx.x] = t;
+    }
+  }
+}
+
+// Norms of the positive and the negative part of each mode-n slice of Y, a
+// tensor viewed as (L, k, T): out[2 j] = ||max(Y[:, j, :], 0)||,
+// out[2 j + 1] = ||min(Y[:, j, :], 0)||.  One block per slice.
+template <typename T>
+__global__ void k_posneg_norms(const T* __restrict__ Y, int64_t L, int k, int64_t Tt, T* out) {
+  __shared__ double rp[32], rn[32];
+  const int j = blockIdx.x;
+  double sp = 0.0, sn = 0.0;
+  for (int64_t x = threadIdx.x; x < L * Tt; x += blockDim.x) {
+    const int64_t l = x / Tt, t = x - (x / Tt) * Tt;
+    const double v = (double)Y[(l * k + j) * Tt + t];
+    if (v > 0.0) sp += v * v; else sn += v * v;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    sp += __shfl_xor_sync(0xffffffffu, sp, o);
+    sn += __shfl_xor_sync(0xffffffffu, sn, o);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) { rp[warp] = sp; rn[warp] = sn; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { a += rp[w]; b += rn[w]; }
+    out[2 * blockIdx.x] = (T)sqrt(a);
+    out[2 * blockIdx.x + 1] = (T)sqrt(b);
+  }
+}
+
+// NNDSVD columns of W (I x k, row-major) from U (I x k), S (k) and the norms
+// of the row parts of U^T M (2 k; V = S^-1 U^T M).  Column 0 = sqrt(S_0) |U_0|;
+// column j >= 1 takes U_j's positive or negative part, whichever side has the
+// larger product of norms, divided by its norm and scaled by
+// sqrt(S_j * that product); with `fill`, entries below eps become `avg`
+// ('nndsvda'), else they are soft-thresholded by eps ('nndsvd').
+template <typename T>
+__global__ void k_nndsvd_columns(const T* __restrict__ U, const T* __restrict__ S,
+                                 const T* __restrict__ vnorms, int64_t I, int k, T eps, int fill,
+                                 T avg, T* W) {
+  // one block per column; the column's positive / negative norms first
+  __shared__ double rp[32], rn[32];
+  const int j = blockIdx.x;
+  double sp = 0.0, sn = 0.0;
+  for (int64_t i = threadIdx.x; i < I; i += blockDim.x) {
+    const double v = (double)U[i * k + j];
+    if (v > 0.0) sp += v * v; else sn += v * v;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    sp += __shfl_xor_sync(0xffffffffu, sp, o);
+    sn += __shfl_xor_sync(0xffffffffu, sn, o);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) { rp[warp] = sp; rn[warp] = sn; }
+  __syncthreads();
+  double xp = 0.0, xn = 0.0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { xp += rp[w]; xn += rn[w]; }
+  const T x_p = (T)sqrt(xp), x_n = (T)sqrt(xn);
+  // the rows of V are those of U^T M divided by the singular values
+  const T y_p = vnorms[2 * j] / S[j], y_n = vnorms[2 * j + 1] / S[j];
+  const T m_p = x_p * y_p, m_n = x_n * y_n;
+  const bool pos = m_p > m_n;
+  const T nrm = pos ? x_p : x_n;
+  const T lbd = (j == 0) ? (T)0 : (T)sqrt((double)S[j] * (double)(pos ? m_p : m_n));
+  const T s0 = (T)sqrt((double)S[0]);
+  for (int64_t i = threadIdx.x; i < I; i += blockDim.x) {
+    const T x = U[i * k + j];
+    T w;
+    if (j == 0) w = s0 * (x < (T)0 ? -x : x);
+    else {
+      const T part = pos ? (x > (T)0 ? x : (T)0) : (x < (T)0 ? -x : (T)0);
+      w = lbd * (part / nrm);
+    }
+    if (fill) w = (w < eps) ? avg : w;
+    else w = (w > eps) ? w - eps : ((w < -eps) ? w + eps : (T)0);
+    W[i * k + j] = w;
+  }
+}
+
+// Sum of a tensor in f64 (block partials, then one block), for the mean
+// that 'nndsvda' fills with.
+template <typename T>
+__global__ void k_sum_part(const T* __restrict__ X, int64_t n, double* part) {
+  __shared__ double red[32];
+  double s0 = 0.0, s1 = 0.0;
+  const int64_t step = (int64_t)gridDim.x * blockDim.x;
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  for (; i + step < n; i += 2 * step) { s0 += (double)X[i]; s1 += (double)X[i + step]; }
+  if (i < n) s0 += (double)X[i];
+  double s = s0 + s1;
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    part[blockIdx.x] = t;
+  }
+}
+__global__ void k_sum_final(const double* part, int n, double* out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double t = 0.0;
+    for (int i = 0; i < n; ++i) t += part[i];
+    *out = t;
+  }
+}
+
+struct MuLayout {
+  size_t ctrl, errors, G, V, partial, gpart, ipart, sumsq, bytes;
+};
+
+int64_t mu_rows_per_block(int64_t I, int R, int nparts);
+
+template <typename T>
+int mu_layout(const Shape& sh, int64_t R, int n_iter_max, std::vector<MttkrpPlan>* plans,
+              int* nparts, MuLayout* L) {
+  const int dtype = TypeCode<T>::value;
+  plans->resize(sh.ndim);
+  size_t pmax = 0;
+  int64_t imax = 0;
+  for (int k = 0; k < sh.ndim; ++k) {
+    int rc = mttkrp_make_plan(dtype, sh, R, k, &(*plans)[k]);
+    if (rc) return rc;
+    pmax = std::max(pmax, (*plans)[k].partial_bytes);
+    imax = std::max(imax, sh.dim[k]);
+  }
+  *nparts = solve_blocks_for(imax);
+  int64_t nb_max = 1;
+  for (int k = 0; k < sh.ndim; ++k)
+    nb_max = std::max<int64_t>(nb_max, ceil_div(sh.dim[k], mu_rows_per_block(sh.dim[k], (int)R,
+                                                                              *nparts)));
+  size_t off = 0;
+  auto take = [&](size_t b) { off = align_up(off, 256); const size_t o = off; off += b; return o; };
+  const size_t RR = (size_t)R * R;
+  L->ctrl = take(sizeof(AlsCtrl));
+  L->errors = take(sizeof(double) * (size_t)std::max(1, n_iter_max));
+  L->G = take(sizeof(double) * RR * sh.ndim);
+  L->V = take(sizeof(double) * RR);
+  L->partial = take(pmax);
+  L->gpart = take(sizeof(double) * RR * (size_t)*nparts);
+  L->ipart = take(sizeof(double) * (size_t)nb_max);
+  L->sumsq = take(sizeof(double) * kMuSumsqBlocks);
+  L->bytes = align_up(off, 256);
+  return TLGB_OK;
+}
+
+// Rows per update block: about `nparts` blocks, the block's rows (f64) within
+// 48 KiB of shared memory.
+int64_t mu_rows_per_block(int64_t I, int R, int nparts) {
+  const int64_t cap = std::max<int64_t>(1, (48 * 1024 / 8) / R);
+  return std::max<int64_t>(1, std::min<int64_t>(ceil_div(I, (int64_t)nparts), cap));
+}
+
+template <typename T>
+int mu_run(const T* X, const Shape& sh, T* const* factors, int64_t R, const int* free_modes,
+           int n_free, int n_iter_max, double tol, int crit, double* errors, int* n_errors,
+           void* ws, size_t ws_bytes, cudaStream_t st) {
+  std::vector<MttkrpPlan> plans;
+  int nparts = 0;
+  MuLayout L;
+  int rc = mu_layout<T>(sh, R, n_iter_max, &plans, &nparts, &L);
+  if (rc) return rc;
+  if (!ws || ws_bytes < L.bytes) return set_error(TLGB_EWORKSPACE, "cp_nn_mu: workspace too small");
+  rc = als_prepare(TypeCode<T>::value);
+  if (rc) return rc;
+  char* base = static_cast<char*>(ws);
+  AlsCtrl* ctrl = reinterpret_cast<AlsCtrl*>(base + L.ctrl);
+  double* derr = reinterpret_cast<double*>(base + L.errors);
+  double* G = reinterpret_cast<double*>(base + L.G);
+  double* V = reinterpret_cast<double*>(base + L.V);
+  T* partial = reinterpret_cast<T*>(base + L.partial);
+  double* gpart = reinterpret_cast<double*>(base + L.gpart);
+  double* ipart = reinterpret_cast<double*>(base + L.ipart);
+  double* sumsq = reinterpret_cast<double*>(base + L.sumsq);
+  const int N = sh.ndim;
+  const int RR = (int)(R * R);
+  const int* done = &ctrl->done;
+  const T eps = std::numeric_limits<T>::epsilon();
+
+  TLGB_CUDA_TRY(cudaMemsetAsync(ctrl, 0, sizeof(AlsCtrl), st));
+  rc = als_launch_sumsq(TypeCode<T>::value, X, sh.numel, sumsq, kMuSumsqBlocks, ctrl, st);
+  if (rc) return rc;
+  for (int k = 0; k < N; ++k) {
+    rc = als_launch_gram<T>(factors[k], sh.dim[k], (int)R, gpart, nparts, G + (size_t)k * RR,
+                            done, st);
+    if (rc) return rc;
+  }
+  const T* cf[kMaxModes];
+  for (int k = 0; k < N; ++k) cf[k] = factors[k];
+  const int last = free_modes[n_free - 1];
+  int it = 0;
+  AlsCtrl hc{};
+  for (; it < n_iter_max; ++it) {
+    int last_nb = 0;
+    for (int q = 0; q < n_free; ++q) {
+      const int mode = free_modes[q];
+      k_mu_accum<<<(RR + 255) / 256, 256, 0, st>>>(G, N, mode, (int)R, V, done);
+      TLGB_LAUNCH_CHECK();
+      rc = mttkrp_launch_partials<T>(plans[mode], X, cf, nullptr, partial, done, st);
+      if (rc) return rc;
+      const int64_t I = sh.dim[mode];
+      const int64_t rpb = mu_rows_per_block(I, (int)R, nparts);
+      const int nb = (int)ceil_div(I, rpb);
+      k_mu_update<T><<<nb, kMuThreads, (size_t)rpb * R * sizeof(double), st>>>(
+          partial, plans[mode].splits, I, (int)R, V, eps, factors[mode],
+          mode == last ? ipart : nullptr, done, rpb);
+      TLGB_LAUNCH_CHECK();
+      if (mode == last) last_nb = nb;
+      rc = als_launch_gram<T>(factors[mode], I, (int)R, gpart, nparts, G + (size_t)mode * RR,
+                              done, st);
+      if (rc) return rc;
+    }
+    if (tol > 0.0) {
+      rc = als_launch_fit<T>(G, N, (int)R, nullptr, ipart, last_nb, ctrl, derr, n_iter_max, tol,
+                             crit, st);
+      if (rc) return rc;
+      if (((it + 1) % kMuCheckEvery) == 0 || it + 1 == n_iter_max) {
+        TLGB_CUDA_TRY(cudaMemcpyAsync(&hc, ctrl, sizeof(AlsCtrl), cudaMemcpyDeviceToHost, st));
+        TLGB_CUDA_TRY(cudaStreamSynchronize(st));
+        if (hc.done) break;
+      }
+    }
+  }
+  TLGB_CUDA_TRY(cudaMemcpyAsync(&hc, ctrl, sizeof(AlsCtrl), cudaMemcpyDeviceToHost, st));
+  TLGB_CUDA_TRY(cudaStreamSynchronize(st));
+  const int ne = (tol > 0.0) ? std::min(hc.iter, n_iter_max) : 0;
+  if (n_errors) *n_errors = ne;
+  if (errors && ne > 0)
+    TLGB_CUDA_TRY(cudaMemcpy(errors, derr, sizeof(double) * ne, cudaMemcpyDeviceToHost));
+  return TLGB_OK;
+}
+
+int check_nn_args(int dtype, const int64_t* shape, int ndim, int64_t rank) {
+  TLGB_CHECK_ARG(dtype == TLGB_F32 || dtype == TLGB_F64, "cp_nn_mu: dtype must be f32 or f64");
+  TLGB_CHECK_ARG(shape != nullptr, "cp_nn_mu: null shape");
+  TLGB_CHECK_ARG(ndim >= 2 && ndim <= kMaxModes, "cp_nn_mu: ndim must be in [2, 8]");
+  TLGB_CHECK_ARG(rank >= 1, "cp_nn_mu: rank must be >= 1");
+  for (int k = 0; k < ndim; ++k) TLGB_CHECK_ARG(shape[k] >= 1, "cp_nn_mu: empty mode");
+  return TLGB_OK;
+}
+
+}  // namespace
+}  // namespace tlgb
+
+using namespace tlgb;
+
+extern "C" int tlgb_cp_nn_mu_workspace_size(int dtype, int ndim, const int64_t* shape,
+                                            int64_t rank, int n_iter_max, size_t* bytes) {
+  clear_error();
+  int rc = check_nn_args(dtype, shape, ndim, rank);
+  if (rc) return rc;
+  TLGB_CHECK_ARG(bytes != nullptr && n_iter_max >= 0, "cp_nn_mu_workspace_size: bad argument");
+  Shape sh = make_shape(ndim, shape);
+  std::vector<MttkrpPlan> plans;
+  int nparts = 0;
+  MuLayout L;
+  rc = (dtype == TLGB_F64) ? mu_layout<double>(sh, rank, n_iter_max, &plans, &nparts, &L)
+                           : mu_layout<float>(sh, rank, n_iter_max, &plans, &nparts, &L);
+  if (rc) return rc;
+  *bytes = L.bytes;
+  return TLGB_OK;
+}
+
+extern "C" int tlgb_cp_nn_mu(int dtype, const void* X, int ndim, const int64_t* shape,
+                             void* const* factors, int64_t rank, const int* free_modes,
+                             int n_free, int n_iter_max, double tol, int cvg_criterion,
+                             double* errors, int* n_errors, void* workspace,
+                             size_t workspace_bytes, void* stream) {
+  clear_error();
+  int rc = check_nn_args(dtype, shape, ndim, rank);
+  if (rc) return rc;
+  TLGB_CHECK_ARG(X && factors && free_modes, "cp_nn_mu: null pointer");
+  TLGB_CHECK_ARG(n_free >= 1 && n_free <= ndim, "cp_nn_mu: bad number of free modes");
+  TLGB_CHECK_ARG(free_modes[n_free - 1] == ndim - 1, "cp_nn_mu: the last mode must be free");
+  for (int q = 0; q < n_free; ++q)
+    TLGB_CHECK_ARG(free_modes[q] >= 0 && free_modes[q] < ndim &&
+                       (q == 0 || free_modes[q] > free_modes[q - 1]),
+                   "cp_nn_mu: free modes must be ascending and in range");
+  for (int k = 0; k < ndim; ++k) TLGB_CHECK_ARG(factors[k] != nullptr, "cp_nn_mu: null factor");
+  TLGB_CHECK_ARG(n_iter_max >= 0 && tol >= 0.0, "cp_nn_mu: bad n_iter_max or tol");
+  TLGB_CHECK_ARG(cvg_criterion == 0 || cvg_criterion == 1, "cp_nn_mu: bad cvg_criterion");
+  Shape sh = make_shape(ndim, shape);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (dtype == TLGB_F64)
+    return mu_run<double>((const double*)X, sh, (double* const*)factors, rank, free_modes, n_free,
+                          n_iter_max, tol, cvg_criterion, errors, n_errors, workspace,
+                          workspace_bytes, st);
+  return mu_run<float>((const float*)X, sh, (float* const*)factors, rank, free_modes, n_free,
+                       n_iter_max, tol, cvg_criterion, errors, n_errors, workspace,
+                       workspace_bytes, st);
+}
+
+extern "C" int tlgb_sum(int dtype, const void* X, int64_t n, double* out, void* workspace,
+                        size_t workspace_bytes, void* stream) {
+  clear_error();
+  TLGB_CHECK_ARG(dtype == TLGB_F32 || dtype == TLGB_F64, "sum: dtype must be f32 or f64");
+  TLGB_CHECK_ARG(X && out && n >= 1, "sum: bad argument");
+  constexpr int kBlocks = 256;
+  TLGB_CHECK_ARG(workspace && workspace_bytes >= kBlocks * sizeof(double),
+                 "sum: workspace too small");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  double* part = static_cast<double*>(workspace);
+  if (dtype == TLGB_F64)
+    k_sum_part<double><<<kBlocks, 256, 0, st>>>((const double*)X, n, part);
+  else
+    k_sum_part<float><<<kBlocks, 256, 0, st>>>((const float*)X, n, part);
+  TLGB_LAUNCH_CHECK();
+  k_sum_final<<<1, 32, 0, st>>>(part, kBlocks, out);
+  TLGB_LAUNCH_CHECK();
+  return TLGB_OK;
+}
+
+extern "C" int tlgb_nndsvd_columns(int dtype, const void* U, const void* S, const void* Y,
+                                   int64_t I, int64_t k, int64_t L, int64_t Tt, int fill,
+                                   double avg, void* W, void* workspace, size_t workspace_bytes,
+                                   void* stream) {
+  clear_error();
+  TLGB_CHECK_ARG(dtype == TLGB_F32 || dtype == TLGB_F64, "nndsvd: dtype must be f32 or f64");
+  TLGB_CHECK_ARG(U && S && Y && W && I >= 1 && k >= 1 && L >= 1 && Tt >= 1,
+                 "nndsvd: bad argument");
+  const size_t es = dtype == TLGB_F64 ? 8 : 4;
+  TLGB_CHECK_ARG(workspace && workspace_bytes >= 2 * (size_t)k * es, "nndsvd: workspace too small");
+  TLGB_CHECK_ARG(k <= 65535, "nndsvd: too many columns");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (dtype == TLGB_F64) {
+    k_posneg_norms<double><<<(unsigned)k, 256, 0, st>>>((const double*)Y, L, (int)k, Tt,
+                                                        (double*)workspace);
+    TLGB_LAUNCH_CHECK();
+    k_nndsvd_columns<double><<<(unsigned)k, 256, 0, st>>>(
+        (const double*)U, (const double*)S, (const double*)workspace, I, (int)k,
+        std::numeric_limits<double>::epsilon(), fill, avg, (double*)W);
+  } else {
+    k_posneg_norms<float><<<(unsigned)k, 256, 0, st>>>((const float*)Y, L, (int)k, Tt,
+                                                       (float*)workspace);
+    TLGB_LAUNCH_CHECK();
+    k_nndsvd_columns<float><<<(unsigned)k, 256, 0, st>>>(
+        (const float*)U, (const float*)S, (const float*)workspace, I, (int)k,
+        std::numeric_limits<float>::epsilon(), fill, (float)avg, (float*)W);
+  }
+  TLGB_LAUNCH_CHECK();
+  return TLGB_OK;
+}

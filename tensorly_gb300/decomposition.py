@@ -474,6 +474,102 @@ class Tucker(DecompositionMixin):
 # ----------------------------------------------------------------------------
 # Batched CP-ALS
 # ----------------------------------------------------------------------------
+def non_negative_parafac(tensor, rank, n_iter_max=100, init="svd", svd="truncated_svd",
+                         tol=10e-7, random_state=None, verbose=0, normalize_factors=False,
+                         return_errors=False, mask=None, cvg_criterion="abs_rec_error",
+                         fixed_modes=None):
+    """Non-negative CP by multiplicative updates
+    (tensorly/decomposition/_nn_cp.py:26-183), same signature and returns.
+
+    The initial factors are ``initialize_cp(..., non_negative=True)``: for
+    ``init='svd'`` the NNDSVDA form of each unfolding's SVD, then absolute
+    values.  The loop runs in ``tlgb_cp_nn_mu``: per free mode, the Hadamard
+    product of the other Grams, the MTTKRP and the update
+    ``A * clip(M, eps) / clip(A accum, eps)``; with ``tol`` the error of every
+    iteration and the reference's stop test.  ``normalize_factors`` and masks
+    are not supported.
+    """
+    if mask is not None:
+        raise NotImplementedError("masked non_negative_parafac is not supported by tensorly_gb300")
+    if normalize_factors:
+        raise NotImplementedError("non_negative_parafac with normalize_factors=True is not "
+                                  "supported by tensorly_gb300")
+    if tol and n_iter_max > 1 and cvg_criterion not in ("abs_rec_error", "rec_error"):
+        raise TypeError("Unknown convergence criterion")   # _nn_cp.py:166-167
+    x, placement = to_device(tensor)
+    code = dtype_code(x)
+    x = x.contiguous()
+    rank = validate_cp_rank(tuple(x.shape), rank=rank)
+    if x.ndim < 2:
+        raise NotImplementedError("non_negative_parafac needs at least two modes")
+    _, factors = initialize_cp(x, rank, init=init, svd=svd, non_negative=True,
+                               random_state=random_state, normalize_factors=False)
+    factors = [f.to(x.dtype).contiguous().clone() for f in factors]
+    fixed = [] if fixed_modes is None else list(fixed_modes)
+    if x.ndim - 1 in fixed:
+        warnings.warn("You asked for fixing the last mode, which is not supported while tol "
+                      "is fixed.\n The last mode will not be fixed. Consider using tl.moveaxis()")
+        fixed.remove(x.ndim - 1)
+    free = [m for m in range(x.ndim) if m not in fixed]
+    lib = _lib.lib()
+    shape = (ctypes.c_int64 * x.ndim)(*x.shape)
+    nbytes = ctypes.c_size_t(0)
+    _lib.check(lib.tlgb_cp_nn_mu_workspace_size(code, x.ndim, shape, rank, int(n_iter_max),
+                                                ctypes.byref(nbytes)))
+    ws = workspace(nbytes.value, x.device)
+    fptrs = (ctypes.c_void_p * x.ndim)(*[f.data_ptr() for f in factors])
+    free_arr = (ctypes.c_int * len(free))(*free)
+    errs = (ctypes.c_double * max(1, int(n_iter_max)))()
+    n_err = ctypes.c_int(0)
+    _lib.check(lib.tlgb_cp_nn_mu(code, x.data_ptr(), x.ndim, shape, fptrs, rank, free_arr,
+                                 len(free), int(n_iter_max), float(tol) if tol else 0.0,
+                                 0 if cvg_criterion == "abs_rec_error" else 1, errs,
+                                 ctypes.byref(n_err), ptr(ws), ws.numel(), stream_of(x)))
+    weights = torch.ones(rank, dtype=x.dtype, device=x.device)
+    cp = CPTensor((placement.back(weights), [placement.back(f) for f in factors]))
+    if return_errors:
+        return cp, [float(errs[i]) for i in range(n_err.value)]
+    return cp
+
+
+class CP_NN:
+    """sklearn-style wrapper of ``non_negative_parafac``
+    (tensorly/decomposition/_nn_cp.py:382-514): every keyword is passed
+    through; ``decomposition_`` and ``errors_`` hold the last fit."""
+
+    def __init__(self, rank, n_iter_max=100, init="svd", svd="truncated_svd", tol=10e-7,
+                 random_state=None, verbose=0, normalize_factors=False, mask=None,
+                 cvg_criterion="abs_rec_error", fixed_modes=None):
+        self.rank = rank
+        self.n_iter_max = n_iter_max
+        self.init = init
+        self.svd = svd
+        self.tol = tol
+        self.random_state = random_state
+        self.verbose = verbose
+        self.normalize_factors = normalize_factors
+        self.mask = mask
+        self.cvg_criterion = cvg_criterion
+        self.fixed_modes = fixed_modes
+
+    def fit_transform(self, tensor):
+        cp, errors = non_negative_parafac(
+            tensor, rank=self.rank, n_iter_max=self.n_iter_max, init=self.init, svd=self.svd,
+            tol=self.tol, random_state=self.random_state, verbose=self.verbose,
+            normalize_factors=self.normalize_factors, mask=self.mask,
+            cvg_criterion=self.cvg_criterion, fixed_modes=self.fixed_modes, return_errors=True)
+        self.decomposition_ = cp
+        self.errors_ = errors
+        return self.decomposition_
+
+    def fit(self, tensor):
+        self.fit_transform(tensor)
+        return self
+
+    def __repr__(self):
+        return f"Rank-{self.rank} Non-Negative CP decomposition."
+
+
 class BatchedProblem:
     """Many small 3-way f32 tensors packed for ``tlgb_cp_als_batched``.
 

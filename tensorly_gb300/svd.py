@@ -58,10 +58,13 @@ def _n_eigenvecs(rows, cols, n_eigenvecs):
 
 def svd_interface_unfolding(tensor, mode, n_eigenvecs, method="truncated_svd",
                             non_negative=False, flip_sign=True):
-    """(U, S) of ``svd_interface(unfold(tensor, mode), n_eigenvecs, method)``
-    (tensorly/tenalg/svd.py:366-447) without forming the unfolding."""
-    if non_negative:
-        raise NotImplementedError("non-negative SVD initialisation is not supported")
+    """(U, S) of ``svd_interface(unfold(tensor, mode), n_eigenvecs, method,
+    non_negative=non_negative)`` (tensorly/tenalg/svd.py:366-447) without
+    forming the unfolding; ``non_negative`` (True = 'nndsvda', or 'nndsvd')
+    replaces U by the NNDSVD factor W (``:443-444``, ``:68-134``)."""
+    if non_negative not in (None, False, True, "nndsvd", "nndsvda"):
+        raise ValueError(f'Invalid nntype parameter: got {non_negative} instead of one of '
+                         '("nndsvd", "nndsvda")')
     if not (method in SVD_FUNS):
         if callable(method) or method == "randomized_svd":
             raise NotImplementedError(f"svd method {method!r} is not supported by tensorly_gb300")
@@ -73,7 +76,41 @@ def svd_interface_unfolding(tensor, mode, n_eigenvecs, method="truncated_svd",
     cols = x.numel() // max(1, rows)
     ucols, scount = _n_eigenvecs(rows, cols, n_eigenvecs)
     U, S = _svd_unfolding_raw(x, mode, ucols, flip=flip_sign)
-    return U, S[:scount]
+    S = S[:scount]
+    if non_negative not in (None, False):
+        U = _nndsvd_unfolding(x, mode, U, S, "nndsvda" if non_negative is True else non_negative)
+    return U, S
+
+
+def _nndsvd_unfolding(x, mode, U, S, nntype):
+    """W of NNDSVD (tensorly/tenalg/svd.py:68-134) for the mode-`mode`
+    unfolding M of x from its (U, S).  V's rows enter through U^T M = S V,
+    which is the mode-n product of x with U^T; the norms of their positive
+    and negative parts, the column choice and the fill run in the library."""
+    from .tenalg import mode_dot
+    lib = _lib.lib()
+    k = min(int(U.shape[1]), int(S.shape[0]))
+    Uk = U[:, :k].contiguous()
+    Y = mode_dot(x, Uk.t().contiguous(), mode)
+    L = int(np.prod(x.shape[:mode])) if mode > 0 else 1
+    Tt = int(np.prod(x.shape[mode + 1:])) if mode + 1 < x.ndim else 1
+    code = dtype_code(x)
+    ws = torch.empty(max(256, 2 * k) * 8, dtype=torch.uint8, device=x.device)
+    total = torch.zeros(1, dtype=torch.float64, device=x.device)
+    st = stream_of(x)
+    _lib.check(lib.tlgb_sum(code, x.data_ptr(), x.numel(), total.data_ptr(), ws.data_ptr(),
+                            ws.numel(), st))
+    fill = 1 if nntype == "nndsvda" else 0
+    avg = float(total.item()) / x.numel() if fill else 0.0
+    W = torch.empty_like(Uk)
+    _lib.check(lib.tlgb_nndsvd_columns(code, Uk.data_ptr(), S.contiguous().data_ptr(),
+                                       Y.contiguous().data_ptr(), int(Uk.shape[0]), k, L, Tt,
+                                       fill, avg, W.data_ptr(), ws.data_ptr(), ws.numel(), st))
+    if U.shape[1] > k:   # columns past the singular values stay zero before the fill
+        extra = torch.full((U.shape[0], U.shape[1] - k), avg if fill else 0.0,
+                           dtype=U.dtype, device=U.device)
+        W = torch.cat([W, extra], dim=1)
+    return W
 
 
 def svd_flip(U, V, u_based_decision=True):

@@ -14,7 +14,8 @@ Outputs (committed, small, platform independent):
   backend with ``np.random.seed(0)``; the recorders wrap the functions the
   test modules call and the ``assert_*`` helpers they use (which additionally
   records the known answers the tests compare against).
-* ``reference_runs.pkl``: reference ``parafac`` / ``tucker`` / ``svd_interface``
+* ``reference_runs.pkl``: reference ``parafac`` / ``non_negative_parafac`` /
+  ``tucker`` / ``svd_interface``
   outputs on seeded inputs (the tensors are regenerated from their seeds by
   ``tensorly_gb300.workloads`` or by the case's own RandomState; each record
   stores a checksum of the input so a regeneration mismatch is caught).
@@ -154,6 +155,29 @@ def reference_runs():
             cp, errs = parafac(x, g["rank"], return_errors=True, **copy.deepcopy(kw))
         except Exception as e:
             raise RuntimeError(f"reference parafac failed on case {name}") from e
+        runs.append({"case": name, "gen": {"fn": "small", **g}, "checksum": cs(x),
+                     "kwargs": {"rank": g["rank"], **kw},
+                     "weights": np.array(cp.weights),
+                     "factors": [np.array(f) for f in cp.factors],
+                     "errors": [float(e) for e in errs]})
+
+    # non-negative CP by multiplicative updates (tensorly/decomposition/_nn_cp.py)
+    from tensorly.decomposition import non_negative_parafac
+    nn_variants = [
+        ("nn_mu_random", dict(shape=(9, 8, 7), rank=3, seed=51),
+         dict(init="random", random_state=13, n_iter_max=60, tol=1e-12)),
+        ("nn_mu_svd", dict(shape=(12, 10, 9), rank=3, seed=52),
+         dict(init="svd", n_iter_max=40, tol=1e-12)),
+        ("nn_mu_4way_fixed", dict(shape=(6, 5, 7, 4), rank=2, seed=53),
+         dict(init="random", random_state=14, n_iter_max=30, tol=1e-12, fixed_modes=[1])),
+        ("nn_mu_stop", dict(shape=(10, 9, 8), rank=2, seed=54),
+         dict(init="svd", n_iter_max=500, tol=1e-7)),
+        ("nn_mu_f32", dict(shape=(16, 12, 10), rank=4, seed=55, dtype=np.float32),
+         dict(init="random", random_state=15, n_iter_max=30, tol=1e-12)),
+    ]
+    for name, g, kw in nn_variants:
+        x = small(g["seed"], g["shape"], g["rank"], g.get("dtype", np.float64))
+        cp, errs = non_negative_parafac(x, g["rank"], return_errors=True, **copy.deepcopy(kw))
         runs.append({"case": name, "gen": {"fn": "small", **g}, "checksum": cs(x),
                      "kwargs": {"rank": g["rank"], **kw},
                      "weights": np.array(cp.weights),

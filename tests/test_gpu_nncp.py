@@ -1,0 +1,76 @@
+"""Non-negative CP (multiplicative updates) and the NNDSVD initialisation on
+the GPU against the reference runs (tests/golden) and the NumPy oracle.
+
+Tolerances: f64 runs match the reference to 1e-9 relative (factors, error
+list, same number of iterations); the f32 run to 1e-3 on the factors and 1e-4
+on the errors."""
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from golden_inputs import regenerate
+
+pytestmark = pytest.mark.gpu
+
+NN_CASES = ["nn_mu_random", "nn_mu_svd", "nn_mu_4way_fixed", "nn_mu_stop", "nn_mu_f32"]
+
+
+def host(t):
+    return t.detach().cpu().numpy()
+
+
+@pytest.mark.parametrize("case", NN_CASES)
+def test_non_negative_parafac_matches_reference(gb300, golden, case):
+    run = golden["runs"][case]
+    x = regenerate(run)
+    kw = dict(run["kwargs"])
+    rank = kw.pop("rank")
+    (w, f), errs = gb300.non_negative_parafac(torch.as_tensor(x, device="cuda"), rank,
+                                              return_errors=True, **kw)
+    f32 = x.dtype == np.float32
+    assert len(errs) == len(run["errors"])
+    np.testing.assert_allclose(errs, run["errors"], rtol=1e-4 if f32 else 1e-9,
+                               atol=1e-6 if f32 else 1e-12)
+    np.testing.assert_allclose(host(w), run["weights"])
+    for a, b in zip(f, run["factors"]):
+        a = host(a)
+        assert (a >= 0).all()
+        tol = 1e-3 if f32 else 1e-9
+        np.testing.assert_allclose(a, b, rtol=tol, atol=tol * np.abs(b).max())
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_nndsvda_unfolding_matches_oracle(gb300, mode):
+    from tensorly_gb300.svd import svd_interface_unfolding
+    rs = np.random.RandomState(3 + mode)
+    x = rs.rand(11, 9, 13) + 0.1 * rs.randn(11, 9, 13)
+    W, S = svd_interface_unfolding(torch.as_tensor(x, device="cuda"), mode, 4,
+                                   non_negative=True)
+    Wo, So, _ = oracle.svd_interface(oracle.unfold(x, mode), n_eigenvecs=4, non_negative=True)
+    np.testing.assert_allclose(host(S), So, rtol=1e-10)
+    np.testing.assert_allclose(host(W), Wo, rtol=1e-9, atol=1e-12)
+
+
+def test_cp_nn_estimator_and_host_inputs(gb300, golden):
+    run = golden["runs"]["nn_mu_random"]
+    x = regenerate(run)
+    kw = dict(run["kwargs"])
+    rank = kw.pop("rank")
+    est = gb300.CP_NN(rank, **kw)
+    cp = est.fit_transform(x)                      # NumPy in, NumPy out
+    assert isinstance(cp.factors[0], np.ndarray)
+    np.testing.assert_allclose(est.errors_, run["errors"], rtol=1e-9, atol=1e-12)
+    for a, b in zip(cp.factors, run["factors"]):
+        np.testing.assert_allclose(a, b, rtol=1e-9, atol=1e-9 * np.abs(b).max())
+
+
+def test_non_negative_parafac_unsupported_options_raise(gb300):
+    x = torch.rand(5, 6, 7, device="cuda", dtype=torch.float64)
+    with pytest.raises(NotImplementedError):
+        gb300.non_negative_parafac(x, 2, normalize_factors=True)
+    with pytest.raises(NotImplementedError):
+        gb300.non_negative_parafac(x, 2, mask=torch.ones_like(x))
+    with pytest.raises(TypeError):
+        gb300.non_negative_parafac(x, 2, cvg_criterion="nope")

@@ -67,6 +67,23 @@ def test_oracle_parafac_matches_reference(golden, case):
         np.testing.assert_allclose(a, b, rtol=tol, atol=tol * np.abs(b).max())
 
 
+@pytest.mark.parametrize("case", ["nn_mu_random", "nn_mu_svd", "nn_mu_4way_fixed",
+                                  "nn_mu_stop", "nn_mu_f32"])
+def test_oracle_non_negative_parafac_matches_reference(golden, case):
+    run = golden["runs"][case]
+    x = regenerate(run)
+    kw = dict(run["kwargs"])
+    rank = kw.pop("rank")
+    (w, f), errs = oracle.non_negative_parafac(x, rank, return_errors=True, **kw)
+    tol = 1e-5 if x.dtype == np.float32 else 1e-11
+    assert len(errs) == len(run["errors"])
+    np.testing.assert_allclose(errs, run["errors"], rtol=tol, atol=tol * 1e-2)
+    np.testing.assert_allclose(w, run["weights"], rtol=tol, atol=tol)
+    for a, b in zip(f, run["factors"]):
+        assert (a >= 0).all()
+        np.testing.assert_allclose(a, b, rtol=tol, atol=tol * np.abs(b).max())
+
+
 @pytest.mark.parametrize("case", ["tucker_svd", "tucker_random", "tucker_4way"])
 def test_oracle_tucker_matches_reference(golden, case):
     run = golden["runs"][case]
