@@ -27,7 +27,7 @@ __all__ = [
     "truncated_svd", "svd_interface", "random_cp", "cp_to_tensor", "cp_norm",
     "cp_normalize", "validate_cp_rank", "initialize_cp", "error_calc",
     "parafac", "initialize_tucker", "partial_tucker", "tucker", "non_negative_parafac",
-    "make_svd_non_negative",
+    "make_svd_non_negative", "hals_nnls", "non_negative_parafac_hals",
     "tucker_to_tensor", "validate_tucker_rank", "parafac_sweeps",
 ]
 
@@ -422,6 +422,121 @@ def non_negative_parafac(tensor, rank, n_iter_max=100, init="svd", svd="truncate
                 weights, factors = cp_normalize((weights, factors))
         if tol:
             rec_error = error_calc(tensor, norm_tensor, weights, factors, mttkrp) / norm_tensor
+            rec_errors.append(rec_error)
+            if iteration >= 1:
+                dec = rec_errors[-2] - rec_errors[-1]
+                if cvg_criterion == "abs_rec_error":
+                    stop = abs(dec) < tol
+                elif cvg_criterion == "rec_error":
+                    stop = dec < tol
+                else:
+                    raise TypeError("Unknown convergence criterion")
+                if stop:
+                    break
+        if normalize_factors:
+            weights, factors = cp_normalize((weights, factors))
+    cp = (weights, factors)
+    return (cp, rec_errors) if return_errors else cp
+
+
+def hals_nnls(UtM, UtU, V=None, n_iter_max=500, tol=1e-8, sparsity_coefficient=None,
+              ridge_coefficient=None, nonzero_rows=False, exact=False, epsilon=0.0):
+    """tensorly/solvers/nnls.py:5-150: row-wise (Gauss-Seidel) HALS for
+    min_{V >= epsilon} ||M - U V||.  The inner stop test compares the sum,
+    over the rows k updated in an iteration, of ||V - newV||^2 with newV
+    broadcast against every row of V (the reference's expression), to tol
+    times the first iteration's sum."""
+    rank = UtM.shape[0]
+    if V is None:
+        V = np.linalg.solve(UtU, UtM)
+        V = np.clip(V, 0, None)
+        scale = np.sum(UtM * V) / np.sum(UtU * (V @ V.T))
+        V = V * scale
+    V = np.array(V, copy=True)
+    if exact:
+        n_iter_max = 50000
+        tol = 1e-16
+    rec_error0 = None
+    for iteration in range(n_iter_max):
+        rec_error = 0
+        for k in range(rank):
+            if UtU[k, k]:
+                num = UtM[k, :] - UtU[k, :] @ V + UtU[k, k] * V[k, :]
+                den = UtU[k, k]
+                if sparsity_coefficient is not None:
+                    num = num - sparsity_coefficient
+                if ridge_coefficient is not None:
+                    den = den + 2 * ridge_coefficient
+                newV = np.clip(num / den, epsilon, None)
+                rec_error += np.linalg.norm(V - newV) ** 2
+                V[k, :] = newV
+                if nonzero_rows and np.all(V[k, :] == 0):
+                    V[k, :] = np.finfo(V.dtype).eps * np.max(V)
+            elif nonzero_rows:
+                raise ValueError("Column " + str(k) + " of U is zero with nonzero condition")
+        if iteration == 0:
+            rec_error0 = rec_error
+        if rec_error < tol * rec_error0:
+            break
+    return V
+
+
+def non_negative_parafac_hals(tensor, rank, n_iter_max=100, init="svd", svd="truncated_svd",
+                              tol=10e-8, random_state=None, sparsity_coefficients=None,
+                              fixed_modes=None, nn_modes="all", exact=False,
+                              normalize_factors=False, verbose=False, return_errors=False,
+                              cvg_criterion="abs_rec_error"):
+    """tensorly/decomposition/_nn_cp.py:186-377: non-negative CP by HALS
+    (Gillis & Glineur 2012).  Per free mode: the Hadamard of the other Grams,
+    the MTTKRP, then ``hals_nnls(M^T, pinv, A^T, n_iter_max=100)`` (or the
+    unconstrained solve for modes outside ``nn_modes``); the error from the
+    last MTTKRP when ``tol``."""
+    tensor = np.asarray(tensor)
+    weights, factors = initialize_cp(tensor, rank, init=init, svd=svd, random_state=random_state,
+                                     normalize_factors=normalize_factors, non_negative=True)
+    if weights is None:
+        weights = np.ones(rank, dtype=tensor.dtype)
+    factors = list(factors)
+    norm_tensor = norm(tensor)
+    n_modes = tensor.ndim
+    if sparsity_coefficients is None or isinstance(sparsity_coefficients, float):
+        sparsity_coefficients = [sparsity_coefficients] * n_modes
+    sparsity_coefficients = list(sparsity_coefficients)
+    fixed_modes = [] if fixed_modes is None else list(fixed_modes)
+    if nn_modes == "all":
+        nn_modes = set(range(n_modes))
+    elif nn_modes is None:
+        nn_modes = set()
+    for fixed_value in fixed_modes:
+        sparsity_coefficients[fixed_value] = None
+    for mode in range(n_modes):
+        if sparsity_coefficients[mode] is not None:
+            warnings.warn("Sparsity coefficient is ignored in unconstrained modes.")
+    modes = [m for m in range(n_modes) if m not in fixed_modes]
+    rec_errors = []
+    mttkrp = None
+    for iteration in range(n_iter_max):
+        for mode in modes:
+            pseudo_inverse = np.ones((rank, rank), dtype=tensor.dtype)
+            for i, factor in enumerate(factors):
+                if i != mode:
+                    pseudo_inverse = pseudo_inverse * (factor.T @ factor)
+            pseudo_inverse = weights.reshape(-1, 1) * pseudo_inverse * weights.reshape(1, -1)
+            mttkrp = unfolding_dot_khatri_rao(tensor, (weights, factors), mode)
+            if mode in nn_modes:
+                nn_factor = hals_nnls(mttkrp.T, pseudo_inverse, factors[mode].T, n_iter_max=100,
+                                      sparsity_coefficient=sparsity_coefficients[mode],
+                                      exact=exact)
+                factors[mode] = nn_factor.T
+            else:
+                factors[mode] = np.linalg.solve(pseudo_inverse.T, mttkrp.T).T
+            if normalize_factors and mode != modes[-1]:
+                weights, factors = cp_normalize((weights, factors))
+        if tol:
+            factors_norm = cp_norm((weights, factors))
+            iprod = np.sum(np.sum(mttkrp * factors[-1], axis=0))
+            rec_error = np.sqrt(np.abs(norm_tensor ** 2 + factors_norm ** 2 - 2 * iprod)) \
+                / norm_tensor
             rec_errors.append(rec_error)
             if iteration >= 1:
                 dec = rec_errors[-2] - rec_errors[-1]

@@ -184,6 +184,31 @@ def reference_runs():
                      "factors": [np.array(f) for f in cp.factors],
                      "errors": [float(e) for e in errs]})
 
+    # non-negative CP by HALS (tensorly/decomposition/_nn_cp.py:186-377)
+    from tensorly.decomposition import non_negative_parafac_hals
+    hals_variants = [
+        ("nn_hals_random", dict(shape=(9, 8, 7), rank=3, seed=61),
+         dict(init="random", random_state=16, n_iter_max=25, tol=1e-12)),
+        ("nn_hals_svd", dict(shape=(12, 10, 9), rank=3, seed=62),
+         dict(init="svd", n_iter_max=20, tol=1e-12)),
+        ("nn_hals_sparse_fixed", dict(shape=(8, 7, 6, 5), rank=2, seed=63),
+         dict(init="random", random_state=17, n_iter_max=15, tol=1e-12,
+              sparsity_coefficients=[0.01, None, 0.02, None], fixed_modes=[1])),
+        ("nn_hals_stop", dict(shape=(10, 9, 8), rank=2, seed=64),
+         dict(init="svd", n_iter_max=300, tol=1e-9)),
+        ("nn_hals_f32", dict(shape=(16, 12, 10), rank=4, seed=65, dtype=np.float32),
+         dict(init="random", random_state=18, n_iter_max=15, tol=1e-12)),
+    ]
+    for name, g, kw in hals_variants:
+        x = small(g["seed"], g["shape"], g["rank"], g.get("dtype", np.float64))
+        cp, errs = non_negative_parafac_hals(x, g["rank"], return_errors=True,
+                                             **copy.deepcopy(kw))
+        runs.append({"case": name, "gen": {"fn": "small", **g}, "checksum": cs(x),
+                     "kwargs": {"rank": g["rank"], **kw},
+                     "weights": np.array(cp.weights),
+                     "factors": [np.array(f) for f in cp.factors],
+                     "errors": [float(e) for e in errs]})
+
     # Tucker (HOOI) small cases
     tcases = [
         ("tucker_svd", dict(shape=(12, 10, 8), seed=31), dict(rank=[3, 4, 2], init="svd",

@@ -1,6 +1,8 @@
 """Pins the NumPy oracle to the reference: replays the reference's own
 tenalg unit-test calls and its parafac / tucker / svd runs (tests/golden)."""
 
+import warnings
+
 import numpy as np
 import pytest
 
@@ -79,6 +81,24 @@ def test_oracle_non_negative_parafac_matches_reference(golden, case):
     assert len(errs) == len(run["errors"])
     np.testing.assert_allclose(errs, run["errors"], rtol=tol, atol=tol * 1e-2)
     np.testing.assert_allclose(w, run["weights"], rtol=tol, atol=tol)
+    for a, b in zip(f, run["factors"]):
+        assert (a >= 0).all()
+        np.testing.assert_allclose(a, b, rtol=tol, atol=tol * np.abs(b).max())
+
+
+@pytest.mark.parametrize("case", ["nn_hals_random", "nn_hals_svd", "nn_hals_sparse_fixed",
+                                  "nn_hals_stop", "nn_hals_f32"])
+def test_oracle_non_negative_parafac_hals_matches_reference(golden, case):
+    run = golden["runs"][case]
+    x = regenerate(run)
+    kw = dict(run["kwargs"])
+    rank = kw.pop("rank")
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        (w, f), errs = oracle.non_negative_parafac_hals(x, rank, return_errors=True, **kw)
+    tol = 1e-5 if x.dtype == np.float32 else 1e-10
+    assert len(errs) == len(run["errors"])
+    np.testing.assert_allclose(errs, run["errors"], rtol=tol, atol=tol * 1e-2)
     for a, b in zip(f, run["factors"]):
         assert (a >= 0).all()
         np.testing.assert_allclose(a, b, rtol=tol, atol=tol * np.abs(b).max())
