@@ -323,6 +323,20 @@ int tlgb_cp_nn_mu(int dtype, const void* X, int ndim, const int64_t* shape, void
                   size_t workspace_bytes, void* stream);
 
 /*
+ * Non-negative CP by HALS: the loop of tensorly/decomposition/_nn_cp.py:186-377
+ * (non_negative_parafac_hals with nn_modes 'all', weights all one,
+ * normalize_factors=False) and its inner solver tensorly/solvers/nnls.py:5-150
+ * (hals_nnls, 100 iterations or, with exact, 50000 at tol 1e-16).  Arguments
+ * as tlgb_cp_nn_mu; sparsity: host array of ndim coefficients (NaN = none) or
+ * NULL.  The workspace is tlgb_cp_nn_mu_workspace_size's.
+ */
+int tlgb_cp_nn_hals(int dtype, const void* X, int ndim, const int64_t* shape,
+                    void* const* factors, int64_t rank, const int* free_modes, int n_free,
+                    int n_iter_max, double tol, int cvg_criterion, const double* sparsity,
+                    int exact, double* errors, int* n_errors, void* workspace,
+                    size_t workspace_bytes, void* stream);
+
+/*
  * Pieces of the non-negative SVD (NNDSVD, tensorly/tenalg/svd.py:68-134):
  *   tlgb_sum             sum of n elements into *out (device f64); workspace
  *                        >= 256 doubles

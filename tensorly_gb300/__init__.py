@@ -2,7 +2,8 @@
 
 Public API mirrors ``tensorly.decomposition`` and ``tensorly.tenalg``:
 
-    parafac, CP, initialize_cp, tucker, partial_tucker, Tucker, non_negative_parafac, CP_NN
+    parafac, CP, initialize_cp, tucker, partial_tucker, Tucker,
+    non_negative_parafac, CP_NN, non_negative_parafac_hals, CP_NN_HALS
     khatri_rao, unfolding_dot_khatri_rao, mode_dot, multi_mode_dot
     CPTensor, TuckerTensor, cp_norm, cp_normalize, cp_to_tensor, tucker_to_tensor
 
@@ -14,9 +15,9 @@ C ABI (``include/tensorly_gb300.h``); tensors are PyTorch CUDA tensors.
 from ._lib import GB300Error, SingularMatrixError, build, lib
 from .cp_tensor import (CPTensor, TuckerTensor, cp_norm, cp_normalize, cp_to_tensor,
                         tucker_to_tensor, validate_cp_rank, validate_tucker_rank)
-from .decomposition import (CP, CP_NN, Tucker, initialize_cp, initialize_tucker,
-                            non_negative_parafac, parafac, parafac_batched, partial_tucker,
-                            tucker)
+from .decomposition import (CP, CP_NN, CP_NN_HALS, Tucker, initialize_cp, initialize_tucker,
+                            non_negative_parafac, non_negative_parafac_hals, parafac,
+                            parafac_batched, partial_tucker, tucker)
 from .svd import svd_flip, svd_interface, truncated_svd
 from .random import check_random_state, random_cp
 from .tenalg import khatri_rao, mode_dot, multi_mode_dot, unfolding_dot_khatri_rao

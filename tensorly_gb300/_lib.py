@@ -142,6 +142,11 @@ SIGNATURES = [
       ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
       ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int), ctypes.c_void_p,
       ctypes.c_size_t, ctypes.c_void_p]),
+    ("tlgb_cp_nn_hals", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, _c_i64p, _c_vpp, ctypes.c_int64,
+      ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+      ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+      ctypes.POINTER(ctypes.c_int), ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     ("tlgb_sum", ctypes.c_int,
      [ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
       ctypes.c_size_t, ctypes.c_void_p]),

@@ -204,8 +204,139 @@ __global__ void k_sum_final(const double* part, int n, double* out) {
   }
 }
 
+// ---------------------------------------------------------------- HALS
+// HALS (tensorly/decomposition/_nn_cp.py:186-377 with the inner solver
+// tensorly/solvers/nnls.py:5-150): per free mode, M = MTTKRP is summed once,
+// then up to n_inner iterations of row-wise (Gauss-Seidel over k) updates of
+// V = A^T.  Every column of V (row of A) is an independent problem, so one
+// warp owns one row of A, keeps it in shared memory and runs the k loop; the
+// rows are coupled only by the inner stop test, whose sum over the block's
+// rows goes to a per-block partial, summed in a fixed order by k_hals_check
+// between iterations.
+
+// M (I x R, in the factor type) = the sum of the MTTKRP's split partials.
+template <typename T>
+__global__ void k_sum_splits_to(const T* __restrict__ partial, int splits, int64_t IR, T* M) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < IR;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    double m0 = 0.0, m1 = 0.0;
+    int p = 0;
+    for (; p + 1 < splits; p += 2) {
+      m0 += (double)partial[(int64_t)p * IR + e];
+      m1 += (double)partial[(int64_t)(p + 1) * IR + e];
+    }
+    if (p < splits) m0 += (double)partial[(int64_t)p * IR + e];
+    M[e] = (T)(m0 + m1);
+  }
+}
+
+constexpr int kHalsWarps = 8;
+
+// One HALS iteration: warp w of the block updates row i = block * 8 + w of A
+// for k = 0..R-1:
+//   num = M[i, k] - sum_s P[k, s] A[i, s] + P[k, k] A[i, k] (- sparsity)
+//   A[i, k] <- max(num / P[k, k], 0)            (rows k with P[k, k] == 0 kept)
+// and adds the reference's stop term ||V - newV||^2 (newV broadcast against
+// every row of V), which for this column is S2 - 2 newV S1 + R newV^2 with S1,
+// S2 the column's running sum and sum of squares.
+template <typename T>
+__global__ void __launch_bounds__(32 * kHalsWarps)
+k_hals_iter(const T* __restrict__ M, const double* __restrict__ P, int64_t I, int R, T* A,
+            double sparsity, int use_sparsity, double* part, const int* stop, const int* done) {
+  if (*done || *stop) return;
+  extern __shared__ double shs[];   // [kHalsWarps][R] rows of A (f64 copies)
+  __shared__ double red[kHalsWarps];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t i = (int64_t)blockIdx.x * kHalsWarps + warp;
+  double* v = shs + warp * R;
+  double err = 0.0;
+  if (i < I) {
+    double s1 = 0.0, s2 = 0.0;
+    for (int s = lane; s < R; s += 32) {
+      const double x = (double)A[i * R + s];
+      v[s] = x;
+      s1 += x;
+      s2 += x * x;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+      s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+    }
+    __syncwarp();
+    for (int k = 0; k < R; ++k) {
+      const double pkk = P[(int64_t)k * R + k];
+      if (pkk == 0.0) continue;
+      double dot = 0.0;
+      for (int s = lane; s < R; s += 32) dot = fma(P[(int64_t)k * R + s], v[s], dot);
+      for (int o = 16; o > 0; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
+      const double vk = v[k];
+      T num = (T)((double)M[i * R + k] - dot + pkk * vk);
+      if (use_sparsity) num = num - (T)sparsity;
+      T nv = num / (T)pkk;
+      nv = nv > (T)0 ? nv : (T)0;
+      const double n = (double)nv;
+      err += s2 - 2.0 * n * s1 + (double)R * n * n;
+      s1 += n - vk;
+      s2 += n * n - vk * vk;
+      __syncwarp();
+      if (lane == 0) v[k] = n;
+      __syncwarp();
+    }
+    for (int s = lane; s < R; s += 32) A[i * R + s] = (T)v[s];
+  }
+  if (lane == 0) red[warp] = err;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < kHalsWarps; ++w) t += red[w];
+    part[blockIdx.x] = t;
+  }
+}
+
+// After inner iteration t: total = the sum of the block partials (fixed order);
+// t == 0 records it as the reference error; stop when total < tol * that.
+__global__ void k_hals_check(const double* part, int nb, int t, double tol, double* e0, int* stop,
+                             const int* done) {
+  if (*done || *stop) return;
+  __shared__ double red[32];
+  double s = 0.0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) s += part[b];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
+    if (t == 0) *e0 = tot;
+    if (tot < tol * *e0) *stop = 1;
+  }
+}
+
+// <M, A> partial sums per block of rows (the error's inner product).
+template <typename T>
+__global__ void k_inner_part(const T* __restrict__ M, const T* __restrict__ A, int64_t n,
+                             double* part, const int* done) {
+  if (*done) return;
+  __shared__ double red[32];
+  double s = 0.0;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x)
+    s += (double)M[e] * (double)A[e];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    part[blockIdx.x] = t;
+  }
+}
+
+constexpr int kInnerBlocks = 128;
+
 struct MuLayout {
   size_t ctrl, errors, G, V, partial, gpart, ipart, sumsq, bytes;
+  size_t M, hpart, hstate;   // HALS: summed MTTKRP, inner-iteration partials, e0 + stop
 };
 
 int64_t mu_rows_per_block(int64_t I, int R, int nparts);
@@ -237,8 +368,12 @@ int mu_layout(const Shape& sh, int64_t R, int n_iter_max, std::vector<MttkrpPlan
   L->V = take(sizeof(double) * RR);
   L->partial = take(pmax);
   L->gpart = take(sizeof(double) * RR * (size_t)*nparts);
-  L->ipart = take(sizeof(double) * (size_t)nb_max);
+  L->ipart = take(sizeof(double) * (size_t)std::max<int64_t>(nb_max, kInnerBlocks));
   L->sumsq = take(sizeof(double) * kMuSumsqBlocks);
+  L->M = take(sizeof(T) * (size_t)imax * R);
+  L->hpart = take(sizeof(double) * (size_t)std::max<int64_t>(kInnerBlocks,
+                                                             ceil_div(imax, kHalsWarps)));
+  L->hstate = take(sizeof(double) * 2);
   L->bytes = align_up(off, 256);
   return TLGB_OK;
 }
@@ -329,6 +464,107 @@ int mu_run(const T* X, const Shape& sh, T* const* factors, int64_t R, const int*
   return TLGB_OK;
 }
 
+template <typename T>
+int hals_run(const T* X, const Shape& sh, T* const* factors, int64_t R, const int* free_modes,
+             int n_free, int n_iter_max, double tol, int crit, const double* sparsity,
+             int exact, double* errors, int* n_errors, void* ws, size_t ws_bytes,
+             cudaStream_t st) {
+  std::vector<MttkrpPlan> plans;
+  int nparts = 0;
+  MuLayout L;
+  int rc = mu_layout<T>(sh, R, n_iter_max, &plans, &nparts, &L);
+  if (rc) return rc;
+  if (!ws || ws_bytes < L.bytes) return set_error(TLGB_EWORKSPACE, "cp_nn_hals: workspace too small");
+  rc = als_prepare(TypeCode<T>::value);
+  if (rc) return rc;
+  char* base = static_cast<char*>(ws);
+  AlsCtrl* ctrl = reinterpret_cast<AlsCtrl*>(base + L.ctrl);
+  double* derr = reinterpret_cast<double*>(base + L.errors);
+  double* G = reinterpret_cast<double*>(base + L.G);
+  double* P = reinterpret_cast<double*>(base + L.V);
+  T* partial = reinterpret_cast<T*>(base + L.partial);
+  double* gpart = reinterpret_cast<double*>(base + L.gpart);
+  double* ipart = reinterpret_cast<double*>(base + L.ipart);
+  double* sumsq = reinterpret_cast<double*>(base + L.sumsq);
+  T* M = reinterpret_cast<T*>(base + L.M);
+  double* hpart = reinterpret_cast<double*>(base + L.hpart);
+  double* e0 = reinterpret_cast<double*>(base + L.hstate);
+  int* stop = reinterpret_cast<int*>(e0 + 1);
+  const int N = sh.ndim;
+  const int RR = (int)(R * R);
+  const int* done = &ctrl->done;
+  // tensorly/decomposition/_nn_cp.py:329-336: hals_nnls(..., n_iter_max=100), or exact
+  const int n_inner = exact ? 50000 : 100;
+  const double tol_inner = exact ? 1e-16 : 1e-8;
+  constexpr int kChunk = 10;   // inner iterations between host reads of the stop flag
+
+  TLGB_CUDA_TRY(cudaMemsetAsync(ctrl, 0, sizeof(AlsCtrl), st));
+  rc = als_launch_sumsq(TypeCode<T>::value, X, sh.numel, sumsq, kMuSumsqBlocks, ctrl, st);
+  if (rc) return rc;
+  for (int k = 0; k < N; ++k) {
+    rc = als_launch_gram<T>(factors[k], sh.dim[k], (int)R, gpart, nparts, G + (size_t)k * RR,
+                            done, st);
+    if (rc) return rc;
+  }
+  const T* cf[kMaxModes];
+  for (int k = 0; k < N; ++k) cf[k] = factors[k];
+  const int last = free_modes[n_free - 1];
+  AlsCtrl hc{};
+  for (int it = 0; it < n_iter_max; ++it) {
+    for (int q = 0; q < n_free; ++q) {
+      const int mode = free_modes[q];
+      const int64_t I = sh.dim[mode];
+      const int64_t IR = I * R;
+      k_mu_accum<<<(RR + 255) / 256, 256, 0, st>>>(G, N, mode, (int)R, P, done);
+      TLGB_LAUNCH_CHECK();
+      rc = mttkrp_launch_partials<T>(plans[mode], X, cf, nullptr, partial, done, st);
+      if (rc) return rc;
+      k_sum_splits_to<T><<<(unsigned)std::min<int64_t>(ceil_div(IR, 256), 4096), 256, 0, st>>>(
+          partial, plans[mode].splits, IR, M);
+      TLGB_LAUNCH_CHECK();
+      TLGB_CUDA_TRY(cudaMemsetAsync(e0, 0, 2 * sizeof(double), st));
+      const int nb = (int)ceil_div(I, (int64_t)kHalsWarps);
+      const double sp = sparsity ? sparsity[mode] : 0.0;
+      const int use_sp = (sparsity && !std::isnan(sp)) ? 1 : 0;
+      for (int t = 0; t < n_inner; ++t) {
+        k_hals_iter<T><<<nb, 32 * kHalsWarps, (size_t)kHalsWarps * R * sizeof(double), st>>>(
+            M, P, I, (int)R, factors[mode], sp, use_sp, hpart, stop, done);
+        TLGB_LAUNCH_CHECK();
+        k_hals_check<<<1, 256, 0, st>>>(hpart, nb, t, tol_inner, e0, stop, done);
+        TLGB_LAUNCH_CHECK();
+        if ((t + 1) % kChunk == 0 && t + 1 < n_inner) {
+          int hs = 0;
+          TLGB_CUDA_TRY(cudaMemcpyAsync(&hs, stop, sizeof(int), cudaMemcpyDeviceToHost, st));
+          TLGB_CUDA_TRY(cudaStreamSynchronize(st));
+          if (hs) break;
+        }
+      }
+      if (mode == last) {
+        k_inner_part<T><<<kInnerBlocks, 256, 0, st>>>(M, factors[mode], IR, ipart, done);
+        TLGB_LAUNCH_CHECK();
+      }
+      rc = als_launch_gram<T>(factors[mode], I, (int)R, gpart, nparts, G + (size_t)mode * RR,
+                              done, st);
+      if (rc) return rc;
+    }
+    if (tol > 0.0) {
+      rc = als_launch_fit<T>(G, N, (int)R, nullptr, ipart, kInnerBlocks, ctrl, derr, n_iter_max,
+                             tol, crit, st);
+      if (rc) return rc;
+      TLGB_CUDA_TRY(cudaMemcpyAsync(&hc, ctrl, sizeof(AlsCtrl), cudaMemcpyDeviceToHost, st));
+      TLGB_CUDA_TRY(cudaStreamSynchronize(st));
+      if (hc.done) break;
+    }
+  }
+  TLGB_CUDA_TRY(cudaMemcpyAsync(&hc, ctrl, sizeof(AlsCtrl), cudaMemcpyDeviceToHost, st));
+  TLGB_CUDA_TRY(cudaStreamSynchronize(st));
+  const int ne = (tol > 0.0) ? std::min(hc.iter, n_iter_max) : 0;
+  if (n_errors) *n_errors = ne;
+  if (errors && ne > 0)
+    TLGB_CUDA_TRY(cudaMemcpy(errors, derr, sizeof(double) * ne, cudaMemcpyDeviceToHost));
+  return TLGB_OK;
+}
+
 int check_nn_args(int dtype, const int64_t* shape, int ndim, int64_t rank) {
   TLGB_CHECK_ARG(dtype == TLGB_F32 || dtype == TLGB_F64, "cp_nn_mu: dtype must be f32 or f64");
   TLGB_CHECK_ARG(shape != nullptr, "cp_nn_mu: null shape");
@@ -387,6 +623,36 @@ extern "C" int tlgb_cp_nn_mu(int dtype, const void* X, int ndim, const int64_t* 
   return mu_run<float>((const float*)X, sh, (float* const*)factors, rank, free_modes, n_free,
                        n_iter_max, tol, cvg_criterion, errors, n_errors, workspace,
                        workspace_bytes, st);
+}
+
+extern "C" int tlgb_cp_nn_hals(int dtype, const void* X, int ndim, const int64_t* shape,
+                               void* const* factors, int64_t rank, const int* free_modes,
+                               int n_free, int n_iter_max, double tol, int cvg_criterion,
+                               const double* sparsity, int exact, double* errors, int* n_errors,
+                               void* workspace, size_t workspace_bytes, void* stream) {
+  clear_error();
+  int rc = check_nn_args(dtype, shape, ndim, rank);
+  if (rc) return rc;
+  TLGB_CHECK_ARG(X && factors && free_modes, "cp_nn_hals: null pointer");
+  TLGB_CHECK_ARG(n_free >= 1 && n_free <= ndim, "cp_nn_hals: bad number of free modes");
+  TLGB_CHECK_ARG(free_modes[n_free - 1] == ndim - 1, "cp_nn_hals: the last mode must be free");
+  for (int q = 0; q < n_free; ++q)
+    TLGB_CHECK_ARG(free_modes[q] >= 0 && free_modes[q] < ndim &&
+                       (q == 0 || free_modes[q] > free_modes[q - 1]),
+                   "cp_nn_hals: free modes must be ascending and in range");
+  for (int k = 0; k < ndim; ++k) TLGB_CHECK_ARG(factors[k] != nullptr, "cp_nn_hals: null factor");
+  TLGB_CHECK_ARG(n_iter_max >= 0 && tol >= 0.0, "cp_nn_hals: bad n_iter_max or tol");
+  TLGB_CHECK_ARG(cvg_criterion == 0 || cvg_criterion == 1, "cp_nn_hals: bad cvg_criterion");
+  TLGB_CHECK_ARG(rank <= kMaxAlsRank, "cp_nn_hals: rank above 160 is not supported");
+  Shape sh = make_shape(ndim, shape);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (dtype == TLGB_F64)
+    return hals_run<double>((const double*)X, sh, (double* const*)factors, rank, free_modes,
+                            n_free, n_iter_max, tol, cvg_criterion, sparsity, exact, errors,
+                            n_errors, workspace, workspace_bytes, st);
+  return hals_run<float>((const float*)X, sh, (float* const*)factors, rank, free_modes, n_free,
+                         n_iter_max, tol, cvg_criterion, sparsity, exact, errors, n_errors,
+                         workspace, workspace_bytes, st);
 }
 
 extern "C" int tlgb_sum(int dtype, const void* X, int64_t n, double* out, void* workspace,

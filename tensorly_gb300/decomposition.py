@@ -532,6 +532,115 @@ def non_negative_parafac(tensor, rank, n_iter_max=100, init="svd", svd="truncate
     return cp
 
 
+def non_negative_parafac_hals(tensor, rank, n_iter_max=100, init="svd", svd="truncated_svd",
+                              tol=10e-8, random_state=None, sparsity_coefficients=None,
+                              fixed_modes=None, nn_modes="all", exact=False,
+                              normalize_factors=False, verbose=False, return_errors=False,
+                              cvg_criterion="abs_rec_error"):
+    """Non-negative CP by HALS (tensorly/decomposition/_nn_cp.py:186-377),
+    same signature and returns.  The loop runs in ``tlgb_cp_nn_hals``: per
+    free mode the Hadamard of the other Grams, the MTTKRP and the
+    ``hals_nnls`` row updates (tensorly/solvers/nnls.py:5-150) with their own
+    stop test; with ``tol`` the error of every iteration and the outer test.
+    ``nn_modes`` other than 'all', ``normalize_factors`` and a fixed last mode
+    are not supported."""
+    if normalize_factors:
+        raise NotImplementedError("non_negative_parafac_hals with normalize_factors=True is not "
+                                  "supported by tensorly_gb300")
+    if nn_modes != "all":
+        raise NotImplementedError("non_negative_parafac_hals supports nn_modes='all' only")
+    if tol and n_iter_max > 1 and cvg_criterion not in ("abs_rec_error", "rec_error"):
+        raise TypeError("Unknown convergence criterion")   # _nn_cp.py:363-364
+    x, placement = to_device(tensor)
+    code = dtype_code(x)
+    x = x.contiguous()
+    if x.ndim < 2:
+        raise NotImplementedError("non_negative_parafac_hals needs at least two modes")
+    _, factors = initialize_cp(x, rank, init=init, svd=svd, non_negative=True,
+                               random_state=random_state, normalize_factors=False)
+    factors = [f.to(x.dtype).contiguous().clone() for f in factors]
+    n_modes = x.ndim
+    if sparsity_coefficients is None or isinstance(sparsity_coefficients, float):
+        sparsity_coefficients = [sparsity_coefficients] * n_modes
+    sparsity_coefficients = list(sparsity_coefficients)
+    fixed = [] if fixed_modes is None else list(fixed_modes)
+    for m in fixed:
+        sparsity_coefficients[m] = None
+    for m in range(n_modes):
+        if sparsity_coefficients[m] is not None:
+            warnings.warn("Sparsity coefficient is ignored in unconstrained modes.")
+    free = [m for m in range(n_modes) if m not in fixed]
+    if not free or free[-1] != n_modes - 1:
+        raise NotImplementedError("non_negative_parafac_hals with a fixed last mode is not "
+                                  "supported by tensorly_gb300")
+    lib = _lib.lib()
+    shape = (ctypes.c_int64 * n_modes)(*x.shape)
+    nbytes = ctypes.c_size_t(0)
+    _lib.check(lib.tlgb_cp_nn_mu_workspace_size(code, n_modes, shape, int(rank), int(n_iter_max),
+                                                ctypes.byref(nbytes)))
+    ws = workspace(nbytes.value, x.device)
+    fptrs = (ctypes.c_void_p * n_modes)(*[f.data_ptr() for f in factors])
+    free_arr = (ctypes.c_int * len(free))(*free)
+    sp = (ctypes.c_double * n_modes)(*[float("nan") if c is None else float(c)
+                                       for c in sparsity_coefficients])
+    errs = (ctypes.c_double * max(1, int(n_iter_max)))()
+    n_err = ctypes.c_int(0)
+    _lib.check(lib.tlgb_cp_nn_hals(code, x.data_ptr(), n_modes, shape, fptrs, int(rank),
+                                   free_arr, len(free), int(n_iter_max),
+                                   float(tol) if tol else 0.0,
+                                   0 if cvg_criterion == "abs_rec_error" else 1, sp,
+                                   1 if exact else 0, errs, ctypes.byref(n_err), ptr(ws),
+                                   ws.numel(), stream_of(x)))
+    weights = torch.ones(int(rank), dtype=x.dtype, device=x.device)
+    cp = CPTensor((placement.back(weights), [placement.back(f) for f in factors]))
+    if return_errors:
+        return cp, [float(errs[i]) for i in range(n_err.value)]
+    return cp
+
+
+class CP_NN_HALS:
+    """sklearn-style wrapper of ``non_negative_parafac_hals``
+    (tensorly/decomposition/_nn_cp.py:517-656): every keyword is passed
+    through; ``decomposition_`` and ``errors_`` hold the last fit."""
+
+    def __init__(self, rank, n_iter_max=100, init="svd", svd="truncated_svd", tol=10e-8,
+                 sparsity_coefficients=None, fixed_modes=None, nn_modes="all", exact=False,
+                 verbose=False, normalize_factors=False, cvg_criterion="abs_rec_error",
+                 random_state=None):
+        self.rank = rank
+        self.random_state = random_state
+        self.n_iter_max = n_iter_max
+        self.init = init
+        self.svd = svd
+        self.tol = tol
+        self.sparsity_coefficients = sparsity_coefficients
+        self.fixed_modes = fixed_modes
+        self.nn_modes = nn_modes
+        self.exact = exact
+        self.verbose = verbose
+        self.normalize_factors = normalize_factors
+        self.cvg_criterion = cvg_criterion
+
+    def fit_transform(self, tensor):
+        cp, errors = non_negative_parafac_hals(
+            tensor, rank=self.rank, n_iter_max=self.n_iter_max, init=self.init, svd=self.svd,
+            tol=self.tol, random_state=self.random_state,
+            sparsity_coefficients=self.sparsity_coefficients,
+            fixed_modes=self.fixed_modes, nn_modes=self.nn_modes, exact=self.exact,
+            verbose=self.verbose, normalize_factors=self.normalize_factors,
+            cvg_criterion=self.cvg_criterion, return_errors=True)
+        self.decomposition_ = cp
+        self.errors_ = errors
+        return self.decomposition_
+
+    def fit(self, tensor):
+        self.fit_transform(tensor)
+        return self
+
+    def __repr__(self):
+        return f"Rank-{self.rank} Non-Negative CP decomposition."
+
+
 class CP_NN:
     """sklearn-style wrapper of ``non_negative_parafac``
     (tensorly/decomposition/_nn_cp.py:382-514): every keyword is passed

@@ -2,8 +2,8 @@
 the GPU against the reference runs (tests/golden) and the NumPy oracle.
 
 Tolerances: f64 runs match the reference to 1e-9 relative (factors, error
-list, same number of iterations); the f32 run to 1e-3 on the factors and 1e-4
-on the errors."""
+list, same number of iterations); f32 runs to 1e-3 on the factors and 1e-4 on
+the errors (multiplicative updates) or 1e-2 and 1e-3 (HALS)."""
 
 import numpy as np
 import pytest
@@ -74,3 +74,56 @@ def test_non_negative_parafac_unsupported_options_raise(gb300):
         gb300.non_negative_parafac(x, 2, mask=torch.ones_like(x))
     with pytest.raises(TypeError):
         gb300.non_negative_parafac(x, 2, cvg_criterion="nope")
+
+
+HALS_CASES = ["nn_hals_random", "nn_hals_svd", "nn_hals_stop", "nn_hals_f32"]
+
+
+@pytest.mark.parametrize("case", HALS_CASES)
+def test_non_negative_parafac_hals_matches_reference(gb300, golden, case):
+    run = golden["runs"][case]
+    x = regenerate(run)
+    kw = dict(run["kwargs"])
+    rank = kw.pop("rank")
+    (w, f), errs = gb300.non_negative_parafac_hals(torch.as_tensor(x, device="cuda"), rank,
+                                                   return_errors=True, **kw)
+    f32 = x.dtype == np.float32
+    assert len(errs) == len(run["errors"])
+    # f32: rounding in the Gauss-Seidel inner sweeps compounds along a run that
+    # is still descending, so the f32 tolerance is 1e-3 on the error list
+    np.testing.assert_allclose(errs, run["errors"], rtol=1e-3 if f32 else 1e-9,
+                               atol=1e-6 if f32 else 1e-12)
+    for a, b in zip(f, run["factors"]):
+        a = host(a)
+        assert (a >= 0).all()
+        tol = 1e-2 if f32 else 1e-8
+        np.testing.assert_allclose(a, b, rtol=tol, atol=tol * np.abs(b).max())
+
+
+def test_hals_sparsity_and_fixed_mode_match_reference(gb300, golden):
+    run = golden["runs"]["nn_hals_sparse_fixed"]
+    x = regenerate(run)
+    kw = dict(run["kwargs"])
+    rank = kw.pop("rank")
+    with pytest.warns(UserWarning):
+        (w, f), errs = gb300.non_negative_parafac_hals(torch.as_tensor(x, device="cuda"), rank,
+                                                       return_errors=True, **kw)
+    np.testing.assert_allclose(errs, run["errors"], rtol=1e-9, atol=1e-12)
+    for a, b in zip(f, run["factors"]):
+        np.testing.assert_allclose(host(a), b, rtol=1e-8, atol=1e-8 * np.abs(b).max())
+
+
+def test_hals_estimator_and_unsupported_options(gb300, golden):
+    run = golden["runs"]["nn_hals_random"]
+    x = regenerate(run)
+    kw = dict(run["kwargs"])
+    rank = kw.pop("rank")
+    est = gb300.CP_NN_HALS(rank, **kw)
+    cp = est.fit_transform(x)
+    np.testing.assert_allclose(est.errors_, run["errors"], rtol=1e-9, atol=1e-12)
+    assert isinstance(cp.factors[0], np.ndarray)
+    xt = torch.as_tensor(x, device="cuda")
+    with pytest.raises(NotImplementedError):
+        gb300.non_negative_parafac_hals(xt, 2, nn_modes=[0])
+    with pytest.raises(NotImplementedError):
+        gb300.non_negative_parafac_hals(xt, 2, fixed_modes=[2])
