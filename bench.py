@@ -50,11 +50,12 @@ def parse():
     p.add_argument("--cpu-sweeps", type=int, default=40)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--workload", default="dense",
-                   choices=["dense", "batched", "learned", "tucker"],
+                   choices=["dense", "batched", "learned", "tucker", "nncp"],
                    help="dense: 512^3 rank-64 CP-ALS (the headline); batched: 4096 uneven "
                         "3-way tensors, 100 sweeps each; learned: time to fit 10000 32^3 "
                         "rank-8 tensors from the learned warm start vs init='svd'; tucker: "
-                        "128^4 Tucker-HOOI rank 16^4 (20 iterations) and CP rank 32")
+                        "128^4 Tucker-HOOI rank 16^4 (20 iterations) and CP rank 32; nncp: "
+                        "non-negative CP (multiplicative updates and HALS) at 512^3 rank 64")
     p.add_argument("--train-samples", type=int, default=200_000,
                    help="learned: tensors the network is trained on (before the timed steps)")
     p.add_argument("--count", type=int, default=4096, help="batched: number of tensors")
@@ -765,6 +766,99 @@ def run_tucker(args):
     print(json.dumps(line), flush=True)
 
 
+NNCP_METRIC = "non-negative CP iterations/s at 512^3 f32 rank 64 (multiplicative updates)"
+
+
+def _nncp_cpu_sample(x, init, n_iter):
+    """The NumPy restatement of non_negative_parafac (multiplicative updates)
+    for `n_iter` iterations from `init`: iterations/s."""
+    import oracle
+    t0 = time.perf_counter()
+    oracle.non_negative_parafac(x, init[0].shape[1], n_iter_max=n_iter, init=(None, init), tol=0)
+    dt = time.perf_counter() - t0
+    return n_iter / dt, dt
+
+
+def run_nncp(args):
+    import torch
+    import tensorly_gb300 as tg
+    from tensorly_gb300 import _lib, workloads
+    ws_n, rank, _ = dist_env()
+    if rank != 0:
+        return
+    n_iter = 50
+    x_np, _ = workloads.dense_cp_large(size=args.size, rank=args.rank)
+    x_np = np.abs(x_np)
+    rs = np.random.RandomState(0)
+    init_np = [rs.random_sample((args.size, args.rank)).astype(np.float32) for _ in range(3)]
+    workload = (f"|dense CP {args.size}^3 f32| (non-negative), rank {args.rank}, "
+                f"{n_iter} iterations from a fixed random non-negative init, tol=0")
+    if args.impl == "reference":
+        v, dt = _nncp_cpu_sample(x_np, init_np, 2)
+        line = {"metric": NNCP_METRIC, "value": v, "unit": "iterations/s", "n_gpus": args.gpus,
+                "steps": 1, "warmup": 0, "ms_per_step": 1000.0 * dt / 2, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "impl": "reference",
+                "config": {"workload": workload, "step": "2 iterations (bounded sample)"},
+                "cpu_baseline": {"value": v, "unit": "iterations/s", "cores": os.cpu_count(),
+                                 "kind": "port", "sample": "2 iterations of the NumPy restatement"},
+                "e2e": {"value": v, "unit": "iterations/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+    tg.build() if not os.path.exists(_lib.library_path()) else None
+    dev = torch.device("cuda", torch.cuda.current_device())
+    x = torch.from_numpy(x_np).to(dev)
+    init = tg.CPTensor((None, [torch.from_numpy(f).to(dev) for f in init_np]))
+    st = torch.cuda.current_stream()
+
+    def timed(fn, reps):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(reps):
+            out = fn()
+        e1.record(st)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps, out
+
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    ms, _ = timed(lambda: tg.non_negative_parafac(x, args.rank, n_iter_max=n_iter, init=init,
+                                                  tol=0), args.steps)
+    clk = clocks.stop()
+    ms_h, _ = timed(lambda: tg.non_negative_parafac_hals(x, args.rank, n_iter_max=10, init=init,
+                                                         tol=0), 1)
+    _, (cp, errs) = timed(lambda: tg.non_negative_parafac(x, args.rank, n_iter_max=n_iter,
+                                                          init=init, tol=1e-30,
+                                                          return_errors=True), 1)
+    h0 = time.perf_counter()
+    tg.non_negative_parafac(x_np, args.rank, n_iter_max=n_iter,
+                            init=(None, [f.copy() for f in init_np]), tol=0)
+    e2e_s = time.perf_counter() - h0
+    cpu = None
+    if not args.no_cpu_baseline:
+        v, dt = _nncp_cpu_sample(x_np, init_np, 2)
+        cpu = {"value": v, "unit": "iterations/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"2 iterations of the NumPy restatement ({dt:.1f} s)"}
+    line = {"metric": NNCP_METRIC, "value": n_iter / (ms / 1000.0), "unit": "iterations/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": {"workload": workload, "l2": "512 MiB input > L2"},
+            "final_rel_error_50": float(errs[-1]),
+            "hals_iterations_per_s": 10 / (ms_h / 1000.0),
+            "cpu_baseline": cpu,
+            "e2e": {"value": n_iter / e2e_s, "unit": "iterations/s",
+                    "h2d_bytes_per_step": int(x_np.nbytes + sum(f.nbytes for f in init_np)),
+                    "d2h_bytes_per_step": int(sum(f.nbytes for f in init_np))},
+            # per iteration and mode: accum, MTTKRP split kernel, update, Gram partial + reduce
+            "clocks": clk, "gpu_launches": 3 * 5 * n_iter * args.steps}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.workload == "batched":
@@ -773,6 +867,8 @@ def main():
         run_learned(args)
     elif args.workload == "tucker":
         run_tucker(args)
+    elif args.workload == "nncp":
+        run_nncp(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

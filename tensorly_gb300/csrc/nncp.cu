@@ -236,53 +236,51 @@ constexpr int kHalsWarps = 8;
 // for k = 0..R-1:
 //   num = M[i, k] - sum_s P[k, s] A[i, s] + P[k, k] A[i, k] (- sparsity)
 //   A[i, k] <- max(num / P[k, k], 0)            (rows k with P[k, k] == 0 kept)
-// and adds the reference's stop term ||V - newV||^2 (newV broadcast against
-// every row of V), which for this column is S2 - 2 newV S1 + R newV^2 with S1,
-// S2 the column's running sum and sum of squares.
+// in the factor type T, as the reference computes, and adds the reference's
+// stop term ||V - newV||^2 (newV broadcast against every row of V), which for
+// this column is sum_s (A[i, s] - newV)^2 before the update.  P (when it fits)
+// and the warp's rows of A and M live in shared memory.
 template <typename T>
 __global__ void __launch_bounds__(32 * kHalsWarps)
-k_hals_iter(const T* __restrict__ M, const double* __restrict__ P, int64_t I, int R, T* A,
-            double sparsity, int use_sparsity, double* part, const int* stop, const int* done) {
+k_hals_iter(const T* __restrict__ M, const T* __restrict__ Pg, int64_t I, int R, T* A,
+            double sparsity, int use_sparsity, int p_in_smem, double* part, const int* stop,
+            const int* done) {
   if (*done || *stop) return;
-  extern __shared__ double shs[];   // [kHalsWarps][R] rows of A (f64 copies)
+  extern __shared__ __align__(16) unsigned char hsm[];
+  T* Ps = reinterpret_cast<T*>(hsm);                      // R x R (if p_in_smem)
+  T* rows = Ps + (p_in_smem ? R * R : 0);                 // [kHalsWarps][2][R]: A row, M row
   __shared__ double red[kHalsWarps];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (p_in_smem)
+    for (int e = threadIdx.x; e < R * R; e += 32 * kHalsWarps) Ps[e] = Pg[e];
+  const T* P = p_in_smem ? Ps : Pg;
   const int64_t i = (int64_t)blockIdx.x * kHalsWarps + warp;
-  double* v = shs + warp * R;
+  T* v = rows + warp * 2 * R;
+  T* m = v + R;
   double err = 0.0;
+  if (i < I)
+    for (int s = lane; s < R; s += 32) { v[s] = A[i * R + s]; m[s] = M[i * R + s]; }
+  __syncthreads();
   if (i < I) {
-    double s1 = 0.0, s2 = 0.0;
-    for (int s = lane; s < R; s += 32) {
-      const double x = (double)A[i * R + s];
-      v[s] = x;
-      s1 += x;
-      s2 += x * x;
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      s1 += __shfl_xor_sync(0xffffffffu, s1, o);
-      s2 += __shfl_xor_sync(0xffffffffu, s2, o);
-    }
-    __syncwarp();
     for (int k = 0; k < R; ++k) {
-      const double pkk = P[(int64_t)k * R + k];
-      if (pkk == 0.0) continue;
-      double dot = 0.0;
-      for (int s = lane; s < R; s += 32) dot = fma(P[(int64_t)k * R + s], v[s], dot);
+      const T pkk = P[k * R + k];
+      if (pkk == (T)0) continue;
+      T dot = (T)0;
+      for (int s = lane; s < R; s += 32) dot = fma(P[k * R + s], v[s], dot);
       for (int o = 16; o > 0; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
-      const double vk = v[k];
-      T num = (T)((double)M[i * R + k] - dot + pkk * vk);
+      T num = m[k] - dot + pkk * v[k];
       if (use_sparsity) num = num - (T)sparsity;
-      T nv = num / (T)pkk;
+      T nv = num / pkk;
       nv = nv > (T)0 ? nv : (T)0;
-      const double n = (double)nv;
-      err += s2 - 2.0 * n * s1 + (double)R * n * n;
-      s1 += n - vk;
-      s2 += n * n - vk * vk;
+      T sq = (T)0;
+      for (int s = lane; s < R; s += 32) { const T d = v[s] - nv; sq = fma(d, d, sq); }
+      for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
+      err += (double)sq;
       __syncwarp();
-      if (lane == 0) v[k] = n;
+      if (lane == 0) v[k] = nv;
       __syncwarp();
     }
-    for (int s = lane; s < R; s += 32) A[i * R + s] = (T)v[s];
+    for (int s = lane; s < R; s += 32) A[i * R + s] = v[s];
   }
   if (lane == 0) red[warp] = err;
   __syncthreads();
@@ -291,6 +289,14 @@ k_hals_iter(const T* __restrict__ M, const double* __restrict__ P, int64_t I, in
     for (int w = 0; w < kHalsWarps; ++w) t += red[w];
     part[blockIdx.x] = t;
   }
+}
+
+// P in the factor type (the Hadamard of the other Grams), for the HALS kernel.
+template <typename T>
+__global__ void k_to_type(const double* __restrict__ V, int n, T* out, const int* done) {
+  if (*done) return;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x)
+    out[e] = (T)V[e];
 }
 
 // After inner iteration t: total = the sum of the block partials (fixed order);
@@ -336,7 +342,7 @@ constexpr int kInnerBlocks = 128;
 
 struct MuLayout {
   size_t ctrl, errors, G, V, partial, gpart, ipart, sumsq, bytes;
-  size_t M, hpart, hstate;   // HALS: summed MTTKRP, inner-iteration partials, e0 + stop
+  size_t M, hpart, hstate, Pt;   // HALS: summed MTTKRP, inner partials, e0 + stop, typed P
 };
 
 int64_t mu_rows_per_block(int64_t I, int R, int nparts);
@@ -374,6 +380,7 @@ int mu_layout(const Shape& sh, int64_t R, int n_iter_max, std::vector<MttkrpPlan
   L->hpart = take(sizeof(double) * (size_t)std::max<int64_t>(kInnerBlocks,
                                                              ceil_div(imax, kHalsWarps)));
   L->hstate = take(sizeof(double) * 2);
+  L->Pt = take(sizeof(T) * RR);
   L->bytes = align_up(off, 256);
   return TLGB_OK;
 }
@@ -490,13 +497,21 @@ int hals_run(const T* X, const Shape& sh, T* const* factors, int64_t R, const in
   double* hpart = reinterpret_cast<double*>(base + L.hpart);
   double* e0 = reinterpret_cast<double*>(base + L.hstate);
   int* stop = reinterpret_cast<int*>(e0 + 1);
+  T* Pt = reinterpret_cast<T*>(base + L.Pt);
+  const int p_in_smem = ((size_t)R * R * sizeof(T) <= 32 * 1024) ? 1 : 0;
+  const size_t hals_smem = (p_in_smem ? (size_t)R * R * sizeof(T) : 0) +
+                           (size_t)kHalsWarps * 2 * R * sizeof(T);
   const int N = sh.ndim;
   const int RR = (int)(R * R);
   const int* done = &ctrl->done;
   // tensorly/decomposition/_nn_cp.py:329-336: hals_nnls(..., n_iter_max=100), or exact
   const int n_inner = exact ? 50000 : 100;
   const double tol_inner = exact ? 1e-16 : 1e-8;
-  constexpr int kChunk = 10;   // inner iterations between host reads of the stop flag
+  // Inner iterations between host reads of the stop flag.  Launches after a
+  // stop return at once; the reference's stop term (the column against the
+  // broadcast new row) rarely falls below tol, so 100 iterations usually run
+  // and an early read would only idle the GPU; exact mode allows 50000.
+  const int kChunk = exact ? 1000 : n_inner;
 
   TLGB_CUDA_TRY(cudaMemsetAsync(ctrl, 0, sizeof(AlsCtrl), st));
   rc = als_launch_sumsq(TypeCode<T>::value, X, sh.numel, sumsq, kMuSumsqBlocks, ctrl, st);
@@ -517,6 +532,8 @@ int hals_run(const T* X, const Shape& sh, T* const* factors, int64_t R, const in
       const int64_t IR = I * R;
       k_mu_accum<<<(RR + 255) / 256, 256, 0, st>>>(G, N, mode, (int)R, P, done);
       TLGB_LAUNCH_CHECK();
+      k_to_type<T><<<(RR + 255) / 256, 256, 0, st>>>(P, RR, Pt, done);
+      TLGB_LAUNCH_CHECK();
       rc = mttkrp_launch_partials<T>(plans[mode], X, cf, nullptr, partial, done, st);
       if (rc) return rc;
       k_sum_splits_to<T><<<(unsigned)std::min<int64_t>(ceil_div(IR, 256), 4096), 256, 0, st>>>(
@@ -527,8 +544,8 @@ int hals_run(const T* X, const Shape& sh, T* const* factors, int64_t R, const in
       const double sp = sparsity ? sparsity[mode] : 0.0;
       const int use_sp = (sparsity && !std::isnan(sp)) ? 1 : 0;
       for (int t = 0; t < n_inner; ++t) {
-        k_hals_iter<T><<<nb, 32 * kHalsWarps, (size_t)kHalsWarps * R * sizeof(double), st>>>(
-            M, P, I, (int)R, factors[mode], sp, use_sp, hpart, stop, done);
+        k_hals_iter<T><<<nb, 32 * kHalsWarps, hals_smem, st>>>(
+            M, Pt, I, (int)R, factors[mode], sp, use_sp, p_in_smem, hpart, stop, done);
         TLGB_LAUNCH_CHECK();
         k_hals_check<<<1, 256, 0, st>>>(hpart, nb, t, tol_inner, e0, stop, done);
         TLGB_LAUNCH_CHECK();
