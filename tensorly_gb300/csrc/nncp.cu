@@ -209,10 +209,11 @@ __global__ void k_sum_final(const double* part, int n, double* out) {
 // tensorly/solvers/nnls.py:5-150): per free mode, M = MTTKRP is summed once,
 // then up to n_inner iterations of row-wise (Gauss-Seidel over k) updates of
 // V = A^T.  Every column of V (row of A) is an independent problem, so one
-// warp owns one row of A, keeps it in shared memory and runs the k loop; the
-// rows are coupled only by the inner stop test, whose sum over the block's
-// rows goes to a per-block partial, summed in a fixed order by k_hals_check
-// between iterations.
+// warp owns one row of A in registers and runs all iterations of a chunk in
+// one launch; the rows are coupled only by the inner stop test, whose per-row
+// terms k_hals_scan sums after the launch.  A test that stops before the end
+// of the chunk reruns the rows from their saved start for exactly the
+// iterations the reference runs.
 
 // M (I x R, in the factor type) = the sum of the MTTKRP's split partials.
 template <typename T>
@@ -230,92 +231,231 @@ __global__ void k_sum_splits_to(const T* __restrict__ partial, int splits, int64
   }
 }
 
-constexpr int kHalsWarps = 8;
+constexpr int kHalsWarps = 4;       // rows (one per warp) per block
+constexpr int kHalsChunk = 100;     // speculative inner iterations per launch
+constexpr int64_t kHalsPartCap = int64_t(8) << 20;   // doubles of per-row stop partials
 
-// One HALS iteration: warp w of the block updates row i = block * 8 + w of A
-// for k = 0..R-1:
-//   num = M[i, k] - sum_s P[k, s] A[i, s] + P[k, k] A[i, k] (- sparsity)
-//   A[i, k] <- max(num / P[k, k], 0)            (rows k with P[k, k] == 0 kept)
-// in the factor type T, as the reference computes, and adds the reference's
-// stop term ||V - newV||^2 (newV broadcast against every row of V), which for
-// this column is sum_s (A[i, s] - newV)^2 before the update.  P (when it fits)
-// and the warp's rows of A and M live in shared memory.
-template <typename T>
+// Inner iterations per speculative launch: kHalsChunk, fewer when the per-row
+// partials of that many iterations would pass kHalsPartCap doubles.
+int hals_chunk(int64_t rows) {
+  return (int)std::max<int64_t>(
+      1, std::min<int64_t>(kHalsChunk, kHalsPartCap / std::max<int64_t>(rows, 1)));
+}
+
+// Products and sums of the row update with one rounding each, so that a
+// rerun of the same rows repeats the speculative launch bit for bit.
+__device__ __forceinline__ float rn_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double rn_mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float rn_add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double rn_add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float rn_sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double rn_sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float rn_div(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double rn_div(double a, double b) { return __ddiv_rn(a, b); }
+
+// n HALS iterations of row i = block * kHalsWarps + warp of A (a column of the
+// reference's V = A^T), k = 0..R-1 in order (rows k with P[k, k] == 0 kept):
+//   num = (M[i, k] - sum_s P[k, s] A[i, s]) + P[k, k] A[i, k]   (- sparsity)
+//   A[i, k] <- max(num / P[k, k], 0)
+// computed in the factor type T, as the reference computes (without a
+// sparsity coefficient sp is 0, and num - 0 is num).  Lane l holds elements
+// s = l + 32 j (j < NJ) of the row, of M's row and of P's diagonal in
+// registers, with w = P A[i, :]^T: w is formed afresh at the start of each
+// iteration and, after step k, moved by P[:, k] (A_new[i, k] - A_old[i, k]),
+// so a step costs the owner lane's arithmetic, one broadcast and one FMA per
+// element instead of two warp reductions; steps run in unrolled groups of 8.  The reference's stop term
+// ||V - newV||^2 (newV broadcast against every row of V) is, for this column,
+// sum_s (A[i, s] - newV)^2 before the update; each lane sums its elements'
+// share and the warp's total for iteration t goes to part[t * rows + row].
+// The rows are independent: the launch runs all n iterations, and the stop
+// test over all rows is applied afterwards by k_hals_scan, which asks for a
+// rerun of the first t + 1 iterations from the rows saved in `save` when the
+// test stopped early.  Rows are read from src and written to dst (the same
+// buffer in place).  PS: P staged in shared memory (else read from global).
+template <typename T, int NJ, bool PS>
 __global__ void __launch_bounds__(32 * kHalsWarps)
-k_hals_iter(const T* __restrict__ M, const T* __restrict__ Pg, int64_t I, int R, T* A,
-            double sparsity, int use_sparsity, int p_in_smem, double* part, const int* stop,
+k_hals_rows(const T* __restrict__ M, const T* __restrict__ Pg, int64_t I, int R, const T* src,
+            T* dst, T* save, int n_iter, const int* n_dev, double sparsity, double* part,
             const int* done) {
-  if (*done || *stop) return;
-  extern __shared__ __align__(16) unsigned char hsm[];
-  T* Ps = reinterpret_cast<T*>(hsm);                      // R x R (if p_in_smem)
-  T* rows = Ps + (p_in_smem ? R * R : 0);                 // [kHalsWarps][2][R]: A row, M row
-  __shared__ double red[kHalsWarps];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (p_in_smem)
-    for (int e = threadIdx.x; e < R * R; e += 32 * kHalsWarps) Ps[e] = Pg[e];
-  const T* P = p_in_smem ? Ps : Pg;
-  const int64_t i = (int64_t)blockIdx.x * kHalsWarps + warp;
-  T* v = rows + warp * 2 * R;
-  T* m = v + R;
-  double err = 0.0;
-  if (i < I)
-    for (int s = lane; s < R; s += 32) { v[s] = A[i * R + s]; m[s] = M[i * R + s]; }
-  __syncthreads();
-  if (i < I) {
-    for (int k = 0; k < R; ++k) {
-      const T pkk = P[k * R + k];
-      if (pkk == (T)0) continue;
-      T dot = (T)0;
-      for (int s = lane; s < R; s += 32) dot = fma(P[k * R + s], v[s], dot);
-      for (int o = 16; o > 0; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
-      T num = m[k] - dot + pkk * v[k];
-      if (use_sparsity) num = num - (T)sparsity;
-      T nv = num / pkk;
-      nv = nv > (T)0 ? nv : (T)0;
-      T sq = (T)0;
-      for (int s = lane; s < R; s += 32) { const T d = v[s] - nv; sq = fma(d, d, sq); }
-      for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
-      err += (double)sq;
-      __syncwarp();
-      if (lane == 0) v[k] = nv;
-      __syncwarp();
-    }
-    for (int s = lane; s < R; s += 32) A[i * R + s] = v[s];
-  }
-  if (lane == 0) red[warp] = err;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int w = 0; w < kHalsWarps; ++w) t += red[w];
-    part[blockIdx.x] = t;
-  }
-}
-
-// P in the factor type (the Hadamard of the other Grams), for the HALS kernel.
-template <typename T>
-__global__ void k_to_type(const double* __restrict__ V, int n, T* out, const int* done) {
   if (*done) return;
-  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x)
-    out[e] = (T)V[e];
+  const int n = n_dev ? *n_dev : n_iter;
+  if (n <= 0) return;
+  extern __shared__ __align__(16) unsigned char hsm[];
+  T* Ps = reinterpret_cast<T*>(hsm);                       // R x R (PS)
+  T* vbuf = Ps + (PS ? R * R : 0);                         // [kHalsWarps][R]
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if constexpr (PS) {
+    for (int e = threadIdx.x; e < R * R; e += 32 * kHalsWarps) Ps[e] = Pg[e];
+    __syncthreads();
+  }
+  const T* P = PS ? Ps : Pg;
+  T* vw = vbuf + warp * R;
+  const int64_t row = (int64_t)blockIdx.x * kHalsWarps + warp;
+  const int64_t rows = (int64_t)gridDim.x * kHalsWarps;
+  const bool live = row < I;
+  const T sp = (T)sparsity;
+  T v[NJ], w[NJ], m[NJ], pd[NJ];
+  int sx[NJ];                                               // in-range element index for P reads
+  unsigned zero[NJ];                                        // steps with P[k, k] == 0 (uniform)
+#pragma unroll
+  for (int j = 0; j < NJ; ++j) {
+    const int s = 32 * j + lane;
+    sx[j] = s < R ? s : 0;
+    v[j] = (T)0;
+    m[j] = (T)0;
+    pd[j] = P[sx[j] * R + sx[j]];
+    zero[j] = __ballot_sync(0xffffffffu, s < R && pd[j] == (T)0);
+    if (live && s < R) {
+      v[j] = src[row * R + s];
+      m[j] = M[row * R + s];
+      if (save) save[row * R + s] = v[j];
+    }
+  }
+  for (int t = 0; t < n; ++t) {
+#pragma unroll
+    for (int j = 0; j < NJ; ++j)
+      if (32 * j + lane < R) vw[32 * j + lane] = v[j];
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < NJ; ++j) {
+      T a0 = (T)0, a1 = (T)0;
+      int q = 0;
+      for (; q + 1 < R; q += 2) {
+        a0 = fma(P[q * R + sx[j]], vw[q], a0);
+        a1 = fma(P[(q + 1) * R + sx[j]], vw[q + 1], a1);
+      }
+      if (q < R) a0 = fma(P[q * R + sx[j]], vw[q], a0);
+      w[j] = rn_add(a0, a1);
+    }
+    __syncwarp();
+    T sq = (T)0;
+#pragma unroll
+    for (int J = 0; J < NJ; ++J) {
+      const int kn = (J == NJ - 1) ? R - 32 * J : 32;      // steps of slot J
+#pragma unroll 1
+      for (int kb = 0; kb < kn; kb += 8) {
+        const unsigned zb = zero[J] >> kb;
+        const T* prow = P + (32 * J + kb) * R;             // row k of P
+#pragma unroll
+        for (int u = 0; u < 8; ++u, prow += R) {
+          const int kk = kb + u;
+          if (J == NJ - 1 && kk >= kn) break;
+          if ((zb >> u) & 1u) continue;
+          // lane kk's w[J], v[J], m[J], pd[J] are element k = 32 J + kk's
+          const T num = rn_sub(rn_add(rn_sub(m[J], w[J]), rn_mul(pd[J], v[J])), sp);
+          T nv = rn_div(num, pd[J]);
+          nv = nv > (T)0 ? nv : (T)0;
+          nv = __shfl_sync(0xffffffffu, nv, kk);
+          const T delta = rn_sub(nv, __shfl_sync(0xffffffffu, v[J], kk));
+#pragma unroll
+          for (int j = 0; j < NJ; ++j) {
+            if (j < NJ - 1 || 32 * j + lane < R) {
+              const T d = rn_sub(v[j], nv);
+              sq = fma(d, d, sq);
+            }
+            w[j] = fma(prow[sx[j]], delta, w[j]);
+          }
+          if (lane == kk) v[J] = nv;
+        }
+      }
+    }
+    if (part) {
+      double e = live ? (double)sq : 0.0;
+      for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+      if (lane == 0) part[(int64_t)t * rows + row] = e;
+    }
+  }
+  if (live) {
+#pragma unroll
+    for (int j = 0; j < NJ; ++j)
+      if (32 * j + lane < R) dst[row * R + 32 * j + lane] = v[j];
+  }
 }
 
-// After inner iteration t: total = the sum of the block partials (fixed order);
-// t == 0 records it as the reference error; stop when total < tol * that.
-__global__ void k_hals_check(const double* part, int nb, int t, double tol, double* e0, int* stop,
-                             const int* done) {
-  if (*done || *stop) return;
-  __shared__ double red[32];
-  double s = 0.0;
-  for (int b = threadIdx.x; b < nb; b += blockDim.x) s += part[b];
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+// P in the factor type, symmetric (the upper triangle mirrored, as the
+// reference's Gram products are), for the HALS kernel.
+template <typename T>
+__global__ void k_to_type(const double* __restrict__ V, int R, T* out, const int* done) {
+  if (*done) return;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < R * R; e += gridDim.x * blockDim.x) {
+    const int r = e / R, c = e - r * R;
+    out[e] = (T)(r <= c ? V[e] : V[c * R + r]);
+  }
+}
+
+// After a speculative launch of n iterations (global iterations t0..t0+n-1):
+// tot[t] = the sum of the row partials of iteration t (fixed order, lane 0's
+// butterfly); iteration 0's total is the reference e0, and the first t with
+// tot[t] < tol * e0 ends the inner loop (tensorly/solvers/nnls.py:169-172).
+// rerun = t + 1 iterations from the saved rows when that t is not the last
+// of the launch, else 0 (the speculative rows stand).
+__global__ void k_hals_scan(const double* __restrict__ part, int64_t rows, int t0, int n,
+                            double tol, double* e0, int* stop, int* rerun, const int* done) {
+  if (*done) return;
+  extern __shared__ double tot[];                          // n
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int t = warp; t < n; t += nw) {
+    double s = 0.0;
+    for (int64_t r = lane; r < rows; r += 32) s += part[(int64_t)t * rows + r];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) tot[t] = s;
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
-    double tot = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
-    if (t == 0) *e0 = tot;
-    if (tot < tol * *e0) *stop = 1;
+    int st = 0, rr = 0;
+    for (int t = 0; t < n; ++t) {
+      if (t0 + t == 0) *e0 = tot[t];
+      if (tot[t] < tol * *e0) {
+        st = 1;
+        rr = (t + 1 < n) ? t + 1 : 0;
+        break;
+      }
+    }
+    *stop = st;
+    *rerun = rr;
   }
+}
+
+constexpr size_t kHalsPSmemMax = 112 * 1024;   // P staged in shared memory up to this size
+
+template <typename T, int NJ, bool PS>
+int hals_launch_nj(int R, int nb, size_t smem, cudaStream_t st, const T* M, const T* P,
+                   int64_t I, const T* src, T* dst, T* save, int n, const int* n_dev, double sp,
+                   double* part, const int* done) {
+  if (smem > 48 * 1024)
+    TLGB_CUDA_TRY(cudaFuncSetAttribute(k_hals_rows<T, NJ, PS>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_hals_rows<T, NJ, PS><<<nb, 32 * kHalsWarps, smem, st>>>(M, P, I, R, src, dst, save, n, n_dev,
+                                                            sp, part, done);
+  TLGB_LAUNCH_CHECK();
+  return TLGB_OK;
+}
+
+// k_hals_rows with NJ = ceil(R / 32) register slots per lane (R <= 160), P in
+// shared memory when it fits kHalsPSmemMax (every f32 rank: 160^2 * 4 bytes
+// fit; f64 up to rank 119).
+template <typename T>
+int hals_launch_rows(int R, int nb, size_t smem, int ps, cudaStream_t st, const T* M,
+                     const T* P, int64_t I, const T* src, T* dst, T* save, int n,
+                     const int* n_dev, double sp, double* part, const int* done) {
+#define TLGB_HALS_NJ(NJ)                                                                      \
+  if constexpr (sizeof(T) == 4)                                                                \
+    return hals_launch_nj<T, NJ, true>(R, nb, smem, st, M, P, I, src, dst, save, n, n_dev, sp, \
+                                       part, done);                                            \
+  else                                                                                         \
+    return ps ? hals_launch_nj<T, NJ, true>(R, nb, smem, st, M, P, I, src, dst, save, n,       \
+                                            n_dev, sp, part, done)                             \
+              : hals_launch_nj<T, NJ, false>(R, nb, smem, st, M, P, I, src, dst, save, n,      \
+                                             n_dev, sp, part, done)
+  switch ((R + 31) / 32) {
+    case 1: TLGB_HALS_NJ(1);
+    case 2: TLGB_HALS_NJ(2);
+    case 3: TLGB_HALS_NJ(3);
+    case 4: TLGB_HALS_NJ(4);
+    case 5: TLGB_HALS_NJ(5);
+    default: return set_error(TLGB_EINVAL, "cp_nn_hals: rank above 160 is not supported");
+  }
+#undef TLGB_HALS_NJ
 }
 
 // <M, A> partial sums per block of rows (the error's inner product).
@@ -342,7 +482,8 @@ constexpr int kInnerBlocks = 128;
 
 struct MuLayout {
   size_t ctrl, errors, G, V, partial, gpart, ipart, sumsq, bytes;
-  size_t M, hpart, hstate, Pt;   // HALS: summed MTTKRP, inner partials, e0 + stop, typed P
+  size_t M, hpart, hstate, Pt, save;   // HALS: summed MTTKRP, stop partials, e0 + stop +
+                                       // rerun, typed P, rows at the start of a chunk
 };
 
 int64_t mu_rows_per_block(int64_t I, int R, int nparts);
@@ -377,10 +518,11 @@ int mu_layout(const Shape& sh, int64_t R, int n_iter_max, std::vector<MttkrpPlan
   L->ipart = take(sizeof(double) * (size_t)std::max<int64_t>(nb_max, kInnerBlocks));
   L->sumsq = take(sizeof(double) * kMuSumsqBlocks);
   L->M = take(sizeof(T) * (size_t)imax * R);
-  L->hpart = take(sizeof(double) * (size_t)std::max<int64_t>(kInnerBlocks,
-                                                             ceil_div(imax, kHalsWarps)));
+  const int64_t hrows = ceil_div(imax, (int64_t)kHalsWarps) * kHalsWarps;
+  L->hpart = take(sizeof(double) * (size_t)(hrows * hals_chunk(hrows)));
   L->hstate = take(sizeof(double) * 2);
   L->Pt = take(sizeof(T) * RR);
+  L->save = take(sizeof(T) * (size_t)imax * R);
   L->bytes = align_up(off, 256);
   return TLGB_OK;
 }
@@ -497,21 +639,21 @@ int hals_run(const T* X, const Shape& sh, T* const* factors, int64_t R, const in
   double* hpart = reinterpret_cast<double*>(base + L.hpart);
   double* e0 = reinterpret_cast<double*>(base + L.hstate);
   int* stop = reinterpret_cast<int*>(e0 + 1);
+  int* rerun = stop + 1;
   T* Pt = reinterpret_cast<T*>(base + L.Pt);
-  const int p_in_smem = ((size_t)R * R * sizeof(T) <= 32 * 1024) ? 1 : 0;
+  T* save = reinterpret_cast<T*>(base + L.save);
+  const int p_in_smem = ((size_t)R * R * sizeof(T) <= kHalsPSmemMax) ? 1 : 0;
   const size_t hals_smem = (p_in_smem ? (size_t)R * R * sizeof(T) : 0) +
-                           (size_t)kHalsWarps * 2 * R * sizeof(T);
+                           (size_t)kHalsWarps * R * sizeof(T);
+  int64_t imax = 0;
+  for (int k = 0; k < sh.ndim; ++k) imax = std::max(imax, sh.dim[k]);
+  const int chunk = hals_chunk(ceil_div(imax, (int64_t)kHalsWarps) * kHalsWarps);
   const int N = sh.ndim;
   const int RR = (int)(R * R);
   const int* done = &ctrl->done;
   // tensorly/decomposition/_nn_cp.py:329-336: hals_nnls(..., n_iter_max=100), or exact
   const int n_inner = exact ? 50000 : 100;
   const double tol_inner = exact ? 1e-16 : 1e-8;
-  // Inner iterations between host reads of the stop flag.  Launches after a
-  // stop return at once; the reference's stop term (the column against the
-  // broadcast new row) rarely falls below tol, so 100 iterations usually run
-  // and an early read would only idle the GPU; exact mode allows 50000.
-  const int kChunk = exact ? 1000 : n_inner;
 
   TLGB_CUDA_TRY(cudaMemsetAsync(ctrl, 0, sizeof(AlsCtrl), st));
   rc = als_launch_sumsq(TypeCode<T>::value, X, sh.numel, sumsq, kMuSumsqBlocks, ctrl, st);
@@ -532,7 +674,7 @@ int hals_run(const T* X, const Shape& sh, T* const* factors, int64_t R, const in
       const int64_t IR = I * R;
       k_mu_accum<<<(RR + 255) / 256, 256, 0, st>>>(G, N, mode, (int)R, P, done);
       TLGB_LAUNCH_CHECK();
-      k_to_type<T><<<(RR + 255) / 256, 256, 0, st>>>(P, RR, Pt, done);
+      k_to_type<T><<<(RR + 255) / 256, 256, 0, st>>>(P, (int)R, Pt, done);
       TLGB_LAUNCH_CHECK();
       rc = mttkrp_launch_partials<T>(plans[mode], X, cf, nullptr, partial, done, st);
       if (rc) return rc;
@@ -541,15 +683,22 @@ int hals_run(const T* X, const Shape& sh, T* const* factors, int64_t R, const in
       TLGB_LAUNCH_CHECK();
       TLGB_CUDA_TRY(cudaMemsetAsync(e0, 0, 2 * sizeof(double), st));
       const int nb = (int)ceil_div(I, (int64_t)kHalsWarps);
-      const double sp = sparsity ? sparsity[mode] : 0.0;
-      const int use_sp = (sparsity && !std::isnan(sp)) ? 1 : 0;
-      for (int t = 0; t < n_inner; ++t) {
-        k_hals_iter<T><<<nb, 32 * kHalsWarps, hals_smem, st>>>(
-            M, Pt, I, (int)R, factors[mode], sp, use_sp, p_in_smem, hpart, stop, done);
+      const int64_t hrows = (int64_t)nb * kHalsWarps;
+      // no sparsity coefficient (NaN): subtract 0, which leaves num unchanged
+      const double sp = (sparsity && !std::isnan(sparsity[mode])) ? sparsity[mode] : 0.0;
+      T* A = factors[mode];
+      for (int t0 = 0; t0 < n_inner; t0 += chunk) {
+        const int n = std::min(chunk, n_inner - t0);
+        rc = hals_launch_rows<T>((int)R, nb, hals_smem, p_in_smem, st, M, Pt, I, A, A, save, n,
+                                 nullptr, sp, hpart, done);
+        if (rc) return rc;
+        k_hals_scan<<<1, 1024, sizeof(double) * n, st>>>(hpart, hrows, t0, n, tol_inner, e0, stop,
+                                                         rerun, done);
         TLGB_LAUNCH_CHECK();
-        k_hals_check<<<1, 256, 0, st>>>(hpart, nb, t, tol_inner, e0, stop, done);
-        TLGB_LAUNCH_CHECK();
-        if ((t + 1) % kChunk == 0 && t + 1 < n_inner) {
+        rc = hals_launch_rows<T>((int)R, nb, hals_smem, p_in_smem, st, M, Pt, I, save, A, nullptr,
+                                 0, rerun, sp, nullptr, done);
+        if (rc) return rc;
+        if (t0 + n < n_inner) {
           int hs = 0;
           TLGB_CUDA_TRY(cudaMemcpyAsync(&hs, stop, sizeof(int), cudaMemcpyDeviceToHost, st));
           TLGB_CUDA_TRY(cudaStreamSynchronize(st));

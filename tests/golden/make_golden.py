@@ -198,6 +198,12 @@ def reference_runs():
          dict(init="svd", n_iter_max=300, tol=1e-9)),
         ("nn_hals_f32", dict(shape=(16, 12, 10), rank=4, seed=65, dtype=np.float32),
          dict(init="random", random_state=18, n_iter_max=15, tol=1e-12)),
+        # rank 1: the inner stop test ends each hals_nnls call after 2 iterations
+        ("nn_hals_rank1", dict(shape=(9, 8, 7), rank=1, seed=66),
+         dict(init="random", random_state=19, n_iter_max=6, tol=1e-12)),
+        # exact=True: 50000 inner iterations per call, no early stop at rank 2
+        ("nn_hals_exact", dict(shape=(8, 7, 6), rank=2, seed=67),
+         dict(init="svd", n_iter_max=2, tol=1e-12, exact=True)),
     ]
     for name, g, kw in hals_variants:
         x = small(g["seed"], g["shape"], g["rank"], g.get("dtype", np.float64))

@@ -76,7 +76,8 @@ def test_non_negative_parafac_unsupported_options_raise(gb300):
         gb300.non_negative_parafac(x, 2, cvg_criterion="nope")
 
 
-HALS_CASES = ["nn_hals_random", "nn_hals_svd", "nn_hals_stop", "nn_hals_f32"]
+HALS_CASES = ["nn_hals_random", "nn_hals_svd", "nn_hals_stop", "nn_hals_f32", "nn_hals_rank1",
+              "nn_hals_exact"]
 
 
 @pytest.mark.parametrize("case", HALS_CASES)
@@ -127,3 +128,21 @@ def test_hals_estimator_and_unsupported_options(gb300, golden):
         gb300.non_negative_parafac_hals(xt, 2, nn_modes=[0])
     with pytest.raises(NotImplementedError):
         gb300.non_negative_parafac_hals(xt, 2, fixed_modes=[2])
+
+
+@pytest.mark.parametrize("dtype,rank", [(np.float64, 130), (np.float64, 100),
+                                        (np.float32, 100), (np.float64, 33)])
+def test_hals_wide_ranks_match_oracle(gb300, dtype, rank):
+    """Ranks that fill 2 to 5 register slots per lane; f64 rank 130 reads the
+    Gram product from global memory (it does not fit shared memory)."""
+    rs = np.random.RandomState(rank)
+    x = rs.rand(14, 12, 10).astype(dtype)
+    kw = dict(init="random", random_state=3, n_iter_max=2, tol=1e-12)
+    (_, fo), eo = oracle.non_negative_parafac_hals(x, rank, return_errors=True, **kw)
+    (_, fg), eg = gb300.non_negative_parafac_hals(torch.as_tensor(x, device="cuda"), rank,
+                                                  return_errors=True, **kw)
+    f32 = dtype == np.float32
+    np.testing.assert_allclose(eg, eo, rtol=1e-4 if f32 else 1e-9)
+    for a, b in zip(fg, fo):
+        tol = 1e-2 if f32 else 1e-8
+        np.testing.assert_allclose(host(a), b, rtol=tol, atol=tol * np.abs(b).max())

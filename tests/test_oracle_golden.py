@@ -87,7 +87,8 @@ def test_oracle_non_negative_parafac_matches_reference(golden, case):
 
 
 @pytest.mark.parametrize("case", ["nn_hals_random", "nn_hals_svd", "nn_hals_sparse_fixed",
-                                  "nn_hals_stop", "nn_hals_f32"])
+                                  "nn_hals_stop", "nn_hals_f32", "nn_hals_rank1",
+                                  "nn_hals_exact"])
 def test_oracle_non_negative_parafac_hals_matches_reference(golden, case):
     run = golden["runs"][case]
     x = regenerate(run)
