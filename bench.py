@@ -50,7 +50,7 @@ def parse():
     p.add_argument("--cpu-sweeps", type=int, default=40)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--workload", default="dense",
-                   choices=["dense", "batched", "learned", "tucker", "nncp"],
+                   choices=["dense", "batched", "learned", "tucker", "nncp", "reconstruct"],
                    help="dense: 512^3 rank-64 CP-ALS (the headline); batched: 4096 uneven "
                         "3-way tensors, 100 sweeps each; learned: time to fit 10000 32^3 "
                         "rank-8 tensors from the learned warm start vs init='svd'; tucker: "
@@ -859,6 +859,114 @@ def run_nncp(args):
     print(json.dumps(line), flush=True)
 
 
+def recon_metric(n, r):
+    return f"CP reconstructions/s at {n}^3 f32 rank {r} (cp_to_tensor)"
+
+
+def _recon_cpu_sample(w, fs, reps):
+    """The NumPy restatement of cp_to_tensor (dot with the explicit Khatri-Rao
+    matrix, BLAS threads on the host cores) `reps` times: calls/s."""
+    import oracle
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        oracle.cp_to_tensor((w, fs))
+    dt = time.perf_counter() - t0
+    return reps / dt, dt
+
+
+def run_reconstruct(args):
+    """cp_to_tensor of a 512^3 rank-64 f32 model: one fused kernel a call,
+    writing the 512 MiB tensor (tensorly/cp_tensor.py:433-485)."""
+    import torch
+    import tensorly_gb300 as tg
+    from tensorly_gb300 import _lib
+    ws_n, rank, _ = dist_env()
+    if rank != 0:
+        return
+    n, r = args.size, args.rank
+    rs = np.random.RandomState(0)
+    fs_np = [rs.randn(n, r).astype(np.float32) for _ in range(3)]
+    w_np = (rs.rand(r) + 0.5).astype(np.float32)
+    workload = f"cp_to_tensor of a {n}^3 f32 rank-{r} CP model (weights, Gaussian factors)"
+    if args.impl == "reference":
+        v, dt = _recon_cpu_sample(w_np, fs_np, 2)
+        line = {"metric": recon_metric(n, r), "value": v, "unit": "reconstructions/s",
+                "n_gpus": args.gpus, "steps": 1, "warmup": 0, "ms_per_step": 1000.0 * dt / 2,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic", "impl": "reference",
+                "config": {"workload": workload, "step": "2 calls (bounded sample)"},
+                "cpu_baseline": {"value": v, "unit": "reconstructions/s",
+                                 "cores": os.cpu_count(), "kind": "port",
+                                 "sample": "2 calls of the NumPy restatement"},
+                "e2e": {"value": v, "unit": "reconstructions/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+    tg.build() if not os.path.exists(_lib.library_path()) else None
+    dev = torch.device("cuda", torch.cuda.current_device())
+    fs = [torch.from_numpy(f).to(dev) for f in fs_np]
+    w = torch.from_numpy(w_np).to(dev)
+    st = torch.cuda.current_stream()
+    for _ in range(max(args.warmup, 3)):
+        full = tg.cp_to_tensor((w, fs))
+    torch.cuda.synchronize()
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    for e0, e1 in evs:
+        e0.record(st)
+        full = tg.cp_to_tensor((w, fs))
+        e1.record(st)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = statistics.mean(e0.elapsed_time(e1) for e0, e1 in evs)
+    del full
+    # end to end: factors from pinned host memory, the full tensor back into it
+    fs_h = [torch.from_numpy(f).pin_memory() for f in fs_np]
+    w_h = torch.from_numpy(w_np).pin_memory()
+    out_h = torch.empty((n, n, n), dtype=torch.float32).pin_memory()
+    for _ in range(2):
+        out_h.copy_(tg.cp_to_tensor((w_h.to(dev, non_blocking=True),
+                                     [f.to(dev, non_blocking=True) for f in fs_h])),
+                    non_blocking=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        out_h.copy_(tg.cp_to_tensor((w_h.to(dev, non_blocking=True),
+                                     [f.to(dev, non_blocking=True) for f in fs_h])),
+                    non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    cpu = None
+    if not args.no_cpu_baseline:
+        v, dt = _recon_cpu_sample(w_np, fs_np, 2)
+        cpu = {"value": v, "unit": "reconstructions/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"2 calls of the NumPy restatement ({dt:.1f} s)"}
+    peak, peak_kind = measured_peaks()
+    out_bytes = n ** 3 * 4
+    alg_bytes = out_bytes + 3 * n * r * 4 + r * 4
+    achieved = alg_bytes / (ms / 1000.0) / 1e9
+    flops = 2.0 * n ** 3 * r
+    sm_mhz = clk.get("sm_mhz") or 2070.0
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12          # FFMA pipe, TFLOP/s at that clock
+    line = {"metric": recon_metric(n, r), "value": 1000.0 / ms, "unit": "reconstructions/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": {"workload": workload, "l2": "512 MiB output > L2"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "peak_kind": peak_kind, "alg_bytes_per_launch": alg_bytes},
+            "fp32_tflops": flops / (ms / 1000.0) / 1e12, "fp32_pipe_peak_tflops": fp32_peak,
+            "cpu_baseline": cpu,
+            "e2e": {"value": 1.0 / e2e_s, "unit": "reconstructions/s",
+                    "h2d_bytes_per_step": int(sum(f.nbytes for f in fs_np) + w_np.nbytes),
+                    "d2h_bytes_per_step": int(out_bytes)},
+            "clocks": clk, "gpu_launches": args.steps}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.workload == "batched":
@@ -869,6 +977,8 @@ def main():
         run_tucker(args)
     elif args.workload == "nncp":
         run_nncp(args)
+    elif args.workload == "reconstruct":
+        run_reconstruct(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -415,6 +415,34 @@ int tlgb_cp_norm(int dtype, int ndim, const int64_t* rows, int64_t rank,
                  const void* const* factors, const void* weights, double* out,
                  void* workspace, size_t workspace_bytes, void* stream);
 
+/*
+ * cp_to_tensor: the full C-order tensor (shape[0] x ... x shape[ndim-1]) of
+ * [[weights; factors]], factors[k] row-major shape[k] x rank, computed as the
+ * mode-0 unfolding (factors[0] * weights) . khatri_rao(factors[1:])^T without
+ * forming the Khatri-Rao matrix.  weights (rank) and mask (the full shape,
+ * multiplies the result) may be NULL.  ndim 1 gives sum_r w_r factors[0][:, r].
+ * Replaces tensorly/cp_tensor.py:433-485 (cp_to_tensor); cp_to_unfolded
+ * (:488-521) and cp_to_vec (:524-546) are this call on reordered factors and
+ * a reshape.  dtype: TLGB_F32 or TLGB_F64.  The workspace holds the factors
+ * transposed (sum_k shape[k] * rank elements).
+ */
+int tlgb_cp_to_tensor_workspace_size(int dtype, int ndim, const int64_t* shape, int64_t rank,
+                                     size_t* bytes);
+int tlgb_cp_to_tensor(int dtype, int ndim, const int64_t* shape, int64_t rank,
+                      const void* const* factors, const void* weights, const void* mask,
+                      void* out, void* workspace, size_t workspace_bytes, void* stream);
+
+/*
+ * unfold: out (shape[mode] x prod(other modes)) = the mode-`mode` unfolding of
+ * the C-order tensor X, columns in the C order of the other modes
+ * (tensorly/base.py:39-53, moveaxis(X, mode, 0).reshape(shape[mode], -1)).
+ * fold: its inverse, out = the tensor of `shape` (tensorly/base.py:56-79).
+ */
+int tlgb_unfold(int dtype, const void* X, int ndim, const int64_t* shape, int mode, void* out,
+                void* stream);
+int tlgb_fold(int dtype, const void* unfolded, int ndim, const int64_t* shape, int mode,
+              void* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -28,7 +28,8 @@ __all__ = [
     "cp_normalize", "validate_cp_rank", "initialize_cp", "error_calc",
     "parafac", "initialize_tucker", "partial_tucker", "tucker", "non_negative_parafac",
     "make_svd_non_negative", "hals_nnls", "non_negative_parafac_hals",
-    "tucker_to_tensor", "validate_tucker_rank", "parafac_sweeps",
+    "tucker_to_tensor", "validate_tucker_rank", "parafac_sweeps", "cp_to_unfolded",
+    "cp_to_vec", "tucker_to_unfolded", "tucker_to_vec",
 ]
 
 
@@ -297,16 +298,32 @@ def random_cp(shape, rank, random_state=None, dtype=np.float64):
     return np.ones(rank, dtype=dtype), factors
 
 
-def cp_to_tensor(cp_tensor):
-    """tensorly/cp_tensor.py:433-485 (no mask): mode-0 unfolding
-    ``dot(factors[0]*weights, KR(factors[1:]).T)`` folded back."""
+def cp_to_tensor(cp_tensor, mask=None):
+    """tensorly/cp_tensor.py:433-485: mode-0 unfolding
+    ``dot(factors[0]*weights, KR(factors[1:]).T)`` folded back; with a mask,
+    the sum over r of the masked Khatri-Rao product of all factors."""
     weights, factors = cp_tensor
     shape = tuple(f.shape[0] for f in factors)
     if len(shape) == 1:
         return np.sum(weights * factors[0], axis=1)
     w = 1 if weights is None else weights
-    full = np.dot(factors[0] * w, np.transpose(khatri_rao(factors, skip_matrix=0)))
+    if mask is None:
+        full = np.dot(factors[0] * w, np.transpose(khatri_rao(factors, skip_matrix=0)))
+    else:
+        full = np.sum(khatri_rao([factors[0] * w] + list(factors[1:]), mask=mask), axis=1)
     return fold(full, 0, shape)
+
+
+def cp_to_unfolded(cp_tensor, mode):
+    """tensorly/cp_tensor.py:488-521."""
+    weights, factors = cp_tensor
+    a = factors[mode] if weights is None else factors[mode] * weights
+    return np.dot(a, np.transpose(khatri_rao(factors, skip_matrix=mode)))
+
+
+def cp_to_vec(cp_tensor):
+    """tensorly/cp_tensor.py:524-546."""
+    return np.reshape(cp_to_tensor(cp_tensor), (-1,))
 
 
 def cp_norm(cp_tensor):
@@ -683,6 +700,18 @@ def tucker_to_tensor(tucker_tensor, skip_factor=None, transpose_factors=False, m
     core, factors = tucker_tensor
     return multi_mode_dot(core, factors, skip=skip_factor,
                           transpose=transpose_factors, modes=modes)
+
+
+def tucker_to_unfolded(tucker_tensor, mode=0, skip_factor=None, transpose_factors=False):
+    """tensorly/tucker_tensor.py:105-131."""
+    return unfold(tucker_to_tensor(tucker_tensor, skip_factor=skip_factor,
+                                   transpose_factors=transpose_factors), mode)
+
+
+def tucker_to_vec(tucker_tensor, skip_factor=None, transpose_factors=False):
+    """tensorly/tucker_tensor.py:134-162."""
+    return np.reshape(tucker_to_tensor(tucker_tensor, skip_factor=skip_factor,
+                                       transpose_factors=transpose_factors), (-1,))
 
 
 def initialize_tucker(tensor, rank, modes, random_state, init="svd", svd="truncated_svd"):

@@ -13,8 +13,10 @@ C ABI (``include/tensorly_gb300.h``); tensors are PyTorch CUDA tensors.
 """
 
 from ._lib import GB300Error, SingularMatrixError, build, lib
+from .base import fold, tensor_to_vec, unfold, vec_to_tensor
 from .cp_tensor import (CPTensor, TuckerTensor, cp_norm, cp_normalize, cp_to_tensor,
-                        tucker_to_tensor, validate_cp_rank, validate_tucker_rank)
+                        cp_to_unfolded, cp_to_vec, tucker_to_tensor, tucker_to_unfolded,
+                        tucker_to_vec, validate_cp_rank, validate_tucker_rank)
 from .decomposition import (CP, CP_NN, CP_NN_HALS, Tucker, initialize_cp, initialize_tucker,
                             non_negative_parafac, non_negative_parafac_hals, parafac,
                             parafac_batched, partial_tucker, tucker)

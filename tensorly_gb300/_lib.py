@@ -201,6 +201,17 @@ SIGNATURES = [
     ("tlgb_cp_norm", ctypes.c_int,
      [ctypes.c_int, ctypes.c_int, _c_i64p, ctypes.c_int64, _c_vpp, ctypes.c_void_p,
       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    ("tlgb_cp_to_tensor_workspace_size", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_int, _c_i64p, ctypes.c_int64, ctypes.POINTER(ctypes.c_size_t)]),
+    ("tlgb_cp_to_tensor", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_int, _c_i64p, ctypes.c_int64, _c_vpp, ctypes.c_void_p,
+      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    ("tlgb_unfold", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, _c_i64p, ctypes.c_int, ctypes.c_void_p,
+      ctypes.c_void_p]),
+    ("tlgb_fold", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, _c_i64p, ctypes.c_int, ctypes.c_void_p,
+      ctypes.c_void_p]),
 ]
 
 _lock = threading.Lock()

@@ -199,26 +199,58 @@ def cp_norm(cp_tensor):
 
 
 def cp_to_tensor(cp_tensor, mask=None):
-    """Full tensor of a CP model (tensorly/cp_tensor.py:433-485): mode-0
-    unfolding ``(A_0 * w) . KR(A_1..A_{N-1})^T`` refolded, with the
-    Khatri-Rao product and the product computed by the library's kernels."""
-    from .tenalg import khatri_rao, mode_dot
-    if mask is not None:
-        raise NotImplementedError("cp_to_tensor with a mask is not supported")
+    """Full tensor of a CP model (tensorly/cp_tensor.py:433-485): the mode-0
+    unfolding ``(A_0 * w) . KR(A_1..A_{N-1})^T`` by ``tlgb_cp_to_tensor``, which
+    forms the Khatri-Rao entries in shared memory instead of in HBM.  A mask
+    (broadcastable to the full shape) multiplies the result.  A 1-way model
+    gives ``sum_r w_r A_0[:, r]``."""
     weights, factors = _factors_cuda(cp_tensor)
+    factors = [f.contiguous() for f in factors]
+    f0 = factors[0]
+    rank = int(f0.shape[1])
     shape = tuple(int(f.shape[0]) for f in factors)
-    if len(shape) == 1:
-        a0w = khatri_rao([factors[0]], weights=weights) if weights is not None else factors[0]
-        return a0w.sum(dim=1)
-    a0w = factors[0] if weights is None else _scaled(factors[0], weights)
-    kr = khatri_rao(factors, skip_matrix=0)
-    full = mode_dot(a0w, kr, 1)          # (I_0, prod others) = A0w . KR^T
-    return full.reshape(shape)
+    for f in factors:
+        if f.ndim != 2 or int(f.shape[1]) != rank or f.dtype != f0.dtype or f.device != f0.device:
+            raise ValueError("cp_to_tensor: factors must be matrices with the same rank, "
+                             "dtype and device")
+    if weights is None and len(shape) == 1:
+        # the reference multiplies None by the factor here (cp_tensor.py:470-471)
+        raise TypeError("cp_to_tensor of a 1-way model needs weights")
+    w = None
+    if weights is not None:
+        w = torch.as_tensor(weights).to(device=f0.device, dtype=f0.dtype).reshape(-1).contiguous()
+        if w.numel() != rank:
+            raise ValueError(f"cp_to_tensor: {w.numel()} weights for rank {rank}")
+    m = None
+    if mask is not None and len(shape) > 1:
+        m = torch.as_tensor(mask).to(device=f0.device, dtype=f0.dtype).expand(shape).contiguous()
+    out = torch.empty(shape, dtype=f0.dtype, device=f0.device)
+    lib = _lib.lib()
+    dims = _lib.i64_array(shape)
+    nbytes = _lib.ctypes.c_size_t(0)
+    _lib.check(lib.tlgb_cp_to_tensor_workspace_size(dtype_code(f0), len(shape), dims, rank,
+                                                    _lib.ctypes.byref(nbytes)))
+    ws = workspace(nbytes.value, f0.device)
+    _lib.check(lib.tlgb_cp_to_tensor(dtype_code(f0), len(shape), dims, rank,
+                                     _lib.ptr_array([ptr(f) for f in factors]), ptr(w), ptr(m),
+                                     ptr(out), ptr(ws), ws.numel(), stream_of(f0)))
+    return out
 
 
-def _scaled(matrix, weights):
-    from .tenalg import _khatri_rao_raw
-    return _khatri_rao_raw([matrix], weights)
+def cp_to_unfolded(cp_tensor, mode):
+    """Mode-``mode`` unfolding of the full tensor (tensorly/cp_tensor.py:488-521):
+    ``(A_mode * w) . KR(others)^T``, i.e. ``cp_to_tensor`` of the factors with
+    ``A_mode`` moved first, read as a matrix."""
+    weights, factors = _factors_cuda(cp_tensor)
+    mode = int(mode)
+    order = [mode] + [k for k in range(len(factors)) if k != mode]
+    full = cp_to_tensor((weights, [factors[k] for k in order]))
+    return full.reshape(int(factors[mode].shape[0]), -1)
+
+
+def cp_to_vec(cp_tensor):
+    """C-order vectorisation of the full tensor (tensorly/cp_tensor.py:524-546)."""
+    return cp_to_tensor(cp_tensor).reshape(-1)
 
 
 def tucker_to_tensor(tucker_tensor, skip_factor=None, transpose_factors=False, modes=None):
@@ -226,3 +258,16 @@ def tucker_to_tensor(tucker_tensor, skip_factor=None, transpose_factors=False, m
     from .tenalg import multi_mode_dot
     core, factors = tucker_tensor
     return multi_mode_dot(core, factors, skip=skip_factor, transpose=transpose_factors, modes=modes)
+
+
+def tucker_to_unfolded(tucker_tensor, mode=0, skip_factor=None, transpose_factors=False):
+    """tensorly/tucker_tensor.py:106-131: unfold of ``tucker_to_tensor``."""
+    from .base import unfold
+    return unfold(tucker_to_tensor(tucker_tensor, skip_factor=skip_factor,
+                                   transpose_factors=transpose_factors), mode)
+
+
+def tucker_to_vec(tucker_tensor, skip_factor=None, transpose_factors=False):
+    """tensorly/tucker_tensor.py:134-162: vectorised ``tucker_to_tensor``."""
+    return tucker_to_tensor(tucker_tensor, skip_factor=skip_factor,
+                            transpose_factors=transpose_factors).reshape(-1)

@@ -30,5 +30,7 @@ def golden():
         kats = pickle.load(f)
     with open(os.path.join(here, "reference_runs.pkl"), "rb") as f:
         runs = pickle.load(f)
+    with open(os.path.join(here, "reconstruction_kats.pkl"), "rb") as f:
+        recon = pickle.load(f)
     return {"kats": kats["records"], "runs": {r["case"]: r for r in runs["runs"]},
-            "versions": runs["versions"]}
+            "recon": recon["records"], "versions": runs["versions"]}

@@ -14,6 +14,10 @@ Outputs (committed, small, platform independent):
   backend with ``np.random.seed(0)``; the recorders wrap the functions the
   test modules call and the ``assert_*`` helpers they use (which additionally
   records the known answers the tests compare against).
+* ``reconstruction_kats.pkl``: the same for cp_to_tensor / cp_to_unfolded /
+  cp_to_vec / tucker_to_tensor / tucker_to_unfolded / tucker_to_vec, recorded
+  from their tests in tensorly/tests/test_cp_tensor.py and
+  test_tucker_tensor.py (CP and Tucker arguments stored as plain tuples).
 * ``reference_runs.pkl``: reference ``parafac`` / ``non_negative_parafac`` /
   ``tucker`` / ``svd_interface``
   outputs on seeded inputs (the tensors are regenerated from their seeds by
@@ -84,6 +88,66 @@ def record_kats():
             if hasattr(mod, aname):
                 setattr(mod, aname, wrap_assert(aname, getattr(mod, aname)))
         for tname in sorted(n for n in dir(mod) if n.startswith("test_")):
+            np.random.seed(0)
+            records.append({"fn": "__test__", "name": f"{mname}.{tname}"})
+            getattr(mod, tname)()
+    return records
+
+
+def _plain(x):
+    """CPTensor / TuckerTensor arguments as plain (weights|core, [factors]) tuples,
+    so the fixture loads without TensorLy."""
+    if hasattr(x, "factors") and hasattr(x, "weights"):
+        return (_np(x.weights), [_np(f) for f in x.factors])
+    if hasattr(x, "factors") and hasattr(x, "core"):
+        return (_np(x.core), [_np(f) for f in x.factors])
+    if isinstance(x, tuple):
+        return tuple(_plain(v) for v in x)
+    if isinstance(x, list):
+        return [_plain(v) for v in x]
+    return _np(x)
+
+
+def record_reconstruction():
+    """Calls of cp_to_tensor / cp_to_unfolded / cp_to_vec / tucker_to_tensor /
+    tucker_to_unfolded / tucker_to_vec (and the assertions with their known
+    answers) made by the reference's tests of them
+    (tensorly/tests/test_cp_tensor.py, tensorly/tests/test_tucker_tensor.py)."""
+    import tensorly as tl
+    tl.set_backend("numpy")
+    records = []
+
+    def wrap(name, fn):
+        def recorder(*args, **kwargs):
+            rec = {"fn": name, "args": _plain(list(args)), "kwargs": _plain(dict(kwargs))}
+            out = fn(*args, **kwargs)
+            rec["result"] = _np(out)
+            records.append(rec)
+            return out
+        return recorder
+
+    def wrap_assert(name, fn):
+        def recorder(*args, **kwargs):
+            records.append({"fn": name, "args": _plain(list(args)), "kwargs": _np(dict(kwargs))})
+            return fn(*args, **kwargs)
+        return recorder
+
+    plan = {"tensorly.tests.test_cp_tensor":
+            (("cp_to_tensor", "cp_to_unfolded", "cp_to_vec"),
+             ("test_cp_to_tensor", "test_cp_to_tensor_with_weights", "test_cp_to_unfolded",
+              "test_cp_to_vec")),
+            "tensorly.tests.test_tucker_tensor":
+            (("tucker_to_tensor", "tucker_to_unfolded", "tucker_to_vec"),
+             ("test_tucker_to_tensor", "test_tucker_to_tensor_with_partial_modes",
+              "test_tucker_to_unfolded", "test_tucker_to_vec"))}
+    for mname, (fns, tests) in plan.items():
+        mod = importlib.import_module(mname)
+        for fname in fns:
+            setattr(mod, fname, wrap(fname, getattr(mod, fname)))
+        for aname in ("assert_array_equal", "assert_array_almost_equal"):
+            if hasattr(mod, aname):
+                setattr(mod, aname, wrap_assert(aname, getattr(mod, aname)))
+        for tname in tests:
             np.random.seed(0)
             records.append({"fn": "__test__", "name": f"{mname}.{tname}"})
             getattr(mod, tname)()
@@ -254,7 +318,11 @@ def main():
     runs = reference_runs()
     with open(os.path.join(HERE, "reference_runs.pkl"), "wb") as f:
         pickle.dump({"versions": _versions(), "runs": runs}, f, protocol=4)
-    print(f"{len(kats)} tenalg records, {len(runs)} reference runs")
+    recon = record_reconstruction()
+    with open(os.path.join(HERE, "reconstruction_kats.pkl"), "wb") as f:
+        pickle.dump({"versions": _versions(), "records": recon}, f, protocol=4)
+    print(f"{len(kats)} tenalg records, {len(runs)} reference runs, "
+          f"{len(recon)} reconstruction records")
 
 
 if __name__ == "__main__":

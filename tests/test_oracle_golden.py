@@ -37,6 +37,27 @@ def test_oracle_replays_reference_tenalg_calls(golden):
     assert n >= 30
 
 
+RFN = {"cp_to_tensor": oracle.cp_to_tensor, "cp_to_unfolded": oracle.cp_to_unfolded,
+       "cp_to_vec": oracle.cp_to_vec, "tucker_to_tensor": oracle.tucker_to_tensor,
+       "tucker_to_unfolded": oracle.tucker_to_unfolded, "tucker_to_vec": oracle.tucker_to_vec}
+
+
+def test_oracle_replays_reference_reconstruction_calls(golden):
+    """Every cp_to_* / tucker_to_* call of the reference's own tests
+    (tensorly/tests/test_cp_tensor.py, test_tucker_tensor.py) gives the
+    reference's output bit for bit."""
+    n = 0
+    for rec in golden["recon"]:
+        fn = RFN.get(rec["fn"])
+        if fn is None:
+            continue
+        out = fn(*rec["args"], **rec["kwargs"])
+        np.testing.assert_array_equal(np.asarray(out), np.asarray(rec["result"]))
+        n += 1
+    assert n >= 20
+    assert sum(1 for r in golden["recon"] if r["fn"] == "__test__") == 8
+
+
 def test_known_answers_hold_for_oracle(golden):
     """The reference tests' hard-coded answers (assert_array_equal operands
     that are constants) agree with the oracle's outputs recorded above."""
