@@ -433,6 +433,48 @@ int tlgb_cp_to_tensor(int dtype, int ndim, const int64_t* shape, int64_t rank,
                       void* out, void* workspace, size_t workspace_bytes, void* stream);
 
 /*
+ * cp_residual_norm: *out (one double, device) = ||X - [[weights; factors]]||_F
+ * by the cp_to_tensor kernels with X read in place of the store (the full
+ * tensor is never written).  Workspace: tlgb_cp_to_tensor_workspace_size.
+ * Replaces tl.norm(tensor - cp_to_tensor(cp), 2) in
+ * tensorly/decomposition/_cp.py:723-726 (randomised_parafac's error).
+ */
+int tlgb_cp_residual_norm(int dtype, const void* X, int ndim, const int64_t* shape, int64_t rank,
+                          const void* const* factors, const void* weights, double* out,
+                          void* workspace, size_t workspace_bytes, void* stream);
+
+/*
+ * sample_khatri_rao: out (n_samples x rank) = rows of khatri_rao(mats) at the
+ * given positions, out[s, r] = prod_k mats[k][indices[k * n_samples + s], r]
+ * in matrix order (indices: device int64, n_mats x n_samples, each in
+ * [0, rows[k]); out-of-range indices read row 0).
+ * Replaces the product of tensorly/decomposition/_cp.py:546-630
+ * (sample_khatri_rao); the indices are drawn by the caller.
+ */
+int tlgb_sample_khatri_rao(int dtype, int n_mats, const void* const* mats, const int64_t* rows,
+                           int64_t rank, int64_t n_samples, const int64_t* indices, void* out,
+                           void* stream);
+
+/*
+ * One iteration of randomised CP-ALS (tensorly/decomposition/_cp.py:633-762):
+ * for each mode in order, the factor becomes the least-squares solution
+ * from n_samples sampled rows, solve(KR_s^T KR_s, KR_s^T X_s)^T, with KR_s
+ * the sampled Khatri-Rao rows of the other factors and X_s the matching
+ * rows of the unfolding; then *rec_error (host) = ||X - [[factors]]||_F
+ * (weights one).  indices: device int64, ndim x (ndim-1) x n_samples: for
+ * each mode the rows of the other modes in ascending mode order (the
+ * reference's per-mode sample_khatri_rao draws).  Synchronises `stream`.
+ * Returns TLGB_EINVAL for an out-of-range index, TLGB_ESINGULAR for
+ * singular sampled normal equations.  rank <= 160.
+ */
+int tlgb_cp_randomised_workspace_size(int dtype, int ndim, const int64_t* shape, int64_t rank,
+                                      int64_t n_samples, size_t* bytes);
+int tlgb_cp_randomised_iteration(int dtype, const void* X, int ndim, const int64_t* shape,
+                                 int64_t rank, void* const* factors, int64_t n_samples,
+                                 const int64_t* indices, double* rec_error, void* workspace,
+                                 size_t workspace_bytes, void* stream);
+
+/*
  * unfold: out (shape[mode] x prod(other modes)) = the mode-`mode` unfolding of
  * the C-order tensor X, columns in the C order of the other modes
  * (tensorly/base.py:39-53, moveaxis(X, mode, 0).reshape(shape[mode], -1)).

@@ -29,7 +29,8 @@ __all__ = [
     "parafac", "initialize_tucker", "partial_tucker", "tucker", "non_negative_parafac",
     "make_svd_non_negative", "hals_nnls", "non_negative_parafac_hals",
     "tucker_to_tensor", "validate_tucker_rank", "parafac_sweeps", "cp_to_unfolded",
-    "cp_to_vec", "tucker_to_unfolded", "tucker_to_vec",
+    "cp_to_vec", "tucker_to_unfolded", "tucker_to_vec", "sample_khatri_rao",
+    "randomised_parafac",
 ]
 
 
@@ -569,6 +570,75 @@ def non_negative_parafac_hals(tensor, rank, n_iter_max=100, init="svd", svd="tru
             weights, factors = cp_normalize((weights, factors))
     cp = (weights, factors)
     return (cp, rec_errors) if return_errors else cp
+
+
+def sample_khatri_rao(matrices, n_samples, skip_matrix=None, indices_list=None,
+                      return_sampled_rows=False, random_state=None):
+    """tensorly/decomposition/_cp.py:546-630 (no warning text)."""
+    if skip_matrix is not None:
+        matrices = [matrices[i] for i in range(len(matrices)) if i != skip_matrix]
+    if indices_list is None:
+        rng = random_state if isinstance(random_state, np.random.RandomState) \
+            else check_random_state(random_state)
+        indices_list = [rng.randint(0, m.shape[0], size=n_samples, dtype=int) for m in matrices]
+    rank = matrices[0].shape[1]
+    sizes = [m.shape[0] for m in matrices]
+    if return_sampled_rows:
+        indices_kr = np.zeros((n_samples), dtype=int)
+        for size, indices in zip(sizes, indices_list):
+            indices_kr = indices_kr * size + indices
+    sampled_kr = np.ones((n_samples, rank), dtype=matrices[0].dtype)
+    for indices, matrix in zip(indices_list, matrices):
+        sampled_kr = sampled_kr * matrix[indices, :]
+    if return_sampled_rows:
+        return sampled_kr, indices_list, indices_kr
+    return sampled_kr, indices_list
+
+
+def randomised_parafac(tensor, rank, n_samples, n_iter_max=100, init="random",
+                       svd="truncated_svd", tol=10e-9, max_stagnation=20, return_errors=False,
+                       random_state=None):
+    """tensorly/decomposition/_cp.py:633-762 (no callback, not verbose):
+    per mode the least-squares update from sampled Khatri-Rao rows, the error
+    ||X - [[A]]|| / ||X|| after each iteration, the tol and stagnation stops."""
+    rank = validate_cp_rank(tensor.shape, rank=rank)
+    rng = check_random_state(random_state)
+    _, factors = initialize_cp(tensor, rank, init=init, svd=svd, random_state=random_state)
+    factors = list(factors)
+    rec_errors = []
+    n_dims = tensor.ndim
+    norm_tensor = norm(tensor)
+    min_error = 0
+    weights = np.ones(rank, dtype=tensor.dtype)
+    for iteration in range(n_iter_max):
+        for mode in range(n_dims):
+            kr_prod, indices_list = sample_khatri_rao(factors, n_samples, skip_matrix=mode,
+                                                      random_state=rng)
+            indices_list = [i.tolist() for i in indices_list]
+            indices_list.insert(mode, slice(None, None, None))
+            indices_list = tuple(indices_list)
+            if mode:
+                sampled_unfolding = tensor[indices_list]
+            else:
+                sampled_unfolding = np.transpose(tensor[indices_list])
+            pseudo_inverse = np.dot(np.transpose(kr_prod), kr_prod)
+            factor = np.dot(np.transpose(kr_prod), sampled_unfolding)
+            factor = np.transpose(np.linalg.solve(pseudo_inverse, factor))
+            factors[mode] = factor
+        if max_stagnation or tol:
+            rec_error = norm(tensor - cp_to_tensor((weights, factors))) / norm_tensor
+            if not min_error or rec_error < min_error:
+                min_error = rec_error
+                stagnation = -1
+            stagnation += 1
+            rec_errors.append(rec_error)
+            if iteration > 1:
+                if (tol and abs(rec_errors[-2] - rec_errors[-1]) < tol) or (
+                        stagnation and (stagnation > max_stagnation)):
+                    break
+    if return_errors:
+        return (weights, factors), rec_errors
+    return weights, factors
 
 
 def error_calc(tensor, norm_tensor, weights, factors, mttkrp):

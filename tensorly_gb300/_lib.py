@@ -206,6 +206,19 @@ SIGNATURES = [
     ("tlgb_cp_to_tensor", ctypes.c_int,
      [ctypes.c_int, ctypes.c_int, _c_i64p, ctypes.c_int64, _c_vpp, ctypes.c_void_p,
       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    ("tlgb_cp_residual_norm", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, _c_i64p, ctypes.c_int64, _c_vpp,
+      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    ("tlgb_cp_randomised_workspace_size", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_int, _c_i64p, ctypes.c_int64, ctypes.c_int64,
+      ctypes.POINTER(ctypes.c_size_t)]),
+    ("tlgb_cp_randomised_iteration", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, _c_i64p, ctypes.c_int64, _c_vpp,
+      ctypes.c_int64, ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_void_p,
+      ctypes.c_size_t, ctypes.c_void_p]),
+    ("tlgb_sample_khatri_rao", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_int, _c_vpp, _c_i64p, ctypes.c_int64, ctypes.c_int64,
+      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     ("tlgb_unfold", ctypes.c_int,
      [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, _c_i64p, ctypes.c_int, ctypes.c_void_p,
       ctypes.c_void_p]),

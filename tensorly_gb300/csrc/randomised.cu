@@ -1,0 +1,282 @@
+// Randomised CP-ALS (tensorly/decomposition/_cp.py:546-762): per mode, the
+// least-squares update from n_samples sampled rows of the Khatri-Rao product,
+//   KR_s[s, r] = prod_{k != mode} A_k[idx_k[s], r]       (sample_khatri_rao)
+//   X_s[s, i]  = X[idx_0[s], .., i (at mode), .., idx_{N-1}[s]]
+//   A_mode     = solve(KR_s^T KR_s, KR_s^T X_s)^T = (X_s^T KR_s) (KR_s^T KR_s)^-1
+// and after each iteration ||X - [[A]]|| by the fused reconstruction kernel
+// in its residual form (the full tensor is never written).  The sample
+// indices come from the caller: the reference draws them with NumPy's
+// RandomState on the host, mode by mode, and the host mirror does the same.
+// The normal equations go through the CP-ALS factorisation and solve
+// kernels with the sampled Gram in place of the Hadamard of Grams.
+#include "als_kernels.cuh"
+#include "reconstruct.cuh"
+
+namespace tlgb {
+namespace {
+
+struct SampleArgs {
+  const void* mats[kMaxModes];   // the factors sampled (the others than `mode`), in order
+  const int64_t* idx[kMaxModes]; // their n_samples row indices (device)
+  int64_t rows[kMaxModes];
+  int64_t stride[kMaxModes];     // X strides of those modes (unfolding gather)
+  int n;
+};
+
+// kr[s, r]: the reference starts from ones and multiplies one sampled matrix
+// at a time (1 * a = a exactly).  Out-of-range indices read row 0 and set
+// *bad (when given).
+template <typename T>
+__global__ void k_sample_kr(const SampleArgs a, int64_t ns, int R, T* __restrict__ kr, int* bad) {
+  const int64_t total = ns * R;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s = e / R;
+    const int r = (int)(e - s * R);
+    T v = (T)1;
+    for (int k = 0; k < a.n; ++k) {
+      int64_t i = a.idx[k][s];
+      if (i < 0 || i >= a.rows[k]) {
+        if (bad) *bad = 1;
+        i = 0;
+      }
+      v = v * static_cast<const T*>(a.mats[k])[i * R + r];
+    }
+    kr[e] = v;
+  }
+}
+
+// xs[s, i] = X at the sampled position of the other modes and i at `mode`.
+template <typename T>
+__global__ void k_sample_unfolding(const T* __restrict__ X, const SampleArgs a, int64_t ns,
+                                   int64_t I, int64_t stride_mode, T* __restrict__ xs, int* bad) {
+  const int64_t total = ns * I;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s = e / I;
+    const int64_t i = e - s * I;
+    int64_t off = i * stride_mode;
+    for (int k = 0; k < a.n; ++k) {
+      int64_t j = a.idx[k][s];
+      if (j < 0 || j >= a.rows[k]) {
+        *bad = 1;
+        j = 0;
+      }
+      off += j * a.stride[k];
+    }
+    xs[e] = X[off];
+  }
+}
+
+// G[r, q] = sum_s kr[s, r] kr[s, q], accumulated in the factor type (the
+// reference's dot(kr^T, kr)), stored as f64 for the factorisation.
+template <typename T>
+__global__ void k_sampled_gram(const T* __restrict__ kr, int64_t ns, int R, double* G) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= R * R) return;
+  const int r = e / R, q = e - r * R;
+  T acc = (T)0;
+  for (int64_t s = 0; s < ns; ++s) acc = fma(kr[s * R + r], kr[s * R + q], acc);
+  G[e] = (double)acc;
+}
+
+// M[i, r] = sum_s xs[s, i] kr[s, r] (the reference's dot(kr^T, X_s), transposed).
+template <typename T>
+__global__ void k_sampled_mttkrp(const T* __restrict__ xs, const T* __restrict__ kr, int64_t ns,
+                                 int64_t I, int R, T* __restrict__ M) {
+  const int64_t total = I * R;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / R;
+    const int r = (int)(e - i * R);
+    T acc = (T)0;
+    for (int64_t s = 0; s < ns; ++s) acc = fma(xs[s * I + i], kr[s * R + r], acc);
+    M[e] = acc;
+  }
+}
+
+struct RandLayout {
+  size_t ctrl, G, fac, perm, vmat, w32, gpart, kr, xs, M, resid, bad, rec, bytes;
+};
+
+RandLayout rand_layout(int dtype, int ndim, const int64_t* shape, int64_t R, int64_t ns) {
+  RandLayout L{};
+  const size_t esz = dtype == TLGB_F64 ? 8 : 4;
+  int64_t imax = 0;
+  for (int k = 0; k < ndim; ++k) imax = std::max(imax, shape[k]);
+  size_t off = 0;
+  auto take = [&](size_t b) { off = align_up(off, 256); const size_t o = off; off += b; return o; };
+  const size_t RR = (size_t)R * R;
+  L.ctrl = take(sizeof(AlsCtrl));
+  L.G = take(sizeof(double) * 2 * RR);
+  L.fac = take(sizeof(double) * (RR + R));
+  L.perm = take(sizeof(int) * R);
+  L.vmat = take(sizeof(double) * RR);
+  L.w32 = take(sizeof(float) * 3 * RR);
+  L.gpart = take(sizeof(double) * RR * (size_t)solve_blocks_for(imax));
+  L.kr = take(esz * (size_t)ns * R);
+  L.xs = take(esz * (size_t)ns * imax);
+  L.M = take(esz * (size_t)imax * R);
+  L.resid = take(sizeof(double));
+  L.bad = take(sizeof(int));
+  L.rec = take(cp_full_ws_bytes(dtype, ndim, shape, R));
+  L.bytes = align_up(off, 256);
+  return L;
+}
+
+int rand_check(int dtype, int ndim, const int64_t* shape, int64_t rank, int64_t ns) {
+  TLGB_CHECK_ARG(dtype == TLGB_F32 || dtype == TLGB_F64, "randomised_parafac: dtype f32 or f64");
+  TLGB_CHECK_ARG(ndim >= 2 && ndim <= kMaxModes, "randomised_parafac: ndim must be in [2, 8]");
+  TLGB_CHECK_ARG(shape != nullptr, "randomised_parafac: null shape");
+  TLGB_CHECK_ARG(rank >= 1 && rank <= kMaxAlsRank, "randomised_parafac: rank must be in [1, 160]");
+  TLGB_CHECK_ARG(ns >= 1, "randomised_parafac: n_samples must be >= 1");
+  for (int k = 0; k < ndim; ++k)
+    TLGB_CHECK_ARG(shape[k] >= 1 && shape[k] <= INT32_MAX, "randomised_parafac: bad mode size");
+  return TLGB_OK;
+}
+
+template <typename T>
+int rand_iteration(const T* X, int ndim, const int64_t* shape, int64_t R, T* const* factors,
+                   int64_t ns, const int64_t* indices, double* rec_error, void* ws,
+                   cudaStream_t st) {
+  const int dtype = TypeCode<T>::value;
+  const RandLayout L = rand_layout(dtype, ndim, shape, R, ns);
+  char* base = static_cast<char*>(ws);
+  AlsCtrl* ctrl = reinterpret_cast<AlsCtrl*>(base + L.ctrl);
+  double* G = reinterpret_cast<double*>(base + L.G);
+  double* fac = reinterpret_cast<double*>(base + L.fac);
+  int* perm = reinterpret_cast<int*>(base + L.perm);
+  double* vmat = reinterpret_cast<double*>(base + L.vmat);
+  float* w32 = reinterpret_cast<float*>(base + L.w32);
+  double* gpart = reinterpret_cast<double*>(base + L.gpart);
+  T* kr = reinterpret_cast<T*>(base + L.kr);
+  T* xs = reinterpret_cast<T*>(base + L.xs);
+  T* M = reinterpret_cast<T*>(base + L.M);
+  double* resid = reinterpret_cast<double*>(base + L.resid);
+  int* bad = reinterpret_cast<int*>(base + L.bad);
+  int64_t stride[kMaxModes];
+  stride[ndim - 1] = 1;
+  for (int k = ndim - 2; k >= 0; --k) stride[k] = stride[k + 1] * shape[k + 1];
+  TLGB_CUDA_TRY(cudaMemsetAsync(ctrl, 0, sizeof(AlsCtrl), st));
+  TLGB_CUDA_TRY(cudaMemsetAsync(bad, 0, sizeof(int), st));
+  const int RR = (int)(R * R);
+  for (int mode = 0; mode < ndim; ++mode) {
+    SampleArgs a{};
+    a.n = ndim - 1;
+    for (int k = 0, q = 0; k < ndim; ++k) {
+      if (k == mode) continue;
+      a.mats[q] = factors[k];
+      a.idx[q] = indices + ((int64_t)mode * (ndim - 1) + q) * ns;
+      a.rows[q] = shape[k];
+      a.stride[q] = stride[k];
+      ++q;
+    }
+    const int64_t I = shape[mode];
+    const unsigned bk = (unsigned)std::min<int64_t>(ceil_div(ns * R, (int64_t)256), 152 * 8);
+    k_sample_kr<T><<<bk, 256, 0, st>>>(a, ns, (int)R, kr, bad);
+    TLGB_LAUNCH_CHECK();
+    const unsigned bx = (unsigned)std::min<int64_t>(ceil_div(ns * I, (int64_t)256), 152 * 8);
+    k_sample_unfolding<T><<<bx, 256, 0, st>>>(X, a, ns, I, stride[mode], xs, bad);
+    TLGB_LAUNCH_CHECK();
+    // G slot 1 holds the sampled Gram: the factorisation of mode 0 of a
+    // 2-mode problem uses exactly that matrix
+    k_sampled_gram<T><<<(RR + 127) / 128, 128, 0, st>>>(kr, ns, (int)R, G + RR);
+    TLGB_LAUNCH_CHECK();
+    const unsigned bm = (unsigned)std::min<int64_t>(ceil_div(I * R, (int64_t)128), 152 * 16);
+    k_sampled_mttkrp<T><<<bm, 128, 0, st>>>(xs, kr, ns, I, (int)R, M);
+    TLGB_LAUNCH_CHECK();
+    int rc = als_launch_factorize<T>(G, 2, 0, (int)R, nullptr, 0.0, fac, perm, vmat, w32, ctrl,
+                                     st);
+    if (rc) return rc;
+    int nb = 0;
+    rc = als_launch_solve<T>(M, 1, I, (int)R, fac, perm, vmat, w32, factors[mode], nullptr, gpart,
+                             nullptr, ctrl, kIrMaxPasses, &nb, st);
+    if (rc) return rc;
+  }
+  const void* fp[kMaxModes];
+  for (int k = 0; k < ndim; ++k) fp[k] = factors[k];
+  int rc = cp_full_run(dtype, ndim, shape, R, fp, nullptr, nullptr, nullptr, X, resid,
+                       base + L.rec, cp_full_ws_bytes(dtype, ndim, shape, R), st);
+  if (rc) return rc;
+  struct { double resid; int bad; AlsCtrl ctrl; } h{};
+  TLGB_CUDA_TRY(cudaMemcpyAsync(&h.resid, resid, sizeof(double), cudaMemcpyDeviceToHost, st));
+  TLGB_CUDA_TRY(cudaMemcpyAsync(&h.bad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+  TLGB_CUDA_TRY(cudaMemcpyAsync(&h.ctrl, ctrl, sizeof(AlsCtrl), cudaMemcpyDeviceToHost, st));
+  TLGB_CUDA_TRY(cudaStreamSynchronize(st));
+  if (h.bad) return set_error(TLGB_EINVAL, "randomised_parafac: sample index out of range");
+  if (h.ctrl.status == TLGB_ESINGULAR)
+    return set_error(TLGB_ESINGULAR, "randomised_parafac: sampled normal equations singular");
+  if (rec_error) *rec_error = h.resid;
+  return TLGB_OK;
+}
+
+}  // namespace
+}  // namespace tlgb
+
+using namespace tlgb;
+
+extern "C" int tlgb_cp_randomised_workspace_size(int dtype, int ndim, const int64_t* shape,
+                                                 int64_t rank, int64_t n_samples,
+                                                 size_t* bytes) {
+  clear_error();
+  int rc = rand_check(dtype, ndim, shape, rank, n_samples);
+  if (rc) return rc;
+  TLGB_CHECK_ARG(bytes != nullptr, "randomised_parafac: null bytes");
+  *bytes = rand_layout(dtype, ndim, shape, rank, n_samples).bytes;
+  return TLGB_OK;
+}
+
+extern "C" int tlgb_cp_randomised_iteration(int dtype, const void* X, int ndim,
+                                            const int64_t* shape, int64_t rank,
+                                            void* const* factors, int64_t n_samples,
+                                            const int64_t* indices, double* rec_error,
+                                            void* workspace, size_t workspace_bytes,
+                                            void* stream) {
+  clear_error();
+  int rc = rand_check(dtype, ndim, shape, rank, n_samples);
+  if (rc) return rc;
+  TLGB_CHECK_ARG(X && factors && indices, "randomised_parafac: null pointer");
+  for (int k = 0; k < ndim; ++k)
+    TLGB_CHECK_ARG(factors[k] != nullptr, "randomised_parafac: null factor");
+  if (!workspace || workspace_bytes < rand_layout(dtype, ndim, shape, rank, n_samples).bytes)
+    return set_error(TLGB_EWORKSPACE, "randomised_parafac: workspace too small");
+  rc = als_prepare(dtype);
+  if (rc) return rc;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (dtype == TLGB_F64)
+    return rand_iteration<double>(static_cast<const double*>(X), ndim, shape, rank,
+                                  reinterpret_cast<double* const*>(factors), n_samples, indices,
+                                  rec_error, workspace, st);
+  return rand_iteration<float>(static_cast<const float*>(X), ndim, shape, rank,
+                               reinterpret_cast<float* const*>(factors), n_samples, indices,
+                               rec_error, workspace, st);
+}
+
+extern "C" int tlgb_sample_khatri_rao(int dtype, int n_mats, const void* const* mats,
+                                      const int64_t* rows, int64_t rank, int64_t n_samples,
+                                      const int64_t* indices, void* out, void* stream) {
+  clear_error();
+  TLGB_CHECK_ARG(dtype == TLGB_F32 || dtype == TLGB_F64, "sample_khatri_rao: dtype f32 or f64");
+  TLGB_CHECK_ARG(n_mats >= 1 && n_mats <= kMaxModes, "sample_khatri_rao: 1..8 matrices");
+  TLGB_CHECK_ARG(mats && rows && indices && out, "sample_khatri_rao: null pointer");
+  TLGB_CHECK_ARG(rank >= 1 && n_samples >= 0, "sample_khatri_rao: bad rank or n_samples");
+  if (n_samples == 0) return TLGB_OK;
+  SampleArgs a{};
+  a.n = n_mats;
+  for (int k = 0; k < n_mats; ++k) {
+    TLGB_CHECK_ARG(mats[k] != nullptr && rows[k] >= 1, "sample_khatri_rao: bad matrix");
+    a.mats[k] = mats[k];
+    a.idx[k] = indices + (int64_t)k * n_samples;
+    a.rows[k] = rows[k];
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const unsigned bk = (unsigned)std::min<int64_t>(ceil_div(n_samples * rank, (int64_t)256), 152 * 8);
+  if (dtype == TLGB_F64)
+    k_sample_kr<double><<<bk, 256, 0, st>>>(a, n_samples, (int)rank, static_cast<double*>(out),
+                                            nullptr);
+  else
+    k_sample_kr<float><<<bk, 256, 0, st>>>(a, n_samples, (int)rank, static_cast<float*>(out),
+                                           nullptr);
+  TLGB_LAUNCH_CHECK();
+  return TLGB_OK;
+}

@@ -679,6 +679,185 @@ class CP_NN:
         return f"Rank-{self.rank} Non-Negative CP decomposition."
 
 
+def sample_khatri_rao(matrices, n_samples, skip_matrix=None, indices_list=None,
+                      return_sampled_rows=False, random_state=None):
+    """Rows of the Khatri-Rao product at random positions
+    (tensorly/decomposition/_cp.py:546-630), same signature and returns.
+
+    The row indices are drawn on the host with NumPy's RandomState exactly as
+    the reference draws them (one ``randint`` per matrix, in order); the
+    product of the sampled rows is formed by ``tlgb_sample_khatri_rao``."""
+    if skip_matrix is not None:
+        matrices = [matrices[i] for i in range(len(matrices)) if i != skip_matrix]
+    if indices_list is None:
+        if random_state is None or not isinstance(random_state, np.random.RandomState):
+            rng = check_random_state(random_state)
+            warnings.warn(
+                "You are creating a new random number generator at each call.\n"
+                "If you are calling sample_khatri_rao inside a loop this will be slow:"
+                " best to create a rng outside and pass it as argument (random_state=rng).")
+        else:
+            rng = random_state
+        indices_list = [rng.randint(0, m.shape[0], size=n_samples, dtype=int) for m in matrices]
+    mats = [to_device(m)[0].contiguous() for m in matrices]
+    pl = to_device(matrices[0])[1]
+    m0 = mats[0]
+    rank = int(m0.shape[1])
+    sizes = [int(m.shape[0]) for m in mats]
+    idx = np.stack([np.asarray(i, dtype=np.int64).reshape(-1) for i in indices_list])
+    if idx.shape[1] != n_samples:
+        raise ValueError(f"{idx.shape[1]} indices for {n_samples} samples")
+    for size, i in zip(sizes, idx):
+        if i.size and (i.min() < 0 or i.max() >= size):
+            raise IndexError("sample_khatri_rao: index out of range")
+    out = torch.empty((n_samples, rank), dtype=m0.dtype, device=m0.device)
+    d_idx = torch.from_numpy(np.ascontiguousarray(idx)).to(m0.device)
+    _lib.check(_lib.lib().tlgb_sample_khatri_rao(
+        dtype_code(m0), len(mats), _lib.ptr_array([m.data_ptr() for m in mats]),
+        (ctypes.c_int64 * len(sizes))(*sizes), rank, int(n_samples), d_idx.data_ptr(),
+        out.data_ptr(), stream_of(m0)))
+    sampled_kr = pl.back(out)
+    if return_sampled_rows:
+        indices_kr = np.zeros((n_samples), dtype=int)
+        for size, indices in zip(sizes, indices_list):
+            indices_kr = indices_kr * size + indices
+        return sampled_kr, indices_list, indices_kr
+    return sampled_kr, indices_list
+
+
+def _norm_on_device(x):
+    """||X||_F by the residual kernel against a zero rank-1 model."""
+    zeros = [torch.zeros((s, 1), dtype=x.dtype, device=x.device) for s in x.shape]
+    return _residual_norm(x, zeros)
+
+
+def _residual_norm(x, factors, weights=None):
+    lib = _lib.lib()
+    shape = (ctypes.c_int64 * x.ndim)(*x.shape)
+    rank = int(factors[0].shape[1])
+    nbytes = ctypes.c_size_t(0)
+    _lib.check(lib.tlgb_cp_to_tensor_workspace_size(dtype_code(x), x.ndim, shape, rank,
+                                                    ctypes.byref(nbytes)))
+    ws = workspace(nbytes.value, x.device)
+    out = torch.empty(1, dtype=torch.float64, device=x.device)
+    _lib.check(lib.tlgb_cp_residual_norm(dtype_code(x), x.data_ptr(), x.ndim, shape, rank,
+                                         _lib.ptr_array([f.data_ptr() for f in factors]),
+                                         ptr(weights), out.data_ptr(), ptr(ws), ws.numel(),
+                                         stream_of(x)))
+    return float(out.item())
+
+
+def randomised_parafac(tensor, rank, n_samples, n_iter_max=100, init="random",
+                       svd="truncated_svd", tol=10e-9, max_stagnation=20, return_errors=False,
+                       random_state=None, verbose=0, callback=None):
+    """Randomised CP-ALS (tensorly/decomposition/_cp.py:633-762), same
+    signature, stop rules and returns.
+
+    Per iteration the host draws every mode's sample indices with NumPy's
+    RandomState in the reference's order; ``tlgb_cp_randomised_iteration``
+    then runs the mode updates (sampled Khatri-Rao rows, sampled unfolding,
+    the normal equations of the sampled least-squares problem) and the
+    reconstruction error ||X - [[A]]|| without forming the full tensor."""
+    x, placement = to_device(tensor)
+    code = dtype_code(x)
+    x = x.contiguous()
+    rank = validate_cp_rank(tuple(x.shape), rank=rank)
+    rng = check_random_state(random_state)
+    _, factors = initialize_cp(x, rank, init=init, svd=svd, random_state=random_state)
+    factors = [f.to(x.dtype).contiguous().clone() for f in factors]
+    n_dims = x.ndim
+    norm_tensor = _norm_on_device(x)
+    weights = torch.ones(rank, dtype=x.dtype, device=x.device)
+
+    def cp_now():
+        return CPTensor((placement.back(weights), [placement.back(f) for f in factors]))
+
+    rec_errors = []
+    min_error = 0
+    stagnation = 0
+    if callback is not None:
+        callback(cp_now())
+    lib = _lib.lib()
+    shape = (ctypes.c_int64 * n_dims)(*x.shape)
+    nbytes = ctypes.c_size_t(0)
+    _lib.check(lib.tlgb_cp_randomised_workspace_size(code, n_dims, shape, rank, int(n_samples),
+                                                     ctypes.byref(nbytes)))
+    ws = workspace(nbytes.value, x.device)
+    fptrs = (ctypes.c_void_p * n_dims)(*[f.data_ptr() for f in factors])
+    rec = ctypes.c_double(0.0)
+    for iteration in range(n_iter_max):
+        idx = np.empty((n_dims, n_dims - 1, n_samples), dtype=np.int64)
+        for mode in range(n_dims):
+            others = [k for k in range(n_dims) if k != mode]
+            for q, k in enumerate(others):          # sample_khatri_rao(..., random_state=rng)
+                idx[mode, q] = rng.randint(0, x.shape[k], size=n_samples, dtype=int)
+        d_idx = torch.from_numpy(idx).to(x.device)
+        _lib.check(lib.tlgb_cp_randomised_iteration(code, x.data_ptr(), n_dims, shape, rank,
+                                                    fptrs, int(n_samples), d_idx.data_ptr(),
+                                                    ctypes.byref(rec), ptr(ws), ws.numel(),
+                                                    stream_of(x)))
+        rec_error = rec.value / norm_tensor
+        if callback is not None:
+            if callback(cp_now(), rec_error) is True:
+                if verbose:
+                    print("Received True from callback function. Exiting.")
+                break
+        if max_stagnation or tol:                    # _cp.py:731-755
+            if not min_error or rec_error < min_error:
+                min_error = rec_error
+                stagnation = -1
+            stagnation += 1
+            rec_errors.append(rec_error)
+            if iteration > 1:
+                if verbose:
+                    print(f"reconstruction error={rec_errors[-1]}, "
+                          f"variation={rec_errors[-2] - rec_errors[-1]}.")
+                if (tol and abs(rec_errors[-2] - rec_errors[-1]) < tol) or \
+                        (stagnation and (stagnation > max_stagnation)):
+                    if verbose:
+                        print(f"converged in {iteration} iterations.")
+                    break
+    if return_errors:
+        return cp_now(), rec_errors
+    return cp_now()
+
+
+class RandomizedCP:
+    """sklearn-style wrapper of ``randomised_parafac``
+    (tensorly/decomposition/_cp.py:919-1004); ``decomposition_`` and
+    ``errors_`` hold the last fit."""
+
+    def __init__(self, rank, n_samples, n_iter_max=100, init="random", svd="truncated_svd",
+                 tol=10e-9, max_stagnation=20, return_errors=False, random_state=None,
+                 verbose=0, callback=None):
+        self.rank = rank
+        self.n_samples = n_samples
+        self.n_iter_max = n_iter_max
+        self.init = init
+        self.svd = svd
+        self.tol = tol
+        self.max_stagnation = max_stagnation
+        self.return_errors = return_errors
+        self.random_state = random_state
+        self.verbose = verbose
+        self.callback = callback
+
+    def fit_transform(self, tensor):
+        self.decomposition_, self.errors_ = randomised_parafac(
+            tensor, rank=self.rank, n_samples=self.n_samples, n_iter_max=self.n_iter_max,
+            init=self.init, svd=self.svd, tol=self.tol, return_errors=True,
+            max_stagnation=self.max_stagnation, random_state=self.random_state,
+            verbose=self.verbose, callback=self.callback)
+        return self.decomposition_
+
+    def fit(self, tensor):
+        self.fit_transform(tensor)
+        return self
+
+    def __repr__(self):
+        return f"Rank-{self.rank} Randomized CP decomposition."
+
+
 class BatchedProblem:
     """Many small 3-way f32 tensors packed for ``tlgb_cp_als_batched``.
 

@@ -279,6 +279,37 @@ def reference_runs():
                      "factors": [np.array(f) for f in cp.factors],
                      "errors": [float(e) for e in errs]})
 
+    # randomised CP-ALS (tensorly/decomposition/_cp.py:546-762)
+    from tensorly.decomposition import randomised_parafac
+    from tensorly.decomposition._cp import sample_khatri_rao
+    rand_variants = [
+        ("rand_random", dict(shape=(10, 10, 10), rank=4, seed=71),
+         dict(n_samples=100, n_iter_max=30, tol=0, init="random", random_state=5)),
+        ("rand_svd_tol", dict(shape=(12, 11, 10), rank=3, seed=72),
+         dict(n_samples=50, n_iter_max=40, tol=1e-6, init="svd", random_state=6)),
+        ("rand_4way", dict(shape=(6, 5, 7, 4), rank=3, seed=73),
+         dict(n_samples=40, n_iter_max=15, tol=0, init="random", random_state=7)),
+        ("rand_f32", dict(shape=(14, 12, 10), rank=4, seed=74, dtype=np.float32),
+         dict(n_samples=80, n_iter_max=20, tol=0, init="random", random_state=8)),
+    ]
+    for name, g, kw in rand_variants:
+        x = small(g["seed"], g["shape"], g["rank"], g.get("dtype", np.float64))
+        cp, errs = randomised_parafac(x, g["rank"], return_errors=True, **copy.deepcopy(kw))
+        runs.append({"case": name, "gen": {"fn": "small", **g}, "checksum": cs(x),
+                     "kwargs": {"rank": g["rank"], **kw},
+                     "weights": np.array(cp.weights),
+                     "factors": [np.array(f) for f in cp.factors],
+                     "errors": [float(e) for e in errs]})
+    rs = np.random.RandomState(9)
+    fs = [rs.random_sample((s, 3)) for s in (8, 9, 10)]
+    skr, ind, ind_kr = sample_khatri_rao(fs, 6, skip_matrix=1, return_sampled_rows=True,
+                                         random_state=np.random.RandomState(11))
+    runs.append({"case": "sample_kr", "gen": {"fn": "factors", "seed": 9},
+                 "checksum": cs(np.concatenate([f.ravel() for f in fs])),
+                 "kwargs": {"n_samples": 6, "skip_matrix": 1, "random_state": 11},
+                 "factors_in": fs, "sampled_kr": np.array(skr),
+                 "indices_list": [np.array(i) for i in ind], "indices_kr": np.array(ind_kr)})
+
     # Tucker (HOOI) small cases
     tcases = [
         ("tucker_svd", dict(shape=(12, 10, 8), seed=31), dict(rank=[3, 4, 2], init="svd",

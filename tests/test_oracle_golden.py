@@ -126,6 +126,32 @@ def test_oracle_non_negative_parafac_hals_matches_reference(golden, case):
         np.testing.assert_allclose(a, b, rtol=tol, atol=tol * np.abs(b).max())
 
 
+@pytest.mark.parametrize("case", ["rand_random", "rand_svd_tol", "rand_4way", "rand_f32"])
+def test_oracle_randomised_parafac_matches_reference(golden, case):
+    run = golden["runs"][case]
+    x = regenerate(run)
+    kw = dict(run["kwargs"])
+    rank = kw.pop("rank")
+    (w, f), errs = oracle.randomised_parafac(x, rank, return_errors=True, **kw)
+    tol = 1e-5 if x.dtype == np.float32 else 1e-12
+    assert len(errs) == len(run["errors"])
+    np.testing.assert_allclose(errs, run["errors"], rtol=tol, atol=tol * 1e-2)
+    for a, b in zip(f, run["factors"]):
+        np.testing.assert_allclose(a, b, rtol=tol, atol=tol * np.abs(b).max())
+
+
+def test_oracle_sample_khatri_rao_matches_reference(golden):
+    run = golden["runs"]["sample_kr"]
+    kw = run["kwargs"]
+    kr, ind, ind_kr = oracle.sample_khatri_rao(
+        run["factors_in"], kw["n_samples"], skip_matrix=kw["skip_matrix"],
+        return_sampled_rows=True, random_state=np.random.RandomState(kw["random_state"]))
+    np.testing.assert_array_equal(kr, run["sampled_kr"])
+    np.testing.assert_array_equal(ind_kr, run["indices_kr"])
+    for a, b in zip(ind, run["indices_list"]):
+        np.testing.assert_array_equal(a, b)
+
+
 @pytest.mark.parametrize("case", ["tucker_svd", "tucker_random", "tucker_4way"])
 def test_oracle_tucker_matches_reference(golden, case):
     run = golden["runs"][case]
