@@ -50,7 +50,8 @@ def parse():
     p.add_argument("--cpu-sweeps", type=int, default=40)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--workload", default="dense",
-                   choices=["dense", "batched", "learned", "tucker", "nncp", "reconstruct"],
+                   choices=["dense", "batched", "learned", "tucker", "nncp", "reconstruct",
+                            "randomised"],
                    help="dense: 512^3 rank-64 CP-ALS (the headline); batched: 4096 uneven "
                         "3-way tensors, 100 sweeps each; learned: time to fit 10000 32^3 "
                         "rank-8 tensors from the learned warm start vs init='svd'; tucker: "
@@ -967,6 +968,89 @@ def run_reconstruct(args):
     print(json.dumps(line), flush=True)
 
 
+def rand_metric(n, r, ns):
+    return f"randomised CP iterations/s at {n}^3 f32 rank {r} ({ns} samples a mode)"
+
+
+def run_randomised(args):
+    """randomised_parafac on the 512^3 rank-64 dense CP tensor: per iteration
+    three sampled mode updates and the reconstruction error
+    (tensorly/decomposition/_cp.py:633-762)."""
+    import torch
+    import tensorly_gb300 as tg
+    from tensorly_gb300 import _lib, workloads
+    ws_n, rank, _ = dist_env()
+    if rank != 0:
+        return
+    n, r, ns, n_iter = args.size, args.rank, 4096, 20
+    x_np, _ = workloads.dense_cp_large(size=n, rank=r)
+    workload = (f"randomised_parafac of the dense CP {n}^3 f32 tensor, rank {r}, {ns} samples a "
+                f"mode, {n_iter} iterations, init='random' (seed 0), tol=0, max_stagnation=20")
+
+    def cpu_sample(iters):
+        import oracle
+        t0 = time.perf_counter()
+        oracle.randomised_parafac(x_np, r, ns, n_iter_max=iters, tol=0, random_state=0)
+        dt = time.perf_counter() - t0
+        return iters / dt, dt
+
+    if args.impl == "reference":
+        v, dt = cpu_sample(2)
+        line = {"metric": rand_metric(n, r, ns), "value": v, "unit": "iterations/s",
+                "n_gpus": args.gpus, "steps": 1, "warmup": 0, "ms_per_step": 1000.0 * dt / 2,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic", "impl": "reference",
+                "config": {"workload": workload, "step": "2 iterations (bounded sample)"},
+                "cpu_baseline": {"value": v, "unit": "iterations/s", "cores": os.cpu_count(),
+                                 "kind": "port", "sample": "2 iterations of the NumPy restatement"},
+                "e2e": {"value": v, "unit": "iterations/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+    tg.build() if not os.path.exists(_lib.library_path()) else None
+    dev = torch.device("cuda", torch.cuda.current_device())
+    x = torch.from_numpy(x_np).to(dev)
+    st = torch.cuda.current_stream()
+    run = lambda: tg.randomised_parafac(x, r, ns, n_iter_max=n_iter, tol=0, random_state=0,
+                                        return_errors=True)
+    for _ in range(max(args.warmup, 3)):
+        run()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(args.steps):
+        _, errs = run()
+    e1.record(st)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    h0 = time.perf_counter()
+    for _ in range(args.steps):
+        tg.randomised_parafac(x_np, r, ns, n_iter_max=n_iter, tol=0, random_state=0)
+    e2e_s = (time.perf_counter() - h0) / args.steps
+    cpu = None
+    if not args.no_cpu_baseline:
+        v, dt = cpu_sample(2)
+        cpu = {"value": v, "unit": "iterations/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"2 iterations of the NumPy restatement ({dt:.1f} s)"}
+    line = {"metric": rand_metric(n, r, ns), "value": n_iter / (ms / 1000.0),
+            "unit": "iterations/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": workload, "l2": "512 MiB input > L2"},
+            "final_rel_error": float(errs[-1]), "cpu_baseline": cpu,
+            "e2e": {"value": n_iter / e2e_s, "unit": "iterations/s",
+                    "h2d_bytes_per_step": int(x_np.nbytes),
+                    "d2h_bytes_per_step": int(3 * n * r * 4)},
+            # per iteration: 3 x (gather KR, gather unfolding, Gram, products, factorise, solve)
+            # + transpose + residual + final reduction
+            "clocks": clk, "gpu_launches": args.steps * n_iter * (3 * 6 + 3)}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.workload == "batched":
@@ -979,6 +1063,8 @@ def main():
         run_nncp(args)
     elif args.workload == "reconstruct":
         run_reconstruct(args)
+    elif args.workload == "randomised":
+        run_randomised(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -68,35 +68,83 @@ __global__ void k_sample_unfolding(const T* __restrict__ X, const SampleArgs a, 
   }
 }
 
-// G[r, q] = sum_s kr[s, r] kr[s, q], accumulated in the factor type (the
-// reference's dot(kr^T, kr)), stored as f64 for the factorisation.
-template <typename T>
-__global__ void k_sampled_gram(const T* __restrict__ kr, int64_t ns, int R, double* G) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= R * R) return;
-  const int r = e / R, q = e - r * R;
-  T acc = (T)0;
-  for (int64_t s = 0; s < ns; ++s) acc = fma(kr[s * R + r], kr[s * R + q], acc);
-  G[e] = (double)acc;
-}
+// C_p[m, n] = sum over the samples s of split p of A[s, m] B[s, n]
+// (A: ns x M, B: ns x N, row-major), in the factor type, one partial plane
+// per split: 64 x 64 output tiles, 16 samples a step staged in shared
+// memory, 4 x 4 outputs a thread.  With A = X_s, B = KR_s the planes are
+// the split partials of M = X_s^T KR_s that the solve sums; with A = B = KR_s
+// they are those of the sampled Gram.
+constexpr int kAtbTile = 64, kAtbStep = 16;
 
-// M[i, r] = sum_s xs[s, i] kr[s, r] (the reference's dot(kr^T, X_s), transposed).
 template <typename T>
-__global__ void k_sampled_mttkrp(const T* __restrict__ xs, const T* __restrict__ kr, int64_t ns,
-                                 int64_t I, int R, T* __restrict__ M) {
-  const int64_t total = I * R;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = e / R;
-    const int r = (int)(e - i * R);
-    T acc = (T)0;
-    for (int64_t s = 0; s < ns; ++s) acc = fma(xs[s * I + i], kr[s * R + r], acc);
-    M[e] = acc;
+__global__ void __launch_bounds__(256)
+k_atb_split(const T* __restrict__ A, int64_t M, const T* __restrict__ B, int64_t N, int64_t ns,
+            int64_t per_split, T* __restrict__ C) {
+  __shared__ T As[kAtbStep][kAtbTile];
+  __shared__ T Bs[kAtbStep][kAtbTile];
+  const int tid = threadIdx.x, tm = tid >> 4, tn = tid & 15;
+  const int64_t m0 = (int64_t)blockIdx.x * kAtbTile, n0 = (int64_t)blockIdx.y * kAtbTile;
+  const int64_t s_begin = (int64_t)blockIdx.z * per_split;
+  const int64_t s_end = s_begin + per_split < ns ? s_begin + per_split : ns;
+  T acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = (T)0;
+  for (int64_t s0 = s_begin; s0 < s_end; s0 += kAtbStep) {
+    for (int e = tid; e < kAtbStep * kAtbTile; e += 256) {
+      const int ss = e / kAtbTile, c = e - ss * kAtbTile;
+      const int64_t s = s0 + ss;
+      As[ss][c] = (s < s_end && m0 + c < M) ? A[s * M + m0 + c] : (T)0;
+      Bs[ss][c] = (s < s_end && n0 + c < N) ? B[s * N + n0 + c] : (T)0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int ss = 0; ss < kAtbStep; ++ss) {
+      T av[4], bv[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) av[i] = As[ss][tm + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) bv[j] = Bs[ss][tn + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fma(av[i], bv[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+  T* Cp = C + (int64_t)blockIdx.z * M * N;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int64_t m = m0 + tm + 16 * i;
+    if (m >= M) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int64_t n = n0 + tn + 16 * j;
+      if (n < N) Cp[m * N + n] = acc[i][j];
+    }
   }
 }
 
+// G[e] = sum_p parts[p][e] in split order, as f64 for the factorisation.
+template <typename T>
+__global__ void k_sum_parts(const T* __restrict__ parts, int splits, int n, double* G) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  double s = 0.0;
+  for (int p = 0; p < splits; ++p) s += (double)parts[(int64_t)p * n + e];
+  G[e] = s;
+}
+
+// Sample splits: about 2 waves of 256-thread CTAs over the larger product.
+int atb_splits(int64_t ns, int64_t M, int64_t N) {
+  const int64_t tiles = ceil_div(M, (int64_t)kAtbTile) * ceil_div(N, (int64_t)kAtbTile);
+  const int64_t want = std::max<int64_t>(1, ceil_div((int64_t)152 * 6, tiles));
+  return (int)std::max<int64_t>(1, std::min<int64_t>(want, ceil_div(ns, (int64_t)(4 * kAtbStep))));
+}
+
 struct RandLayout {
-  size_t ctrl, G, fac, perm, vmat, w32, gpart, kr, xs, M, resid, bad, rec, bytes;
+  size_t ctrl, G, fac, perm, vmat, w32, gpart, kr, xs, M, Vp, resid, bad, rec, bytes;
 };
 
 RandLayout rand_layout(int dtype, int ndim, const int64_t* shape, int64_t R, int64_t ns) {
@@ -116,7 +164,11 @@ RandLayout rand_layout(int dtype, int ndim, const int64_t* shape, int64_t R, int
   L.gpart = take(sizeof(double) * RR * (size_t)solve_blocks_for(imax));
   L.kr = take(esz * (size_t)ns * R);
   L.xs = take(esz * (size_t)ns * imax);
-  L.M = take(esz * (size_t)imax * R);
+  size_t mparts = 0;                     // the largest split-partial set over the modes
+  for (int k = 0; k < ndim; ++k)
+    mparts = std::max(mparts, (size_t)shape[k] * R * atb_splits(ns, shape[k], R));
+  L.M = take(esz * mparts);
+  L.Vp = take(esz * (size_t)R * R * atb_splits(ns, R, R));
   L.resid = take(sizeof(double));
   L.bad = take(sizeof(int));
   L.rec = take(cp_full_ws_bytes(dtype, ndim, shape, R));
@@ -180,16 +232,28 @@ int rand_iteration(const T* X, int ndim, const int64_t* shape, int64_t R, T* con
     TLGB_LAUNCH_CHECK();
     // G slot 1 holds the sampled Gram: the factorisation of mode 0 of a
     // 2-mode problem uses exactly that matrix
-    k_sampled_gram<T><<<(RR + 127) / 128, 128, 0, st>>>(kr, ns, (int)R, G + RR);
-    TLGB_LAUNCH_CHECK();
-    const unsigned bm = (unsigned)std::min<int64_t>(ceil_div(I * R, (int64_t)128), 152 * 16);
-    k_sampled_mttkrp<T><<<bm, 128, 0, st>>>(xs, kr, ns, I, (int)R, M);
-    TLGB_LAUNCH_CHECK();
+    T* Vp = reinterpret_cast<T*>(base + L.Vp);
+    const int sv = atb_splits(ns, R, R);
+    {
+      dim3 g((unsigned)ceil_div(R, (int64_t)kAtbTile), (unsigned)ceil_div(R, (int64_t)kAtbTile),
+             (unsigned)sv);
+      k_atb_split<T><<<g, 256, 0, st>>>(kr, R, kr, R, ns, ceil_div(ns, (int64_t)sv), Vp);
+      TLGB_LAUNCH_CHECK();
+      k_sum_parts<T><<<(RR + 255) / 256, 256, 0, st>>>(Vp, sv, RR, G + RR);
+      TLGB_LAUNCH_CHECK();
+    }
+    const int sm = atb_splits(ns, I, R);
+    {
+      dim3 g((unsigned)ceil_div(I, (int64_t)kAtbTile), (unsigned)ceil_div(R, (int64_t)kAtbTile),
+             (unsigned)sm);
+      k_atb_split<T><<<g, 256, 0, st>>>(xs, I, kr, R, ns, ceil_div(ns, (int64_t)sm), M);
+      TLGB_LAUNCH_CHECK();
+    }
     int rc = als_launch_factorize<T>(G, 2, 0, (int)R, nullptr, 0.0, fac, perm, vmat, w32, ctrl,
                                      st);
     if (rc) return rc;
     int nb = 0;
-    rc = als_launch_solve<T>(M, 1, I, (int)R, fac, perm, vmat, w32, factors[mode], nullptr, gpart,
+    rc = als_launch_solve<T>(M, sm, I, (int)R, fac, perm, vmat, w32, factors[mode], nullptr, gpart,
                              nullptr, ctrl, kIrMaxPasses, &nb, st);
     if (rc) return rc;
   }
