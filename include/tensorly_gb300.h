@@ -474,6 +474,44 @@ int tlgb_cp_randomised_iteration(int dtype, const void* X, int ndim, const int64
                                  const int64_t* indices, double* rec_error, void* workspace,
                                  size_t workspace_bytes, void* stream);
 
+/* constraint kinds of tlgb_cp_constrained / tlgb_proximal */
+#define TLGB_CONS_NONE 0
+#define TLGB_CONS_NON_NEGATIVE 1   /* clip(x, 0, max(x)) */
+#define TLGB_CONS_L1 2             /* soft thresholding by param */
+#define TLGB_CONS_L2 3             /* x - x * param / max(||x||, param) */
+#define TLGB_CONS_L2_SQUARE 4      /* x / (1 + 2 param) */
+#define TLGB_CONS_NORMALIZE 5      /* x / max |x| */
+
+/*
+ * Constrained CP by AO-ADMM (tensorly/decomposition/_constrained_cp.py:166-435,
+ * ADMM tensorly/solvers/admm.py:5-135).  factors[k] (shape[k] x rank) hold
+ * the initial factors (already passed through their proximal operator, as
+ * initialize_constrained_parafac does) and receive the result; the dual
+ * variables start at zero.  kinds/params: per mode, the TLGB_CONS_* kind and
+ * its parameter (the proximal operators of tensorly/tenalg/proximal.py that
+ * act on the whole matrix).  free_modes ascending, the last mode free.
+ * errors (host, n_iter_max) receive the relative errors; *n_errors their
+ * count.  Synchronises `stream` once per outer iteration.
+ */
+int tlgb_cp_constrained_workspace_size(int dtype, int ndim, const int64_t* shape, int64_t rank,
+                                       size_t* bytes);
+int tlgb_cp_constrained(int dtype, const void* X, int ndim, const int64_t* shape,
+                        void* const* factors, int64_t rank, const int* free_modes, int n_free,
+                        const int* kinds, const double* params, int n_iter_max,
+                        int n_iter_max_inner, double tol_outer, double tol_inner,
+                        int cvg_criterion, double* errors, int* n_errors, void* workspace,
+                        size_t workspace_bytes, void* stream);
+
+/*
+ * proximal: out = the proximal operator `kind` (TLGB_CONS_*) with `param` of
+ * the n values of X (tensorly/tenalg/proximal.py:148-267, the whole-matrix
+ * operators).  Workspace of tlgb_proximal_workspace_bytes() bytes for
+ * non_negative, l2 and normalize (a global max or norm), else may be NULL.
+ */
+size_t tlgb_proximal_workspace_bytes(void);
+int tlgb_proximal(int dtype, const void* X, int64_t n, int kind, double param, void* out,
+                  void* workspace, size_t workspace_bytes, void* stream);
+
 /*
  * unfold: out (shape[mode] x prod(other modes)) = the mode-`mode` unfolding of
  * the C-order tensor X, columns in the C order of the other modes

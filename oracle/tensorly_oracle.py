@@ -30,7 +30,8 @@ __all__ = [
     "make_svd_non_negative", "hals_nnls", "non_negative_parafac_hals",
     "tucker_to_tensor", "validate_tucker_rank", "parafac_sweeps", "cp_to_unfolded",
     "cp_to_vec", "tucker_to_unfolded", "tucker_to_vec", "sample_khatri_rao",
-    "randomised_parafac",
+    "randomised_parafac", "validate_constraints", "proximal_operator", "admm",
+    "initialize_constrained_parafac", "constrained_parafac",
 ]
 
 
@@ -635,6 +636,187 @@ def randomised_parafac(tensor, rank, n_samples, n_iter_max=100, init="random",
             if iteration > 1:
                 if (tol and abs(rec_errors[-2] - rec_errors[-1]) < tol) or (
                         stagnation and (stagnation > max_stagnation)):
+                    break
+    if return_errors:
+        return (weights, factors), rec_errors
+    return weights, factors
+
+
+_CONSTRAINT_NAMES = ("non_negative", "l1_reg", "l2_reg", "l2_square_reg", "unimodality",
+                     "normalize", "simplex", "normalized_sparsity", "soft_sparsity",
+                     "smoothness", "monotonicity", "hard_sparsity")
+
+
+def validate_constraints(n_const=1, order=0, **given):
+    """tensorly/tenalg/proximal.py:4-145: (constraint name, parameter) of mode
+    ``order``.  A scalar applies to every mode; a list gives every mode the
+    constraint with its own entry; a dict constrains the listed modes."""
+    constraints = [None] * n_const
+    parameters = [None] * n_const
+    values = [given.get(n) for n in _CONSTRAINT_NAMES]
+    seen = set()
+    for v in values:
+        if v:
+            if isinstance(v, dict):
+                for mode in v:
+                    if mode in seen:
+                        raise ValueError("You selected two constraints for the same mode. "
+                                         "Consider to check your input")
+                    seen.add(mode)
+            elif isinstance(v, list):
+                for mode in range(len(v)):
+                    if v[mode]:
+                        if mode in seen:
+                            raise ValueError("You selected two constraints for the same "
+                                             "mode. Consider to check your input")
+                        seen.add(mode)
+            else:
+                if len(seen) > 0:
+                    raise ValueError("You selected two constraints for the same mode. "
+                                     "Consider to check your input")
+                for i in range(n_const):
+                    seen.add(i)
+    for v, name in zip(values, _CONSTRAINT_NAMES):
+        if v:
+            if isinstance(v, dict):
+                for mode in v:
+                    constraints[mode] = name
+                    parameters[mode] = v[mode]
+            else:
+                for i in range(n_const):
+                    constraints[i] = name
+                    parameters[i] = v[i] if isinstance(v, list) else v
+    return constraints[order], parameters[order]
+
+
+def proximal_operator(tensor, n_const=1, order=0, **given):
+    """tensorly/tenalg/proximal.py:148-267 for the constraints that act on the
+    whole matrix (non_negative, l1_reg, l2_reg, l2_square_reg, normalize)."""
+    if n_const is None:
+        return tensor
+    constraint, parameter = validate_constraints(n_const=n_const, order=order, **given)
+    if constraint is None:
+        return tensor
+    if constraint == "non_negative":
+        return np.clip(tensor, 0, np.max(tensor))
+    if constraint == "l1_reg":                      # soft_thresholding, :631-671
+        return np.sign(tensor) * np.clip(np.abs(tensor) - parameter, a_min=0, a_max=None)
+    if constraint == "l2_reg":                      # l2_prox, :466-493
+        nrm = norm(tensor)
+        bigger = nrm if nrm > parameter else parameter
+        return tensor - (tensor * parameter / bigger)
+    if constraint == "l2_square_reg":               # l2_square_prox, :444-463
+        return tensor / (1 + 2 * parameter)
+    if constraint == "normalize":
+        return tensor / np.max(np.abs(tensor))
+    raise NotImplementedError(f"oracle restates no {constraint} proximal operator")
+
+
+def admm(UtM, UtU, x, dual_var, n_iter_max=100, n_const=None, order=None, tol=1e-4, **given):
+    """tensorly/solvers/admm.py:5-135."""
+    rho = np.trace(UtU) / x.shape[1]
+    x_split = None
+    for _ in range(n_iter_max):
+        x_old = np.copy(x)
+        x_split = np.linalg.solve(np.transpose(UtU + rho * np.eye(UtU.shape[1])),
+                                  np.transpose(UtM + rho * (x + dual_var)))
+        x = proximal_operator(np.transpose(x_split) - dual_var, n_const=n_const, order=order,
+                              **given)
+        if n_const is None:
+            x = np.transpose(np.linalg.solve(np.transpose(UtU), np.transpose(UtM)))
+            return x, x_split, dual_var
+        dual_var = dual_var + x - np.transpose(x_split)
+        dual_residual = x - np.transpose(x_split)
+        primal_residual = x - x_old
+        if norm(dual_residual) < tol * norm(x) and norm(primal_residual) < tol * norm(dual_var):
+            break
+    return x, x_split, dual_var
+
+
+def initialize_constrained_parafac(tensor, rank, init="svd", svd="truncated_svd",
+                                   random_state=None, **given):
+    """tensorly/decomposition/_constrained_cp.py:22-163 ('random': the global
+    NumPy generator, as the reference's random_cp without a seed)."""
+    n_modes = tensor.ndim
+    rng = check_random_state(random_state)
+    if init == "random":
+        rns = check_random_state(None)
+        factors = [rns.random_sample((s, rank)).astype(tensor.dtype) for s in tensor.shape]
+    elif init == "svd":
+        factors = []
+        for mode in range(n_modes):
+            U, S, _ = svd_interface(unfold(tensor, mode), n_eigenvecs=rank, method=svd)
+            if mode == 0:
+                idx = min(rank, S.shape[0])
+                U = U.copy()
+                U[:, :idx] = U[:, :idx] * S[:idx]
+            if tensor.shape[mode] < rank:
+                random_part = rng.random_sample((U.shape[0], rank - tensor.shape[mode]))
+                U = np.concatenate([U, random_part.astype(U.dtype)], axis=1)
+            factors.append(U[:, :rank])
+    else:
+        weights, factors = init
+        factors = list(factors)
+        if not np.all(weights == 1):
+            weights_avg = np.prod(weights) ** (1.0 / weights.shape[0])
+            factors = [f * weights_avg for f in factors]
+        return None, factors
+    for i in range(n_modes):
+        factors[i] = proximal_operator(factors[i], n_const=n_modes, order=i, **given)
+    return None, factors
+
+
+def constrained_parafac(tensor, rank, n_iter_max=100, n_iter_max_inner=10, init="svd",
+                        svd="truncated_svd", tol_outer=1e-8, tol_inner=1e-6, random_state=None,
+                        return_errors=False, cvg_criterion="abs_rec_error", fixed_modes=None,
+                        **given):
+    """tensorly/decomposition/_constrained_cp.py:166-435 (AO-ADMM)."""
+    rank = validate_cp_rank(tensor.shape, rank=rank)
+    _, factors = initialize_constrained_parafac(tensor, rank, init=init, svd=svd,
+                                                random_state=random_state, **given)
+    weights = np.ones(rank, dtype=tensor.dtype)
+    rec_errors = []
+    norm_tensor = norm(tensor)
+    fixed_modes = [] if fixed_modes is None else list(fixed_modes)
+    if tensor.ndim - 1 in fixed_modes:
+        warnings.warn("You asked for fixing the last mode, which is not supported.\n "
+                      "The last mode will not be fixed. Consider using tl.moveaxis()")
+        fixed_modes.remove(tensor.ndim - 1)
+    modes_list = [m for m in range(tensor.ndim) if m not in fixed_modes]
+    dual_variables = [np.zeros(f.shape) for f in factors]
+    factors_aux = [np.transpose(np.zeros(f.shape)) for f in factors]
+    mttkrp = None
+    for iteration in range(n_iter_max):
+        for mode in modes_list:
+            pseudo_inverse = np.ones((rank, rank), dtype=tensor.dtype)
+            for i, factor in enumerate(factors):
+                if i != mode:
+                    pseudo_inverse = pseudo_inverse * np.dot(np.transpose(factor), factor)
+            mttkrp = unfolding_dot_khatri_rao(tensor, (None, factors), mode)
+            factors[mode], factors_aux[mode], dual_variables[mode] = admm(
+                mttkrp, pseudo_inverse, factors[mode], dual_variables[mode],
+                n_iter_max=n_iter_max_inner, n_const=tensor.ndim, order=mode, tol=tol_inner,
+                **given)
+        factors_norm = cp_norm((weights, factors))
+        iprod = np.sum(np.sum(mttkrp * factors[-1], axis=0) * weights)
+        rec_error = np.sqrt(np.abs(norm_tensor ** 2 + factors_norm ** 2 - 2 * iprod)) / norm_tensor
+        rec_errors.append(rec_error)
+        constraint_error = 0
+        for mode in modes_list:
+            constraint_error += norm(factors[mode] - np.transpose(factors_aux[mode])) / \
+                norm(factors[mode])
+        if tol_outer:
+            if iteration >= 1:
+                dec = rec_errors[-2] - rec_errors[-1]
+                if constraint_error < tol_outer:
+                    break
+                if cvg_criterion == "abs_rec_error":
+                    stop_flag = abs(dec) < tol_outer
+                elif cvg_criterion == "rec_error":
+                    stop_flag = dec < tol_outer
+                else:
+                    raise TypeError("Unknown convergence criterion")
+                if stop_flag:
                     break
     if return_errors:
         return (weights, factors), rec_errors

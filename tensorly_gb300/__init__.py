@@ -17,10 +17,11 @@ from .base import fold, tensor_to_vec, unfold, vec_to_tensor
 from .cp_tensor import (CPTensor, TuckerTensor, cp_norm, cp_normalize, cp_to_tensor,
                         cp_to_unfolded, cp_to_vec, tucker_to_tensor, tucker_to_unfolded,
                         tucker_to_vec, validate_cp_rank, validate_tucker_rank)
-from .decomposition import (CP, CP_NN, CP_NN_HALS, RandomizedCP, Tucker, initialize_cp,
+from .decomposition import (CP, CP_NN, CP_NN_HALS, ConstrainedCP, RandomizedCP, Tucker,
+                            constrained_parafac, initialize_constrained_parafac, initialize_cp,
                             initialize_tucker, non_negative_parafac, non_negative_parafac_hals,
-                            parafac, parafac_batched, partial_tucker, randomised_parafac,
-                            sample_khatri_rao, tucker)
+                            parafac, parafac_batched, partial_tucker, proximal_operator,
+                            randomised_parafac, sample_khatri_rao, tucker, validate_constraints)
 from .svd import svd_flip, svd_interface, truncated_svd
 from .random import check_random_state, random_cp
 from .tenalg import khatri_rao, mode_dot, multi_mode_dot, unfolding_dot_khatri_rao

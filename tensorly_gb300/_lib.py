@@ -219,6 +219,18 @@ SIGNATURES = [
     ("tlgb_sample_khatri_rao", ctypes.c_int,
      [ctypes.c_int, ctypes.c_int, _c_vpp, _c_i64p, ctypes.c_int64, ctypes.c_int64,
       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    ("tlgb_cp_constrained_workspace_size", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_int, _c_i64p, ctypes.c_int64, ctypes.POINTER(ctypes.c_size_t)]),
+    ("tlgb_cp_constrained", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, _c_i64p, _c_vpp, ctypes.c_int64,
+      ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+      ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.c_int, ctypes.c_double,
+      ctypes.c_double, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+      ctypes.POINTER(ctypes.c_int), ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    ("tlgb_proximal_workspace_bytes", ctypes.c_size_t, []),
+    ("tlgb_proximal", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_double,
+      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     ("tlgb_unfold", ctypes.c_int,
      [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, _c_i64p, ctypes.c_int, ctypes.c_void_p,
       ctypes.c_void_p]),

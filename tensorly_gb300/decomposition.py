@@ -858,6 +858,241 @@ class RandomizedCP:
         return f"Rank-{self.rank} Randomized CP decomposition."
 
 
+_CONSTRAINT_NAMES = ("non_negative", "l1_reg", "l2_reg", "l2_square_reg", "unimodality",
+                     "normalize", "simplex", "normalized_sparsity", "soft_sparsity",
+                     "smoothness", "monotonicity", "hard_sparsity")
+# library kinds of the whole-matrix proximal operators (TLGB_CONS_*)
+_CONSTRAINT_KIND = {None: 0, "non_negative": 1, "l1_reg": 2, "l2_reg": 3, "l2_square_reg": 4,
+                    "normalize": 5}
+
+
+def validate_constraints(non_negative=None, l1_reg=None, l2_reg=None, l2_square_reg=None,
+                         unimodality=None, normalize=None, simplex=None, normalized_sparsity=None,
+                         soft_sparsity=None, smoothness=None, monotonicity=None,
+                         hard_sparsity=None, n_const=1, order=0):
+    """(constraint, parameter) of mode ``order`` (tensorly/tenalg/proximal.py:4-145):
+    a scalar applies to every mode; a list gives every mode the constraint with
+    its own entry; a dict constrains the listed modes; a mode constrained twice
+    raises ValueError."""
+    values = [non_negative, l1_reg, l2_reg, l2_square_reg, unimodality, normalize, simplex,
+              normalized_sparsity, soft_sparsity, smoothness, monotonicity, hard_sparsity]
+    constraints = [None] * n_const
+    parameters = [None] * n_const
+    seen = set()
+    twice = "You selected two constraints for the same mode. Consider to check your input"
+    for v in values:
+        if not v:
+            continue
+        if isinstance(v, dict):
+            for mode in v:
+                if mode in seen:
+                    raise ValueError(twice)
+                seen.add(mode)
+        elif isinstance(v, list):
+            for mode in range(len(v)):
+                if v[mode]:
+                    if mode in seen:
+                        raise ValueError(twice)
+                    seen.add(mode)
+        else:
+            if len(seen) > 0:
+                raise ValueError(twice)
+            seen.update(range(n_const))
+    for v, name in zip(values, _CONSTRAINT_NAMES):
+        if not v:
+            continue
+        if isinstance(v, dict):
+            for mode in v:
+                constraints[mode] = name
+                parameters[mode] = v[mode]
+        else:
+            for i in range(n_const):
+                constraints[i] = name
+                parameters[i] = v[i] if isinstance(v, list) else v
+    return constraints[order], parameters[order]
+
+
+def _constraint_kind(constraint, parameter):
+    if constraint not in _CONSTRAINT_KIND:
+        raise NotImplementedError(f"the {constraint} proximal operator (a column-wise projection) "
+                                  "is not supported by tensorly_gb300")
+    if constraint in ("l1_reg", "l2_reg", "l2_square_reg") and parameter is None:
+        raise TypeError(f"{constraint} needs a numeric parameter for every constrained mode")
+    return _CONSTRAINT_KIND[constraint], float(parameter) if constraint in (
+        "l1_reg", "l2_reg", "l2_square_reg") else 0.0
+
+
+def proximal_operator(tensor, n_const=1, order=0, **constraints):
+    """The proximal operator of mode ``order``'s constraint applied to a whole
+    matrix (tensorly/tenalg/proximal.py:148-267) by ``tlgb_proximal``:
+    non_negative, l1_reg, l2_reg, l2_square_reg and normalize."""
+    x, pl = to_device(tensor)
+    if n_const is None:
+        return pl.back(x)
+    constraint, parameter = validate_constraints(n_const=n_const, order=order, **constraints)
+    if constraint is None:
+        return pl.back(x)
+    kind, param = _constraint_kind(constraint, parameter)
+    x = x.contiguous()
+    out = torch.empty_like(x)
+    lib = _lib.lib()
+    ws = workspace(lib.tlgb_proximal_workspace_bytes(), x.device)
+    _lib.check(lib.tlgb_proximal(dtype_code(x), x.data_ptr(), x.numel(), kind, param,
+                                 out.data_ptr(), ptr(ws), ws.numel(), stream_of(x)))
+    return pl.back(out)
+
+
+def initialize_constrained_parafac(tensor, rank, init="svd", svd="truncated_svd",
+                                   random_state=None, **constraints):
+    """tensorly/decomposition/_constrained_cp.py:22-163: the 'svd' start of
+    ``initialize_cp``, or for 'random' factors drawn from NumPy's global
+    generator as the reference's random_cp without a seed does; then every
+    factor passes through its mode's proximal operator.  A CPTensor start is
+    returned with its weights folded into the factors, without the operator."""
+    x, pl = to_device(tensor)
+    n_modes = x.ndim
+    if init == "random":
+        rns = check_random_state(None)
+        factors = [torch.from_numpy(rns.random_sample((s, rank))).to(x.device, x.dtype)
+                   for s in x.shape]
+    elif init == "svd":
+        _, factors = initialize_cp(x, rank, init="svd", svd=svd, random_state=random_state)
+        factors = [f.to(x.dtype) for f in factors]
+    elif isinstance(init, (tuple, list, CPTensor)):
+        weights, factors = init
+        factors = [to_device(f)[0].to(x.dtype) for f in factors]
+        w = to_device(weights)[0] if weights is not None else None
+        if w is not None and not bool((w == 1).all()):
+            weights_avg = float(torch.prod(w.double()) ** (1.0 / w.shape[0]))
+            factors = [_scale_all(f, weights_avg) for f in factors]
+        return CPTensor((None, [pl.back(f) for f in factors]))
+    else:
+        raise ValueError(f'Initialization method "{init}" not recognized')
+    factors = [to_device(proximal_operator(f, n_const=n_modes, order=i, **constraints))[0]
+               for i, f in enumerate(factors)]
+    return CPTensor((None, [pl.back(f) for f in factors]))
+
+
+def constrained_parafac(tensor, rank, n_iter_max=100, n_iter_max_inner=10, init="svd",
+                        svd="truncated_svd", tol_outer=1e-8, tol_inner=1e-6, random_state=None,
+                        verbose=0, return_errors=False, cvg_criterion="abs_rec_error",
+                        fixed_modes=None, non_negative=None, l1_reg=None, l2_reg=None,
+                        l2_square_reg=None, unimodality=None, normalize=None, simplex=None,
+                        normalized_sparsity=None, soft_sparsity=None, smoothness=None,
+                        monotonicity=None, hard_sparsity=None):
+    """Constrained CP by AO-ADMM (tensorly/decomposition/_constrained_cp.py:166-435),
+    same signature and returns.
+
+    The outer and inner (ADMM) loops run in ``tlgb_cp_constrained``: per free
+    mode the factorisation of (Hadamard of Grams) + rho I, the MTTKRP, and
+    ADMM iterations (solve, proximal operator, dual update, stop test) with no
+    host round trip; one synchronisation per outer iteration for the error
+    and the stop tests.  The proximal operators that act on the whole factor
+    matrix are supported (non_negative, l1_reg, l2_reg, l2_square_reg,
+    normalize); the column-wise ones (unimodality, simplex, the sparsity
+    projections, smoothness, monotonicity) raise NotImplementedError."""
+    cons = dict(non_negative=non_negative, l1_reg=l1_reg, l2_reg=l2_reg,
+                l2_square_reg=l2_square_reg, unimodality=unimodality, normalize=normalize,
+                simplex=simplex, normalized_sparsity=normalized_sparsity,
+                soft_sparsity=soft_sparsity, smoothness=smoothness, monotonicity=monotonicity,
+                hard_sparsity=hard_sparsity)
+    x, placement = to_device(tensor)
+    code = dtype_code(x)
+    x = x.contiguous()
+    n_modes = x.ndim
+    if n_modes < 2:
+        raise NotImplementedError("constrained_parafac needs at least two modes")
+    rank = validate_cp_rank(tuple(x.shape), rank=rank)
+    kinds, params = [], []
+    for mode in range(n_modes):
+        k, p = _constraint_kind(*validate_constraints(n_const=n_modes, order=mode, **cons))
+        kinds.append(k)
+        params.append(p)
+    if cvg_criterion not in ("abs_rec_error", "rec_error") and tol_outer and n_iter_max > 1:
+        raise TypeError("Unknown convergence criterion")
+    _, factors = initialize_constrained_parafac(x, rank, init=init, svd=svd,
+                                                random_state=random_state, **cons)
+    factors = [to_device(f)[0].to(x.dtype).contiguous().clone() for f in factors]
+    fixed = [] if fixed_modes is None else list(fixed_modes)
+    if n_modes - 1 in fixed:
+        warnings.warn("You asked for fixing the last mode, which is not supported.\n "
+                      "The last mode will not be fixed. Consider using tl.moveaxis()")
+        fixed.remove(n_modes - 1)
+    free = [m for m in range(n_modes) if m not in fixed]
+    lib = _lib.lib()
+    shape = (ctypes.c_int64 * n_modes)(*x.shape)
+    nbytes = ctypes.c_size_t(0)
+    _lib.check(lib.tlgb_cp_constrained_workspace_size(code, n_modes, shape, rank,
+                                                      ctypes.byref(nbytes)))
+    ws = workspace(nbytes.value, x.device)
+    fptrs = (ctypes.c_void_p * n_modes)(*[f.data_ptr() for f in factors])
+    errs = (ctypes.c_double * max(1, int(n_iter_max)))()
+    n_err = ctypes.c_int(0)
+    _lib.check(lib.tlgb_cp_constrained(
+        code, x.data_ptr(), n_modes, shape, fptrs, rank, (ctypes.c_int * len(free))(*free),
+        len(free), (ctypes.c_int * n_modes)(*kinds), (ctypes.c_double * n_modes)(*params),
+        int(n_iter_max), int(n_iter_max_inner), float(tol_outer or 0.0), float(tol_inner),
+        0 if cvg_criterion == "abs_rec_error" else 1, errs, ctypes.byref(n_err), ptr(ws),
+        ws.numel(), stream_of(x)))
+    weights = torch.ones(rank, dtype=x.dtype, device=x.device)
+    cp = CPTensor((placement.back(weights), [placement.back(f) for f in factors]))
+    if return_errors:
+        return cp, [float(errs[i]) for i in range(n_err.value)]
+    return cp
+
+
+class ConstrainedCP(DecompositionMixin):
+    """sklearn-style wrapper of ``constrained_parafac``
+    (tensorly/decomposition/_constrained_cp.py:426-612)."""
+
+    def __init__(self, rank, n_iter_max=100, n_iter_max_inner=10, init="svd",
+                 svd="truncated_svd", tol_outer=1e-8, tol_inner=1e-6, random_state=None,
+                 verbose=0, return_errors=False, cvg_criterion="abs_rec_error", fixed_modes=None,
+                 non_negative=None, l1_reg=None, l2_reg=None, l2_square_reg=None,
+                 unimodality=None, normalize=None, simplex=None, normalized_sparsity=None,
+                 soft_sparsity=None, smoothness=None, monotonicity=None, hard_sparsity=None):
+        self.rank = rank
+        self.n_iter_max = n_iter_max
+        self.n_iter_max_inner = n_iter_max_inner
+        self.init = init
+        self.svd = svd
+        self.tol_outer = tol_outer
+        self.tol_inner = tol_inner
+        self.random_state = random_state
+        self.verbose = verbose
+        self.return_errors = return_errors
+        self.cvg_criterion = cvg_criterion
+        self.fixed_modes = fixed_modes
+        self.non_negative = non_negative
+        self.l1_reg = l1_reg
+        self.l2_reg = l2_reg
+        self.l2_square_reg = l2_square_reg
+        self.unimodality = unimodality
+        self.normalize = normalize
+        self.simplex = simplex
+        self.normalized_sparsity = normalized_sparsity
+        self.soft_sparsity = soft_sparsity
+        self.smoothness = smoothness
+        self.monotonicity = monotonicity
+        self.hard_sparsity = hard_sparsity
+
+    def fit_transform(self, tensor):
+        cp, errors = constrained_parafac(
+            tensor, rank=self.rank, n_iter_max=self.n_iter_max,
+            n_iter_max_inner=self.n_iter_max_inner, init=self.init, svd=self.svd,
+            tol_outer=self.tol_outer, tol_inner=self.tol_inner, random_state=self.random_state,
+            verbose=self.verbose, cvg_criterion=self.cvg_criterion,
+            fixed_modes=self.fixed_modes, non_negative=self.non_negative, l1_reg=self.l1_reg,
+            l2_reg=self.l2_reg, l2_square_reg=self.l2_square_reg, unimodality=self.unimodality,
+            normalize=self.normalize, simplex=self.simplex,
+            normalized_sparsity=self.normalized_sparsity, soft_sparsity=self.soft_sparsity,
+            smoothness=self.smoothness, monotonicity=self.monotonicity,
+            hard_sparsity=self.hard_sparsity, return_errors=True)
+        self.decomposition_ = cp
+        self.errors_ = errors
+        return self.decomposition_
+
+
 class BatchedProblem:
     """Many small 3-way f32 tensors packed for ``tlgb_cp_als_batched``.
 

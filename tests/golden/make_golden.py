@@ -310,6 +310,41 @@ def reference_runs():
                  "factors_in": fs, "sampled_kr": np.array(skr),
                  "indices_list": [np.array(i) for i in ind], "indices_kr": np.array(ind_kr)})
 
+    # constrained CP by AO-ADMM (tensorly/decomposition/_constrained_cp.py:166-435);
+    # init='random' draws from NumPy's global generator, seeded per case
+    from tensorly.decomposition import constrained_parafac
+    cons_variants = [
+        ("cons_nonneg_svd", dict(shape=(10, 9, 8), rank=3, seed=81),
+         dict(non_negative=True, init="svd", n_iter_max=20, tol_outer=1e-10), None),
+        ("cons_l1_random", dict(shape=(9, 8, 7), rank=3, seed=82),
+         dict(l1_reg=0.05, init="random", n_iter_max=15, tol_outer=1e-10), 5),
+        ("cons_l2sq_list", dict(shape=(8, 7, 6), rank=2, seed=83),
+         dict(l2_square_reg=[0.1, 0.2, 0.3], init="svd", n_iter_max=15, tol_outer=1e-10), None),
+        ("cons_l2_dict_fixed", dict(shape=(8, 7, 6, 5), rank=2, seed=84),
+         dict(l2_reg={0: 0.01, 2: 0.02}, fixed_modes=[1], init="svd", n_iter_max=10,
+              tol_outer=1e-10, cvg_criterion="rec_error"), None),
+        ("cons_normalize_mixed", dict(shape=(9, 8, 7), rank=3, seed=85),
+         dict(normalize={1: True}, non_negative={0: True, 2: True}, init="svd", n_iter_max=12,
+              tol_outer=1e-10), None),
+        ("cons_inner", dict(shape=(10, 9, 8), rank=2, seed=86),
+         dict(non_negative=True, init="svd", n_iter_max=8, n_iter_max_inner=30,
+              tol_inner=1e-10, tol_outer=1e-10), None),
+        ("cons_stop", dict(shape=(10, 9, 8), rank=2, seed=87),
+         dict(l2_square_reg=0.01, init="svd", n_iter_max=200, tol_outer=1e-7), None),
+        ("cons_f32", dict(shape=(12, 10, 9), rank=3, seed=88, dtype=np.float32),
+         dict(non_negative=True, init="svd", n_iter_max=10, tol_outer=1e-10), None),
+    ]
+    for name, g, kw, gseed in cons_variants:
+        x = small(g["seed"], g["shape"], g["rank"], g.get("dtype", np.float64))
+        if gseed is not None:
+            np.random.seed(gseed)
+        cp, errs = constrained_parafac(x, g["rank"], return_errors=True, **copy.deepcopy(kw))
+        runs.append({"case": name, "gen": {"fn": "small", **g}, "checksum": cs(x),
+                     "kwargs": {"rank": g["rank"], **kw}, "global_seed": gseed,
+                     "weights": np.array(cp.weights),
+                     "factors": [np.array(f) for f in cp.factors],
+                     "errors": [float(e) for e in errs]})
+
     # Tucker (HOOI) small cases
     tcases = [
         ("tucker_svd", dict(shape=(12, 10, 8), seed=31), dict(rank=[3, 4, 2], init="svd",

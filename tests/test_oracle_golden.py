@@ -152,6 +152,27 @@ def test_oracle_sample_khatri_rao_matches_reference(golden):
         np.testing.assert_array_equal(a, b)
 
 
+CONS_CASES = ["cons_nonneg_svd", "cons_l1_random", "cons_l2sq_list", "cons_l2_dict_fixed",
+              "cons_normalize_mixed", "cons_inner", "cons_stop", "cons_f32"]
+
+
+@pytest.mark.parametrize("case", CONS_CASES)
+def test_oracle_constrained_parafac_matches_reference(golden, case):
+    run = golden["runs"][case]
+    x = regenerate(run)
+    kw = dict(run["kwargs"])
+    rank = kw.pop("rank")
+    if run["global_seed"] is not None:
+        np.random.seed(run["global_seed"])
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        (w, f), errs = oracle.constrained_parafac(x, rank, return_errors=True, **kw)
+    assert len(errs) == len(run["errors"])
+    np.testing.assert_allclose(errs, run["errors"], rtol=1e-10, atol=1e-12)
+    for a, b in zip(f, run["factors"]):
+        np.testing.assert_allclose(a, b, rtol=1e-9, atol=1e-9 * np.abs(b).max())
+
+
 @pytest.mark.parametrize("case", ["tucker_svd", "tucker_random", "tucker_4way"])
 def test_oracle_tucker_matches_reference(golden, case):
     run = golden["runs"][case]
