@@ -513,6 +513,28 @@ int tlgb_proximal(int dtype, const void* X, int64_t n, int kind, double param, v
                   void* workspace, size_t workspace_bytes, void* stream);
 
 /*
+ * gemm: C (M x N, row-major) = sum_k A[m*sam + k*sak] * B[k*sbk + n*sbn]
+ * (any transposition through the strides), accumulated in the input type.
+ * For the core-sized products of the Tucker updates (tl.dot on unfolded
+ * cores and factor Grams); not a tuned large GEMM.
+ */
+int tlgb_gemm(int dtype, int64_t M, int64_t N, int64_t K, const void* A, int64_t sam,
+              int64_t sak, const void* B, int64_t sbk, int64_t sbn, void* C, void* stream);
+
+/*
+ * mu_update: A <- A * max(num, eps) / max(den, eps), elementwise over n
+ * values (the multiplicative updates of tensorly/decomposition/_tucker.py:
+ * 396-418, clip(a_min=eps)).
+ */
+int tlgb_mu_update(int dtype, void* A, const void* num, const void* den, int64_t n, double eps,
+                   void* stream);
+
+/* dot: *out (device double) = sum_e a[e] * b[e], f64, in a fixed order. */
+size_t tlgb_dot_workspace_bytes(void);
+int tlgb_dot(int dtype, const void* a, const void* b, int64_t n, double* out, void* workspace,
+             size_t workspace_bytes, void* stream);
+
+/*
  * unfold: out (shape[mode] x prod(other modes)) = the mode-`mode` unfolding of
  * the C-order tensor X, columns in the C order of the other modes
  * (tensorly/base.py:39-53, moveaxis(X, mode, 0).reshape(shape[mode], -1)).

@@ -31,7 +31,7 @@ __all__ = [
     "tucker_to_tensor", "validate_tucker_rank", "parafac_sweeps", "cp_to_unfolded",
     "cp_to_vec", "tucker_to_unfolded", "tucker_to_vec", "sample_khatri_rao",
     "randomised_parafac", "validate_constraints", "proximal_operator", "admm",
-    "initialize_constrained_parafac", "constrained_parafac",
+    "initialize_constrained_parafac", "constrained_parafac", "non_negative_tucker",
 ]
 
 
@@ -966,12 +966,14 @@ def tucker_to_vec(tucker_tensor, skip_factor=None, transpose_factors=False):
                                        transpose_factors=transpose_factors), (-1,))
 
 
-def initialize_tucker(tensor, rank, modes, random_state, init="svd", svd="truncated_svd"):
-    """tensorly/decomposition/_tucker.py:25-102 (non_negative=False, no mask)."""
+def initialize_tucker(tensor, rank, modes, random_state, init="svd", svd="truncated_svd",
+                      non_negative=False):
+    """tensorly/decomposition/_tucker.py:25-102 (no mask)."""
     if isinstance(init, str) and init == "svd":
         factors = []
         for index, mode in enumerate(modes):
-            U, _, _ = svd_interface(unfold(tensor, mode), n_eigenvecs=rank[index], method=svd)
+            U, _, _ = svd_interface(unfold(tensor, mode), n_eigenvecs=rank[index], method=svd,
+                                    non_negative=non_negative)
             factors.append(U)
         core = multi_mode_dot(tensor, factors, modes=modes, transpose=True)
     elif isinstance(init, str) and init == "random":
@@ -981,7 +983,48 @@ def initialize_tucker(tensor, rank, modes, random_state, init="svd", svd="trunca
                    for index, mode in enumerate(modes)]
     else:
         core, factors = init
+    if non_negative is True:
+        factors = [np.abs(f) for f in factors]
+        core = np.abs(core)
     return core, list(factors)
+
+
+def non_negative_tucker(tensor, rank, n_iter_max=10, init="svd", tol=10e-5, random_state=None,
+                        return_errors=False):
+    """tensorly/decomposition/_tucker.py:348-454 (multiplicative updates, not
+    verbose, normalize_factors=False), with the reference's explicit B."""
+    rank = validate_tucker_rank(tensor.shape, rank=rank)
+    epsilon = 10e-12
+    nn_core, nn_factors = initialize_tucker(tensor, rank, range(tensor.ndim), init=init,
+                                            random_state=random_state, non_negative=True)
+    nn_factors = list(nn_factors)
+    norm_tensor = norm(tensor)
+    rec_errors = []
+    for iteration in range(n_iter_max):
+        for mode in range(tensor.ndim):
+            B = tucker_to_tensor((nn_core, nn_factors), skip_factor=mode)
+            B = np.transpose(unfold(B, mode))
+            numerator = np.dot(unfold(tensor, mode), B)
+            numerator = np.clip(numerator, a_min=epsilon, a_max=None)
+            denominator = np.dot(nn_factors[mode], np.dot(np.transpose(B), B))
+            denominator = np.clip(denominator, a_min=epsilon, a_max=None)
+            nn_factors[mode] = nn_factors[mode] * (numerator / denominator)
+        numerator = tucker_to_tensor((tensor, nn_factors), transpose_factors=True)
+        numerator = np.clip(numerator, a_min=epsilon, a_max=None)
+        for i, f in enumerate(nn_factors):
+            if i:
+                denominator = mode_dot(denominator, np.dot(np.transpose(f), f), i)
+            else:
+                denominator = mode_dot(nn_core, np.dot(np.transpose(f), f), i)
+        denominator = np.clip(denominator, a_min=epsilon, a_max=None)
+        nn_core = nn_core * (numerator / denominator)
+        rec_error = norm(tensor - tucker_to_tensor((nn_core, nn_factors))) / norm_tensor
+        rec_errors.append(rec_error)
+        if iteration > 1 and abs(rec_errors[-2] - rec_errors[-1]) < tol:
+            break
+    if return_errors:
+        return (nn_core, nn_factors), rec_errors
+    return nn_core, nn_factors
 
 
 def partial_tucker(tensor, rank, modes=None, n_iter_max=100, init="svd", tol=10e-5,

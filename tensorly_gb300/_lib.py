@@ -231,6 +231,17 @@ SIGNATURES = [
     ("tlgb_proximal", ctypes.c_int,
      [ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_double,
       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    ("tlgb_gemm", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p,
+      ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
+      ctypes.c_void_p, ctypes.c_void_p]),
+    ("tlgb_mu_update", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+      ctypes.c_double, ctypes.c_void_p]),
+    ("tlgb_dot_workspace_bytes", ctypes.c_size_t, []),
+    ("tlgb_dot", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+      ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     ("tlgb_unfold", ctypes.c_int,
      [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, _c_i64p, ctypes.c_int, ctypes.c_void_p,
       ctypes.c_void_p]),

@@ -1,0 +1,162 @@
+// Small dense operations the non-negative Tucker update is composed of: a
+// strided GEMM for the core-sized products (tensorly's tl.dot on unfolded
+// cores and factor Grams), the multiplicative update
+// A <- A * clip(num, eps) / clip(den, eps) (tensorly/decomposition/_tucker.py:
+// 396-406 and 410-418), and an f64 inner product.
+#include "common.cuh"
+
+namespace tlgb {
+namespace {
+
+constexpr int kGemmTile = 32;
+
+// C[m, n] = sum_k A[m * sam + k * sak] * B[k * sbk + n * sbn] (C row-major,
+// ldc = N); accumulated in T in k order.  32 x 32 output tiles, 16 k a step
+// staged in shared memory, 4 outputs a thread.
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_gemm_strided(int64_t M, int64_t N, int64_t K, const T* __restrict__ A, int64_t sam,
+               int64_t sak, const T* __restrict__ B, int64_t sbk, int64_t sbn, T* __restrict__ C) {
+  constexpr int KS = 16;
+  __shared__ T As[KS][kGemmTile + 1];
+  __shared__ T Bs[KS][kGemmTile + 1];
+  const int tid = threadIdx.x;
+  const int tn = tid & 31, tm = tid >> 5;              // 8 row groups of 4
+  const int64_t m0 = (int64_t)blockIdx.y * kGemmTile, n0 = (int64_t)blockIdx.x * kGemmTile;
+  T acc[4] = {(T)0, (T)0, (T)0, (T)0};
+  for (int64_t k0 = 0; k0 < K; k0 += KS) {
+    for (int e = tid; e < KS * kGemmTile; e += 256) {
+      const int kk = e / kGemmTile, c = e - kk * kGemmTile;
+      const int64_t k = k0 + kk;
+      As[kk][c] = (k < K && m0 + c < M) ? A[(m0 + c) * sam + k * sak] : (T)0;
+      Bs[kk][c] = (k < K && n0 + c < N) ? B[k * sbk + (n0 + c) * sbn] : (T)0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < KS; ++kk) {
+      const T b = Bs[kk][tn];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) acc[i] = fma(As[kk][tm * 4 + i], b, acc[i]);
+    }
+    __syncthreads();
+  }
+  const int64_t n = n0 + tn;
+  if (n >= N) return;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int64_t m = m0 + tm * 4 + i;
+    if (m < M) C[m * N + n] = acc[i];
+  }
+}
+
+// A <- A * max(num, eps) / max(den, eps)  (the reference's clip(a_min=eps)).
+template <typename T>
+__global__ void k_mu_apply(T* __restrict__ A, const T* __restrict__ num,
+                           const T* __restrict__ den, int64_t n, T eps) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const T a = num[e] > eps ? num[e] : eps;
+    const T b = den[e] > eps ? den[e] : eps;
+    A[e] = A[e] * (a / b);
+  }
+}
+
+constexpr int kDotBlocks = 128;
+
+template <typename T>
+__global__ void k_dot_part(const T* __restrict__ a, const T* __restrict__ b, int64_t n,
+                           double* part) {
+  __shared__ double red[8];
+  double s = 0.0;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x)
+    s += (double)a[e] * (double)b[e];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < 8; ++w) t += red[w];
+    part[blockIdx.x] = t;
+  }
+}
+
+__global__ void k_dot_final(const double* part, int nb, double* out) {
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int b = 0; b < nb; ++b) t += part[b];
+    *out = t;
+  }
+}
+
+}  // namespace
+}  // namespace tlgb
+
+using namespace tlgb;
+
+extern "C" int tlgb_gemm(int dtype, int64_t M, int64_t N, int64_t K, const void* A, int64_t sam,
+                         int64_t sak, const void* B, int64_t sbk, int64_t sbn, void* C,
+                         void* stream) {
+  clear_error();
+  TLGB_CHECK_ARG(dtype == TLGB_F32 || dtype == TLGB_F64, "gemm: dtype must be f32 or f64");
+  TLGB_CHECK_ARG(M >= 0 && N >= 0 && K >= 0, "gemm: negative size");
+  TLGB_CHECK_ARG(C != nullptr && (K == 0 || (A && B)), "gemm: null pointer");
+  if (M == 0 || N == 0) return TLGB_OK;
+  const int64_t gx = ceil_div(N, (int64_t)kGemmTile), gy = ceil_div(M, (int64_t)kGemmTile);
+  TLGB_CHECK_ARG(gx <= INT32_MAX && gy <= 65535, "gemm: too large");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  dim3 grid((unsigned)gx, (unsigned)gy);
+  if (dtype == TLGB_F64)
+    k_gemm_strided<double><<<grid, 256, 0, st>>>(M, N, K, static_cast<const double*>(A), sam, sak,
+                                                 static_cast<const double*>(B), sbk, sbn,
+                                                 static_cast<double*>(C));
+  else
+    k_gemm_strided<float><<<grid, 256, 0, st>>>(M, N, K, static_cast<const float*>(A), sam, sak,
+                                                static_cast<const float*>(B), sbk, sbn,
+                                                static_cast<float*>(C));
+  TLGB_LAUNCH_CHECK();
+  return TLGB_OK;
+}
+
+extern "C" int tlgb_mu_update(int dtype, void* A, const void* num, const void* den, int64_t n,
+                              double eps, void* stream) {
+  clear_error();
+  TLGB_CHECK_ARG(dtype == TLGB_F32 || dtype == TLGB_F64, "mu_update: dtype must be f32 or f64");
+  TLGB_CHECK_ARG(A && num && den && n >= 0, "mu_update: bad argument");
+  if (n == 0) return TLGB_OK;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const unsigned nb = (unsigned)std::min<int64_t>(ceil_div(n, (int64_t)256), 152 * 8);
+  if (dtype == TLGB_F64)
+    k_mu_apply<double><<<nb, 256, 0, st>>>(static_cast<double*>(A),
+                                           static_cast<const double*>(num),
+                                           static_cast<const double*>(den), n, eps);
+  else
+    k_mu_apply<float><<<nb, 256, 0, st>>>(static_cast<float*>(A), static_cast<const float*>(num),
+                                          static_cast<const float*>(den), n, (float)eps);
+  TLGB_LAUNCH_CHECK();
+  return TLGB_OK;
+}
+
+extern "C" size_t tlgb_dot_workspace_bytes(void) { return sizeof(double) * kDotBlocks; }
+
+extern "C" int tlgb_dot(int dtype, const void* a, const void* b, int64_t n, double* out,
+                        void* workspace, size_t workspace_bytes, void* stream) {
+  clear_error();
+  TLGB_CHECK_ARG(dtype == TLGB_F32 || dtype == TLGB_F64, "dot: dtype must be f32 or f64");
+  TLGB_CHECK_ARG(a && b && out && n >= 0, "dot: bad argument");
+  if (!workspace || workspace_bytes < sizeof(double) * kDotBlocks)
+    return set_error(TLGB_EWORKSPACE, "dot: workspace too small");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  double* part = static_cast<double*>(workspace);
+  const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, (int64_t)256), kDotBlocks));
+  if (dtype == TLGB_F64)
+    k_dot_part<double><<<nb, 256, 0, st>>>(static_cast<const double*>(a),
+                                           static_cast<const double*>(b), n, part);
+  else
+    k_dot_part<float><<<nb, 256, 0, st>>>(static_cast<const float*>(a),
+                                          static_cast<const float*>(b), n, part);
+  TLGB_LAUNCH_CHECK();
+  k_dot_final<<<1, 32, 0, st>>>(part, nb, out);
+  TLGB_LAUNCH_CHECK();
+  return TLGB_OK;
+}

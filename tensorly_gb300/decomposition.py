@@ -8,6 +8,7 @@ options raise ``NotImplementedError``; there is no CPU fallback.
 """
 
 import ctypes
+import math
 import warnings
 
 import numpy as np
@@ -1091,6 +1092,103 @@ class ConstrainedCP(DecompositionMixin):
         self.decomposition_ = cp
         self.errors_ = errors
         return self.decomposition_
+
+
+def _gemm(M, N, K, A, sam, sak, B, sbk, sbn):
+    """C (M x N) = sum_k A[m*sam + k*sak] B[k*sbk + n*sbn] by ``tlgb_gemm``."""
+    C = torch.empty((M, N), dtype=A.dtype, device=A.device)
+    _lib.check(_lib.lib().tlgb_gemm(dtype_code(A), M, N, K, A.data_ptr(), sam, sak, B.data_ptr(),
+                                    sbk, sbn, C.data_ptr(), stream_of(A)))
+    return C
+
+
+def _mat_nt(A, B):      # A B^T, A: M x K, B: N x K (row-major)
+    A, B = A.contiguous(), B.contiguous()
+    return _gemm(A.shape[0], B.shape[0], A.shape[1], A, A.shape[1], 1, B, 1, B.shape[1])
+
+
+def _mat_tn(A, B):      # A^T B, A: K x M, B: K x N
+    A, B = A.contiguous(), B.contiguous()
+    return _gemm(A.shape[1], B.shape[1], A.shape[0], A, 1, A.shape[1], B, B.shape[1], 1)
+
+
+def _mat_nn(A, B):      # A B, A: M x K, B: K x N
+    A, B = A.contiguous(), B.contiguous()
+    return _gemm(A.shape[0], B.shape[1], A.shape[1], A, A.shape[1], 1, B, B.shape[1], 1)
+
+
+def _mu_update(A, num, den, eps):
+    _lib.check(_lib.lib().tlgb_mu_update(dtype_code(A), A.data_ptr(), num.contiguous().data_ptr(),
+                                         den.contiguous().data_ptr(), A.numel(), float(eps),
+                                         stream_of(A)))
+
+
+def _dot(a, b):
+    lib = _lib.lib()
+    ws = workspace(lib.tlgb_dot_workspace_bytes(), a.device)
+    out = torch.empty(1, dtype=torch.float64, device=a.device)
+    a, b = a.contiguous(), b.contiguous()
+    _lib.check(lib.tlgb_dot(dtype_code(a), a.data_ptr(), b.data_ptr(), a.numel(), out.data_ptr(),
+                            ptr(ws), ws.numel(), stream_of(a)))
+    return out
+
+
+def non_negative_tucker(tensor, rank, n_iter_max=10, init="svd", tol=10e-5, random_state=None,
+                        verbose=False, return_errors=False, normalize_factors=False):
+    """Non-negative Tucker by multiplicative updates
+    (tensorly/decomposition/_tucker.py:348-454), same signature and returns.
+
+    The reference forms B = unfold(tucker_to_tensor(core, factors, skip=mode))^T
+    (prod(I_k) x R_mode); here the same products come from the TTM chain:
+    X_(n) B = [X x_{k!=n} U_k^T]_(n) G_(n)^T and B^T B = [G x_{k!=n} U_k^T U_k]_(n)
+    G_(n)^T, so nothing of the size of the tensor is formed besides the chain.
+    The error ||X - [[G; U]]|| comes from ||X||^2 - 2 <X x_k U_k^T, G> + <G,
+    G x_k U_k^T U_k>.  ``normalize_factors`` is not supported."""
+    from .base import unfold
+    from .cp_tensor import validate_tucker_rank
+    from .tenalg import multi_mode_dot
+    if normalize_factors:
+        raise NotImplementedError("non_negative_tucker with normalize_factors=True is not "
+                                  "supported by tensorly_gb300")
+    x, placement = to_device(tensor)
+    x = x.contiguous()
+    n_modes = x.ndim
+    rank = validate_tucker_rank(tuple(x.shape), rank=rank)
+    epsilon = 10e-12
+    core, factors = initialize_tucker(x, rank, range(n_modes), init=init,
+                                      random_state=random_state, non_negative=True)
+    core = core.to(x.dtype).contiguous().clone()
+    factors = [f.to(x.dtype).contiguous().clone() for f in factors]
+    norm_x2 = float(_dot(x, x).item())
+    rec_errors = []
+    for iteration in range(n_iter_max):
+        for mode in range(n_modes):
+            grams = [_mat_tn(f, f) for f in factors]
+            y = multi_mode_dot(x, factors, skip=mode, transpose=True)
+            num = _mat_nt(unfold(y, mode), unfold(core, mode))
+            w = multi_mode_dot(core, grams, skip=mode)
+            btb = _mat_nt(unfold(w, mode), unfold(core, mode))
+            den = _mat_nn(factors[mode], btb)
+            _mu_update(factors[mode], num, den, epsilon)
+        grams = [_mat_tn(f, f) for f in factors]
+        num_c = multi_mode_dot(x, factors, transpose=True).contiguous()
+        den_c = multi_mode_dot(core, grams).contiguous()
+        _mu_update(core, num_c, den_c, epsilon)
+        t2 = float(_dot(core, multi_mode_dot(core, grams)).item())
+        xt = float(_dot(num_c, core).item())
+        rec_error = math.sqrt(max(norm_x2 - 2.0 * xt + t2, 0.0) / norm_x2)
+        rec_errors.append(rec_error)
+        if iteration > 1 and verbose:
+            print(f"reconstruction error={rec_errors[-1]}, "
+                  f"variation={rec_errors[-2] - rec_errors[-1]}.")
+        if iteration > 1 and abs(rec_errors[-2] - rec_errors[-1]) < tol:
+            if verbose:
+                print(f"converged in {iteration} iterations.")
+            break
+    out = TuckerTensor((placement.back(core), [placement.back(f) for f in factors]))
+    if return_errors:
+        return out, rec_errors
+    return out
 
 
 class BatchedProblem:

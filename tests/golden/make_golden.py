@@ -345,6 +345,26 @@ def reference_runs():
                      "factors": [np.array(f) for f in cp.factors],
                      "errors": [float(e) for e in errs]})
 
+    # non-negative Tucker by multiplicative updates (tensorly/decomposition/_tucker.py:348-454)
+    from tensorly.decomposition import non_negative_tucker
+    nnt_variants = [
+        ("nnt_svd", dict(shape=(10, 9, 8), rank=3, seed=91),
+         dict(rank=[3, 4, 2], n_iter_max=15, init="svd", tol=1e-12)),
+        ("nnt_random", dict(shape=(9, 8, 7, 6), rank=2, seed=92),
+         dict(rank=[2, 3, 2, 3], n_iter_max=12, init="random", random_state=3, tol=1e-12)),
+        ("nnt_stop", dict(shape=(12, 10, 9), rank=2, seed=93),
+         dict(rank=[2, 2, 2], n_iter_max=100, init="svd", tol=1e-6)),
+        ("nnt_f32", dict(shape=(14, 12, 10), rank=3, seed=94, dtype=np.float32),
+         dict(rank=[3, 3, 3], n_iter_max=10, init="svd", tol=1e-12)),
+    ]
+    for name, g, kw in nnt_variants:
+        x = np.abs(small(g["seed"], g["shape"], g["rank"], g.get("dtype", np.float64)))
+        tt, errs = non_negative_tucker(x, return_errors=True, **copy.deepcopy(kw))
+        runs.append({"case": name, "gen": {"fn": "small", "abs": True, **g}, "checksum": cs(x),
+                     "kwargs": kw, "core": np.array(tt.core),
+                     "factors": [np.array(f) for f in tt.factors],
+                     "errors": [float(e) for e in errs]})
+
     # Tucker (HOOI) small cases
     tcases = [
         ("tucker_svd", dict(shape=(12, 10, 8), seed=31), dict(rank=[3, 4, 2], init="svd",

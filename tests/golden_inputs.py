@@ -21,6 +21,8 @@ def regenerate(run):
         x, _ = workloads.dense_cp_small()
     elif g["fn"] == "small":
         x = small_cp(g["seed"], g["shape"], g["rank"], g.get("dtype", np.float64))
+        if g.get("abs"):
+            x = np.abs(x)
     elif g["fn"] == "randn":
         x = np.random.RandomState(g["seed"]).randn(*g["shape"])
     else:
