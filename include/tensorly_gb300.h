@@ -535,6 +535,34 @@ int tlgb_dot(int dtype, const void* a, const void* b, int64_t n, double* out, vo
              size_t workspace_bytes, void* stream);
 
 /*
+ * hals_nnls: the reference's HALS non-negative least squares
+ * (tensorly/solvers/nnls.py:5-175) on the transposed layout: V (I x R, in/out)
+ * is its V^T, MtU (I x R) its UtM^T, UtU (R x R) its UtU (symmetrised from the
+ * upper triangle).  Up to n_iter_max iterations with its stop test (tol), an
+ * optional sparsity coefficient (NaN for none).  Synchronises `stream`
+ * between chunks of 100 iterations.  rank <= 160.
+ */
+int tlgb_hals_nnls_workspace_size(int dtype, int64_t I, int64_t R, size_t* bytes);
+int tlgb_hals_nnls(int dtype, const void* MtU, const void* UtU, void* V, int64_t I, int64_t R,
+                   int n_iter_max, double tol, double sparsity, void* workspace,
+                   size_t workspace_bytes, void* stream);
+
+/*
+ * fista_tucker_core: the reference's FISTA (tensorly/solvers/nnls.py:177-272,
+ * non_negative, no ridge) for a Tucker core: x (the core, shape[], in/out)
+ * minimises 1/2 <x, x x_k G_k> - <UtM, x> (+ sparsity sum x), gradient
+ * -UtM + x x_k grams[k] + sparsity, step lr, floor eps, the momentum of the
+ * reference, stop when |sum(x - x_new)| < tol * its first value.  No host
+ * round trip (a device stop flag).
+ */
+int tlgb_fista_tucker_core_workspace_size(int dtype, int ndim, const int64_t* shape,
+                                          size_t* bytes);
+int tlgb_fista_tucker_core(int dtype, const void* UtM, int ndim, const int64_t* shape,
+                           const void* const* grams, void* x, int n_iter_max, double sparsity,
+                           double lr, double tol, double eps, void* workspace,
+                           size_t workspace_bytes, void* stream);
+
+/*
  * unfold: out (shape[mode] x prod(other modes)) = the mode-`mode` unfolding of
  * the C-order tensor X, columns in the C order of the other modes
  * (tensorly/base.py:39-53, moveaxis(X, mode, 0).reshape(shape[mode], -1)).

@@ -31,7 +31,8 @@ __all__ = [
     "tucker_to_tensor", "validate_tucker_rank", "parafac_sweeps", "cp_to_unfolded",
     "cp_to_vec", "tucker_to_unfolded", "tucker_to_vec", "sample_khatri_rao",
     "randomised_parafac", "validate_constraints", "proximal_operator", "admm",
-    "initialize_constrained_parafac", "constrained_parafac", "non_negative_tucker",
+    "initialize_constrained_parafac", "constrained_parafac", "non_negative_tucker", "fista",
+    "non_negative_tucker_hals",
 ]
 
 
@@ -731,6 +732,85 @@ def admm(UtM, UtU, x, dual_var, n_iter_max=100, n_const=None, order=None, tol=1e
         if norm(dual_residual) < tol * norm(x) and norm(primal_residual) < tol * norm(dual_var):
             break
     return x, x_split, dual_var
+
+
+def fista(UtM, UtU, x=None, n_iter_max=100, non_negative=True, sparsity_coef=0, ridge_coef=0,
+          lr=None, tol=1e-8, epsilon=1e-8):
+    """tensorly/solvers/nnls.py:177-272."""
+    if sparsity_coef is None:
+        sparsity_coef = 0
+    if x is None:
+        x = np.zeros(UtM.shape, dtype=UtM.dtype)
+    if lr is None:
+        lr = 1 / (truncated_svd(UtU)[1][0] + 2 * ridge_coef)
+    momentum_old = 1.0
+    norm_0 = 0.0
+    x_update = np.copy(x)
+    for iteration in range(n_iter_max):
+        if isinstance(UtU, list):
+            x_gradient = (-UtM + multi_mode_dot(x_update, UtU, transpose=False) + sparsity_coef
+                          + 2 * ridge_coef * x_update)
+        else:
+            x_gradient = -UtM + np.dot(UtU, x_update) + sparsity_coef + 2 * ridge_coef * x_update
+        x_new = x_update - lr * x_gradient
+        if non_negative:
+            x_new = np.where(x_new < epsilon, epsilon, x_new)
+        momentum = (1 + math.sqrt(1 + 4 * momentum_old ** 2)) / 2
+        x_update = x_new + ((momentum_old - 1) / momentum) * (x_new - x)
+        momentum_old = momentum
+        nrm = abs(np.sum(x - x_new))
+        x = np.copy(x_new)
+        if iteration == 0:
+            norm_0 = nrm
+        if nrm < tol * norm_0:
+            break
+    return x
+
+
+def non_negative_tucker_hals(tensor, rank, n_iter_max=100, init="svd", svd="truncated_svd",
+                             tol=1e-8, sparsity_coefficients=None, core_sparsity_coefficient=None,
+                             random_state=None, return_errors=False, exact=False):
+    """tensorly/decomposition/_tucker.py:457-691 (algorithm='fista', no fixed
+    modes, not normalised)."""
+    rank = validate_tucker_rank(tensor.shape, rank=rank)
+    n_modes = tensor.ndim
+    if sparsity_coefficients is None or not isinstance(sparsity_coefficients, (list, tuple)):
+        sparsity_coefficients = [sparsity_coefficients] * n_modes
+    modes = list(range(n_modes))
+    nn_core, nn_factors = initialize_tucker(tensor, rank, modes, init=init, svd=svd,
+                                            random_state=random_state, non_negative=True)
+    nn_factors = list(nn_factors)
+    norm_tensor = norm(tensor)
+    rec_errors = []
+    for iteration in range(n_iter_max):
+        for mode in modes:
+            pseudo_inverse = list(nn_factors)
+            for i, factor in enumerate(nn_factors):
+                if i != mode:
+                    pseudo_inverse[i] = np.dot(np.conj(np.transpose(factor)), factor)
+            core_cross = multi_mode_dot(nn_core, pseudo_inverse, skip=mode)
+            UtU = np.dot(unfold(core_cross, mode), np.transpose(unfold(nn_core, mode)))
+            tensor_cross = multi_mode_dot(tensor, nn_factors, skip=mode, transpose=True)
+            MtU = np.dot(unfold(tensor_cross, mode), np.transpose(unfold(nn_core, mode)))
+            UtM = np.transpose(MtU)
+            nn_factor = hals_nnls(UtM, UtU, np.transpose(nn_factors[mode]), n_iter_max=100,
+                                  sparsity_coefficient=sparsity_coefficients[mode], exact=exact)
+            nn_factors[mode] = np.transpose(nn_factor)
+        pseudo_inverse[-1] = np.dot(np.transpose(nn_factors[-1]), nn_factors[-1])
+        core_estimation = multi_mode_dot(tensor, nn_factors, transpose=True)
+        learning_rate = 1
+        for MtM in pseudo_inverse:
+            learning_rate *= 1 / (truncated_svd(MtM)[1][0])
+        nn_core = fista(core_estimation, pseudo_inverse, x=nn_core, n_iter_max=n_iter_max,
+                        sparsity_coef=core_sparsity_coefficient, lr=learning_rate)
+        rec_error = norm(tensor - tucker_to_tensor((nn_core, nn_factors))) / norm_tensor
+        rec_errors.append(rec_error)
+        if iteration > 1:
+            if tol and abs(rec_errors[-2] - rec_errors[-1]) < tol:
+                break
+    if return_errors:
+        return (nn_core, nn_factors), rec_errors
+    return nn_core, nn_factors
 
 
 def initialize_constrained_parafac(tensor, rank, init="svd", svd="truncated_svd",

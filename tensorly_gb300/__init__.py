@@ -20,7 +20,7 @@ from .cp_tensor import (CPTensor, TuckerTensor, cp_norm, cp_normalize, cp_to_ten
 from .decomposition import (CP, CP_NN, CP_NN_HALS, ConstrainedCP, RandomizedCP, Tucker,
                             constrained_parafac, initialize_constrained_parafac, initialize_cp,
                             initialize_tucker, non_negative_parafac, non_negative_parafac_hals,
-                            non_negative_tucker,
+                            non_negative_tucker, non_negative_tucker_hals, hals_nnls,
                             parafac, parafac_batched, partial_tucker, proximal_operator,
                             randomised_parafac, sample_khatri_rao, tucker, validate_constraints)
 from .svd import svd_flip, svd_interface, truncated_svd

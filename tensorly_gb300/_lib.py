@@ -242,6 +242,18 @@ SIGNATURES = [
     ("tlgb_dot", ctypes.c_int,
      [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
       ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    ("tlgb_hals_nnls_workspace_size", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_int64, ctypes.c_int64, ctypes.POINTER(ctypes.c_size_t)]),
+    ("tlgb_hals_nnls", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+      ctypes.c_int64, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_void_p,
+      ctypes.c_size_t, ctypes.c_void_p]),
+    ("tlgb_fista_tucker_core_workspace_size", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_int, _c_i64p, ctypes.POINTER(ctypes.c_size_t)]),
+    ("tlgb_fista_tucker_core", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, _c_i64p, _c_vpp, ctypes.c_void_p,
+      ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+      ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     ("tlgb_unfold", ctypes.c_int,
      [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, _c_i64p, ctypes.c_int, ctypes.c_void_p,
       ctypes.c_void_p]),

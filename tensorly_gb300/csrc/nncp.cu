@@ -613,6 +613,51 @@ int mu_run(const T* X, const Shape& sh, T* const* factors, int64_t R, const int*
   return TLGB_OK;
 }
 
+// One hals_nnls call (tensorly/solvers/nnls.py:5-175) on the rows of A
+// (I x R, the reference's V transposed), given M (I x R, the reference's
+// UtM transposed) and the typed symmetric P (R x R, its UtU): chunks of
+// speculative iterations with the stop test applied afterwards and an exact
+// rerun when it stopped inside a chunk; a host read of the stop flag between
+// chunks.  state: e0 (double), then the stop and rerun ints.
+template <typename T>
+int hals_solve(const T* M, const T* Pt, T* A, int64_t I, int R, int n_inner, double tol_inner,
+               double sp, T* save, double* hpart, double* state, int chunk, size_t hals_smem,
+               int p_in_smem, const int* done, cudaStream_t st) {
+  int* stop = reinterpret_cast<int*>(state + 1);
+  int* rerun = stop + 1;
+  TLGB_CUDA_TRY(cudaMemsetAsync(state, 0, 2 * sizeof(double), st));
+  const int nb = (int)ceil_div(I, (int64_t)kHalsWarps);
+  const int64_t hrows = (int64_t)nb * kHalsWarps;
+  for (int t0 = 0; t0 < n_inner; t0 += chunk) {
+    const int n = std::min(chunk, n_inner - t0);
+    int rc = hals_launch_rows<T>(R, nb, hals_smem, p_in_smem, st, M, Pt, I, A, A, save, n,
+                                 nullptr, sp, hpart, done);
+    if (rc) return rc;
+    k_hals_scan<<<1, 1024, sizeof(double) * n, st>>>(hpart, hrows, t0, n, tol_inner, state, stop,
+                                                     rerun, done);
+    TLGB_LAUNCH_CHECK();
+    rc = hals_launch_rows<T>(R, nb, hals_smem, p_in_smem, st, M, Pt, I, save, A, nullptr, 0,
+                             rerun, sp, nullptr, done);
+    if (rc) return rc;
+    if (t0 + n < n_inner) {
+      int hs = 0;
+      TLGB_CUDA_TRY(cudaMemcpyAsync(&hs, stop, sizeof(int), cudaMemcpyDeviceToHost, st));
+      TLGB_CUDA_TRY(cudaStreamSynchronize(st));
+      if (hs) break;
+    }
+  }
+  return TLGB_OK;
+}
+
+// P symmetric in the factor type: the upper triangle of the input mirrored.
+template <typename T>
+__global__ void k_sym_typed(const T* __restrict__ in, int R, T* out) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < R * R; e += gridDim.x * blockDim.x) {
+    const int r = e / R, c = e - r * R;
+    out[e] = r <= c ? in[e] : in[c * R + r];
+  }
+}
+
 template <typename T>
 int hals_run(const T* X, const Shape& sh, T* const* factors, int64_t R, const int* free_modes,
              int n_free, int n_iter_max, double tol, int crit, const double* sparsity,
@@ -638,8 +683,6 @@ int hals_run(const T* X, const Shape& sh, T* const* factors, int64_t R, const in
   T* M = reinterpret_cast<T*>(base + L.M);
   double* hpart = reinterpret_cast<double*>(base + L.hpart);
   double* e0 = reinterpret_cast<double*>(base + L.hstate);
-  int* stop = reinterpret_cast<int*>(e0 + 1);
-  int* rerun = stop + 1;
   T* Pt = reinterpret_cast<T*>(base + L.Pt);
   T* save = reinterpret_cast<T*>(base + L.save);
   const int p_in_smem = ((size_t)R * R * sizeof(T) <= kHalsPSmemMax) ? 1 : 0;
@@ -681,30 +724,11 @@ int hals_run(const T* X, const Shape& sh, T* const* factors, int64_t R, const in
       k_sum_splits_to<T><<<(unsigned)std::min<int64_t>(ceil_div(IR, 256), 4096), 256, 0, st>>>(
           partial, plans[mode].splits, IR, M);
       TLGB_LAUNCH_CHECK();
-      TLGB_CUDA_TRY(cudaMemsetAsync(e0, 0, 2 * sizeof(double), st));
-      const int nb = (int)ceil_div(I, (int64_t)kHalsWarps);
-      const int64_t hrows = (int64_t)nb * kHalsWarps;
       // no sparsity coefficient (NaN): subtract 0, which leaves num unchanged
       const double sp = (sparsity && !std::isnan(sparsity[mode])) ? sparsity[mode] : 0.0;
-      T* A = factors[mode];
-      for (int t0 = 0; t0 < n_inner; t0 += chunk) {
-        const int n = std::min(chunk, n_inner - t0);
-        rc = hals_launch_rows<T>((int)R, nb, hals_smem, p_in_smem, st, M, Pt, I, A, A, save, n,
-                                 nullptr, sp, hpart, done);
-        if (rc) return rc;
-        k_hals_scan<<<1, 1024, sizeof(double) * n, st>>>(hpart, hrows, t0, n, tol_inner, e0, stop,
-                                                         rerun, done);
-        TLGB_LAUNCH_CHECK();
-        rc = hals_launch_rows<T>((int)R, nb, hals_smem, p_in_smem, st, M, Pt, I, save, A, nullptr,
-                                 0, rerun, sp, nullptr, done);
-        if (rc) return rc;
-        if (t0 + n < n_inner) {
-          int hs = 0;
-          TLGB_CUDA_TRY(cudaMemcpyAsync(&hs, stop, sizeof(int), cudaMemcpyDeviceToHost, st));
-          TLGB_CUDA_TRY(cudaStreamSynchronize(st));
-          if (hs) break;
-        }
-      }
+      rc = hals_solve<T>(M, Pt, factors[mode], I, (int)R, n_inner, tol_inner, sp, save, hpart,
+                         e0, chunk, hals_smem, p_in_smem, done, st);
+      if (rc) return rc;
       if (mode == last) {
         k_inner_part<T><<<kInnerBlocks, 256, 0, st>>>(M, factors[mode], IR, ipart, done);
         TLGB_LAUNCH_CHECK();
@@ -870,4 +894,82 @@ extern "C" int tlgb_nndsvd_columns(int dtype, const void* U, const void* S, cons
   }
   TLGB_LAUNCH_CHECK();
   return TLGB_OK;
+}
+
+// ---- standalone hals_nnls ----------------------------------------------------
+
+namespace {
+
+struct HalsLayout {
+  size_t done, state, Pt, save, hpart, bytes;
+};
+
+HalsLayout hals_layout(int dtype, int64_t I, int64_t R) {
+  HalsLayout L{};
+  const size_t esz = dtype == TLGB_F64 ? 8 : 4;
+  const int64_t hrows = ceil_div(I, (int64_t)kHalsWarps) * kHalsWarps;
+  size_t off = 0;
+  auto take = [&](size_t b) { off = align_up(off, 256); const size_t o = off; off += b; return o; };
+  L.done = take(sizeof(int));
+  L.state = take(2 * sizeof(double));
+  L.Pt = take(esz * (size_t)R * R);
+  L.save = take(esz * (size_t)I * R);
+  L.hpart = take(sizeof(double) * (size_t)(hrows * hals_chunk(hrows)));
+  L.bytes = align_up(off, 256);
+  return L;
+}
+
+template <typename T>
+int hals_nnls_run(const T* MtU, const T* UtU, T* V, int64_t I, int64_t R, int n_iter_max,
+                  double tol, double sparsity, void* ws, cudaStream_t st) {
+  const HalsLayout L = hals_layout(TypeCode<T>::value, I, R);
+  char* base = static_cast<char*>(ws);
+  int* done = reinterpret_cast<int*>(base + L.done);
+  double* state = reinterpret_cast<double*>(base + L.state);
+  T* Pt = reinterpret_cast<T*>(base + L.Pt);
+  T* save = reinterpret_cast<T*>(base + L.save);
+  double* hpart = reinterpret_cast<double*>(base + L.hpart);
+  TLGB_CUDA_TRY(cudaMemsetAsync(done, 0, sizeof(int), st));
+  const int RR = (int)(R * R);
+  k_sym_typed<T><<<(RR + 255) / 256, 256, 0, st>>>(UtU, (int)R, Pt);
+  TLGB_LAUNCH_CHECK();
+  const int p_in_smem = ((size_t)R * R * sizeof(T) <= kHalsPSmemMax) ? 1 : 0;
+  const size_t hals_smem = (p_in_smem ? (size_t)R * R * sizeof(T) : 0) +
+                           (size_t)kHalsWarps * R * sizeof(T);
+  const int chunk = hals_chunk(ceil_div(I, (int64_t)kHalsWarps) * kHalsWarps);
+  const double sp = std::isnan(sparsity) ? 0.0 : sparsity;
+  return hals_solve<T>(MtU, Pt, V, I, (int)R, n_iter_max, tol, sp, save, hpart, state, chunk,
+                       hals_smem, p_in_smem, done, st);
+}
+
+}  // namespace
+
+extern "C" int tlgb_hals_nnls_workspace_size(int dtype, int64_t I, int64_t R, size_t* bytes) {
+  clear_error();
+  TLGB_CHECK_ARG(dtype == TLGB_F32 || dtype == TLGB_F64, "hals_nnls: dtype must be f32 or f64");
+  TLGB_CHECK_ARG(I >= 1 && R >= 1 && R <= kMaxAlsRank && bytes, "hals_nnls: bad argument");
+  *bytes = hals_layout(dtype, I, R).bytes;
+  return TLGB_OK;
+}
+
+extern "C" int tlgb_hals_nnls(int dtype, const void* MtU, const void* UtU, void* V, int64_t I,
+                              int64_t R, int n_iter_max, double tol, double sparsity,
+                              void* workspace, size_t workspace_bytes, void* stream) {
+  clear_error();
+  TLGB_CHECK_ARG(dtype == TLGB_F32 || dtype == TLGB_F64, "hals_nnls: dtype must be f32 or f64");
+  TLGB_CHECK_ARG(MtU && UtU && V, "hals_nnls: null pointer");
+  TLGB_CHECK_ARG(I >= 1 && R >= 1 && R <= kMaxAlsRank, "hals_nnls: rank must be in [1, 160]");
+  TLGB_CHECK_ARG(n_iter_max >= 0 && tol >= 0.0, "hals_nnls: bad n_iter_max or tol");
+  if (!workspace || workspace_bytes < hals_layout(dtype, I, R).bytes)
+    return set_error(TLGB_EWORKSPACE, "hals_nnls: workspace too small");
+  int rc = als_prepare(dtype);
+  if (rc) return rc;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (dtype == TLGB_F64)
+    return hals_nnls_run<double>(static_cast<const double*>(MtU), static_cast<const double*>(UtU),
+                                 static_cast<double*>(V), I, R, n_iter_max, tol, sparsity,
+                                 workspace, st);
+  return hals_nnls_run<float>(static_cast<const float*>(MtU), static_cast<const float*>(UtU),
+                              static_cast<float*>(V), I, R, n_iter_max, tol, sparsity, workspace,
+                              st);
 }

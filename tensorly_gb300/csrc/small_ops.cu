@@ -89,10 +89,136 @@ __global__ void k_dot_final(const double* part, int nb, double* out) {
   }
 }
 
+// One FISTA iteration on the core (tensorly/solvers/nnls.py:177-272, the
+// list-of-Grams branch, non_negative, no ridge):
+//   x_new = max-floor(x_upd - lr ((-UtM + g) + sparsity), eps)   (g = x_upd x_k G_k)
+//   x_upd = x_new + coef (x_new - x);  x = x_new
+// and per-CTA sums of (x - x_new) for the stop test.  Returns at once once
+// the stop flag is set.
+struct FistaState {
+  double norm0;
+  int stop;
+};
+
+template <typename T>
+__global__ void k_fista_step(const T* __restrict__ UtM, const T* __restrict__ g, T* __restrict__ x,
+                             T* __restrict__ xu, int64_t n, T lr, T sparsity, T coef, T eps,
+                             const FistaState* fs, double* part) {
+  if (fs->stop) return;
+  __shared__ double red[8];
+  double s = 0.0;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const T grad = ((-UtM[e] + g[e]) + sparsity);
+    T xn = xu[e] - lr * grad;
+    xn = xn < eps ? eps : xn;
+    const T xo = x[e];
+    xu[e] = xn + coef * (xn - xo);
+    x[e] = xn;
+    s += (double)(xo - xn);
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < 8; ++w) t += red[w];
+    part[blockIdx.x] = t;
+  }
+}
+
+__global__ void k_fista_check(const double* part, int nb, int it, double tol, FistaState* fs) {
+  if (fs->stop || threadIdx.x != 0) return;
+  double t = 0.0;
+  for (int b = 0; b < nb; ++b) t += part[b];
+  const double nrm = fabs(t);
+  if (it == 0) fs->norm0 = nrm;
+  if (nrm < tol * fs->norm0) fs->stop = 1;
+}
+
 }  // namespace
 }  // namespace tlgb
 
 using namespace tlgb;
+
+extern "C" int tlgb_mode_dot(int dtype, const void* X, int ndim, const int64_t* shape,
+                             const void* U, int64_t J, int transpose, int mode, void* out,
+                             void* stream);
+
+static size_t fista_ws_bytes(int dtype, int64_t n) {
+  const size_t esz = dtype == TLGB_F64 ? 8 : 4;
+  return align_up(3 * esz * (size_t)n, 256) + align_up(sizeof(double) * kDotBlocks, 256) +
+         align_up(sizeof(FistaState), 256);
+}
+
+extern "C" int tlgb_fista_tucker_core_workspace_size(int dtype, int ndim, const int64_t* shape,
+                                                     size_t* bytes) {
+  clear_error();
+  TLGB_CHECK_ARG(dtype == TLGB_F32 || dtype == TLGB_F64, "fista: dtype must be f32 or f64");
+  TLGB_CHECK_ARG(ndim >= 1 && ndim <= kMaxModes && shape && bytes, "fista: bad argument");
+  int64_t n = 1;
+  for (int k = 0; k < ndim; ++k) n *= shape[k];
+  *bytes = fista_ws_bytes(dtype, n);
+  return TLGB_OK;
+}
+
+extern "C" int tlgb_fista_tucker_core(int dtype, const void* UtM, int ndim, const int64_t* shape,
+                                      const void* const* grams, void* x, int n_iter_max,
+                                      double sparsity, double lr, double tol, double eps,
+                                      void* workspace, size_t workspace_bytes, void* stream) {
+  clear_error();
+  TLGB_CHECK_ARG(dtype == TLGB_F32 || dtype == TLGB_F64, "fista: dtype must be f32 or f64");
+  TLGB_CHECK_ARG(ndim >= 1 && ndim <= kMaxModes && shape && UtM && grams && x,
+                 "fista: bad argument");
+  int64_t n = 1;
+  for (int k = 0; k < ndim; ++k) {
+    TLGB_CHECK_ARG(shape[k] >= 1 && grams[k] != nullptr, "fista: bad shape or Gram");
+    n *= shape[k];
+  }
+  if (!workspace || workspace_bytes < fista_ws_bytes(dtype, n))
+    return set_error(TLGB_EWORKSPACE, "fista: workspace too small");
+  const size_t esz = dtype == TLGB_F64 ? 8 : 4;
+  char* base = static_cast<char*>(workspace);
+  char* xu = base;
+  char* b0 = base + esz * n;
+  char* b1 = base + 2 * esz * n;
+  double* part = reinterpret_cast<double*>(base + align_up(3 * esz * (size_t)n, 256));
+  FistaState* fs = reinterpret_cast<FistaState*>(
+      base + align_up(3 * esz * (size_t)n, 256) + align_up(sizeof(double) * kDotBlocks, 256));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  TLGB_CUDA_TRY(cudaMemcpyAsync(xu, x, esz * n, cudaMemcpyDeviceToDevice, st));
+  TLGB_CUDA_TRY(cudaMemsetAsync(fs, 0, sizeof(FistaState), st));
+  const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, (int64_t)256), kDotBlocks));
+  double m_old = 1.0;
+  for (int it = 0; it < n_iter_max; ++it) {
+    // g = x_upd x_0 G_0 x_1 G_1 ... (ping-pong between b0 and b1)
+    const void* src = xu;
+    char* dst = b0;
+    for (int k = 0; k < ndim; ++k) {
+      int rc = tlgb_mode_dot(dtype, src, ndim, shape, grams[k], shape[k], 0, k, dst, stream);
+      if (rc) return rc;
+      src = dst;
+      dst = dst == b0 ? b1 : b0;
+    }
+    const double m = (1.0 + std::sqrt(1.0 + 4.0 * m_old * m_old)) / 2.0;
+    const double coef = (m_old - 1.0) / m;
+    m_old = m;
+    if (dtype == TLGB_F64)
+      k_fista_step<double><<<nb, 256, 0, st>>>(
+          static_cast<const double*>(UtM), static_cast<const double*>(src),
+          static_cast<double*>(x), reinterpret_cast<double*>(xu), n, lr, sparsity, coef, eps, fs,
+          part);
+    else
+      k_fista_step<float><<<nb, 256, 0, st>>>(
+          static_cast<const float*>(UtM), static_cast<const float*>(src), static_cast<float*>(x),
+          reinterpret_cast<float*>(xu), n, (float)lr, (float)sparsity, (float)coef, (float)eps, fs,
+          part);
+    TLGB_LAUNCH_CHECK();
+    k_fista_check<<<1, 32, 0, st>>>(part, nb, it, tol, fs);
+    TLGB_LAUNCH_CHECK();
+  }
+  return TLGB_OK;
+}
 
 extern "C" int tlgb_gemm(int dtype, int64_t M, int64_t N, int64_t K, const void* A, int64_t sam,
                          int64_t sak, const void* B, int64_t sbk, int64_t sbn, void* C,

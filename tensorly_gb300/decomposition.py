@@ -1191,6 +1191,150 @@ def non_negative_tucker(tensor, rank, n_iter_max=10, init="svd", tol=10e-5, rand
     return out
 
 
+def hals_nnls(UtM, UtU, V=None, n_iter_max=500, tol=1e-8, sparsity_coefficient=None,
+              ridge_coefficient=None, nonzero_rows=False, exact=False, epsilon=0.0,
+              callback=None):
+    """HALS non-negative least squares (tensorly/solvers/nnls.py:5-175), same
+    signature and return (V, R x n), by ``tlgb_hals_nnls``: one warp per
+    column of V, the reference's stop test applied after each chunk of
+    iterations.  A starting V is required; ridge, nonzero_rows, epsilon and
+    callback are not supported."""
+    from .base import unfold
+    if V is None:
+        raise NotImplementedError("hals_nnls without a starting V is not supported by "
+                                  "tensorly_gb300")
+    if ridge_coefficient is not None or nonzero_rows or epsilon != 0.0 or callback is not None:
+        raise NotImplementedError("hals_nnls with ridge_coefficient, nonzero_rows, epsilon or "
+                                  "callback is not supported by tensorly_gb300")
+    utm, pl = to_device(UtM)
+    utu = to_device(UtU)[0].to(utm.dtype).contiguous()
+    v = to_device(V)[0].to(utm.dtype)
+    if exact:
+        n_iter_max, tol = 50000, 1e-16
+    rank, n = int(utm.shape[0]), int(utm.shape[1])
+    mtu = unfold(utm, 1)                      # n x rank: the transposed layout
+    vt = unfold(v, 1).contiguous()
+    _hals_nnls_t(mtu, utu, vt, int(n_iter_max), float(tol), sparsity_coefficient)
+    return pl.back(unfold(vt, 1))
+
+
+def _hals_nnls_t(mtu, utu, vt, n_iter_max, tol, sparsity):
+    lib = _lib.lib()
+    n, rank = int(vt.shape[0]), int(vt.shape[1])
+    nbytes = ctypes.c_size_t(0)
+    _lib.check(lib.tlgb_hals_nnls_workspace_size(dtype_code(vt), n, rank, ctypes.byref(nbytes)))
+    ws = workspace(nbytes.value, vt.device)
+    sp = float("nan") if sparsity is None else float(sparsity)
+    _lib.check(lib.tlgb_hals_nnls(dtype_code(vt), mtu.contiguous().data_ptr(),
+                                  utu.contiguous().data_ptr(), vt.data_ptr(), n, rank,
+                                  int(n_iter_max), float(tol), sp, ptr(ws), ws.numel(),
+                                  stream_of(vt)))
+
+
+def _largest_eig(a):
+    """Largest eigenvalue of a symmetric matrix (the first singular value of a
+    Gram, tl.truncated_svd(MtM)[1][0]) by the library's eigensolver."""
+    lib = _lib.lib()
+    n = int(a.shape[0])
+    nbytes = ctypes.c_size_t(0)
+    _lib.check(lib.tlgb_sym_eig_workspace_size(dtype_code(a), n, 1, ctypes.byref(nbytes)))
+    ws = workspace(nbytes.value, a.device)
+    u = torch.empty((n, 1), dtype=a.dtype, device=a.device)
+    ev = torch.empty(1, dtype=a.dtype, device=a.device)
+    _lib.check(lib.tlgb_sym_eig(dtype_code(a), a.contiguous().data_ptr(), n, 1, u.data_ptr(),
+                                ev.data_ptr(), 0, ptr(ws), ws.numel(), stream_of(a)))
+    return float(ev.item())
+
+
+def non_negative_tucker_hals(tensor, rank, n_iter_max=100, init="svd", svd="truncated_svd",
+                             tol=1e-8, sparsity_coefficients=None, core_sparsity_coefficient=None,
+                             fixed_modes=None, random_state=None, verbose=False,
+                             normalize_factors=False, return_errors=False, exact=False,
+                             algorithm="fista"):
+    """Non-negative Tucker by HALS (tensorly/decomposition/_tucker.py:457-691),
+    same signature and returns, for algorithm='fista'.
+
+    Per mode the factor update is the reference's hals_nnls call on
+    UtU = [G x_{k!=n} U_k^T U_k]_(n) G_(n)^T and MtU = [X x_{k!=n} U_k^T]_(n) G_(n)^T
+    (``tlgb_hals_nnls``); the core update is the reference's FISTA with the
+    step prod_k 1 / lambda_max(U_k^T U_k) (``tlgb_fista_tucker_core``, the
+    eigenvalues from the library's eigensolver).  The error comes from the
+    norm expansion.  'active_set', fixed modes and normalize_factors are not
+    supported."""
+    from collections.abc import Iterable
+    from .base import unfold
+    from .cp_tensor import validate_tucker_rank
+    from .tenalg import multi_mode_dot
+    if algorithm != "fista":
+        raise NotImplementedError("non_negative_tucker_hals supports algorithm='fista' only")
+    if normalize_factors:
+        raise NotImplementedError("non_negative_tucker_hals with normalize_factors=True is not "
+                                  "supported by tensorly_gb300")
+    x, placement = to_device(tensor)
+    x = x.contiguous()
+    n_modes = x.ndim
+    rank = validate_tucker_rank(tuple(x.shape), rank=rank)
+    if sparsity_coefficients is None or not isinstance(sparsity_coefficients, Iterable):
+        sparsity_coefficients = [sparsity_coefficients] * n_modes
+    fixed = [] if fixed_modes is None else list(fixed_modes)
+    if n_modes - 1 in fixed:
+        warnings.warn("You asked for fixing the last mode, which is not supported. The last mode "
+                      "will not be fixed. Consider using tl.moveaxis() to permute it to another "
+                      "position and keep it fixed there.")
+        fixed.remove(n_modes - 1)
+    if fixed:
+        raise NotImplementedError("non_negative_tucker_hals with fixed modes is not supported by "
+                                  "tensorly_gb300")
+    n_inner, tol_inner = (50000, 1e-16) if exact else (100, 1e-8)
+    core, factors = initialize_tucker(x, rank, range(n_modes), init=init, svd=svd,
+                                      random_state=random_state, non_negative=True)
+    core = core.to(x.dtype).contiguous().clone()
+    factors = [f.to(x.dtype).contiguous().clone() for f in factors]
+    norm_x2 = float(_dot(x, x).item())
+    lib = _lib.lib()
+    cshape = (ctypes.c_int64 * n_modes)(*core.shape)
+    nbytes = ctypes.c_size_t(0)
+    _lib.check(lib.tlgb_fista_tucker_core_workspace_size(dtype_code(x), n_modes, cshape,
+                                                         ctypes.byref(nbytes)))
+    fws = workspace(nbytes.value, x.device)
+    csp = 0.0 if core_sparsity_coefficient is None else float(core_sparsity_coefficient)
+    rec_errors = []
+    for iteration in range(n_iter_max):
+        for mode in range(n_modes):
+            grams = [_mat_tn(f, f) for f in factors]
+            core_cross = multi_mode_dot(core, grams, skip=mode)
+            utu = _mat_nt(unfold(core_cross, mode), unfold(core, mode))
+            y = multi_mode_dot(x, factors, skip=mode, transpose=True)
+            mtu = _mat_nt(unfold(y, mode), unfold(core, mode))
+            _hals_nnls_t(mtu, utu, factors[mode], n_inner, tol_inner,
+                         sparsity_coefficients[mode])
+        grams = [_mat_tn(f, f).contiguous() for f in factors]
+        core_est = multi_mode_dot(x, factors, transpose=True).contiguous()
+        lr = 1.0
+        for g in grams:
+            lr *= 1.0 / _largest_eig(g)
+        _lib.check(lib.tlgb_fista_tucker_core(
+            dtype_code(x), core_est.data_ptr(), n_modes, cshape,
+            _lib.ptr_array([g.data_ptr() for g in grams]), core.data_ptr(), int(n_iter_max), csp,
+            lr, 1e-8, 1e-8, ptr(fws), fws.numel(), stream_of(x)))
+        t2 = float(_dot(core, multi_mode_dot(core, grams)).item())
+        xt = float(_dot(core_est, core).item())
+        rec_error = math.sqrt(max(norm_x2 - 2.0 * xt + t2, 0.0) / norm_x2)
+        rec_errors.append(rec_error)
+        if iteration > 1:
+            if verbose:
+                print(f"reconstruction error={rec_errors[-1]}, "
+                      f"variation={rec_errors[-2] - rec_errors[-1]}.")
+            if tol and abs(rec_errors[-2] - rec_errors[-1]) < tol:
+                if verbose:
+                    print(f"converged in {iteration} iterations.")
+                break
+    out = TuckerTensor((placement.back(core), [placement.back(f) for f in factors]))
+    if return_errors:
+        return out, rec_errors
+    return out
+
+
 class BatchedProblem:
     """Many small 3-way f32 tensors packed for ``tlgb_cp_als_batched``.
 

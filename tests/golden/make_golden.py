@@ -365,6 +365,27 @@ def reference_runs():
                      "factors": [np.array(f) for f in tt.factors],
                      "errors": [float(e) for e in errs]})
 
+    # non-negative Tucker by HALS + FISTA (tensorly/decomposition/_tucker.py:457-691)
+    from tensorly.decomposition import non_negative_tucker_hals
+    nnth_variants = [
+        ("nnth_svd", dict(shape=(10, 9, 8), rank=3, seed=95),
+         dict(rank=[3, 4, 2], n_iter_max=10, init="svd", tol=1e-12)),
+        ("nnth_random", dict(shape=(9, 8, 7, 6), rank=2, seed=96),
+         dict(rank=[2, 3, 2, 3], n_iter_max=8, init="random", random_state=4, tol=1e-12)),
+        ("nnth_sparse", dict(shape=(10, 9, 8), rank=3, seed=97),
+         dict(rank=[3, 3, 3], n_iter_max=8, init="svd", tol=1e-12,
+              sparsity_coefficients=[0.01, None, 0.02], core_sparsity_coefficient=0.001)),
+        ("nnth_f32", dict(shape=(12, 10, 9), rank=3, seed=98, dtype=np.float32),
+         dict(rank=[3, 3, 3], n_iter_max=8, init="svd", tol=1e-12)),
+    ]
+    for name, g, kw in nnth_variants:
+        x = np.abs(small(g["seed"], g["shape"], g["rank"], g.get("dtype", np.float64)))
+        tt, errs = non_negative_tucker_hals(x, return_errors=True, **copy.deepcopy(kw))
+        runs.append({"case": name, "gen": {"fn": "small", "abs": True, **g}, "checksum": cs(x),
+                     "kwargs": kw, "core": np.array(tt.core),
+                     "factors": [np.array(f) for f in tt.factors],
+                     "errors": [float(e) for e in errs]})
+
     # Tucker (HOOI) small cases
     tcases = [
         ("tucker_svd", dict(shape=(12, 10, 8), seed=31), dict(rank=[3, 4, 2], init="svd",

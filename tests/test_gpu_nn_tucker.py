@@ -76,3 +76,44 @@ def test_small_ops_match_numpy(gb300, dtype):
                                rtol=tol)
     np.testing.assert_allclose(d._dot(ta, ta).item(), float((a.astype(np.float64) ** 2).sum()),
                                rtol=1e-12 if dtype == np.float64 else 1e-6)
+
+
+@pytest.mark.parametrize("case", ["nnth_svd", "nnth_random", "nnth_sparse", "nnth_f32"])
+def test_non_negative_tucker_hals_matches_reference(gb300, golden, case):
+    """HALS factor updates and the FISTA core update; f64 1e-8 on the error
+    list and 1e-6 on core and factors (the HALS rows move P A incrementally),
+    f32 1e-3 and 1e-2."""
+    run = golden["runs"][case]
+    x = regenerate(run)
+    kw = dict(run["kwargs"])
+    rank = kw.pop("rank")
+    (core, factors), errs = gb300.non_negative_tucker_hals(torch.as_tensor(x, device="cuda"),
+                                                           rank, return_errors=True, **kw)
+    f32 = x.dtype == np.float32
+    assert len(errs) == len(run["errors"])
+    np.testing.assert_allclose(errs, run["errors"], rtol=1e-3 if f32 else 1e-8)
+    tol = 1e-2 if f32 else 1e-6
+    np.testing.assert_allclose(host(core), run["core"], rtol=tol,
+                               atol=tol * np.abs(run["core"]).max())
+    for a, b in zip(factors, run["factors"]):
+        np.testing.assert_allclose(host(a), b, rtol=tol, atol=tol * np.abs(b).max())
+
+
+@pytest.mark.parametrize("exact", [False, True])
+def test_hals_nnls_matches_oracle(gb300, exact):
+    rs = np.random.RandomState(5)
+    U = np.abs(rs.randn(40, 6))
+    M = np.abs(rs.randn(40, 30))
+    UtM, UtU = U.T @ M, U.T @ U
+    V0 = np.abs(rs.randn(6, 30))
+    ref = oracle.hals_nnls(UtM, UtU, V0.copy(), n_iter_max=200, sparsity_coefficient=0.01,
+                           exact=exact)
+    out = gb300.hals_nnls(UtM, UtU, V0.copy(), n_iter_max=200, sparsity_coefficient=0.01,
+                          exact=exact)
+    assert isinstance(out, np.ndarray) and out.shape == (6, 30)
+    np.testing.assert_allclose(out, ref, rtol=1e-9, atol=1e-9 * np.abs(ref).max())
+    with pytest.raises(NotImplementedError):
+        gb300.hals_nnls(UtM, UtU)
+    x = torch.rand(8, 7, 6, device="cuda", dtype=torch.float64)
+    with pytest.raises(NotImplementedError):
+        gb300.non_negative_tucker_hals(x, [2, 2, 2], algorithm="active_set")

@@ -188,6 +188,21 @@ def test_oracle_non_negative_tucker_matches_reference(golden, case):
         np.testing.assert_allclose(a, b, rtol=tol, atol=tol * np.abs(b).max())
 
 
+@pytest.mark.parametrize("case", ["nnth_svd", "nnth_random", "nnth_sparse", "nnth_f32"])
+def test_oracle_non_negative_tucker_hals_matches_reference(golden, case):
+    run = golden["runs"][case]
+    x = regenerate(run)
+    kw = dict(run["kwargs"])
+    rank = kw.pop("rank")
+    (core, factors), errs = oracle.non_negative_tucker_hals(x, rank, return_errors=True, **kw)
+    tol = 1e-5 if x.dtype == np.float32 else 1e-10
+    assert len(errs) == len(run["errors"])
+    np.testing.assert_allclose(errs, run["errors"], rtol=tol, atol=tol * 1e-2)
+    np.testing.assert_allclose(core, run["core"], rtol=tol, atol=tol * np.abs(run["core"]).max())
+    for a, b in zip(factors, run["factors"]):
+        np.testing.assert_allclose(a, b, rtol=tol, atol=tol * np.abs(b).max())
+
+
 @pytest.mark.parametrize("case", ["tucker_svd", "tucker_random", "tucker_4way"])
 def test_oracle_tucker_matches_reference(golden, case):
     run = golden["runs"][case]
