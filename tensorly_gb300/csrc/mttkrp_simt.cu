@@ -32,7 +32,7 @@ template <> struct TileCfg<float> { static constexpr int BM = 128, TM = 8, BK = 
 template <> struct TileCfg<double> { static constexpr int BM = 64, TM = 4, BK = 16; };
 
 template <typename T, int BN>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 3)
 mttkrp_split_kernel(const MttkrpArgs<T> a) {
   if (a.skip_flag && *a.skip_flag) return;
   constexpr int BM = TileCfg<T>::BM, TM = TileCfg<T>::TM, BK = TileCfg<T>::BK;
@@ -57,15 +57,24 @@ mttkrp_split_kernel(const MttkrpArgs<T> a) {
   const int64_t t_begin = (int64_t)split * a.steps_per_split;
   const int64_t t_end = min(t_begin + a.steps_per_split, a.total_steps);
 
-  T acc[TM][TN], P[TM][TN];
+  T acc[TM][TN];
 #pragma unroll
   for (int i = 0; i < TM; ++i)
 #pragma unroll
-    for (int j = 0; j < TN; ++j) { acc[i][j] = T(0); P[i][j] = T(0); }
+    for (int j = 0; j < TN; ++j) acc[i][j] = T(0);
 
   // register staging for the next step's tiles
   T xr[XV][VEC];
   T fr[FV][VEC];
+  // The factor tile is staged as F_inner[c, r] * s(o, r), s(o, r) = w_r *
+  // prod_k A_k(i_k(o), r) (the Khatri-Rao row of the outer modes), so one
+  // accumulator set carries the whole contraction.  This thread stages the
+  // columns r0 + (tid % (BN / VEC)) * VEC + j of every B row; sv holds their
+  // scales for the staged step's o (recomputed when o changes).
+  static_assert(kThreads % (BN / VEC) == 0, "staging columns must be fixed per thread");
+  const int64_t rcol = r0 + (tid % (BN / VEC)) * VEC;
+  T sv[VEC];
+  int64_t s_o = -1;
 
   auto outer_offset = [&](int64_t o) -> int64_t {
     int64_t off = 0;
@@ -78,10 +87,31 @@ mttkrp_split_kernel(const MttkrpArgs<T> a) {
     return off;
   };
 
+  auto load_scales = [&](int64_t o) {
+    int64_t idx[kMaxModes];
+    int64_t oo = o;
+    for (int k = a.n_outer - 1; k >= 0; --k) {
+      idx[k] = oo % a.outer_dim[k];
+      oo /= a.outer_dim[k];
+    }
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) {
+      const int64_t r = rcol + j;
+      T v = T(0);
+      if (r < a.R) {
+        v = a.weights ? a.weights[r] : T(1);
+        for (int k = 0; k < a.n_outer; ++k) v *= a.outer_f[k][idx[k] * a.R + r];
+      }
+      sv[j] = v;
+    }
+    s_o = o;
+  };
+
   auto load_step = [&](int64_t t) {
     const int64_t o = t / a.KC;
     const int64_t c0 = (t % a.KC) * BK;
     const T* Xo = a.X + outer_offset(o);
+    if (o != s_o) load_scales(o);
 #pragma unroll
     for (int v = 0; v < XV; ++v) {
       const int e = v * kThreads + tid;
@@ -158,7 +188,7 @@ mttkrp_split_kernel(const MttkrpArgs<T> a) {
         const int c = e / (BN / VEC);
         const int r = (e % (BN / VEC)) * VEC;
 #pragma unroll
-        for (int j = 0; j < VEC; ++j) B[c * PADN + r + j] = fr[v][j];
+        for (int j = 0; j < VEC; ++j) B[c * PADN + r + j] = fr[v][j] * sv[j];
       }
     }
   };
@@ -179,30 +209,6 @@ mttkrp_split_kernel(const MttkrpArgs<T> a) {
 #pragma unroll
     for (int j = 0; j < TN; ++j) ncol[j] = ln * TN + j;
   }
-
-  auto finish_o = [&](int64_t o) {
-    // s(o, r) = w_r * prod_k A_k(i_k, r) for this thread's columns
-    int64_t idx[kMaxModes];
-    int64_t oo = o;
-    for (int k = a.n_outer - 1; k >= 0; --k) {
-      idx[k] = oo % a.outer_dim[k];
-      oo /= a.outer_dim[k];
-    }
-#pragma unroll
-    for (int j = 0; j < TN; ++j) {
-      const int64_t r = r0 + ncol[j];
-      T s = T(0);
-      if (r < a.R) {
-        s = a.weights ? a.weights[r] : T(1);
-        for (int k = 0; k < a.n_outer; ++k) s *= a.outer_f[k][idx[k] * a.R + r];
-      }
-#pragma unroll
-      for (int i = 0; i < TM; ++i) {
-        acc[i][j] = fma(s, P[i][j], acc[i][j]);
-        P[i][j] = T(0);
-      }
-    }
-  };
 
   if (t_begin < t_end) {
     load_step(t_begin);
@@ -239,10 +245,8 @@ mttkrp_split_kernel(const MttkrpArgs<T> a) {
 #pragma unroll
         for (int i = 0; i < TM; ++i)
 #pragma unroll
-          for (int j = 0; j < TN; ++j) P[i][j] = fma(av[i], bv[j], P[i][j]);
+          for (int j = 0; j < TN; ++j) acc[i][j] = fma(av[i], bv[j], acc[i][j]);
       }
-      const int64_t o = t / a.KC;
-      if ((t % a.KC) == a.KC - 1 || !has_next) finish_o(o);
       if (has_next) store_step(buf ^ 1);
       __syncthreads();
       buf ^= 1;
