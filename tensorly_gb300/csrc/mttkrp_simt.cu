@@ -220,7 +220,9 @@ mttkrp_split_kernel(const MttkrpArgs<T> a) {
       if (has_next) load_step(t + 1);
       const T* A = As + buf * BK * PADM;
       const T* B = Bs + buf * BK * PADN;
-#pragma unroll
+      // unrolled by 8: the fully unrolled step (BK x TM x TN FMAs) outgrows
+      // the instruction cache
+#pragma unroll 8
       for (int k = 0; k < BK; ++k) {
         T av[TM], bv[TN];
 #pragma unroll
