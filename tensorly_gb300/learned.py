@@ -16,7 +16,7 @@ saddle at a zero output.
 ``warm_start`` falls back, per tensor, to TensorLy's ``init='svd'`` factors
 (tensorly/decomposition/_cp.py:70-96) when the network's model explains
 almost nothing of the tensor (or, with ``probe`` > 0, when the SVD start is
-ahead after that many plain ALS sweeps).  Plain ALS convergence judges the network: ``evaluate`` counts
+ahead after that many plain ALS sweeps).  Plain ALS convergence measures the network: ``evaluate`` counts
 the sweeps and times the whole path to the reference's stop test from each
 start.
 """
@@ -233,7 +233,7 @@ def warm_start(net, X, omega, probe=0, max_err=0.99):
     tensors whose predicted model explains almost nothing (relative error at
     its best scale >= ``max_err``, read from the loss the prediction already
     computes); the SVD start is computed for those tensors only.
-    ``probe`` > 0: plain ALS judges instead: ``probe`` sweeps run from both
+    ``probe`` > 0: plain ALS decides instead: ``probe`` sweeps run from both
     starts and the one with the lower error afterwards is kept, in its state
     after the probe.  Returns (factors, used_svd, probe sweeps taken)."""
     feats, xnorm = sketch(X, omega)

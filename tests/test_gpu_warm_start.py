@@ -197,7 +197,7 @@ def test_warm_start_gain_over_svd_start(ws, gen, trained):
     print("falling back for every tensor (256 tensors): svd %.1f, warm %.1f mean sweeps"
           % (resc["sweeps_svd"].mean(), resc["sweeps_warm"].mean()))
     np.testing.assert_array_equal(resc["sweeps_warm"], resc["sweeps_svd"])
-    print("with 5 ALS probe sweeps as the judge (256 tensors): svd %.1f, warm %.1f mean sweeps, "
+    print("with 5 ALS probe sweeps choosing the start (256 tensors): svd %.1f, warm %.1f mean sweeps, "
           "network kept for %.1f %%" % (res5["sweeps_svd"].mean(), res5["sweeps_warm"].mean(),
                                          100 * (1 - res5["used_svd"].mean())))
     assert (res5["sweeps_warm"] >= 5).all()
