@@ -386,6 +386,32 @@ def reference_runs():
                      "factors": [np.array(f) for f in tt.factors],
                      "errors": [float(e) for e in errs]})
 
+    # PARAFAC2 (tensorly/decomposition/_parafac2.py:399-707), ragged slices
+    from tensorly.decomposition import parafac2
+    p2_variants = [
+        ("p2_random", dict(seed=101, rows=[8, 9, 10, 11, 12], cols=6),
+         dict(rank=3, n_iter_max=12, random_state=1)),
+        ("p2_svd", dict(seed=102, rows=[7, 9, 8, 10], cols=5),
+         dict(rank=2, n_iter_max=10, init="svd")),
+        ("p2_nols", dict(seed=103, rows=[9, 9, 10, 8, 11, 12], cols=7),
+         dict(rank=3, n_iter_max=15, random_state=2, linesearch=False)),
+        ("p2_normalize", dict(seed=104, rows=[8, 10, 9], cols=6),
+         dict(rank=2, n_iter_max=8, random_state=3, normalize_factors=True)),
+        ("p2_f32", dict(seed=105, rows=[10, 11, 12, 9], cols=6, dtype=np.float32),
+         dict(rank=3, n_iter_max=10, random_state=4)),
+    ]
+    for name, g, kw in p2_variants:
+        rsl = np.random.RandomState(g["seed"])
+        xs = [rsl.rand(r, g["cols"]).astype(g.get("dtype", np.float64)) for r in g["rows"]]
+        ck = [float(sum(np.asarray(t, np.float64).sum() for t in xs)),
+              float(np.sqrt(sum((np.asarray(t, np.float64) ** 2).sum() for t in xs)))]
+        out, errs = parafac2(xs, return_errors=True, **copy.deepcopy(kw))
+        w, fs, ps = out
+        runs.append({"case": name, "gen": {"fn": "slices", **g}, "checksum": ck, "kwargs": kw,
+                     "weights": np.array(w), "factors": [np.array(f) for f in fs],
+                     "projections": [np.array(p) for p in ps],
+                     "errors": [float(e) for e in errs]})
+
     # Tucker (HOOI) small cases
     tcases = [
         ("tucker_svd", dict(shape=(12, 10, 8), seed=31), dict(rank=[3, 4, 2], init="svd",

@@ -25,6 +25,13 @@ def regenerate(run):
             x = np.abs(x)
     elif g["fn"] == "randn":
         x = np.random.RandomState(g["seed"]).randn(*g["shape"])
+    elif g["fn"] == "slices":             # PARAFAC2 input: uniform slices of ragged height
+        rs = np.random.RandomState(g["seed"])
+        xs = [rs.rand(r, g["cols"]).astype(g.get("dtype", np.float64)) for r in g["rows"]]
+        cs = [float(sum(np.asarray(t, np.float64).sum() for t in xs)),
+              float(np.sqrt(sum((np.asarray(t, np.float64) ** 2).sum() for t in xs)))]
+        np.testing.assert_allclose(cs, run["checksum"], rtol=1e-12, atol=1e-12)
+        return xs
     else:
         raise KeyError(g["fn"])
     cs = [float(np.asarray(x, np.float64).sum()), float(np.linalg.norm(np.asarray(x, np.float64)))]

@@ -203,6 +203,22 @@ def test_oracle_non_negative_tucker_hals_matches_reference(golden, case):
         np.testing.assert_allclose(a, b, rtol=tol, atol=tol * np.abs(b).max())
 
 
+@pytest.mark.parametrize("case", ["p2_random", "p2_svd", "p2_nols", "p2_normalize", "p2_f32"])
+def test_oracle_parafac2_matches_reference(golden, case):
+    from oracle import parafac2_oracle
+    run = golden["runs"][case]
+    xs = regenerate(run)
+    kw = dict(run["kwargs"])
+    rank = kw.pop("rank")
+    (w, f, p), errs = parafac2_oracle.parafac2(xs, rank, return_errors=True, **kw)
+    tol = 1e-4 if xs[0].dtype == np.float32 else 1e-9
+    assert len(errs) == len(run["errors"])
+    np.testing.assert_allclose(errs, run["errors"], rtol=tol, atol=tol * 1e-2)
+    np.testing.assert_allclose(w, run["weights"], rtol=tol, atol=tol)
+    for a, b in zip(list(f) + list(p), run["factors"] + run["projections"]):
+        np.testing.assert_allclose(a, b, rtol=tol, atol=tol * np.abs(b).max())
+
+
 @pytest.mark.parametrize("case", ["tucker_svd", "tucker_random", "tucker_4way"])
 def test_oracle_tucker_matches_reference(golden, case):
     run = golden["runs"][case]
