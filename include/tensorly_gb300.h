@@ -562,6 +562,23 @@ int tlgb_fista_tucker_core(int dtype, const void* UtM, int ndim, const int64_t* 
                            double lr, double tol, double eps, void* workspace,
                            size_t workspace_bytes, void* stream);
 
+/* inv_sqrt: out = 1 / sqrt(x) over n values (PARAFAC2 polar factors). */
+int tlgb_inv_sqrt(int dtype, const void* x, int64_t n, void* out, void* stream);
+
+/* lerp: out = x + (y - x) * s over n values (PARAFAC2 line search). */
+int tlgb_lerp(int dtype, const void* x, const void* y, int64_t n, double s, void* out,
+              void* stream);
+
+/*
+ * qr: Q (m x n, row-major) of the Householder QR of A (m x n, m >= n,
+ * n <= 256) in LAPACK's conventions (dgeqr2 reflectors, dorg2r's explicit Q),
+ * so its column signs are NumPy's linalg.qr.  One CTA; for the small tall
+ * matrices of tensorly/random/base.py:18-61 (random_parafac2's projections).
+ */
+int tlgb_qr_workspace_size(int dtype, int64_t m, int64_t n, size_t* bytes);
+int tlgb_qr(int dtype, const void* A, int64_t m, int64_t n, void* Q, void* workspace,
+            size_t workspace_bytes, void* stream);
+
 /*
  * unfold: out (shape[mode] x prod(other modes)) = the mode-`mode` unfolding of
  * the C-order tensor X, columns in the C order of the other modes

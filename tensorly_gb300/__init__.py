@@ -24,6 +24,8 @@ from .decomposition import (CP, CP_NN, CP_NN_HALS, ConstrainedCP, RandomizedCP, 
                             parafac, parafac_batched, partial_tucker, proximal_operator,
                             randomised_parafac, sample_khatri_rao, tucker, validate_constraints)
 from .svd import svd_flip, svd_interface, truncated_svd
+from .parafac2 import (Parafac2, Parafac2Tensor, parafac2, parafac2_to_slices,
+                       parafac2_to_tensor, random_parafac2)
 from .random import check_random_state, random_cp
 from .tenalg import khatri_rao, mode_dot, multi_mode_dot, unfolding_dot_khatri_rao
 

@@ -254,6 +254,16 @@ SIGNATURES = [
      [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, _c_i64p, _c_vpp, ctypes.c_void_p,
       ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
       ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    ("tlgb_inv_sqrt", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p]),
+    ("tlgb_lerp", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_double,
+      ctypes.c_void_p, ctypes.c_void_p]),
+    ("tlgb_qr_workspace_size", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_int64, ctypes.c_int64, ctypes.POINTER(ctypes.c_size_t)]),
+    ("tlgb_qr", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p,
+      ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     ("tlgb_unfold", ctypes.c_int,
      [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, _c_i64p, ctypes.c_int, ctypes.c_void_p,
       ctypes.c_void_p]),

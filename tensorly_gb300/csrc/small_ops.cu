@@ -136,10 +136,177 @@ __global__ void k_fista_check(const double* part, int nb, int it, double tol, Fi
   if (nrm < tol * fs->norm0) fs->stop = 1;
 }
 
+// out = x + (y - x) * s (the line search extrapolation of
+// tensorly/decomposition/_parafac2.py:261-264).
+template <typename T>
+__global__ void k_lerp(const T* __restrict__ x, const T* __restrict__ y, int64_t n, T s,
+                       T* __restrict__ out) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x)
+    out[e] = x[e] + (y[e] - x[e]) * s;
+}
+
+// out = 1 / sqrt(x) (inverse square roots of eigenvalues, PARAFAC2 projections).
+template <typename T>
+__global__ void k_inv_sqrt(const T* __restrict__ x, int64_t n, T* __restrict__ out) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x)
+    out[e] = (T)1 / sqrt(x[e]);
+}
+
+constexpr int kQrThreads = 256;
+
+// Householder QR of an m x n row-major matrix A (m >= n) with LAPACK's
+// conventions (dgeqr2 / dlarfg: beta = -sign(alpha) sqrt(alpha^2 + |x|^2),
+// tau = (beta - alpha) / beta, v = x / (alpha - beta) with v_0 = 1; a zero
+// column below the diagonal gives tau = 0), then the explicit Q (m x n) =
+// H_0 H_1 ... H_{n-1} [I; 0] as dorg2r forms it.  One CTA; a warp per column
+// for the reflector applications.  W (m x n) and V (m x n) are scratch.
+template <typename T>
+__global__ void __launch_bounds__(kQrThreads)
+k_qr_householder(const T* __restrict__ A, int64_t m, int n, T* W, T* V, T* Q) {
+  __shared__ double red[kQrThreads / 32];
+  __shared__ double taus[256];
+  __shared__ T sh_scale, sh_beta;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = kQrThreads / 32;
+  for (int64_t e = tid; e < m * n; e += kQrThreads) W[e] = A[e];
+  __syncthreads();
+  for (int k = 0; k < n; ++k) {
+    double s = 0.0;
+    for (int64_t i = k + 1 + tid; i < m; i += kQrThreads) {
+      const double w = (double)W[i * n + k];
+      s += w * w;
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) red[warp] = s;
+    __syncthreads();
+    if (tid == 0) {
+      double t = 0.0;
+      for (int w = 0; w < nw; ++w) t += red[w];
+      const double alpha = (double)W[(int64_t)k * n + k];
+      const double xnorm = sqrt(t);
+      if (xnorm == 0.0) {
+        taus[k] = 0.0;
+        sh_beta = (T)alpha;
+        sh_scale = (T)0;
+      } else {
+        const double beta = -copysign(sqrt(alpha * alpha + t), alpha);
+        taus[k] = (beta - alpha) / beta;
+        sh_beta = (T)beta;
+        sh_scale = (T)(1.0 / (alpha - beta));
+      }
+    }
+    __syncthreads();
+    for (int64_t i = k + 1 + tid; i < m; i += kQrThreads) V[i * n + k] = W[i * n + k] * sh_scale;
+    if (tid == 0) {
+      V[(int64_t)k * n + k] = (T)1;
+      W[(int64_t)k * n + k] = sh_beta;
+    }
+    __syncthreads();
+    const T tau = (T)taus[k];
+    if (tau != (T)0) {
+      for (int j = k + 1 + warp; j < n; j += nw) {      // W[k:, j] -= tau v (v^T W[k:, j])
+        T d = (T)0;
+        for (int64_t i = k + lane; i < m; i += 32) d += V[i * n + k] * W[i * n + j];
+        for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+        const T f = tau * d;
+        for (int64_t i = k + lane; i < m; i += 32) W[i * n + j] -= f * V[i * n + k];
+      }
+    }
+    __syncthreads();
+  }
+  for (int64_t e = tid; e < m * n; e += kQrThreads) {
+    const int64_t i = e / n;
+    const int j = (int)(e - i * n);
+    Q[e] = (i == j) ? (T)1 : (T)0;
+  }
+  __syncthreads();
+  for (int k = n - 1; k >= 0; --k) {
+    const T tau = (T)taus[k];
+    if (tau != (T)0) {
+      for (int j = k + warp; j < n; j += nw) {          // Q[k:, j] -= tau v (v^T Q[k:, j])
+        T d = (T)0;
+        for (int64_t i = k + lane; i < m; i += 32) d += V[i * n + k] * Q[i * n + j];
+        for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+        const T f = tau * d;
+        for (int64_t i = k + lane; i < m; i += 32) Q[i * n + j] -= f * V[i * n + k];
+      }
+    }
+    __syncthreads();
+  }
+}
+
 }  // namespace
 }  // namespace tlgb
 
 using namespace tlgb;
+
+extern "C" int tlgb_lerp(int dtype, const void* x, const void* y, int64_t n, double s, void* out,
+                         void* stream) {
+  clear_error();
+  TLGB_CHECK_ARG(dtype == TLGB_F32 || dtype == TLGB_F64, "lerp: dtype must be f32 or f64");
+  TLGB_CHECK_ARG(x && y && out && n >= 0, "lerp: bad argument");
+  if (n == 0) return TLGB_OK;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const unsigned nb = (unsigned)std::min<int64_t>(ceil_div(n, (int64_t)256), 152 * 8);
+  if (dtype == TLGB_F64)
+    k_lerp<double><<<nb, 256, 0, st>>>(static_cast<const double*>(x),
+                                       static_cast<const double*>(y), n, s,
+                                       static_cast<double*>(out));
+  else
+    k_lerp<float><<<nb, 256, 0, st>>>(static_cast<const float*>(x), static_cast<const float*>(y),
+                                      n, (float)s, static_cast<float*>(out));
+  TLGB_LAUNCH_CHECK();
+  return TLGB_OK;
+}
+
+extern "C" int tlgb_inv_sqrt(int dtype, const void* x, int64_t n, void* out, void* stream) {
+  clear_error();
+  TLGB_CHECK_ARG(dtype == TLGB_F32 || dtype == TLGB_F64, "inv_sqrt: dtype must be f32 or f64");
+  TLGB_CHECK_ARG(x && out && n >= 0, "inv_sqrt: bad argument");
+  if (n == 0) return TLGB_OK;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const unsigned nb = (unsigned)std::min<int64_t>(ceil_div(n, (int64_t)256), 152 * 8);
+  if (dtype == TLGB_F64)
+    k_inv_sqrt<double><<<nb, 256, 0, st>>>(static_cast<const double*>(x), n,
+                                           static_cast<double*>(out));
+  else
+    k_inv_sqrt<float><<<nb, 256, 0, st>>>(static_cast<const float*>(x), n,
+                                          static_cast<float*>(out));
+  TLGB_LAUNCH_CHECK();
+  return TLGB_OK;
+}
+
+extern "C" int tlgb_qr_workspace_size(int dtype, int64_t m, int64_t n, size_t* bytes) {
+  clear_error();
+  TLGB_CHECK_ARG(dtype == TLGB_F32 || dtype == TLGB_F64, "qr: dtype must be f32 or f64");
+  TLGB_CHECK_ARG(m >= n && n >= 1 && n <= 256 && bytes, "qr: need m >= n, 1 <= n <= 256");
+  *bytes = align_up(2 * (size_t)m * n * (dtype == TLGB_F64 ? 8 : 4), 256);
+  return TLGB_OK;
+}
+
+extern "C" int tlgb_qr(int dtype, const void* A, int64_t m, int64_t n, void* Q, void* workspace,
+                       size_t workspace_bytes, void* stream) {
+  clear_error();
+  TLGB_CHECK_ARG(dtype == TLGB_F32 || dtype == TLGB_F64, "qr: dtype must be f32 or f64");
+  TLGB_CHECK_ARG(A && Q, "qr: null pointer");
+  TLGB_CHECK_ARG(m >= n && n >= 1 && n <= 256, "qr: need m >= n, 1 <= n <= 256");
+  const size_t esz = dtype == TLGB_F64 ? 8 : 4;
+  if (!workspace || workspace_bytes < 2 * (size_t)m * n * esz)
+    return set_error(TLGB_EWORKSPACE, "qr: workspace too small");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  char* w = static_cast<char*>(workspace);
+  if (dtype == TLGB_F64)
+    k_qr_householder<double><<<1, kQrThreads, 0, st>>>(
+        static_cast<const double*>(A), m, (int)n, reinterpret_cast<double*>(w),
+        reinterpret_cast<double*>(w + (size_t)m * n * esz), static_cast<double*>(Q));
+  else
+    k_qr_householder<float><<<1, kQrThreads, 0, st>>>(
+        static_cast<const float*>(A), m, (int)n, reinterpret_cast<float*>(w),
+        reinterpret_cast<float*>(w + (size_t)m * n * esz), static_cast<float*>(Q));
+  TLGB_LAUNCH_CHECK();
+  return TLGB_OK;
+}
 
 extern "C" int tlgb_mode_dot(int dtype, const void* X, int ndim, const int64_t* shape,
                              const void* U, int64_t J, int transpose, int mode, void* out,
