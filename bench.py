@@ -767,7 +767,8 @@ def run_tucker(args):
     print(json.dumps(line), flush=True)
 
 
-NNCP_METRIC = "non-negative CP iterations/s at 512^3 f32 rank 64 (multiplicative updates)"
+def nncp_metric(n, r):
+    return f"non-negative CP iterations/s at {n}^3 f32 rank {r} (multiplicative updates)"
 
 
 def _nncp_cpu_sample(x, init, n_iter):
@@ -796,7 +797,7 @@ def run_nncp(args):
                 f"{n_iter} iterations from a fixed random non-negative init, tol=0")
     if args.impl == "reference":
         v, dt = _nncp_cpu_sample(x_np, init_np, 2)
-        line = {"metric": NNCP_METRIC, "value": v, "unit": "iterations/s", "n_gpus": args.gpus,
+        line = {"metric": nncp_metric(args.size, args.rank), "value": v, "unit": "iterations/s", "n_gpus": args.gpus,
                 "steps": 1, "warmup": 0, "ms_per_step": 1000.0 * dt / 2, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "impl": "reference",
@@ -847,7 +848,7 @@ def run_nncp(args):
         v, dt = _nncp_cpu_sample(x_np, init_np, 2)
         cpu = {"value": v, "unit": "iterations/s", "cores": os.cpu_count(), "kind": "port",
                "sample": f"2 iterations of the NumPy restatement ({dt:.1f} s)"}
-    line = {"metric": NNCP_METRIC, "value": n_iter / (ms / 1000.0), "unit": "iterations/s",
+    line = {"metric": nncp_metric(args.size, args.rank), "value": n_iter / (ms / 1000.0), "unit": "iterations/s",
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "config": {"workload": workload, "l2": "512 MiB input > L2"},
