@@ -30,7 +30,7 @@ __all__ = [
     "make_svd_non_negative", "hals_nnls", "non_negative_parafac_hals",
     "tucker_to_tensor", "validate_tucker_rank", "parafac_sweeps", "cp_to_unfolded",
     "cp_to_vec", "tucker_to_unfolded", "tucker_to_vec", "sample_khatri_rao",
-    "randomised_parafac", "validate_constraints", "proximal_operator", "admm",
+    "randomised_parafac", "sparsify_tensor", "error_calc_ext", "validate_constraints", "proximal_operator", "admm",
     "initialize_constrained_parafac", "constrained_parafac", "non_negative_tucker", "fista",
     "non_negative_tucker_hals",
 ]
@@ -912,24 +912,66 @@ def error_calc(tensor, norm_tensor, weights, factors, mttkrp):
     return np.sqrt(np.abs(norm_tensor ** 2 + factors_norm ** 2 - 2 * iprod))
 
 
+def sparsify_tensor(tensor, card):
+    """tensorly/decomposition/_cp.py:140-159: keep the ``card`` entries of
+    largest magnitude."""
+    if card >= np.prod(tensor.shape):
+        return tensor
+    bound = np.sort(np.abs(tensor), axis=None)[-card]
+    return np.where(np.abs(tensor) < bound, np.zeros(tensor.shape, dtype=tensor.dtype), tensor)
+
+
+def error_calc_ext(tensor, norm_tensor, weights, factors, sparsity, mask, mttkrp=None):
+    """tensorly/decomposition/_cp.py:162-227 (all branches): returns
+    (unnormalised error, tensor, norm_tensor); with a mask the tensor's
+    missing entries are refilled from the model."""
+    if (mask is not None) or (mttkrp is None):
+        low_rank_component = cp_to_tensor((weights, factors))
+        if mask is not None:
+            tensor = tensor * mask + low_rank_component * (1 - mask)
+            norm_tensor = norm(tensor)
+        if sparsity:
+            sparse_component = sparsify_tensor(tensor - low_rank_component, sparsity)
+        else:
+            sparse_component = 0.0
+        unnorm = norm(tensor - low_rank_component - sparse_component)
+    else:
+        if sparsity:
+            low_rank_component = cp_to_tensor((weights, factors))
+            sparse_component = sparsify_tensor(tensor - low_rank_component, sparsity)
+            unnorm = norm(tensor - low_rank_component - sparse_component)
+        else:
+            unnorm = error_calc(tensor, norm_tensor, weights, factors, mttkrp)
+    return unnorm, tensor, norm_tensor
+
+
 def parafac(tensor, rank, n_iter_max=100, init="svd", svd="truncated_svd",
             normalize_factors=False, orthogonalise=False, tol=1e-8, random_state=None,
             verbose=0, return_errors=False, sparsity=None, l2_reg=0, mask=None,
             cvg_criterion="abs_rec_error", fixed_modes=None, svd_mask_repeats=5,
             linesearch=False, callback=None):
-    """tensorly/decomposition/_cp.py:230-543 (dense ALS; no sparsity, mask,
-    linesearch or orthogonalisation).
+    """tensorly/decomposition/_cp.py:230-543.
 
     Per sweep and mode (``:407-428``): Hadamard of the other factors' Grams
     plus ``l2_reg*I``, scaled by ``w w^T``; MTTKRP; ``solve(V^H, M^T)^T``
     (LAPACK gesv).  Error from the last mode's MTTKRP (``:437-440``), stop on
     ``|e[-2]-e[-1]| < tol`` (``:505-524``), then optional normalisation
-    (``:529-530``).  Returns ``((weights, factors), errors)`` or
-    ``(weights, factors)``.
+    (``:529-530``).  Also the orthogonalisation (QR of the factors in the
+    first sweeps, ``:392-397``), the line search (``:398-401``, ``:430-478``),
+    the sparse component (``:366-370``, ``:532-536``) and the mask (missing
+    entries refilled from the model, ``:441-446``); a masked 'svd' start is
+    not restated.  Returns ``((weights, factors), errors)`` or
+    ``(weights, factors)``; with sparsity ``((weights, factors), sparse)``
+    in place of the CP pair.
     """
-    if sparsity or mask is not None or linesearch or orthogonalise:
-        raise NotImplementedError("oracle restates the dense unmasked ALS only")
+    if mask is not None and isinstance(init, str) and init == "svd":
+        raise NotImplementedError("oracle restates masked runs from 'random' or given starts")
+    if callback is not None and sparsity:
+        raise NotImplementedError("oracle restates callbacks without sparsity")
     rank = validate_cp_rank(tensor.shape, rank=rank)
+    if orthogonalise and not isinstance(orthogonalise, int):
+        orthogonalise = n_iter_max
+    acc_pow, acc_fail, max_fail = 2.0, 0, 4
     weights, factors = initialize_cp(tensor, rank, init=init, svd=svd,
                                      random_state=random_state,
                                      normalize_factors=normalize_factors)
@@ -946,11 +988,22 @@ def parafac(tensor, rank, n_iter_max=100, init="svd", svd="truncated_svd",
         warnings.warn("You asked for fixing the last mode, which is not supported.")
         fixed_modes.remove(tensor.ndim - 1)
     modes_list = [m for m in range(tensor.ndim) if m not in fixed_modes]
+    if sparsity:
+        if isinstance(sparsity, float):
+            sparsity = int(sparsity * np.prod(tensor.shape))
+        else:
+            sparsity = int(sparsity)
     if callback is not None:
         unnorm = error_calc_full(tensor, weights, factors)
         callback((weights, factors), unnorm / norm_tensor)
     mttkrp = None
+    unnorm = None
     for iteration in range(n_iter_max):
+        if orthogonalise and iteration <= orthogonalise:
+            factors = [np.linalg.qr(f)[0] if min(f.shape) >= rank else f for f in factors]
+        if linesearch and iteration % 2 == 0:
+            factors_last = [np.copy(f) for f in factors]
+            weights_last = np.copy(weights)
         for mode in modes_list:
             V = np.ones((rank, rank), dtype=tensor.dtype)
             for i, f in enumerate(factors):
@@ -961,8 +1014,32 @@ def parafac(tensor, rank, n_iter_max=100, init="svd", svd="truncated_svd",
             mttkrp = unfolding_dot_khatri_rao(tensor, (weights, factors), mode)
             factors[mode] = np.transpose(
                 np.linalg.solve(np.conj(np.transpose(V)), np.transpose(mttkrp)))
-        if tol or return_errors:
-            unnorm = error_calc(tensor, norm_tensor, weights, factors, mttkrp)
+        line_iter = bool(linesearch and iteration % 2 == 0 and iteration > 5)
+        if (tol or return_errors) and not line_iter:
+            unnorm, tensor, norm_tensor = error_calc_ext(tensor, norm_tensor, weights, factors,
+                                                         sparsity, mask, mttkrp)
+        elif mask is not None:
+            tensor = tensor * mask + cp_to_tensor((weights, factors), mask=1 - mask)
+        if line_iter:
+            jump = iteration ** (1.0 / acc_pow)
+            new_weights = weights_last + (weights - weights_last) * jump
+            new_factors = [factors_last[ii] + (factors[ii] - factors_last[ii]) * jump
+                           for ii in range(tensor.ndim)]
+            new_err, new_tensor, new_norm = error_calc_ext(tensor, norm_tensor, new_weights,
+                                                           new_factors, sparsity, mask)
+            if (new_err / new_norm) < rec_errors[-1]:
+                factors, weights = new_factors, new_weights
+                tensor, norm_tensor = new_tensor, new_norm
+                unnorm = new_err
+                acc_fail = 0
+            else:
+                unnorm, tensor, norm_tensor = error_calc_ext(tensor, norm_tensor, weights,
+                                                             factors, sparsity, mask, mttkrp)
+                acc_fail += 1
+                if acc_fail == max_fail:
+                    acc_pow += 1.0
+                    acc_fail = 0
+        if (tol or return_errors) and not line_iter:
             rec_errors.append(unnorm / norm_tensor)
         if callback is not None:
             if callback((weights, factors), rec_errors[-1]) is True:
@@ -979,9 +1056,13 @@ def parafac(tensor, rank, n_iter_max=100, init="svd", svd="truncated_svd",
                 break
         if normalize_factors:
             weights, factors = cp_normalize((weights, factors))
+            factors = list(factors)
+    cp = (weights, factors)
+    if sparsity:
+        cp = (cp, sparsify_tensor(tensor - cp_to_tensor(cp), sparsity))
     if return_errors:
-        return (weights, factors), rec_errors
-    return (weights, factors)
+        return cp, rec_errors
+    return cp
 
 
 def error_calc_full(tensor, weights, factors):

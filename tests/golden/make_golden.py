@@ -412,6 +412,41 @@ def reference_runs():
                      "projections": [np.array(p) for p in ps],
                      "errors": [float(e) for e in errs]})
 
+    # parafac branches the GPU path does not take yet: line search,
+    # orthogonalisation, sparse component, mask (tensorly/decomposition/_cp.py:230-543)
+    cp_branches = [
+        ("cp_linesearch", dict(shape=(12, 11, 10), rank=3, seed=111),
+         dict(init="random", random_state=11, linesearch=True, n_iter_max=30, tol=1e-10), None),
+        ("cp_orth", dict(shape=(10, 9, 8), rank=3, seed=112),
+         dict(init="svd", orthogonalise=5, n_iter_max=15, tol=1e-10), None),
+        ("cp_sparsity", dict(shape=(10, 9, 8), rank=3, seed=113),
+         dict(init="svd", sparsity=0.05, n_iter_max=10, tol=1e-10), None),
+        ("cp_mask", dict(shape=(10, 9, 8), rank=3, seed=114),
+         dict(init="random", random_state=12, n_iter_max=10, tol=1e-10), 0.8),
+        ("cp_mask_linesearch", dict(shape=(10, 9, 8), rank=2, seed=115),
+         dict(init="random", random_state=13, n_iter_max=12, tol=1e-10, linesearch=True), 0.7),
+    ]
+    for name, g, kw, keep in cp_branches:
+        x = small(g["seed"], g["shape"], g["rank"], g.get("dtype", np.float64))
+        kwr = copy.deepcopy(kw)
+        mask = None
+        if keep is not None:
+            mask = (np.random.RandomState(g["seed"] + 1000).rand(*g["shape"]) < keep).astype(
+                x.dtype)
+            kwr["mask"] = mask
+        out, errs = parafac(x, g["rank"], return_errors=True, **kwr)
+        rec = {"case": name, "gen": {"fn": "small", **g}, "checksum": cs(x),
+               "kwargs": {"rank": g["rank"], **kw}, "mask_keep": keep,
+               "errors": [float(e) for e in errs]}
+        if kw.get("sparsity"):
+            (w, f), sparse = out
+            rec["sparse"] = np.array(sparse)
+        else:
+            w, f = out
+        rec["weights"] = np.array(w)
+        rec["factors"] = [np.array(m) for m in f]
+        runs.append(rec)
+
     # Tucker (HOOI) small cases
     tcases = [
         ("tucker_svd", dict(shape=(12, 10, 8), seed=31), dict(rank=[3, 4, 2], init="svd",

@@ -219,6 +219,30 @@ def test_oracle_parafac2_matches_reference(golden, case):
         np.testing.assert_allclose(a, b, rtol=tol, atol=tol * np.abs(b).max())
 
 
+@pytest.mark.parametrize("case", ["cp_linesearch", "cp_orth", "cp_sparsity", "cp_mask",
+                                  "cp_mask_linesearch"])
+def test_oracle_parafac_branches_match_reference(golden, case):
+    run = golden["runs"][case]
+    x = regenerate(run)
+    kw = dict(run["kwargs"])
+    rank = kw.pop("rank")
+    if run["mask_keep"] is not None:
+        shape = run["gen"]["shape"]
+        kw["mask"] = (np.random.RandomState(run["gen"]["seed"] + 1000).rand(*shape)
+                      < run["mask_keep"]).astype(x.dtype)
+    out, errs = oracle.parafac(x, rank, return_errors=True, **kw)
+    if "sparse" in run:
+        (w, f), sparse = out
+        np.testing.assert_allclose(sparse, run["sparse"], rtol=1e-10, atol=1e-12)
+    else:
+        w, f = out
+    assert len(errs) == len(run["errors"])
+    np.testing.assert_allclose(errs, run["errors"], rtol=1e-10, atol=1e-12)
+    np.testing.assert_allclose(w, run["weights"], rtol=1e-10, atol=1e-12)
+    for a, b in zip(f, run["factors"]):
+        np.testing.assert_allclose(a, b, rtol=1e-9, atol=1e-9 * np.abs(b).max())
+
+
 @pytest.mark.parametrize("case", ["tucker_svd", "tucker_random", "tucker_4way"])
 def test_oracle_tucker_matches_reference(golden, case):
     run = golden["runs"][case]
