@@ -18,6 +18,8 @@ Outputs (committed, small, platform independent):
   cp_to_vec / tucker_to_tensor / tucker_to_unfolded / tucker_to_vec, recorded
   from their tests in tensorly/tests/test_cp_tensor.py and
   test_tucker_tensor.py (CP and Tucker arguments stored as plain tuples).
+* ``proximal_kats.pkl``: the same for the proximal operators called by
+  tensorly/tenalg/tests/test_proximal.py.
 * ``reference_runs.pkl``: reference ``parafac`` / ``non_negative_parafac`` /
   ``tucker`` / ``svd_interface``
   outputs on seeded inputs (the tensors are regenerated from their seeds by
@@ -151,6 +153,46 @@ def record_reconstruction():
             np.random.seed(0)
             records.append({"fn": "__test__", "name": f"{mname}.{tname}"})
             getattr(mod, tname)()
+    return records
+
+
+def record_proximal():
+    """Every proximal-operator call of the reference's tests
+    (tensorly/tenalg/tests/test_proximal.py), with its output, and the
+    assertions with their known answers."""
+    import tensorly as tl
+    tl.set_backend("numpy")
+    records = []
+    names = ("svd_thresholding", "smoothness_prox", "soft_thresholding", "procrustes",
+             "hard_thresholding", "soft_sparsity_prox", "simplex_prox",
+             "normalized_sparsity_prox", "monotonicity_prox", "unimodality_prox", "l2_prox",
+             "l2_square_prox")
+
+    def wrap(name, fn):
+        def recorder(*args, **kwargs):
+            rec = {"fn": name, "args": _np(list(args)), "kwargs": _np(dict(kwargs))}
+            out = fn(*args, **kwargs)
+            rec["result"] = _np(out)
+            records.append(rec)
+            return out
+        return recorder
+
+    def wrap_assert(name, fn):
+        def recorder(*args, **kwargs):
+            records.append({"fn": name, "args": _np(list(args)), "kwargs": _np(dict(kwargs))})
+            return fn(*args, **kwargs)
+        return recorder
+
+    mod = importlib.import_module("tensorly.tenalg.tests.test_proximal")
+    for fname in names:
+        setattr(mod, fname, wrap(fname, getattr(mod, fname)))
+    for aname in ("assert_array_equal", "assert_array_almost_equal"):
+        if hasattr(mod, aname):
+            setattr(mod, aname, wrap_assert(aname, getattr(mod, aname)))
+    for tname in sorted(n for n in dir(mod) if n.startswith("test_")):
+        np.random.seed(0)
+        records.append({"fn": "__test__", "name": f"tensorly.tenalg.tests.test_proximal.{tname}"})
+        getattr(mod, tname)()
     return records
 
 
@@ -489,8 +531,11 @@ def main():
     recon = record_reconstruction()
     with open(os.path.join(HERE, "reconstruction_kats.pkl"), "wb") as f:
         pickle.dump({"versions": _versions(), "records": recon}, f, protocol=4)
+    prox = record_proximal()
+    with open(os.path.join(HERE, "proximal_kats.pkl"), "wb") as f:
+        pickle.dump({"versions": _versions(), "records": prox}, f, protocol=4)
     print(f"{len(kats)} tenalg records, {len(runs)} reference runs, "
-          f"{len(recon)} reconstruction records")
+          f"{len(recon)} reconstruction records, {len(prox)} proximal records")
 
 
 if __name__ == "__main__":
