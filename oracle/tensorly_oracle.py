@@ -1191,9 +1191,12 @@ def non_negative_tucker(tensor, rank, n_iter_max=10, init="svd", tol=10e-5, rand
 def partial_tucker(tensor, rank, modes=None, n_iter_max=100, init="svd", tol=10e-5,
                    svd="truncated_svd", random_state=None, verbose=False, mask=None,
                    svd_mask_repeats=5):
-    """tensorly/decomposition/_tucker.py:105-221 (HOOI, no mask)."""
-    if mask is not None:
-        raise NotImplementedError("oracle restates the unmasked HOOI only")
+    """tensorly/decomposition/_tucker.py:105-221 (HOOI); with a mask the
+    missing entries are refilled from the model at each iteration (``:194-197``)
+    and the starts are 'random' or given (a masked 'svd' start imputes inside
+    svd_interface and is not restated)."""
+    if mask is not None and isinstance(init, str) and init == "svd":
+        raise NotImplementedError("oracle restates masked HOOI from 'random' or given starts")
     if modes is None:
         modes = list(range(tensor.ndim))
     if rank is None:
@@ -1207,6 +1210,9 @@ def partial_tucker(tensor, rank, modes=None, n_iter_max=100, init="svd", tol=10e
     rec_errors = []
     norm_tensor = norm(tensor)
     for iteration in range(n_iter_max):
+        if mask is not None:
+            tensor = tensor * mask + multi_mode_dot(core, factors, modes=modes,
+                                                    transpose=False) * (1 - mask)
         for index, mode in enumerate(modes):
             core_approximation = multi_mode_dot(tensor, factors, modes=modes, skip=index,
                                                 transpose=True)

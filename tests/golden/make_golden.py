@@ -508,6 +508,21 @@ def reference_runs():
                      "factors": [np.array(f) for f in tt.factors],
                      "errors": [float(e) for e in errs]})
 
+    # masked Tucker (missing entries refilled from the model each iteration)
+    for name, g, kw, keep in (
+            ("tucker_mask", dict(shape=(10, 9, 8), seed=34),
+             dict(rank=[3, 3, 2], init="random", random_state=5, n_iter_max=12, tol=1e-9), 0.8),
+            ("tucker_mask_4way", dict(shape=(6, 7, 5, 6), seed=35),
+             dict(rank=[2, 3, 2, 2], init="random", random_state=6, n_iter_max=8, tol=0), 0.7)):
+        rs = np.random.RandomState(g["seed"])
+        x = rs.randn(*g["shape"])
+        mask = (np.random.RandomState(g["seed"] + 1000).rand(*g["shape"]) < keep).astype(x.dtype)
+        tt, errs = tucker(x, return_errors=True, mask=mask, **copy.deepcopy(kw))
+        runs.append({"case": name, "gen": {"fn": "randn", **g}, "checksum": cs(x),
+                     "kwargs": kw, "mask_keep": keep, "core": np.array(tt.core),
+                     "factors": [np.array(f) for f in tt.factors],
+                     "errors": [float(e) for e in errs]})
+
     # svd_interface of a tall and a wide matrix
     for name, shape, k in (("svd_wide", (7, 30), 4), ("svd_tall", (25, 6), 3)):
         rs = np.random.RandomState(40 + shape[0])

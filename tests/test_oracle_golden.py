@@ -254,6 +254,20 @@ def test_oracle_tucker_matches_reference(golden, case):
         np.testing.assert_allclose(a, b, rtol=1e-9, atol=1e-10)
 
 
+@pytest.mark.parametrize("case", ["tucker_mask", "tucker_mask_4way"])
+def test_oracle_masked_tucker_matches_reference(golden, case):
+    run = golden["runs"][case]
+    x = regenerate(run)
+    g = run["gen"]
+    mask = (np.random.RandomState(g["seed"] + 1000).rand(*g["shape"])
+            < run["mask_keep"]).astype(x.dtype)
+    (core, factors), errs = oracle.tucker(x, return_errors=True, mask=mask, **run["kwargs"])
+    np.testing.assert_allclose(errs, run["errors"], rtol=1e-10, atol=1e-12)
+    np.testing.assert_allclose(core, run["core"], rtol=1e-9, atol=1e-10)
+    for a, b in zip(factors, run["factors"]):
+        np.testing.assert_allclose(a, b, rtol=1e-9, atol=1e-10)
+
+
 @pytest.mark.parametrize("case", ["svd_wide", "svd_tall"])
 def test_oracle_svd_interface_matches_reference(golden, case):
     run = golden["runs"][case]
