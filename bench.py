@@ -65,6 +65,17 @@ def parse():
     return p.parse_args()
 
 
+def job_time_ms(ms, ws, device="cpu"):
+    """The job's timed region: the max over the ranks' own timings (ms); one
+    rank returns its own."""
+    if ws <= 1:
+        return ms
+    import torch
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -273,10 +284,7 @@ def run_gpu(args):
             print(json.dumps({"profile": True, "ms_per_step": ms / args.steps,
                               "final_rel_error": errs[-1]}), flush=True)
         return
-    if ws > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = job_time_ms(ms, ws, device=dev)
     total_sweeps = args.sweeps * args.steps * ws
     value = total_sweeps / (ms / 1000.0)
     final_err = errs[-1]
