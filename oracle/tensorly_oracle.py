@@ -32,7 +32,7 @@ __all__ = [
     "cp_to_vec", "tucker_to_unfolded", "tucker_to_vec", "sample_khatri_rao",
     "randomised_parafac", "sparsify_tensor", "error_calc_ext", "validate_constraints", "proximal_operator", "admm",
     "initialize_constrained_parafac", "constrained_parafac", "non_negative_tucker", "fista",
-    "non_negative_tucker_hals",
+    "non_negative_tucker_hals", "active_set_nnls", "kronecker",
 ]
 
 
@@ -767,11 +767,72 @@ def fista(UtM, UtU, x=None, n_iter_max=100, non_negative=True, sparsity_coef=0, 
     return x
 
 
+def kronecker(matrices):
+    """tensorly/tenalg/core_tenalg/_kronecker.py: left-to-right Kronecker product."""
+    res = matrices[0]
+    for m in matrices[1:]:
+        res = np.kron(res, m)
+    return res
+
+
+def _active_solve(UtU, Utm, passive_set, support_vec):
+    """Solve on the passive set and scatter into the support vector."""
+    passive_solution = np.linalg.solve(UtU[passive_set, :][:, passive_set], Utm[passive_set])
+    support_vec = np.zeros(support_vec.shape, dtype=support_vec.dtype)
+    support_vec[passive_set] = passive_solution
+    return support_vec
+
+
+def active_set_nnls(Utm, UtU, x=None, n_iter_max=100, tol=10e-8):
+    """tensorly/solvers/nnls.py:275-406: Lawson-Hanson style active set."""
+    x_vec = np.zeros(UtU.shape[1], dtype=UtU.dtype) if x is None else np.reshape(x, (-1,))
+    x_gradient = Utm - np.dot(UtU, x_vec)
+    passive_set = x_vec > 0
+    active_set = x_vec <= 0
+    support_vec = np.zeros(x_vec.shape, dtype=x_vec.dtype)
+    for iteration in range(n_iter_max):
+        if iteration > 0 or np.all(x_vec == 0):
+            indice = np.argmax(x_gradient)
+            passive_set = passive_set.copy()
+            active_set = active_set.copy()
+            passive_set[indice] = True
+            active_set[indice] = False
+        try:
+            support_vec = _active_solve(UtU, Utm, passive_set, support_vec)
+        except Exception:
+            x_vec = np.zeros(UtU.shape[1])
+            support_vec = np.zeros(x_vec.shape, dtype=x_vec.dtype)
+            passive_set = x_vec > 0
+            active_set = x_vec <= 0
+            if np.any(active_set):
+                indice = np.argmax(x_gradient)
+                passive_set[indice] = True
+                active_set[indice] = False
+            support_vec = _active_solve(UtU, Utm, passive_set, support_vec)
+        if np.min(support_vec[passive_set]) <= 0:
+            for _ in range(len(passive_set)):
+                sel = support_vec[passive_set] <= 0
+                alpha = np.min(x_vec[passive_set][sel]
+                               / (x_vec[passive_set][sel] - support_vec[passive_set][sel]))
+                x_vec = x_vec + alpha * (support_vec - x_vec)
+                passive_set = x_vec > 0
+                active_set = x_vec <= 0
+                support_vec = _active_solve(UtU, Utm, passive_set, support_vec)
+                if np.any(passive_set) != True or np.min(support_vec[passive_set]) > 0:
+                    break
+        x_vec = np.clip(support_vec, 0, np.max(support_vec))
+        x_gradient = Utm - np.dot(UtU, x_vec)
+        if np.any(active_set) != True or np.max(x_gradient[active_set]) <= tol:
+            break
+    return x_vec
+
+
 def non_negative_tucker_hals(tensor, rank, n_iter_max=100, init="svd", svd="truncated_svd",
                              tol=1e-8, sparsity_coefficients=None, core_sparsity_coefficient=None,
-                             random_state=None, return_errors=False, exact=False):
-    """tensorly/decomposition/_tucker.py:457-691 (algorithm='fista', no fixed
-    modes, not normalised)."""
+                             random_state=None, return_errors=False, exact=False,
+                             algorithm="fista"):
+    """tensorly/decomposition/_tucker.py:457-691 (no fixed modes, not
+    normalised; algorithm 'fista' or 'active_set')."""
     rank = validate_tucker_rank(tensor.shape, rank=rank)
     n_modes = tensor.ndim
     if sparsity_coefficients is None or not isinstance(sparsity_coefficients, (list, tuple)):
@@ -797,12 +858,19 @@ def non_negative_tucker_hals(tensor, rank, n_iter_max=100, init="svd", svd="trun
                                   sparsity_coefficient=sparsity_coefficients[mode], exact=exact)
             nn_factors[mode] = np.transpose(nn_factor)
         pseudo_inverse[-1] = np.dot(np.transpose(nn_factors[-1]), nn_factors[-1])
-        core_estimation = multi_mode_dot(tensor, nn_factors, transpose=True)
-        learning_rate = 1
-        for MtM in pseudo_inverse:
-            learning_rate *= 1 / (truncated_svd(MtM)[1][0])
-        nn_core = fista(core_estimation, pseudo_inverse, x=nn_core, n_iter_max=n_iter_max,
-                        sparsity_coef=core_sparsity_coefficient, lr=learning_rate)
+        if algorithm == "fista":
+            core_estimation = multi_mode_dot(tensor, nn_factors, transpose=True)
+            learning_rate = 1
+            for MtM in pseudo_inverse:
+                learning_rate *= 1 / (truncated_svd(MtM)[1][0])
+            nn_core = fista(core_estimation, pseudo_inverse, x=nn_core, n_iter_max=n_iter_max,
+                            sparsity_coef=core_sparsity_coefficient, lr=learning_rate)
+        elif algorithm == "active_set":
+            core_estimation_vec = np.reshape(
+                mode_dot(tensor_cross, np.transpose(nn_factors[modes[-1]]), modes[-1]), (-1,))
+            vectorcore = active_set_nnls(core_estimation_vec, kronecker(pseudo_inverse),
+                                         x=nn_core, n_iter_max=n_iter_max)
+            nn_core = np.reshape(vectorcore, nn_core.shape)
         rec_error = norm(tensor - tucker_to_tensor((nn_core, nn_factors))) / norm_tensor
         rec_errors.append(rec_error)
         if iteration > 1:

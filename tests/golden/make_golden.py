@@ -419,6 +419,11 @@ def reference_runs():
               sparsity_coefficients=[0.01, None, 0.02], core_sparsity_coefficient=0.001)),
         ("nnth_f32", dict(shape=(12, 10, 9), rank=3, seed=98, dtype=np.float32),
          dict(rank=[3, 3, 3], n_iter_max=8, init="svd", tol=1e-12)),
+        ("nnth_active_set", dict(shape=(9, 8, 7), rank=2, seed=99),
+         dict(rank=[2, 3, 2], n_iter_max=6, init="svd", tol=1e-12, algorithm="active_set")),
+        ("nnth_active_set_4way", dict(shape=(7, 6, 5, 6), rank=2, seed=100),
+         dict(rank=[2, 2, 2, 2], n_iter_max=5, init="random", random_state=7, tol=1e-12,
+              algorithm="active_set")),
     ]
     for name, g, kw in nnth_variants:
         x = np.abs(small(g["seed"], g["shape"], g["rank"], g.get("dtype", np.float64)))

@@ -188,7 +188,8 @@ def test_oracle_non_negative_tucker_matches_reference(golden, case):
         np.testing.assert_allclose(a, b, rtol=tol, atol=tol * np.abs(b).max())
 
 
-@pytest.mark.parametrize("case", ["nnth_svd", "nnth_random", "nnth_sparse", "nnth_f32"])
+@pytest.mark.parametrize("case", ["nnth_svd", "nnth_random", "nnth_sparse", "nnth_f32",
+                                  "nnth_active_set", "nnth_active_set_4way"])
 def test_oracle_non_negative_tucker_hals_matches_reference(golden, case):
     run = golden["runs"][case]
     x = regenerate(run)
