@@ -1,9 +1,10 @@
 """NumPy restatement of PARAFAC2 (TEST INFRASTRUCTURE ONLY).
 
-Follows tensorly/decomposition/_parafac2.py:69-707 for the dense, unmasked,
-unconstrained (nn_modes=None) case, with the reference's line search
-(_BroThesisLineSearch, :186-297), projections (:158-171), projected slices
-(:174-178) and error expansion (:300-362), and the random start of
+Follows tensorly/decomposition/_parafac2.py:21-707, with non-negative modes
+(nn_modes, through non_negative_parafac_hals) and masks (missing entries
+imputed, :21-66), with the reference's line search
+(_BroThesisLineSearch, :183-318), projections (:158-171), projected slices
+(:174-178) and error expansion (:321-396), and the random start of
 tensorly/random/base.py:18-61 (QR of uniform draws, then random_cp).  Only
 ``tests/`` import it; it is pinned by the reference runs in tests/golden.
 """
@@ -70,9 +71,38 @@ def initialize_decomposition(tensor_slices, rank, init="random", svd="truncated_
     return weights, list(factors), list(projections)
 
 
+def parafac2_to_slices(decomposition):
+    """tensorly/parafac2_tensor.py:310-372: slice i = (P_i B) (A_i w) C^T."""
+    weights, (A, B, C), projections = decomposition
+    out = []
+    for i, p in enumerate(projections):
+        a = A[i] if weights is None else A[i] * weights
+        out.append(np.dot(np.dot(p, B) * a, np.transpose(C)))
+    return out
+
+
+def update_imputed(tensor_slices, mask, decomposition, method):
+    """tensorly/decomposition/_parafac2.py:21-66: the missing entries become
+    the slice's observed mean ('mode-2') or the model's value ('factors')."""
+    if method == "mode-2":
+        out = []
+        for s, m in zip(tensor_slices, mask):
+            mean = np.sum(s * m) / np.sum(m)
+            out.append(np.where(m == 0, mean, s))
+        return out
+    rec = parafac2_to_slices(decomposition)
+    return [np.where(m == 0, r, s) for s, r, m in zip(tensor_slices, rec, mask)]
+
+
 def reconstruction_error(tensor_slices, decomposition, norm_matrices=None,
-                         projected_tensor=None):
-    """tensorly/decomposition/_parafac2.py:300-362 (mask None)."""
+                         projected_tensor=None, mask=None):
+    """tensorly/decomposition/_parafac2.py:321-396."""
+    if mask is not None:
+        rec = parafac2_to_slices(decomposition)
+        total = 0.0
+        for s, r, m in zip(tensor_slices, rec, mask):
+            total += tlo.norm(m * s - m * r) ** 2
+        return np.sqrt(total)
     if norm_matrices is None:
         norm_X_sq = sum(tlo.norm(t) ** 2 for t in tensor_slices)
     else:
@@ -95,12 +125,14 @@ def reconstruction_error(tensor_slices, decomposition, norm_matrices=None,
 
 
 class LineSearch:
-    """tensorly/decomposition/_parafac2.py:186-297 (_BroThesisLineSearch, no
-    nn_modes, no mask)."""
+    """tensorly/decomposition/_parafac2.py:183-318 (_BroThesisLineSearch), clipping
+    the non-negative modes 0 and 2 of the extrapolated step."""
 
-    def __init__(self, norm_tensor, svd, acc_pow=2.0, max_fail=4):
+    def __init__(self, norm_tensor, svd, nn_modes=None, mask=None, acc_pow=2.0, max_fail=4):
         self.norm_tensor = norm_tensor
         self.svd = svd
+        self.nn_modes = nn_modes
+        self.mask = mask
         self.acc_pow = acc_pow
         self.max_fail = max_fail
         self.acc_fail = 0
@@ -110,9 +142,14 @@ class LineSearch:
         jump = iteration ** (1.0 / self.acc_pow)
         factors_ls = [factors_last[ii] + (factors[ii] - factors_last[ii]) * jump
                       for ii, _ in enumerate(factors)]
+        if self.nn_modes:
+            if 0 in self.nn_modes:
+                factors_ls[0] = np.clip(factors_ls[0], 0, None)
+            if 2 in self.nn_modes:
+                factors_ls[2] = np.clip(factors_ls[2], 0, None)
         projections_ls = compute_projections(tensor_slices, factors_ls, self.svd)
         ls_rec_error = reconstruction_error(tensor_slices, (weights, factors_ls, projections_ls),
-                                            norm_matrices=self.norm_tensor)
+                                            norm_matrices=self.norm_tensor, mask=self.mask)
         ls_rec_error /= self.norm_tensor
         if ls_rec_error < rec_error:
             self.acc_fail = 0
@@ -125,15 +162,24 @@ class LineSearch:
 
 
 def parafac2(tensor_slices, rank, n_iter_max=2000, init="random", svd="truncated_svd",
-             normalize_factors=False, tol=1.0e-8, random_state=None, return_errors=False,
-             n_iter_parafac=5, linesearch=True):
-    """tensorly/decomposition/_parafac2.py:399-707 (nn_modes=None, no mask)."""
+             normalize_factors=False, tol=1.0e-8, nn_modes=None, random_state=None,
+             return_errors=False, n_iter_parafac=5, linesearch=True, mask=None):
+    """tensorly/decomposition/_parafac2.py:399-707."""
     weights, factors, projections = initialize_decomposition(tensor_slices, rank, init=init,
                                                              svd=svd, random_state=random_state)
     factors = list(factors)
+    if mask is not None:
+        if init in ("random", "svd"):
+            tensor_slices = update_imputed(list(tensor_slices), mask, None, "mode-2")
+        else:
+            tensor_slices = update_imputed(tensor_slices, mask,
+                                           (weights, factors, projections), "factors")
     rec_errors = []
-    norm_tensor = np.sqrt(sum(tlo.norm(t) ** 2 for t in tensor_slices))
-    ls = LineSearch(norm_tensor, svd) if linesearch else None
+    if mask is not None:
+        norm_tensor = np.sqrt(sum(tlo.norm(t * m) ** 2 for t, m in zip(tensor_slices, mask)))
+    else:
+        norm_tensor = np.sqrt(sum(tlo.norm(t) ** 2 for t in tensor_slices))
+    ls = LineSearch(norm_tensor, svd, nn_modes=nn_modes, mask=mask) if linesearch else None
     if weights is None:
         weights = np.ones(rank, dtype=tensor_slices[0].dtype)
     for iteration in range(n_iter_max):
@@ -146,20 +192,28 @@ def parafac2(tensor_slices, rank, n_iter_max=2000, init="random", svd="truncated
             line_iter = False
         projections = compute_projections(tensor_slices, factors, svd)
         projected_tensor = project_tensor_slices(tensor_slices, projections)
-        (_, factors) = tlo.parafac(projected_tensor, rank, n_iter_max=n_iter_parafac,
-                                   init=(weights, factors), svd=svd, normalize_factors=False,
-                                   random_state=random_state, tol=1e-100)
+        if nn_modes is None:
+            (_, factors) = tlo.parafac(projected_tensor, rank, n_iter_max=n_iter_parafac,
+                                       init=(weights, factors), svd=svd, normalize_factors=False,
+                                       random_state=random_state, tol=1e-100)
+        else:
+            (_, factors) = tlo.non_negative_parafac_hals(
+                projected_tensor, rank, n_iter_max=n_iter_parafac, init=(weights, factors),
+                svd=svd, nn_modes=nn_modes, tol=1e-100)
         factors = list(factors)
         if line_iter:
             factors, projections, rec_errors[-1] = ls.line_step(
                 iteration, tensor_slices, factors_last, weights, factors, projections,
                 rec_errors[-1])
+        if mask is not None:
+            tensor_slices = update_imputed(tensor_slices, mask,
+                                           (weights, factors, projections), "factors")
         if normalize_factors:
             weights, factors = tlo.cp_normalize((weights, factors))
             factors = list(factors)
         if tol and not line_iter:
             rec_error = reconstruction_error(tensor_slices, (weights, factors, projections),
-                                             norm_tensor, projected_tensor)
+                                             norm_tensor, projected_tensor, mask)
             rec_errors.append(rec_error / norm_tensor)
         if tol:
             if iteration >= 1:

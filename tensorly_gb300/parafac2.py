@@ -158,7 +158,7 @@ def _project(slices, projections):
 
 
 def _reconstruction_error(slices, decomposition, norm_x, projected=None):
-    """tensorly/decomposition/_parafac2.py:300-362 (no mask)."""
+    """tensorly/decomposition/_parafac2.py:321-396 (no mask)."""
     weights, (A, B, C), projections = decomposition
     if weights is not None:
         A = _scale_cols(A, weights)
@@ -219,7 +219,7 @@ def _initialize(slices, rank, init, svd, random_state):
 
 
 class _LineSearch:
-    """tensorly/decomposition/_parafac2.py:186-297 (no nn_modes, no mask)."""
+    """tensorly/decomposition/_parafac2.py:183-318 (no nn_modes, no mask)."""
 
     def __init__(self, norm_tensor, acc_pow=2.0, max_fail=4, verbose=False):
         self.norm_tensor = norm_tensor

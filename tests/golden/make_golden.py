@@ -202,7 +202,9 @@ def reference_runs():
     from tensorly.decomposition._cp import initialize_cp
     from tensorly.tenalg.svd import svd_interface
     sys.path.insert(0, REPO)
+    sys.path.insert(0, os.path.join(REPO, "tests"))
     from tensorly_gb300 import workloads
+    from golden_inputs import slice_masks
     tl.set_backend("numpy")
     runs = []
 
@@ -447,12 +449,28 @@ def reference_runs():
         ("p2_f32", dict(seed=105, rows=[10, 11, 12, 9], cols=6, dtype=np.float32),
          dict(rank=3, n_iter_max=10, random_state=4)),
     ]
+    # non-negative modes (HALS inner solve) and masked slices (imputation);
+    # nn_modes="all" only without line search: the reference's line search
+    # tests ``0 in nn_modes``, a TypeError on the string
+    p2_variants += [
+        ("p2_nn_all", dict(seed=106, rows=[8, 9, 10, 11], cols=6),
+         dict(rank=3, n_iter_max=10, random_state=5, nn_modes="all", linesearch=False)),
+        ("p2_nn_02", dict(seed=107, rows=[9, 8, 10, 12, 11], cols=7),
+         dict(rank=3, n_iter_max=12, random_state=6, nn_modes=[0, 2])),
+        ("p2_mask", dict(seed=108, rows=[8, 10, 9, 11], cols=6, mask_keep=0.8),
+         dict(rank=2, n_iter_max=12, random_state=7)),
+        ("p2_mask_svd", dict(seed=109, rows=[7, 9, 8], cols=5, mask_keep=0.7),
+         dict(rank=2, n_iter_max=8, init="svd", linesearch=False)),
+    ]
     for name, g, kw in p2_variants:
         rsl = np.random.RandomState(g["seed"])
         xs = [rsl.rand(r, g["cols"]).astype(g.get("dtype", np.float64)) for r in g["rows"]]
         ck = [float(sum(np.asarray(t, np.float64).sum() for t in xs)),
               float(np.sqrt(sum((np.asarray(t, np.float64) ** 2).sum() for t in xs)))]
-        out, errs = parafac2(xs, return_errors=True, **copy.deepcopy(kw))
+        kw_call = copy.deepcopy(kw)
+        if "mask_keep" in g:
+            kw_call["mask"] = slice_masks(g)
+        out, errs = parafac2(xs, return_errors=True, **kw_call)
         w, fs, ps = out
         runs.append({"case": name, "gen": {"fn": "slices", **g}, "checksum": ck, "kwargs": kw,
                      "weights": np.array(w), "factors": [np.array(f) for f in fs],

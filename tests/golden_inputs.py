@@ -15,6 +15,14 @@ def small_cp(seed, shape, rank, dtype=np.float64, noise=0.01):
     return t.astype(dtype)
 
 
+def slice_masks(g):
+    """0/1 masks of PARAFAC2 slices, keeping each entry with probability
+    ``g["mask_keep"]`` (seeded by ``g["seed"] + 1000``)."""
+    rs = np.random.RandomState(g["seed"] + 1000)
+    dtype = g.get("dtype", np.float64)
+    return [(rs.rand(r, g["cols"]) < g["mask_keep"]).astype(dtype) for r in g["rows"]]
+
+
 def regenerate(run):
     g = run["gen"]
     if g["fn"] == "dense_cp_small":

@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 import oracle
-from golden_inputs import regenerate
+from golden_inputs import regenerate, slice_masks
 
 FN = {"khatri_rao": oracle.khatri_rao, "mode_dot": oracle.mode_dot,
       "multi_mode_dot": oracle.multi_mode_dot,
@@ -204,13 +204,16 @@ def test_oracle_non_negative_tucker_hals_matches_reference(golden, case):
         np.testing.assert_allclose(a, b, rtol=tol, atol=tol * np.abs(b).max())
 
 
-@pytest.mark.parametrize("case", ["p2_random", "p2_svd", "p2_nols", "p2_normalize", "p2_f32"])
+@pytest.mark.parametrize("case", ["p2_random", "p2_svd", "p2_nols", "p2_normalize", "p2_f32",
+                                  "p2_nn_all", "p2_nn_02", "p2_mask", "p2_mask_svd"])
 def test_oracle_parafac2_matches_reference(golden, case):
     from oracle import parafac2_oracle
     run = golden["runs"][case]
     xs = regenerate(run)
     kw = dict(run["kwargs"])
     rank = kw.pop("rank")
+    if "mask_keep" in run["gen"]:
+        kw["mask"] = slice_masks(run["gen"])
     (w, f, p), errs = parafac2_oracle.parafac2(xs, rank, return_errors=True, **kw)
     tol = 1e-4 if xs[0].dtype == np.float32 else 1e-9
     assert len(errs) == len(run["errors"])
