@@ -312,6 +312,12 @@ def reference_runs():
         # exact=True: 50000 inner iterations per call, no early stop at rank 2
         ("nn_hals_exact", dict(shape=(8, 7, 6), rank=2, seed=67),
          dict(init="svd", n_iter_max=2, tol=1e-12, exact=True)),
+        # unconstrained mode 1 (solved by the normal equations), normalised factors
+        ("nn_hals_modes_02", dict(shape=(10, 9, 8), rank=3, seed=68),
+         dict(init="svd", n_iter_max=12, tol=1e-12, nn_modes=[0, 2])),
+        ("nn_hals_normalize", dict(shape=(9, 8, 7), rank=3, seed=69),
+         dict(init="random", random_state=20, n_iter_max=10, tol=1e-12,
+              normalize_factors=True)),
     ]
     for name, g, kw in hals_variants:
         x = small(g["seed"], g["shape"], g["rank"], g.get("dtype", np.float64))

@@ -109,7 +109,7 @@ def test_oracle_non_negative_parafac_matches_reference(golden, case):
 
 @pytest.mark.parametrize("case", ["nn_hals_random", "nn_hals_svd", "nn_hals_sparse_fixed",
                                   "nn_hals_stop", "nn_hals_f32", "nn_hals_rank1",
-                                  "nn_hals_exact"])
+                                  "nn_hals_exact", "nn_hals_modes_02", "nn_hals_normalize"])
 def test_oracle_non_negative_parafac_hals_matches_reference(golden, case):
     run = golden["runs"][case]
     x = regenerate(run)
@@ -121,8 +121,10 @@ def test_oracle_non_negative_parafac_hals_matches_reference(golden, case):
     tol = 1e-5 if x.dtype == np.float32 else 1e-10
     assert len(errs) == len(run["errors"])
     np.testing.assert_allclose(errs, run["errors"], rtol=tol, atol=tol * 1e-2)
-    for a, b in zip(f, run["factors"]):
-        assert (a >= 0).all()
+    nn_modes = kw.get("nn_modes", "all")
+    for mode, (a, b) in enumerate(zip(f, run["factors"])):
+        if nn_modes == "all" or mode in nn_modes:
+            assert (a >= 0).all()
         np.testing.assert_allclose(a, b, rtol=tol, atol=tol * np.abs(b).max())
 
 
