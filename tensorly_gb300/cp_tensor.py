@@ -119,13 +119,17 @@ def validate_cp_rank(tensor_shape, rank="same", rounding="round"):
 
 
 def validate_tucker_rank(tensor_shape, rank="same", rounding="round", fixed_modes=None):
-    """tensorly/tucker_tensor.py:344-447 (int and sequence ranks; 'same' and
-    fractional ranks follow the reference's parameter-count rule)."""
+    """tensorly/tucker_tensor.py:344-447: a list of per-mode ranks.  'same'
+    and fractional ranks keep that fraction of the tensor's parameter count
+    (core plus factors), an int is used for every free mode, a sequence is
+    returned as given."""
+    fun_r = {"ceil": np.ceil, "floor": np.floor, "round": np.round}.get(rounding)
+    if fun_r is None:
+        raise ValueError(f"Rounding should be round, floor or ceil, but got {rounding}")
     if rank == "same":
         rank = float(1)
     if isinstance(rank, float):
         from scipy.optimize import brentq
-        fun_r = {"ceil": np.ceil, "floor": np.floor, "round": np.round}[rounding]
         n_modes = len(tensor_shape)
         n_param = np.prod(tensor_shape)
         shape = list(tensor_shape)
@@ -142,15 +146,15 @@ def validate_tucker_rank(tensor_shape, rank="same", rounding="round", fixed_mode
         if fixed is not None:
             for m, s in fixed:
                 out.insert(m, s)
-        return tuple(out)
+        return out
     if isinstance(rank, int):
         warnings.warn(
             f"Given only one int for 'rank' for decomposition a tensor of order "
-            f"{len(tensor_shape)}. Using this rank for all modes.")
+            f"{len(tensor_shape)}. Using this rank for all modes.", RuntimeWarning)
         if fixed_modes is None:
-            return tuple([rank] * len(tensor_shape))
-        return tuple(rank if i not in fixed_modes else s for i, s in enumerate(tensor_shape))
-    return tuple(rank)
+            return [rank] * len(tensor_shape)
+        return [rank if i not in fixed_modes else s for i, s in enumerate(tensor_shape)]
+    return rank
 
 
 def _factors_cuda(cp_tensor):

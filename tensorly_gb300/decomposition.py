@@ -1393,7 +1393,8 @@ class BatchedProblem:
             host = np.empty(foff[-1], dtype=np.float32)
             q = 0
             for t, (sh, r) in enumerate(zip(self.shapes, self.ranks)):
-                rng = check_random_state(seeds[t])
+                s = seeds[t]
+                rng = check_random_state(int(s) if isinstance(s, np.integer) else s)
                 for d in sh:
                     host[foff[q]:foff[q + 1]] = rng.random_sample((d, r)).astype(np.float32).ravel()
                     q += 1

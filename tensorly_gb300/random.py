@@ -12,11 +12,13 @@ import torch
 
 
 def check_random_state(seed):
-    """None -> NumPy's global RandomState, int -> RandomState(seed), RandomState -> itself."""
+    """None -> NumPy's global RandomState, int -> RandomState(seed), RandomState
+    -> itself, anything else ValueError.  As in the reference, a Python int
+    (bool included) is a seed and a NumPy integer is not."""
     if seed is None:
         return np.random.mtrand._rand
-    if isinstance(seed, (int, np.integer)) and not isinstance(seed, bool):
-        return np.random.RandomState(int(seed))
+    if isinstance(seed, int):
+        return np.random.RandomState(seed)
     if isinstance(seed, np.random.RandomState):
         return seed
     raise ValueError("Seed should be None, int or np.random.RandomState")

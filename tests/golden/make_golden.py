@@ -196,6 +196,55 @@ def record_proximal():
     return records
 
 
+def record_host_validators():
+    """The reference's host-side helpers on a grid of arguments
+    (tensorly/cp_tensor.py:240-275 validate_cp_rank,
+    tensorly/tucker_tensor.py:344-447 validate_tucker_rank,
+    tensorly/backend/core.py:163-188 check_random_state): the value, or the
+    exception type, and the warning category raised."""
+    import warnings
+    import tensorly as tl
+    from tensorly.cp_tensor import validate_cp_rank
+    from tensorly.tucker_tensor import validate_tucker_rank
+    records = []
+
+    def call(fn, name, *args, **kwargs):
+        rec = {"fn": name, "args": args, "kwargs": kwargs}
+        with warnings.catch_warnings(record=True) as w:
+            warnings.simplefilter("always")
+            try:
+                out = fn(*args, **kwargs)
+                rec["out"] = [int(v) for v in out] if isinstance(out, list) else out
+                rec["type"] = type(out).__name__
+            except Exception as e:      # noqa: BLE001 (the exception type is the record)
+                rec["raises"] = type(e).__name__
+        rec["warns"] = sorted({type(x.message).__name__ for x in w})
+        records.append(rec)
+
+    shapes = [(3, 4, 5), (10, 10, 10), (7, 2, 9, 4), (100, 3), (30, 5, 12)]
+    for shape in shapes:
+        for rank in ("same", 0.5, 0.25, 1.7, 4):
+            for rounding in ("round", "floor", "ceil"):
+                call(validate_cp_rank, "validate_cp_rank", shape, rank=rank, rounding=rounding)
+        call(validate_cp_rank, "validate_cp_rank", shape, rank=2, rounding="bad")
+        for rank in ("same", 0.5, 0.1, 2.0, 3, [2] * len(shape)):
+            for rounding in ("round", "floor", "ceil"):
+                call(validate_tucker_rank, "validate_tucker_rank", shape, rank=rank,
+                     rounding=rounding)
+            for fixed in ([0], [1, len(shape) - 1]):
+                call(validate_tucker_rank, "validate_tucker_rank", shape, rank=rank,
+                     fixed_modes=fixed)
+        call(validate_tucker_rank, "validate_tucker_rank", shape, rank=0.5, rounding="bad")
+    crs = tl.check_random_state
+    for seed in (0, 5, 123456, True):
+        rec = {"fn": "check_random_state", "args": (seed,), "kwargs": {},
+               "out": crs(seed).random_sample(4), "warns": []}
+        records.append(rec)
+    for seed in (np.int64(5), 1.5, "seed"):
+        call(crs, "check_random_state", seed)
+    return records
+
+
 def reference_runs():
     import tensorly as tl
     from tensorly.decomposition import parafac, tucker
@@ -578,8 +627,12 @@ def main():
     prox = record_proximal()
     with open(os.path.join(HERE, "proximal_kats.pkl"), "wb") as f:
         pickle.dump({"versions": _versions(), "records": prox}, f, protocol=4)
+    host = record_host_validators()
+    with open(os.path.join(HERE, "host_kats.pkl"), "wb") as f:
+        pickle.dump({"versions": _versions(), "records": host}, f, protocol=4)
     print(f"{len(kats)} tenalg records, {len(runs)} reference runs, "
-          f"{len(recon)} reconstruction records, {len(prox)} proximal records")
+          f"{len(recon)} reconstruction records, {len(prox)} proximal records, "
+          f"{len(host)} host-helper records")
 
 
 if __name__ == "__main__":
