@@ -13,18 +13,81 @@ from . import _lib
 from ._tensor import dtype_code, ptr, stream_of, workspace
 
 
+def _shape_of(x):
+    return tuple(int(v) for v in x.shape)
+
+
+def _validate_cp_tensor(cp_tensor):
+    """(shape, rank) of a (weights, factors) pair, with the reference's
+    ValueErrors for malformed input (tensorly/cp_tensor.py:163-214)."""
+    if isinstance(cp_tensor, CPTensor):
+        return cp_tensor.shape, cp_tensor.rank
+    if isinstance(cp_tensor, (float, int)):
+        return 0, 0
+    weights, factors = cp_tensor
+    f0 = _shape_of(factors[0])
+    if len(f0) == 2:
+        rank = f0[1]
+    elif len(f0) == 1:
+        rank = 1
+    else:
+        raise ValueError("Got a factor with 3 dimensions but CP factors should be at most 2D, "
+                         "of shape (size, rank).")
+    shape = []
+    for i, factor in enumerate(factors):
+        s = _shape_of(factor)
+        if len(s) == 2:
+            size, current_rank = s
+        else:
+            size, current_rank = s[0], 1
+        if current_rank != rank:
+            # s[1] is read as the reference reads it (an IndexError for a 1-D factor)
+            raise ValueError("All the factors of a CP tensor should have the same number of "
+                             f"column.However, factors[0].shape[1]={rank} but "
+                             f"factors[{i}].shape[1]={s[1]}.")
+        shape.append(size)
+    if weights is not None and _shape_of(weights) != (rank,):
+        raise ValueError(f"Given factors for a rank-{rank} CP tensor but "
+                         f"len(weights)={_shape_of(weights)}.")
+    return tuple(shape), rank
+
+
+def _validate_tucker_tensor(tucker_tensor):
+    """(shape, rank) of a (core, factors) pair, with the reference's
+    ValueErrors for malformed input (tensorly/tucker_tensor.py:19-47)."""
+    core, factors = tucker_tensor
+    if len(factors) < 2:
+        raise ValueError("A Tucker tensor should be composed of at least two factors and a "
+                         f"core.However, {len(factors)} factor was given.")
+    core_shape = _shape_of(core)
+    if len(factors) != len(core_shape):
+        raise ValueError("Tucker decompositions should have one factor per more of the core "
+                         f"tensor.However, core has {len(core_shape)} modes but {len(factors)} "
+                         "factors have been provided")
+    shape, rank = [], []
+    for i, factor in enumerate(factors):
+        current_shape, current_rank = _shape_of(factor)
+        if current_rank != core_shape[i]:
+            raise ValueError("Factor `n` of Tucker decomposition should verify:\n"
+                             "factors[n].shape[1] = core.shape[n]."
+                             f"However, factors[{i}].shape[1]={current_rank} but "
+                             f"core.shape[{i}]={core_shape[i]}.")
+        shape.append(current_shape)
+        rank.append(current_rank)
+    return tuple(shape), tuple(rank)
+
+
 class CPTensor:
     """(weights, factors) pair; tensorly/cp_tensor.py:17-160.
 
+    Validated on construction as the reference does (``_validate_cp_tensor``);
     ``weights`` default to ones (``:25-26``).
     """
 
     def __init__(self, cp_tensor):
+        shape, rank = _validate_cp_tensor(cp_tensor)
         weights, factors = cp_tensor
         factors = list(factors)
-        if len(factors) == 0:
-            raise ValueError("A CP tensor needs at least one factor")
-        rank = factors[0].shape[1] if factors[0].ndim == 2 else 1
         if weights is None:
             f0 = factors[0]
             if isinstance(f0, torch.Tensor):
@@ -33,7 +96,7 @@ class CPTensor:
                 weights = np.ones(rank, dtype=np.asarray(f0).dtype)
         self.weights = weights
         self.factors = factors
-        self.shape = tuple(int(f.shape[0]) for f in factors)
+        self.shape = tuple(shape)
         self.rank = int(rank)
 
     def __getitem__(self, i):
@@ -79,11 +142,12 @@ class TuckerTensor:
     """(core, factors) pair; tensorly/tucker_tensor.py:227-320."""
 
     def __init__(self, tucker_tensor):
+        shape, rank = _validate_tucker_tensor(tucker_tensor)
         core, factors = tucker_tensor
         self.core = core
         self.factors = list(factors)
-        self.shape = tuple(int(f.shape[0]) for f in self.factors)
-        self.rank = tuple(int(s) for s in core.shape)
+        self.shape = shape
+        self.rank = rank
 
     def __getitem__(self, i):
         if i == 0:

@@ -1097,7 +1097,7 @@ int als_launch_gram(const T* A, int64_t I, int R, double* gpart, int nparts_max,
   nparts = (int)ceil_div(I, rpb);
   const int threads = 256;
   const size_t smem = ((size_t)R * R + (size_t)kGramRows * R) * sizeof(double);
-  static bool attr[64] = {};
+  static std::atomic<bool> attr[64];  // per-device set-up flags, read and set by any host thread
   const int dev = current_device();
   if (dev < 64 && !attr[dev]) {
     TLGB_CUDA_TRY(cudaFuncSetAttribute(
@@ -1257,7 +1257,7 @@ static cudaError_t set_carveout_fast() {
 
 template <typename T>
 static int als_prepare_typed() {
-  static bool done[64] = {};
+  static std::atomic<bool> done[64];  // per-device set-up flags, read and set by any host thread
   const int dev = current_device();
   if (dev >= 0 && dev < 64 && done[dev]) return TLGB_OK;
   // The factorisation kernels run on a side stream next to the tensor-core

@@ -559,7 +559,7 @@ int64_t padded_elems(const int64_t* d) {
 
 template <int NT>
 int launch_variant(BArgs a, int grid_max, cudaStream_t st) {
-  static bool attr[64] = {};
+  static std::atomic<bool> attr[64];  // per-device set-up flags, read and set by any host thread
   const int dev = current_device();
   if (dev >= 0 && dev < 64 && !attr[dev]) {
     TLGB_CUDA_TRY(cudaFuncSetAttribute(k_cp_als_batched<NT>,

@@ -5,6 +5,7 @@
 #include <cuda_bf16.h>
 #include <stdint.h>
 #include <stddef.h>
+#include <atomic>
 #include <string>
 
 #include "../../include/tensorly_gb300.h"

@@ -394,7 +394,7 @@ int sym_eig_batched_launch(const T* A, int n, int k, int batch, T* U, T* lam, in
     return set_error(TLGB_EUNSUPPORTED, "sym_eig: matrix order above " +
                                             std::to_string(EigLimits<T>::max_n) +
                                             " is not supported");
-  static bool attr[64] = {};
+  static std::atomic<bool> attr[64];  // per-device set-up flags, read and set by any host thread
   const int dev = current_device();
   if (dev >= 0 && dev < 64 && !attr[dev]) {
     TLGB_CUDA_TRY(cudaFuncSetAttribute(k_sym_eig<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -462,7 +462,7 @@ extern "C" int tlgb_ws_generate(const int64_t* seeds, int batch, void* X, void* 
   clear_error();
   TLGB_CHECK_ARG(seeds && X && feats && xnorm && omega && batch >= 1, "ws_generate: bad argument");
   const size_t smem = (size_t)(kN3 + 3 * kI * kR + 32 + kI * kI * kS) * sizeof(float);
-  static bool attr[64] = {};
+  static std::atomic<bool> attr[64];  // per-device set-up flags, read and set by any host thread
   const int dev = current_device();
   if (dev >= 0 && dev < 64 && !attr[dev]) {
     TLGB_CUDA_TRY(cudaFuncSetAttribute(k_generate, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -480,7 +480,7 @@ extern "C" int tlgb_ws_sketch(const void* X, int batch, void* feats, void* xnorm
   clear_error();
   TLGB_CHECK_ARG(X && feats && xnorm && omega && batch >= 1, "ws_sketch: bad argument");
   const size_t smem = (size_t)(kN3 + 32 + kI * kI * kS) * sizeof(float);
-  static bool attr[64] = {};
+  static std::atomic<bool> attr[64];  // per-device set-up flags, read and set by any host thread
   const int dev = current_device();
   if (dev >= 0 && dev < 64 && !attr[dev]) {
     TLGB_CUDA_TRY(cudaFuncSetAttribute(k_sketch, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -520,7 +520,7 @@ extern "C" int tlgb_ws_cp_loss(const void* X, const void* out, const void* xnorm
   clear_error();
   TLGB_CHECK_ARG(X && out && xnorm && loss && batch >= 1, "ws_cp_loss: bad argument");
   const size_t smem = (size_t)(kN3 + 6 * kI * kR + 3 * kR * kR + 32) * sizeof(float);
-  static bool attr[64] = {};
+  static std::atomic<bool> attr[64];  // per-device set-up flags, read and set by any host thread
   const int dev = current_device();
   if (dev >= 0 && dev < 64 && !attr[dev]) {
     TLGB_CUDA_TRY(cudaFuncSetAttribute(k_cp_loss, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -591,7 +591,7 @@ extern "C" int tlgb_ws_svd_init(const void* X, int batch, void* factors, void* w
                 align_up((size_t)batch * 3 * kR * 4, 256);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const size_t smem = (size_t)kN3 * sizeof(float);
-  static bool attr[64] = {};
+  static std::atomic<bool> attr[64];  // per-device set-up flags, read and set by any host thread
   const int dev = current_device();
   if (dev >= 0 && dev < 64 && !attr[dev]) {
     TLGB_CUDA_TRY(cudaFuncSetAttribute(k_gram3, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -13,6 +13,13 @@
 //    address lookup and the kernels' shared-memory attributes), so make one
 //    call on each device before any stream capture that contains this entry
 //    point;
+//  * the device address of the scratch is looked up once per device and kept
+//    for the life of the process: the entry point assumes one context per
+//    device for that time (no cudaDeviceReset, no primary-context teardown
+//    and re-creation between calls);
+//  * the 16 MiB array is part of the library's device code, so it stays
+//    resident on every device where the library's module is loaded, whether
+//    or not this entry point is ever called;
 //  * nothing in the scratch has to start at zero: every call overwrites all
 //    of the partial space it reads;
 //  * there is ONE scratch per device and process: two calls that are in

@@ -297,7 +297,7 @@ int set_attr() {
 
 template <typename T>
 int prepare_typed() {
-  static bool done[64] = {};
+  static std::atomic<bool> done[64];  // per-device set-up flags, read and set by any host thread
   const int dev = current_device();
   if (dev >= 0 && dev < 64 && done[dev]) return TLGB_OK;
   int rc = set_attr<T, 16>();

@@ -609,7 +609,7 @@ int launch_mn(const TcPlan& p, const CUtensorMap& tx, const CUtensorMap& tf, con
 }  // namespace
 
 int mttkrp_tc_prepare() {
-  static bool done[64] = {};
+  static std::atomic<bool> done[64];  // per-device set-up flags, read and set by any host thread
   const int dev = current_device();
   if (dev >= 0 && dev < 64 && done[dev]) return TLGB_OK;
   if (!encode_fn()) return set_error(TLGB_EUNSUPPORTED, "cuTensorMapEncodeTiled unavailable");

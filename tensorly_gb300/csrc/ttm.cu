@@ -263,7 +263,7 @@ template <typename T, int JP, int V>
 int launch_stream(const T* X, const T* U, T* Y, int64_t L, int I, int64_t Tt, int J,
                   int transpose, cudaStream_t st) {
   const size_t smem = (size_t)I * JP * sizeof(T);
-  static bool attr[64] = {};
+  static std::atomic<bool> attr[64];  // per-device set-up flags, read and set by any host thread
   const int dev = current_device();
   if (dev >= 0 && dev < 64 && !attr[dev]) {
     TLGB_CUDA_TRY(cudaFuncSetAttribute(ttm_stream_kernel<T, JP, V>,
@@ -283,7 +283,7 @@ int launch(const TtmArgs<T>& a, cudaStream_t st) {
   constexpr int VEC = TVec<T>::n;
   const size_t smem = (size_t)2 * TCfg<T>::BK * (TCfg<T>::BM + VEC) * sizeof(T) +
                       (size_t)2 * TCfg<T>::BK * (BN + VEC) * sizeof(T);
-  static bool attr[64] = {};
+  static std::atomic<bool> attr[64];  // per-device set-up flags, read and set by any host thread
   const int dev = current_device();
   if (dev < 64 && !attr[dev]) {
     TLGB_CUDA_TRY(cudaFuncSetAttribute(ttm_kernel<T, BN>,

@@ -2,7 +2,10 @@
 
 Run where the reference source tree is available (it is pure Python):
 
-    TENSORLY_REFERENCE=/root/reference python tests/golden/make_golden.py
+    TENSORLY_REFERENCE=<path of the TensorLy source tree> python tests/golden/make_golden.py
+
+The path comes from the environment only; the script stops with a message
+when it is unset.
 
 Outputs (committed, small, platform independent):
 
@@ -39,7 +42,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("TENSORLY_REFERENCE", "/root/reference")
+REF = os.environ.get("TENSORLY_REFERENCE")
 
 
 def _versions():
@@ -612,9 +615,63 @@ def reference_runs():
     return runs
 
 
+def record_container_validation():
+    """CPTensor and TuckerTensor construction on well-formed and malformed
+    inputs (tensorly/cp_tensor.py:17-29 with _validate_cp_tensor :163-214;
+    tensorly/tucker_tensor.py:227-236 with _validate_tucker_tensor :19-47):
+    the shape and rank, or the exception type and message."""
+    from tensorly.cp_tensor import CPTensor
+    from tensorly.tucker_tensor import TuckerTensor
+    rs = np.random.RandomState(7)
+    records = []
+
+    def call(kind, value):
+        rec = {"kind": kind, "value": value}
+        try:
+            obj = (CPTensor if kind == "cp" else TuckerTensor)(value)
+            rec["shape"] = tuple(int(v) for v in obj.shape)
+            rec["rank"] = (int(obj.rank) if kind == "cp" else tuple(int(v) for v in obj.rank))
+        except Exception as e:      # noqa: BLE001 (the exception is the record)
+            rec["raises"] = type(e).__name__
+            rec["message"] = str(e)
+        records.append(rec)
+
+    m = lambda *s: rs.random_sample(s)   # noqa: E731
+    call("cp", (None, [m(4, 3), m(5, 3), m(6, 3)]))
+    call("cp", (np.ones(3), [m(4, 3), m(5, 3), m(6, 3)]))
+    call("cp", (np.ones(2), [m(4, 3), m(5, 3), m(6, 3)]))
+    call("cp", (np.ones((3, 1)), [m(4, 3), m(5, 3)]))
+    call("cp", (None, [m(4, 3), m(5, 2), m(6, 3)]))
+    call("cp", (None, [m(4, 3), m(5, 3), m(6, 4)]))
+    call("cp", (None, [m(4), m(5), m(6)]))
+    call("cp", (np.ones(1), [m(4), m(5, 1)]))
+    call("cp", (None, [m(4), m(5, 2)]))
+    call("cp", (None, [m(4, 3, 2), m(5, 3)]))
+    call("cp", (None, [m(7, 1)]))
+    call("cp", (np.ones(5), [m(3, 5), m(2, 5), m(4, 5), m(1, 5)]))
+    call("tucker", (m(2, 3, 4), [m(5, 2), m(6, 3), m(7, 4)]))
+    call("tucker", (m(2, 3), [m(5, 2), m(6, 3)]))
+    call("tucker", (m(2, 3, 4), [m(5, 2), m(6, 3)]))
+    call("tucker", (m(2, 3), [m(5, 2), m(6, 3), m(7, 4)]))
+    call("tucker", (m(2, 3, 4), [m(5, 2), m(6, 4), m(7, 4)]))
+    call("tucker", (m(2,), [m(5, 2)]))
+    call("tucker", (m(3, 3, 3, 3), [m(4, 3)] * 4))
+    call("tucker", (m(3, 3, 3, 3), [m(4, 3)] * 3 + [m(4, 2)]))
+    return records
+
+
 def main():
+    if not REF or not os.path.isdir(os.path.join(REF, "tensorly")):
+        sys.exit("make_golden: set TENSORLY_REFERENCE to the TensorLy source tree "
+                 "(the directory that holds the tensorly package)")
     sys.path.insert(0, REF)
     import tensorly  # noqa: F401  (the reference)
+    cont = record_container_validation()
+    with open(os.path.join(HERE, "container_kats.pkl"), "wb") as f:
+        pickle.dump({"versions": _versions(), "records": cont}, f, protocol=4)
+    if "containers" in sys.argv[1:]:
+        print(f"{len(cont)} container records")
+        return
     kats = record_kats()
     with open(os.path.join(HERE, "tenalg_kats.pkl"), "wb") as f:
         pickle.dump({"versions": _versions(), "records": kats}, f, protocol=4)

@@ -81,7 +81,9 @@ def test_noalloc_matches_workspace_entry_point(gb300, shape, rank, dtype):
 def test_noalloc_rejects_oversized_plan(gb300):
     from tensorly_gb300 import _lib
     lib = _lib.lib()
-    shape, rank, mode = (10000, 8, 8), 128, 0
+    # one split's partial tile alone is 20000 x 128 x 8 B = 20.5 MB, so the
+    # plan exceeds the scratch whatever split count the device's SM count gives
+    shape, rank, mode = (20000, 8, 8), 128, 0
     code = _lib.TLGB_F64
     sh = _lib.i64_array(shape)
     nb = ctypes.c_size_t(0)
