@@ -60,6 +60,8 @@ def parse():
     p.add_argument("--train-samples", type=int, default=200_000,
                    help="learned: tensors the network is trained on (before the timed steps)")
     p.add_argument("--count", type=int, default=4096, help="batched: number of tensors")
+    p.add_argument("--no-extras", action="store_true",
+                   help="dense: headline line only (no plain-f32, batched and 128^4 sub-objects)")
     p.add_argument("--profile", action="store_true",
                    help="run only the warm-up and timed steps (for ncu launch lists)")
     return p.parse_args()
@@ -158,31 +160,45 @@ def cpu_sample(x, init, rank, sweeps):
 
 
 def run_reference(args):
+    """The reference arm: TensorLy's CPU path for this workload, timed on the
+    host cores.  TensorLy is pure Python and its source tree is not present
+    where the bench runs, so the arm runs the NumPy restatement of its
+    parafac (oracle/), which makes the same NumPy/LAPACK calls.  The steps
+    continue ONE run, as parafac does: ||X|| is computed once before the
+    timed steps (tensorly/decomposition/_cp.py:350) and each step carries the
+    factors on by `sweeps_per_step` sweeps."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
     from tensorly_gb300 import workloads
+    import oracle
     x, _ = workloads.dense_cp_large(size=args.size, rank=args.rank)
     rs = np.random.RandomState(0)
-    init = [rs.random_sample((args.size, args.rank)).astype(np.float32) for _ in range(3)]
+    factors = [rs.random_sample((args.size, args.rank)).astype(np.float32) for _ in range(3)]
+    weights = np.ones(args.rank, dtype=x.dtype)
     cores = os.cpu_count()
+    per_step = 2
+    norm_x = oracle.tensorly_oracle.norm(x)
     for _ in range(args.warmup):
-        cpu_sample(x, init, args.rank, 1)
+        weights, factors, _ = oracle.parafac_sweeps(x, weights, factors, per_step, norm_tensor=norm_x)
     times = []
     for _ in range(args.steps):
-        _, dt = cpu_sample(x, init, args.rank, 1)
-        times.append(dt)
-    value = args.steps / sum(times)
+        t0 = time.perf_counter()
+        weights, factors, _ = oracle.parafac_sweeps(x, weights, factors, per_step, norm_tensor=norm_x)
+        times.append(time.perf_counter() - t0)
+    value = per_step * args.steps / sum(times)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * sum(times) / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "impl": "reference",
             "config": {"workload": f"dense CP-ALS {args.size}^3 f32 rank {args.rank}",
-                       "step": "1 ALS sweep (bounded sample of the 50-sweep run)",
+                       "step": f"{per_step} ALS sweeps of one continuing run (bounded sample of "
+                               f"the {args.sweeps}-sweep run); ||X|| once, as parafac does",
                        "l2": "input larger than L2"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"{args.steps} sweeps of the NumPy restatement of "
-                                       "tensorly parafac (explicit KR + GEMM + LAPACK gesv)"},
+                             "sample": f"{per_step * args.steps} sweeps of the NumPy restatement "
+                                       "of tensorly parafac (explicit KR + GEMM + LAPACK gesv), "
+                                       "BLAS on all host cores"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -211,9 +227,8 @@ def launches_per_step(ndim, sweeps, refine, precision, rank=64):
     return n
 
 
-# DRAM bytes (read + write) per launch of the dominant kernel, from the ncu
-# captures summarised in profiles/mttkrp_tc_kernel_512_r64.md and
-# profiles/mttkrp_split_kernel_f32_512_r64.md (512^3, rank 64).
+# DRAM bytes (read + write) per launch of the dominant kernel at 512^3 rank 64,
+# from one-kernel ncu captures (dram__bytes_read.sum + dram__bytes_write.sum).
 NCU_TRAFFIC = {"native": 537485312 + 13983488, "bf16": 268757504 + 3681536}
 KERNEL = {"native": "mttkrp_split_kernel<float,64> + reduce (SIMT f32)",
           "bf16": "mttkrp_tc_kernel (tcgen05 bf16, TMA)"}
@@ -292,16 +307,49 @@ def run_gpu(args):
     # ---- accuracy against an f64 run from the same initial factors (the f64
     # GPU path matches the NumPy reference to 1e-10 in the parity tests)
     acc = None
+    f64_factors = None
+    errs64 = None
     if rank == 0:
         x64 = x.double()
         cp64, errs64 = tg.parafac(x64, args.rank, init=tg.CPTensor((None, [f.double() for f in init])),
                                   n_iter_max=args.sweeps, tol=0, return_errors=True,
                                   check_every=args.sweeps)
         del x64
+        f64_factors = [f.cpu().numpy() for f in cp64.factors]
         acc = {"final_rel_error": final_err, "f64_final_rel_error": errs64[-1],
                "rel_diff": abs(final_err - errs64[-1]) / errs64[-1],
                "congruence": congruence([f.double().cpu().numpy() for f in cp.factors],
-                                        [f.cpu().numpy() for f in cp64.factors])}
+                                        f64_factors)}
+
+    # ---- the plain FP32 GPU path on the same step (the metric's comparator):
+    # SIMT f32 MTTKRP, same normal equations, same 50 sweeps from the same init
+    fp32 = None
+    if rank == 0 and ws == 1 and args.precision == "bf16" and not args.no_extras:
+        kw32 = dict(kw, precision="native")
+
+        def step32():
+            return tg.parafac(x, args.rank, init=tg.CPTensor((None, init)), **kw32)
+
+        for _ in range(max(3, args.warmup // 2)):
+            step32()
+        n32 = max(3, args.steps // 4)
+        barrier()
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(st)
+        for _ in range(n32):
+            cp32, errs32 = step32()
+        f1.record(st)
+        barrier()
+        ms32 = f0.elapsed_time(f1) / n32
+        v32 = args.sweeps / (ms32 / 1000.0)
+        fp32 = {"value": v32, "unit": UNIT, "steps": n32, "ms_per_step": ms32,
+                "kernel": KERNEL["native"],
+                "final_rel_error": errs32[-1],
+                "rel_diff_vs_f64": abs(errs32[-1] - errs64[-1]) / errs64[-1],
+                "congruence_vs_f64": congruence([f.double().cpu().numpy() for f in cp32.factors],
+                                                f64_factors),
+                "bf16_over_fp32": value / v32}
 
     # ---- end to end through the public API with host buffers (pinned input,
     # results copied back each step)
@@ -365,6 +413,8 @@ def run_gpu(args):
                    "parallelism": "replicas" if ws > 1 else "single GPU",
                    "l2": "input 512 MiB > L2, no flush"},
         "accuracy_vs_f64": acc,
+        "fp32": fp32,
+        "bf16_over_fp32": fp32["bf16_over_fp32"] if fp32 else None,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if achieved else None, "peak_source": peak_kind,
                      "kernel": KERNEL[args.precision],
@@ -380,6 +430,14 @@ def run_gpu(args):
         "gpu_launches": launches_per_step(3, args.sweeps, args.refine, args.precision,
                                           args.rank) * args.steps,
     }
+    if ws == 1 and not args.no_extras:
+        # the metric's batched half (4096 uneven tensors) and the 128^4 four-way
+        # config, each measured here with its own clocks, accuracy and CPU sample
+        del x, x_host
+        torch.cuda.empty_cache()
+        line["batched"] = measure_batched(args, steps=3, warmup=3)
+        torch.cuda.empty_cache()
+        line["tucker_cp_128x4"] = measure_tucker(args, steps=3, warmup=3)
     print(json.dumps(line), flush=True)
 
 
@@ -406,17 +464,13 @@ def _batched_cpu_sample(xs, ranks, seeds, sweeps, n_sample):
 
 
 def run_batched(args):
-    import ctypes
-    import torch
-    import tensorly_gb300 as tg
-    from tensorly_gb300 import _lib
     ws_n, rank, _ = dist_env()
     if rank != 0:
         return
     sweeps = args.sweeps if args.sweeps != 50 else 100
-    xs, ranks, seeds = _batched_workload(args.count)
-    n = len(xs)
     if args.impl == "reference":
+        xs, ranks, seeds = _batched_workload(args.count)
+        n = len(xs)
         v, dt = _batched_cpu_sample(xs, ranks, seeds, sweeps, max(1, min(n, 16)))
         line = {"metric": BATCH_METRIC, "value": v, "unit": "decomps/s", "n_gpus": args.gpus,
                 "steps": 1, "warmup": 0, "ms_per_step": 1000.0 * dt, "higher_is_better": True,
@@ -430,6 +484,22 @@ def run_batched(args):
                         "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
+    print(json.dumps(measure_batched(args, args.steps, args.warmup)), flush=True)
+
+
+FP32_FFMA_PEAK_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12   # nominal, 2070 MHz
+
+
+def measure_batched(args, steps, warmup):
+    """C4 on the GPU: the batched persistent kernel over all tensors, tensors
+    resident; accuracy against per-tensor f64 oracle runs on a sample; e2e
+    from host tensors; plain per-tensor parafac on the same GPU; CPU sample."""
+    import torch
+    import tensorly_gb300 as tg
+    from tensorly_gb300 import _lib
+    sweeps = args.sweeps if args.sweeps != 50 else 100
+    xs, ranks, seeds = _batched_workload(args.count)
+    n = len(xs)
     tg.build() if not os.path.exists(_lib.library_path()) else None
     from tensorly_gb300 import autotune
     from tensorly_gb300.decomposition import BatchedProblem
@@ -443,7 +513,7 @@ def run_batched(args):
     def step():
         prob.run(sweeps)
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         step()
     torch.cuda.synchronize()
     ev0 = torch.cuda.Event(enable_timing=True)
@@ -451,18 +521,19 @@ def run_batched(args):
     clocks = ClockSampler(dev.index)
     clocks.start()
     ev0.record(st)
-    for _ in range(args.steps):
+    for _ in range(steps):
         step()
     ev1.record(st)
     torch.cuda.synchronize()
     clk = clocks.stop()
-    ms = ev0.elapsed_time(ev1) / args.steps
+    ms = ev0.elapsed_time(ev1) / steps
     value = n / (ms / 1000.0)
     # accuracy: final errors against per-tensor f64 oracle runs on a sample
     import oracle
     fin = final.cpu().numpy()
     rel = []
-    for t in range(min(n, 8)):
+    sample = sorted(set(np.linspace(0, n - 1, min(n, 16)).astype(int).tolist()))
+    for t in sample:
         init = oracle.random_cp(xs[t].shape, ranks[t], random_state=seeds[t])[1]
         x64 = xs[t].astype(np.float64)
         _, f64, _ = oracle.parafac_sweeps(x64, np.ones(ranks[t]), init, sweeps)
@@ -492,23 +563,27 @@ def run_batched(args):
     per_tensor = n_pt / (time.perf_counter() - p0)
     flops = sum(3 * 2 * x.size * r * sweeps for x, r in zip(xs, ranks))
     line = {"metric": BATCH_METRIC, "value": value, "unit": "decomps/s", "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "steps": steps, "warmup": warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
             "config": {"workload": f"{n} uneven 3-way tensors, dims 8-64, rank 4-16, "
                                    f"{sweeps} sweeps", "l2": "0.76 GB of tensors > L2",
                        "autotuned_threads": choice},
-            "accuracy_vs_f64": {"max_rel_diff_final_error_8": float(max(rel)),
-                                "median": float(np.median(rel))},
+            "accuracy_vs_f64": {"max_rel_diff_final_error": float(max(rel)),
+                                "median": float(np.median(rel)),
+                                "within_1e-4": f"{sum(r < 1e-4 for r in rel)}/{len(rel)}",
+                                "sample": f"{len(sample)} tensors spread over the batch, "
+                                          "per-tensor f64 oracle runs from the same init"},
             "mttkrp_tflops": flops / (ms / 1000.0) / 1e12,
+            "fp32_pipe_frac_of_nominal": flops / (ms / 1000.0) / 1e12 / FP32_FFMA_PEAK_TFLOPS,
             "per_tensor_gpu": {"value": per_tensor, "unit": "decomps/s",
                                "sample": f"{n_pt} tensors, one parafac call each (f32)"},
             "cpu_baseline": cpu,
             "e2e": {"value": n / e_s, "unit": "decomps/s",
                     "h2d_bytes_per_step": int(sum(x.nbytes for x in xs)),
                     "d2h_bytes_per_step": 0},
-            "clocks": clk, "gpu_launches": args.steps}
-    print(json.dumps(line), flush=True)
+            "clocks": clk, "gpu_launches": steps}
+    return line
 
 
 LEARNED_METRIC = ("time-to-fit decompositions/s, 10000 held-out 32^3 rank-8 f32 tensors, "
@@ -661,23 +736,18 @@ def _tucker_cpu_sample(x, n_iter):
 
 
 def run_tucker(args):
-    import torch
-    import tensorly_gb300 as tg
-    from tensorly_gb300 import _lib, workloads
     ws_n, rank, _ = dist_env()
     if rank != 0:
         return
-    n_iter = 20
-    x_np = workloads.cp_tucker_4way()
-    workload = ("128^4 f32: rank-32 CP + 16^4 Tucker (orthonormal factors) + 1 % noise; "
-                f"tucker(rank=[16]*4, n_iter_max={n_iter}, tol=0, init='svd')")
     if args.impl == "reference":
+        from tensorly_gb300 import workloads
+        x_np = workloads.cp_tucker_4way()
         v, dt = _tucker_cpu_sample(x_np, 1)
         line = {"metric": TUCKER_METRIC, "value": v, "unit": "iterations/s", "n_gpus": args.gpus,
                 "steps": 1, "warmup": 0, "ms_per_step": 1000.0 * dt, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "impl": "reference",
-                "config": {"workload": workload,
+                "config": {"workload": TUCKER_WORKLOAD,
                            "step": "1 HOOI iteration from init='random' (bounded sample)"},
                 "cpu_baseline": {"value": v, "unit": "iterations/s", "cores": os.cpu_count(),
                                  "kind": "port", "sample": "1 HOOI iteration, NumPy restatement"},
@@ -685,6 +755,22 @@ def run_tucker(args):
                         "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
+    print(json.dumps(measure_tucker(args, args.steps, args.warmup)), flush=True)
+
+
+TUCKER_WORKLOAD = ("128^4 f32: rank-32 CP + 16^4 Tucker (orthonormal factors) + 1 % noise; "
+                   "tucker(rank=[16]*4, n_iter_max=20, tol=0, init='svd')")
+
+
+def measure_tucker(args, steps, warmup):
+    """C3 on the GPU: tucker (HOOI, 20 iterations, SVD init) and 4-way CP
+    rank 32 (30 sweeps, bf16 and plain f32) on the 128^4 tensor."""
+    import torch
+    import tensorly_gb300 as tg
+    from tensorly_gb300 import _lib, workloads
+    n_iter = 20
+    x_np = workloads.cp_tucker_4way()
+    workload = TUCKER_WORKLOAD
     tg.build() if not os.path.exists(_lib.library_path()) else None
     dev = torch.device("cuda", torch.cuda.current_device())
     x = torch.from_numpy(x_np).to(dev)
@@ -693,19 +779,19 @@ def run_tucker(args):
     def step(it=n_iter):
         return tg.tucker(x, rank=[16] * 4, n_iter_max=it, tol=0, init="svd")
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         step()
     torch.cuda.synchronize()
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
     clocks = ClockSampler(dev.index)
     clocks.start()
     ev[0].record(st)
-    for _ in range(args.steps):
+    for _ in range(steps):
         core, factors = step()
     ev[1].record(st)
     torch.cuda.synchronize()
     clk = clocks.stop()
-    ms = ev[0].elapsed_time(ev[1]) / args.steps
+    ms = ev[0].elapsed_time(ev[1]) / steps
     ev[2].record(st)
     step(1)
     ev[3].record(st)
@@ -753,7 +839,7 @@ def run_tucker(args):
         cpu = {"value": v, "unit": "iterations/s", "cores": os.cpu_count(), "kind": "port",
                "sample": f"1 HOOI iteration from init='random' of the NumPy restatement ({dt:.1f} s)"}
     line = {"metric": TUCKER_METRIC, "value": n_iter / (ms / 1000.0), "unit": "iterations/s",
-            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "n_gpus": 1, "steps": steps, "warmup": warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
             "config": {"workload": workload, "l2": "1 GiB input > L2"},
@@ -771,8 +857,10 @@ def run_tucker(args):
                     "d2h_bytes_per_step": int(np.prod(np.shape(core_h))) * 4 + 4 * 128 * 16 * 4},
             # per call: norm (2), init 4 x (Gram tiles, finish, eig, sqrt), per iteration
             # 4 x (3 TTMs + the 4 SVD kernels) + the core's 4 TTMs + its norm (2)
-            "clocks": clk, "gpu_launches": (18 + 34 * n_iter) * args.steps}
-    print(json.dumps(line), flush=True)
+            "clocks": clk, "gpu_launches": (18 + 34 * n_iter) * steps}
+    return line
+
+
 
 
 def nncp_metric(n, r):

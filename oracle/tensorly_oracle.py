@@ -1139,13 +1139,17 @@ def error_calc_full(tensor, weights, factors):
     return norm(tensor - cp_to_tensor((weights, factors)))
 
 
-def parafac_sweeps(tensor, weights, factors, n_sweeps, l2_reg=0.0):
+def parafac_sweeps(tensor, weights, factors, n_sweeps, l2_reg=0.0, norm_tensor=None):
     """A bounded number of ALS sweeps from given factors (the body of
     tensorly/decomposition/_cp.py:394-440), used to time a CPU sample of a
-    long run.  Returns (weights, factors, errors)."""
+    long run.  ``norm_tensor``: ||X|| when the caller already has it (parafac
+    computes it once per run, tensorly/decomposition/_cp.py:350), so that
+    consecutive samples of one run do not recompute it.  Returns (weights,
+    factors, errors)."""
     rank = factors[0].shape[1]
     factors = [np.array(f, copy=True) for f in factors]
-    norm_tensor = norm(tensor)
+    if norm_tensor is None:
+        norm_tensor = norm(tensor)
     Id = np.eye(rank, dtype=tensor.dtype) * l2_reg if l2_reg else 0
     errors = []
     for _ in range(n_sweeps):

@@ -133,10 +133,8 @@ def parafac(tensor, rank, n_iter_max=100, init="svd", svd="truncated_svd",
         raise NotImplementedError("parafac with sparsity is not supported by tensorly_gb300")
     if mask is not None:
         raise NotImplementedError("masked parafac is not supported by tensorly_gb300")
-    if linesearch:
-        raise NotImplementedError("parafac line search is not supported by tensorly_gb300")
-    if orthogonalise:
-        raise NotImplementedError("parafac orthogonalise is not supported by tensorly_gb300")
+    if (linesearch or orthogonalise) and precision != "native":
+        raise NotImplementedError("parafac line search and orthogonalise run at native precision")
     if precision not in _PRECISIONS:
         raise ValueError(f"precision must be one of {sorted(_PRECISIONS)}")
     x, pl = to_device(tensor)
@@ -165,6 +163,14 @@ def parafac(tensor, rank, n_iter_max=100, init="svd", svd="truncated_svd",
     fixed_mask = 0
     for m in fixed:
         fixed_mask |= 1 << int(m)
+
+    if linesearch or orthogonalise:
+        return _parafac_host_loop(x, pl, rank, weights, factors, n_iter_max=n_iter_max,
+                                  orthogonalise=orthogonalise, tol=tol, verbose=verbose,
+                                  return_errors=return_errors, l2_reg=l2_reg,
+                                  cvg_criterion=cvg_criterion, fixed_mask=fixed_mask,
+                                  normalize_factors=normalize_factors, linesearch=linesearch,
+                                  callback=callback)
 
     lib = _lib.lib()
     opts = _lib.CpAlsOptions()
@@ -219,6 +225,111 @@ def parafac(tensor, rank, n_iter_max=100, init="svd", svd="truncated_svd",
     if verbose:
         for i, e in enumerate(rec_errors):
             print(f"iteration {i}, reconstruction error: {e}")
+    cp = _place_cp(weights, factors, pl)
+    if return_errors:
+        return cp, rec_errors
+    return cp
+
+
+def _parafac_host_loop(x, pl, rank, weights, factors, *, n_iter_max, orthogonalise, tol,
+                       verbose, return_errors, l2_reg, cvg_criterion, fixed_mask,
+                       normalize_factors, linesearch, callback):
+    """parafac with orthogonalisation and / or the line search
+    (tensorly/decomposition/_cp.py:392-401, :430-478): the reference's
+    iteration loop on the host around single-sweep ``tlgb_cp_als`` calls.
+
+    Per iteration: QR of each factor while ``iteration <= orthogonalise``
+    (``tlgb_qr``, LAPACK's sign convention); one ALS sweep in the library,
+    which also returns the error from the last mode's MTTKRP; on every even
+    iteration after the fifth, the extrapolated model
+    ``last + (current - last) * iteration ** (1 / acc_pow)`` (``tlgb_lerp``)
+    is scored by the explicit residual (``tlgb_cp_residual_norm``) and kept if
+    it lowers the error.  Line-search iterations record no error, as in the
+    reference.  The stop test and the normalisation follow ``:505-530``."""
+    from .parafac2 import _lerp, _qr
+    if orthogonalise and not isinstance(orthogonalise, int):
+        orthogonalise = n_iter_max
+    lib = _lib.lib()
+    opts = _lib.CpAlsOptions()
+    lib.tlgb_cp_als_default_options(ctypes.byref(opts))
+    opts.n_iter_max = 1
+    opts.tol = 0.0
+    opts.l2_reg = float(l2_reg) if l2_reg else 0.0
+    opts.cvg_criterion = 0
+    opts.normalize_factors = 0
+    opts.fixed_modes = fixed_mask
+    opts.precision = _lib.TLGB_PREC_NATIVE
+    opts.use_graph = 0
+    shape = _lib.i64_array(x.shape)
+    nbytes = ctypes.c_size_t(0)
+    _lib.check(lib.tlgb_cp_als_workspace_size(dtype_code(x), x.ndim, shape, rank,
+                                              ctypes.byref(opts), ctypes.byref(nbytes)))
+    ws = workspace(nbytes.value, x.device)
+    errs = (ctypes.c_double * 1)()
+    n_err = ctypes.c_int(0)
+
+    def sweep():
+        _lib.check(lib.tlgb_cp_als(dtype_code(x), ptr(x), x.ndim, shape, rank,
+                                   _lib.ptr_array([ptr(f) for f in factors]), ptr(weights),
+                                   ctypes.byref(opts), errs, ctypes.byref(n_err), ptr(ws),
+                                   ws.numel(), stream_of(x)))
+        return float(errs[0])
+
+    norm_tensor = _norm_on_device(x)
+    if callback is not None:
+        callback(_place_cp(weights.clone(), [f.clone() for f in factors], pl),
+                 _residual_norm(x, factors, weights) / norm_tensor)
+    acc_pow, acc_fail, max_fail = 2.0, 0, 4
+    rec_errors = []
+    rec_error = None
+    for iteration in range(n_iter_max):
+        if orthogonalise and iteration <= orthogonalise:
+            factors = [_qr(f) if min(f.shape) >= rank else f for f in factors]
+        if linesearch and iteration % 2 == 0:
+            factors_last = [f.clone() for f in factors]
+            weights_last = weights.clone()
+        fast_error = sweep()
+        line_iter = bool(linesearch and iteration % 2 == 0 and iteration > 5)
+        if not line_iter:
+            unnorm = fast_error * norm_tensor
+        else:
+            jump = iteration ** (1.0 / acc_pow)
+            new_weights = _lerp(weights_last, weights, jump)
+            new_factors = [_lerp(a, b, jump) for a, b in zip(factors_last, factors)]
+            new_error = _residual_norm(x, new_factors, new_weights)
+            if new_error / norm_tensor < rec_errors[-1]:
+                factors, weights = new_factors, new_weights
+                unnorm = new_error
+                acc_fail = 0
+                if verbose:
+                    print(f"Accepted line search jump of {jump}.")
+            else:
+                unnorm = fast_error * norm_tensor
+                acc_fail += 1
+                if verbose:
+                    print(f"Line search failed for jump of {jump}.")
+                if acc_fail == max_fail:
+                    acc_pow += 1.0
+                    acc_fail = 0
+        if not line_iter:
+            rec_error = unnorm / norm_tensor
+            rec_errors.append(rec_error)
+        if callback is not None:
+            ret = callback(_place_cp(weights.clone(), [f.clone() for f in factors], pl),
+                           rec_error)
+            if ret is True:
+                break
+        if tol and iteration >= 1:
+            dec = rec_errors[-2] - rec_errors[-1]
+            if verbose:
+                print(f"iteration {iteration}, reconstruction error: {rec_error}, "
+                      f"decrease = {dec}")
+            stop = abs(dec) < tol if cvg_criterion == "abs_rec_error" else dec < tol
+            if stop:
+                break
+        if normalize_factors:
+            weights, factors = cp_normalize((weights, factors))
+            factors = list(factors)
     cp = _place_cp(weights, factors, pl)
     if return_errors:
         return cp, rec_errors

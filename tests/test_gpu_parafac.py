@@ -133,12 +133,29 @@ def test_cp_estimator(gb300, golden):
     assert repr(est) == "CP decomposition of rank 8."
 
 
+@pytest.mark.parametrize("case", ["cp_linesearch", "cp_orth"])
+def test_parafac_linesearch_and_orthogonalise_match_reference(gb300, golden, case):
+    """The line search (tensorly/decomposition/_cp.py:398-401, :447-478) and the
+    QR orthogonalisation of the first sweeps (:392-397), f64, against the
+    reference's runs: same error list (line-search iterations record none),
+    weights and factors to 1e-10."""
+    run = golden["runs"][case]
+    (w, f), errs = run_case(gb300, run)
+    assert len(errs) == len(run["errors"]), "different number of recorded errors"
+    np.testing.assert_allclose(errs, run["errors"], rtol=1e-10, atol=1e-13)
+    assert rel(host(w), run["weights"]) < 1e-10
+    for a, b in zip(f, run["factors"]):
+        assert rel(host(a), b) < 1e-10
+
+
 def test_unsupported_options_raise(gb300):
     x = torch.rand(4, 5, 6, device="cuda", dtype=torch.float64)
-    for kw in ({"mask": torch.ones_like(x)}, {"sparsity": 0.1}, {"linesearch": True},
-               {"orthogonalise": True}):
+    for kw in ({"mask": torch.ones_like(x)}, {"sparsity": 0.1}):
         with pytest.raises(NotImplementedError):
             gb300.parafac(x, 2, init="random", **kw)
+    for kw in ({"linesearch": True}, {"orthogonalise": True}):
+        with pytest.raises(NotImplementedError):
+            gb300.parafac(x.float(), 2, init="random", precision="bf16", **kw)
     with pytest.raises(ValueError):
         gb300.parafac(x, 2, init="bogus")
     with pytest.raises(TypeError):
