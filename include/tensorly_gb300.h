@@ -128,6 +128,11 @@ int tlgb_mttkrp_bf16(const void* X, int ndim, const int64_t* shape, const void* 
  * "refine_simt" = 1 makes the f32
  * refinement sweeps of TLGB_PREC_BF16 use the SIMT f32 MTTKRP instead of the
  * tensor-core one on the exact three-plane bf16 split of the f32 tensor;
+ * "f64_factorize" = 1
+ * sends every CP-ALS normal-equation factorisation to the f64 Cholesky (LU
+ * when Cholesky fails) that otherwise serves only ill-conditioned V;
+ * "no_pdl" = 1 launches the kernels of a CP-ALS sweep without programmatic
+ * dependent launch (each then starts only when its predecessor has ended);
  * "batched_threads_small" / "_medium" / "_large" = threads per CTA (128, 256
  * or 512; 4, 2 or 1 CTAs per SM) of tlgb_cp_als_batched for the tensors
  * whose padded size fits 128-, 256-thread CTAs' shared memory, or neither.
@@ -324,17 +329,22 @@ int tlgb_cp_nn_mu(int dtype, const void* X, int ndim, const int64_t* shape, void
 
 /*
  * Non-negative CP by HALS: the loop of tensorly/decomposition/_nn_cp.py:186-377
- * (non_negative_parafac_hals with nn_modes 'all', weights all one,
- * normalize_factors=False) and its inner solver tensorly/solvers/nnls.py:5-150
- * (hals_nnls, 100 iterations or, with exact, 50000 at tol 1e-16).  Arguments
- * as tlgb_cp_nn_mu; sparsity: host array of ndim coefficients (NaN = none) or
- * NULL.  The workspace is tlgb_cp_nn_mu_workspace_size's.
+ * (non_negative_parafac_hals) and its inner solver
+ * tensorly/solvers/nnls.py:5-150 (hals_nnls, 100 iterations or, with exact,
+ * 50000 at tol 1e-16).  Arguments as tlgb_cp_nn_mu, plus: weights: device,
+ * rank entries, in/out, or NULL for weights all one (required when
+ * normalize_factors is set); nn_modes_mask: bit k set = mode k is updated by
+ * HALS, else by the least-squares solve of CP-ALS (the reference's nn_modes);
+ * normalize_factors: cp_normalize after every updated mode but the last and
+ * after every iteration.  sparsity: host array of ndim coefficients (NaN =
+ * none) or NULL.  The workspace is tlgb_cp_nn_mu_workspace_size's.
  */
 int tlgb_cp_nn_hals(int dtype, const void* X, int ndim, const int64_t* shape,
-                    void* const* factors, int64_t rank, const int* free_modes, int n_free,
-                    int n_iter_max, double tol, int cvg_criterion, const double* sparsity,
-                    int exact, double* errors, int* n_errors, void* workspace,
-                    size_t workspace_bytes, void* stream);
+                    void* const* factors, void* weights, int64_t rank, const int* free_modes,
+                    int n_free, unsigned nn_modes_mask, int normalize_factors, int n_iter_max,
+                    double tol, int cvg_criterion, const double* sparsity, int exact,
+                    double* errors, int* n_errors, void* workspace, size_t workspace_bytes,
+                    void* stream);
 
 /*
  * Pieces of the non-negative SVD (NNDSVD, tensorly/tenalg/svd.py:68-134):
@@ -431,6 +441,42 @@ int tlgb_cp_to_tensor_workspace_size(int dtype, int ndim, const int64_t* shape, 
 int tlgb_cp_to_tensor(int dtype, int ndim, const int64_t* shape, int64_t rank,
                       const void* const* factors, const void* weights, const void* mask,
                       void* out, void* workspace, size_t workspace_bytes, void* stream);
+
+/*
+ * mask_impute: x = x * mask + rec * (1 - mask) in place (n entries, x, mask
+ * and rec in the same dtype), and out[0] = ||x||_F, out[1] = ||x - rec||_F
+ * (two doubles, device) of the refilled tensor.  Workspace:
+ * tlgb_mask_impute_workspace_bytes().  Replaces the mask branch of
+ * error_calc, tensorly/decomposition/_cp.py:194-207 (with rec =
+ * cp_to_tensor((weights, factors))), and the refill at :441-446.
+ */
+size_t tlgb_mask_impute_workspace_bytes(void);
+int tlgb_mask_impute(int dtype, void* x, const void* mask, const void* rec, int64_t n,
+                     double* out, void* workspace, size_t workspace_bytes, void* stream);
+
+/*
+ * mask_where: x = where(mask == 0, rec, x) in place, or the constant `fill`
+ * in place of rec when rec is NULL (n entries, x, mask and rec in one dtype).
+ * Replaces _update_imputed of tensorly/decomposition/_parafac2.py:21-65
+ * (the "factors" and "mode-2" refills of masked slices).
+ */
+int tlgb_mask_where(int dtype, void* x, const void* mask, const void* rec, double fill,
+                    int64_t n, void* stream);
+
+/*
+ * masked_sq_diff: *out (one double, device) = sum((mask * x - mask * rec)^2),
+ * the per-slice term of the masked error of
+ * tensorly/decomposition/_parafac2.py:389-396.  Workspace:
+ * tlgb_dot_workspace_bytes().
+ */
+int tlgb_masked_sq_diff(int dtype, const void* x, const void* mask, const void* rec, int64_t n,
+                        double* out, void* workspace, size_t workspace_bytes, void* stream);
+
+/*
+ * clip_min: x = max(x, lo) in place (NaN kept); tl.clip(x, 0) of the PARAFAC2
+ * line search for non-negative modes (tensorly/decomposition/_parafac2.py:282-286).
+ */
+int tlgb_clip_min(int dtype, void* x, int64_t n, double lo, void* stream);
 
 /*
  * cp_residual_norm: *out (one double, device) = ||X - [[weights; factors]]||_F

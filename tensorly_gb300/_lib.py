@@ -143,10 +143,11 @@ SIGNATURES = [
       ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int), ctypes.c_void_p,
       ctypes.c_size_t, ctypes.c_void_p]),
     ("tlgb_cp_nn_hals", ctypes.c_int,
-     [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, _c_i64p, _c_vpp, ctypes.c_int64,
-      ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
-      ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.POINTER(ctypes.c_double),
-      ctypes.POINTER(ctypes.c_int), ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+     [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, _c_i64p, _c_vpp, ctypes.c_void_p,
+      ctypes.c_int64, ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.c_uint, ctypes.c_int,
+      ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+      ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int),
+      ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     ("tlgb_sum", ctypes.c_int,
      [ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
       ctypes.c_size_t, ctypes.c_void_p]),
@@ -256,6 +257,18 @@ SIGNATURES = [
       ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     ("tlgb_inv_sqrt", ctypes.c_int,
      [ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p]),
+    ("tlgb_mask_where", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double,
+      ctypes.c_int64, ctypes.c_void_p]),
+    ("tlgb_masked_sq_diff", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    ("tlgb_clip_min", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_double, ctypes.c_void_p]),
+    ("tlgb_mask_impute_workspace_bytes", ctypes.c_size_t, []),
+    ("tlgb_mask_impute", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     ("tlgb_lerp", ctypes.c_int,
      [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_double,
       ctypes.c_void_p, ctypes.c_void_p]),

@@ -11,6 +11,7 @@
 // pivoting (what gesv does), and an exactly zero LU pivot reports
 // TLGB_ESINGULAR.  All of this runs in f64 regardless of the tensor dtype.
 #include "als_kernels.cuh"
+#include "mttkrp_tc.cuh"
 
 namespace tlgb {
 namespace {
@@ -578,6 +579,8 @@ k_solve(const T* __restrict__ partial, int splits, int64_t I, int R_in,
         __nv_bfloat16* A_bt, double* gpart, double* ipart, AlsCtrl* ctrl, int64_t rpb,
         int mats_in_smem, int max_passes) {
   const int R = (RT > 0) ? RT : R_in;
+  griddep_wait();   // the MTTKRP partials (programmatic launch inside a sweep)
+  griddep_launch_dependents();
   if (ctrl->done) return;
   extern __shared__ double sm[];
   const int RR = R * R;
@@ -929,6 +932,7 @@ __global__ void __launch_bounds__(256)
 k_gram_reduce_fit(const double* __restrict__ gpart, int nparts, int R, double* G_all, int mode,
                   int ndim, int df, const T* w, const double* ipart, int nip, double* fpart,
                   AlsCtrl* ctrl, double* errors, int n_iter_max, double tol, int crit) {
+  griddep_wait();   // the solve's Gram and <M, A> partials
   if (ctrl->done) return;
   const int RR = R * R;
   const double t = gram_reduce_block(gpart, nparts, R, G_all + (int64_t)mode * RR, df);
@@ -1125,13 +1129,20 @@ static void launch_fast(const double* G, int ndim, int mode, int R, const T* w, 
                                                              ctrl);
 }
 
+// Hands every factorisation to the f64 kernel (the "f64_factorize" tuning key).
+__global__ void k_force_f64_factorize(AlsCtrl* ctrl) {
+  if (!ctrl->done && threadIdx.x == 0) ctrl->fac_kind = 3;
+}
+
 template <typename T>
 int als_launch_factorize(const double* G, int ndim, int mode, int R, const T* weights,
                          double l2_reg, double* fac, int* perm, double* vmat, float* w32,
                          AlsCtrl* ctrl, cudaStream_t st) {
   int rc = als_prepare(TypeCode<T>::value);
   if (rc) return rc;
-  if (R <= 32)
+  if (tc_tuning().f64_factorize)
+    k_force_f64_factorize<<<1, 32, 0, st>>>(ctrl);
+  else if (R <= 32)
     launch_fast<T, 8, 16, 4, 2>(G, ndim, mode, R, weights, l2_reg, vmat, w32, ctrl, st);
   else if (R <= 64)
     launch_fast<T, 16, 16, 4, 4>(G, ndim, mode, R, weights, l2_reg, vmat, w32, ctrl, st);
@@ -1161,7 +1172,7 @@ template <typename T>
 int als_launch_solve(const T* partial, int splits, int64_t I, int R, const double* fac,
                      const int* perm, const double* vmat, const float* w32, T* A,
                      __nv_bfloat16* A_bt, double* gpart, double* ipart, AlsCtrl* ctrl,
-                     int max_passes, int* nblocks, cudaStream_t st) {
+                     int max_passes, int* nblocks, cudaStream_t st, bool pdl) {
   const int nb = solve_blocks_for(I);
   const int64_t rpb = ceil_div(I, nb);
   const int nbe = (int)ceil_div(I, rpb);
@@ -1169,17 +1180,17 @@ int als_launch_solve(const T* partial, int splits, int64_t I, int R, const doubl
   if (rc) return rc;
   const int mats = R <= kSolveDfMaxRank ? 1 : 0;
   if (R == 64)
-    k_solve<T, 64><<<nbe, kSolveThreads, solve_smem(R), st>>>(
-        partial, splits, I, R, fac, perm, vmat, w32, A, A_bt, gpart, ipart, ctrl, rpb, mats,
-        max_passes);
+    TLGB_CUDA_TRY(launch_maybe_pdl(pdl, k_solve<T, 64>, dim3(nbe), dim3(kSolveThreads),
+                                   solve_smem(R), st, partial, splits, I, R, fac, perm, vmat,
+                                   w32, A, A_bt, gpart, ipart, ctrl, rpb, mats, max_passes));
   else if (R == 32)
-    k_solve<T, 32><<<nbe, kSolveThreads, solve_smem(R), st>>>(
-        partial, splits, I, R, fac, perm, vmat, w32, A, A_bt, gpart, ipart, ctrl, rpb, mats,
-        max_passes);
+    TLGB_CUDA_TRY(launch_maybe_pdl(pdl, k_solve<T, 32>, dim3(nbe), dim3(kSolveThreads),
+                                   solve_smem(R), st, partial, splits, I, R, fac, perm, vmat,
+                                   w32, A, A_bt, gpart, ipart, ctrl, rpb, mats, max_passes));
   else
-    k_solve<T, 0><<<nbe, kSolveThreads, solve_smem(R), st>>>(
-        partial, splits, I, R, fac, perm, vmat, w32, A, A_bt, gpart, ipart, ctrl, rpb, mats,
-        max_passes);
+    TLGB_CUDA_TRY(launch_maybe_pdl(pdl, k_solve<T, 0>, dim3(nbe), dim3(kSolveThreads),
+                                   solve_smem(R), st, partial, splits, I, R, fac, perm, vmat,
+                                   w32, A, A_bt, gpart, ipart, ctrl, rpb, mats, max_passes));
   TLGB_LAUNCH_CHECK();
   *nblocks = nbe;
   return TLGB_OK;
@@ -1199,12 +1210,12 @@ template <typename T>
 int als_launch_gram_reduce_fit(const double* gpart, int nparts, int R, double* G_all, int mode,
                                int ndim, int df, const T* weights, const double* ipart, int nip,
                                double* fpart, AlsCtrl* ctrl, double* errors, int n_iter_max,
-                               double tol, int cvg_criterion, cudaStream_t st) {
+                               double tol, int cvg_criterion, cudaStream_t st, bool pdl) {
   const int RR = R * R;
-  k_gram_reduce_fit<T><<<(int)ceil_div(RR, 32), 256, 0, st>>>(
-      gpart, nparts, R, G_all, mode, ndim, df, weights, ipart, nip, fpart, ctrl, errors,
-      n_iter_max, tol, cvg_criterion);
-  TLGB_LAUNCH_CHECK();
+  TLGB_CUDA_TRY(launch_maybe_pdl(pdl, k_gram_reduce_fit<T>, dim3((unsigned)ceil_div(RR, 32)),
+                                 dim3(256), 0, st, gpart, nparts, R, G_all, mode, ndim, df,
+                                 weights, ipart, nip, fpart, ctrl, errors, n_iter_max, tol,
+                                 cvg_criterion));
   return TLGB_OK;
 }
 
@@ -1300,12 +1311,12 @@ int als_prepare(int dtype) {
                                        cudaStream_t);                                        \
   template int als_launch_solve<T>(const T*, int, int64_t, int, const double*, const int*,   \
                                    const double*, const float*, T*, __nv_bfloat16*, double*, \
-                                   double*, AlsCtrl*, int, int*, cudaStream_t);              \
+                                   double*, AlsCtrl*, int, int*, cudaStream_t, bool);        \
   template int als_launch_fit<T>(const double*, int, int, const T*, const double*, int,      \
                                  AlsCtrl*, double*, int, double, int, cudaStream_t);         \
   template int als_launch_gram_reduce_fit<T>(const double*, int, int, double*, int, int, int,  \
                                              const T*, const double*, int, double*, AlsCtrl*, \
-                                             double*, int, double, int, cudaStream_t);       \
+                                             double*, int, double, int, cudaStream_t, bool); \
   template int als_launch_normalize<T>(T* const*, const int64_t*, int, int, T*, const int*,  \
                                        cudaStream_t);
 TLGB_INST(float)

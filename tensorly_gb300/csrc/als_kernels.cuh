@@ -35,14 +35,15 @@ int als_launch_factorize(const double* G, int ndim, int mode, int R, const T* we
 
 // Sums the MTTKRP partials of each row, solves with the factorisation, stores
 // the factor (and optionally its bf16 transpose), and writes per-CTA Gram and
-// <M, A> partial sums.  Returns the number of CTAs used via *nblocks.
+// <M, A> partial sums.  Returns the number of CTAs used via *nblocks.  pdl:
+// programmatic dependent launch behind the MTTKRP that wrote `partial`.
 template <typename T>
 // max_passes: refinement passes allowed on the f32-inverse path (each pass
 // stops early once the correction is below 1e-12 of the solution).
 int als_launch_solve(const T* partial, int splits, int64_t I, int R, const double* fac,
                      const int* perm, const double* vmat, const float* w32, T* A,
                      __nv_bfloat16* A_bf16_t, double* gpart, double* ipart, AlsCtrl* ctrl,
-                     int max_passes, int* nblocks, cudaStream_t st);
+                     int max_passes, int* nblocks, cudaStream_t st, bool pdl = false);
 
 constexpr int kIrMaxPasses = 4;
 
@@ -64,7 +65,7 @@ template <typename T>
 int als_launch_gram_reduce_fit(const double* gpart, int nparts, int R, double* G_all, int mode,
                                int ndim, int df, const T* weights, const double* ipart, int nip,
                                double* fpart, AlsCtrl* ctrl, double* errors, int n_iter_max,
-                               double tol, int cvg_criterion, cudaStream_t st);
+                               double tol, int cvg_criterion, cudaStream_t st, bool pdl = false);
 
 template <typename T>
 int als_launch_normalize(T* const* factors, const int64_t* rows, int ndim, int R, T* weights,

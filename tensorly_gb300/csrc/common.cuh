@@ -19,6 +19,33 @@ void clear_error();
 // Tuning keys of the batched CP-ALS kernel variants (batched.cu).
 int batched_set_tuning(const std::string& key, int value);
 
+// Programmatic dependent launch.  A kernel launched by launch_maybe_pdl(true,
+// ...) may start while the previous kernel of its stream is still running;
+// it must call griddep_wait() before it reads anything an earlier kernel
+// wrote (or writes anything an earlier kernel reads).  griddep_wait() is a
+// no-op in a kernel launched the ordinary way.  griddep_launch_dependents()
+// lets the next such kernel of the stream be scheduled early.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void griddep_launch_dependents() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_maybe_pdl(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block,
+                                    size_t smem, cudaStream_t st, Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<Args&&>(args)...);
+}
+
 // Number of SMs of the current device (cached per device).
 int sm_count();
 int current_device();

@@ -79,7 +79,7 @@ int layout(int dtype, const Shape& sh, int64_t R, const tlgb_cp_als_options& o,
   B->ipart = c.take<double>(nparts);
   B->sumsq_part = c.take<double>(kSumsqBlocks);
   B->probe = c.take<double>(1);
-  B->fpart = c.take<double>((size_t)ceil_div(RR, 32));
+  B->fpart = c.take<double>((size_t)ceil_div(RR, 32));   // per-block fit terms of k_gram_reduce_fit
   B->xbf = nullptr;
   B->xsplit[0] = B->xsplit[1] = nullptr;
   for (int k = 0; k < kMaxModes; ++k) B->fbt[k] = nullptr;
@@ -138,12 +138,14 @@ int make_plans(int dtype, const Shape& sh, int64_t R, const tlgb_cp_als_options&
     if (mixed) {
       rc = mttkrp_tc_make_plan(sh, R, k, 2, kAuxSms, &P->tc[k]);
       if (rc) return rc;
+      P->tc[k].pdl = 1;   // programmatic launch behind the previous solve
     }
     if (P->refine_tc) {
       for (int j = 0; j < 3; ++j) {
         rc = mttkrp_tc_make_plan(sh, R, k, 3 - j, kAuxSms, &P->tcr[k][j]);
         if (rc) return rc;
         if (!P->tcr[k][j].valid) P->refine_tc = false;
+        P->tcr[k][j].pdl = 1;
       }
     }
   }
@@ -197,6 +199,10 @@ struct Runner {
     // MTTKRP is unweighted there; kept for parity.
     const T* mw = (N == 2) ? nullptr : weights;
     const int df = (sizeof(T) == 4 && R <= kSolveDfMaxRank) ? 1 : 0;
+    // Main-stream kernels that follow a kernel of this sweep start by
+    // programmatic dependent launch: they are scheduled while their
+    // predecessor drains and wait for it on the device.
+    const bool pdl = !tc_tuning().no_pdl;
     // The Gram reduction of a mode other than the last runs on the aux
     // stream in front of the next mode's factorisation (the only consumer of
     // that Gram), so the next MTTKRP does not wait for it.
@@ -260,14 +266,13 @@ struct Runner {
                                last ? B.ipart : nullptr, B.ctrl,
                                // the bf16 MTTKRP is accurate to ~1e-6, so one refinement
                                // pass (solve error ~(cond * 6e-8)^2) is enough there
-                               (tc && P->tc[mode].valid) ? 1 : kIrMaxPasses, &nb, st);
+                               (tc && P->tc[mode].valid) ? 1 : kIrMaxPasses, &nb, st, pdl);
       if (rc) return rc;
       if (last) last_nb = nb;
       if (last) {   // the last mode's Gram reduction also computes the fit (in order)
         rc = als_launch_gram_reduce_fit<T>(B.gpart, nb, (int)R, B.G, mode, N, df, weights,
-                                           B.ipart, nb, B.fpart, B.ctrl, B.errors, o.n_iter_max,
-                                           o.tol,
-                                           o.cvg_criterion, st);
+                                           B.ipart, nb, B.fpart, B.ctrl, B.errors,
+                                           o.n_iter_max, o.tol, o.cvg_criterion, st, pdl);
         if (rc) return rc;
       } else {      // reduced on the aux stream before the next factorisation
         pending_mode = mode;

@@ -223,7 +223,6 @@ template <int RP, bool MN, int NPL>
 __global__ void __launch_bounds__(kThreads, 1)
 mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmF,
                  const TcArgs a) {
-  if (a.skip && *a.skip) return;
   constexpr int NB = NPL * RP;             // MMA N (one RP-wide block per factor plane)
   constexpr int TS = tmem_stride(NB);      // TMEM columns per accumulator buffer
   static_assert(NB <= 256 && 2 * TS <= 512, "accumulators exceed one MMA or TMEM");
@@ -255,6 +254,11 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant_
   // partial tile index: every (group, split) CTA of an output tile writes its own
   const int64_t pidx = (int64_t)cg * a.gsplits + split;
 
+  if (threadIdx.x == 32) {
+    // the tensor maps live in parameter space: fetch them while the CTA sets up
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmX)) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmF)) : "memory");
+  }
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; ++s) {
       mbar_init(&full[s], 1);
@@ -280,18 +284,17 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant_
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
   bool failed = false;
+  // The next kernel of the stream may be scheduled now.  Everything below
+  // that reads an earlier kernel's output (the factors, the stop flag) or
+  // writes the partial tiles (which the previous solve reads) comes after
+  // griddep_wait(); only the tensor tiles of the first ring stages are
+  // fetched before it (the tensor is never written during a run).
+  griddep_launch_dependents();
 
   if (t_begin < t_end) {
     if (warp == 0) {
       // ------------------------------------------------------------ producer
       if (lane == 0) {
-        mbar_expect_tx(bfull, (uint32_t)b_bytes);
-        for (int kc = 0; kc < KC; ++kc) {
-          unsigned char* dst = sB + kc * NB * 128;
-#pragma unroll
-          for (int pl = 0; pl < NPL; ++pl)   // rows of factor plane pl
-            tma_load_3d(dst + pl * RP * 128, &tmF, bfull, (kc0 + kc) * kChunk, 0, pl);
-        }
         // Coordinates advance incrementally (no 64-bit division per step:
         // this single thread's issue rate bounds the whole CTA's bandwidth).
         const int64_t o0 = t_begin / KC;
@@ -300,8 +303,8 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant_
         int stage = 0;
         uint32_t phase = 0;
         int64_t i = 0;
-        for (int64_t t = t_begin; t < t_end; ++t, ++i) {
-          if (!mbar_wait(&empty[stage], phase ^ 1u, a.err, failed)) break;
+        auto issue = [&]() -> bool {   // the tensor tile of the next step
+          if (!mbar_wait(&empty[stage], phase ^ 1u, a.err, failed)) return false;
           mbar_expect_tx(&full[stage], kStageBytes);
           unsigned char* dst = sA + stage * kStageBytes;
           const int cx = (kc0 + kc) * kChunk;
@@ -316,9 +319,28 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant_
             if (++c2 == a.g2) { c2 = 0; ++c3; }
           }
           if (++stage == S) { stage = 0; phase ^= 1u; }
+          ++i;
+          return true;
+        };
+        const int64_t pre = min((int64_t)S, t_end - t_begin);
+        int64_t t = t_begin;
+        for (; t < t_begin + pre; ++t)
+          if (!issue()) break;
+        griddep_wait();
+        const bool skipped = a.skip && *a.skip;
+        if (!skipped && !failed) {
+          mbar_expect_tx(bfull, (uint32_t)b_bytes);
+          for (int kcb = 0; kcb < KC; ++kcb) {
+            unsigned char* dst = sB + kcb * NB * 128;
+#pragma unroll
+            for (int pl = 0; pl < NPL; ++pl)   // rows of factor plane pl
+              tma_load_3d(dst + pl * RP * 128, &tmF, bfull, (kc0 + kcb) * kChunk, 0, pl);
+          }
+          for (; t < t_end; ++t)
+            if (!issue()) break;
+          // every issued copy has landed before the CTA may exit
+          mbar_drain(bfull, 0);
         }
-        // every issued copy has landed before the CTA may exit
-        mbar_drain(bfull, 0);
         {
           const int n = (int)(i < S ? i : S);
           int st_j = stage, ph_j = (int)phase;   // walk back over the last n issued steps
@@ -330,7 +352,9 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant_
       }
     } else if (warp == 1) {
       // ------------------------------------------------------------ MMA issue
-      if (lane == 0) {
+      griddep_wait();
+      const bool skipped = a.skip && *a.skip;
+      if (lane == 0 && !skipped) {
         constexpr uint32_t idesc = make_idesc(NB, MN ? 1 : 0);
         mbar_wait(bfull, 0, a.err, failed);
         int64_t oc = 0;
@@ -371,92 +395,115 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant_
       }
     } else {
       // ------------------------------------------------------------ epilogue
-      const int e = threadIdx.x - 64;            // 0..127
-      const int q = warp & 3;                    // TMEM lane quarter of this warp
-      const int row = 32 * q + lane;
-      float acc[RP];
+      griddep_wait();   // the scales read the factors; the partial tiles are rewritten
+      if (!(a.skip && *a.skip)) {
+        const int e = threadIdx.x - 64;            // 0..127
+        const int q = warp & 3;                    // TMEM lane quarter of this warp
+        const int row = 32 * q + lane;
+        float acc[RP];
 #pragma unroll
-      for (int r = 0; r < RP; ++r) acc[r] = 0.f;
-      const int64_t o_first = t_begin / KC, o_last = (t_end - 1) / KC;
-      // s(o, r) = w_r * prod_{outer k} A_k(i_k, r) for r = e (one entry per thread)
-      // outer multi-index of the next slice, advanced with carries (no division)
-      int64_t nidx[kMaxModes];
-      {
-        int64_t rem = o_first;
-        for (int k = a.n_outer - 1; k >= 0; --k) {
-          nidx[k] = rem % a.outer_dim[k];
-          rem /= a.outer_dim[k];
+        for (int r = 0; r < RP; ++r) acc[r] = 0.f;
+        const int64_t o_first = t_begin / KC, o_last = (t_end - 1) / KC;
+        // s(o, r) = w_r * prod_{outer k} A_k(i_k, r) for r = e (one entry per thread)
+        // outer multi-index of the next slice, advanced with carries (no division)
+        int64_t nidx[kMaxModes];
+        {
+          int64_t rem = o_first;
+          for (int k = a.n_outer - 1; k >= 0; --k) {
+            nidx[k] = rem % a.outer_dim[k];
+            rem /= a.outer_dim[k];
+          }
         }
-      }
-      auto scale_of = [&](int64_t) -> float {
-        float s = 0.f;
-        if (e < a.R) {
-          s = a.weights ? a.weights[e] : 1.f;
-          for (int k = 0; k < a.n_outer; ++k) s *= a.outer_f[k][nidx[k] * a.R + e];
-        }
-        for (int k = a.n_outer - 1; k >= 0; --k) {
-          if (++nidx[k] < a.outer_dim[k]) break;
-          nidx[k] = 0;
-        }
-        return s;
-      };
-      float s_next = (e < RP) ? scale_of(o_first) : 0.f;
-      int64_t oc = 0;
-      for (int64_t o = o_first; o <= o_last; ++o, ++oc) {
-        const int buf = (int)(oc & 1);
-        if (e < RP) s_sm[buf * RP + e] = s_next;
-        // the next slice's scale loads overlap this slice's TMEM traffic
-        if (e < RP && o < o_last) s_next = scale_of(o + 1);
-        if (e == 0) ep_ok[buf] = mbar_wait(&dfull[buf], (uint32_t)((oc >> 1) & 1), a.err, failed) ? 1 : 0;
-        asm volatile("bar.sync 1, 128;" ::: "memory");
-        if (!ep_ok[buf]) break;  // uniform across the four epilogue warps
-        __syncwarp();            // tcgen05.ld is warp-collective
-        tc_fence_after();
-        const uint32_t lane_addr = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(buf * TS);
-        if constexpr (RP >= 32) {
+        auto scale_of = [&](int64_t) -> float {
+          float s = 0.f;
+          if (e < a.R) {
+            s = a.weights ? a.weights[e] : 1.f;
+            for (int k = 0; k < a.n_outer; ++k) s *= a.outer_f[k][nidx[k] * a.R + e];
+          }
+          for (int k = a.n_outer - 1; k >= 0; --k) {
+            if (++nidx[k] < a.outer_dim[k]) break;
+            nidx[k] = 0;
+          }
+          return s;
+        };
+        float s_next = (e < RP) ? scale_of(o_first) : 0.f;
+        bool ep_broken = false;   // a wait expired (the same value in every epilogue thread)
+        int64_t oc = 0;
+        for (int64_t o = o_first; o <= o_last; ++o, ++oc) {
+          const int buf = (int)(oc & 1);
+          if (e < RP) s_sm[buf * RP + e] = s_next;
+          // the next slice's scale loads overlap this slice's TMEM traffic
+          if (e < RP && o < o_last) s_next = scale_of(o + 1);
+          if (e == 0) ep_ok[buf] = mbar_wait(&dfull[buf], (uint32_t)((oc >> 1) & 1), a.err, failed) ? 1 : 0;
+          asm volatile("bar.sync 1, 128;" ::: "memory");
+          if (!ep_ok[buf]) { ep_broken = true; break; }  // uniform across the four epilogue warps
+          __syncwarp();            // tcgen05.ld is warp-collective
+          tc_fence_after();
+          const uint32_t lane_addr = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(buf * TS);
+          if constexpr (RP >= 32) {
 #pragma unroll
-          for (int c = 0; c < RP / 32; ++c) {
-            uint32_t pv[NPL][32];
+            for (int c = 0; c < RP / 32; ++c) {
+              uint32_t pv[NPL][32];
 #pragma unroll
-            for (int pl = 0; pl < NPL; ++pl)
-              tmem_ld32_nowait(lane_addr + (uint32_t)(pl * RP + c * 32), pv[pl]);
-            tmem_wait_ld();
+              for (int pl = 0; pl < NPL; ++pl)
+                tmem_ld32_nowait(lane_addr + (uint32_t)(pl * RP + c * 32), pv[pl]);
+              tmem_wait_ld();
 #pragma unroll
-            for (int j = 0; j < 32; ++j) {
-              float v = __uint_as_float(pv[NPL - 1][j]);   // smallest plane first
+              for (int j = 0; j < 32; ++j) {
+                float v = __uint_as_float(pv[NPL - 1][j]);   // smallest plane first
 #pragma unroll
-              for (int pl = NPL - 2; pl >= 0; --pl) v += __uint_as_float(pv[pl][j]);
-              acc[c * 32 + j] = fmaf(s_sm[buf * RP + c * 32 + j], v, acc[c * 32 + j]);
+                for (int pl = NPL - 2; pl >= 0; --pl) v += __uint_as_float(pv[pl][j]);
+                acc[c * 32 + j] = fmaf(s_sm[buf * RP + c * 32 + j], v, acc[c * 32 + j]);
+              }
+            }
+          } else {
+            float pv[NPL][16];
+#pragma unroll
+            for (int pl = 0; pl < NPL; ++pl) tmem_ld16(lane_addr + (uint32_t)(pl * RP), pv[pl]);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+              float v = pv[NPL - 1][j];
+#pragma unroll
+              for (int pl = NPL - 2; pl >= 0; --pl) v += pv[pl][j];
+              acc[j] = fmaf(s_sm[buf * RP + j], v, acc[j]);
             }
           }
-        } else {
-          float pv[NPL][16];
+          tc_fence_before();
+          mbar_arrive(&dempty[buf]);
+        }
+        // The partial tile leaves through shared memory: a thread holds one
+        // output row, so direct stores would put 32 rows (32 lines) in every
+        // warp store.  Staged in the idle operand buffers (every MMA and copy
+        // has completed once the last accumulator was read) with row stride
+        // RP + 1 (conflict-free), then written with consecutive threads on
+        // consecutive addresses.  The tile's rows are contiguous in `partial`.
+        if (!ep_broken) {
+          constexpr int SR = RP + 1;
+          float* stile = reinterpret_cast<float*>(sA);
 #pragma unroll
-          for (int pl = 0; pl < NPL; ++pl) tmem_ld16(lane_addr + (uint32_t)(pl * RP), pv[pl]);
-#pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            float v = pv[NPL - 1][j];
-#pragma unroll
-            for (int pl = NPL - 2; pl >= 0; --pl) v += pv[pl][j];
-            acc[j] = fmaf(s_sm[buf * RP + j], v, acc[j]);
+          for (int r = 0; r < RP; ++r)
+            if (r < a.R) stile[row * SR + r] = acc[r];
+          asm volatile("bar.sync 1, 128;" ::: "memory");
+          const int rows = (int)(a.I_out - m0 < kTileM ? a.I_out - m0 : kTileM);
+          const int n = rows * a.R;
+          float* out = a.partial + (pidx * a.I_out + m0) * a.R;
+          int rr = e / a.R, cc = e - (e / a.R) * a.R;
+          const int dr = kTileM / a.R, dc = kTileM - dr * a.R;   // advance of the flat index by 128
+          for (int idx = e; idx < n; idx += kTileM) {
+            out[idx] = stile[rr * SR + cc];
+            rr += dr;
+            cc += dc;
+            if (cc >= a.R) { cc -= a.R; ++rr; }
           }
         }
-        tc_fence_before();
-        mbar_arrive(&dempty[buf]);
-      }
-      const int64_t m = m0 + row;
-      if (m < a.I_out) {
-        float* out = a.partial + (pidx * a.I_out + m) * a.R;
-#pragma unroll
-        for (int r = 0; r < RP; ++r)
-          if (r < a.R) out[r] = acc[r];
       }
     }
   } else if (warp >= 2) {
     // empty range: this split contributes zeros
+    griddep_wait();
     const int q = warp & 3;
     const int64_t m = m0 + 32 * q + lane;
-    if (m < a.I_out)
+    if (m < a.I_out && !(a.skip && *a.skip))
       for (int r = 0; r < a.R; ++r) a.partial[(pidx * a.I_out + m) * a.R + r] = 0.f;
   }
 
@@ -594,8 +641,8 @@ template <int RP, bool MN, int NPL>
 int launch_tc(const TcPlan& p, const CUtensorMap& tx, const CUtensorMap& tf, const TcArgs& a,
               cudaStream_t st) {
   dim3 grid((unsigned)p.gsplits, (unsigned)p.n_cg, (unsigned)p.m_tiles);
-  mttkrp_tc_kernel<RP, MN, NPL><<<grid, kThreads, smem_for(p), st>>>(tx, tf, a);
-  TLGB_LAUNCH_CHECK();
+  TLGB_CUDA_TRY(launch_maybe_pdl(p.pdl && !tc_tuning().no_pdl, mttkrp_tc_kernel<RP, MN, NPL>,
+                                 grid, dim3(kThreads), smem_for(p), st, tx, tf, a));
   return TLGB_OK;
 }
 
@@ -667,7 +714,10 @@ int mttkrp_tc_make_plan(const Shape& sh, int64_t rank, int mode, int npl, int fr
   const int64_t room = (int64_t)kSmemBudget - 1024 - (int64_t)bbytes - (int64_t)tail_bytes(p.n_pad);
   p.stages = (int)std::min<int64_t>(kMaxStages, room > 0 ? room / kStageBytes : 0);
   if (tc_tuning().stages > 0) p.stages = std::min(p.stages, tc_tuning().stages);
-  bool ok = rank <= 128 && npl >= 1 && npl <= 3 && (npl == 2 || p.n_pad <= 64) && (p.C % 8 == 0) && (p.I_out % (p.out_contig ? 8 : 1) == 0) &&
+  // the epilogue stages the 128 x (n_pad + 1) f32 partial tile in the operand buffers
+  const bool stage_fits = (size_t)kTileM * (p.n_pad + 1) * sizeof(float) <=
+                          (size_t)p.stages * kStageBytes + bbytes;
+  bool ok = stage_fits && rank <= 128 && npl >= 1 && npl <= 3 && (npl == 2 || p.n_pad <= 64) && (p.C % 8 == 0) && (p.I_out % (p.out_contig ? 8 : 1) == 0) &&
             p.stages >= kMinStages && p.I_out < (1ll << 31) && p.C < (1ll << 31) &&
             p.O < (1ll << 31) && p.m_tiles <= 65535 && p.n_cg <= 65535;
   if (!ok) {
@@ -928,6 +978,8 @@ extern "C" int tlgb_set_tuning(const char* key, int value) {
   else if (k == "tc_waves") tc_tuning().waves = value;
   else if (k == "refine_simt") tc_tuning().refine_simt = value;
   else if (k == "tc_reserve_sms") tc_tuning().reserve_sms = value;
+  else if (k == "f64_factorize") tc_tuning().f64_factorize = value;
+  else if (k == "no_pdl") tc_tuning().no_pdl = value;
   else return batched_set_tuning(k, value);   // the batched CP-ALS variants
   return TLGB_OK;
 }

@@ -27,6 +27,7 @@ struct TcPlan {
   size_t partial_bytes;
   int ndim;
   int64_t dim[kMaxModes];
+  int pdl;              // launch with programmatic stream serialisation (inside CP-ALS sweeps)
 };
 
 // Plan knobs set by tlgb_set_tuning (0 = default): resident factor slice per
@@ -37,6 +38,8 @@ struct TcTuning {
   int waves = 0;
   int refine_simt = 0;  // 1: CP-ALS refinement sweeps use the SIMT f32 MTTKRP
   int reserve_sms = 0;  // overrides the SMs a plan leaves free (0 = the plan's own)
+  int f64_factorize = 0;      // 1: every CP-ALS factorisation takes the f64 Cholesky / LU path
+  int no_pdl = 0;             // 1: CP-ALS sweep kernels launch without programmatic dependence
 };
 TcTuning& tc_tuning();
 

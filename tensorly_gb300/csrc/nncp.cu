@@ -484,6 +484,7 @@ struct MuLayout {
   size_t ctrl, errors, G, V, partial, gpart, ipart, sumsq, bytes;
   size_t M, hpart, hstate, Pt, save;   // HALS: summed MTTKRP, stop partials, e0 + stop +
                                        // rerun, typed P, rows at the start of a chunk
+  size_t fac, perm, vmat, w32;         // HALS modes outside nn_modes: the CP-ALS solve
 };
 
 int64_t mu_rows_per_block(int64_t I, int R, int nparts);
@@ -523,6 +524,10 @@ int mu_layout(const Shape& sh, int64_t R, int n_iter_max, std::vector<MttkrpPlan
   L->hstate = take(sizeof(double) * 2);
   L->Pt = take(sizeof(T) * RR);
   L->save = take(sizeof(T) * (size_t)imax * R);
+  L->fac = take(sizeof(double) * (RR + R));
+  L->perm = take(sizeof(int) * R);
+  L->vmat = take(sizeof(double) * RR);
+  L->w32 = take(sizeof(float) * 3 * RR);
   L->bytes = align_up(off, 256);
   return TLGB_OK;
 }
@@ -658,11 +663,26 @@ __global__ void k_sym_typed(const T* __restrict__ in, int R, T* out) {
   }
 }
 
+// P = (w_r * P) * w_s, the weights of tensorly/decomposition/_nn_cp.py:316-320.
 template <typename T>
-int hals_run(const T* X, const Shape& sh, T* const* factors, int64_t R, const int* free_modes,
-             int n_free, int n_iter_max, double tol, int crit, const double* sparsity,
-             int exact, double* errors, int* n_errors, void* ws, size_t ws_bytes,
-             cudaStream_t st) {
+__global__ void k_weight_outer(double* __restrict__ P, const T* __restrict__ w, int R,
+                               const int* done) {
+  if (*done) return;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < R * R; e += gridDim.x * blockDim.x) {
+    const int r = e / R, c = e - r * R;
+    P[e] = ((double)w[r] * P[e]) * (double)w[c];
+  }
+}
+
+// nn_mask: bit k set = mode k is updated by HALS, else by the least-squares
+// solve (tensorly/decomposition/_nn_cp.py:324-341).  weights: device, rank
+// entries, in/out, or null (all ones).  normalize: cp_normalize after every
+// updated mode but the last and after every iteration (:342-343, :373-374).
+template <typename T>
+int hals_run(const T* X, const Shape& sh, T* const* factors, T* weights, int64_t R,
+             const int* free_modes, int n_free, unsigned nn_mask, int normalize, int n_iter_max,
+             double tol, int crit, const double* sparsity, int exact, double* errors,
+             int* n_errors, void* ws, size_t ws_bytes, cudaStream_t st) {
   std::vector<MttkrpPlan> plans;
   int nparts = 0;
   MuLayout L;
@@ -685,6 +705,10 @@ int hals_run(const T* X, const Shape& sh, T* const* factors, int64_t R, const in
   double* e0 = reinterpret_cast<double*>(base + L.hstate);
   T* Pt = reinterpret_cast<T*>(base + L.Pt);
   T* save = reinterpret_cast<T*>(base + L.save);
+  double* fac = reinterpret_cast<double*>(base + L.fac);
+  int* perm = reinterpret_cast<int*>(base + L.perm);
+  double* vmat = reinterpret_cast<double*>(base + L.vmat);
+  float* w32 = reinterpret_cast<float*>(base + L.w32);
   const int p_in_smem = ((size_t)R * R * sizeof(T) <= kHalsPSmemMax) ? 1 : 0;
   const size_t hals_smem = (p_in_smem ? (size_t)R * R * sizeof(T) : 0) +
                            (size_t)kHalsWarps * R * sizeof(T);
@@ -709,25 +733,52 @@ int hals_run(const T* X, const Shape& sh, T* const* factors, int64_t R, const in
   const T* cf[kMaxModes];
   for (int k = 0; k < N; ++k) cf[k] = factors[k];
   const int last = free_modes[n_free - 1];
+  // cp_normalize of the model, then the Grams of every (rescaled) factor
+  auto normalize_all = [&]() -> int {
+    int r2 = als_launch_normalize<T>(factors, sh.dim, N, (int)R, weights, done, st);
+    for (int k = 0; k < N && !r2; ++k)
+      r2 = als_launch_gram<T>(factors[k], sh.dim[k], (int)R, gpart, nparts, G + (size_t)k * RR,
+                              done, st);
+    return r2;
+  };
   AlsCtrl hc{};
   for (int it = 0; it < n_iter_max; ++it) {
     for (int q = 0; q < n_free; ++q) {
       const int mode = free_modes[q];
       const int64_t I = sh.dim[mode];
       const int64_t IR = I * R;
-      k_mu_accum<<<(RR + 255) / 256, 256, 0, st>>>(G, N, mode, (int)R, P, done);
-      TLGB_LAUNCH_CHECK();
-      k_to_type<T><<<(RR + 255) / 256, 256, 0, st>>>(P, (int)R, Pt, done);
-      TLGB_LAUNCH_CHECK();
-      rc = mttkrp_launch_partials<T>(plans[mode], X, cf, nullptr, partial, done, st);
+      const bool nn = (nn_mask >> mode) & 1u;
+      if (nn) {
+        k_mu_accum<<<(RR + 255) / 256, 256, 0, st>>>(G, N, mode, (int)R, P, done);
+        TLGB_LAUNCH_CHECK();
+        if (weights) {
+          k_weight_outer<T><<<(RR + 255) / 256, 256, 0, st>>>(P, weights, (int)R, done);
+          TLGB_LAUNCH_CHECK();
+        }
+        k_to_type<T><<<(RR + 255) / 256, 256, 0, st>>>(P, (int)R, Pt, done);
+        TLGB_LAUNCH_CHECK();
+      } else {
+        // factorisation of V = (prod G) * w w^T for the least-squares update
+        rc = als_launch_factorize<T>(G, N, mode, (int)R, weights, 0.0, fac, perm, vmat, w32,
+                                     ctrl, st);
+        if (rc) return rc;
+      }
+      rc = mttkrp_launch_partials<T>(plans[mode], X, cf, weights, partial, done, st);
       if (rc) return rc;
       k_sum_splits_to<T><<<(unsigned)std::min<int64_t>(ceil_div(IR, 256), 4096), 256, 0, st>>>(
           partial, plans[mode].splits, IR, M);
       TLGB_LAUNCH_CHECK();
-      // no sparsity coefficient (NaN): subtract 0, which leaves num unchanged
-      const double sp = (sparsity && !std::isnan(sparsity[mode])) ? sparsity[mode] : 0.0;
-      rc = hals_solve<T>(M, Pt, factors[mode], I, (int)R, n_inner, tol_inner, sp, save, hpart,
-                         e0, chunk, hals_smem, p_in_smem, done, st);
+      if (nn) {
+        // no sparsity coefficient (NaN): subtract 0, which leaves num unchanged
+        const double sp = (sparsity && !std::isnan(sparsity[mode])) ? sparsity[mode] : 0.0;
+        rc = hals_solve<T>(M, Pt, factors[mode], I, (int)R, n_inner, tol_inner, sp, save, hpart,
+                           e0, chunk, hals_smem, p_in_smem, done, st);
+      } else {
+        int nb = 0;
+        rc = als_launch_solve<T>(partial, plans[mode].splits, I, (int)R, fac, perm, vmat, w32,
+                                 factors[mode], nullptr, gpart, nullptr, ctrl, kIrMaxPasses, &nb,
+                                 st);
+      }
       if (rc) return rc;
       if (mode == last) {
         k_inner_part<T><<<kInnerBlocks, 256, 0, st>>>(M, factors[mode], IR, ipart, done);
@@ -736,14 +787,24 @@ int hals_run(const T* X, const Shape& sh, T* const* factors, int64_t R, const in
       rc = als_launch_gram<T>(factors[mode], I, (int)R, gpart, nparts, G + (size_t)mode * RR,
                               done, st);
       if (rc) return rc;
+      if (normalize && q + 1 < n_free) {
+        rc = normalize_all();
+        if (rc) return rc;
+      }
     }
     if (tol > 0.0) {
-      rc = als_launch_fit<T>(G, N, (int)R, nullptr, ipart, kInnerBlocks, ctrl, derr, n_iter_max,
+      rc = als_launch_fit<T>(G, N, (int)R, weights, ipart, kInnerBlocks, ctrl, derr, n_iter_max,
                              tol, crit, st);
       if (rc) return rc;
       TLGB_CUDA_TRY(cudaMemcpyAsync(&hc, ctrl, sizeof(AlsCtrl), cudaMemcpyDeviceToHost, st));
       TLGB_CUDA_TRY(cudaStreamSynchronize(st));
+      if (hc.status == TLGB_ESINGULAR)
+        return set_error(TLGB_ESINGULAR, "cp_nn_hals: normal equations singular");
       if (hc.done) break;
+    }
+    if (normalize) {
+      rc = normalize_all();
+      if (rc) return rc;
     }
   }
   TLGB_CUDA_TRY(cudaMemcpyAsync(&hc, ctrl, sizeof(AlsCtrl), cudaMemcpyDeviceToHost, st));
@@ -816,10 +877,12 @@ extern "C" int tlgb_cp_nn_mu(int dtype, const void* X, int ndim, const int64_t* 
 }
 
 extern "C" int tlgb_cp_nn_hals(int dtype, const void* X, int ndim, const int64_t* shape,
-                               void* const* factors, int64_t rank, const int* free_modes,
-                               int n_free, int n_iter_max, double tol, int cvg_criterion,
-                               const double* sparsity, int exact, double* errors, int* n_errors,
-                               void* workspace, size_t workspace_bytes, void* stream) {
+                               void* const* factors, void* weights, int64_t rank,
+                               const int* free_modes, int n_free, unsigned nn_modes_mask,
+                               int normalize_factors, int n_iter_max, double tol,
+                               int cvg_criterion, const double* sparsity, int exact,
+                               double* errors, int* n_errors, void* workspace,
+                               size_t workspace_bytes, void* stream) {
   clear_error();
   int rc = check_nn_args(dtype, shape, ndim, rank);
   if (rc) return rc;
@@ -834,15 +897,19 @@ extern "C" int tlgb_cp_nn_hals(int dtype, const void* X, int ndim, const int64_t
   TLGB_CHECK_ARG(n_iter_max >= 0 && tol >= 0.0, "cp_nn_hals: bad n_iter_max or tol");
   TLGB_CHECK_ARG(cvg_criterion == 0 || cvg_criterion == 1, "cp_nn_hals: bad cvg_criterion");
   TLGB_CHECK_ARG(rank <= kMaxAlsRank, "cp_nn_hals: rank above 160 is not supported");
+  TLGB_CHECK_ARG(!normalize_factors || weights != nullptr,
+                 "cp_nn_hals: normalize_factors needs a weights buffer");
   Shape sh = make_shape(ndim, shape);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (dtype == TLGB_F64)
-    return hals_run<double>((const double*)X, sh, (double* const*)factors, rank, free_modes,
-                            n_free, n_iter_max, tol, cvg_criterion, sparsity, exact, errors,
-                            n_errors, workspace, workspace_bytes, st);
-  return hals_run<float>((const float*)X, sh, (float* const*)factors, rank, free_modes, n_free,
-                         n_iter_max, tol, cvg_criterion, sparsity, exact, errors, n_errors,
-                         workspace, workspace_bytes, st);
+    return hals_run<double>((const double*)X, sh, (double* const*)factors, (double*)weights, rank,
+                            free_modes, n_free, nn_modes_mask, normalize_factors, n_iter_max, tol,
+                            cvg_criterion, sparsity, exact, errors, n_errors, workspace,
+                            workspace_bytes, st);
+  return hals_run<float>((const float*)X, sh, (float* const*)factors, (float*)weights, rank,
+                         free_modes, n_free, nn_modes_mask, normalize_factors, n_iter_max, tol,
+                         cvg_criterion, sparsity, exact, errors, n_errors, workspace,
+                         workspace_bytes, st);
 }
 
 extern "C" int tlgb_sum(int dtype, const void* X, int64_t n, double* out, void* workspace,

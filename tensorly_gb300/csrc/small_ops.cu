@@ -81,6 +81,91 @@ __global__ void k_dot_part(const T* __restrict__ a, const T* __restrict__ b, int
   }
 }
 
+// Missing-entry refill of a masked decomposition:
+// x = x * mask + rec * (1 - mask), in place, with the block partials of
+// ||x||^2 and ||x - rec||^2 (f64) in part[2 * block + {0, 1}].
+template <typename T>
+__global__ void k_mask_impute_part(T* __restrict__ x, const T* __restrict__ mask,
+                                   const T* __restrict__ rec, int64_t n, double* part) {
+  __shared__ double red[2][8];
+  double s0 = 0.0, s1 = 0.0;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const T m = mask[e], r = rec[e];
+    const T v = x[e] * m + r * (T(1) - m);
+    x[e] = v;
+    const double dv = (double)v, dr = (double)v - (double)r;
+    s0 = fma(dv, dv, s0);
+    s1 = fma(dr, dr, s1);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+    s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = s0;
+    red[1][threadIdx.x >> 5] = s1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t0 = 0.0, t1 = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { t0 += red[0][w]; t1 += red[1][w]; }
+    part[2 * blockIdx.x] = t0;
+    part[2 * blockIdx.x + 1] = t1;
+  }
+}
+
+__global__ void k_mask_impute_final(const double* part, int nb, double* out) {
+  if (threadIdx.x == 0) {
+    double t0 = 0.0, t1 = 0.0;
+    for (int b = 0; b < nb; ++b) { t0 += part[2 * b]; t1 += part[2 * b + 1]; }
+    out[0] = sqrt(t0);
+    out[1] = sqrt(t1);
+  }
+}
+
+// x = where(mask == 0, rec (or fill when rec is null), x), in place
+// (tensorly/decomposition/_parafac2.py:21-65, the missing-entry refill).
+template <typename T>
+__global__ void k_mask_where(T* __restrict__ x, const T* __restrict__ mask,
+                             const T* __restrict__ rec, T fill, int64_t n) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x)
+    if (mask[e] == T(0)) x[e] = rec ? rec[e] : fill;
+}
+
+// Block partials of sum((mask * x - mask * rec)^2) in f64.
+template <typename T>
+__global__ void k_masked_sq_diff_part(const T* __restrict__ x, const T* __restrict__ mask,
+                                      const T* __restrict__ rec, int64_t n, double* part) {
+  __shared__ double red[8];
+  double s = 0.0;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const T m = mask[e];
+    const double d = (double)(m * x[e] - m * rec[e]);
+    s = fma(d, d, s);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    part[blockIdx.x] = t;
+  }
+}
+
+// x = max(x, lo) in place (NaN stays NaN, as numpy's clip keeps it).
+template <typename T>
+__global__ void k_clip_min(T* __restrict__ x, int64_t n, T lo) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x)
+    if (x[e] < lo) x[e] = lo;
+}
+
 __global__ void k_dot_final(const double* part, int nb, double* out) {
   if (threadIdx.x == 0) {
     double t = 0.0;
@@ -450,6 +535,94 @@ extern "C" int tlgb_dot(int dtype, const void* a, const void* b, int64_t n, doub
                                           static_cast<const float*>(b), n, part);
   TLGB_LAUNCH_CHECK();
   k_dot_final<<<1, 32, 0, st>>>(part, nb, out);
+  TLGB_LAUNCH_CHECK();
+  return TLGB_OK;
+}
+
+extern "C" size_t tlgb_mask_impute_workspace_bytes(void) { return 2 * sizeof(double) * kDotBlocks; }
+
+extern "C" int tlgb_mask_impute(int dtype, void* x, const void* mask, const void* rec, int64_t n,
+                                double* out, void* workspace, size_t workspace_bytes,
+                                void* stream) {
+  clear_error();
+  TLGB_CHECK_ARG(dtype == TLGB_F32 || dtype == TLGB_F64, "mask_impute: dtype must be f32 or f64");
+  TLGB_CHECK_ARG(x && mask && rec && out && n >= 1, "mask_impute: bad argument");
+  if (!workspace || workspace_bytes < 2 * sizeof(double) * kDotBlocks)
+    return set_error(TLGB_EWORKSPACE, "mask_impute: workspace too small");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  double* part = static_cast<double*>(workspace);
+  const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, (int64_t)256), kDotBlocks));
+  if (dtype == TLGB_F64)
+    k_mask_impute_part<double><<<nb, 256, 0, st>>>(static_cast<double*>(x),
+                                                   static_cast<const double*>(mask),
+                                                   static_cast<const double*>(rec), n, part);
+  else
+    k_mask_impute_part<float><<<nb, 256, 0, st>>>(static_cast<float*>(x),
+                                                  static_cast<const float*>(mask),
+                                                  static_cast<const float*>(rec), n, part);
+  TLGB_LAUNCH_CHECK();
+  k_mask_impute_final<<<1, 32, 0, st>>>(part, nb, out);
+  TLGB_LAUNCH_CHECK();
+  return TLGB_OK;
+}
+
+extern "C" int tlgb_mask_where(int dtype, void* x, const void* mask, const void* rec, double fill,
+                               int64_t n, void* stream) {
+  clear_error();
+  TLGB_CHECK_ARG(dtype == TLGB_F32 || dtype == TLGB_F64, "mask_where: dtype must be f32 or f64");
+  TLGB_CHECK_ARG(x && mask && n >= 0, "mask_where: bad argument");
+  if (n == 0) return TLGB_OK;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const unsigned nb = (unsigned)std::min<int64_t>(ceil_div(n, (int64_t)256), 152 * 8);
+  if (dtype == TLGB_F64)
+    k_mask_where<double><<<nb, 256, 0, st>>>(static_cast<double*>(x),
+                                             static_cast<const double*>(mask),
+                                             static_cast<const double*>(rec), fill, n);
+  else
+    k_mask_where<float><<<nb, 256, 0, st>>>(static_cast<float*>(x),
+                                            static_cast<const float*>(mask),
+                                            static_cast<const float*>(rec), (float)fill, n);
+  TLGB_LAUNCH_CHECK();
+  return TLGB_OK;
+}
+
+extern "C" int tlgb_masked_sq_diff(int dtype, const void* x, const void* mask, const void* rec,
+                                   int64_t n, double* out, void* workspace,
+                                   size_t workspace_bytes, void* stream) {
+  clear_error();
+  TLGB_CHECK_ARG(dtype == TLGB_F32 || dtype == TLGB_F64,
+                 "masked_sq_diff: dtype must be f32 or f64");
+  TLGB_CHECK_ARG(x && mask && rec && out && n >= 1, "masked_sq_diff: bad argument");
+  if (!workspace || workspace_bytes < sizeof(double) * kDotBlocks)
+    return set_error(TLGB_EWORKSPACE, "masked_sq_diff: workspace too small");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  double* part = static_cast<double*>(workspace);
+  const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, (int64_t)256), kDotBlocks));
+  if (dtype == TLGB_F64)
+    k_masked_sq_diff_part<double><<<nb, 256, 0, st>>>(static_cast<const double*>(x),
+                                                      static_cast<const double*>(mask),
+                                                      static_cast<const double*>(rec), n, part);
+  else
+    k_masked_sq_diff_part<float><<<nb, 256, 0, st>>>(static_cast<const float*>(x),
+                                                     static_cast<const float*>(mask),
+                                                     static_cast<const float*>(rec), n, part);
+  TLGB_LAUNCH_CHECK();
+  k_dot_final<<<1, 32, 0, st>>>(part, nb, out);
+  TLGB_LAUNCH_CHECK();
+  return TLGB_OK;
+}
+
+extern "C" int tlgb_clip_min(int dtype, void* x, int64_t n, double lo, void* stream) {
+  clear_error();
+  TLGB_CHECK_ARG(dtype == TLGB_F32 || dtype == TLGB_F64, "clip_min: dtype must be f32 or f64");
+  TLGB_CHECK_ARG(x && n >= 0, "clip_min: bad argument");
+  if (n == 0) return TLGB_OK;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const unsigned nb = (unsigned)std::min<int64_t>(ceil_div(n, (int64_t)256), 152 * 8);
+  if (dtype == TLGB_F64)
+    k_clip_min<double><<<nb, 256, 0, st>>>(static_cast<double*>(x), n, lo);
+  else
+    k_clip_min<float><<<nb, 256, 0, st>>>(static_cast<float*>(x), n, (float)lo);
   TLGB_LAUNCH_CHECK();
   return TLGB_OK;
 }

@@ -48,8 +48,8 @@ def initialize_cp(tensor, rank, init="svd", svd="truncated_svd", non_negative=Fa
     mean (``:102-126``).
     """
     x, _ = to_device(tensor)
-    if mask is not None:
-        raise NotImplementedError("masked initialisation is not supported")
+    if mask is not None and isinstance(init, str) and init == "svd":
+        raise NotImplementedError("masked 'svd' initialisation is not supported")
     rng = check_random_state(random_state)
     if isinstance(init, str) and init == "random":
         factors = [torch.from_numpy(rng.random_sample((int(s), int(rank)))).to(x.device, x.dtype)
@@ -131,10 +131,9 @@ def parafac(tensor, rank, n_iter_max=100, init="svd", svd="truncated_svd",
     """
     if sparsity:
         raise NotImplementedError("parafac with sparsity is not supported by tensorly_gb300")
-    if mask is not None:
-        raise NotImplementedError("masked parafac is not supported by tensorly_gb300")
-    if (linesearch or orthogonalise) and precision != "native":
-        raise NotImplementedError("parafac line search and orthogonalise run at native precision")
+    if (linesearch or orthogonalise or mask is not None) and precision != "native":
+        raise NotImplementedError("parafac line search, orthogonalise and masks run at native "
+                                  "precision")
     if precision not in _PRECISIONS:
         raise ValueError(f"precision must be one of {sorted(_PRECISIONS)}")
     x, pl = to_device(tensor)
@@ -164,13 +163,13 @@ def parafac(tensor, rank, n_iter_max=100, init="svd", svd="truncated_svd",
     for m in fixed:
         fixed_mask |= 1 << int(m)
 
-    if linesearch or orthogonalise:
+    if linesearch or orthogonalise or mask is not None:
         return _parafac_host_loop(x, pl, rank, weights, factors, n_iter_max=n_iter_max,
                                   orthogonalise=orthogonalise, tol=tol, verbose=verbose,
                                   return_errors=return_errors, l2_reg=l2_reg,
                                   cvg_criterion=cvg_criterion, fixed_mask=fixed_mask,
                                   normalize_factors=normalize_factors, linesearch=linesearch,
-                                  callback=callback)
+                                  callback=callback, mask=mask)
 
     lib = _lib.lib()
     opts = _lib.CpAlsOptions()
@@ -233,10 +232,17 @@ def parafac(tensor, rank, n_iter_max=100, init="svd", svd="truncated_svd",
 
 def _parafac_host_loop(x, pl, rank, weights, factors, *, n_iter_max, orthogonalise, tol,
                        verbose, return_errors, l2_reg, cvg_criterion, fixed_mask,
-                       normalize_factors, linesearch, callback):
-    """parafac with orthogonalisation and / or the line search
-    (tensorly/decomposition/_cp.py:392-401, :430-478): the reference's
-    iteration loop on the host around single-sweep ``tlgb_cp_als`` calls.
+                       normalize_factors, linesearch, callback, mask=None):
+    """parafac with orthogonalisation, the line search and / or a mask
+    (tensorly/decomposition/_cp.py:392-401, :430-478, :194-207, :441-446):
+    the reference's iteration loop on the host around single-sweep
+    ``tlgb_cp_als`` calls.
+
+    With a mask the sweeps run on a working copy of the tensor whose missing
+    entries are refilled from the model after every sweep
+    (x = x * mask + cp_to_tensor(model) * (1 - mask), ``tlgb_cp_to_tensor`` and
+    ``tlgb_mask_impute``); the error is then the norm of the explicit residual
+    over the refilled tensor's norm, as the reference's error_calc computes it.
 
     Per iteration: QR of each factor while ``iteration <= orthogonalise``
     (``tlgb_qr``, LAPACK's sign convention); one ALS sweep in the library,
@@ -269,6 +275,7 @@ def _parafac_host_loop(x, pl, rank, weights, factors, *, n_iter_max, orthogonali
     n_err = ctypes.c_int(0)
 
     def sweep():
+        # `x` is read at call time: with a mask it is the refilled working tensor
         _lib.check(lib.tlgb_cp_als(dtype_code(x), ptr(x), x.ndim, shape, rank,
                                    _lib.ptr_array([ptr(f) for f in factors]), ptr(weights),
                                    ctypes.byref(opts), errs, ctypes.byref(n_err), ptr(ws),
@@ -276,9 +283,37 @@ def _parafac_host_loop(x, pl, rank, weights, factors, *, n_iter_max, orthogonali
         return float(errs[0])
 
     norm_tensor = _norm_on_device(x)
+    if mask is not None:
+        mask_t = like(mask, x).expand(x.shape).contiguous()
+        x = x.clone()   # the refilled working tensor; the caller's tensor is not modified
+        rec = torch.empty_like(x)
+        imp_ws = workspace(int(lib.tlgb_mask_impute_workspace_bytes()), x.device)
+        imp_out = torch.empty(2, dtype=torch.float64, device=x.device)
+        dims = _lib.i64_array(x.shape)
+        rec_bytes = ctypes.c_size_t(0)
+        _lib.check(lib.tlgb_cp_to_tensor_workspace_size(dtype_code(x), x.ndim, dims, rank,
+                                                        ctypes.byref(rec_bytes)))
+        rec_ws = workspace(rec_bytes.value, x.device)
+
+    def refill(target, w, fs):
+        """target = target * mask + [[w; fs]] * (1 - mask); (||target||, ||target - [[w; fs]]||)."""
+        _lib.check(lib.tlgb_cp_to_tensor(dtype_code(x), x.ndim, dims, rank,
+                                         _lib.ptr_array([ptr(f) for f in fs]), ptr(w), None,
+                                         ptr(rec), ptr(rec_ws), rec_ws.numel(), stream_of(x)))
+        _lib.check(lib.tlgb_mask_impute(dtype_code(x), ptr(target), ptr(mask_t), ptr(rec),
+                                        target.numel(), ptr(imp_out), ptr(imp_ws),
+                                        imp_ws.numel(), stream_of(x)))
+        v = imp_out.cpu()
+        return float(v[0]), float(v[1])
+
     if callback is not None:
+        if mask is not None:
+            # the reference refills a copy for this first error and keeps its norm
+            norm_tensor, unnorm0 = refill(x.clone(), weights, factors)
+        else:
+            unnorm0 = _residual_norm(x, factors, weights)
         callback(_place_cp(weights.clone(), [f.clone() for f in factors], pl),
-                 _residual_norm(x, factors, weights) / norm_tensor)
+                 unnorm0 / norm_tensor)
     acc_pow, acc_fail, max_fail = 2.0, 0, 4
     rec_errors = []
     rec_error = None
@@ -291,20 +326,35 @@ def _parafac_host_loop(x, pl, rank, weights, factors, *, n_iter_max, orthogonali
         fast_error = sweep()
         line_iter = bool(linesearch and iteration % 2 == 0 and iteration > 5)
         if not line_iter:
-            unnorm = fast_error * norm_tensor
+            if mask is not None:
+                norm_tensor, unnorm = refill(x, weights, factors)
+            else:
+                unnorm = fast_error * norm_tensor
         else:
+            if mask is not None:
+                refill(x, weights, factors)
             jump = iteration ** (1.0 / acc_pow)
             new_weights = _lerp(weights_last, weights, jump)
             new_factors = [_lerp(a, b, jump) for a, b in zip(factors_last, factors)]
-            new_error = _residual_norm(x, new_factors, new_weights)
-            if new_error / norm_tensor < rec_errors[-1]:
+            if mask is not None:
+                x_new = x.clone()
+                new_norm, new_error = refill(x_new, new_weights, new_factors)
+            else:
+                new_norm, new_error = norm_tensor, _residual_norm(x, new_factors, new_weights)
+            if new_error / new_norm < rec_errors[-1]:
                 factors, weights = new_factors, new_weights
+                if mask is not None:
+                    x = x_new
+                norm_tensor = new_norm
                 unnorm = new_error
                 acc_fail = 0
                 if verbose:
                     print(f"Accepted line search jump of {jump}.")
             else:
-                unnorm = fast_error * norm_tensor
+                if mask is not None:
+                    norm_tensor, unnorm = refill(x, weights, factors)
+                else:
+                    unnorm = fast_error * norm_tensor
                 acc_fail += 1
                 if verbose:
                     print(f"Line search failed for jump of {jump}.")
@@ -653,14 +703,12 @@ def non_negative_parafac_hals(tensor, rank, n_iter_max=100, init="svd", svd="tru
     same signature and returns.  The loop runs in ``tlgb_cp_nn_hals``: per
     free mode the Hadamard of the other Grams, the MTTKRP and the
     ``hals_nnls`` row updates (tensorly/solvers/nnls.py:5-150) with their own
-    stop test; with ``tol`` the error of every iteration and the outer test.
-    ``nn_modes`` other than 'all', ``normalize_factors`` and a fixed last mode
-    are not supported."""
-    if normalize_factors:
-        raise NotImplementedError("non_negative_parafac_hals with normalize_factors=True is not "
-                                  "supported by tensorly_gb300")
-    if nn_modes != "all":
-        raise NotImplementedError("non_negative_parafac_hals supports nn_modes='all' only")
+    stop test, or, for a mode outside ``nn_modes``, the least-squares update
+    of CP-ALS; with ``normalize_factors`` the model is renormalised after
+    every updated mode but the last and after every iteration, and the
+    weights enter the normal equations and the MTTKRP; with ``tol`` the error
+    of every iteration and the outer test.  A fixed last mode is not
+    supported."""
     if tol and n_iter_max > 1 and cvg_criterion not in ("abs_rec_error", "rec_error"):
         raise TypeError("Unknown convergence criterion")   # _nn_cp.py:363-364
     x, placement = to_device(tensor)
@@ -668,10 +716,24 @@ def non_negative_parafac_hals(tensor, rank, n_iter_max=100, init="svd", svd="tru
     x = x.contiguous()
     if x.ndim < 2:
         raise NotImplementedError("non_negative_parafac_hals needs at least two modes")
-    _, factors = initialize_cp(x, rank, init=init, svd=svd, non_negative=True,
-                               random_state=random_state, normalize_factors=False)
-    factors = [f.to(x.dtype).contiguous().clone() for f in factors]
     n_modes = x.ndim
+    if nn_modes == "all":
+        nn_set = set(range(n_modes))
+    elif nn_modes is None:
+        nn_set = set()
+    else:
+        nn_set = set(int(m) for m in nn_modes)
+    nn_mask = 0
+    for m in nn_set:
+        if 0 <= m < n_modes:
+            nn_mask |= 1 << m
+    weights, factors = initialize_cp(x, rank, init=init, svd=svd, non_negative=True,
+                                     random_state=random_state,
+                                     normalize_factors=normalize_factors)
+    factors = [f.to(x.dtype).contiguous().clone() for f in factors]
+    if weights is None:
+        weights = torch.ones(int(rank), dtype=x.dtype, device=x.device)
+    weights = weights.to(x.dtype).contiguous().clone()
     if sparsity_coefficients is None or isinstance(sparsity_coefficients, float):
         sparsity_coefficients = [sparsity_coefficients] * n_modes
     sparsity_coefficients = list(sparsity_coefficients)
@@ -697,13 +759,13 @@ def non_negative_parafac_hals(tensor, rank, n_iter_max=100, init="svd", svd="tru
                                        for c in sparsity_coefficients])
     errs = (ctypes.c_double * max(1, int(n_iter_max)))()
     n_err = ctypes.c_int(0)
-    _lib.check(lib.tlgb_cp_nn_hals(code, x.data_ptr(), n_modes, shape, fptrs, int(rank),
-                                   free_arr, len(free), int(n_iter_max),
+    _lib.check(lib.tlgb_cp_nn_hals(code, x.data_ptr(), n_modes, shape, fptrs, weights.data_ptr(),
+                                   int(rank), free_arr, len(free), nn_mask,
+                                   1 if normalize_factors else 0, int(n_iter_max),
                                    float(tol) if tol else 0.0,
                                    0 if cvg_criterion == "abs_rec_error" else 1, sp,
                                    1 if exact else 0, errs, ctypes.byref(n_err), ptr(ws),
                                    ws.numel(), stream_of(x)))
-    weights = torch.ones(int(rank), dtype=x.dtype, device=x.device)
     cp = CPTensor((placement.back(weights), [placement.back(f) for f in factors]))
     if return_errors:
         return cp, [float(errs[i]) for i in range(n_err.value)]

@@ -1,7 +1,6 @@
 """PARAFAC2 (tensorly/decomposition/_parafac2.py, tensorly/parafac2_tensor.py).
 
-The dense, unmasked, unconstrained algorithm of the reference, composed of
-the library's kernels:
+The reference's algorithm, composed of the library's kernels:
 
 * the projections P_k = (U Vh)^T of M_k = B (A_k * C)^T X_k^T are the polar
   factor M_k^T (M_k M_k^T)^(-1/2), from the R x R eigenproblem of M_k M_k^T
@@ -11,6 +10,13 @@ the library's kernels:
   ``n_iter_parafac`` sweeps from the current factors;
 * the line search (``_BroThesisLineSearch``) extrapolates with ``tlgb_lerp``;
 * the error is the reference's expansion (:300-362) on the GPU;
+* ``nn_modes``: the projected slices feed ``non_negative_parafac_hals``
+  (HALS on the constrained modes, least squares on the others) and the line
+  search clips the non-negative modes (``tlgb_clip_min``);
+* masks: missing entries start at their slice's observed mean (or the given
+  model) and are refilled from the model after every iteration
+  (``tlgb_mask_where``); the error is then the masked residual
+  (``tlgb_masked_sq_diff``);
 * the random start draws as the reference (uniform blocks, then random_cp)
   and orthonormalises with ``tlgb_qr`` (LAPACK's Householder conventions,
   so the signs are NumPy's).
@@ -22,7 +28,7 @@ import math
 import torch
 
 from . import _lib
-from ._tensor import dtype_code, ptr, stream_of, to_device, workspace
+from ._tensor import dtype_code, like, ptr, stream_of, to_device, workspace
 from .random import check_random_state
 
 
@@ -157,8 +163,57 @@ def _project(slices, projections):
     return y
 
 
-def _reconstruction_error(slices, decomposition, norm_x, projected=None):
-    """tensorly/decomposition/_parafac2.py:321-396 (no mask)."""
+def _sum(x):
+    lib = _lib.lib()
+    ws = workspace(256 * 8, x.device)
+    total = torch.zeros(1, dtype=torch.float64, device=x.device)
+    _lib.check(lib.tlgb_sum(dtype_code(x), x.data_ptr(), x.numel(), total.data_ptr(), ptr(ws),
+                            ws.numel(), stream_of(x)))
+    return float(total.item())
+
+
+def _where(x, mask, rec=None, fill=0.0):
+    """x = where(mask == 0, rec or fill, x), in place."""
+    _lib.check(_lib.lib().tlgb_mask_where(dtype_code(x), x.data_ptr(), mask.data_ptr(), ptr(rec),
+                                          float(fill), x.numel(), stream_of(x)))
+
+
+def _masked_sq(x, mask, rec):
+    """sum((mask * x - mask * rec)^2)."""
+    lib = _lib.lib()
+    ws = workspace(int(lib.tlgb_dot_workspace_bytes()), x.device)
+    out = torch.empty(1, dtype=torch.float64, device=x.device)
+    _lib.check(lib.tlgb_masked_sq_diff(dtype_code(x), x.data_ptr(), mask.data_ptr(),
+                                       rec.contiguous().data_ptr(), x.numel(), out.data_ptr(),
+                                       ptr(ws), ws.numel(), stream_of(x)))
+    return float(out.item())
+
+
+def _clip_min0(x):
+    x = x.contiguous().clone()
+    _lib.check(_lib.lib().tlgb_clip_min(dtype_code(x), x.data_ptr(), x.numel(), 0.0,
+                                        stream_of(x)))
+    return x
+
+
+def _update_imputed(slices, masks, decomposition, method):
+    """tensorly/decomposition/_parafac2.py:21-65, in place: 'mode-2' fills the
+    missing entries of each slice with the mean of its observed entries,
+    'factors' with the model's reconstruction."""
+    if method == "mode-2":
+        for x, m in zip(slices, masks):
+            _where(x, m, fill=_dot(x, m) / _sum(m))
+    else:
+        for x, m, r in zip(slices, masks, parafac2_to_slices(decomposition)):
+            _where(x, m, r.contiguous())
+
+
+def _reconstruction_error(slices, decomposition, norm_x, projected=None, masks=None):
+    """tensorly/decomposition/_parafac2.py:321-396."""
+    if masks is not None:
+        total = sum(_masked_sq(x, m, r) for x, m, r in
+                    zip(slices, masks, parafac2_to_slices(decomposition)))
+        return math.sqrt(total)
     weights, (A, B, C), projections = decomposition
     if weights is not None:
         A = _scale_cols(A, weights)
@@ -219,10 +274,13 @@ def _initialize(slices, rank, init, svd, random_state):
 
 
 class _LineSearch:
-    """tensorly/decomposition/_parafac2.py:183-318 (no nn_modes, no mask)."""
+    """tensorly/decomposition/_parafac2.py:183-318."""
 
-    def __init__(self, norm_tensor, acc_pow=2.0, max_fail=4, verbose=False):
+    def __init__(self, norm_tensor, acc_pow=2.0, max_fail=4, verbose=False, nn_modes=None,
+                 masks=None):
         self.norm_tensor = norm_tensor
+        self.nn_modes = nn_modes
+        self.masks = masks
         self.acc_pow = acc_pow
         self.max_fail = max_fail
         self.acc_fail = 0
@@ -232,9 +290,16 @@ class _LineSearch:
                   rec_error):
         jump = iteration ** (1.0 / self.acc_pow)
         factors_ls = [_lerp(factors_last[ii], factors[ii], jump) for ii in range(len(factors))]
+        if self.nn_modes:
+            # `0 in nn_modes` as the reference writes it (a TypeError for 'all')
+            if 0 in self.nn_modes:
+                factors_ls[0] = _clip_min0(factors_ls[0])
+            if 2 in self.nn_modes:
+                factors_ls[2] = _clip_min0(factors_ls[2])
         projections_ls = _compute_projections(slices, factors_ls)
         ls_rec_error = _reconstruction_error(slices, (weights, factors_ls, projections_ls),
-                                             self.norm_tensor) / self.norm_tensor
+                                             self.norm_tensor,
+                                             masks=self.masks) / self.norm_tensor
         if ls_rec_error < rec_error:
             self.acc_fail = 0
             if self.verbose:
@@ -253,15 +318,12 @@ def parafac2(tensor_slices, rank, n_iter_max=2000, init="random", svd="truncated
              normalize_factors=False, tol=1.0e-8, nn_modes=None, random_state=None,
              verbose=False, return_errors=False, n_iter_parafac=5, linesearch=True, mask=None):
     """PARAFAC2 by ALS (tensorly/decomposition/_parafac2.py:399-707), same
-    signature and returns, for the dense unconstrained case (``nn_modes`` and
-    ``mask`` raise NotImplementedError).  f32 slices are computed in f64 and
-    the results returned in f32."""
+    signature and returns, with non-negative modes and masks.  f32 slices are
+    computed in f64 and the results returned in f32; the caller's slices are
+    not modified (the masked refill works on copies)."""
+    from warnings import warn
     from .cp_tensor import cp_normalize
-    from .decomposition import parafac
-    if nn_modes is not None:
-        raise NotImplementedError("parafac2 with nn_modes is not supported by tensorly_gb300")
-    if mask is not None:
-        raise NotImplementedError("masked parafac2 is not supported by tensorly_gb300")
+    from .decomposition import non_negative_parafac_hals, parafac
     placement = to_device(tensor_slices[0])[1]
     slices = [to_device(t)[0].contiguous() for t in tensor_slices]
     # f32 slices run the f64 path (the R x R eigenproblems of the projections
@@ -276,12 +338,27 @@ def parafac2(tensor_slices, rank, n_iter_max=2000, init="random", svd="truncated
         assert slices[0].shape[1] == slices[ii].shape[1], \
             "All tensor slices must have the same number of columns."
     dt, dev = slices[0].dtype, slices[0].device
+    masks = None if mask is None else [like(m, slices[0]) for m in mask]
     weights, factors, projections = _initialize(slices, rank, init, svd, random_state)
     factors = [f.to(dt).contiguous() for f in factors]
+    if masks is not None:
+        slices = [t.clone() for t in slices]
+        if isinstance(init, str) and init in ("random", "svd"):
+            _update_imputed(slices, masks, None, "mode-2")
+        else:
+            _update_imputed(slices, masks, (weights, factors, projections), "factors")
     if weights is None:
         weights = torch.ones(rank, dtype=dt, device=dev)
-    norm_x = math.sqrt(sum(_dot(t, t) for t in slices))
-    ls = _LineSearch(norm_x, verbose=verbose) if linesearch else None
+    if masks is not None:
+        norm_x = math.sqrt(sum(_masked_sq(t, m, torch.zeros_like(t))
+                               for t, m in zip(slices, masks)))
+    else:
+        norm_x = math.sqrt(sum(_dot(t, t) for t in slices))
+    ls = (_LineSearch(norm_x, verbose=verbose, nn_modes=nn_modes, masks=masks)
+          if linesearch else None)
+    if nn_modes is not None and (nn_modes == "all" or 1 in nn_modes):
+        warn("Mode `1` of PARAFAC2 fitted with ALS cannot be constrained to be truly "
+             "non-negative. See the documentation for more info.")
     rec_errors = []
     for iteration in range(n_iter_max):
         factors[1] = _scale_cols(factors[1], weights.to(dt))
@@ -291,18 +368,25 @@ def parafac2(tensor_slices, rank, n_iter_max=2000, init="random", svd="truncated
             factors_last = [f.clone() for f in factors]
         projections = _compute_projections(slices, factors)
         projected = _project(slices, projections)
-        cp = parafac(projected, rank, n_iter_max=n_iter_parafac, init=(weights, factors),
-                     svd=svd, normalize_factors=False, tol=1e-100)
+        if nn_modes is None:
+            cp = parafac(projected, rank, n_iter_max=n_iter_parafac, init=(weights, factors),
+                         svd=svd, normalize_factors=False, tol=1e-100)
+        else:
+            cp = non_negative_parafac_hals(projected, rank, n_iter_max=n_iter_parafac,
+                                           init=(weights, factors), svd=svd, nn_modes=nn_modes,
+                                           tol=1e-100)
         factors = [f.contiguous() for f in cp.factors]
         if line_iter:
             factors, projections, rec_errors[-1] = ls.line_step(
                 iteration, slices, factors_last, weights, factors, projections, rec_errors[-1])
+        if masks is not None:
+            _update_imputed(slices, masks, (weights, factors, projections), "factors")
         if normalize_factors:
             weights, factors = cp_normalize((weights, factors))
             factors = list(factors)
         if tol and not line_iter:
             rec_error = _reconstruction_error(slices, (weights, factors, projections), norm_x,
-                                              projected)
+                                              projected, masks)
             rec_errors.append(rec_error / norm_x)
         if tol and iteration >= 1:
             if verbose:

@@ -125,9 +125,27 @@ def test_hals_estimator_and_unsupported_options(gb300, golden):
     assert isinstance(cp.factors[0], np.ndarray)
     xt = torch.as_tensor(x, device="cuda")
     with pytest.raises(NotImplementedError):
-        gb300.non_negative_parafac_hals(xt, 2, nn_modes=[0])
-    with pytest.raises(NotImplementedError):
         gb300.non_negative_parafac_hals(xt, 2, fixed_modes=[2])
+
+
+@pytest.mark.parametrize("case", ["nn_hals_modes_02", "nn_hals_normalize"])
+def test_hals_nn_modes_subset_and_normalize_match_reference(gb300, golden, case):
+    """A mode outside nn_modes takes the least-squares update
+    (tensorly/decomposition/_nn_cp.py:337-341); normalize_factors renormalises
+    after every updated mode but the last and after every iteration, with the
+    weights in the normal equations (:316-320, :342-343, :373-374).  f64,
+    against the reference's runs."""
+    run = golden["runs"][case]
+    x = regenerate(run)
+    kw = dict(run["kwargs"])
+    rank = kw.pop("rank")
+    (w, f), errs = gb300.non_negative_parafac_hals(torch.as_tensor(x, device="cuda"), rank,
+                                                   return_errors=True, **kw)
+    assert len(errs) == len(run["errors"])
+    np.testing.assert_allclose(errs, run["errors"], rtol=1e-9, atol=1e-12)
+    np.testing.assert_allclose(host(w), run["weights"], rtol=1e-8, atol=1e-10)
+    for a, b in zip(f, run["factors"]):
+        np.testing.assert_allclose(host(a), b, rtol=1e-8, atol=1e-8 * np.abs(b).max())
 
 
 @pytest.mark.parametrize("dtype,rank", [(np.float64, 130), (np.float64, 100),

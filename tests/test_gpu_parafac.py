@@ -148,12 +148,35 @@ def test_parafac_linesearch_and_orthogonalise_match_reference(gb300, golden, cas
         assert rel(host(a), b) < 1e-10
 
 
+@pytest.mark.parametrize("case", ["cp_mask", "cp_mask_linesearch"])
+def test_masked_parafac_matches_reference(gb300, golden, case):
+    """Missing entries refilled from the model after every sweep
+    (tensorly/decomposition/_cp.py:194-207, :441-446), with and without the
+    line search, f64, against the reference's runs to 1e-10."""
+    run = golden["runs"][case]
+    x = regenerate(run)
+    kw = dict(run["kwargs"])
+    rank = kw.pop("rank")
+    shape = run["gen"]["shape"]
+    mask = (np.random.RandomState(run["gen"]["seed"] + 1000).rand(*shape)
+            < run["mask_keep"]).astype(x.dtype)
+    xt = torch.as_tensor(x, device="cuda")
+    (w, f), errs = gb300.parafac(xt, rank, mask=torch.as_tensor(mask, device="cuda"),
+                                 return_errors=True, **kw)
+    assert len(errs) == len(run["errors"])
+    np.testing.assert_allclose(errs, run["errors"], rtol=1e-10, atol=1e-13)
+    assert rel(host(w), run["weights"]) < 1e-10
+    for a, b in zip(f, run["factors"]):
+        assert rel(host(a), b) < 1e-10
+    assert torch.equal(xt, torch.as_tensor(x, device="cuda")), "the input tensor was modified"
+
+
 def test_unsupported_options_raise(gb300):
     x = torch.rand(4, 5, 6, device="cuda", dtype=torch.float64)
-    for kw in ({"mask": torch.ones_like(x)}, {"sparsity": 0.1}):
+    for kw in ({"sparsity": 0.1}, {"mask": torch.ones_like(x), "init": "svd"}):
         with pytest.raises(NotImplementedError):
-            gb300.parafac(x, 2, init="random", **kw)
-    for kw in ({"linesearch": True}, {"orthogonalise": True}):
+            gb300.parafac(x, 2, **dict({"init": "random"}, **kw))
+    for kw in ({"linesearch": True}, {"orthogonalise": True}, {"mask": torch.ones_like(x)}):
         with pytest.raises(NotImplementedError):
             gb300.parafac(x.float(), 2, init="random", precision="bf16", **kw)
     with pytest.raises(ValueError):

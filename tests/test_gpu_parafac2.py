@@ -6,11 +6,13 @@ factors and projections (the projections are polar factors from R x R
 eigenproblems instead of the reference's SVD); f32 1e-3 and 1e-2.  The QR of
 the random start matches NumPy's linalg.qr, signs included, to 1e-12."""
 
+import warnings
+
 import numpy as np
 import pytest
 import torch
 
-from golden_inputs import regenerate
+from golden_inputs import regenerate, slice_masks
 
 pytestmark = pytest.mark.gpu
 
@@ -19,14 +21,24 @@ def host(t):
     return t.detach().cpu().numpy() if isinstance(t, torch.Tensor) else np.asarray(t)
 
 
-@pytest.mark.parametrize("case", ["p2_random", "p2_svd", "p2_nols", "p2_normalize", "p2_f32"])
+@pytest.mark.parametrize("case", ["p2_random", "p2_svd", "p2_nols", "p2_normalize", "p2_f32",
+                                  "p2_nn_all", "p2_nn_02", "p2_mask", "p2_mask_svd"])
 def test_parafac2_matches_reference(gb300, golden, case):
+    """Dense, non-negative (nn_modes through non_negative_parafac_hals and
+    the clipped line search) and masked (refilled missing entries, masked
+    error) runs against the reference's."""
     run = golden["runs"][case]
     xs = regenerate(run)
     kw = dict(run["kwargs"])
     rank = kw.pop("rank")
-    (w, f, p), errs = gb300.parafac2([torch.as_tensor(x, device="cuda") for x in xs], rank,
-                                     return_errors=True, **kw)
+    if "mask_keep" in run["gen"]:
+        kw["mask"] = [torch.as_tensor(m, device="cuda") for m in slice_masks(run["gen"])]
+    xt = [torch.as_tensor(x, device="cuda") for x in xs]
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore", UserWarning)   # the reference's mode-1 warning
+        (w, f, p), errs = gb300.parafac2(xt, rank, return_errors=True, **kw)
+    for x, t in zip(xs, xt):
+        assert np.array_equal(host(t), x), "the input slices were modified"
     f32 = xs[0].dtype == np.float32
     assert len(errs) == len(run["errors"])
     np.testing.assert_allclose(errs, run["errors"], rtol=1e-3 if f32 else 1e-7)
@@ -60,5 +72,5 @@ def test_parafac2_to_tensor_and_host_input(gb300, golden):
         ref = (pk @ B) * (A[k] * w) @ C.T
         np.testing.assert_allclose(full[k, :pk.shape[0]], ref, rtol=1e-12, atol=1e-12)
         assert (full[k, pk.shape[0]:] == 0).all()
-    with pytest.raises(NotImplementedError):
-        gb300.parafac2(xs, rank, nn_modes="all")
+    with pytest.warns(UserWarning, match="Mode `1` of PARAFAC2"):
+        gb300.parafac2(xs, rank, nn_modes=[1], n_iter_max=2)
