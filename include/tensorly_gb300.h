@@ -133,6 +133,9 @@ int tlgb_mttkrp_bf16(const void* X, int ndim, const int64_t* shape, const void* 
  * when Cholesky fails) that otherwise serves only ill-conditioned V;
  * "no_pdl" = 1 launches the kernels of a CP-ALS sweep without programmatic
  * dependent launch (each then starts only when its predecessor has ended);
+ * "tc_test_starve" = 1 is for testing the timeout path: the tensor-core
+ * MTTKRP issues no copies, its waits give up after 1 ms, and the workspace
+ * status (tlgb_workspace_status) reads TLGB_ETIMEOUT;
  * "batched_threads_small" / "_medium" / "_large" = threads per CTA (128, 256
  * or 512; 4, 2 or 1 CTAs per SM) of tlgb_cp_als_batched for the tensors
  * whose padded size fits 128-, 256-thread CTAs' shared memory, or neither.
@@ -527,6 +530,14 @@ int tlgb_cp_randomised_iteration(int dtype, const void* X, int ndim, const int64
 #define TLGB_CONS_L2 3             /* x - x * param / max(||x||, param) */
 #define TLGB_CONS_L2_SQUARE 4      /* x / (1 + 2 param) */
 #define TLGB_CONS_NORMALIZE 5      /* x / max |x| */
+/* column-wise and rank-based operators (tlgb_proximal_matrix, tlgb_cp_constrained) */
+#define TLGB_CONS_UNIMODALITY 6    /* unimodal fit of each column */
+#define TLGB_CONS_SIMPLEX 7        /* projection of each column on the simplex of size param */
+#define TLGB_CONS_NORM_SPARSITY 8  /* the param largest |x| kept, then x / ||x|| */
+#define TLGB_CONS_SOFT_SPARSITY 9  /* simplex projection of |x| (size param) times sign(x) */
+#define TLGB_CONS_SMOOTHNESS 10    /* (I (1 + 2 param) - param (sub + super diagonal))^-1 x */
+#define TLGB_CONS_MONOTONICITY 11  /* non-decreasing fit of each column (param != 0: non-increasing) */
+#define TLGB_CONS_HARD_SPARSITY 12 /* the param largest |x| kept, the rest set to 0 */
 
 /*
  * Constrained CP by AO-ADMM (tensorly/decomposition/_constrained_cp.py:166-435,
@@ -557,6 +568,24 @@ int tlgb_cp_constrained(int dtype, const void* X, int ndim, const int64_t* shape
 size_t tlgb_proximal_workspace_bytes(void);
 int tlgb_proximal(int dtype, const void* X, int64_t n, int kind, double param, void* out,
                   void* workspace, size_t workspace_bytes, void* stream);
+
+/*
+ * proximal_matrix: out = the proximal operator `kind` of a rows x cols
+ * row-major matrix Y (a factor matrix; tensorly/tenalg/proximal.py:148-628),
+ * including the column-wise operators unimodality_prox (:359-441),
+ * simplex_prox (:558-599), soft_sparsity_prox (:529-555), smoothness_prox
+ * (:270-289), monotonicity_prox (:292-356) and the rank-based
+ * hard_thresholding (:602-628) and normalized_sparsity_prox (:496-526);
+ * the whole-matrix kinds are tlgb_proximal's.  A column must fit one CTA's
+ * shared memory (else TLGB_EUNSUPPORTED).  Entries of equal magnitude at the
+ * hard-thresholding cut are kept in index order (the reference's argsort
+ * leaves that order unspecified).  out must not alias Y.
+ */
+int tlgb_proximal_matrix_workspace_size(int dtype, int64_t rows, int64_t cols, int kind,
+                                        size_t* bytes);
+int tlgb_proximal_matrix(int dtype, const void* Y, int64_t rows, int64_t cols, int kind,
+                         double param, void* out, void* workspace, size_t workspace_bytes,
+                         void* stream);
 
 /*
  * gemm: C (M x N, row-major) = sum_k A[m*sam + k*sak] * B[k*sbk + n*sbn]
@@ -592,6 +621,36 @@ int tlgb_hals_nnls_workspace_size(int dtype, int64_t I, int64_t R, size_t* bytes
 int tlgb_hals_nnls(int dtype, const void* MtU, const void* UtU, void* V, int64_t I, int64_t R,
                    int n_iter_max, double tol, double sparsity, void* workspace,
                    size_t workspace_bytes, void* stream);
+
+/*
+ * kronecker: out = mats[0] (x) mats[1] (x) ... (row-major matrices of
+ * rows[k] x cols[k]), the first varying slowest
+ * (tensorly/tenalg/core_tenalg/_kronecker.py).
+ */
+int tlgb_kronecker(int dtype, int n_mats, const void* const* mats, const int64_t* rows,
+                   const int64_t* cols, void* out, void* stream);
+
+/*
+ * tucker_normalize: in place, every column of factor k (rows[k] x ranks[k],
+ * row-major) divided by its norm (a zero column kept) and the core
+ * (ranks[0] x ... , row-major) multiplied along each mode by those norms.
+ * Replaces tensorly/tucker_tensor.py:78-102 (tucker_normalize).
+ */
+int tlgb_tucker_normalize_workspace_size(int ndim, const int64_t* ranks, size_t* bytes);
+int tlgb_tucker_normalize(int dtype, int ndim, const int64_t* rows, const int64_t* ranks,
+                          void* const* factors, void* core, void* workspace,
+                          size_t workspace_bytes, void* stream);
+
+/*
+ * active_set_nnls: x (n, device, in/out, the start) minimises
+ * ||Utm - UtU x|| subject to x >= 0 by the active-set method of
+ * tensorly/solvers/nnls.py:275-406, at most n_iter_max iterations, stop when
+ * the largest gradient entry on the active set is <= tol.  One CTA; n <= 128
+ * (else TLGB_EUNSUPPORTED).  *status (device int) receives TLGB_OK, or
+ * TLGB_ESINGULAR where the reference's solve would raise.
+ */
+int tlgb_active_set_nnls(int dtype, const void* UtU, const void* Utm, void* x, int64_t n,
+                         int n_iter_max, double tol, int* status, void* stream);
 
 /*
  * fista_tucker_core: the reference's FISTA (tensorly/solvers/nnls.py:177-272,

@@ -32,7 +32,7 @@ __all__ = [
     "cp_to_vec", "tucker_to_unfolded", "tucker_to_vec", "sample_khatri_rao",
     "randomised_parafac", "sparsify_tensor", "error_calc_ext", "validate_constraints", "proximal_operator", "admm",
     "initialize_constrained_parafac", "constrained_parafac", "non_negative_tucker", "fista",
-    "non_negative_tucker_hals", "active_set_nnls", "kronecker",
+    "non_negative_tucker_hals", "active_set_nnls", "kronecker", "tucker_normalize",
 ]
 
 
@@ -691,8 +691,8 @@ def validate_constraints(n_const=1, order=0, **given):
 
 
 def proximal_operator(tensor, n_const=1, order=0, **given):
-    """tensorly/tenalg/proximal.py:148-267 for the constraints that act on the
-    whole matrix (non_negative, l1_reg, l2_reg, l2_square_reg, normalize)."""
+    """tensorly/tenalg/proximal.py:148-267: the whole-matrix operators here,
+    the column-wise and sparsity ones from proximal_oracle (:270-628)."""
     if n_const is None:
         return tensor
     constraint, parameter = validate_constraints(n_const=n_const, order=order, **given)
@@ -710,6 +710,21 @@ def proximal_operator(tensor, n_const=1, order=0, **given):
         return tensor / (1 + 2 * parameter)
     if constraint == "normalize":
         return tensor / np.max(np.abs(tensor))
+    from . import proximal_oracle as po             # the column-wise and sparsity operators
+    if constraint == "unimodality":
+        return po.unimodality_prox(tensor)
+    if constraint == "simplex":
+        return po.simplex_prox(tensor, parameter)
+    if constraint == "normalized_sparsity":
+        return po.normalized_sparsity_prox(tensor, parameter)
+    if constraint == "soft_sparsity":
+        return po.soft_sparsity_prox(tensor, parameter)
+    if constraint == "smoothness":
+        return po.smoothness_prox(tensor, parameter)
+    if constraint == "monotonicity":
+        return po.monotonicity_prox(tensor)
+    if constraint == "hard_sparsity":
+        return po.hard_thresholding(tensor, parameter)
     raise NotImplementedError(f"oracle restates no {constraint} proximal operator")
 
 
@@ -765,6 +780,19 @@ def fista(UtM, UtU, x=None, n_iter_max=100, non_negative=True, sparsity_coef=0, 
         if nrm < tol * norm_0:
             break
     return x
+
+
+def tucker_normalize(tucker_tensor):
+    """tensorly/tucker_tensor.py:78-102: unit-norm factor columns, the norms
+    multiplied into the core along each mode in mode order."""
+    core, factors = tucker_tensor
+    out = []
+    for i, factor in enumerate(factors):
+        scales = np.linalg.norm(factor, axis=0)
+        nz = np.where(scales == 0, np.ones(scales.shape, dtype=factor.dtype), scales)
+        core = core * np.reshape(scales, (1,) * i + (-1,) + (1,) * (core.ndim - i - 1))
+        out.append(factor / np.reshape(nz, (1, -1)))
+    return core, out
 
 
 def kronecker(matrices):
@@ -830,9 +858,9 @@ def active_set_nnls(Utm, UtU, x=None, n_iter_max=100, tol=10e-8):
 def non_negative_tucker_hals(tensor, rank, n_iter_max=100, init="svd", svd="truncated_svd",
                              tol=1e-8, sparsity_coefficients=None, core_sparsity_coefficient=None,
                              random_state=None, return_errors=False, exact=False,
-                             algorithm="fista"):
-    """tensorly/decomposition/_tucker.py:457-691 (no fixed modes, not
-    normalised; algorithm 'fista' or 'active_set')."""
+                             algorithm="fista", normalize_factors=False):
+    """tensorly/decomposition/_tucker.py:457-691 (no fixed modes; algorithm
+    'fista' or 'active_set')."""
     rank = validate_tucker_rank(tensor.shape, rank=rank)
     n_modes = tensor.ndim
     if sparsity_coefficients is None or not isinstance(sparsity_coefficients, (list, tuple)):
@@ -876,6 +904,8 @@ def non_negative_tucker_hals(tensor, rank, n_iter_max=100, init="svd", svd="trun
         if iteration > 1:
             if tol and abs(rec_errors[-2] - rec_errors[-1]) < tol:
                 break
+        if normalize_factors:
+            nn_core, nn_factors = tucker_normalize((nn_core, nn_factors))
     if return_errors:
         return (nn_core, nn_factors), rec_errors
     return nn_core, nn_factors
@@ -1223,9 +1253,9 @@ def initialize_tucker(tensor, rank, modes, random_state, init="svd", svd="trunca
 
 
 def non_negative_tucker(tensor, rank, n_iter_max=10, init="svd", tol=10e-5, random_state=None,
-                        return_errors=False):
+                        return_errors=False, normalize_factors=False):
     """tensorly/decomposition/_tucker.py:348-454 (multiplicative updates, not
-    verbose, normalize_factors=False), with the reference's explicit B."""
+    verbose), with the reference's explicit B."""
     rank = validate_tucker_rank(tensor.shape, rank=rank)
     epsilon = 10e-12
     nn_core, nn_factors = initialize_tucker(tensor, rank, range(tensor.ndim), init=init,
@@ -1255,6 +1285,8 @@ def non_negative_tucker(tensor, rank, n_iter_max=10, init="svd", tol=10e-5, rand
         rec_errors.append(rec_error)
         if iteration > 1 and abs(rec_errors[-2] - rec_errors[-1]) < tol:
             break
+        if normalize_factors:
+            nn_core, nn_factors = tucker_normalize((nn_core, nn_factors))
     if return_errors:
         return (nn_core, nn_factors), rec_errors
     return nn_core, nn_factors

@@ -232,6 +232,12 @@ SIGNATURES = [
     ("tlgb_proximal", ctypes.c_int,
      [ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_double,
       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    ("tlgb_proximal_matrix_workspace_size", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_int64, ctypes.c_int64, ctypes.c_int,
+      ctypes.POINTER(ctypes.c_size_t)]),
+    ("tlgb_proximal_matrix", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int,
+      ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     ("tlgb_gemm", ctypes.c_int,
      [ctypes.c_int, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p,
       ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
@@ -257,6 +263,16 @@ SIGNATURES = [
       ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     ("tlgb_inv_sqrt", ctypes.c_int,
      [ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p]),
+    ("tlgb_kronecker", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_int, _c_vpp, _c_i64p, _c_i64p, ctypes.c_void_p, ctypes.c_void_p]),
+    ("tlgb_active_set_nnls", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+      ctypes.c_int, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p]),
+    ("tlgb_tucker_normalize_workspace_size", ctypes.c_int,
+     [ctypes.c_int, _c_i64p, ctypes.POINTER(ctypes.c_size_t)]),
+    ("tlgb_tucker_normalize", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_int, _c_i64p, _c_i64p, _c_vpp, ctypes.c_void_p, ctypes.c_void_p,
+      ctypes.c_size_t, ctypes.c_void_p]),
     ("tlgb_mask_where", ctypes.c_int,
      [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double,
       ctypes.c_int64, ctypes.c_void_p]),

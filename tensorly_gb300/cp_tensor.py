@@ -321,6 +321,30 @@ def cp_to_vec(cp_tensor):
     return cp_to_tensor(cp_tensor).reshape(-1)
 
 
+def tucker_normalize(tucker_tensor):
+    """Unit-norm factor columns with the norms multiplied into the core
+    (tensorly/tucker_tensor.py:78-102), by ``tlgb_tucker_normalize``.
+    Returns a new TuckerTensor of CUDA tensors."""
+    core, factors = tucker_tensor
+    if not isinstance(core, torch.Tensor) or not core.is_cuda:
+        raise TypeError("tensorly_gb300 Tucker helpers take CUDA tensors")
+    core = core.contiguous().clone()
+    factors = [f.to(core.dtype).contiguous().clone() for f in factors]
+    n = len(factors)
+    ranks = _lib.i64_array([int(f.shape[1]) for f in factors])
+    rows = _lib.i64_array([int(f.shape[0]) for f in factors])
+    if tuple(core.shape) != tuple(int(f.shape[1]) for f in factors):
+        raise ValueError("tucker_normalize: the core shape must match the factor ranks")
+    lib = _lib.lib()
+    nbytes = _lib.ctypes.c_size_t(0)
+    _lib.check(lib.tlgb_tucker_normalize_workspace_size(n, ranks, _lib.ctypes.byref(nbytes)))
+    ws = workspace(nbytes.value, core.device)
+    _lib.check(lib.tlgb_tucker_normalize(dtype_code(core), n, rows, ranks,
+                                         _lib.ptr_array([ptr(f) for f in factors]), ptr(core),
+                                         ptr(ws), ws.numel(), stream_of(core)))
+    return TuckerTensor((core, factors))
+
+
 def tucker_to_tensor(tucker_tensor, skip_factor=None, transpose_factors=False, modes=None):
     """tensorly/tucker_tensor.py:50-75: multi_mode_dot of the core."""
     from .tenalg import multi_mode_dot

@@ -1,8 +1,10 @@
 // Constrained CP by AO-ADMM (tensorly/decomposition/_constrained_cp.py:166-435)
 // with the ADMM solver tensorly/solvers/admm.py:5-135 and the proximal
-// operators tensorly/tenalg/proximal.py:148-671 that act on a whole factor
-// matrix: non_negative, l1_reg (soft thresholding), l2_reg, l2_square_reg,
-// normalize.
+// operators tensorly/tenalg/proximal.py:148-671: those that act on a whole
+// factor matrix entry by entry (non_negative, l1_reg (soft thresholding),
+// l2_reg, l2_square_reg, normalize) here, the column-wise and rank-based ones
+// (unimodality, simplex, soft / normalized / hard sparsity, smoothness,
+// monotonicity) by the kernels of prox_columns.cu.
 //
 // Per free mode: V = (Hadamard of the other Grams) + rho I, rho = trace / R,
 // factorised once (the CP-ALS factorisation, f64); M = MTTKRP; then up to
@@ -19,6 +21,7 @@
 
 #include "als_kernels.cuh"
 #include "mttkrp_simt.cuh"
+#include "prox_columns.cuh"
 
 namespace tlgb {
 namespace {
@@ -212,6 +215,48 @@ __global__ void k_cons_inner(const T* __restrict__ M, const T* __restrict__ A, i
   if (threadIdx.x == 0) part[blockIdx.x] = t;
 }
 
+// y = S - dual, the input of a column-wise proximal operator.
+template <typename T>
+__global__ void k_cons_diff(const T* __restrict__ S, const T* __restrict__ dual, int64_t n,
+                            const ConsState* cs, T* __restrict__ Y) {
+  if (cs->stop) return;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x)
+    Y[e] = S[e] - dual[e];
+}
+
+// As k_cons_prox, with x = P, the proximal operator already applied.
+template <typename T>
+__global__ void k_cons_take(const T* __restrict__ S, T* __restrict__ x, T* __restrict__ dual,
+                            const T* __restrict__ P, int64_t n, const ConsState* cs,
+                            double* part) {
+  if (cs->stop) return;
+  __shared__ double red[kConsThreads / 32];
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const T s = S[e];
+    const T xo = x[e];
+    const T xn = P[e];
+    const T dn = (dual[e] + xn) - s;
+    x[e] = xn;
+    dual[e] = dn;
+    const double dr = (double)(xn - s), pr = (double)(xn - xo);
+    a0 += dr * dr;
+    a1 += pr * pr;
+    a2 += (double)xn * (double)xn;
+    a3 += (double)dn * (double)dn;
+  }
+  const double t0 = cta_sum(a0, red), t1 = cta_sum(a1, red), t2 = cta_sum(a2, red),
+               t3 = cta_sum(a3, red);
+  if (threadIdx.x == 0) {
+    part[4 * blockIdx.x + 0] = t0;
+    part[4 * blockIdx.x + 1] = t1;
+    part[4 * blockIdx.x + 2] = t2;
+    part[4 * blockIdx.x + 3] = t3;
+  }
+}
+
 // Whole-matrix proximal operator out = prox(X) (no ADMM state).
 template <typename T>
 __global__ void k_prox_apply(const T* __restrict__ X, int64_t n, int kind, double param,
@@ -224,6 +269,7 @@ __global__ void k_prox_apply(const T* __restrict__ X, int64_t n, int kind, doubl
 
 struct ConsLayout {
   size_t ctrl, cs, G, V2, fac, perm, vmat, w32, gpart, partial, M, B, S, dual, part, bytes;
+  size_t P, pscratch;   // column-wise operators: their output and scratch
 };
 
 template <typename T>
@@ -257,6 +303,9 @@ int cons_layout(const Shape& sh, int64_t R, std::vector<MttkrpPlan>* plans, Cons
   L->S = take(sizeof(T) * (size_t)imax * R);
   L->dual = take(sizeof(T) * (size_t)dual_total);
   L->part = take(sizeof(double) * 4 * kConsBlocks);
+  L->P = take(sizeof(T) * (size_t)imax * R);
+  L->pscratch = take(std::max(prox_matrix_scratch_bytes(dtype, imax, R, TLGB_CONS_UNIMODALITY),
+                              prox_matrix_scratch_bytes(dtype, imax, R, TLGB_CONS_HARD_SPARSITY)));
   L->bytes = align_up(off, 256);
   return TLGB_OK;
 }
@@ -290,7 +339,16 @@ int cons_run(const T* X, const Shape& sh, T* const* factors, int64_t R, const in
   T* S = reinterpret_cast<T*>(base + L.S);
   T* dual0 = reinterpret_cast<T*>(base + L.dual);
   double* part = reinterpret_cast<double*>(base + L.part);
+  T* Pbuf = reinterpret_cast<T*>(base + L.P);
+  void* pscratch = base + L.pscratch;
   const int N = sh.ndim;
+  for (int q = 0; q < n_free; ++q) {
+    const int mode = free_modes[q];
+    if (prox_is_matrix_kind(kinds[mode])) {
+      rc = prox_matrix_check(TypeCode<T>::value, sh.dim[mode], R, kinds[mode]);
+      if (rc) return rc;
+    }
+  }
   const int RR = (int)(R * R);
   const int nparts = solve_blocks_for([&] {
     int64_t m = 0;
@@ -351,15 +409,25 @@ int cons_run(const T* X, const Shape& sh, T* const* factors, int64_t R, const in
         rc = als_launch_solve<T>(B, 1, I, (int)R, fac, perm, vmat, w32, S, nullptr, gpart,
                                  nullptr, ctrl, kIrMaxPasses, &sb, st);
         if (rc) return rc;
-        if (glob) {
-          k_cons_glob<T><<<nb, kConsThreads, 0, st>>>(S, dual[mode], IR, kind, cs, part);
+        if (prox_is_matrix_kind(kind)) {
+          k_cons_diff<T><<<nb, kConsThreads, 0, st>>>(S, dual[mode], IR, cs, B);
           TLGB_LAUNCH_CHECK();
-          k_cons_glob_final<<<1, 32, 0, st>>>(part, (int)nb, kind, cs);
+          rc = prox_matrix_launch<T>(B, Pbuf, I, R, kind, params[mode], pscratch, &cs->stop, st);
+          if (rc) return rc;
+          k_cons_take<T><<<nb, kConsThreads, 0, st>>>(S, factors[mode], dual[mode], Pbuf, IR,
+                                                      cs, part);
+          TLGB_LAUNCH_CHECK();
+        } else {
+          if (glob) {
+            k_cons_glob<T><<<nb, kConsThreads, 0, st>>>(S, dual[mode], IR, kind, cs, part);
+            TLGB_LAUNCH_CHECK();
+            k_cons_glob_final<<<1, 32, 0, st>>>(part, (int)nb, kind, cs);
+            TLGB_LAUNCH_CHECK();
+          }
+          k_cons_prox<T><<<nb, kConsThreads, 0, st>>>(S, factors[mode], dual[mode], IR, kind,
+                                                      params[mode], cs, part);
           TLGB_LAUNCH_CHECK();
         }
-        k_cons_prox<T><<<nb, kConsThreads, 0, st>>>(S, factors[mode], dual[mode], IR, kind,
-                                                    params[mode], cs, part);
-        TLGB_LAUNCH_CHECK();
         k_cons_check<<<1, 32, 0, st>>>(part, (int)nb, tol_inner, cs);
         TLGB_LAUNCH_CHECK();
       }
@@ -462,7 +530,7 @@ extern "C" int tlgb_cp_constrained(int dtype, const void* X, int ndim, const int
                    "constrained_parafac: free modes must be ascending and in range");
   for (int k = 0; k < ndim; ++k) {
     TLGB_CHECK_ARG(factors[k] != nullptr, "constrained_parafac: null factor");
-    TLGB_CHECK_ARG(kinds[k] >= kConsNone && kinds[k] <= kConsNormalize,
+    TLGB_CHECK_ARG(kinds[k] >= TLGB_CONS_NONE && kinds[k] <= TLGB_CONS_HARD_SPARSITY,
                    "constrained_parafac: unknown constraint kind");
   }
   TLGB_CHECK_ARG(n_iter_max >= 0 && n_iter_max_inner >= 1, "constrained_parafac: bad iterations");

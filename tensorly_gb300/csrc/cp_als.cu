@@ -177,6 +177,26 @@ struct Runner {
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   // optional timing events around each mode's MTTKRP (recorded into the graph)
   cudaEvent_t ev_mt[2][kMaxModes] = {};
+  // TMA descriptors of the tensor-core MTTKRPs, encoded once per run
+  TcMaps tc_maps[kMaxModes];
+  TcMaps tcr_maps[kMaxModes][3];
+
+  int encode_maps() {
+    const __nv_bfloat16* planes[3] = {B.xbf, B.xsplit[0], B.xsplit[1]};
+    for (int k = 0; k < sh.ndim; ++k) {
+      if (P->tc[k].valid) {
+        int rc = mttkrp_tc_encode(P->tc[k], B.xbf, B.fbt, kFactorPlanes, &tc_maps[k]);
+        if (rc) return rc;
+      }
+      if (P->refine_tc)
+        for (int j = 0; j < 3; ++j) {
+          int rc = mttkrp_tc_encode(P->tcr[k][j], planes[j], B.fbt, kFactorPlanes,
+                                    &tcr_maps[k][j]);
+          if (rc) return rc;
+        }
+    }
+    return TLGB_OK;
+  }
 
   // Enqueues one sweep.  kind: kSweepNative (SIMT MTTKRP in the tensor dtype),
   // kSweepBf16 (bf16 tensor, two-plane factor, tensor cores), kSweepF32Tc
@@ -228,9 +248,9 @@ struct Runner {
       const void* partial;
       if (tc && P->tc[mode].valid) {
         if constexpr (sizeof(T) == 4) {
-          rc = mttkrp_tc_launch(P->tc[mode], B.xbf, (const float* const*)cf, B.fbt,
-                                kFactorPlanes, (const float*)mw, (float*)B.tc_partial, done,
-                                &B.ctrl->tc_err, st);
+          rc = mttkrp_tc_launch_maps(P->tc[mode], tc_maps[mode], (const float* const*)cf,
+                                     (const float*)mw, (float*)B.tc_partial, done,
+                                     &B.ctrl->tc_err, st);
         }
         if (rc) return rc;
         splits = P->tc[mode].splits;
@@ -240,13 +260,12 @@ struct Runner {
         // its own run of partial tiles; the solve sums all of them
         splits = 0;
         if constexpr (sizeof(T) == 4) {
-          const __nv_bfloat16* planes[3] = {B.xbf, B.xsplit[0], B.xsplit[1]};
           for (int j = 0; j < 3 && !rc; ++j) {
             const TcPlan& tp = P->tcr[mode][j];
-            rc = mttkrp_tc_launch(tp, planes[j], (const float* const*)cf, B.fbt, kFactorPlanes,
-                                  (const float*)mw,
-                                  (float*)B.tc_partial + (size_t)splits * tp.I_out * tp.R, done,
-                                  &B.ctrl->tc_err, st);
+            rc = mttkrp_tc_launch_maps(tp, tcr_maps[mode][j], (const float* const*)cf,
+                                       (const float*)mw,
+                                       (float*)B.tc_partial + (size_t)splits * tp.I_out * tp.R,
+                                       done, &B.ctrl->tc_err, st);
             splits += tp.splits;
           }
         }
@@ -380,6 +399,8 @@ int run(const T* X, const Shape& sh, int64_t R, T* const* factors, T* weights,
   if (mixed) {
     rc = mttkrp_tc_prepare();
     if (rc) return rc;
+    rc = run.encode_maps();
+    if (rc) return rc;
   }
 
   StreamGuard aux;
@@ -482,10 +503,12 @@ int run(const T* X, const Shape& sh, int64_t R, T* const* factors, T* weights,
       if (((s + 1) % check_every) == 0 || end_of_phase) {
         TLGB_CUDA_TRY(cudaMemcpyAsync(&hc, run.B.ctrl, sizeof(AlsCtrl), cudaMemcpyDeviceToHost, st));
         TLGB_CUDA_TRY(cudaStreamSynchronize(st));
-        if (hc.status != TLGB_OK)
-          return set_error(hc.status, "cp_als: singular normal equations (LU found a zero pivot)");
+        // a timed-out MTTKRP leaves garbage partials behind it, so it is
+        // reported before anything that garbage may have caused
         if (hc.tc_err != 0)
           return set_error(TLGB_ETIMEOUT, "cp_als: tensor-core MTTKRP pipeline wait timed out");
+        if (hc.status != TLGB_OK)
+          return set_error(hc.status, "cp_als: singular normal equations (LU found a zero pivot)");
         if (o.callback) {
           while (reported < hc.iter) {
             double e = 0.0;
@@ -512,6 +535,8 @@ int run(const T* X, const Shape& sh, int64_t R, T* const* factors, T* weights,
   }
   TLGB_CUDA_TRY(cudaMemcpyAsync(&hc, run.B.ctrl, sizeof(AlsCtrl), cudaMemcpyDeviceToHost, st));
   TLGB_CUDA_TRY(cudaStreamSynchronize(st));
+  if (hc.tc_err != 0)
+    return set_error(TLGB_ETIMEOUT, "cp_als: tensor-core MTTKRP pipeline wait timed out");
   if (hc.status != TLGB_OK)
     return set_error(hc.status, "cp_als: singular normal equations (LU found a zero pivot)");
   const int n = std::min(hc.iter, o.n_iter_max);

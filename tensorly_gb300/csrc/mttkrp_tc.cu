@@ -58,7 +58,11 @@ struct TcArgs {
   float* partial;
   int* err;
   const int* skip;
+  // Test of the timeout path (tuning key "tc_test_starve"): the producer
+  // issues no copies, and the MMA and epilogue waits give up after 1 ms.
+  int starve;
 };
+constexpr unsigned long long kStarveWaitNs = 1000000ull;  // 1 ms
 
 // ------------------------------------------------------------ PTX helpers
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -90,15 +94,17 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t addr, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait; returns false (and records the timeout) if it gave up.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, bool& failed) {
+// Bounded wait (limit_ns of wall time); returns false (and records the
+// timeout) if it gave up.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, bool& failed,
+                                          unsigned long long limit_ns = kWaitNs) {
   if (failed) return false;
   const uint32_t addr = smem_u32(bar);
   if (mbar_try_wait(addr, parity)) return true;
   const unsigned long long t0 = now_ns();
   while (true) {
     if (mbar_try_wait(addr, parity)) return true;
-    if (now_ns() - t0 > kWaitNs) {
+    if (now_ns() - t0 > limit_ns) {
       atomicExch(err, TLGB_ETIMEOUT);
       failed = true;
       return false;
@@ -322,13 +328,13 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant_
           ++i;
           return true;
         };
-        const int64_t pre = min((int64_t)S, t_end - t_begin);
+        const int64_t pre = a.starve ? 0 : min((int64_t)S, t_end - t_begin);
         int64_t t = t_begin;
         for (; t < t_begin + pre; ++t)
           if (!issue()) break;
         griddep_wait();
         const bool skipped = a.skip && *a.skip;
-        if (!skipped && !failed) {
+        if (!skipped && !failed && !a.starve) {
           mbar_expect_tx(bfull, (uint32_t)b_bytes);
           for (int kcb = 0; kcb < KC; ++kcb) {
             unsigned char* dst = sB + kcb * NB * 128;
@@ -354,9 +360,10 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant_
       // ------------------------------------------------------------ MMA issue
       griddep_wait();
       const bool skipped = a.skip && *a.skip;
+      const unsigned long long lim = a.starve ? kStarveWaitNs : kWaitNs;
       if (lane == 0 && !skipped) {
         constexpr uint32_t idesc = make_idesc(NB, MN ? 1 : 0);
-        mbar_wait(bfull, 0, a.err, failed);
+        mbar_wait(bfull, 0, a.err, failed, lim);
         int64_t oc = 0;
         int kc = (int)(t_begin % KC);
         int stage = 0;
@@ -366,10 +373,11 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant_
           const bool last_of_o = (t + 1 == t_end) || (kc == KC - 1);
           const int buf = (int)(oc & 1);
           if (first_of_o) {
-            if (!mbar_wait(&dempty[buf], (uint32_t)(((oc >> 1) & 1) ^ 1), a.err, failed)) break;
+            if (!mbar_wait(&dempty[buf], (uint32_t)(((oc >> 1) & 1) ^ 1), a.err, failed, lim))
+              break;
             tc_fence_after();
           }
-          if (!mbar_wait(&full[stage], phase, a.err, failed)) break;
+          if (!mbar_wait(&full[stage], phase, a.err, failed, lim)) break;
           tc_fence_after();
           const uint32_t a_base = smem_u32(sA + stage * kStageBytes);
           const uint32_t b_base = smem_u32(sB + kc * NB * 128);
@@ -434,7 +442,9 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant_
           if (e < RP) s_sm[buf * RP + e] = s_next;
           // the next slice's scale loads overlap this slice's TMEM traffic
           if (e < RP && o < o_last) s_next = scale_of(o + 1);
-          if (e == 0) ep_ok[buf] = mbar_wait(&dfull[buf], (uint32_t)((oc >> 1) & 1), a.err, failed) ? 1 : 0;
+          if (e == 0)
+            ep_ok[buf] = mbar_wait(&dfull[buf], (uint32_t)((oc >> 1) & 1), a.err, failed,
+                                   a.starve ? kStarveWaitNs : kWaitNs) ? 1 : 0;
           asm volatile("bar.sync 1, 128;" ::: "memory");
           if (!ep_ok[buf]) { ep_broken = true; break; }  // uniform across the four epilogue warps
           __syncwarp();            // tcgen05.ld is warp-collective
@@ -744,9 +754,8 @@ int mttkrp_tc_make_plan(const Shape& sh, int64_t rank, int mode, int npl, int fr
   return TLGB_OK;
 }
 
-int mttkrp_tc_launch(const TcPlan& p, const __nv_bfloat16* Xbf, const float* const* factors,
-                     __nv_bfloat16* const* fbt, int fplanes, const float* weights,
-                     float* partial, const int* skip_flag, int* err, cudaStream_t st) {
+int mttkrp_tc_encode(const TcPlan& p, const __nv_bfloat16* Xbf, __nv_bfloat16* const* fbt,
+                     int fplanes, TcMaps* maps) {
   if (!p.valid) return set_error(TLGB_EUNSUPPORTED, "mttkrp_bf16: shape not supported");
   auto enc = encode_fn();
   if (!enc) return set_error(TLGB_EUNSUPPORTED, "cuTensorMapEncodeTiled unavailable");
@@ -800,7 +809,9 @@ int mttkrp_tc_launch(const TcPlan& p, const __nv_bfloat16* Xbf, const float* con
   box[3] = 1;
   for (int j = 0; j < 3; ++j)
     if (gstride[j] % 16 != 0) return set_error(TLGB_EUNSUPPORTED, "mttkrp_bf16: stride not 16-byte aligned");
-  CUtensorMap tx, tf;
+  CUtensorMap& tx = maps->x;
+  CUtensorMap& tf = maps->f;
+  maps->g2 = g2;
   CUresult cr = enc(&tx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<__nv_bfloat16*>(Xbf), gdim,
                     gstride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
                     CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -815,7 +826,15 @@ int mttkrp_tc_launch(const TcPlan& p, const __nv_bfloat16* Xbf, const float* con
            fbox, estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (cr != CUDA_SUCCESS) return set_error(TLGB_ECUDA, "mttkrp_bf16: tensor map for F failed");
+  return TLGB_OK;
+}
 
+int mttkrp_tc_launch_maps(const TcPlan& p, const TcMaps& maps, const float* const* factors,
+                          const float* weights, float* partial, const int* skip_flag, int* err,
+                          cudaStream_t st) {
+  if (!p.valid) return set_error(TLGB_EUNSUPPORTED, "mttkrp_bf16: shape not supported");
+  const CUtensorMap& tx = maps.x;
+  const CUtensorMap& tf = maps.f;
   TcArgs a{};
   a.stages = p.stages;
   for (int j = 0; j < p.n_outer; ++j) {
@@ -823,7 +842,7 @@ int mttkrp_tc_launch(const TcPlan& p, const __nv_bfloat16* Xbf, const float* con
     a.outer_dim[j] = p.outer_dim[j];
   }
   a.n_outer = p.n_outer;
-  a.g2 = g2;
+  a.g2 = maps.g2;
   a.weights = weights;
   a.R = (int)p.R;
   a.I_out = p.I_out;
@@ -835,6 +854,7 @@ int mttkrp_tc_launch(const TcPlan& p, const __nv_bfloat16* Xbf, const float* con
   a.partial = partial;
   a.err = err;
   a.skip = skip_flag;
+  a.starve = tc_tuning().test_starve;
   if (p.npl == 2) {
     switch (p.n_pad) {
       case 16: return launch_mn<16, 2>(p, tx, tf, a, st);
@@ -856,6 +876,15 @@ int mttkrp_tc_launch(const TcPlan& p, const __nv_bfloat16* Xbf, const float* con
     case 32: return launch_mn<32, 3>(p, tx, tf, a, st);
     default: return launch_mn<64, 3>(p, tx, tf, a, st);
   }
+}
+
+int mttkrp_tc_launch(const TcPlan& p, const __nv_bfloat16* Xbf, const float* const* factors,
+                     __nv_bfloat16* const* fbt, int fplanes, const float* weights,
+                     float* partial, const int* skip_flag, int* err, cudaStream_t st) {
+  TcMaps maps;
+  int rc = mttkrp_tc_encode(p, Xbf, fbt, fplanes, &maps);
+  if (rc) return rc;
+  return mttkrp_tc_launch_maps(p, maps, factors, weights, partial, skip_flag, err, st);
 }
 
 int tc_launch_sum_partials(const TcPlan& p, const float* partial, float* out, cudaStream_t st) {
@@ -980,6 +1009,7 @@ extern "C" int tlgb_set_tuning(const char* key, int value) {
   else if (k == "tc_reserve_sms") tc_tuning().reserve_sms = value;
   else if (k == "f64_factorize") tc_tuning().f64_factorize = value;
   else if (k == "no_pdl") tc_tuning().no_pdl = value;
+  else if (k == "tc_test_starve") tc_tuning().test_starve = value;
   else return batched_set_tuning(k, value);   // the batched CP-ALS variants
   return TLGB_OK;
 }

@@ -1,5 +1,6 @@
 // BF16 tensor-core MTTKRP (tcgen05 + TMA, sm_103a).
 #pragma once
+#include <cuda.h>
 #include "common.cuh"
 
 namespace tlgb {
@@ -40,6 +41,7 @@ struct TcTuning {
   int reserve_sms = 0;  // overrides the SMs a plan leaves free (0 = the plan's own)
   int f64_factorize = 0;      // 1: every CP-ALS factorisation takes the f64 Cholesky / LU path
   int no_pdl = 0;             // 1: CP-ALS sweep kernels launch without programmatic dependence
+  int test_starve = 0;        // 1: tensor-core MTTKRP issues no copies (timeout-path test)
 };
 TcTuning& tc_tuning();
 
@@ -58,6 +60,19 @@ int mttkrp_tc_make_plan(const Shape& sh, int64_t rank, int mode, int npl, int fr
 int mttkrp_tc_launch(const TcPlan& p, const __nv_bfloat16* Xbf, const float* const* factors,
                      __nv_bfloat16* const* fbt, int fplanes, const float* weights,
                      float* partial, const int* skip_flag, int* err, cudaStream_t st);
+
+// The launch split in two: the TMA descriptors of a plan and its operands
+// (host work, done once per run by callers that launch the same plan many
+// times), then the launch itself.
+struct TcMaps {
+  CUtensorMap x, f;
+  int64_t g2;
+};
+int mttkrp_tc_encode(const TcPlan& p, const __nv_bfloat16* Xbf, __nv_bfloat16* const* fbt,
+                     int fplanes, TcMaps* maps);
+int mttkrp_tc_launch_maps(const TcPlan& p, const TcMaps& maps, const float* const* factors,
+                          const float* weights, float* partial, const int* skip_flag, int* err,
+                          cudaStream_t st);
 
 // out = sum over splits of partial (I_out x R, f32).
 int tc_launch_sum_partials(const TcPlan& p, const float* partial, float* out, cudaStream_t st);

@@ -166,6 +166,306 @@ __global__ void k_clip_min(T* __restrict__ x, int64_t n, T lo) {
     if (x[e] < lo) x[e] = lo;
 }
 
+// Kronecker product of n_mats matrices, left to right (the first matrix
+// varies slowest), each entry the product of one entry of every matrix taken
+// in that order (tensorly/tenalg/core_tenalg/_kronecker.py).
+struct KronArgs {
+  const void* m[kMaxModes];
+  int64_t rows[kMaxModes], cols[kMaxModes];
+  int n;
+};
+template <typename T>
+__global__ void k_kronecker(KronArgs a, int64_t out_rows, int64_t out_cols, T* __restrict__ out) {
+  const int64_t total = out_rows * out_cols;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t i = e / out_cols, j = e - (e / out_cols) * out_cols;
+    int64_t ri[kMaxModes], ci[kMaxModes];
+    for (int k = a.n - 1; k >= 0; --k) {
+      ri[k] = i % a.rows[k];
+      i /= a.rows[k];
+      ci[k] = j % a.cols[k];
+      j /= a.cols[k];
+    }
+    T v = static_cast<const T*>(a.m[0])[ri[0] * a.cols[0] + ci[0]];
+    for (int k = 1; k < a.n; ++k) v = v * static_cast<const T*>(a.m[k])[ri[k] * a.cols[k] + ci[k]];
+    out[e] = v;
+  }
+}
+
+// tucker_normalize (tensorly/tucker_tensor.py:78-102): every factor column
+// scaled to unit norm, the core multiplied along each mode by the column
+// norms of that mode, in mode order; a zero column is left as it is.
+struct TnArgs {
+  void* f[kMaxModes];
+  int64_t rows[kMaxModes], ranks[kMaxModes];
+  int64_t foff[kMaxModes + 1];   // cumulative factor entries
+  int64_t soff[kMaxModes + 1];   // cumulative columns (offsets into the scales)
+  void* core;
+  int64_t core_n;
+  int n;
+};
+template <typename T>
+__global__ void k_tn_colnorms(TnArgs a, double* __restrict__ scales) {
+  const int64_t col = blockIdx.x;
+  int m = 0;
+  while (col >= a.soff[m + 1]) ++m;
+  const int64_t c = col - a.soff[m], R = a.ranks[m];
+  const T* f = static_cast<const T*>(a.f[m]);
+  double acc = 0.0;
+  for (int64_t r = threadIdx.x; r < a.rows[m]; r += blockDim.x) {
+    const double v = (double)f[r * R + c];
+    acc += v * v;
+  }
+  __shared__ double red[32];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    acc = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (threadIdx.x == 0) scales[col] = (double)(T)sqrt(acc);
+  }
+}
+template <typename T>
+__global__ void k_tn_apply(TnArgs a, const double* __restrict__ scales) {
+  const int64_t nf = a.foff[a.n], total = nf + a.core_n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    if (e < nf) {
+      int m = 0;
+      while (e >= a.foff[m + 1]) ++m;
+      const int64_t k = e - a.foff[m];
+      const T s = (T)scales[a.soff[m] + k % a.ranks[m]];
+      T* f = static_cast<T*>(a.f[m]);
+      f[k] = f[k] / (s == T(0) ? T(1) : s);
+    } else {
+      int64_t k = e - nf, rem = k;
+      int64_t idx[kMaxModes];
+      for (int m = a.n - 1; m >= 0; --m) {
+        idx[m] = rem % a.ranks[m];
+        rem /= a.ranks[m];
+      }
+      T* g = static_cast<T*>(a.core);
+      T v = g[k];
+      for (int m = 0; m < a.n; ++m) v = v * (T)scales[a.soff[m] + idx[m]];
+      g[k] = v;
+    }
+  }
+}
+
+// Active-set NNLS of tensorly/solvers/nnls.py:275-406 (Bro and De Jong's
+// variant of Lawson-Hanson) for one system of n <= kAsMax unknowns, one CTA:
+// x minimises ||Utm - UtU x|| with x >= 0, starting from x.  The passive-set
+// systems are solved by LU with partial pivoting (the reference's
+// np.linalg.solve); a zero pivot is the reference's singular-matrix
+// exception: on the first solve of an iteration it restarts from zero as the
+// reference's except branch does, elsewhere it ends the call with
+// TLGB_ESINGULAR in *status (the reference raises there).
+constexpr int kAsMax = 128;
+
+template <typename T>
+__device__ bool as_solve(const T* __restrict__ UtU, const T* __restrict__ Utm, int n,
+                         const int* passive, T* A, T* b, int* idx, int* s_m, int* s_sing,
+                         int* s_piv, T* support) {
+  if (threadIdx.x == 0) {
+    int m = 0;
+    for (int i = 0; i < n; ++i)
+      if (passive[i]) idx[m++] = i;
+    *s_m = m;
+    *s_sing = 0;
+  }
+  __syncthreads();
+  const int m = *s_m;
+  for (int e = threadIdx.x; e < m * m; e += blockDim.x)
+    A[e] = UtU[(int64_t)idx[e / m] * n + idx[e % m]];
+  for (int e = threadIdx.x; e < m; e += blockDim.x) b[e] = Utm[idx[e]];
+  __syncthreads();
+  for (int k = 0; k < m; ++k) {
+    if (threadIdx.x == 0) {   // partial pivoting (first largest magnitude), row swap
+      int p = k;
+      T best = fabs(A[k * m + k]);
+      for (int i = k + 1; i < m; ++i)
+        if (fabs(A[i * m + k]) > best) { best = fabs(A[i * m + k]); p = i; }
+      if (best == T(0)) *s_sing = 1;
+      *s_piv = p;
+    }
+    __syncthreads();
+    if (*s_sing) break;   // uniform: read after the barrier
+    const int p = *s_piv;
+    if (p != k) {
+      for (int j = threadIdx.x; j < m; j += blockDim.x) {
+        const T t = A[k * m + j];
+        A[k * m + j] = A[p * m + j];
+        A[p * m + j] = t;
+      }
+      if (threadIdx.x == 0) { const T t = b[k]; b[k] = b[p]; b[p] = t; }
+    }
+    __syncthreads();
+    const T inv = T(1) / A[k * m + k];
+    for (int i = k + 1 + threadIdx.x; i < m; i += blockDim.x) A[i * m + k] *= inv;
+    __syncthreads();
+    const int w = m - k - 1;
+    for (int e = threadIdx.x; e < w * w; e += blockDim.x) {
+      const int i = k + 1 + e / w, j = k + 1 + e % w;
+      A[i * m + j] -= A[i * m + k] * A[k * m + j];
+    }
+    __syncthreads();
+  }
+  if (*s_sing) return false;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < m; ++i) {            // forward, unit lower
+      T v = b[i];
+      for (int j = 0; j < i; ++j) v -= A[i * m + j] * b[j];
+      b[i] = v;
+    }
+    for (int i = m - 1; i >= 0; --i) {       // back, upper
+      T v = b[i];
+      for (int j = i + 1; j < m; ++j) v -= A[i * m + j] * b[j];
+      b[i] = v / A[i * m + i];
+    }
+    for (int i = 0; i < n; ++i) support[i] = T(0);
+    for (int j = 0; j < m; ++j) support[idx[j]] = b[j];
+  }
+  __syncthreads();
+  return true;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_active_set_nnls(const T* __restrict__ UtU, const T* __restrict__ Utm, T* __restrict__ xg,
+                  int n, int n_iter_max, double tol, int* status) {
+  extern __shared__ __align__(16) unsigned char as_smem[];
+  T* A = reinterpret_cast<T*>(as_smem);   // n x n
+  T* b = A + n * n;
+  T* x = b + n;
+  T* grad = x + n;
+  T* support = grad + n;
+  int* passive = reinterpret_cast<int*>(support + n);
+  int* idx = passive + n;
+  __shared__ int s_m, s_sing, s_piv, s_flag, s_fail;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = xg[i];
+  if (threadIdx.x == 0) s_fail = 0;
+  __syncthreads();
+  auto gradient = [&]() {   // grad = Utm - UtU x
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      T v = T(0);
+      for (int j = 0; j < n; ++j) v += UtU[(int64_t)i * n + j] * x[j];
+      grad[i] = Utm[i] - v;
+    }
+    __syncthreads();
+  };
+  auto argmax_grad = [&]() {   // first index of the largest gradient entry
+    int best = 0;
+    for (int i = 1; i < n; ++i)
+      if (grad[i] > grad[best]) best = i;
+    return best;
+  };
+  gradient();
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < n; ++i) { passive[i] = x[i] > T(0); support[i] = T(0); }
+  }
+  __syncthreads();
+  for (int it = 0; it < n_iter_max; ++it) {
+    if (threadIdx.x == 0) {
+      bool all0 = true;
+      for (int i = 0; i < n; ++i) all0 = all0 && (x[i] == T(0));
+      if (it > 0 || all0) passive[argmax_grad()] = 1;
+    }
+    __syncthreads();
+    if (!as_solve(UtU, Utm, n, passive, A, b, idx, &s_m, &s_sing, &s_piv, support)) {
+      // the reference's except branch: restart from zero with one passive index
+      if (threadIdx.x == 0) {
+        for (int i = 0; i < n; ++i) { x[i] = T(0); support[i] = T(0); passive[i] = 0; }
+        passive[argmax_grad()] = 1;
+      }
+      __syncthreads();
+      if (!as_solve(UtU, Utm, n, passive, A, b, idx, &s_m, &s_sing, &s_piv, support)) {
+        if (threadIdx.x == 0) s_fail = 1;
+        __syncthreads();
+        break;
+      }
+    }
+    // step back along the segment to x while a passive entry is not positive
+    if (threadIdx.x == 0) {
+      bool any = false, nonpos = false;
+      T mn = T(0);
+      for (int i = 0; i < n; ++i)
+        if (passive[i]) {
+          mn = any ? (support[i] < mn ? support[i] : mn) : support[i];
+          any = true;
+        }
+      nonpos = any && mn <= T(0);
+      if (!any) s_fail = 2;                  // the reference's min of an empty selection
+      s_flag = nonpos ? 1 : 0;
+    }
+    __syncthreads();
+    if (s_fail) break;
+    if (s_flag) {
+      for (int rep = 0; rep < n; ++rep) {
+        if (threadIdx.x == 0) {
+          T alpha = T(0);
+          bool first = true;
+          for (int i = 0; i < n; ++i)
+            if (passive[i] && support[i] <= T(0)) {
+              const T r = x[i] / (x[i] - support[i]);
+              if (first || r < alpha) alpha = r;
+              first = false;
+            }
+          for (int i = 0; i < n; ++i) {
+            x[i] = x[i] + alpha * (support[i] - x[i]);
+            passive[i] = x[i] > T(0);
+          }
+        }
+        __syncthreads();
+        if (!as_solve(UtU, Utm, n, passive, A, b, idx, &s_m, &s_sing, &s_piv, support)) {
+          if (threadIdx.x == 0) s_fail = 1;
+          __syncthreads();
+          break;
+        }
+        if (threadIdx.x == 0) {
+          bool any = false;
+          T mn = T(0);
+          for (int i = 0; i < n; ++i)
+            if (passive[i]) {
+              mn = any ? (support[i] < mn ? support[i] : mn) : support[i];
+              any = true;
+            }
+          s_flag = (!any || mn > T(0)) ? 1 : 0;
+        }
+        __syncthreads();
+        if (s_flag) break;
+      }
+      if (s_fail) break;
+    }
+    // x = clip(support, 0, max(support)); the gradient; the stop test
+    if (threadIdx.x == 0) {
+      T mx = support[0];
+      for (int i = 1; i < n; ++i) mx = support[i] > mx ? support[i] : mx;
+      for (int i = 0; i < n; ++i) {   // min(max(v, 0), mx), the order of np.clip
+        const T v = support[i] < T(0) ? T(0) : support[i];
+        x[i] = v > mx ? mx : v;
+      }
+    }
+    __syncthreads();
+    gradient();
+    if (threadIdx.x == 0) {   // the active set is the complement of the passive set,
+      bool any_active = false;  // which the clip above does not recompute
+      T gmax = T(0);
+      for (int i = 0; i < n; ++i)
+        if (!passive[i]) {
+          gmax = any_active ? (grad[i] > gmax ? grad[i] : gmax) : grad[i];
+          any_active = true;
+        }
+      s_flag = (!any_active || (double)gmax <= tol) ? 1 : 0;
+    }
+    __syncthreads();
+    if (s_flag) break;
+  }
+  for (int i = threadIdx.x; i < n; i += blockDim.x) xg[i] = x[i];
+  if (threadIdx.x == 0 && status) *status = s_fail ? TLGB_ESINGULAR : TLGB_OK;
+}
+
 __global__ void k_dot_final(const double* part, int nb, double* out) {
   if (threadIdx.x == 0) {
     double t = 0.0;
@@ -623,6 +923,120 @@ extern "C" int tlgb_clip_min(int dtype, void* x, int64_t n, double lo, void* str
     k_clip_min<double><<<nb, 256, 0, st>>>(static_cast<double*>(x), n, lo);
   else
     k_clip_min<float><<<nb, 256, 0, st>>>(static_cast<float*>(x), n, (float)lo);
+  TLGB_LAUNCH_CHECK();
+  return TLGB_OK;
+}
+
+extern "C" int tlgb_kronecker(int dtype, int n_mats, const void* const* mats, const int64_t* rows,
+                              const int64_t* cols, void* out, void* stream) {
+  clear_error();
+  TLGB_CHECK_ARG(dtype == TLGB_F32 || dtype == TLGB_F64, "kronecker: dtype must be f32 or f64");
+  TLGB_CHECK_ARG(n_mats >= 1 && n_mats <= kMaxModes && mats && rows && cols && out,
+                 "kronecker: bad argument");
+  KronArgs a{};
+  a.n = n_mats;
+  int64_t R = 1, C = 1;
+  for (int k = 0; k < n_mats; ++k) {
+    TLGB_CHECK_ARG(mats[k] && rows[k] >= 1 && cols[k] >= 1, "kronecker: bad matrix");
+    a.m[k] = mats[k];
+    a.rows[k] = rows[k];
+    a.cols[k] = cols[k];
+    R *= rows[k];
+    C *= cols[k];
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const unsigned nb = (unsigned)std::min<int64_t>(ceil_div(R * C, (int64_t)256), 152 * 8);
+  if (dtype == TLGB_F64)
+    k_kronecker<double><<<nb, 256, 0, st>>>(a, R, C, static_cast<double*>(out));
+  else
+    k_kronecker<float><<<nb, 256, 0, st>>>(a, R, C, static_cast<float*>(out));
+  TLGB_LAUNCH_CHECK();
+  return TLGB_OK;
+}
+
+extern "C" int tlgb_active_set_nnls(int dtype, const void* UtU, const void* Utm, void* x,
+                                    int64_t n, int n_iter_max, double tol, int* status,
+                                    void* stream) {
+  clear_error();
+  TLGB_CHECK_ARG(dtype == TLGB_F32 || dtype == TLGB_F64, "active_set_nnls: f32 or f64");
+  TLGB_CHECK_ARG(UtU && Utm && x && status && n >= 1 && n_iter_max >= 0,
+                 "active_set_nnls: bad argument");
+  if (n > kAsMax)
+    return set_error(TLGB_EUNSUPPORTED, "active_set_nnls: more than 128 unknowns");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const size_t esz = dtype == TLGB_F64 ? 8 : 4;
+  const size_t smem = esz * ((size_t)n * n + 4 * n) + 2 * sizeof(int) * n;
+  static std::atomic<bool> attr[64];   // per-device set-up flags, read and set by any host thread
+  const int dev = current_device();
+  if (dev >= 0 && dev < 64 && !attr[dev]) {
+    TLGB_CUDA_TRY(cudaFuncSetAttribute(k_active_set_nnls<double>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024));
+    TLGB_CUDA_TRY(cudaFuncSetAttribute(k_active_set_nnls<float>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024));
+    attr[dev] = true;
+  }
+  if (dtype == TLGB_F64)
+    k_active_set_nnls<double><<<1, 256, smem, st>>>(static_cast<const double*>(UtU),
+                                                    static_cast<const double*>(Utm),
+                                                    static_cast<double*>(x), (int)n, n_iter_max,
+                                                    tol, status);
+  else
+    k_active_set_nnls<float><<<1, 256, smem, st>>>(static_cast<const float*>(UtU),
+                                                   static_cast<const float*>(Utm),
+                                                   static_cast<float*>(x), (int)n, n_iter_max, tol,
+                                                   status);
+  TLGB_LAUNCH_CHECK();
+  return TLGB_OK;
+}
+
+extern "C" int tlgb_tucker_normalize_workspace_size(int ndim, const int64_t* ranks, size_t* bytes) {
+  clear_error();
+  TLGB_CHECK_ARG(ndim >= 1 && ndim <= kMaxModes && ranks && bytes,
+                 "tucker_normalize: bad argument");
+  int64_t cols = 0;
+  for (int k = 0; k < ndim; ++k) {
+    TLGB_CHECK_ARG(ranks[k] >= 1, "tucker_normalize: ranks must be >= 1");
+    cols += ranks[k];
+  }
+  *bytes = sizeof(double) * (size_t)cols;
+  return TLGB_OK;
+}
+
+extern "C" int tlgb_tucker_normalize(int dtype, int ndim, const int64_t* rows, const int64_t* ranks,
+                                     void* const* factors, void* core, void* workspace,
+                                     size_t workspace_bytes, void* stream) {
+  clear_error();
+  TLGB_CHECK_ARG(dtype == TLGB_F32 || dtype == TLGB_F64, "tucker_normalize: f32 or f64");
+  TLGB_CHECK_ARG(ndim >= 1 && ndim <= kMaxModes && rows && ranks && factors && core,
+                 "tucker_normalize: bad argument");
+  TnArgs a{};
+  a.n = ndim;
+  a.core = core;
+  a.core_n = 1;
+  for (int k = 0; k < ndim; ++k) {
+    TLGB_CHECK_ARG(factors[k] && rows[k] >= 1 && ranks[k] >= 1, "tucker_normalize: bad factor");
+    a.f[k] = factors[k];
+    a.rows[k] = rows[k];
+    a.ranks[k] = ranks[k];
+    a.foff[k + 1] = a.foff[k] + rows[k] * ranks[k];
+    a.soff[k + 1] = a.soff[k] + ranks[k];
+    a.core_n *= ranks[k];
+  }
+  if (!workspace || workspace_bytes < sizeof(double) * (size_t)a.soff[ndim])
+    return set_error(TLGB_EWORKSPACE, "tucker_normalize: workspace too small");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  double* scales = static_cast<double*>(workspace);
+  const unsigned nb =
+      (unsigned)std::min<int64_t>(ceil_div(a.foff[ndim] + a.core_n, (int64_t)256), 152 * 8);
+  if (dtype == TLGB_F64) {
+    k_tn_colnorms<double><<<(unsigned)a.soff[ndim], 256, 0, st>>>(a, scales);
+    TLGB_LAUNCH_CHECK();
+    k_tn_apply<double><<<nb, 256, 0, st>>>(a, scales);
+  } else {
+    k_tn_colnorms<float><<<(unsigned)a.soff[ndim], 256, 0, st>>>(a, scales);
+    TLGB_LAUNCH_CHECK();
+    k_tn_apply<float><<<nb, 256, 0, st>>>(a, scales);
+  }
   TLGB_LAUNCH_CHECK();
   return TLGB_OK;
 }

@@ -1035,9 +1035,14 @@ class RandomizedCP:
 _CONSTRAINT_NAMES = ("non_negative", "l1_reg", "l2_reg", "l2_square_reg", "unimodality",
                      "normalize", "simplex", "normalized_sparsity", "soft_sparsity",
                      "smoothness", "monotonicity", "hard_sparsity")
-# library kinds of the whole-matrix proximal operators (TLGB_CONS_*)
+# library kinds of the proximal operators (TLGB_CONS_*): whole-matrix 1-5,
+# column-wise and rank-based 6-12
 _CONSTRAINT_KIND = {None: 0, "non_negative": 1, "l1_reg": 2, "l2_reg": 3, "l2_square_reg": 4,
-                    "normalize": 5}
+                    "normalize": 5, "unimodality": 6, "simplex": 7, "normalized_sparsity": 8,
+                    "soft_sparsity": 9, "smoothness": 10, "monotonicity": 11,
+                    "hard_sparsity": 12}
+_PARAMETRIC = ("l1_reg", "l2_reg", "l2_square_reg", "simplex", "normalized_sparsity",
+               "soft_sparsity", "smoothness", "hard_sparsity")
 
 
 def validate_constraints(non_negative=None, l1_reg=None, l2_reg=None, l2_square_reg=None,
@@ -1088,18 +1093,19 @@ def validate_constraints(non_negative=None, l1_reg=None, l2_reg=None, l2_square_
 
 def _constraint_kind(constraint, parameter):
     if constraint not in _CONSTRAINT_KIND:
-        raise NotImplementedError(f"the {constraint} proximal operator (a column-wise projection) "
-                                  "is not supported by tensorly_gb300")
-    if constraint in ("l1_reg", "l2_reg", "l2_square_reg") and parameter is None:
+        raise RuntimeError("Invalid constraint name")        # tensorly/tenalg/proximal.py:267
+    if constraint in _PARAMETRIC and parameter is None:
         raise TypeError(f"{constraint} needs a numeric parameter for every constrained mode")
-    return _CONSTRAINT_KIND[constraint], float(parameter) if constraint in (
-        "l1_reg", "l2_reg", "l2_square_reg") else 0.0
+    return _CONSTRAINT_KIND[constraint], float(parameter) if constraint in _PARAMETRIC else 0.0
 
 
 def proximal_operator(tensor, n_const=1, order=0, **constraints):
-    """The proximal operator of mode ``order``'s constraint applied to a whole
-    matrix (tensorly/tenalg/proximal.py:148-267) by ``tlgb_proximal``:
-    non_negative, l1_reg, l2_reg, l2_square_reg and normalize."""
+    """The proximal operator of mode ``order``'s constraint
+    (tensorly/tenalg/proximal.py:148-267) by ``tlgb_proximal_matrix``: the
+    whole-matrix operators entry by entry, the column-wise ones (unimodality,
+    simplex, soft_sparsity, smoothness, monotonicity) per column of a matrix
+    (a vector is one column), the rank-based ones (hard_sparsity,
+    normalized_sparsity) over all entries."""
     x, pl = to_device(tensor)
     if n_const is None:
         return pl.back(x)
@@ -1108,11 +1114,21 @@ def proximal_operator(tensor, n_const=1, order=0, **constraints):
         return pl.back(x)
     kind, param = _constraint_kind(constraint, parameter)
     x = x.contiguous()
+    if constraint in ("unimodality", "monotonicity") and x.ndim > 2:
+        raise ValueError(f"{constraint.capitalize()} prox doesn't support an input which has "
+                         "more than 2 dimensions.")
+    rows = int(x.shape[0]) if x.ndim >= 1 else 1
+    cols = x.numel() // max(rows, 1) if x.ndim >= 2 else 1
+    if constraint in ("hard_sparsity", "normalized_sparsity") or kind <= 5:
+        rows, cols = x.numel(), 1                     # the entries in any layout
     out = torch.empty_like(x)
     lib = _lib.lib()
-    ws = workspace(lib.tlgb_proximal_workspace_bytes(), x.device)
-    _lib.check(lib.tlgb_proximal(dtype_code(x), x.data_ptr(), x.numel(), kind, param,
-                                 out.data_ptr(), ptr(ws), ws.numel(), stream_of(x)))
+    nbytes = ctypes.c_size_t(0)
+    _lib.check(lib.tlgb_proximal_matrix_workspace_size(dtype_code(x), rows, cols, kind,
+                                                       ctypes.byref(nbytes)))
+    ws = workspace(max(nbytes.value, 256), x.device)
+    _lib.check(lib.tlgb_proximal_matrix(dtype_code(x), x.data_ptr(), rows, cols, kind, param,
+                                        out.data_ptr(), ptr(ws), ws.numel(), stream_of(x)))
     return pl.back(out)
 
 
@@ -1161,10 +1177,10 @@ def constrained_parafac(tensor, rank, n_iter_max=100, n_iter_max_inner=10, init=
     mode the factorisation of (Hadamard of Grams) + rho I, the MTTKRP, and
     ADMM iterations (solve, proximal operator, dual update, stop test) with no
     host round trip; one synchronisation per outer iteration for the error
-    and the stop tests.  The proximal operators that act on the whole factor
-    matrix are supported (non_negative, l1_reg, l2_reg, l2_square_reg,
-    normalize); the column-wise ones (unimodality, simplex, the sparsity
-    projections, smoothness, monotonicity) raise NotImplementedError."""
+    and the stop tests.  Every proximal operator of the reference is
+    supported: entry-wise (non_negative, l1_reg, l2_reg, l2_square_reg,
+    normalize), per column (unimodality, simplex, soft_sparsity, smoothness,
+    monotonicity) and rank-based (hard_sparsity, normalized_sparsity)."""
     cons = dict(non_negative=non_negative, l1_reg=l1_reg, l2_reg=l2_reg,
                 l2_square_reg=l2_square_reg, unimodality=unimodality, normalize=normalize,
                 simplex=simplex, normalized_sparsity=normalized_sparsity,
@@ -1316,13 +1332,11 @@ def non_negative_tucker(tensor, rank, n_iter_max=10, init="svd", tol=10e-5, rand
     X_(n) B = [X x_{k!=n} U_k^T]_(n) G_(n)^T and B^T B = [G x_{k!=n} U_k^T U_k]_(n)
     G_(n)^T, so nothing of the size of the tensor is formed besides the chain.
     The error ||X - [[G; U]]|| comes from ||X||^2 - 2 <X x_k U_k^T, G> + <G,
-    G x_k U_k^T U_k>.  ``normalize_factors`` is not supported."""
+    G x_k U_k^T U_k>.  normalize_factors applies ``tucker_normalize`` after
+    every iteration that does not stop, as the reference does."""
     from .base import unfold
-    from .cp_tensor import validate_tucker_rank
+    from .cp_tensor import tucker_normalize, validate_tucker_rank
     from .tenalg import multi_mode_dot
-    if normalize_factors:
-        raise NotImplementedError("non_negative_tucker with normalize_factors=True is not "
-                                  "supported by tensorly_gb300")
     x, placement = to_device(tensor)
     x = x.contiguous()
     n_modes = x.ndim
@@ -1358,6 +1372,8 @@ def non_negative_tucker(tensor, rank, n_iter_max=10, init="svd", tol=10e-5, rand
             if verbose:
                 print(f"converged in {iteration} iterations.")
             break
+        if normalize_factors:
+            core, factors = tucker_normalize((core, factors))
     out = TuckerTensor((placement.back(core), [placement.back(f) for f in factors]))
     if return_errors:
         return out, rec_errors
@@ -1404,6 +1420,79 @@ def _hals_nnls_t(mtu, utu, vt, n_iter_max, tol, sparsity):
                                   stream_of(vt)))
 
 
+def active_set_nnls(Utm, UtU, x=None, n_iter_max=100, tol=10e-8):
+    """Active-set non-negative least squares (tensorly/solvers/nnls.py:279-426,
+    Bro and De Jong), same signature and return (the solution vector), by
+    ``tlgb_active_set_nnls`` (one CTA, up to 128 unknowns).  Where the
+    reference's np.linalg.solve would raise on an exactly singular passive
+    system, SingularMatrixError is raised."""
+    utu, pl = to_device(UtU)
+    utu = utu.contiguous()
+    n = int(utu.shape[1])
+    utm = like(Utm, utu).reshape(-1).contiguous()
+    xv = (torch.zeros(n, dtype=utu.dtype, device=utu.device) if x is None
+          else like(x, utu).reshape(-1).clone())
+    _active_set_t(utm, utu, xv, int(n_iter_max), float(tol))
+    return pl.back(xv)
+
+
+def _active_set_t(utm, utu, xv, n_iter_max, tol):
+    n = int(xv.numel())
+    status = torch.zeros(1, dtype=torch.int32, device=xv.device)
+    _lib.check(_lib.lib().tlgb_active_set_nnls(dtype_code(xv), ptr(utu), ptr(utm), ptr(xv), n,
+                                               n_iter_max, tol, ptr(status), stream_of(xv)))
+    rc = int(status.item())
+    if rc != _lib.TLGB_OK:
+        raise _lib.SingularMatrixError(rc, "active_set_nnls: singular passive-set system")
+
+
+def _tucker_fixed_modes_error(shape, rank, fixed, init="svd"):
+    """The ValueError the reference's non_negative_tucker_hals raises with
+    fixed modes, or None where this walk does not find it.  Its
+    initialize_tucker then gives the j-th free mode the rank rank[j] and keeps
+    only the free modes' factors, while the first mode loop indexes that list
+    by mode number; the first misaligned mode_dot of that loop raises
+    (tensorly/decomposition/_tucker.py:591-630, _tucker.py:22-110).  Only the
+    shapes are walked, nothing is computed."""
+    n = len(shape)
+    modes = [m for m in range(n) if m not in fixed]
+    if init == "svd":
+        core = list(shape)
+        for j, m in enumerate(modes):
+            core[m] = rank[j]
+    elif init == "random":
+        core = [rank[j] for j in range(len(modes))]
+    else:
+        return None
+    mode = modes[0]
+
+    def misaligned(dims, mat, i):
+        return ValueError(f"shapes {tuple(dims)} and {mat} not aligned in mode-{i} "
+                          f"multiplication: {dims[i]} (mode {i}) != {mat[1]} (dim 1 of matrix)")
+
+    # multi_mode_dot(core, grams, skip=mode): list entry i, the Gram of the
+    # factor of free mode modes[i] (rank[i] x rank[i]), acts on core mode i
+    for i in range(len(modes)):
+        if i == mode:
+            continue
+        if i >= len(core):
+            return None
+        if core[i] != rank[i]:
+            return misaligned(core, (rank[i], rank[i]), i)
+    if mode >= len(core):
+        return None
+    # multi_mode_dot(tensor, factors, skip=mode, transpose=True): entry i is
+    # the transposed factor of free mode modes[i], rank[i] x shape[modes[i]]
+    dims = list(shape)
+    for i in range(len(modes)):
+        if i == mode:
+            continue
+        if dims[i] != shape[modes[i]]:
+            return misaligned(dims, (rank[i], shape[modes[i]]), i)
+        dims[i] = rank[i]
+    return None
+
+
 def _largest_eig(a):
     """Largest eigenvalue of a symmetric matrix (the first singular value of a
     Gram, tl.truncated_svd(MtM)[1][0]) by the library's eigensolver."""
@@ -1431,18 +1520,21 @@ def non_negative_tucker_hals(tensor, rank, n_iter_max=100, init="svd", svd="trun
     UtU = [G x_{k!=n} U_k^T U_k]_(n) G_(n)^T and MtU = [X x_{k!=n} U_k^T]_(n) G_(n)^T
     (``tlgb_hals_nnls``); the core update is the reference's FISTA with the
     step prod_k 1 / lambda_max(U_k^T U_k) (``tlgb_fista_tucker_core``, the
-    eigenvalues from the library's eigensolver).  The error comes from the
-    norm expansion.  'active_set', fixed modes and normalize_factors are not
-    supported."""
+    eigenvalues from the library's eigensolver).  With algorithm='active_set'
+    the core is the reference's active_set_nnls on the Kronecker product of
+    the factor Grams and vec(X x_k U_k^T) (``tlgb_kronecker``,
+    ``tlgb_active_set_nnls``; up to 128 core entries).  normalize_factors
+    applies ``tucker_normalize`` after every iteration that does not stop, as
+    the reference does.  The error comes from the norm expansion.  With fixed
+    modes the reference's own loop fails on its first mode_dot; the same
+    ValueError is raised here before any work."""
     from collections.abc import Iterable
     from .base import unfold
-    from .cp_tensor import validate_tucker_rank
-    from .tenalg import multi_mode_dot
-    if algorithm != "fista":
-        raise NotImplementedError("non_negative_tucker_hals supports algorithm='fista' only")
-    if normalize_factors:
-        raise NotImplementedError("non_negative_tucker_hals with normalize_factors=True is not "
-                                  "supported by tensorly_gb300")
+    from .cp_tensor import tucker_normalize, validate_tucker_rank
+    from .tenalg import kronecker, multi_mode_dot
+    if algorithm not in ("fista", "active_set"):
+        raise NotImplementedError("non_negative_tucker_hals supports algorithm='fista' or "
+                                  "'active_set'")
     x, placement = to_device(tensor)
     x = x.contiguous()
     n_modes = x.ndim
@@ -1456,8 +1548,12 @@ def non_negative_tucker_hals(tensor, rank, n_iter_max=100, init="svd", svd="trun
                       "position and keep it fixed there.")
         fixed.remove(n_modes - 1)
     if fixed:
-        raise NotImplementedError("non_negative_tucker_hals with fixed modes is not supported by "
-                                  "tensorly_gb300")
+        err = (_tucker_fixed_modes_error(tuple(x.shape), rank, fixed, init)
+               if n_iter_max > 0 and isinstance(init, str) else None)
+        if err is not None:
+            raise err
+        raise NotImplementedError("non_negative_tucker_hals with these fixed modes is not "
+                                  "supported by tensorly_gb300")
     n_inner, tol_inner = (50000, 1e-16) if exact else (100, 1e-8)
     core, factors = initialize_tucker(x, rank, range(n_modes), init=init, svd=svd,
                                       random_state=random_state, non_negative=True)
@@ -1471,6 +1567,9 @@ def non_negative_tucker_hals(tensor, rank, n_iter_max=100, init="svd", svd="trun
                                                          ctypes.byref(nbytes)))
     fws = workspace(nbytes.value, x.device)
     csp = 0.0 if core_sparsity_coefficient is None else float(core_sparsity_coefficient)
+    if algorithm == "active_set" and core.numel() > 128:
+        raise NotImplementedError("non_negative_tucker_hals(algorithm='active_set') supports "
+                                  "cores of up to 128 entries")
     rec_errors = []
     for iteration in range(n_iter_max):
         for mode in range(n_modes):
@@ -1483,13 +1582,18 @@ def non_negative_tucker_hals(tensor, rank, n_iter_max=100, init="svd", svd="trun
                          sparsity_coefficients[mode])
         grams = [_mat_tn(f, f).contiguous() for f in factors]
         core_est = multi_mode_dot(x, factors, transpose=True).contiguous()
-        lr = 1.0
-        for g in grams:
-            lr *= 1.0 / _largest_eig(g)
-        _lib.check(lib.tlgb_fista_tucker_core(
-            dtype_code(x), core_est.data_ptr(), n_modes, cshape,
-            _lib.ptr_array([g.data_ptr() for g in grams]), core.data_ptr(), int(n_iter_max), csp,
-            lr, 1e-8, 1e-8, ptr(fws), fws.numel(), stream_of(x)))
+        if algorithm == "fista":
+            lr = 1.0
+            for g in grams:
+                lr *= 1.0 / _largest_eig(g)
+            _lib.check(lib.tlgb_fista_tucker_core(
+                dtype_code(x), core_est.data_ptr(), n_modes, cshape,
+                _lib.ptr_array([g.data_ptr() for g in grams]), core.data_ptr(), int(n_iter_max),
+                csp, lr, 1e-8, 1e-8, ptr(fws), fws.numel(), stream_of(x)))
+        else:
+            cvec = core.reshape(-1)
+            _active_set_t(core_est.reshape(-1), kronecker(grams).contiguous(), cvec,
+                          int(n_iter_max), 10e-8)
         t2 = float(_dot(core, multi_mode_dot(core, grams)).item())
         xt = float(_dot(core_est, core).item())
         rec_error = math.sqrt(max(norm_x2 - 2.0 * xt + t2, 0.0) / norm_x2)
@@ -1502,6 +1606,8 @@ def non_negative_tucker_hals(tensor, rank, n_iter_max=100, init="svd", svd="trun
                 if verbose:
                     print(f"converged in {iteration} iterations.")
                 break
+        if normalize_factors:
+            core, factors = tucker_normalize((core, factors))
     out = TuckerTensor((placement.back(core), [placement.back(f) for f in factors]))
     if return_errors:
         return out, rec_errors

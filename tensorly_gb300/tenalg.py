@@ -167,9 +167,41 @@ def multi_mode_dot(tensor, matrix_or_vec_list, modes=None, skip=None, transpose=
             continue
         m = like(m, x)
         if transpose and m.ndim == 2:
-            res = mode_dot(res, m, mode - decrement, transpose=True)
+            md = mode - decrement
+            if m.shape[0] != res.shape[md]:   # the reference reports the transposed matrix
+                raise ValueError(
+                    f"shapes {tuple(res.shape)} and {(int(m.shape[1]), int(m.shape[0]))} not "
+                    f"aligned in mode-{md} multiplication: {res.shape[md]} (mode {md}) != "
+                    f"{m.shape[0]} (dim 1 of matrix)")
+            res = mode_dot(res, m, md, transpose=True)
         else:
             res = mode_dot(res, m, mode - decrement)
         if m.ndim == 1:
             decrement += 1
     return pl.back(res)
+
+
+def kronecker(matrices, skip_matrix=None, reverse=False):
+    """Kronecker product of a list of matrices, the first varying slowest
+    (tensorly/tenalg/core_tenalg/_kronecker.py:8-57), by ``tlgb_kronecker``."""
+    if skip_matrix is not None:
+        matrices = [matrices[i] for i in range(len(matrices)) if i != skip_matrix]
+    if reverse:
+        matrices = matrices[::-1]
+    x, pl = to_device(matrices[0])
+    ms = [like(m, x).contiguous() for m in matrices]
+    if len(ms) > MAX_MODES:
+        raise NotImplementedError(f"kronecker of more than {MAX_MODES} matrices is not supported")
+    for m in ms:
+        if m.ndim != 2:
+            raise ValueError("kronecker takes matrices")
+    rows = [int(m.shape[0]) for m in ms]
+    cols = [int(m.shape[1]) for m in ms]
+    out = torch.empty((int(np.prod(rows)), int(np.prod(cols))), dtype=x.dtype, device=x.device)
+    if out.numel() == 0:
+        return pl.back(out)
+    _lib.check(_lib.lib().tlgb_kronecker(dtype_code(x), len(ms),
+                                         _lib.ptr_array([ptr(m) for m in ms]),
+                                         _lib.i64_array(rows), _lib.i64_array(cols), ptr(out),
+                                         stream_of(x)))
+    return pl.back(out)

@@ -32,5 +32,13 @@ def golden():
         runs = pickle.load(f)
     with open(os.path.join(here, "reconstruction_kats.pkl"), "rb") as f:
         recon = pickle.load(f)
-    return {"kats": kats["records"], "runs": {r["case"]: r for r in runs["runs"]},
-            "recon": recon["records"], "versions": runs["versions"]}
+    with open(os.path.join(here, "cons_column_runs.pkl"), "rb") as f:
+        cons_cols = pickle.load(f)
+    with open(os.path.join(here, "tucker_extra_runs.pkl"), "rb") as f:
+        tucker_extra = pickle.load(f)
+    return {"kats": kats["records"],
+            "runs": {r["case"]: r for r in runs["runs"] + cons_cols["runs"]
+                     + tucker_extra["runs"]},
+            "recon": recon["records"], "versions": runs["versions"],
+            "tucker_kats": tucker_extra["kats"],
+            "fixed_mode_errors": tucker_extra["fixed_mode_errors"]}

@@ -660,6 +660,120 @@ def record_container_validation():
     return records
 
 
+def record_cons_columns():
+    """constrained_parafac (tensorly/decomposition/_constrained_cp.py:166-435)
+    with the column-wise proximal operators and the whole-matrix sparsity
+    ones of tensorly/tenalg/proximal.py:270-628: unimodality, monotonicity,
+    simplex, soft_sparsity, normalized_sparsity, smoothness, hard_sparsity,
+    and a mix of three on different modes."""
+    import copy
+    from golden_inputs import small_cp
+    from tensorly.decomposition import constrained_parafac
+    cases = [
+        ("cons_unimodality", dict(unimodality=True)),
+        ("cons_monotonicity", dict(monotonicity=True)),
+        ("cons_simplex", dict(simplex=3.0)),
+        ("cons_soft_sparsity", dict(soft_sparsity=3.0)),
+        ("cons_normalized_sparsity", dict(normalized_sparsity=12)),
+        ("cons_smoothness", dict(smoothness=0.1)),
+        ("cons_hard_sparsity", dict(hard_sparsity=15)),
+        ("cons_columns_mixed", dict(monotonicity={0: True}, smoothness={1: 0.2},
+                                    simplex={2: 2.0})),
+    ]
+    runs = []
+    for i, (name, cons) in enumerate(cases):
+        g = dict(shape=(10, 9, 8), rank=3, seed=101 + i)
+        x = small_cp(g["seed"], g["shape"], g["rank"])
+        kw = dict(cons, init="svd", n_iter_max=8, tol_outer=1e-10)
+        cp, errs = constrained_parafac(x, g["rank"], return_errors=True, **copy.deepcopy(kw))
+        runs.append({"case": name, "gen": {"fn": "small", **g}, "checksum":
+                     [float(np.asarray(x, np.float64).sum()), float(np.linalg.norm(x))],
+                     "kwargs": {"rank": g["rank"], **kw}, "global_seed": None,
+                     "weights": np.array(cp.weights),
+                     "factors": [np.array(f) for f in cp.factors],
+                     "errors": [float(e) for e in errs]})
+    return runs
+
+
+def record_tucker_extras():
+    """Non-negative Tucker with normalize_factors (MU and HALS, both core
+    updates), the reference's tucker_normalize, kronecker and active_set_nnls
+    on fixed inputs (tensorly/solvers/tests/test_nnls.py:45-60 is the shape of
+    the last), and the ValueError non_negative_tucker_hals raises with fixed
+    modes (tensorly/decomposition/_tucker.py:457-691)."""
+    import copy
+    from golden_inputs import small_cp as small
+    import tensorly as tl
+    from tensorly.decomposition import non_negative_tucker, non_negative_tucker_hals
+    from tensorly.solvers.nnls import active_set_nnls
+    from tensorly.tenalg import kronecker
+    from tensorly.tucker_tensor import tucker_normalize
+    runs = []
+    variants = [
+        ("nnt_normalize", non_negative_tucker, dict(shape=(10, 9, 8), rank=3, seed=131),
+         dict(rank=[3, 2, 3], n_iter_max=8, init="svd", tol=1e-12, normalize_factors=True)),
+        ("nnth_normalize", non_negative_tucker_hals, dict(shape=(9, 8, 7), rank=2, seed=132),
+         dict(rank=[2, 3, 2], n_iter_max=6, init="svd", tol=1e-12, normalize_factors=True)),
+        ("nnth_active_set_normalize", non_negative_tucker_hals,
+         dict(shape=(8, 7, 6), rank=2, seed=133),
+         dict(rank=[2, 2, 3], n_iter_max=5, init="random", random_state=11, tol=1e-12,
+              algorithm="active_set", normalize_factors=True)),
+        ("nnth_active_set_f32", non_negative_tucker_hals,
+         dict(shape=(9, 8, 7), rank=2, seed=134, dtype=np.float32),
+         dict(rank=[2, 2, 2], n_iter_max=5, init="svd", tol=1e-12, algorithm="active_set")),
+        ("nnth_active_set_stop", non_negative_tucker_hals, dict(shape=(8, 8, 8), rank=2, seed=135),
+         dict(rank=[2, 2, 2], n_iter_max=60, init="svd", tol=1e-6, algorithm="active_set")),
+    ]
+    for name, fn, g, kw in variants:
+        x = np.abs(small(g["seed"], g["shape"], g["rank"], g.get("dtype", np.float64)))
+        tt, errs = fn(x, return_errors=True, **copy.deepcopy(kw))
+        runs.append({"case": name, "fn": fn.__name__,
+                     "gen": {"fn": "small", "abs": True, **g},
+                     "checksum": [float(np.asarray(x, np.float64).sum()),
+                                  float(np.linalg.norm(np.asarray(x, np.float64)))],
+                     "kwargs": kw, "core": np.array(tt.core),
+                     "factors": [np.array(f) for f in tt.factors],
+                     "errors": [float(e) for e in errs]})
+    kats = []
+    rs = np.random.RandomState(136)
+    for shape, rank in (((3, 4, 5), (3, 2, 4)), ((6, 5, 4, 3), (2, 3, 2, 2)), ((5, 6), (4, 1))):
+        core = rs.randn(*rank)
+        factors = [rs.randn(s, r) for s, r in zip(shape, rank)]
+        factors[0][:, 0] = 0.0                      # a zero column keeps its zeros
+        c2, f2 = tucker_normalize((core.copy(), [f.copy() for f in factors]))
+        kats.append({"op": "tucker_normalize", "core": core, "factors": factors,
+                     "out_core": np.array(c2), "out_factors": [np.array(f) for f in f2]})
+    for dims in (((2, 3), (4, 2)), ((3, 3), (2, 2), (2, 4)), ((1, 5), (3, 1), (2, 2), (2, 3))):
+        ms = [rs.randn(*d) for d in dims]
+        kats.append({"op": "kronecker", "matrices": ms, "out": np.array(kronecker(ms)),
+                     "out_skip1_rev": np.array(kronecker(ms, skip_matrix=1, reverse=True))})
+    for n, m, seed in ((10, 30, 137), (24, 60, 138), (64, 128, 139)):
+        r = np.random.RandomState(seed)
+        a = r.randn(m, n)
+        xtrue = np.abs(r.randn(n)) * (r.rand(n) > 0.4)
+        b = a @ xtrue + 0.01 * r.randn(m)
+        ata, atb = a.T @ a, a.T @ b
+        x0 = None if seed != 138 else np.abs(r.randn(n))
+        out = active_set_nnls(tl.tensor(atb), tl.tensor(ata), x=x0, n_iter_max=100)
+        kats.append({"op": "active_set_nnls", "UtU": ata, "Utm": atb, "x0": x0,
+                     "out": np.array(out)})
+    errors = []
+    for shape, rank, fixed in (((6, 5, 4), [2, 2, 2], [0]), ((6, 5, 4), [2, 2, 2], [1]),
+                               ((7, 6, 5, 4), [2, 3, 2, 2], [0, 2]),
+                               ((7, 6, 5, 4), [3, 2, 4, 2], [1])):
+        for init in ("svd", "random"):
+            x = np.abs(np.random.RandomState(140).randn(*shape))
+            try:
+                non_negative_tucker_hals(x, rank, n_iter_max=2, init=init, random_state=0,
+                                         fixed_modes=list(fixed))
+                msg = None
+            except ValueError as e:
+                msg = str(e)
+            errors.append({"shape": shape, "rank": rank, "fixed": fixed, "init": init,
+                           "message": msg})
+    return {"runs": runs, "kats": kats, "fixed_mode_errors": errors}
+
+
 def main():
     if not REF or not os.path.isdir(os.path.join(REF, "tensorly")):
         sys.exit("make_golden: set TENSORLY_REFERENCE to the TensorLy source tree "
@@ -671,6 +785,20 @@ def main():
         pickle.dump({"versions": _versions(), "records": cont}, f, protocol=4)
     if "containers" in sys.argv[1:]:
         print(f"{len(cont)} container records")
+        return
+    sys.path.insert(0, os.path.dirname(HERE))    # tests/: golden_inputs
+    sys.path.insert(0, REPO)                     # the oracle golden_inputs imports
+    cols = record_cons_columns()
+    with open(os.path.join(HERE, "cons_column_runs.pkl"), "wb") as f:
+        pickle.dump({"versions": _versions(), "runs": cols}, f, protocol=4)
+    if "cons_columns" in sys.argv[1:]:
+        print(f"{len(cols)} constrained runs with column-wise operators")
+        return
+    extras = record_tucker_extras()
+    with open(os.path.join(HERE, "tucker_extra_runs.pkl"), "wb") as f:
+        pickle.dump({"versions": _versions(), **extras}, f, protocol=4)
+    if "tucker_extras" in sys.argv[1:]:
+        print(f"{len(extras['runs'])} Tucker runs, {len(extras['kats'])} records")
         return
     kats = record_kats()
     with open(os.path.join(HERE, "tenalg_kats.pkl"), "wb") as f:

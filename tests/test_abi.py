@@ -105,7 +105,7 @@ def test_new_entry_points_validate_without_gpu(library):
     assert lib.tlgb_cp_constrained_workspace_size(F64, 3, shape, 500,
                                                   ctypes.byref(nbytes)) == EINVAL
     free = (ctypes.c_int * 3)(0, 1, 2)
-    kinds = (ctypes.c_int * 3)(1, 9, 0)
+    kinds = (ctypes.c_int * 3)(1, 13, 0)   # 13: no such constraint kind
     params = (ctypes.c_double * 3)(0.0, 0.0, 0.0)
     errs = (ctypes.c_double * 4)()
     n_err = ctypes.c_int(0)

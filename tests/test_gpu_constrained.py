@@ -20,7 +20,11 @@ from golden_inputs import regenerate
 pytestmark = pytest.mark.gpu
 
 CASES = ["cons_nonneg_svd", "cons_l1_random", "cons_l2sq_list", "cons_l2_dict_fixed",
-         "cons_normalize_mixed", "cons_inner", "cons_stop", "cons_f32"]
+         "cons_normalize_mixed", "cons_inner", "cons_stop", "cons_f32",
+         # the column-wise and rank-based operators (tests/golden/cons_column_runs.pkl)
+         "cons_unimodality", "cons_monotonicity", "cons_simplex", "cons_soft_sparsity",
+         "cons_normalized_sparsity", "cons_smoothness", "cons_hard_sparsity",
+         "cons_columns_mixed"]
 
 
 def host(t):
@@ -74,11 +78,8 @@ def test_proximal_edge_cases_and_constraint_parsing(gb300):
         == ("non_negative", False)
     with pytest.raises(ValueError):
         gb300.validate_constraints(non_negative=True, l1_reg={0: 0.1}, n_const=2, order=0)
-    x = torch.rand(6, 5, 4, device="cuda", dtype=torch.float64)
-    with pytest.raises(NotImplementedError):
-        gb300.constrained_parafac(x, 2, simplex=1.0)
-    with pytest.raises(NotImplementedError):
-        gb300.constrained_parafac(x, 2, monotonicity=True)
+    with pytest.raises(ValueError):
+        gb300.proximal_operator(np.ones((2, 2, 2)), monotonicity=True)
 
 
 def test_constrained_wrapper_and_host_input(gb300, golden):
@@ -91,3 +92,75 @@ def test_constrained_wrapper_and_host_input(gb300, golden):
     assert isinstance(cp.factors[0], np.ndarray)
     np.testing.assert_allclose(est.errors_, run["errors"], rtol=1e-8)
     assert all((f >= 0).all() for f in cp.factors)
+
+
+# library kind and parameter of each recorded call of the reference's
+# tensorly/tenalg/tests/test_proximal.py (tests/golden/proximal_kats.pkl)
+_KAT_KINDS = {"unimodality_prox": (6, lambda a, kw: 0.0),
+              "simplex_prox": (7, lambda a, kw: float(a[1])),
+              "normalized_sparsity_prox": (8, lambda a, kw: float(a[1])),
+              "soft_sparsity_prox": (9, lambda a, kw: float(a[1])),
+              "smoothness_prox": (10, lambda a, kw: float(a[1])),
+              "monotonicity_prox": (11, lambda a, kw: 1.0 if kw.get("decreasing") else 0.0),
+              "hard_thresholding": (12, lambda a, kw: float(a[1]))}
+
+
+def _prox_matrix(y, kind, param, rows_cols=None):
+    import ctypes
+    from tensorly_gb300 import _lib
+    lib = _lib.lib()
+    yt = torch.as_tensor(np.ascontiguousarray(y), device="cuda")
+    rows, cols = rows_cols or (yt.shape[0], yt.numel() // yt.shape[0])
+    code = _lib.TLGB_F64 if yt.dtype == torch.float64 else _lib.TLGB_F32
+    nbytes = ctypes.c_size_t(0)
+    _lib.check(lib.tlgb_proximal_matrix_workspace_size(code, rows, cols, kind,
+                                                       ctypes.byref(nbytes)))
+    ws = torch.empty(max(256, nbytes.value), dtype=torch.uint8, device="cuda")
+    out = torch.empty_like(yt)
+    _lib.check(lib.tlgb_proximal_matrix(code, yt.data_ptr(), rows, cols, kind, param,
+                                        out.data_ptr(), ws.data_ptr(), ws.numel(),
+                                        torch.cuda.current_stream().cuda_stream))
+    return host(out)
+
+
+def test_column_operators_match_reference_test_calls(gb300):
+    """Every call the reference's own proximal tests make of the column-wise
+    and rank-based operators, with the reference's output (f64, 1e-12)."""
+    import os
+    import pickle
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    recs = pickle.load(open(os.path.join(here, "proximal_kats.pkl"), "rb"))["records"]
+    n = 0
+    for rec in recs:
+        if rec["fn"] not in _KAT_KINDS:
+            continue
+        kind, param = _KAT_KINDS[rec["fn"]]
+        y = np.asarray(rec["args"][0], dtype=np.float64)
+        rc = None
+        if kind in (8, 12):
+            rc = (y.size, 1)                  # over all entries
+        elif y.ndim == 1:
+            rc = (y.shape[0], 1)
+        got = _prox_matrix(y, kind, param(rec["args"], rec["kwargs"]), rc)
+        np.testing.assert_allclose(got, np.asarray(rec["result"]), rtol=1e-12, atol=1e-12,
+                                   err_msg=rec["fn"])
+        n += 1
+    assert n == 9
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("name", ["unimodality_prox", "monotonicity_prox", "simplex_prox",
+                                  "soft_sparsity_prox", "smoothness_prox", "hard_thresholding",
+                                  "normalized_sparsity_prox"])
+def test_column_operators_match_oracle(gb300, dtype, name):
+    from oracle import proximal_oracle as po
+    rs = np.random.RandomState(len(name))
+    y = rs.randn(300, 7).astype(dtype)
+    kind = _KAT_KINDS[name][0]
+    param = {"simplex_prox": 2.0, "soft_sparsity_prox": 1.5, "smoothness_prox": 0.3,
+             "hard_thresholding": 111, "normalized_sparsity_prox": 50}.get(name, 0.0)
+    fn = getattr(po, name)
+    ref = fn(y) if param == 0.0 else fn(y, param)
+    got = _prox_matrix(y, kind, param, (y.size, 1) if kind in (8, 12) else None)
+    tol = 1e-11 if dtype == np.float64 else 2e-5
+    np.testing.assert_allclose(got, ref, rtol=tol, atol=tol * np.abs(ref).max())

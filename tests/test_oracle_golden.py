@@ -155,7 +155,11 @@ def test_oracle_sample_khatri_rao_matches_reference(golden):
 
 
 CONS_CASES = ["cons_nonneg_svd", "cons_l1_random", "cons_l2sq_list", "cons_l2_dict_fixed",
-              "cons_normalize_mixed", "cons_inner", "cons_stop", "cons_f32"]
+              "cons_normalize_mixed", "cons_inner", "cons_stop", "cons_f32",
+              # the column-wise and sparsity operators (tests/golden/cons_column_runs.pkl)
+              "cons_unimodality", "cons_monotonicity", "cons_simplex", "cons_soft_sparsity",
+              "cons_normalized_sparsity", "cons_smoothness", "cons_hard_sparsity",
+              "cons_columns_mixed"]
 
 
 @pytest.mark.parametrize("case", CONS_CASES)
@@ -175,7 +179,8 @@ def test_oracle_constrained_parafac_matches_reference(golden, case):
         np.testing.assert_allclose(a, b, rtol=1e-9, atol=1e-9 * np.abs(b).max())
 
 
-@pytest.mark.parametrize("case", ["nnt_svd", "nnt_random", "nnt_stop", "nnt_f32"])
+@pytest.mark.parametrize("case", ["nnt_svd", "nnt_random", "nnt_stop", "nnt_f32",
+                                  "nnt_normalize"])
 def test_oracle_non_negative_tucker_matches_reference(golden, case):
     run = golden["runs"][case]
     x = regenerate(run)
@@ -191,7 +196,9 @@ def test_oracle_non_negative_tucker_matches_reference(golden, case):
 
 
 @pytest.mark.parametrize("case", ["nnth_svd", "nnth_random", "nnth_sparse", "nnth_f32",
-                                  "nnth_active_set", "nnth_active_set_4way"])
+                                  "nnth_active_set", "nnth_active_set_4way", "nnth_normalize",
+                                  "nnth_active_set_normalize", "nnth_active_set_f32",
+                                  "nnth_active_set_stop"])
 def test_oracle_non_negative_tucker_hals_matches_reference(golden, case):
     run = golden["runs"][case]
     x = regenerate(run)
@@ -293,3 +300,37 @@ def test_oracle_cp_helpers():
     w2, f2 = oracle.cp_normalize((w, fs))
     np.testing.assert_allclose(oracle.cp_to_tensor((w2, f2)), full, rtol=1e-12, atol=1e-12)
     np.testing.assert_allclose([np.linalg.norm(f, axis=0) for f in f2], 1.0)
+
+
+def test_oracle_tucker_kats_match_reference(golden):
+    """tucker_normalize, kronecker and active_set_nnls of the oracle against
+    the reference's outputs on the recorded inputs."""
+    seen = set()
+    for k in golden["tucker_kats"]:
+        seen.add(k["op"])
+        if k["op"] == "tucker_normalize":
+            c, f = oracle.tucker_normalize((k["core"], k["factors"]))
+            np.testing.assert_allclose(c, k["out_core"], rtol=1e-13, atol=1e-13)
+            for a, b in zip(f, k["out_factors"]):
+                np.testing.assert_allclose(a, b, rtol=1e-13, atol=1e-13)
+        elif k["op"] == "kronecker":
+            np.testing.assert_array_equal(oracle.kronecker(k["matrices"]), k["out"])
+            ms = [m for i, m in enumerate(k["matrices"]) if i != 1][::-1]
+            np.testing.assert_array_equal(oracle.kronecker(ms), k["out_skip1_rev"])
+        elif k["op"] == "active_set_nnls":
+            x0 = None if k["x0"] is None else k["x0"].copy()
+            out = oracle.active_set_nnls(k["Utm"], k["UtU"], x=x0, n_iter_max=100)
+            np.testing.assert_allclose(out, k["out"], rtol=1e-10,
+                                       atol=1e-10 * np.abs(k["out"]).max())
+    assert seen == {"tucker_normalize", "kronecker", "active_set_nnls"}
+
+
+def test_fixed_modes_error_matches_reference(golden):
+    """non_negative_tucker_hals with fixed modes: the reference's first
+    misaligned mode_dot, reproduced by walking the shapes on the host."""
+    from tensorly_gb300.decomposition import _tucker_fixed_modes_error
+    assert golden["fixed_mode_errors"]
+    for e in golden["fixed_mode_errors"]:
+        err = _tucker_fixed_modes_error(e["shape"], e["rank"], e["fixed"], e["init"])
+        assert e["message"] is not None
+        assert isinstance(err, ValueError) and str(err) == e["message"]
