@@ -623,6 +623,21 @@ int tlgb_hals_nnls(int dtype, const void* MtU, const void* UtU, void* V, int64_t
                    size_t workspace_bytes, void* stream);
 
 /*
+ * sparse_residual: with R = X - L (n entries), *out (device double) =
+ * ||R - sparsify(R, k)||_F, where sparsify keeps the entries of R whose
+ * magnitude is at least the k-th largest |R| and zeroes the rest
+ * (tensorly/decomposition/_cp.py:140-159, the sparse-component error of
+ * error_calc, :202-215); k > n keeps everything (error 0).  When `sparse` is
+ * given it receives sparsify(R, k).  The k-th largest magnitude comes from a
+ * radix select on the device (4 passes for f32, 8 for f64).  Workspace:
+ * tlgb_sparse_residual_workspace_bytes().
+ */
+size_t tlgb_sparse_residual_workspace_bytes(void);
+int tlgb_sparse_residual(int dtype, const void* X, const void* L, int64_t n, int64_t k,
+                         double* out, void* sparse, void* workspace, size_t workspace_bytes,
+                         void* stream);
+
+/*
  * kronecker: out = mats[0] (x) mats[1] (x) ... (row-major matrices of
  * rows[k] x cols[k]), the first varying slowest
  * (tensorly/tenalg/core_tenalg/_kronecker.py).

@@ -33,6 +33,7 @@ __all__ = [
     "randomised_parafac", "sparsify_tensor", "error_calc_ext", "validate_constraints", "proximal_operator", "admm",
     "initialize_constrained_parafac", "constrained_parafac", "non_negative_tucker", "fista",
     "non_negative_tucker_hals", "active_set_nnls", "kronecker", "tucker_normalize",
+    "randomized_svd", "randomized_range_finder",
 ]
 
 
@@ -220,16 +221,63 @@ def truncated_svd(matrix, n_eigenvecs=None, **kwargs):
     return U[:, :n_eigenvecs], S[:n_eigenvecs], V[:n_eigenvecs, :]
 
 
+def randomized_range_finder(A, n_dims, n_iter=2, random_state=None):
+    """tensorly/tenalg/svd.py:138-170 (Halko et al. 2009, algorithm 4.4)."""
+    rng = check_random_state(random_state)
+    dim_1, dim_2 = A.shape
+    Q = rng.normal(size=(dim_2, n_dims)).astype(A.dtype)
+    Q, _ = np.linalg.qr(np.dot(A, Q))
+    A_H = np.conj(np.transpose(A))
+    for _ in range(n_iter):
+        Q, _ = np.linalg.qr(np.dot(A_H, Q))
+        Q, _ = np.linalg.qr(np.dot(A, Q))
+    return Q
+
+
+def randomized_svd(matrix, n_eigenvecs=None, n_oversamples=5, n_iter=2, random_state=None,
+                   **kwargs):
+    """tensorly/tenalg/svd.py:288-357 (Halko et al. 2009, algorithm 5.1),
+    transposing as the reference does to keep the reduced matrix small."""
+    n_eigenvecs, min_dim, max_dim = _svd_checks(matrix, n_eigenvecs=n_eigenvecs)
+    dim_1, dim_2 = matrix.shape
+    n_dims = min(n_eigenvecs + n_oversamples, max_dim)
+    if ((dim_1 > dim_2 and n_eigenvecs > min(min_dim, n_dims))
+            or (dim_1 < dim_2 and n_eigenvecs < min(min_dim, n_dims))):
+        matrix_T = np.transpose(matrix)
+        Q = randomized_range_finder(matrix_T, n_dims=n_dims, n_iter=n_iter,
+                                    random_state=random_state)
+        matrix_reduced = np.transpose(np.dot(np.conj(np.transpose(Q)), matrix_T))
+        U, S, V = truncated_svd(matrix_reduced, n_eigenvecs=n_eigenvecs)
+        V = np.dot(V, np.transpose(Q))
+    else:
+        Q = randomized_range_finder(matrix, n_dims=n_dims, n_iter=n_iter,
+                                    random_state=random_state)
+        matrix_reduced = np.dot(np.conj(np.transpose(Q)), matrix)
+        U, S, V = truncated_svd(matrix_reduced, n_eigenvecs=n_eigenvecs)
+        U = np.dot(Q, U)
+    return U, S, V
+
+
 def svd_interface(matrix, method="truncated_svd", n_eigenvecs=None, flip_sign=True,
                   u_based_flip_sign=True, non_negative=None, mask=None,
                   n_iter_mask_imputation=5, **kwargs):
-    """tensorly/tenalg/svd.py:366-447 (truncated_svd method, no mask); the
-    non-negative branch (``:443-444``) applies ``make_svd_non_negative``."""
-    if method != "truncated_svd":
-        raise NotImplementedError("oracle restates method='truncated_svd' only")
-    if mask is not None:
-        raise NotImplementedError("oracle restates the unmasked branch only")
-    U, S, V = truncated_svd(matrix, n_eigenvecs=n_eigenvecs)
+    """tensorly/tenalg/svd.py:366-447 ('truncated_svd' or 'randomized_svd');
+    the mask refill loop (``:431-439``) and the non-negative branch
+    (``:443-444``, ``make_svd_non_negative``)."""
+    if method == "truncated_svd":
+        svd_fun = truncated_svd
+    elif method == "randomized_svd":
+        svd_fun = randomized_svd
+    else:
+        raise NotImplementedError("oracle restates 'truncated_svd' and 'randomized_svd'")
+    U, S, V = svd_fun(matrix, n_eigenvecs=n_eigenvecs, **kwargs)
+    if mask is not None and n_eigenvecs is not None:
+        for _ in range(n_iter_mask_imputation):
+            St = np.eye(U.shape[1], V.shape[0], dtype=matrix.dtype)
+            for i in range(S.shape[0]):
+                St[i, i] = S[i]
+            matrix = matrix * mask + (U @ St @ V) * (1 - mask)
+            U, S, V = svd_fun(matrix, n_eigenvecs=n_eigenvecs, **kwargs)
     if flip_sign:
         U, V = svd_flip(U, V, u_based_decision=u_based_flip_sign)
     if non_negative is not False and non_negative is not None:
@@ -361,17 +409,20 @@ def cp_normalize(cp_tensor):
 
 
 def initialize_cp(tensor, rank, init="svd", svd="truncated_svd", random_state=None,
-                  normalize_factors=False, non_negative=False):
-    """tensorly/decomposition/_cp.py:26-137 (no mask); ``non_negative`` makes
-    the SVD non-negative (NNDSVDA) and takes absolute values (``:129-131``)."""
+                  normalize_factors=False, non_negative=False, mask=None, svd_mask_repeats=5):
+    """tensorly/decomposition/_cp.py:26-137; ``non_negative`` makes the SVD
+    non-negative (NNDSVDA) and takes absolute values (``:129-131``); a mask
+    refills each unfolding inside svd_interface."""
     rng = check_random_state(random_state)
     if isinstance(init, str) and init == "random":
         weights, factors = random_cp(tensor.shape, rank, random_state=rng, dtype=tensor.dtype)
     elif isinstance(init, str) and init == "svd":
         factors = []
         for mode in range(tensor.ndim):
+            mask_unfold = None if mask is None else unfold(mask, mode)
             U, S, _ = svd_interface(unfold(tensor, mode), n_eigenvecs=rank, method=svd,
-                                    non_negative=non_negative)
+                                    non_negative=non_negative, mask=mask_unfold,
+                                    n_iter_mask_imputation=svd_mask_repeats)
             if mode == 0:
                 idx = min(rank, S.shape[0])
                 U = U.copy()
@@ -1057,13 +1108,11 @@ def parafac(tensor, rank, n_iter_max=100, init="svd", svd="truncated_svd",
     (``:529-530``).  Also the orthogonalisation (QR of the factors in the
     first sweeps, ``:392-397``), the line search (``:398-401``, ``:430-478``),
     the sparse component (``:366-370``, ``:532-536``) and the mask (missing
-    entries refilled from the model, ``:441-446``); a masked 'svd' start is
-    not restated.  Returns ``((weights, factors), errors)`` or
-    ``(weights, factors)``; with sparsity ``((weights, factors), sparse)``
-    in place of the CP pair.
+    entries refilled from the model, ``:441-446``; a masked 'svd' start
+    refills each unfolding inside svd_interface).  Returns
+    ``((weights, factors), errors)`` or ``(weights, factors)``; with sparsity
+    ``((weights, factors), sparse)`` in place of the CP pair.
     """
-    if mask is not None and isinstance(init, str) and init == "svd":
-        raise NotImplementedError("oracle restates masked runs from 'random' or given starts")
     if callback is not None and sparsity:
         raise NotImplementedError("oracle restates callbacks without sparsity")
     rank = validate_cp_rank(tensor.shape, rank=rank)
@@ -1072,7 +1121,8 @@ def parafac(tensor, rank, n_iter_max=100, init="svd", svd="truncated_svd",
     acc_pow, acc_fail, max_fail = 2.0, 0, 4
     weights, factors = initialize_cp(tensor, rank, init=init, svd=svd,
                                      random_state=random_state,
-                                     normalize_factors=normalize_factors)
+                                     normalize_factors=normalize_factors, mask=mask,
+                                     svd_mask_repeats=svd_mask_repeats)
     factors = [np.array(f, copy=True) for f in factors]
     if weights is None:
         weights = np.ones(rank, dtype=tensor.dtype)
@@ -1230,13 +1280,16 @@ def tucker_to_vec(tucker_tensor, skip_factor=None, transpose_factors=False):
 
 
 def initialize_tucker(tensor, rank, modes, random_state, init="svd", svd="truncated_svd",
-                      non_negative=False):
-    """tensorly/decomposition/_tucker.py:25-102 (no mask)."""
+                      non_negative=False, mask=None, svd_mask_repeats=5):
+    """tensorly/decomposition/_tucker.py:25-102."""
     if isinstance(init, str) and init == "svd":
         factors = []
         for index, mode in enumerate(modes):
+            mask_unfold = None if mask is None else unfold(mask, mode)
             U, _, _ = svd_interface(unfold(tensor, mode), n_eigenvecs=rank[index], method=svd,
-                                    non_negative=non_negative)
+                                    non_negative=non_negative, mask=mask_unfold,
+                                    n_iter_mask_imputation=svd_mask_repeats,
+                                    random_state=random_state)
             factors.append(U)
         core = multi_mode_dot(tensor, factors, modes=modes, transpose=True)
     elif isinstance(init, str) and init == "random":
@@ -1296,11 +1349,8 @@ def partial_tucker(tensor, rank, modes=None, n_iter_max=100, init="svd", tol=10e
                    svd="truncated_svd", random_state=None, verbose=False, mask=None,
                    svd_mask_repeats=5):
     """tensorly/decomposition/_tucker.py:105-221 (HOOI); with a mask the
-    missing entries are refilled from the model at each iteration (``:194-197``)
-    and the starts are 'random' or given (a masked 'svd' start imputes inside
-    svd_interface and is not restated)."""
-    if mask is not None and isinstance(init, str) and init == "svd":
-        raise NotImplementedError("oracle restates masked HOOI from 'random' or given starts")
+    missing entries are refilled from the model at each iteration
+    (``:194-197``), and a masked 'svd' start refills inside svd_interface."""
     if modes is None:
         modes = list(range(tensor.ndim))
     if rank is None:
@@ -1310,7 +1360,8 @@ def partial_tucker(tensor, rank, modes=None, n_iter_max=100, init="svd", tol=10e
     else:
         rank = tuple(rank)
     core, factors = initialize_tucker(tensor, rank, modes, init=init, svd=svd,
-                                      random_state=random_state)
+                                      random_state=random_state, mask=mask,
+                                      svd_mask_repeats=svd_mask_repeats)
     rec_errors = []
     norm_tensor = norm(tensor)
     for iteration in range(n_iter_max):

@@ -263,6 +263,10 @@ SIGNATURES = [
       ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     ("tlgb_inv_sqrt", ctypes.c_int,
      [ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p]),
+    ("tlgb_sparse_residual_workspace_bytes", ctypes.c_size_t, []),
+    ("tlgb_sparse_residual", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
+      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     ("tlgb_kronecker", ctypes.c_int,
      [ctypes.c_int, ctypes.c_int, _c_vpp, _c_i64p, _c_i64p, ctypes.c_void_p, ctypes.c_void_p]),
     ("tlgb_active_set_nnls", ctypes.c_int,

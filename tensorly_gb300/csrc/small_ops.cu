@@ -166,6 +166,114 @@ __global__ void k_clip_min(T* __restrict__ x, int64_t n, T lo) {
     if (x[e] < lo) x[e] = lo;
 }
 
+// sparsify_tensor (tensorly/decomposition/_cp.py:140-159) on the residual
+// R = X - L: the card-th largest |R| by a most-significant-digit radix
+// select over the bit patterns of |R| (for non-negative IEEE values the bit
+// order is the numeric order), 8 bits a pass, all on the device; then the
+// norm of the entries below it (the sparse component keeps the others).
+struct SelState {
+  unsigned long long prefix;   // the digits of the selected key found so far
+  unsigned long long k;        // rank still to find below the fixed digits
+};
+constexpr int kSelBlocks = 152 * 4;
+
+template <typename T> struct KeyOf;
+template <> struct KeyOf<float> {
+  using U = unsigned int;
+  static constexpr int kBits = 32;
+  __device__ static U key(float v) { return __float_as_uint(v) & 0x7fffffffu; }
+  __device__ static float from(U k) { return __uint_as_float(k); }
+};
+template <> struct KeyOf<double> {
+  using U = unsigned long long;
+  static constexpr int kBits = 64;
+  __device__ static U key(double v) {
+    return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+  }
+  __device__ static double from(U k) { return __longlong_as_double((long long)k); }
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_sel_hist(const T* __restrict__ X, const T* __restrict__ L, int64_t n, int shift,
+           const SelState* st, unsigned long long* __restrict__ hist) {
+  using K = KeyOf<T>;
+  __shared__ unsigned int h[256];
+  for (int b = threadIdx.x; b < 256; b += blockDim.x) h[b] = 0;
+  __syncthreads();
+  const int hi = shift + 8;
+  const unsigned long long hi_mask = hi >= K::kBits ? 0ull : (~0ull << hi);
+  const unsigned long long want = st->prefix & hi_mask;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned long long key = (unsigned long long)K::key(X[e] - L[e]);
+    if ((key & hi_mask) == want) atomicAdd(&h[(key >> shift) & 255u], 1u);
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < 256; b += blockDim.x)
+    if (h[b]) atomicAdd(&hist[b], (unsigned long long)h[b]);
+}
+
+// Fixes the digit at `shift`: the bin, from the top, where the count of keys
+// at or above it first reaches k; clears the histogram for the next pass.
+__global__ void k_sel_pick(unsigned long long* hist, int shift, SelState* st) {
+  if (threadIdx.x == 0) {
+    unsigned long long cum = 0, k = st->k;
+    int bin = 0;
+    for (int b = 255; b >= 0; --b) {
+      if (cum + hist[b] >= k) { bin = b; break; }
+      cum += hist[b];
+    }
+    st->prefix |= (unsigned long long)bin << shift;
+    st->k = k - cum;
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < 256; b += blockDim.x) hist[b] = 0;
+}
+
+// sum of R^2 over |R| < bound (f64, per-block partials), and the sparse
+// component where(|R| < bound, 0, R) when `sparse` is given.
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_sel_resid(const T* __restrict__ X, const T* __restrict__ L, int64_t n, const SelState* st,
+            int keep_all, T* __restrict__ sparse, double* part) {
+  using K = KeyOf<T>;
+  const T bound = keep_all ? T(0) : K::from((typename K::U)st->prefix);
+  __shared__ double red[8];
+  double acc = 0.0;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const T r = X[e] - L[e];
+    const bool small = !keep_all && fabs(r) < bound;
+    if (small) acc += (double)r * (double)r;
+    if (sparse) sparse[e] = small ? T(0) : r;
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < 8; ++w) t += red[w];
+    part[blockIdx.x] = t;
+  }
+}
+
+__global__ void k_sel_init(SelState* st, unsigned long long k, unsigned long long* hist) {
+  if (threadIdx.x == 0) {
+    st->prefix = 0ull;
+    st->k = k;
+  }
+  for (int b = threadIdx.x; b < 256; b += blockDim.x) hist[b] = 0;
+}
+
+__global__ void k_sel_final(const double* part, int nb, double* out) {
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int b = 0; b < nb; ++b) t += part[b];
+    out[0] = sqrt(t);
+  }
+}
+
 // Kronecker product of n_mats matrices, left to right (the first matrix
 // varies slowest), each entry the product of one entry of every matrix taken
 // in that order (tensorly/tenalg/core_tenalg/_kronecker.py).
@@ -1037,6 +1145,58 @@ extern "C" int tlgb_tucker_normalize(int dtype, int ndim, const int64_t* rows, c
     TLGB_LAUNCH_CHECK();
     k_tn_apply<float><<<nb, 256, 0, st>>>(a, scales);
   }
+  TLGB_LAUNCH_CHECK();
+  return TLGB_OK;
+}
+
+extern "C" size_t tlgb_sparse_residual_workspace_bytes(void) {
+  return align_up(sizeof(SelState), 256) + align_up(sizeof(unsigned long long) * 256, 256) +
+         align_up(sizeof(double) * kSelBlocks, 256);
+}
+
+extern "C" int tlgb_sparse_residual(int dtype, const void* X, const void* L, int64_t n,
+                                    int64_t k, double* out, void* sparse, void* workspace,
+                                    size_t workspace_bytes, void* stream) {
+  clear_error();
+  TLGB_CHECK_ARG(dtype == TLGB_F32 || dtype == TLGB_F64, "sparse_residual: f32 or f64");
+  TLGB_CHECK_ARG(X && L && out && n >= 1 && k >= 1, "sparse_residual: bad argument");
+  if (!workspace || workspace_bytes < tlgb_sparse_residual_workspace_bytes())
+    return set_error(TLGB_EWORKSPACE, "sparse_residual: workspace too small");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  char* base = static_cast<char*>(workspace);
+  SelState* ss = reinterpret_cast<SelState*>(base);
+  unsigned long long* hist =
+      reinterpret_cast<unsigned long long*>(base + align_up(sizeof(SelState), 256));
+  double* part = reinterpret_cast<double*>(base + align_up(sizeof(SelState), 256) +
+                                           align_up(sizeof(unsigned long long) * 256, 256));
+  const int keep_all = k > n ? 1 : 0;   // the reference returns the residual itself
+  const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, (int64_t)256), kSelBlocks));
+  if (!keep_all) {
+    k_sel_init<<<1, 256, 0, st>>>(ss, (unsigned long long)k, hist);
+    TLGB_LAUNCH_CHECK();
+    const int bits = dtype == TLGB_F64 ? 64 : 32;
+    for (int shift = bits - 8; shift >= 0; shift -= 8) {
+      if (dtype == TLGB_F64)
+        k_sel_hist<double><<<nb, 256, 0, st>>>(static_cast<const double*>(X),
+                                               static_cast<const double*>(L), n, shift, ss, hist);
+      else
+        k_sel_hist<float><<<nb, 256, 0, st>>>(static_cast<const float*>(X),
+                                              static_cast<const float*>(L), n, shift, ss, hist);
+      TLGB_LAUNCH_CHECK();
+      k_sel_pick<<<1, 256, 0, st>>>(hist, shift, ss);
+      TLGB_LAUNCH_CHECK();
+    }
+  }
+  if (dtype == TLGB_F64)
+    k_sel_resid<double><<<nb, 256, 0, st>>>(static_cast<const double*>(X),
+                                            static_cast<const double*>(L), n, ss, keep_all,
+                                            static_cast<double*>(sparse), part);
+  else
+    k_sel_resid<float><<<nb, 256, 0, st>>>(static_cast<const float*>(X),
+                                           static_cast<const float*>(L), n, ss, keep_all,
+                                           static_cast<float*>(sparse), part);
+  TLGB_LAUNCH_CHECK();
+  k_sel_final<<<1, 32, 0, st>>>(part, nb, out);
   TLGB_LAUNCH_CHECK();
   return TLGB_OK;
 }

@@ -48,8 +48,6 @@ def initialize_cp(tensor, rank, init="svd", svd="truncated_svd", non_negative=Fa
     mean (``:102-126``).
     """
     x, _ = to_device(tensor)
-    if mask is not None and isinstance(init, str) and init == "svd":
-        raise NotImplementedError("masked 'svd' initialisation is not supported")
     rng = check_random_state(random_state)
     if isinstance(init, str) and init == "random":
         factors = [torch.from_numpy(rng.random_sample((int(s), int(rank)))).to(x.device, x.dtype)
@@ -59,8 +57,11 @@ def initialize_cp(tensor, rank, init="svd", svd="truncated_svd", non_negative=Fa
         from .svd import svd_interface_unfolding
         factors = []
         for mode in range(x.ndim):
+            # the reference passes no random_state here: a randomised SVD draws
+            # from NumPy's global generator
             U, S = svd_interface_unfolding(x, mode, n_eigenvecs=rank, method=svd,
-                                           non_negative=non_negative)
+                                           non_negative=non_negative, mask=mask,
+                                           n_iter_mask_imputation=svd_mask_repeats)
             if mode == 0:
                 idx = min(rank, S.shape[0])
                 U = U.clone()
@@ -129,11 +130,12 @@ def parafac(tensor, rank, n_iter_max=100, init="svd", svd="truncated_svd",
     per-mode MTTKRP durations (ms, CUDA events inside the sweep) of the last
     sweep of that kind.
     """
-    if sparsity:
-        raise NotImplementedError("parafac with sparsity is not supported by tensorly_gb300")
-    if (linesearch or orthogonalise or mask is not None) and precision != "native":
-        raise NotImplementedError("parafac line search, orthogonalise and masks run at native "
-                                  "precision")
+    if sparsity and callback is not None:
+        raise NotImplementedError("parafac with both sparsity and a callback is not supported "
+                                  "by tensorly_gb300")
+    if (linesearch or orthogonalise or mask is not None or sparsity) and precision != "native":
+        raise NotImplementedError("parafac line search, orthogonalise, masks and sparsity run "
+                                  "at native precision")
     if precision not in _PRECISIONS:
         raise ValueError(f"precision must be one of {sorted(_PRECISIONS)}")
     x, pl = to_device(tensor)
@@ -163,13 +165,13 @@ def parafac(tensor, rank, n_iter_max=100, init="svd", svd="truncated_svd",
     for m in fixed:
         fixed_mask |= 1 << int(m)
 
-    if linesearch or orthogonalise or mask is not None:
+    if linesearch or orthogonalise or mask is not None or sparsity:
         return _parafac_host_loop(x, pl, rank, weights, factors, n_iter_max=n_iter_max,
                                   orthogonalise=orthogonalise, tol=tol, verbose=verbose,
                                   return_errors=return_errors, l2_reg=l2_reg,
                                   cvg_criterion=cvg_criterion, fixed_mask=fixed_mask,
                                   normalize_factors=normalize_factors, linesearch=linesearch,
-                                  callback=callback, mask=mask)
+                                  callback=callback, mask=mask, sparsity=sparsity)
 
     lib = _lib.lib()
     opts = _lib.CpAlsOptions()
@@ -232,11 +234,18 @@ def parafac(tensor, rank, n_iter_max=100, init="svd", svd="truncated_svd",
 
 def _parafac_host_loop(x, pl, rank, weights, factors, *, n_iter_max, orthogonalise, tol,
                        verbose, return_errors, l2_reg, cvg_criterion, fixed_mask,
-                       normalize_factors, linesearch, callback, mask=None):
-    """parafac with orthogonalisation, the line search and / or a mask
-    (tensorly/decomposition/_cp.py:392-401, :430-478, :194-207, :441-446):
-    the reference's iteration loop on the host around single-sweep
-    ``tlgb_cp_als`` calls.
+                       normalize_factors, linesearch, callback, mask=None, sparsity=None):
+    """parafac with orthogonalisation, the line search, a mask and / or a
+    sparse component (tensorly/decomposition/_cp.py:392-401, :430-478,
+    :194-215, :441-446, :372-377, :532-538): the reference's iteration loop
+    on the host around single-sweep ``tlgb_cp_als`` calls.
+
+    With ``sparsity`` (a fraction of the entries, or a count) every error is
+    the norm of R - sparsify(R) for the residual R = X - [[w; A]], the model
+    formed by ``tlgb_cp_to_tensor`` and the card-th largest |R| found by the
+    radix select of ``tlgb_sparse_residual``; the sweeps themselves are the
+    plain ones, as in the reference, and the sparse component of the final
+    model is returned beside it.
 
     With a mask the sweeps run on a working copy of the tensor whose missing
     entries are refilled from the model after every sweep
@@ -283,28 +292,66 @@ def _parafac_host_loop(x, pl, rank, weights, factors, *, n_iter_max, orthogonali
         return float(errs[0])
 
     norm_tensor = _norm_on_device(x)
-    if mask is not None:
-        mask_t = like(mask, x).expand(x.shape).contiguous()
-        x = x.clone()   # the refilled working tensor; the caller's tensor is not modified
+    n_entries = x.numel()
+    card = None
+    if sparsity:
+        card = int(sparsity * n_entries) if isinstance(sparsity, float) else int(sparsity)
+        # sparsify_tensor's bound is sort(|R|)[-card]: the card-th largest for
+        # card >= 1, position -card from the smallest otherwise
+        if card >= n_entries:
+            sel_k = n_entries + 1                      # keeps the whole residual
+        elif card >= 1:
+            sel_k = card
+        elif -card < n_entries:
+            sel_k = n_entries + card
+        else:
+            raise IndexError(f"index {-card} is out of bounds for axis 0 with size {n_entries}")
+        sel_ws = workspace(int(lib.tlgb_sparse_residual_workspace_bytes()), x.device)
+        sel_out = torch.empty(1, dtype=torch.float64, device=x.device)
+    if mask is not None or sparsity:
         rec = torch.empty_like(x)
-        imp_ws = workspace(int(lib.tlgb_mask_impute_workspace_bytes()), x.device)
-        imp_out = torch.empty(2, dtype=torch.float64, device=x.device)
         dims = _lib.i64_array(x.shape)
         rec_bytes = ctypes.c_size_t(0)
         _lib.check(lib.tlgb_cp_to_tensor_workspace_size(dtype_code(x), x.ndim, dims, rank,
                                                         ctypes.byref(rec_bytes)))
         rec_ws = workspace(rec_bytes.value, x.device)
+    if mask is not None:
+        mask_t = like(mask, x).expand(x.shape).contiguous()
+        x = x.clone()   # the refilled working tensor; the caller's tensor is not modified
+        imp_ws = workspace(int(lib.tlgb_mask_impute_workspace_bytes()), x.device)
+        imp_out = torch.empty(2, dtype=torch.float64, device=x.device)
 
-    def refill(target, w, fs):
-        """target = target * mask + [[w; fs]] * (1 - mask); (||target||, ||target - [[w; fs]]||)."""
+    def model(w, fs):
         _lib.check(lib.tlgb_cp_to_tensor(dtype_code(x), x.ndim, dims, rank,
                                          _lib.ptr_array([ptr(f) for f in fs]), ptr(w), None,
                                          ptr(rec), ptr(rec_ws), rec_ws.numel(), stream_of(x)))
+
+    def sparse_error(target, sparse_out=None):
+        """||R - sparsify(R)|| for R = target - rec (the model already in rec)."""
+        _lib.check(lib.tlgb_sparse_residual(dtype_code(x), ptr(target), ptr(rec), n_entries,
+                                            sel_k, ptr(sel_out), ptr(sparse_out), ptr(sel_ws),
+                                            sel_ws.numel(), stream_of(x)))
+        return float(sel_out.item())
+
+    def refill(target, w, fs):
+        """target = target * mask + [[w; fs]] * (1 - mask); (||target||, the
+        error of [[w; fs]] against it: ||target - [[w; fs]]||, or with a sparse
+        component ||R - sparsify(R)||)."""
+        model(w, fs)
         _lib.check(lib.tlgb_mask_impute(dtype_code(x), ptr(target), ptr(mask_t), ptr(rec),
                                         target.numel(), ptr(imp_out), ptr(imp_ws),
                                         imp_ws.numel(), stream_of(x)))
         v = imp_out.cpu()
+        if sparsity:
+            return float(v[0]), sparse_error(target)
         return float(v[0]), float(v[1])
+
+    def explicit_error(w, fs):
+        """The unmasked error of [[w; fs]]: explicit residual, sparse if asked."""
+        if sparsity:
+            model(w, fs)
+            return sparse_error(x)
+        return _residual_norm(x, fs, w)
 
     if callback is not None:
         if mask is not None:
@@ -328,6 +375,8 @@ def _parafac_host_loop(x, pl, rank, weights, factors, *, n_iter_max, orthogonali
         if not line_iter:
             if mask is not None:
                 norm_tensor, unnorm = refill(x, weights, factors)
+            elif sparsity:
+                unnorm = explicit_error(weights, factors)
             else:
                 unnorm = fast_error * norm_tensor
         else:
@@ -340,7 +389,7 @@ def _parafac_host_loop(x, pl, rank, weights, factors, *, n_iter_max, orthogonali
                 x_new = x.clone()
                 new_norm, new_error = refill(x_new, new_weights, new_factors)
             else:
-                new_norm, new_error = norm_tensor, _residual_norm(x, new_factors, new_weights)
+                new_norm, new_error = norm_tensor, explicit_error(new_weights, new_factors)
             if new_error / new_norm < rec_errors[-1]:
                 factors, weights = new_factors, new_weights
                 if mask is not None:
@@ -353,6 +402,8 @@ def _parafac_host_loop(x, pl, rank, weights, factors, *, n_iter_max, orthogonali
             else:
                 if mask is not None:
                     norm_tensor, unnorm = refill(x, weights, factors)
+                elif sparsity:
+                    unnorm = explicit_error(weights, factors)
                 else:
                     unnorm = fast_error * norm_tensor
                 acc_fail += 1
@@ -381,6 +432,12 @@ def _parafac_host_loop(x, pl, rank, weights, factors, *, n_iter_max, orthogonali
             weights, factors = cp_normalize((weights, factors))
             factors = list(factors)
     cp = _place_cp(weights, factors, pl)
+    if sparsity:
+        # the sparse component of the final model against the (refilled) tensor
+        model(weights, factors)
+        sparse = torch.empty_like(x)
+        sparse_error(x, sparse)
+        cp = (cp, pl.back(sparse))
     if return_errors:
         return cp, rec_errors
     return cp
@@ -439,18 +496,20 @@ def initialize_tucker(tensor, rank, modes, random_state, init="svd", svd="trunca
     ``'svd'``: the leading left singular vectors of each unfolding from the
     library (Gram eigensolver, svd_flip signs), core = X x_n U_n^T.
     ``'random'``: the reference's host draws (core + 0.01), copied once.
-    A (core, factors) pair is used as given.
+    A (core, factors) pair is used as given.  With a mask, each unfolding's
+    SVD refills the missing entries ``svd_mask_repeats`` times; the core is
+    taken from the tensor as given, as in the reference.
     """
     x, _ = to_device(tensor)
-    if mask is not None:
-        raise NotImplementedError("masked Tucker is not supported by tensorly_gb300")
     if isinstance(init, str) and init == "svd":
         from .svd import svd_interface_unfolding
         from .tenalg import multi_mode_dot
         factors = []
         for index, mode in enumerate(modes):
             U, _ = svd_interface_unfolding(x, mode, n_eigenvecs=rank[index], method=svd,
-                                           non_negative=non_negative)
+                                           non_negative=non_negative, mask=mask,
+                                           n_iter_mask_imputation=svd_mask_repeats,
+                                           random_state=random_state)
             factors.append(U)
         core = multi_mode_dot(x, factors, modes=modes, transpose=True)
     elif isinstance(init, str) and init == "random":
@@ -506,16 +565,42 @@ def _hooi(x, rank, modes, factors, n_iter_max, tol, init_svd):
     return core, factors, [float(errs[i]) for i in range(n_err.value)]
 
 
+def _masked_hooi(x, mask, rank, modes, core, factors, n_iter_max, tol):
+    """The masked iteration of tensorly/decomposition/_tucker.py:184-221:
+    refill, then one HOOI iteration of the library on the refilled tensor."""
+    from .tenalg import multi_mode_dot
+    lib = _lib.lib()
+    m = torch.as_tensor(mask).to(device=x.device, dtype=x.dtype).expand(x.shape).contiguous()
+    norm2 = float(_dot(x, x).item())
+    norm_tensor = math.sqrt(norm2)
+    cur = x.clone()      # the reference refills its working copy in place every iteration
+    ws = workspace(int(lib.tlgb_mask_impute_workspace_bytes()), x.device)
+    norms = torch.empty(2, dtype=torch.float64, device=x.device)
+    rec_errors = []
+    for iteration in range(int(n_iter_max)):
+        rec = multi_mode_dot(core, factors, modes=modes).contiguous()
+        _lib.check(lib.tlgb_mask_impute(dtype_code(x), ptr(cur), ptr(m), ptr(rec), x.numel(),
+                                        ptr(norms), ptr(ws), ws.numel(), stream_of(x)))
+        core, factors, _ = _hooi(cur, rank, modes, factors, 1, 0.0, False)
+        c2 = float(_dot(core, core).item())
+        rec_errors.append(math.sqrt(abs(norm2 - c2)) / norm_tensor)
+        if iteration > 1 and tol and abs(rec_errors[-2] - rec_errors[-1]) < tol:
+            break
+    return core, factors, rec_errors
+
+
 def partial_tucker(tensor, rank, modes=None, n_iter_max=100, init="svd", tol=10e-5,
                    svd="truncated_svd", random_state=None, verbose=False, mask=None,
                    svd_mask_repeats=5):
     """Partial Tucker decomposition by HOOI (tensorly/decomposition/_tucker.py:105-221).
 
     Same signature and return value, ``((core, factors), rec_errors)``; the
-    iteration runs in the library (``tlgb_tucker_hooi``).
+    iteration runs in the library (``tlgb_tucker_hooi``).  With a mask every
+    iteration first refills the missing entries from the current model
+    (``tensor * mask + [[core; factors]] * (1 - mask)``, ``tlgb_mask_impute``)
+    and runs one library iteration on the refilled tensor; the error uses the
+    norm of the tensor as given, as the reference does.
     """
-    if mask is not None:
-        raise NotImplementedError("masked Tucker is not supported by tensorly_gb300")
     x, pl = to_device(tensor)
     x = x.contiguous()
     if modes is None:
@@ -536,21 +621,26 @@ def partial_tucker(tensor, rank, modes=None, n_iter_max=100, init="svd", tol=10e
         # factor list (core_tenalg/n_mode_product.py:117-124), so unsorted
         # modes feed it mismatched factors and end in a shape error
         raise ValueError(f"partial_tucker: modes {modes} are not in ascending order")
-    if isinstance(init, str) and init == "svd" and svd not in ("truncated_svd", "symeig_svd"):
-        raise NotImplementedError(f"svd method {svd!r} is not supported by tensorly_gb300")
-    if isinstance(init, str) and init == "svd":
+    if (isinstance(init, str) and init == "svd" and svd in ("truncated_svd", "symeig_svd")
+            and mask is None):
         init_factors = [None] * len(modes)
         core0 = None
         init_svd = True
     else:
-        core0, init_factors = initialize_tucker(x, rank, modes, random_state, init=init, svd=svd)
+        core0, init_factors = initialize_tucker(x, rank, modes, random_state, init=init, svd=svd,
+                                                mask=mask, svd_mask_repeats=svd_mask_repeats)
         init_svd = False
     if int(n_iter_max) <= 0:
         if init_svd:
             core0, init_factors = initialize_tucker(x, rank, modes, random_state, init=init,
                                                     svd=svd)
         return (pl.back(core0), [pl.back(f) for f in init_factors]), []
-    core, factors, rec_errors = _hooi(x, rank, modes, init_factors, n_iter_max, tol, init_svd)
+    if mask is not None:
+        core, factors, rec_errors = _masked_hooi(x, mask, rank, modes, core0, init_factors,
+                                                 n_iter_max, tol)
+    else:
+        core, factors, rec_errors = _hooi(x, rank, modes, init_factors, n_iter_max, tol,
+                                          init_svd)
     if verbose:
         for i in range(2, len(rec_errors)):
             print(f"reconstruction error={rec_errors[i]}, "

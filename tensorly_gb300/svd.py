@@ -18,7 +18,16 @@ import torch
 from . import _lib
 from ._tensor import dtype_code, ptr, stream_of, to_device, workspace
 
-SVD_FUNS = ["truncated_svd", "symeig_svd"]
+SVD_FUNS = ["truncated_svd", "symeig_svd", "randomized_svd"]
+
+
+def _check_method(method):
+    if method in SVD_FUNS:
+        return
+    if callable(method):
+        raise NotImplementedError("a callable svd method is not supported by tensorly_gb300")
+    raise ValueError(f"Got svd={method}. However, the possible choices are {SVD_FUNS} or to "
+                     "pass a callable.")
 
 
 def _svd_unfolding_raw(x, mode, k, flip=True):
@@ -57,29 +66,85 @@ def _n_eigenvecs(rows, cols, n_eigenvecs):
 
 
 def svd_interface_unfolding(tensor, mode, n_eigenvecs, method="truncated_svd",
-                            non_negative=False, flip_sign=True):
+                            non_negative=False, flip_sign=True, mask=None,
+                            n_iter_mask_imputation=5, random_state=None):
     """(U, S) of ``svd_interface(unfold(tensor, mode), n_eigenvecs, method,
-    non_negative=non_negative)`` (tensorly/tenalg/svd.py:366-447) without
-    forming the unfolding; ``non_negative`` (True = 'nndsvda', or 'nndsvd')
-    replaces U by the NNDSVD factor W (``:443-444``, ``:68-134``)."""
+    non_negative=non_negative, mask=unfold(mask, mode), ...)``
+    (tensorly/tenalg/svd.py:366-447).  The Gram methods never form the
+    unfolding.  ``non_negative`` (True = 'nndsvda', or 'nndsvd') replaces U by
+    the NNDSVD factor W (``:443-444``, ``:68-134``).  With a mask the missing
+    entries are refilled ``n_iter_mask_imputation`` times from the rank
+    ``n_eigenvecs`` reconstruction U U^T M (``:431-439``); the tensor is not
+    changed.  'randomized_svd' works on the explicit unfolding
+    (``randomized_svd``)."""
     if non_negative not in (None, False, True, "nndsvd", "nndsvda"):
         raise ValueError(f'Invalid nntype parameter: got {non_negative} instead of one of '
                          '("nndsvd", "nndsvda")')
-    if not (method in SVD_FUNS):
-        if callable(method) or method == "randomized_svd":
-            raise NotImplementedError(f"svd method {method!r} is not supported by tensorly_gb300")
-        raise ValueError(f"Got svd={method}. However, the possible choices are {SVD_FUNS} or to "
-                         "pass a callable.")
+    _check_method(method)
     x, _ = to_device(tensor)
     x = x.contiguous()
-    rows = x.shape[mode]
-    cols = x.numel() // max(1, rows)
-    ucols, scount = _n_eigenvecs(rows, cols, n_eigenvecs)
-    U, S = _svd_unfolding_raw(x, mode, ucols, flip=flip_sign)
-    S = S[:scount]
+    if mask is not None and n_eigenvecs is not None:
+        m = torch.as_tensor(mask).to(device=x.device, dtype=x.dtype).expand(x.shape).contiguous()
+        x = x.clone()
+        U, S, V = _svd_any(x, mode, n_eigenvecs, method, random_state, flip=False)
+        for _ in range(int(n_iter_mask_imputation)):
+            _refill(x, m, mode, U, S, V)
+            U, S, V = _svd_any(x, mode, n_eigenvecs, method, random_state, flip=False)
+        if flip_sign:
+            U = _flip_columns(U)
+    else:
+        U, S, _ = _svd_any(x, mode, n_eigenvecs, method, random_state, flip=flip_sign)
     if non_negative not in (None, False):
         U = _nndsvd_unfolding(x, mode, U, S, "nndsvda" if non_negative is True else non_negative)
     return U, S
+
+
+def _svd_any(x, mode, n_eigenvecs, method, random_state, flip):
+    """(U, S, V) of unfold(x, mode) by the randomised range finder, or (U, S,
+    None) by the Gram eigensolver (whose V is never needed: U diag(S) V is
+    U U^T M there)."""
+    rows = x.shape[mode]
+    cols = x.numel() // max(1, rows)
+    if method == "randomized_svd":
+        from .base import unfold
+        U, S, V = randomized_svd(x if x.ndim == 2 and mode == 0 else unfold(x, mode),
+                                 n_eigenvecs=n_eigenvecs, random_state=random_state)
+        if flip:
+            U, V = svd_flip(U, V)
+        return U, S, V
+    ucols, scount = _n_eigenvecs(rows, cols, n_eigenvecs)
+    U, S = _svd_unfolding_raw(x, mode, ucols, flip=flip)
+    return U, S[:scount], None
+
+
+def _refill(x, mask, mode, U, S, V):
+    """x = x * mask + R * (1 - mask) in place (``tlgb_mask_impute``), R the
+    rank-k reconstruction U diag(S) V of the mode-`mode` unfolding M of x
+    (tensorly/tenalg/svd.py:431-439).  With the Gram eigensolver's exact
+    singular vectors R = U U^T M, two mode products; the randomised SVD's V
+    is only approximately M's, so there R is formed from U, S and V and
+    folded back."""
+    from .tenalg import _mode_dot_cuda
+    k = int(S.shape[0])
+    Uk = U[:, :k].contiguous()
+    if V is None:
+        rec = _mode_dot_cuda(_mode_dot_cuda(x, Uk, mode, True), Uk, mode, False)
+    else:
+        from .base import fold
+        from .decomposition import _mat_nn, _scale_columns
+        rec_m = _mat_nn(_scale_columns(Uk, S.contiguous()), V[:k].contiguous())
+        rec = rec_m if (x.ndim == 2 and mode == 0) else fold(rec_m, mode, tuple(x.shape))
+    lib = _lib.lib()
+    ws = workspace(int(lib.tlgb_mask_impute_workspace_bytes()), x.device)
+    norms = torch.empty(2, dtype=torch.float64, device=x.device)
+    _lib.check(lib.tlgb_mask_impute(dtype_code(x), ptr(x), ptr(mask), ptr(rec.contiguous()),
+                                    x.numel(), ptr(norms), ptr(ws), ws.numel(), stream_of(x)))
+
+
+def _flip_columns(U):
+    """svd_flip's U-based sign rule (tensorly/tenalg/svd.py:13-65) on U alone."""
+    Ut, _ = svd_flip(U, U[:0].t().contiguous())
+    return Ut
 
 
 def _nndsvd_unfolding(x, mode, U, S, nntype):
@@ -161,20 +226,82 @@ def truncated_svd(matrix, n_eigenvecs=None, **kwargs):
     return pl.back(U), pl.back(S), pl.back(V)
 
 
+def randomized_svd(matrix, n_eigenvecs=None, n_oversamples=5, n_iter=2, random_state=None,
+                   **kwargs):
+    """Truncated randomised SVD (tensorly/tenalg/svd.py:288-357, Halko et al.
+    2009, algorithms 4.4 and 5.1): the reference's Gaussian test matrix drawn
+    from ``random_state`` on the host, then on the GPU the range finder's
+    products (``tlgb_gemm``) and Householder QRs (``tlgb_qr``, NumPy's column
+    signs), and the truncated SVD of the reduced matrix.  The reference's
+    choice of transposing a wide matrix is kept.  The QR'd blocks must be
+    tall and at most 256 columns wide."""
+    from .decomposition import _mat_nn, _mat_tn, _mat_nt
+    from .parafac2 import _qr
+    from .random import check_random_state
+    m, pl = to_device(matrix)
+    if m.ndim != 2:
+        raise ValueError("randomized_svd expects a matrix")
+    m = m.contiguous()
+    dim_1, dim_2 = int(m.shape[0]), int(m.shape[1])
+    min_dim, max_dim = min(dim_1, dim_2), max(dim_1, dim_2)
+    if n_eigenvecs is None:
+        n_eigenvecs = max_dim
+    if n_eigenvecs > max_dim:
+        warnings.warn(f"Trying to compute SVD with n_eigenvecs={n_eigenvecs}, which is larger "
+                      f"than max(matrix.shape)={max_dim}. Setting n_eigenvecs to {max_dim}.")
+        n_eigenvecs = max_dim
+    n_dims = min(n_eigenvecs + n_oversamples, max_dim)
+    transpose = ((dim_1 > dim_2 and n_eigenvecs > min(min_dim, n_dims))
+                 or (dim_1 < dim_2 and n_eigenvecs < min(min_dim, n_dims)))
+    a = m.t().contiguous() if transpose else m          # the matrix whose range is found
+    ra, ca = int(a.shape[0]), int(a.shape[1])
+    if n_dims > min(ra, ca) or n_dims > 256:
+        raise NotImplementedError("randomized_svd: the range finder's blocks must be tall and at "
+                                  "most 256 columns wide")
+    rng = check_random_state(random_state)
+    g = torch.from_numpy(rng.normal(size=(ca, n_dims))).to(device=m.device, dtype=m.dtype)
+    q = _qr(_mat_nn(a, g))
+    for _ in range(int(n_iter)):
+        q = _qr(_mat_tn(a, q))
+        q = _qr(_mat_nn(a, q))
+    if transpose:
+        # matrix_reduced = (Q^H A)^T = M Q (dim_1 x n_dims); V = V_r Q^T
+        U, S, V = truncated_svd(_mat_nn(m, q), n_eigenvecs=n_eigenvecs)
+        V = _mat_nt(V, q)
+    else:
+        U, S, V = truncated_svd(_mat_tn(q, m), n_eigenvecs=n_eigenvecs)
+        U = _mat_nn(q, U)
+    return pl.back(U), pl.back(S), pl.back(V)
+
+
 def svd_interface(matrix, method="truncated_svd", n_eigenvecs=None, flip_sign=True,
                   u_based_flip_sign=True, non_negative=None, mask=None,
                   n_iter_mask_imputation=5, **kwargs):
-    """tensorly/tenalg/svd.py:366-447 for method 'truncated_svd' / 'symeig_svd'."""
-    if mask is not None:
-        raise NotImplementedError("svd with missing-value imputation is not supported")
+    """tensorly/tenalg/svd.py:366-447: 'truncated_svd' / 'symeig_svd' (Gram
+    eigensolver) or 'randomized_svd', the mask refill loop (``:431-439``) and
+    svd_flip.  The non-negative post-processing is not supported here
+    (``svd_interface_unfolding`` provides it for tensor unfoldings)."""
     if non_negative not in (None, False):
-        raise NotImplementedError("non-negative SVD is not supported")
-    if method not in SVD_FUNS:
-        if callable(method) or method == "randomized_svd":
-            raise NotImplementedError(f"svd method {method!r} is not supported by tensorly_gb300")
-        raise ValueError(f"Got svd={method}. However, the possible choices are {SVD_FUNS} or to "
-                         "pass a callable.")
-    U, S, V = truncated_svd(matrix, n_eigenvecs=n_eigenvecs)
-    if flip_sign and not u_based_flip_sign:
-        U, V = svd_flip(U, V, u_based_decision=False)
-    return U, S, V
+        raise NotImplementedError("non-negative SVD of a matrix is not supported")
+    _check_method(method)
+    m, pl = to_device(matrix)
+    if m.ndim != 2:
+        raise ValueError("svd_interface expects a matrix")
+
+    def svd_fun(a):
+        if method == "randomized_svd":
+            return randomized_svd(a, n_eigenvecs=n_eigenvecs, **kwargs)
+        return truncated_svd(a, n_eigenvecs=n_eigenvecs)
+
+    if mask is not None and n_eigenvecs is not None:
+        m = m.contiguous().clone()
+        mk = torch.as_tensor(mask).to(device=m.device, dtype=m.dtype).expand(m.shape).contiguous()
+        U, S, V = svd_fun(m)
+        for _ in range(int(n_iter_mask_imputation)):
+            _refill(m, mk, 0, U, S, V)
+            U, S, V = svd_fun(m)
+    else:
+        U, S, V = svd_fun(m.contiguous())
+    if flip_sign:
+        U, V = svd_flip(U, V, u_based_decision=u_based_flip_sign)
+    return pl.back(U), pl.back(S), pl.back(V)

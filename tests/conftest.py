@@ -36,9 +36,12 @@ def golden():
         cons_cols = pickle.load(f)
     with open(os.path.join(here, "tucker_extra_runs.pkl"), "rb") as f:
         tucker_extra = pickle.load(f)
+    with open(os.path.join(here, "svd_extra_runs.pkl"), "rb") as f:
+        svd_extra = pickle.load(f)
     return {"kats": kats["records"],
             "runs": {r["case"]: r for r in runs["runs"] + cons_cols["runs"]
-                     + tucker_extra["runs"]},
+                     + tucker_extra["runs"] + svd_extra["runs"]},
+            "svd_kats": svd_extra["kats"],
             "recon": recon["records"], "versions": runs["versions"],
             "tucker_kats": tucker_extra["kats"],
             "fixed_mode_errors": tucker_extra["fixed_mode_errors"]}

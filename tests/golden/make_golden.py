@@ -774,6 +774,80 @@ def record_tucker_extras():
     return {"runs": runs, "kats": kats, "fixed_mode_errors": errors}
 
 
+def record_svd_extras():
+    """svd_interface with a mask and with 'randomized_svd'
+    (tensorly/tenalg/svd.py:138-170, :288-357, :431-439), and the callers
+    that reach them: masked tucker (tensorly/decomposition/_tucker.py:25-221)
+    from 'svd' and 'random' starts, tucker and parafac with
+    svd='randomized_svd', and parafac with a mask from an 'svd' start
+    (tensorly/decomposition/_cp.py:26-137).  Randomised runs without a
+    random_state draw from NumPy's global generator, seeded here and in the
+    tests by ``np_seed``."""
+    import copy
+    from golden_inputs import small_cp
+    import tensorly as tl
+    from tensorly.decomposition import parafac, tucker
+    from tensorly.tenalg.svd import randomized_svd, svd_interface
+    rs = np.random.RandomState(150)
+    kats = []
+    for (r, c), k, method, keep in (((30, 20), 4, "truncated_svd", 0.8),
+                                    ((20, 45), 3, "truncated_svd", 0.7),
+                                    ((40, 25), 5, "randomized_svd", 0.85),
+                                    ((18, 60), 4, "randomized_svd", 0.8),
+                                    ((50, 12), 3, "truncated_svd", None),
+                                    ((12, 70), 5, "randomized_svd", None),
+                                    ((64, 30), 6, "randomized_svd", None)):
+        lr = rs.randn(r, k + 1) @ rs.randn(k + 1, c) + 0.05 * rs.randn(r, c)
+        mask = None if keep is None else (rs.rand(r, c) < keep).astype(np.float64)
+        kw = dict(n_eigenvecs=k, method=method)
+        if method == "randomized_svd":
+            kw["random_state"] = 7
+        U, S, V = svd_interface(tl.tensor(lr), mask=None if mask is None else tl.tensor(mask),
+                                n_iter_mask_imputation=4, **kw)
+        kats.append({"op": "svd_interface", "matrix": lr, "mask": mask, "kwargs": kw,
+                     "n_iter_mask_imputation": 4,
+                     "U": np.array(U), "S": np.array(S), "V": np.array(V)})
+    for (r, c), k in (((40, 15), 4), ((15, 40), 4), ((30, 30), 6)):
+        m = rs.randn(r, c)
+        U, S, V = randomized_svd(tl.tensor(m), n_eigenvecs=k, n_iter=3, random_state=11)
+        kats.append({"op": "randomized_svd", "matrix": m, "kwargs": dict(n_eigenvecs=k, n_iter=3),
+                     "random_state": 11, "U": np.array(U), "S": np.array(S), "V": np.array(V)})
+    runs = []
+    variants = [
+        ("tucker_mask_svd", "tucker", dict(shape=(10, 9, 8), rank=3, seed=151, mask_keep=0.85),
+         dict(rank=[3, 3, 2], n_iter_max=6, init="svd", tol=0), None),
+        ("tucker_mask_random", "tucker", dict(shape=(9, 8, 7, 6), rank=2, seed=152,
+                                              mask_keep=0.8),
+         dict(rank=[2, 2, 2, 2], n_iter_max=5, init="random", random_state=3, tol=0), None),
+        ("tucker_randomized", "tucker", dict(shape=(12, 10, 9), rank=3, seed=153),
+         dict(rank=[3, 3, 3], n_iter_max=4, init="svd", svd="randomized_svd", random_state=5,
+              tol=0), None),
+        ("cp_randomized", "parafac", dict(shape=(11, 10, 9), rank=3, seed=154),
+         dict(rank=3, n_iter_max=6, init="svd", svd="randomized_svd", tol=0), 21),
+        ("cp_mask_svd", "parafac", dict(shape=(10, 9, 8), rank=3, seed=155, mask_keep=0.85),
+         dict(rank=3, n_iter_max=8, init="svd", tol=0, svd_mask_repeats=3), None),
+    ]
+    for name, fn, g, kw, np_seed in variants:
+        x = small_cp(g["seed"], g["shape"], g["rank"])
+        kwc = copy.deepcopy(kw)
+        if "mask_keep" in g:
+            kwc["mask"] = tl.tensor((np.random.RandomState(g["seed"] + 1000)
+                                     .rand(*g["shape"]) < g["mask_keep"]).astype(np.float64))
+        rank = kwc.pop("rank")
+        if np_seed is not None:
+            np.random.seed(np_seed)
+        if fn == "tucker":
+            tt, errs = tucker(tl.tensor(x), rank, return_errors=True, **kwc)
+            rec = {"core": np.array(tt.core), "factors": [np.array(f) for f in tt.factors]}
+        else:
+            cp, errs = parafac(tl.tensor(x), rank, return_errors=True, **kwc)
+            rec = {"weights": np.array(cp.weights), "factors": [np.array(f) for f in cp.factors]}
+        runs.append({"case": name, "fn": fn, "gen": {"fn": "small", **g}, "np_seed": np_seed,
+                     "checksum": [float(x.sum()), float(np.linalg.norm(x))], "kwargs": kw,
+                     "errors": [float(e) for e in errs], **rec})
+    return {"runs": runs, "kats": kats}
+
+
 def main():
     if not REF or not os.path.isdir(os.path.join(REF, "tensorly")):
         sys.exit("make_golden: set TENSORLY_REFERENCE to the TensorLy source tree "
@@ -799,6 +873,12 @@ def main():
         pickle.dump({"versions": _versions(), **extras}, f, protocol=4)
     if "tucker_extras" in sys.argv[1:]:
         print(f"{len(extras['runs'])} Tucker runs, {len(extras['kats'])} records")
+        return
+    svdx = record_svd_extras()
+    with open(os.path.join(HERE, "svd_extra_runs.pkl"), "wb") as f:
+        pickle.dump({"versions": _versions(), **svdx}, f, protocol=4)
+    if "svd_extras" in sys.argv[1:]:
+        print(f"{len(svdx['runs'])} runs, {len(svdx['kats'])} records")
         return
     kats = record_kats()
     with open(os.path.join(HERE, "tenalg_kats.pkl"), "wb") as f:

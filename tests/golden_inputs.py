@@ -45,3 +45,10 @@ def regenerate(run):
     cs = [float(np.asarray(x, np.float64).sum()), float(np.linalg.norm(np.asarray(x, np.float64)))]
     np.testing.assert_allclose(cs, run["checksum"], rtol=1e-12, atol=1e-12)
     return x
+
+
+def dense_mask(g):
+    """0/1 mask of a dense tensor, keeping each entry with probability
+    ``g["mask_keep"]`` (seeded by ``g["seed"] + 1000``)."""
+    return (np.random.RandomState(g["seed"] + 1000).rand(*g["shape"])
+            < g["mask_keep"]).astype(np.float64)

@@ -171,12 +171,63 @@ def test_masked_parafac_matches_reference(gb300, golden, case):
     assert torch.equal(xt, torch.as_tensor(x, device="cuda")), "the input tensor was modified"
 
 
+def test_parafac_sparse_component_matches_reference(gb300, golden):
+    """The sparse component (tensorly/decomposition/_cp.py:140-159, :202-215,
+    :532-538): every error is that of the residual minus its largest entries
+    (radix select on the device), and the final sparse component comes back
+    beside the model; f64 against the reference's run to 1e-10."""
+    run = golden["runs"]["cp_sparsity"]
+    (cp, sparse), errs = run_case(gb300, run)
+    w, f = cp
+    assert len(errs) == len(run["errors"])
+    np.testing.assert_allclose(errs, run["errors"], rtol=1e-10, atol=1e-13)
+    assert rel(host(w), run["weights"]) < 1e-10
+    for a, b in zip(f, run["factors"]):
+        assert rel(host(a), b) < 1e-10
+    s = host(sparse)
+    assert (s != 0).sum() == (run["sparse"] != 0).sum()
+    np.testing.assert_allclose(s, run["sparse"], rtol=1e-9, atol=1e-12)
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_sparse_residual_selects_like_sort(gb300, dtype):
+    """tlgb_sparse_residual against NumPy's sort on ties, a count above the
+    size and the negative counts sparsify_tensor's indexing allows."""
+    from tensorly_gb300 import _lib
+    from tensorly_gb300._tensor import dtype_code, workspace
+    rs = np.random.RandomState(9)
+    x = rs.randn(3000)
+    x[::7] = 0.5                    # ties at one magnitude
+    x[5::11] = -0.5
+    lm = rs.randn(3000) * 0.01
+    xt = torch.as_tensor(x, device="cuda", dtype=dtype)
+    lt = torch.as_tensor(lm, device="cuda", dtype=dtype)
+    r = (xt - lt).cpu().numpy().astype(np.float64)
+    lib = _lib.lib()
+    ws = workspace(int(lib.tlgb_sparse_residual_workspace_bytes()), xt.device)
+    out = torch.empty(1, dtype=torch.float64, device="cuda")
+    for k in (1, 17, 429, 1500, 2999, 3000, 3001):
+        sp = torch.empty_like(xt)
+        _lib.check(lib.tlgb_sparse_residual(dtype_code(xt), xt.data_ptr(), lt.data_ptr(), 3000, k,
+                                            out.data_ptr(), sp.data_ptr(), ws.data_ptr(),
+                                            ws.numel(), None))
+        torch.cuda.synchronize()
+        if k > 3000:
+            want = r
+        else:
+            bound = np.sort(np.abs(r))[-k]
+            want = np.where(np.abs(r) < bound, 0.0, r)
+        np.testing.assert_array_equal(host(sp).astype(np.float64), want)
+        ref = np.linalg.norm(r - want)
+        assert abs(out.item() - ref) <= 1e-12 * max(ref, 1.0)
+
+
 def test_unsupported_options_raise(gb300):
     x = torch.rand(4, 5, 6, device="cuda", dtype=torch.float64)
-    for kw in ({"sparsity": 0.1}, {"mask": torch.ones_like(x), "init": "svd"}):
-        with pytest.raises(NotImplementedError):
-            gb300.parafac(x, 2, **dict({"init": "random"}, **kw))
-    for kw in ({"linesearch": True}, {"orthogonalise": True}, {"mask": torch.ones_like(x)}):
+    with pytest.raises(NotImplementedError):
+        gb300.parafac(x, 2, init="random", sparsity=0.1, callback=lambda *a: None)
+    for kw in ({"linesearch": True}, {"orthogonalise": True}, {"mask": torch.ones_like(x)},
+               {"sparsity": 0.1}):
         with pytest.raises(NotImplementedError):
             gb300.parafac(x.float(), 2, init="random", precision="bf16", **kw)
     with pytest.raises(ValueError):

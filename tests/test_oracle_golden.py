@@ -334,3 +334,43 @@ def test_fixed_modes_error_matches_reference(golden):
         err = _tucker_fixed_modes_error(e["shape"], e["rank"], e["fixed"], e["init"])
         assert e["message"] is not None
         assert isinstance(err, ValueError) and str(err) == e["message"]
+
+
+def test_oracle_svd_kats_match_reference(golden):
+    """svd_interface with a mask and with 'randomized_svd', and
+    randomized_svd itself, against the reference on the recorded inputs."""
+    for k in golden["svd_kats"]:
+        if k["op"] == "svd_interface":
+            U, S, V = oracle.svd_interface(k["matrix"], mask=k["mask"],
+                                           n_iter_mask_imputation=k["n_iter_mask_imputation"],
+                                           **k["kwargs"])
+        else:
+            U, S, V = oracle.randomized_svd(k["matrix"], random_state=k["random_state"],
+                                            **k["kwargs"])
+        np.testing.assert_allclose(S, k["S"], rtol=1e-11)
+        np.testing.assert_allclose(U, k["U"], rtol=1e-9, atol=1e-10)
+        np.testing.assert_allclose(V, k["V"], rtol=1e-9, atol=1e-10)
+
+
+@pytest.mark.parametrize("case", ["tucker_mask_svd", "tucker_mask_random", "tucker_randomized",
+                                  "cp_randomized", "cp_mask_svd"])
+def test_oracle_svd_callers_match_reference(golden, case):
+    from golden_inputs import dense_mask
+    run = golden["runs"][case]
+    x = regenerate(run)
+    kw = dict(run["kwargs"])
+    rank = kw.pop("rank")
+    if "mask_keep" in run["gen"]:
+        kw["mask"] = dense_mask(run["gen"])
+    if run["np_seed"] is not None:
+        np.random.seed(run["np_seed"])
+    if run["fn"] == "tucker":
+        (core, factors), errs = oracle.tucker(x, rank, return_errors=True, **kw)
+        np.testing.assert_allclose(core, run["core"], rtol=1e-9,
+                                   atol=1e-9 * np.abs(run["core"]).max())
+    else:
+        (w, factors), errs = oracle.parafac(x, rank, return_errors=True, **kw)
+        np.testing.assert_allclose(w, run["weights"], rtol=1e-9)
+    np.testing.assert_allclose(errs, run["errors"], rtol=1e-10, atol=1e-13)
+    for a, b in zip(factors, run["factors"]):
+        np.testing.assert_allclose(a, b, rtol=1e-9, atol=1e-9 * np.abs(b).max())

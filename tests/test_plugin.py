@@ -85,7 +85,63 @@ def test_register_is_idempotent_and_unregister_restores_core():
 
 
 def test_register_with_real_tensorly_if_installed():
-    tl = pytest.importorskip("tensorly")
+    tl = _real_tensorly()
     from tensorly_gb300 import plugin
     cls = plugin.register(tl.tenalg, activate=False)
     assert tl.tenalg.TenalgBackend._available_tenalg_backends["gb300"] is cls
+
+
+def _real_tensorly():
+    """TensorLy itself, from an installed package or from the source tree
+    named by TENSORLY_REFERENCE; skips when neither is there."""
+    import os
+    import sys
+    ref = os.environ.get("TENSORLY_REFERENCE")
+    if ref and os.path.isdir(os.path.join(ref, "tensorly")) and ref not in sys.path:
+        sys.path.insert(0, ref)
+    return pytest.importorskip("tensorly")
+
+
+def test_real_tensorly_decompositions_dispatch_to_gb300():
+    """With the real registry, tensorly.decomposition.parafac and tucker
+    resolve their tenalg calls to the "gb300" backend.  Without a GPU the
+    backend's hot-path entries are replaced by recording wrappers around the
+    core functions, so what is checked is the dispatch, and that the
+    decompositions still give the core backend's results through it."""
+    tl = _real_tensorly()
+    import numpy as np
+    from tensorly.decomposition import parafac, tucker
+    from tensorly_gb300 import plugin
+    tl.set_backend("numpy")
+    cls = plugin.register(tl.tenalg, activate=False)
+    core = tl.tenalg.TenalgBackendManager.load_backend("core")
+    calls = {}
+    saved = {name: getattr(cls, name) for name in plugin.HOT_PATH}
+
+    def recorder(name):
+        fn = getattr(core, name)
+
+        def wrapped(*args, **kwargs):
+            calls[name] = calls.get(name, 0) + 1
+            return fn(*args, **kwargs)
+        return wrapped
+
+    try:
+        for name in plugin.HOT_PATH:
+            cls.register_method(name, recorder(name))
+        x = np.random.RandomState(0).rand(6, 5, 4)
+        ref_cp = parafac(x, 3, n_iter_max=4, init="random", random_state=1, tol=0)
+        ref_tk = tucker(x, [2, 2, 2], n_iter_max=3, init="random", random_state=1, tol=0)
+        assert not calls
+        tl.tenalg.set_backend("gb300")
+        cp = parafac(x, 3, n_iter_max=4, init="random", random_state=1, tol=0)
+        assert calls.get("unfolding_dot_khatri_rao", 0) == 4 * 3
+        tk = tucker(x, [2, 2, 2], n_iter_max=3, init="random", random_state=1, tol=0)
+        assert calls.get("multi_mode_dot", 0) > 0
+        for a, b in zip(cp.factors, ref_cp.factors):
+            np.testing.assert_array_equal(a, b)
+        np.testing.assert_array_equal(tk.core, ref_tk.core)
+    finally:
+        for name, fn in saved.items():
+            cls.register_method(name, fn)
+        plugin.unregister(tl.tenalg)
