@@ -60,6 +60,8 @@ def parse():
     p.add_argument("--train-samples", type=int, default=200_000,
                    help="learned: tensors the network is trained on (before the timed steps)")
     p.add_argument("--count", type=int, default=4096, help="batched: number of tensors")
+    p.add_argument("--no-tune", action="store_true",
+                   help="dense: keep the library's tensor-core MTTKRP tile defaults")
     p.add_argument("--no-extras", action="store_true",
                    help="dense: headline line only (no plain-f32, batched and 128^4 sub-objects)")
     p.add_argument("--profile", action="store_true",
@@ -269,6 +271,11 @@ def run_gpu(args):
 
     kw = dict(n_iter_max=args.sweeps, tol=0, precision=args.precision,
               refine_sweeps=args.refine, check_every=args.sweeps, return_errors=True)
+    tiles = None
+    if args.precision == "bf16" and not args.no_tune:
+        # tensor-core MTTKRP tile choices for this tensor (outside the timed region)
+        from tensorly_gb300 import autotune
+        tiles = autotune.tune_dense(x, args.rank)
 
     def step(times=None):
         return tg.parafac(x, args.rank, init=tg.CPTensor((None, init)), mttkrp_times=times, **kw)
@@ -411,7 +418,8 @@ def run_gpu(args):
                    "precision": args.precision,
                    "refine_sweeps": args.refine if args.precision == "bf16" else 0,
                    "parallelism": "replicas" if ws > 1 else "single GPU",
-                   "l2": "input 512 MiB > L2, no flush"},
+                   "l2": "input 512 MiB > L2, no flush",
+                   "mttkrp_tiles_autotuned": tiles},
         "accuracy_vs_f64": acc,
         "fp32": fp32,
         "bf16_over_fp32": fp32["bf16_over_fp32"] if fp32 else None,

@@ -1,4 +1,14 @@
-"""Autotuner for the batched CP-ALS kernel variants.
+"""Autotuners for the CP-ALS kernels.
+
+Dense tensor-core MTTKRP (``tune_dense``): the tile shape along the
+contracted modes (the inner-mode group whose slice of the split factor stays
+resident in shared memory, ``tc_group_kib``), the depth of the tensor-tile
+ring (``tc_stages``) and the grid (``tc_waves`` waves of one CTA per SM) are
+searched coordinate by coordinate on the caller's own tensor: each candidate
+runs a few bf16 sweeps of ``parafac`` (CUDA events), the fastest is kept and
+set with ``tlgb_set_tuning``.
+
+Batched CP-ALS kernel variants (``tune_batched``):
 
 ``tlgb_cp_als_batched`` sorts the tensors of a batch into three size classes
 (by the shared-memory footprint of the padded tensor) and runs each class with
@@ -66,3 +76,78 @@ def reset_batched():
     """Back to the library defaults (128 / 256 / 512)."""
     for cls in CLASSES:
         _set(cls, 0)
+
+
+DENSE_SPACE = (
+    ("tc_group_kib", (32, 48, 64, 96)),
+    ("tc_stages", (0, 5, 7, 9)),      # 0: as deep as shared memory allows
+    ("tc_waves", (1, 2)),
+)
+DENSE_DEFAULT = {"tc_group_kib": 64, "tc_stages": 0, "tc_waves": 1}
+_dense_cache = {}
+
+
+def _set_key(key, value):
+    _lib.check(_lib.lib().tlgb_set_tuning(key.encode(), int(value)))
+
+
+def _time_dense(x, rank, init, sweeps, reps):
+    from .cp_tensor import CPTensor
+    from .decomposition import parafac
+
+    def run():
+        parafac(x, rank, init=CPTensor((None, [f.clone() for f in init])), n_iter_max=sweeps,
+                tol=0, precision="bf16", refine_sweeps=0)
+    run()
+    st = torch.cuda.current_stream()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(st)
+    for _ in range(reps):
+        run()
+    b.record(st)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def tune_dense(x, rank, sweeps=8, reps=2, verbose=False):
+    """Pick the tensor-core MTTKRP's inner-mode group size, ring depth and
+    wave count for bf16 CP-ALS of the f32 CUDA tensor ``x`` at ``rank`` by a
+    coordinate search over ``DENSE_SPACE`` (the defaults first); returns
+    {key: value} and leaves it set.  Cached per device, shape and rank."""
+    key = (torch.cuda.get_device_name(x.device), tuple(x.shape), int(rank))
+    if key in _dense_cache:
+        for k, v in _dense_cache[key].items():
+            _set_key(k, v)
+        return dict(_dense_cache[key])
+    gen = torch.Generator(device="cpu").manual_seed(0)
+    init = [torch.rand((int(s), int(rank)), generator=gen).to(x.device, torch.float32)
+            for s in x.shape]
+    choice = dict(DENSE_DEFAULT)
+    for k, v in choice.items():
+        _set_key(k, v)
+    best_ms = _time_dense(x, rank, init, sweeps, reps)
+    if verbose:
+        print(f"dense defaults {choice}: {best_ms:.3f} ms")
+    for k, values in DENSE_SPACE:
+        for v in values:
+            if v == choice[k]:
+                continue
+            _set_key(k, v)
+            try:
+                ms = _time_dense(x, rank, init, sweeps, reps)
+            except NotImplementedError:     # the plan does not fit with this value
+                ms = float("inf")
+            if verbose:
+                print(f"dense {k}={v}: {ms:.3f} ms")
+            if ms < best_ms:
+                best_ms, choice[k] = ms, v
+        _set_key(k, choice[k])
+    _dense_cache[key] = dict(choice)
+    return choice
+
+
+def reset_dense():
+    """Back to the library's tensor-core MTTKRP defaults."""
+    for k in DENSE_DEFAULT:
+        _set_key(k, 0)

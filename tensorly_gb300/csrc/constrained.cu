@@ -21,6 +21,7 @@
 
 #include "als_kernels.cuh"
 #include "mttkrp_simt.cuh"
+#include "mttkrp_tc.cuh"
 #include "prox_columns.cuh"
 
 namespace tlgb {
@@ -270,6 +271,7 @@ __global__ void k_prox_apply(const T* __restrict__ X, int64_t n, int kind, doubl
 struct ConsLayout {
   size_t ctrl, cs, G, V2, fac, perm, vmat, w32, gpart, partial, M, B, S, dual, part, bytes;
   size_t P, pscratch;   // column-wise operators: their output and scratch
+  size_t tcs;           // f32 tensors: the split tensor-core MTTKRP's buffers
 };
 
 template <typename T>
@@ -306,6 +308,14 @@ int cons_layout(const Shape& sh, int64_t R, std::vector<MttkrpPlan>* plans, Cons
   L->P = take(sizeof(T) * (size_t)imax * R);
   L->pscratch = take(std::max(prox_matrix_scratch_bytes(dtype, imax, R, TLGB_CONS_UNIMODALITY),
                               prox_matrix_scratch_bytes(dtype, imax, R, TLGB_CONS_HARD_SPARSITY)));
+  size_t tcs_bytes = 0;
+  if (dtype == TLGB_F32) {
+    SplitMttkrp stc;
+    int rc = split_mttkrp_plan(sh, R, &stc);
+    if (rc) return rc;
+    tcs_bytes = split_mttkrp_bytes(stc);
+  }
+  L->tcs = take(tcs_bytes);
   L->bytes = align_up(off, 256);
   return TLGB_OK;
 }
@@ -376,6 +386,9 @@ int cons_run(const T* X, const Shape& sh, T* const* factors, int64_t R, const in
   // ||X||^2 (f64, fixed order)
   rc = als_launch_sumsq(TypeCode<T>::value, X, sh.numel, part, kConsBlocks, ctrl, st);
   if (rc) return rc;
+  LoopMttkrp<T> mk;
+  rc = mk.setup(X, sh, R, factors, &plans, partial, base + L.tcs, &ctrl->tc_err, st);
+  if (rc) return rc;
   const T* cf[kMaxModes];
   for (int k = 0; k < N; ++k) cf[k] = factors[k];
   const int last = free_modes[n_free - 1];
@@ -394,9 +407,9 @@ int cons_run(const T* X, const Shape& sh, T* const* factors, int64_t R, const in
       rc = als_launch_factorize<T>(V2, 2, 0, (int)R, nullptr, 0.0, fac, perm, vmat, w32, ctrl,
                                    st);
       if (rc) return rc;
-      rc = mttkrp_launch_partials<T>(plans[mode], X, cf, nullptr, partial, done, st);
+      rc = mk.launch(mode, cf, nullptr, done, st);
       if (rc) return rc;
-      rc = mttkrp_launch_reduce<T, T>(plans[mode], partial, M, st);
+      rc = mttkrp_launch_reduce_n<T, T>(mk.partial(), mk.splits(mode), I * R, M, st);
       if (rc) return rc;
       const int kind = kinds[mode];
       const bool glob = kind == kConsNonNeg || kind == kConsL2 || kind == kConsNormalize;
@@ -433,6 +446,8 @@ int cons_run(const T* X, const Shape& sh, T* const* factors, int64_t R, const in
       }
       k_cons_cerr<<<1, 32, 0, st>>>(cs);
       TLGB_LAUNCH_CHECK();
+      rc = mk.refresh(mode, factors[mode], st);
+      if (rc) return rc;
       rc = als_launch_gram<T>(factors[mode], I, (int)R, gpart, nparts, G + (size_t)mode * RR,
                               done, st);
       if (rc) return rc;
@@ -452,6 +467,8 @@ int cons_run(const T* X, const Shape& sh, T* const* factors, int64_t R, const in
     TLGB_CUDA_TRY(cudaStreamSynchronize(st));
     if (hc.status == TLGB_ESINGULAR)
       return set_error(TLGB_ESINGULAR, "constrained_parafac: normal equations singular");
+    if (hc.tc_err != 0)
+      return set_error(TLGB_ETIMEOUT, "constrained_parafac: a tensor-core MTTKRP wait timed out");
     // error (tensorly/decomposition/_constrained_cp.py:391-396), weights one
     double fn2 = 0.0;
     for (int e = 0; e < RR; ++e) {

@@ -412,6 +412,19 @@ int mttkrp_launch_reduce(const MttkrpPlan& p, const T* partial, TO* out, cudaStr
   return TLGB_OK;
 }
 
+template <typename T, typename TO>
+int mttkrp_launch_reduce_n(const T* partial, int splits, int64_t n, TO* out, cudaStream_t stream) {
+  const int threads = 256;
+  const int blocks = (int)std::max<int64_t>(
+      1, std::min<int64_t>(ceil_div(n, (int64_t)threads), (int64_t)sm_count() * 8));
+  mttkrp_reduce_kernel<T, TO><<<blocks, threads, 0, stream>>>(partial, splits, n, out);
+  TLGB_LAUNCH_CHECK();
+  return TLGB_OK;
+}
+template int mttkrp_launch_reduce_n<float, float>(const float*, int, int64_t, float*, cudaStream_t);
+template int mttkrp_launch_reduce_n<double, double>(const double*, int, int64_t, double*,
+                                                    cudaStream_t);
+
 template int mttkrp_launch_partials<float>(const MttkrpPlan&, const float*, const float* const*,
                                            const float*, float*, const int*, cudaStream_t);
 template int mttkrp_launch_partials<double>(const MttkrpPlan&, const double*,

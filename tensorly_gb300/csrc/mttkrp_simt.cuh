@@ -57,6 +57,10 @@ struct MttkrpPlan {
 int mttkrp_prepare(int dtype);
 
 // Builds the geometry and the split count for one mode (no launch).
+// out = sum over `splits` partial tiles of n entries each (partial[split][n]).
+template <typename T, typename TO>
+int mttkrp_launch_reduce_n(const T* partial, int splits, int64_t n, TO* out, cudaStream_t stream);
+
 int mttkrp_make_plan(int dtype, const Shape& sh, int64_t rank, int mode, MttkrpPlan* plan);
 
 // Enqueues the split kernel (writes `partial`, which must hold plan.partial_bytes).

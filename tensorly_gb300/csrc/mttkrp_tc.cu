@@ -925,6 +925,80 @@ int tc_launch_factor_bf16t(const float* A, int64_t rows, int64_t R, int planes,
   return TLGB_OK;
 }
 
+int split_mttkrp_plan(const Shape& sh, int64_t R, SplitMttkrp* s) {
+  *s = SplitMttkrp{};
+  s->sh = sh;
+  s->R = R;
+  if (tc_tuning().split_simt || R > 64) return TLGB_OK;
+  for (int k = 0; k < sh.ndim; ++k)
+    for (int j = 0; j < 3; ++j) {
+      int rc = mttkrp_tc_make_plan(sh, R, k, 3 - j, 0, &s->plan[k][j]);
+      if (rc) return rc;
+      if (!s->plan[k][j].valid) return TLGB_OK;
+    }
+  s->valid = true;
+  return TLGB_OK;
+}
+
+size_t split_mttkrp_bytes(const SplitMttkrp& s) {
+  if (!s.valid) return 0;
+  size_t b = 3 * align_up(sizeof(__nv_bfloat16) * (size_t)s.sh.numel, 256);
+  size_t pmax = 0;
+  for (int k = 0; k < s.sh.ndim; ++k) {
+    b += align_up(sizeof(__nv_bfloat16) * 3 * (size_t)s.R * s.sh.dim[k], 256);
+    pmax = std::max(pmax, s.plan[k][0].partial_bytes + s.plan[k][1].partial_bytes +
+                              s.plan[k][2].partial_bytes);
+  }
+  return b + align_up(pmax, 256);
+}
+
+int split_mttkrp_setup(SplitMttkrp* s, const float* X, const float* const* factors, void* base,
+                       int* err, cudaStream_t st) {
+  if (!s->valid) return set_error(TLGB_EINVAL, "split_mttkrp: no valid plan");
+  TLGB_CHECK_ARG((reinterpret_cast<uintptr_t>(base) & 255) == 0, "split_mttkrp: misaligned base");
+  int rc = mttkrp_tc_prepare();
+  if (rc) return rc;
+  char* p = static_cast<char*>(base);
+  for (int j = 0; j < 3; ++j) {
+    s->xp[j] = reinterpret_cast<__nv_bfloat16*>(p);
+    p += align_up(sizeof(__nv_bfloat16) * (size_t)s->sh.numel, 256);
+  }
+  for (int k = 0; k < s->sh.ndim; ++k) {
+    s->fbt[k] = reinterpret_cast<__nv_bfloat16*>(p);
+    p += align_up(sizeof(__nv_bfloat16) * 3 * (size_t)s->R * s->sh.dim[k], 256);
+  }
+  s->partial = reinterpret_cast<float*>(p);
+  s->err = err;
+  rc = tc_launch_split3(X, s->sh.numel, s->xp[0], s->xp[1], s->xp[2], st);
+  if (rc) return rc;
+  for (int k = 0; k < s->sh.ndim; ++k) {
+    rc = split_mttkrp_refresh(*s, k, factors[k], st);
+    if (rc) return rc;
+    for (int j = 0; j < 3; ++j) {
+      rc = mttkrp_tc_encode(s->plan[k][j], s->xp[j], s->fbt, 3, &s->maps[k][j]);
+      if (rc) return rc;
+    }
+  }
+  return TLGB_OK;
+}
+
+int split_mttkrp_refresh(const SplitMttkrp& s, int mode, const float* A, cudaStream_t st) {
+  return tc_launch_factor_bf16t(A, s.sh.dim[mode], s.R, 3, s.fbt[mode], st);
+}
+
+int split_mttkrp_launch(const SplitMttkrp& s, int mode, const float* const* factors,
+                        const float* weights, const int* skip, cudaStream_t st) {
+  int splits = 0;
+  for (int j = 0; j < 3; ++j) {
+    const TcPlan& tp = s.plan[mode][j];
+    int rc = mttkrp_tc_launch_maps(tp, s.maps[mode][j], factors, weights,
+                                   s.partial + (size_t)splits * tp.I_out * tp.R, skip, s.err, st);
+    if (rc) return rc;
+    splits += tp.splits;
+  }
+  return TLGB_OK;
+}
+
 }  // namespace tlgb
 
 // ---------------------------------------------------------------------------
@@ -1010,6 +1084,7 @@ extern "C" int tlgb_set_tuning(const char* key, int value) {
   else if (k == "f64_factorize") tc_tuning().f64_factorize = value;
   else if (k == "no_pdl") tc_tuning().no_pdl = value;
   else if (k == "tc_test_starve") tc_tuning().test_starve = value;
+  else if (k == "split_simt") tc_tuning().split_simt = value;
   else return batched_set_tuning(k, value);   // the batched CP-ALS variants
   return TLGB_OK;
 }

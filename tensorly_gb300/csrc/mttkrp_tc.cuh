@@ -1,7 +1,9 @@
 // BF16 tensor-core MTTKRP (tcgen05 + TMA, sm_103a).
 #pragma once
 #include <cuda.h>
+#include <vector>
 #include "common.cuh"
+#include "mttkrp_simt.cuh"
 
 namespace tlgb {
 
@@ -42,6 +44,7 @@ struct TcTuning {
   int f64_factorize = 0;      // 1: every CP-ALS factorisation takes the f64 Cholesky / LU path
   int no_pdl = 0;             // 1: CP-ALS sweep kernels launch without programmatic dependence
   int test_starve = 0;        // 1: tensor-core MTTKRP issues no copies (timeout-path test)
+  int split_simt = 0;         // 1: non-negative / constrained CP keep the SIMT f32 MTTKRP
 };
 TcTuning& tc_tuning();
 
@@ -85,5 +88,85 @@ int tc_launch_split3(const float* X, int64_t n, __nv_bfloat16* x0, __nv_bfloat16
 // plane 0 = bf16(A^T), plane k = bf16(A^T - planes before k).
 int tc_launch_factor_bf16t(const float* A, int64_t rows, int64_t R, int planes,
                            __nv_bfloat16* out, cudaStream_t st);
+
+// f32-faithful MTTKRP of an f32 tensor on the tensor cores, for loops that
+// update factors with their own kernels (non-negative and constrained CP):
+// the exact split X = x0 + x1 + x2 and A_k = f0 + f1 + f2 into bf16 planes,
+// and per mode three launches x0.(f0+f1+f2) + x1.(f0+f1) + x2.f0 (the
+// dropped terms are below 2^-26 of |x||f|), each writing its own run of
+// partial tiles, so the result is partial[split][I][R] in the layout of the
+// SIMT MTTKRP with splits(mode) tiles.  The tensor cores' f32 accumulation
+// rounds toward zero (about -2e-7 of |M|).
+struct SplitMttkrp {
+  bool valid = false;
+  Shape sh{};
+  int64_t R = 0;
+  TcPlan plan[kMaxModes][3];
+  TcMaps maps[kMaxModes][3];
+  __nv_bfloat16* xp[3] = {nullptr, nullptr, nullptr};
+  __nv_bfloat16* fbt[kMaxModes] = {};
+  float* partial = nullptr;
+  int* err = nullptr;     // device int: TLGB_ETIMEOUT if a bounded wait expired
+  int splits(int mode) const {
+    return plan[mode][0].splits + plan[mode][1].splits + plan[mode][2].splits;
+  }
+};
+// Plans every mode; s->valid stays false when a plan does not fit (shape,
+// rank > 64) or the split_simt knob is set: the caller keeps the SIMT kernel.
+int split_mttkrp_plan(const Shape& sh, int64_t R, SplitMttkrp* s);
+// Workspace of the planes, the factor planes and the partial tiles (0 if !valid).
+size_t split_mttkrp_bytes(const SplitMttkrp& s);
+// Carves `base` (split_mttkrp_bytes, 256-byte aligned), splits X and every
+// factor into planes and encodes the tensor maps.
+int split_mttkrp_setup(SplitMttkrp* s, const float* X, const float* const* factors, void* base,
+                       int* err, cudaStream_t st);
+// The planes of factor `mode` after the caller rewrote it.
+int split_mttkrp_refresh(const SplitMttkrp& s, int mode, const float* A, cudaStream_t st);
+// partial[splits(mode)][I_mode][R]; skip: the loop's device stop flag.
+int split_mttkrp_launch(const SplitMttkrp& s, int mode, const float* const* factors,
+                        const float* weights, const int* skip, cudaStream_t st);
+
+// The MTTKRP of a loop that updates its factors itself (non-negative and
+// constrained CP): the f32-faithful tensor-core split (SplitMttkrp) for an
+// f32 tensor whose plans fit, else the SIMT kernel; partial() and splits()
+// name the partial tiles either way.  refresh() after a factor changes.
+template <typename T>
+struct LoopMttkrp {
+  SplitMttkrp stc;
+  bool tc = false;
+  const T* X;
+  const std::vector<MttkrpPlan>* plans;
+  T* simt_partial;
+
+  int setup(const T* X_, const Shape& sh, int64_t R, T* const* factors,
+            const std::vector<MttkrpPlan>* plans_, T* simt_partial_, char* tcs_base, int* err,
+            cudaStream_t st) {
+    X = X_;
+    plans = plans_;
+    simt_partial = simt_partial_;
+    if constexpr (sizeof(T) == 4) {
+      int rc = split_mttkrp_plan(sh, R, &stc);
+      if (rc) return rc;
+      if (stc.valid) {
+        rc = split_mttkrp_setup(&stc, reinterpret_cast<const float*>(X), 
+                                reinterpret_cast<const float* const*>(factors), tcs_base, err, st);
+        if (rc) return rc;
+        tc = true;
+      }
+    }
+    return TLGB_OK;
+  }
+  int launch(int mode, const T* const* cf, const T* w, const int* done, cudaStream_t st) {
+    if (tc)
+      return split_mttkrp_launch(stc, mode, reinterpret_cast<const float* const*>(cf),
+                                 reinterpret_cast<const float*>(w), done, st);
+    return mttkrp_launch_partials<T>((*plans)[mode], X, cf, w, simt_partial, done, st);
+  }
+  const T* partial() const { return tc ? reinterpret_cast<const T*>(stc.partial) : simt_partial; }
+  int splits(int mode) const { return tc ? stc.splits(mode) : (*plans)[mode].splits; }
+  int refresh(int mode, const T* A, cudaStream_t st) {
+    return tc ? split_mttkrp_refresh(stc, mode, reinterpret_cast<const float*>(A), st) : TLGB_OK;
+  }
+};
 
 }  // namespace tlgb

@@ -20,6 +20,7 @@
 
 #include "als_kernels.cuh"
 #include "mttkrp_simt.cuh"
+#include "mttkrp_tc.cuh"
 
 namespace tlgb {
 namespace {
@@ -485,6 +486,7 @@ struct MuLayout {
   size_t M, hpart, hstate, Pt, save;   // HALS: summed MTTKRP, stop partials, e0 + stop +
                                        // rerun, typed P, rows at the start of a chunk
   size_t fac, perm, vmat, w32;         // HALS modes outside nn_modes: the CP-ALS solve
+  size_t tcs;                          // f32 tensors: the split tensor-core MTTKRP's buffers
 };
 
 int64_t mu_rows_per_block(int64_t I, int R, int nparts);
@@ -528,6 +530,14 @@ int mu_layout(const Shape& sh, int64_t R, int n_iter_max, std::vector<MttkrpPlan
   L->perm = take(sizeof(int) * R);
   L->vmat = take(sizeof(double) * RR);
   L->w32 = take(sizeof(float) * 3 * RR);
+  size_t tcs_bytes = 0;
+  if (dtype == TLGB_F32) {
+    SplitMttkrp stc;
+    int rc = split_mttkrp_plan(sh, R, &stc);
+    if (rc) return rc;
+    tcs_bytes = split_mttkrp_bytes(stc);
+  }
+  L->tcs = take(tcs_bytes);
   L->bytes = align_up(off, 256);
   return TLGB_OK;
 }
@@ -573,6 +583,9 @@ int mu_run(const T* X, const Shape& sh, T* const* factors, int64_t R, const int*
                             done, st);
     if (rc) return rc;
   }
+  LoopMttkrp<T> mk;
+  rc = mk.setup(X, sh, R, factors, &plans, partial, base + L.tcs, &ctrl->tc_err, st);
+  if (rc) return rc;
   const T* cf[kMaxModes];
   for (int k = 0; k < N; ++k) cf[k] = factors[k];
   const int last = free_modes[n_free - 1];
@@ -584,15 +597,17 @@ int mu_run(const T* X, const Shape& sh, T* const* factors, int64_t R, const int*
       const int mode = free_modes[q];
       k_mu_accum<<<(RR + 255) / 256, 256, 0, st>>>(G, N, mode, (int)R, V, done);
       TLGB_LAUNCH_CHECK();
-      rc = mttkrp_launch_partials<T>(plans[mode], X, cf, nullptr, partial, done, st);
+      rc = mk.launch(mode, cf, nullptr, done, st);
       if (rc) return rc;
       const int64_t I = sh.dim[mode];
       const int64_t rpb = mu_rows_per_block(I, (int)R, nparts);
       const int nb = (int)ceil_div(I, rpb);
       k_mu_update<T><<<nb, kMuThreads, (size_t)rpb * R * sizeof(double), st>>>(
-          partial, plans[mode].splits, I, (int)R, V, eps, factors[mode],
+          mk.partial(), mk.splits(mode), I, (int)R, V, eps, factors[mode],
           mode == last ? ipart : nullptr, done, rpb);
       TLGB_LAUNCH_CHECK();
+      rc = mk.refresh(mode, factors[mode], st);
+      if (rc) return rc;
       if (mode == last) last_nb = nb;
       rc = als_launch_gram<T>(factors[mode], I, (int)R, gpart, nparts, G + (size_t)mode * RR,
                               done, st);
@@ -611,6 +626,8 @@ int mu_run(const T* X, const Shape& sh, T* const* factors, int64_t R, const int*
   }
   TLGB_CUDA_TRY(cudaMemcpyAsync(&hc, ctrl, sizeof(AlsCtrl), cudaMemcpyDeviceToHost, st));
   TLGB_CUDA_TRY(cudaStreamSynchronize(st));
+  if (hc.tc_err != 0)
+    return set_error(TLGB_ETIMEOUT, "cp_nn_mu: a tensor-core MTTKRP wait timed out");
   const int ne = (tol > 0.0) ? std::min(hc.iter, n_iter_max) : 0;
   if (n_errors) *n_errors = ne;
   if (errors && ne > 0)
@@ -730,15 +747,20 @@ int hals_run(const T* X, const Shape& sh, T* const* factors, T* weights, int64_t
                             done, st);
     if (rc) return rc;
   }
+  LoopMttkrp<T> mk;
+  rc = mk.setup(X, sh, R, factors, &plans, partial, base + L.tcs, &ctrl->tc_err, st);
+  if (rc) return rc;
   const T* cf[kMaxModes];
   for (int k = 0; k < N; ++k) cf[k] = factors[k];
   const int last = free_modes[n_free - 1];
-  // cp_normalize of the model, then the Grams of every (rescaled) factor
+  // cp_normalize of the model, then the Grams (and planes) of every rescaled factor
   auto normalize_all = [&]() -> int {
     int r2 = als_launch_normalize<T>(factors, sh.dim, N, (int)R, weights, done, st);
-    for (int k = 0; k < N && !r2; ++k)
+    for (int k = 0; k < N && !r2; ++k) {
       r2 = als_launch_gram<T>(factors[k], sh.dim[k], (int)R, gpart, nparts, G + (size_t)k * RR,
                               done, st);
+      if (!r2) r2 = mk.refresh(k, factors[k], st);
+    }
     return r2;
   };
   AlsCtrl hc{};
@@ -763,10 +785,10 @@ int hals_run(const T* X, const Shape& sh, T* const* factors, T* weights, int64_t
                                      ctrl, st);
         if (rc) return rc;
       }
-      rc = mttkrp_launch_partials<T>(plans[mode], X, cf, weights, partial, done, st);
+      rc = mk.launch(mode, cf, weights, done, st);
       if (rc) return rc;
       k_sum_splits_to<T><<<(unsigned)std::min<int64_t>(ceil_div(IR, 256), 4096), 256, 0, st>>>(
-          partial, plans[mode].splits, IR, M);
+          mk.partial(), mk.splits(mode), IR, M);
       TLGB_LAUNCH_CHECK();
       if (nn) {
         // no sparsity coefficient (NaN): subtract 0, which leaves num unchanged
@@ -775,10 +797,12 @@ int hals_run(const T* X, const Shape& sh, T* const* factors, T* weights, int64_t
                            e0, chunk, hals_smem, p_in_smem, done, st);
       } else {
         int nb = 0;
-        rc = als_launch_solve<T>(partial, plans[mode].splits, I, (int)R, fac, perm, vmat, w32,
+        rc = als_launch_solve<T>(mk.partial(), mk.splits(mode), I, (int)R, fac, perm, vmat, w32,
                                  factors[mode], nullptr, gpart, nullptr, ctrl, kIrMaxPasses, &nb,
                                  st);
       }
+      if (rc) return rc;
+      rc = mk.refresh(mode, factors[mode], st);
       if (rc) return rc;
       if (mode == last) {
         k_inner_part<T><<<kInnerBlocks, 256, 0, st>>>(M, factors[mode], IR, ipart, done);
@@ -809,6 +833,8 @@ int hals_run(const T* X, const Shape& sh, T* const* factors, T* weights, int64_t
   }
   TLGB_CUDA_TRY(cudaMemcpyAsync(&hc, ctrl, sizeof(AlsCtrl), cudaMemcpyDeviceToHost, st));
   TLGB_CUDA_TRY(cudaStreamSynchronize(st));
+  if (hc.tc_err != 0)
+    return set_error(TLGB_ETIMEOUT, "cp_nn_hals: a tensor-core MTTKRP wait timed out");
   const int ne = (tol > 0.0) ? std::min(hc.iter, n_iter_max) : 0;
   if (n_errors) *n_errors = ne;
   if (errors && ne > 0)

@@ -193,3 +193,31 @@ def test_parafac_reports_mttkrp_times(gb300):
     gb300.parafac(x, 8, init=gb300.CPTensor((None, init)), n_iter_max=2, tol=0,
                   mttkrp_times=native, use_graph=False)
     assert set(native) == {"native"} and all(v > 0 for v in native["native"])
+
+
+def test_dense_autotuner_picks_valid_tiles_and_keeps_results(gb300):
+    """autotune.tune_dense searches the inner-mode group, ring depth and wave
+    count on the caller's tensor; every choice is one of the searched values,
+    it is cached, and bf16 parafac under it reaches the same fit as under the
+    defaults (1e-5 relative: only the summation order of the split-K partial
+    tiles changes)."""
+    from tensorly_gb300 import autotune
+    rs = np.random.RandomState(4)
+    fs = [rs.rand(s, 16) for s in (96, 80, 72)]
+    x = torch.as_tensor(np.einsum("ir,jr,kr->ijk", *fs), dtype=torch.float32, device="cuda")
+    init = [torch.as_tensor(rs.rand(s, 16), dtype=torch.float32, device="cuda")
+            for s in x.shape]
+    kw = dict(n_iter_max=12, tol=0, precision="bf16", refine_sweeps=2, return_errors=True)
+    try:
+        autotune.reset_dense()
+        _, e0 = gb300.parafac(x, 16, init=gb300.CPTensor((None, [f.clone() for f in init])), **kw)
+        choice = autotune.tune_dense(x, 16, sweeps=3, reps=1)
+        space = dict(autotune.DENSE_SPACE)
+        assert set(choice) == set(space)
+        for k, v in choice.items():
+            assert v in space[k]
+        assert autotune.tune_dense(x, 16) == choice          # cached
+        _, e1 = gb300.parafac(x, 16, init=gb300.CPTensor((None, [f.clone() for f in init])), **kw)
+        np.testing.assert_allclose(e1, e0, rtol=1e-5, atol=1e-7)
+    finally:
+        autotune.reset_dense()

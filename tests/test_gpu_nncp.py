@@ -164,3 +164,63 @@ def test_hals_wide_ranks_match_oracle(gb300, dtype, rank):
     for a, b in zip(fg, fo):
         tol = 1e-2 if f32 else 1e-8
         np.testing.assert_allclose(host(a), b, rtol=tol, atol=tol * np.abs(b).max())
+
+
+@pytest.mark.parametrize("algo", ["mu", "hals", "admm"])
+def test_f32_split_tensor_core_mttkrp_in_nn_loops(gb300, algo):
+    """f32 tensors whose modes suit the tensor-core plans run the MTTKRP of
+    the multiplicative-update, HALS and AO-ADMM loops as the exact
+    three-plane bf16 split on the tensor cores.  Against the same loops on
+    the SIMT f32 MTTKRP (split_simt knob): the error lists to 1e-4 and the
+    factors to 1e-3 (the tensor cores' f32 accumulation rounds toward zero,
+    about -2e-7 of |M|), and both against the f64 oracle to 1e-3; the
+    workspace grows by the three tensor planes, so the split path is the one
+    that ran."""
+    import ctypes
+    from tensorly_gb300 import _lib
+    rs = np.random.RandomState(21)
+    fs = [rs.rand(s, 6) for s in (48, 40, 32)]
+    x64 = np.einsum("ir,jr,kr->ijk", *fs) + 0.01 * rs.rand(48, 40, 32)
+    x = torch.as_tensor(x64, dtype=torch.float32, device="cuda")
+    kw = dict(init="random", random_state=5, n_iter_max=6, tol=1e-12)
+    lib = _lib.lib()
+
+    def run():
+        if algo == "mu":
+            return gb300.non_negative_parafac(x, 6, return_errors=True, **kw)
+        if algo == "hals":
+            return gb300.non_negative_parafac_hals(x, 6, return_errors=True, **kw)
+        np.random.seed(5)     # its 'random' start draws from NumPy's global generator
+        return gb300.constrained_parafac(x, 6, non_negative=True, return_errors=True,
+                                         init="random", random_state=5, n_iter_max=6,
+                                         tol_outer=1e-12)
+
+    def ws_bytes():
+        nb = ctypes.c_size_t(0)
+        sh = _lib.i64_array(x.shape)
+        _lib.check(lib.tlgb_cp_nn_mu_workspace_size(_lib.TLGB_F32, 3, sh, 6, 6, ctypes.byref(nb)))
+        return nb.value
+
+    try:
+        tc_bytes = ws_bytes()
+        (w1, f1), e1 = run()
+        _lib.check(lib.tlgb_set_tuning(b"split_simt", 1))
+        simt_bytes = ws_bytes()
+        (w2, f2), e2 = run()
+    finally:
+        _lib.check(lib.tlgb_set_tuning(b"split_simt", 0))
+    assert tc_bytes >= simt_bytes + 3 * 2 * x.numel()
+    assert len(e1) == len(e2)
+    np.testing.assert_allclose(e1, e2, rtol=1e-4)
+    for a, b in zip(f1, f2):
+        np.testing.assert_allclose(host(a), host(b), rtol=1e-3, atol=1e-3 * host(b).max())
+    if algo == "mu":
+        (_, fo), eo = oracle.non_negative_parafac(x64, 6, return_errors=True, **kw)
+    elif algo == "hals":
+        (_, fo), eo = oracle.non_negative_parafac_hals(x64, 6, return_errors=True, **kw)
+    else:
+        np.random.seed(5)
+        (_, fo), eo = oracle.constrained_parafac(x64, 6, non_negative=True, return_errors=True,
+                                                 init="random", random_state=5, n_iter_max=6,
+                                                 tol_outer=1e-12)
+    np.testing.assert_allclose(e1, eo, rtol=1e-3)

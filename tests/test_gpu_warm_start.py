@@ -205,7 +205,11 @@ def test_warm_start_gain_over_svd_start(ws, gen, trained):
     for k in ("learned", "warm"):   # same fit as from the SVD start
         rel = (res["err_" + k] - res["err_svd"]) / res["err_svd"]
         assert abs(np.median(rel)) < 1e-4, (k, np.median(rel))
-    # measured at tol 1e-8 on 4096 held-out tensors: 56.8 mean sweeps from the
-    # network's start against 60.4 from the SVD start
-    assert res["sweeps_learned"].mean() <= 1.02 * res["sweeps_svd"].mean()
-    assert res["sweeps_warm"].mean() <= 1.02 * res["sweeps_svd"].mean()
+    # The gain over the method without the network (init='svd'): on these 1024
+    # held-out tensors the network's start needed 42.5 mean sweeps against 47.2
+    # from the SVD start, and the warm start reached the fit in 26.9 ms against
+    # 38.7 ms.  Training itself adds little beyond the sketch skip (42.6 mean
+    # sweeps untrained), which the printout above reports.
+    assert res["sweeps_learned"].mean() <= 0.95 * res["sweeps_svd"].mean()
+    assert res["sweeps_warm"].mean() <= 0.95 * res["sweeps_svd"].mean()
+    assert res["ms_warm"] < res["ms_svd"]
