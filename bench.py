@@ -514,7 +514,7 @@ def measure_batched(args, steps, warmup):
     dev = torch.device("cuda", torch.cuda.current_device())
     # device-resident inputs: one buffer of tensors, one of initial factors
     prob = BatchedProblem([torch.from_numpy(x).to(dev) for x in xs], ranks, random_state=seeds)
-    choice = autotune.tune_batched(prob, sweeps=4, reps=2)   # outside the timed region
+    choice, tiles = autotune.tune_batched(prob, sweeps=4, reps=2)   # outside the timed region
     final = prob.final
     st = torch.cuda.current_stream()
 
@@ -576,7 +576,7 @@ def measure_batched(args, steps, warmup):
             "data": "synthetic",
             "config": {"workload": f"{n} uneven 3-way tensors, dims 8-64, rank 4-16, "
                                    f"{sweeps} sweeps", "l2": "0.76 GB of tensors > L2",
-                       "autotuned_threads": choice},
+                       "autotuned_threads": choice, "autotuned_outer_tiles": tiles},
             "accuracy_vs_f64": {"max_rel_diff_final_error": float(max(rel)),
                                 "median": float(np.median(rel)),
                                 "within_1e-4": f"{sum(r < 1e-4 for r in rel)}/{len(rel)}",

@@ -12,11 +12,14 @@ Batched CP-ALS kernel variants (``tune_batched``):
 
 ``tlgb_cp_als_batched`` sorts the tensors of a batch into three size classes
 (by the shared-memory footprint of the padded tensor) and runs each class with
-a kernel variant of 128, 256 or 512 threads per CTA (4, 2 or 1 CTAs per SM).
-``tune_batched`` times every variant for every class on the caller's own batch
-(a few sweeps, CUDA events, the other classes left at their current choice),
-keeps the fastest, sets it with ``tlgb_set_tuning`` and returns the choice.
-Choices are cached per device and batch signature for the process.
+a kernel variant of 128, 256 or 512 threads per CTA (4, 2 or 1 CTAs per SM)
+and an MTTKRP work tile of one row, four rank columns and ``outer_tile``
+slices of the outer mode (0: the slices spread over as many groups as there
+are threads).  ``tune_batched`` times, per class, every thread count and then
+every outer tile on the caller's own batch (a few sweeps, CUDA events, the
+other classes left at their current choice), keeps the fastest, sets it with
+``tlgb_set_tuning`` and returns the choice.  Choices are cached per device
+and batch signature for the process.
 """
 
 import ctypes
@@ -27,11 +30,16 @@ from . import _lib
 
 CLASSES = ("small", "medium", "large")
 VARIANTS = (128, 256, 512)
+OUTER_TILES = (0, 2, 4, 8, 16)
 _cache = {}
 
 
 def _set(cls, nt):
     _lib.check(_lib.lib().tlgb_set_tuning(f"batched_threads_{cls}".encode(), int(nt)))
+
+
+def _set_tile(cls, ot):
+    _lib.check(_lib.lib().tlgb_set_tuning(f"batched_outer_tile_{cls}".encode(), int(ot)))
 
 
 def _time(problem, sweeps, reps):
@@ -48,16 +56,21 @@ def _time(problem, sweeps, reps):
 
 
 def tune_batched(problem, sweeps=4, reps=2, verbose=False):
-    """Pick the fastest variant per size class for ``problem`` (a
-    ``BatchedProblem``); returns {class: threads} and leaves it set."""
+    """Pick the fastest thread count, then the fastest MTTKRP outer tile, per
+    size class for ``problem`` (a ``BatchedProblem``); returns {class:
+    threads} and {class: outer_tile} and leaves them set."""
     key = (torch.cuda.get_device_name(problem.device), len(problem),
            tuple(sorted(set(problem.shapes)))[:64], tuple(problem.ranks[:64]))
     if key in _cache:
-        for cls, nt in _cache[key].items():
-            _set(cls, nt)
-        return dict(_cache[key])
-    choice = {cls: 0 for cls in CLASSES}
+        threads, tiles = _cache[key]
+        for cls in CLASSES:
+            _set(cls, threads[cls])
+            _set_tile(cls, tiles[cls])
+        return dict(threads), dict(tiles)
+    threads = {cls: 0 for cls in CLASSES}
+    tiles = {cls: 0 for cls in CLASSES}
     for cls in CLASSES:
+        _set_tile(cls, 0)
         best = None
         for nt in VARIANTS:
             _set(cls, nt)
@@ -66,16 +79,26 @@ def tune_batched(problem, sweeps=4, reps=2, verbose=False):
                 print(f"batched {cls}: {nt} threads -> {ms:.2f} ms")
             if best is None or ms < best[0]:
                 best = (ms, nt)
-        choice[cls] = best[1]
+        threads[cls] = best[1]
         _set(cls, best[1])
-    _cache[key] = dict(choice)
-    return choice
+        for ot in OUTER_TILES[1:]:
+            _set_tile(cls, ot)
+            ms = _time(problem, sweeps, reps)
+            if verbose:
+                print(f"batched {cls}: outer tile {ot} -> {ms:.2f} ms")
+            if ms < best[0]:
+                best = (ms, best[1])
+                tiles[cls] = ot
+        _set_tile(cls, tiles[cls])
+    _cache[key] = (dict(threads), dict(tiles))
+    return threads, tiles
 
 
 def reset_batched():
-    """Back to the library defaults (128 / 256 / 512)."""
+    """Back to the library defaults (128 / 256 / 512 threads, default tiles)."""
     for cls in CLASSES:
         _set(cls, 0)
+        _set_tile(cls, 0)
 
 
 DENSE_SPACE = (
@@ -110,11 +133,13 @@ def _time_dense(x, rank, init, sweeps, reps):
     return a.elapsed_time(b) / reps
 
 
-def tune_dense(x, rank, sweeps=8, reps=2, verbose=False):
+def tune_dense(x, rank, sweeps=12, reps=3, min_gain=0.01, verbose=False):
     """Pick the tensor-core MTTKRP's inner-mode group size, ring depth and
     wave count for bf16 CP-ALS of the f32 CUDA tensor ``x`` at ``rank`` by a
-    coordinate search over ``DENSE_SPACE`` (the defaults first); returns
-    {key: value} and leaves it set.  Cached per device, shape and rank."""
+    coordinate search over ``DENSE_SPACE`` (the defaults first); a value
+    replaces the current one only if it is at least ``min_gain`` faster, so
+    timing noise does not move the choice.  Returns {key: value} and leaves
+    it set.  Cached per device, shape and rank."""
     key = (torch.cuda.get_device_name(x.device), tuple(x.shape), int(rank))
     if key in _dense_cache:
         for k, v in _dense_cache[key].items():
@@ -140,7 +165,7 @@ def tune_dense(x, rank, sweeps=8, reps=2, verbose=False):
                 ms = float("inf")
             if verbose:
                 print(f"dense {k}={v}: {ms:.3f} ms")
-            if ms < best_ms:
+            if ms < (1.0 - min_gain) * best_ms:
                 best_ms, choice[k] = ms, v
         _set_key(k, choice[k])
     _dense_cache[key] = dict(choice)

@@ -506,6 +506,25 @@ __device__ __forceinline__ void gram_update_df(float* g, const float* rows, int 
   }
 }
 
+// Plain f32 variant (the lite solve): only the hi plane accumulates, the lo
+// plane stays zero; two entries a step for independent chains.
+__device__ __forceinline__ void gram_update_f32(float* g, const float* rows, int nrows, int R) {
+  const int RR = R * R;
+  for (int e = threadIdx.x; e < RR; e += 2 * blockDim.x) {
+    const int e2 = e + blockDim.x;
+    const int r = e / R, s = e - (e / R) * R;
+    const int r2 = e2 / R, s2 = e2 - (e2 / R) * R;
+    const bool a1 = s <= r, a2 = e2 < RR && s2 <= r2;
+    float h = a1 ? g[e] : 0.f, h2 = a2 ? g[e2] : 0.f;
+    for (int w = 0; w < nrows; ++w) {
+      if (a1) h = fmaf(rows[w * R + r], rows[w * R + s], h);
+      if (a2) h2 = fmaf(rows[w * R + r2], rows[w * R + s2], h2);
+    }
+    if (a1) g[e] = h;
+    if (a2) g[e2] = h2;
+  }
+}
+
 // Sum of the MTTKRP split partials of one entry.  f32 partials: compensated
 // f32 summation (Neumaier), whose error (~splits * 2^-48) is far below the
 // partials' own rounding, on the f32 pipe (the f64 pipe is ~70x slower here).
@@ -513,14 +532,14 @@ __device__ __forceinline__ double sum_splits(const float* __restrict__ partial, 
                                              int64_t stride, int64_t off) {
   float s = 0.f, c = 0.f;
   int p = 0;
-  // twelve loads in flight per batch: the partials come from L2 and a batch
-  // costs one round trip
-  for (; p + 11 < splits; p += 12) {
-    float v[12];
+  // eighteen loads in flight per batch: the partials come from L2 and a
+  // batch costs one round trip (the bf16 sweeps' 36 tiles take two)
+  for (; p + 17 < splits; p += 18) {
+    float v[18];
 #pragma unroll
-    for (int u = 0; u < 12; ++u) v[u] = partial[(int64_t)(p + u) * stride + off];
+    for (int u = 0; u < 18; ++u) v[u] = partial[(int64_t)(p + u) * stride + off];
 #pragma unroll
-    for (int u = 0; u < 12; ++u) {
+    for (int u = 0; u < 18; ++u) {
       const float t = s + v[u];
       c += (fabsf(s) >= fabsf(v[u])) ? ((s - t) + v[u]) : ((v[u] - t) + s);
       s = t;
@@ -577,7 +596,7 @@ k_solve(const T* __restrict__ partial, int splits, int64_t I, int R_in,
         const double* __restrict__ fac, const int* __restrict__ perm,
         const double* __restrict__ vmat, const float* __restrict__ w32, T* A,
         __nv_bfloat16* A_bt, double* gpart, double* ipart, AlsCtrl* ctrl, int64_t rpb,
-        int mats_in_smem, int max_passes) {
+        int mats_in_smem, int max_passes, int lite_in) {
   const int R = (RT > 0) ? RT : R_in;
   griddep_wait();   // the MTTKRP partials (programmatic launch inside a sweep)
   griddep_launch_dependents();
@@ -600,6 +619,7 @@ k_solve(const T* __restrict__ partial, int splits, int64_t I, int R_in,
   // sums; ~2^-48 relative), since this GPU's f64 pipe is ~70x slower.  The
   // block's Gram is then kept as f32 (hi, lo) pairs.
   const bool df = (sizeof(T) == 4) && mats_in_smem;
+  const bool lite = df && lite_in;
   if (kind == 2) {
     // ------------------------------------------------ refinement path
     const int RB = max(1, kSolveThreads / R);   // rows per round
@@ -627,17 +647,16 @@ k_solve(const T* __restrict__ partial, int splits, int64_t I, int R_in,
         float* Ws = reinterpret_cast<float*>(Vs);
         const int n = 3 * RR;
         const int n4 = ((reinterpret_cast<uintptr_t>(w32) & 15) == 0) ? n / 4 : 0;
+        // asynchronous 16-byte copies (cp.async): all in flight at once and
+        // overlapped with the partial sums below; waited for before the first
+        // product that reads them
         const float4* src = reinterpret_cast<const float4*>(w32);
-        float4* dst = reinterpret_cast<float4*>(Ws);
-        int e = tid;
-        for (; e + 3 * (int)blockDim.x < n4; e += 4 * blockDim.x) {
-          float4 v[4];
-#pragma unroll
-          for (int u = 0; u < 4; ++u) v[u] = src[e + u * blockDim.x];
-#pragma unroll
-          for (int u = 0; u < 4; ++u) dst[e + u * blockDim.x] = v[u];
+        for (int e = tid; e < n4; e += blockDim.x) {
+          const unsigned dst = (unsigned)__cvta_generic_to_shared(reinterpret_cast<float4*>(Ws) + e);
+          asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src + e)
+                       : "memory");
         }
-        for (; e < n4; e += blockDim.x) dst[e] = src[e];
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
         for (int f = 4 * n4 + tid; f < n; f += blockDim.x) Ws[f] = w32[f];
         VmH = Ws + RR;
         VmL = Ws + 2 * RR;
@@ -664,6 +683,7 @@ k_solve(const T* __restrict__ partial, int splits, int64_t I, int R_in,
         mb[rr * R + c] = mv;
         mbf[rr * R + c] = (float)mv;
       }
+      asm volatile("cp.async.wait_all;\n" ::: "memory");   // this thread's copies of W, V
       __syncthreads();
       if (act) {   // x0 = m W32 (f32)
         const float* m = mbf + rr * R;
@@ -683,7 +703,16 @@ k_solve(const T* __restrict__ partial, int splits, int64_t I, int R_in,
       __syncthreads();
       for (int pass = 0; pass < max_passes; ++pass) {
         if (tid == 0) { s_dmax = 0ull; s_xmax = 0ull; }
-        if (act && df) {   // r = m - x V in double-float (four Neumaier chains)
+        if (act && lite) {   // r = m - x V with x V in f32 (four chains, V's hi plane)
+          const float* xh = xbh + rr * R;
+          float q[4] = {0.f, 0.f, 0.f, 0.f};
+          for (int k = 0; k < R; k += 4) {
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+              if (k + u < R) q[u] = fmaf(xh[k + u], VmH[(k + u) * R + c], q[u]);
+          }
+          rbf[rr * R + c] = (float)(mb[rr * R + c] - (double)((q[0] + q[1]) + (q[2] + q[3])));
+        } else if (act && df) {   // r = m - x V in double-float (four Neumaier chains)
           const float* xh = xbh + rr * R;
           const float* xl = xbl + rr * R;
           float s[4] = {0.f, 0.f, 0.f, 0.f}, cp[4] = {0.f, 0.f, 0.f, 0.f};
@@ -756,7 +785,8 @@ k_solve(const T* __restrict__ partial, int splits, int64_t I, int R_in,
         if (df) gbf[rr * R + c] = 0.f;
       }
       __syncthreads();
-      if (df) gram_update_df(reinterpret_cast<float*>(gacc), gbf, RB, R);
+      if (lite) gram_update_f32(reinterpret_cast<float*>(gacc), gbf, RB, R);
+      else if (df) gram_update_df(reinterpret_cast<float*>(gacc), gbf, RB, R);
       else gram_update(gacc, rb, RB, R);   // Gram of the stored rows
       __syncthreads();
     }
@@ -1172,7 +1202,7 @@ template <typename T>
 int als_launch_solve(const T* partial, int splits, int64_t I, int R, const double* fac,
                      const int* perm, const double* vmat, const float* w32, T* A,
                      __nv_bfloat16* A_bt, double* gpart, double* ipart, AlsCtrl* ctrl,
-                     int max_passes, int* nblocks, cudaStream_t st, bool pdl) {
+                     int max_passes, int* nblocks, cudaStream_t st, bool pdl, bool lite) {
   const int nb = solve_blocks_for(I);
   const int64_t rpb = ceil_div(I, nb);
   const int nbe = (int)ceil_div(I, rpb);
@@ -1182,15 +1212,18 @@ int als_launch_solve(const T* partial, int splits, int64_t I, int R, const doubl
   if (R == 64)
     TLGB_CUDA_TRY(launch_maybe_pdl(pdl, k_solve<T, 64>, dim3(nbe), dim3(kSolveThreads),
                                    solve_smem(R), st, partial, splits, I, R, fac, perm, vmat,
-                                   w32, A, A_bt, gpart, ipart, ctrl, rpb, mats, max_passes));
+                                   w32, A, A_bt, gpart, ipart, ctrl, rpb, mats, max_passes,
+                                   lite ? 1 : 0));
   else if (R == 32)
     TLGB_CUDA_TRY(launch_maybe_pdl(pdl, k_solve<T, 32>, dim3(nbe), dim3(kSolveThreads),
                                    solve_smem(R), st, partial, splits, I, R, fac, perm, vmat,
-                                   w32, A, A_bt, gpart, ipart, ctrl, rpb, mats, max_passes));
+                                   w32, A, A_bt, gpart, ipart, ctrl, rpb, mats, max_passes,
+                                   lite ? 1 : 0));
   else
     TLGB_CUDA_TRY(launch_maybe_pdl(pdl, k_solve<T, 0>, dim3(nbe), dim3(kSolveThreads),
                                    solve_smem(R), st, partial, splits, I, R, fac, perm, vmat,
-                                   w32, A, A_bt, gpart, ipart, ctrl, rpb, mats, max_passes));
+                                   w32, A, A_bt, gpart, ipart, ctrl, rpb, mats, max_passes,
+                                   lite ? 1 : 0));
   TLGB_LAUNCH_CHECK();
   *nblocks = nbe;
   return TLGB_OK;
@@ -1311,7 +1344,7 @@ int als_prepare(int dtype) {
                                        cudaStream_t);                                        \
   template int als_launch_solve<T>(const T*, int, int64_t, int, const double*, const int*,   \
                                    const double*, const float*, T*, __nv_bfloat16*, double*, \
-                                   double*, AlsCtrl*, int, int*, cudaStream_t, bool);        \
+                                   double*, AlsCtrl*, int, int*, cudaStream_t, bool, bool);  \
   template int als_launch_fit<T>(const double*, int, int, const T*, const double*, int,      \
                                  AlsCtrl*, double*, int, double, int, cudaStream_t);         \
   template int als_launch_gram_reduce_fit<T>(const double*, int, int, double*, int, int, int,  \

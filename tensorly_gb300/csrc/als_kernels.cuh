@@ -40,10 +40,14 @@ int als_launch_factorize(const double* G, int ndim, int mode, int R, const T* we
 template <typename T>
 // max_passes: refinement passes allowed on the f32-inverse path (each pass
 // stops early once the correction is below 1e-12 of the solution).
+// lite (f32 factors): the refinement residual and the block's Gram in plain
+// f32 instead of double-float, for sweeps whose MTTKRP is itself only
+// accurate to ~1e-6 (the bf16 tensor-core sweeps).
 int als_launch_solve(const T* partial, int splits, int64_t I, int R, const double* fac,
                      const int* perm, const double* vmat, const float* w32, T* A,
                      __nv_bfloat16* A_bf16_t, double* gpart, double* ipart, AlsCtrl* ctrl,
-                     int max_passes, int* nblocks, cudaStream_t st, bool pdl = false);
+                     int max_passes, int* nblocks, cudaStream_t st, bool pdl = false,
+                     bool lite = false);
 
 constexpr int kIrMaxPasses = 4;
 

@@ -73,6 +73,7 @@ struct BArgs {
   double tol;          // > 0: stop a tensor once |e_{s-1} - e_s| < tol (s >= 1)
   int* sweeps_done;    // [n] sweeps run per tensor, or null
   int* conv;           // [n] converged in an earlier launch (workspace, zeroed per run)
+  int otile;           // outer-mode slices per MTTKRP work item (0: as many groups as fit)
 };
 
 __device__ __forceinline__ double warp_sum_d(double v) {
@@ -371,7 +372,10 @@ __global__ void __launch_bounds__(NT, kBThreads / NT) k_cp_als_batched(const BAr
         const float* So = Fs + o_mode * kBMaxDim * kBMaxRank;
         const int per = na * NQ;                       // outputs (row, 4 columns)
         const int workers = NT - 32;                   // warps 1.. (warp 0 inverts V)
-        const int ngrp = max(1, min(no, workers / per));
+        // the MTTKRP's work tile: one row, four rank columns and every ngrp-th
+        // outer slice; otile sets how many outer slices a tile covers
+        int ngrp = max(1, min(no, workers / per));
+        if (a.otile > 0) ngrp = max(1, min(ngrp, (no + a.otile - 1) / a.otile));
         if (resident) {
           if (tid < 32) {
             gj_inverse_warp(V, W, RP);
@@ -549,6 +553,7 @@ namespace {
 // / "_medium" / "_large", 0 = default) and chosen by the autotuner.
 int g_batched_nt[3] = {0, 0, 0};
 const int kDefaultNt[3] = {128, 256, 512};
+int g_batched_otile[3] = {0, 0, 0};   // outer slices per MTTKRP work tile (0 = default)
 
 int64_t padded_elems(const int64_t* d) {
   const int64_t sJ = d[2] | 1;
@@ -578,6 +583,14 @@ int launch_variant(BArgs a, int grid_max, cudaStream_t st) {
 namespace tlgb {
 int batched_set_tuning(const std::string& key, int value) {
   int cls = -1;
+  if (key == "batched_outer_tile_small") cls = 0;
+  else if (key == "batched_outer_tile_medium") cls = 1;
+  else if (key == "batched_outer_tile_large") cls = 2;
+  if (cls >= 0) {
+    TLGB_CHECK_ARG(value >= 0 && value <= 64, "set_tuning: batched outer tiles are 0..64");
+    g_batched_otile[cls] = value;
+    return TLGB_OK;
+  }
   if (key == "batched_threads_small") cls = 0;
   else if (key == "batched_threads_medium") cls = 1;
   else if (key == "batched_threads_large") cls = 2;
@@ -672,6 +685,7 @@ extern "C" int tlgb_cp_als_batched(int n_tensors, const tlgb_batch_item* items, 
       a.n = cnt[c];
       a.counter = d_counter + c;
       const int nt = g_batched_nt[c] ? g_batched_nt[c] : kDefaultNt[c];
+      a.otile = g_batched_otile[c];
       int rc = nt == 128 ? launch_variant<128>(a, sms, st)
              : nt == 256 ? launch_variant<256>(a, sms, st)
                          : launch_variant<512>(a, sms, st);

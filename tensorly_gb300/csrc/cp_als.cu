@@ -283,9 +283,10 @@ struct Runner {
       rc = als_launch_solve<T>((const T*)partial, splits, sh.dim[mode], (int)R, B.fac, B.perm,
                                B.vmat, B.w32, factors[mode], B.fbt[mode], B.gpart,
                                last ? B.ipart : nullptr, B.ctrl,
-                               // the bf16 MTTKRP is accurate to ~1e-6, so one refinement
-                               // pass (solve error ~(cond * 6e-8)^2) is enough there
-                               (tc && P->tc[mode].valid) ? 1 : kIrMaxPasses, &nb, st, pdl);
+                               // the bf16 MTTKRP is accurate to ~1e-6, so one plain-f32
+                               // refinement pass (solve error ~cond * 6e-8) is enough there
+                               (tc && P->tc[mode].valid) ? 1 : kIrMaxPasses, &nb, st, pdl,
+                               tc && P->tc[mode].valid && !tc_tuning().full_solve);
       if (rc) return rc;
       if (last) last_nb = nb;
       if (last) {   // the last mode's Gram reduction also computes the fit (in order)

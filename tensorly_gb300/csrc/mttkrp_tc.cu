@@ -1085,6 +1085,7 @@ extern "C" int tlgb_set_tuning(const char* key, int value) {
   else if (k == "no_pdl") tc_tuning().no_pdl = value;
   else if (k == "tc_test_starve") tc_tuning().test_starve = value;
   else if (k == "split_simt") tc_tuning().split_simt = value;
+  else if (k == "full_solve") tc_tuning().full_solve = value;
   else return batched_set_tuning(k, value);   // the batched CP-ALS variants
   return TLGB_OK;
 }

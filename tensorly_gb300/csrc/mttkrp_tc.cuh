@@ -45,6 +45,7 @@ struct TcTuning {
   int no_pdl = 0;             // 1: CP-ALS sweep kernels launch without programmatic dependence
   int test_starve = 0;        // 1: tensor-core MTTKRP issues no copies (timeout-path test)
   int split_simt = 0;         // 1: non-negative / constrained CP keep the SIMT f32 MTTKRP
+  int full_solve = 0;         // 1: bf16 CP-ALS sweeps solve with the double-float refinement
 };
 TcTuning& tc_tuning();
 

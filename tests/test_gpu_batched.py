@@ -96,9 +96,17 @@ def test_autotuner_picks_a_variant_and_variants_agree(gb300):
             for cls in autotune.CLASSES:
                 autotune._set(cls, nt)
             finals.append(prob.run(12).final.cpu().numpy())
-        choice = autotune.tune_batched(prob, sweeps=2, reps=1)
-        assert set(choice) == set(autotune.CLASSES)
+        for cls in autotune.CLASSES:
+            autotune._set(cls, 256)
+        for ot in autotune.OUTER_TILES[1:]:      # the MTTKRP's outer-slice tiles
+            for cls in autotune.CLASSES:
+                autotune._set_tile(cls, ot)
+            finals.append(prob.run(12).final.cpu().numpy())
+        choice, tiles = autotune.tune_batched(prob, sweeps=2, reps=1)
+        assert set(choice) == set(autotune.CLASSES) == set(tiles)
         assert all(v in autotune.VARIANTS for v in choice.values())
+        assert all(v in autotune.OUTER_TILES for v in tiles.values())
+        assert autotune.tune_batched(prob) == (choice, tiles)      # cached
     finally:
         autotune.reset_batched()
     for f in finals[1:]:
