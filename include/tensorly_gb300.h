@@ -398,6 +398,20 @@ int tlgb_ws_sketch(const void* X, int batch, void* feats, void* xnorm, const voi
 int tlgb_ws_gemm(int M, int N, int K, const void* A, int64_t sam, int64_t sak, const void* B,
                  int64_t sbk, int64_t sbn, void* C, int64_t ldc, const void* bias, int relu,
                  const void* mask, void* stream);
+/*
+ * ws_gemm_tc: the same product on the tensor cores (tcgen05): A and B split
+ * exactly into three bf16 planes stored K-major in the workspace, each
+ * 128 x 128 output tile accumulates the products a_i b_j with i + j <= 2
+ * with f32 accumulation (the dropped terms are below 2^-26 of |a||b|).
+ * Workspace
+ * (tlgb_ws_gemm_tc_workspace_size, 256-byte aligned): its first int is a
+ * status word that receives TLGB_ETIMEOUT if a bounded pipeline wait expired
+ * (the caller zeroes it; read it with tlgb_workspace_status).
+ */
+int tlgb_ws_gemm_tc_workspace_size(int M, int N, int K, size_t* bytes);
+int tlgb_ws_gemm_tc(int M, int N, int K, const void* A, int64_t sam, int64_t sak, const void* B,
+                    int64_t sbk, int64_t sbn, void* C, int64_t ldc, const void* bias, int relu,
+                    const void* mask, void* workspace, size_t workspace_bytes, void* stream);
 int tlgb_ws_colsum(const void* Y, int M, int N, int64_t ld, void* out, void* stream);
 int tlgb_ws_cp_loss(const void* X, const void* out, const void* xnorm, int batch, void* loss,
                     void* dout, void* alpha, void* stream);

@@ -263,6 +263,13 @@ SIGNATURES = [
       ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     ("tlgb_inv_sqrt", ctypes.c_int,
      [ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p]),
+    ("tlgb_ws_gemm_tc_workspace_size", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_size_t)]),
+    ("tlgb_ws_gemm_tc", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
+      ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
+      ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+      ctypes.c_void_p]),
     ("tlgb_sparse_residual_workspace_bytes", ctypes.c_size_t, []),
     ("tlgb_sparse_residual", ctypes.c_int,
      [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,

@@ -50,8 +50,9 @@ constexpr int kAuxSms = 1;
 struct Plans {
   MttkrpPlan simt[kMaxModes];
   TcPlan tc[kMaxModes];          // bf16 sweeps (2 factor planes)
-  TcPlan tcr[kMaxModes][3];      // f32-faithful refinement: x0, x1, x2 with 3, 2, 1 planes
+  TcPlan tcr[kMaxModes][3];      // closing sweeps: x0, x1 (, x2) with 3, 2 (, 1) factor planes
   bool refine_tc = false;        // refinement sweeps run on the tensor cores
+  int xplanes = 2;               // tensor planes the closing sweeps contract (2 or 3)
 };
 
 int layout(int dtype, const Shape& sh, int64_t R, const tlgb_cp_als_options& o,
@@ -88,16 +89,18 @@ int layout(int dtype, const Shape& sh, int64_t R, const tlgb_cp_als_options& o,
     B->xbf = c.take<__nv_bfloat16>((size_t)sh.numel);
     if (P.refine_tc) {
       B->xsplit[0] = c.take<__nv_bfloat16>((size_t)sh.numel);
-      B->xsplit[1] = c.take<__nv_bfloat16>((size_t)sh.numel);
+      if (P.xplanes == 3) B->xsplit[1] = c.take<__nv_bfloat16>((size_t)sh.numel);
     }
     for (int k = 0; k < sh.ndim; ++k)
       B->fbt[k] = c.take<__nv_bfloat16>((size_t)kFactorPlanes * R * sh.dim[k]);
     size_t tmax = 0;
     for (int k = 0; k < sh.ndim; ++k) {
       if (P.tc[k].valid) tmax = std::max(tmax, P.tc[k].partial_bytes);
-      if (P.refine_tc)
-        tmax = std::max(tmax, P.tcr[k][0].partial_bytes + P.tcr[k][1].partial_bytes +
-                                  P.tcr[k][2].partial_bytes);
+      if (P.refine_tc) {
+        size_t sum = 0;
+        for (int j = 0; j < P.xplanes; ++j) sum += P.tcr[k][j].partial_bytes;
+        tmax = std::max(tmax, sum);
+      }
     }
     B->tc_partial = c.take<char>(tmax);
   }
@@ -130,6 +133,7 @@ int validate(int dtype, int ndim, const int64_t* shape, int64_t rank,
 int make_plans(int dtype, const Shape& sh, int64_t R, const tlgb_cp_als_options& o, Plans* P) {
   const bool mixed = o.precision == TLGB_PREC_BF16;
   P->refine_tc = mixed && o.refine_sweeps > 0 && !tc_tuning().refine_simt;
+  P->xplanes = tc_tuning().closing_planes == 3 ? 3 : 2;
   for (int k = 0; k < sh.ndim; ++k) {
     int rc = mttkrp_make_plan(dtype, sh, R, k, &P->simt[k]);
     if (rc) return rc;
@@ -141,7 +145,7 @@ int make_plans(int dtype, const Shape& sh, int64_t R, const tlgb_cp_als_options&
       P->tc[k].pdl = 1;   // programmatic launch behind the previous solve
     }
     if (P->refine_tc) {
-      for (int j = 0; j < 3; ++j) {
+      for (int j = 0; j < P->xplanes; ++j) {
         rc = mttkrp_tc_make_plan(sh, R, k, 3 - j, kAuxSms, &P->tcr[k][j]);
         if (rc) return rc;
         if (!P->tcr[k][j].valid) P->refine_tc = false;
@@ -189,7 +193,7 @@ struct Runner {
         if (rc) return rc;
       }
       if (P->refine_tc)
-        for (int j = 0; j < 3; ++j) {
+        for (int j = 0; j < P->xplanes; ++j) {
           int rc = mttkrp_tc_encode(P->tcr[k][j], planes[j], B.fbt, kFactorPlanes,
                                     &tcr_maps[k][j]);
           if (rc) return rc;
@@ -200,7 +204,7 @@ struct Runner {
 
   // Enqueues one sweep.  kind: kSweepNative (SIMT MTTKRP in the tensor dtype),
   // kSweepBf16 (bf16 tensor, two-plane factor, tensor cores), kSweepF32Tc
-  // (three-plane split of the f32 tensor and factor on the tensor cores) or
+  // (the split f32 tensor and three-plane factor on the tensor cores) or
   // kSweepF32TcFinal (the same, but the last mode's MTTKRP on the SIMT f32
   // kernel).  The tensor cores' f32 accumulation rounds toward zero (measured
   // bias about -2e-7 of |M| at 512^3, against ~1e-10 for the SIMT kernel) and
@@ -256,11 +260,12 @@ struct Runner {
         splits = P->tc[mode].splits;
         partial = B.tc_partial;
       } else if (kind == kSweepF32Tc || (kind == kSweepF32TcFinal && !last)) {
-        // x0 . (f0 + f1 + f2) + x1 . (f0 + f1) + x2 . f0, each launch writing
-        // its own run of partial tiles; the solve sums all of them
+        // x0 . (f0 + f1 + f2) + x1 . (f0 + f1) (+ x2 . f0 with three tensor
+        // planes), each launch writing its own run of partial tiles; the solve
+        // sums all of them
         splits = 0;
         if constexpr (sizeof(T) == 4) {
-          for (int j = 0; j < 3 && !rc; ++j) {
+          for (int j = 0; j < P->xplanes && !rc; ++j) {
             const TcPlan& tp = P->tcr[mode][j];
             rc = mttkrp_tc_launch_maps(tp, tcr_maps[mode][j], (const float* const*)cf,
                                        (const float*)mw,
@@ -431,7 +436,7 @@ int run(const T* X, const Shape& sh, int64_t R, T* const* factors, T* weights,
   if (rc) return rc;
   if (mixed) {
     rc = P.refine_tc ? tc_launch_split3((const float*)X, sh.numel, run.B.xbf, run.B.xsplit[0],
-                                        run.B.xsplit[1], st)
+                                        run.B.xsplit[1], st)   // x2 only with three planes
                      : tc_launch_to_bf16((const float*)X, sh.numel, run.B.xbf, st);
     if (rc) return rc;
     rc = run.bf16_factors(st);

@@ -28,6 +28,7 @@
 #include <mutex>
 
 #include "mttkrp_tc.cuh"
+#include "tc_ptx.cuh"
 
 namespace tlgb {
 namespace {
@@ -39,7 +40,6 @@ constexpr int kChunk = 64;                       // bf16 elements per 128-byte s
 constexpr int kStageBytes = kTileM * kChunk * 2;  // 16 KiB
 constexpr int kSmemBudget = 225 * 1024;          // dynamic shared memory used at most
 constexpr int kThreads = 192;
-constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s
 
 struct TcArgs {
   int stages;                 // depth of the tensor-tile ring
@@ -63,139 +63,6 @@ struct TcArgs {
   int starve;
 };
 constexpr unsigned long long kStarveWaitNs = 1000000ull;  // 1 ms
-
-// ------------------------------------------------------------ PTX helpers
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ unsigned long long now_ns() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
-               "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint32_t addr, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(addr), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// Bounded wait (limit_ns of wall time); returns false (and records the
-// timeout) if it gave up.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, bool& failed,
-                                          unsigned long long limit_ns = kWaitNs) {
-  if (failed) return false;
-  const uint32_t addr = smem_u32(bar);
-  if (mbar_try_wait(addr, parity)) return true;
-  const unsigned long long t0 = now_ns();
-  while (true) {
-    if (mbar_try_wait(addr, parity)) return true;
-    if (now_ns() - t0 > limit_ns) {
-      atomicExch(err, TLGB_ETIMEOUT);
-      failed = true;
-      return false;
-    }
-  }
-}
-// Bounded wait used only to drain asynchronous work before the CTA exits.
-__device__ __forceinline__ void mbar_drain(uint64_t* bar, uint32_t parity) {
-  const uint32_t addr = smem_u32(bar);
-  const unsigned long long t0 = now_ns();
-  while (!mbar_try_wait(addr, parity))
-    if (now_ns() - t0 > kWaitNs) return;
-}
-__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar,
-                                            int c0, int c1, int c2) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
-      : "memory");
-}
-__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, uint64_t* bar,
-                                            int c0, int c1, int c2, int c3) {
-  asm volatile(
-      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(smem_u32(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3),
-      "r"(smem_u32(bar))
-      : "memory");
-}
-__device__ __forceinline__ void tc_fence_before() {
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-}
-__device__ __forceinline__ void tc_fence_after() {
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-}
-__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc,
-                                          uint32_t idesc, uint32_t accumulate) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
-      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate));
-}
-__device__ __forceinline__ void umma_commit(uint64_t* bar) {
-  asm volatile(
-      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-          smem_u32(bar))
-      : "memory");
-}
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
-      "%11, %12, %13, %14, %15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
-        "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-__device__ __forceinline__ void tmem_ld32_nowait(uint32_t taddr, uint32_t (&r)[32]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
-      "%11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, "
-      "%28, %29, %30, %31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
-        "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
-        "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
-        "=r"(r[31])
-      : "r"(taddr));
-}
-__device__ __forceinline__ void tmem_wait_ld() {
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-}
-
-// tcgen05 shared-memory descriptor, 128-byte swizzle (layout type 2),
-// version 1, base offset 0 (operand tiles are 1024-byte aligned).
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
-  uint64_t d = 0;
-  d |= (uint64_t)((addr & 0x3FFFFu) >> 4);
-  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
-  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
-  d |= (uint64_t)1 << 46;
-  d |= (uint64_t)2 << 61;
-  return d;
-}
 
 // Instruction descriptor, kind::f16: f32 accumulate, bf16 A and B, B K-major,
 // A K-major (a_mn = 0) or MN-major (a_mn = 1), M = 128, N = n (<= 256).
@@ -552,11 +419,11 @@ __global__ void k_split3_bf16(const float* __restrict__ X, int64_t n, __nv_bfloa
     const __nv_bfloat162 a0 = __floats2bfloat162_rn(v.x, v.y);
     const float2 r1 = make_float2(v.x - __low2float(a0), v.y - __high2float(a0));
     const __nv_bfloat162 a1 = __floats2bfloat162_rn(r1.x, r1.y);
-    const __nv_bfloat162 a2 =
-        __floats2bfloat162_rn(r1.x - __low2float(a1), r1.y - __high2float(a1));
     reinterpret_cast<__nv_bfloat162*>(y0)[i] = a0;
     reinterpret_cast<__nv_bfloat162*>(y1)[i] = a1;
-    reinterpret_cast<__nv_bfloat162*>(y2)[i] = a2;
+    if (y2)   // the third plane is optional
+      reinterpret_cast<__nv_bfloat162*>(y2)[i] =
+          __floats2bfloat162_rn(r1.x - __low2float(a1), r1.y - __high2float(a1));
   }
   if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
     const float x = X[n - 1];
@@ -565,7 +432,7 @@ __global__ void k_split3_bf16(const float* __restrict__ X, int64_t n, __nv_bfloa
     const __nv_bfloat16 a1 = __float2bfloat16_rn(r1);
     y0[n - 1] = a0;
     y1[n - 1] = a1;
-    y2[n - 1] = __float2bfloat16_rn(r1 - __bfloat162float(a1));
+    if (y2) y2[n - 1] = __float2bfloat16_rn(r1 - __bfloat162float(a1));
   }
 }
 
@@ -599,7 +466,10 @@ __global__ void k_sum_partials(const float* __restrict__ partial, int splits, in
 }
 
 // ------------------------------------------------------------ host side
-PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() { return tma_encode_fn(); }
+}  // namespace
+
+PFN_cuTensorMapEncodeTiled_v12000 tma_encode_fn() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
   static std::once_flag once;
   std::call_once(once, [] {
@@ -612,6 +482,8 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   });
   return fn;
 }
+
+namespace {
 
 // barriers, TMEM slot, flags and the per-slice scale rows after the operands
 size_t tail_bytes(int n_pad) {
@@ -909,7 +781,7 @@ int tc_launch_split3(const float* X, int64_t n, __nv_bfloat16* x0, __nv_bfloat16
   TLGB_CHECK_ARG((reinterpret_cast<uintptr_t>(X) % 8) == 0 &&
                      (reinterpret_cast<uintptr_t>(x0) % 4) == 0 &&
                      (reinterpret_cast<uintptr_t>(x1) % 4) == 0 &&
-                     (reinterpret_cast<uintptr_t>(x2) % 4) == 0,
+                     (reinterpret_cast<uintptr_t>(x2) % 4) == 0,   // x2 may be null
                  "split3: misaligned buffers");
   k_split3_bf16<<<sm_count() * 8, 256, 0, st>>>(X, n, x0, x1, x2);
   TLGB_LAUNCH_CHECK();
@@ -1086,6 +958,7 @@ extern "C" int tlgb_set_tuning(const char* key, int value) {
   else if (k == "tc_test_starve") tc_tuning().test_starve = value;
   else if (k == "split_simt") tc_tuning().split_simt = value;
   else if (k == "full_solve") tc_tuning().full_solve = value;
+  else if (k == "closing_planes") tc_tuning().closing_planes = value;
   else return batched_set_tuning(k, value);   // the batched CP-ALS variants
   return TLGB_OK;
 }

@@ -46,6 +46,7 @@ struct TcTuning {
   int test_starve = 0;        // 1: tensor-core MTTKRP issues no copies (timeout-path test)
   int split_simt = 0;         // 1: non-negative / constrained CP keep the SIMT f32 MTTKRP
   int full_solve = 0;         // 1: bf16 CP-ALS sweeps solve with the double-float refinement
+  int closing_planes = 0;     // 3: the closing sweeps also contract the third tensor plane
 };
 TcTuning& tc_tuning();
 
@@ -82,7 +83,8 @@ int mttkrp_tc_launch_maps(const TcPlan& p, const TcMaps& maps, const float* cons
 int tc_launch_sum_partials(const TcPlan& p, const float* partial, float* out, cudaStream_t st);
 
 int tc_launch_to_bf16(const float* X, int64_t n, __nv_bfloat16* out, cudaStream_t st);
-// Exact split X = x0 + x1 + x2 into three bf16 tensors.
+// Exact split X = x0 + x1 + x2 into three bf16 tensors (x2 may be null: only
+// the first two planes are written).
 int tc_launch_split3(const float* X, int64_t n, __nv_bfloat16* x0, __nv_bfloat16* x1,
                      __nv_bfloat16* x2, cudaStream_t st);
 // out (planes x R x rows bf16, planes 2 or 3): the bf16 split of A^T,

@@ -59,10 +59,55 @@ class Generator:
         return X, feats, xnorm
 
 
+# The network's products run on the tensor cores (tlgb_ws_gemm_tc: operands
+# split exactly into three bf16 planes, the products of total order <= 2 with
+# f32 accumulation, f32-faithful) when every dimension is at least TC_MIN;
+# smaller ones, and every product when USE_TENSOR_CORES is False, on the SIMT
+# f32 kernel (tlgb_ws_gemm).
+USE_TENSOR_CORES = True
+TC_MIN = 64
+_tc_ws = {}
+
+
+def _gemm_workspace(device, nbytes):
+    """One workspace per device, grown as needed; its first int is the
+    kernel's status word (TLGB_ETIMEOUT if a bounded wait gave up)."""
+    key = (device.type, device.index)
+    ws = _tc_ws.get(key)
+    if ws is None or ws.numel() < nbytes:
+        old = None if ws is None else ws[:4].clone()
+        ws = torch.zeros(max(nbytes, 1 << 20), dtype=torch.uint8, device=device)
+        if old is not None:
+            ws[:4] = old      # keep a status recorded before the workspace grew
+        _tc_ws[key] = ws
+    return ws
+
+
+def gemm_status(device="cuda"):
+    """Raises GB300Error if a tensor-core GEMM on `device` recorded a timeout."""
+    device = torch.device(device)
+    ws = _tc_ws.get((device.type, device.index))
+    if ws is None:
+        return
+    st = ctypes.c_int(0)
+    _lib.check(_lib.lib().tlgb_workspace_status(ptr(ws), _stream(ws), ctypes.byref(st)))
+    if st.value != 0:
+        raise _lib.GB300Error(st.value, "tensor-core GEMM: a bounded pipeline wait expired")
+
+
 def _gemm(M, N, K, A, sam, sak, B, sbk, sbn, C, ldc, bias=None, relu=False, mask=None):
+    b = ptr(bias) if bias is not None else None
+    m = ptr(mask) if mask is not None else None
+    if USE_TENSOR_CORES and min(M, N, K) >= TC_MIN:
+        lib = _lib.lib()
+        nbytes = ctypes.c_size_t(0)
+        _lib.check(lib.tlgb_ws_gemm_tc_workspace_size(M, N, K, ctypes.byref(nbytes)))
+        ws = _gemm_workspace(C.device, nbytes.value)
+        _lib.check(lib.tlgb_ws_gemm_tc(M, N, K, ptr(A), sam, sak, ptr(B), sbk, sbn, ptr(C), ldc,
+                                       b, 1 if relu else 0, m, ptr(ws), ws.numel(), _stream(C)))
+        return
     _lib.check(_lib.lib().tlgb_ws_gemm(M, N, K, ptr(A), sam, sak, ptr(B), sbk, sbn, ptr(C), ldc,
-                                       ptr(bias) if bias is not None else None, 1 if relu else 0,
-                                       ptr(mask) if mask is not None else None, _stream(C)))
+                                       b, 1 if relu else 0, m, _stream(C)))
 
 
 class WarmStartNet:
@@ -164,6 +209,7 @@ class WarmStartNet:
             losses[s] = loss.mean()
             if log_every and (s + 1) % log_every == 0:
                 print(f"step {s + 1}/{steps}: loss {float(losses[s]):.4e}")
+        gemm_status(self.device)
         return losses.cpu().numpy()
 
     def loss(self, X, feats, xnorm):

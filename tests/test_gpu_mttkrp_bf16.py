@@ -137,13 +137,18 @@ def test_parafac_bf16_reaches_f64_fit(gb300):
     assert abs(errs[-1] - oerr[-1]) <= 1e-4 * oerr[-1], (errs[-1], oerr[-1])
 
 
+@pytest.mark.parametrize("planes", [3, 2])
 @pytest.mark.parametrize("shape,rank", [((64, 48, 40), 24), ((40, 24, 16, 32), 8),
                                         ((128, 96, 80), 64), ((32, 40, 48), 5)])
-def test_f32_split_sweep_matches_simt_f32(gb300, shape, rank):
-    """A sweep whose MTTKRPs run on the tensor cores with the exact three-plane
-    bf16 split of the f32 tensor (x0 . (f0+f1+f2) + x1 . (f0+f1) + x2 . f0)
-    matches the same sweep with the SIMT f32 MTTKRP to f32 accuracy, and both
-    match the f64 oracle sweep on the same f32 bytes."""
+def test_f32_split_sweep_matches_simt_f32(gb300, shape, rank, planes):
+    """A closing sweep whose MTTKRPs run on the tensor cores with the bf16
+    split of the f32 tensor and factor.  With three tensor planes
+    (x0 . (f0+f1+f2) + x1 . (f0+f1) + x2 . f0, tuning key closing_planes = 3)
+    it matches the same sweep with the SIMT f32 MTTKRP to f32 accuracy, and
+    both match the f64 oracle sweep on the same f32 bytes.  With the default
+    two (x2 dropped: the tensor enters with 16 significant bits) the factors
+    stay within 2e-4 of the f64 sweep's largest entry on this incoherent
+    random data and the error within 1e-4 (it is computed on the f32 tensor)."""
     import oracle
     from tensorly_gb300 import _lib
     lib = _lib.lib()
@@ -164,7 +169,11 @@ def test_f32_split_sweep_matches_simt_f32(gb300, shape, rank):
             lib.tlgb_set_tuning(b"refine_simt", 0)
         return [f.double().cpu().numpy() for f in cp.factors], errs[-1]
 
-    f_tc, e_tc = one_sweep(0)
+    try:
+        lib.tlgb_set_tuning(b"closing_planes", planes)
+        f_tc, e_tc = one_sweep(0)
+    finally:
+        lib.tlgb_set_tuning(b"closing_planes", 0)
     f_simt, e_simt = one_sweep(1)
     _, f_o, e_list = oracle.parafac_sweeps(x.astype(np.float64), np.ones(rank),
                                            [f.astype(np.float64) for f in init], 1)
@@ -173,9 +182,11 @@ def test_f32_split_sweep_matches_simt_f32(gb300, shape, rank):
         scale = np.abs(c).max()
         assert np.abs(a - c).max() <= 2e-4 * scale
         assert np.abs(b - c).max() <= 2e-4 * scale
-        # the split path is at least as close to f64 as the SIMT f32 path (x4 slack)
-        assert np.abs(a - c).max() <= 4 * np.abs(b - c).max() + 1e-6 * scale
-    assert abs(e_tc - e_o) <= 1e-5 * e_o and abs(e_simt - e_o) <= 1e-5 * e_o
+        if planes == 3:
+            # the split path is at least as close to f64 as the SIMT f32 path (x4 slack)
+            assert np.abs(a - c).max() <= 4 * np.abs(b - c).max() + 1e-6 * scale
+    assert abs(e_simt - e_o) <= 1e-5 * e_o
+    assert abs(e_tc - e_o) <= (1e-5 if planes == 3 else 1e-4) * e_o
 
 
 def test_parafac_reports_mttkrp_times(gb300):

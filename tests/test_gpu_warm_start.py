@@ -75,6 +75,52 @@ def test_gemm_layouts_with_epilogue(ws, layout):
     np.testing.assert_allclose(C.cpu().numpy(), want * (mask > 0), atol=1e-4)
 
 
+@pytest.mark.parametrize("layout", ["xwT", "dyTx", "dyW"])
+@pytest.mark.parametrize("shape", [(300, 260, 203), (512, 1024, 1536), (129, 64, 64)])
+def test_tensor_core_gemm_layouts_with_epilogue(ws, layout, shape):
+    """tlgb_ws_gemm_tc (exact three-plane bf16 split of both operands, the
+    products a_i b_j with i + j <= 2 on tcgen05, f32 accumulation) in the
+    network's three operand layouts, with ragged sizes (K not a multiple of 8,
+    M and N not multiples of 128) and the network's own; against f64 NumPy and
+    against the SIMT f32 kernel to 3e-5 of the largest entry: the operand
+    split is exact to 2^-26, what remains is the f32 accumulation over up to
+    1536 terms, which the tensor cores truncate (measured 1.2e-5 at K = 1536)."""
+    M, N, K = shape
+    rs = np.random.RandomState(M + N + K)
+    if layout == "xwT":
+        A = rs.randn(M, K); B = rs.randn(N, K)
+        args = (A, K, 1, B, 1, K)
+        want = A @ B.T
+    elif layout == "dyTx":
+        A = rs.randn(K, M); B = rs.randn(K, N)
+        args = (A, 1, M, B, N, 1)
+        want = A.T @ B
+    else:
+        A = rs.randn(M, K); B = rs.randn(K, N)
+        args = (A, K, 1, B, N, 1)
+        want = A @ B
+    bias = rs.randn(N)
+    mask = rs.randn(M, N)
+    dev = lambda a: torch.tensor(a, dtype=torch.float32, device="cuda").contiguous()
+    Ad, sam, sak, Bd, sbk, sbn = dev(args[0]), args[1], args[2], dev(args[3]), args[4], args[5]
+    C = torch.empty((M, N), dtype=torch.float32, device="cuda")
+    assert ws.USE_TENSOR_CORES and min(M, N, K) >= ws.TC_MIN
+    scale = np.abs(want).max()
+    ws._gemm(M, N, K, Ad, sam, sak, Bd, sbk, sbn, C, N, bias=dev(bias), relu=True)
+    c_tc = C.cpu().numpy()
+    assert np.abs(c_tc - np.maximum(want + bias, 0)).max() <= 3e-5 * scale
+    ws._gemm(M, N, K, Ad, sam, sak, Bd, sbk, sbn, C, N, mask=dev(mask))
+    assert np.abs(C.cpu().numpy() - want * (mask > 0)).max() <= 3e-5 * scale
+    try:
+        ws.USE_TENSOR_CORES = False
+        C2 = torch.empty_like(C)
+        ws._gemm(M, N, K, Ad, sam, sak, Bd, sbk, sbn, C2, N, bias=dev(bias), relu=True)
+    finally:
+        ws.USE_TENSOR_CORES = True
+    assert np.abs(c_tc - C2.cpu().numpy()).max() <= 3e-5 * scale
+    ws.gemm_status()
+
+
 def test_forward_backward_and_loss_match_oracle(ws, gen):
     net = ws.WarmStartNet(seed=3)
     X, feats, nrm = gen(np.arange(100, 164))
