@@ -536,6 +536,19 @@ int tlgb_cp_randomised_iteration(int dtype, const void* X, int ndim, const int64
                                  int64_t rank, void* const* factors, int64_t n_samples,
                                  const int64_t* indices, double* rec_error, void* workspace,
                                  size_t workspace_bytes, void* stream);
+/*
+ * The same iteration in two calls: cp_randomised_launch enqueues it on
+ * `stream` and returns (indices must stay valid until it has run);
+ * cp_randomised_finish waits for it and returns its checks and *rec_error,
+ * so the host can draw the next iteration's indices in between.
+ */
+int tlgb_cp_randomised_launch(int dtype, const void* X, int ndim, const int64_t* shape,
+                              int64_t rank, void* const* factors, int64_t n_samples,
+                              const int64_t* indices, void* workspace, size_t workspace_bytes,
+                              void* stream);
+int tlgb_cp_randomised_finish(int dtype, int ndim, const int64_t* shape, int64_t rank,
+                              int64_t n_samples, void* workspace, size_t workspace_bytes,
+                              double* rec_error, void* stream);
 
 /* constraint kinds of tlgb_cp_constrained / tlgb_proximal */
 #define TLGB_CONS_NONE 0

@@ -263,6 +263,12 @@ SIGNATURES = [
       ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     ("tlgb_inv_sqrt", ctypes.c_int,
      [ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p]),
+    ("tlgb_cp_randomised_launch", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, _c_i64p, ctypes.c_int64, _c_vpp,
+      ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    ("tlgb_cp_randomised_finish", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_int, _c_i64p, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p,
+      ctypes.c_size_t, ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]),
     ("tlgb_ws_gemm_tc_workspace_size", ctypes.c_int,
      [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_size_t)]),
     ("tlgb_ws_gemm_tc", ctypes.c_int,

@@ -10,7 +10,9 @@
 // every product a_i b_j with i + j <= 2 in TMEM with f32 accumulation; the
 // dropped terms are below 2^-26 of |a||b|, so the product is f32-faithful.
 //
-// One CTA per output tile, 192 threads:
+// One CTA per output tile and K split (split-K when the tiles alone would
+// leave SMs idle; the splits' raw tiles are then summed in a fixed order by
+// k_gemm_reduce, which applies the epilogue), 192 threads:
 //   warp 0      TMA producer: per 64-wide K step the six 128 x 64 bf16 tiles
 //               (three planes of A and of B; 96 KiB) into a ring of two stages
 //   warp 1      TMEM allocation (128 columns) and the single-thread MMA issue
@@ -42,6 +44,8 @@ constexpr size_t kGSmem = 1024 + (size_t)kGStages * kGStageBytes + 256;
 struct GemmArgs {
   int M, N;
   int ksteps;                 // 64-wide K steps (K padded to a multiple of 8 in the planes)
+  int kps;                    // K steps per split (blockIdx.z selects the split)
+  float* partial;             // splits > 1: raw tiles [split][M][N], reduced by k_gemm_reduce
   float* C;
   int64_t ldc;
   const float* bias;
@@ -69,6 +73,8 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUten
   int* ok_flag = reinterpret_cast<int*>(tmem_slot + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n0 = blockIdx.x * kGN, m0 = blockIdx.y * kGM;
+  const int t0 = blockIdx.z * a.kps;
+  const int t1 = min(t0 + a.kps, a.ksteps);
 
   if (threadIdx.x == 32) {
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmA)) : "memory");
@@ -102,7 +108,7 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUten
       int stage = 0;
       uint32_t phase = 0;
       int issued = 0;
-      for (int t = 0; t < a.ksteps; ++t) {
+      for (int t = t0; t < t1; ++t) {
         if (!mbar_wait(&empty[stage], phase ^ 1u, a.err, failed)) break;
         mbar_expect_tx(&full[stage], (uint32_t)kGStageBytes);
         unsigned char* dst = base + stage * kGStageBytes;
@@ -128,7 +134,7 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUten
     if (lane == 0) {
       int stage = 0;
       uint32_t phase = 0;
-      for (int t = 0; t < a.ksteps && !failed; ++t) {
+      for (int t = t0; t < t1 && !failed; ++t) {
         if (!mbar_wait(&full[stage], phase, a.err, failed)) break;
         tc_fence_after();
         const uint32_t sb = smem_u32(base + stage * kGStageBytes);
@@ -143,7 +149,7 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUten
             const uint32_t ad = sb + (uint32_t)(i * kGTile) + ko;
             const uint32_t bd = sb + (uint32_t)((kGPlanes + j) * kGTile) + ko;
             umma_bf16(tmem, smem_desc(ad, 16, 1024), smem_desc(bd, 16, 1024), kGemmIdesc,
-                      (t == 0 && k == 0 && q == 0) ? 0u : 1u);
+                      (t == t0 && k == 0 && q == 0) ? 0u : 1u);
           }
         }
         umma_commit(&empty[stage]);
@@ -170,7 +176,14 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUten
         uint32_t v[32];
         tmem_ld32_nowait(lane_addr + (uint32_t)(c * 32), v);
         tmem_wait_ld();
-        if (m < a.M) {
+        if (m < a.M && a.partial) {   // a split's raw tile; k_gemm_reduce finishes it
+          float* prow = a.partial + ((int64_t)blockIdx.z * a.M + m) * a.N;
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const int n = n0 + c * 32 + j;
+            if (n < a.N) prow[n] = __uint_as_float(v[j]);
+          }
+        } else if (m < a.M) {
           float* crow = a.C + (int64_t)m * a.ldc;
           const float* mrow = a.mask ? a.mask + (int64_t)m * a.ldc : nullptr;
 #pragma unroll
@@ -199,6 +212,23 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUten
   }
 }
 
+// C(m, n) = epi(sum over splits of partial[split][m][n]), in split order.
+__global__ void k_gemm_reduce(const float* __restrict__ partial, int splits, int M, int N,
+                              float* __restrict__ C, int64_t ldc, const float* __restrict__ bias,
+                              int relu, const float* __restrict__ mask) {
+  const int64_t n_el = (int64_t)M * N;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n_el;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int m = (int)(e / N), n = (int)(e - (e / N) * N);
+    float x = 0.f;
+    for (int s = 0; s < splits; ++s) x += partial[(int64_t)s * n_el + e];
+    if (bias) x += bias[n];
+    if (relu) x = fmaxf(x, 0.f);
+    if (mask && !(mask[(int64_t)m * ldc + n] > 0.f)) x = 0.f;
+    C[(int64_t)m * ldc + n] = x;
+  }
+}
+
 // out[p][r][k] (the three exact bf16 planes; K-major, row length kp) from
 // src(r, k) = src[r * s_r + k * s_k] for r < rows, k < K; zero for K <= k < kp.
 __global__ void k_gemm_split(const float* __restrict__ src, int rows, int K, int kp,
@@ -220,14 +250,23 @@ __global__ void k_gemm_split(const float* __restrict__ src, int rows, int K, int
 int64_t kpad(int K) { return ((int64_t)K + 7) / 8 * 8; }
 
 struct GemmLayout {
-  size_t a_off, b_off, bytes;
+  size_t a_off, b_off, p_off, bytes;
+  int ksteps, splits, kps;
 };
+// Split-K when the output has fewer tiles than SMs: splits of the K steps
+// over blockIdx.z bring the grid to about one CTA per SM (small products).
 GemmLayout gemm_layout(int M, int N, int K) {
   GemmLayout L{};
   const int64_t kp = kpad(K);
+  L.ksteps = (int)ceil_div(kp, (int64_t)kGK);
+  const int64_t tiles = ceil_div((int64_t)M, (int64_t)kGM) * ceil_div((int64_t)N, (int64_t)kGN);
+  const int want = (int)std::max<int64_t>(1, std::min<int64_t>(L.ksteps, sm_count() / tiles));
+  L.kps = (int)ceil_div((int64_t)L.ksteps, (int64_t)want);
+  L.splits = (int)ceil_div((int64_t)L.ksteps, (int64_t)L.kps);
   L.a_off = 256;   // the status word first
   L.b_off = L.a_off + align_up(sizeof(__nv_bfloat16) * kGPlanes * (size_t)M * kp, 256);
-  L.bytes = L.b_off + align_up(sizeof(__nv_bfloat16) * kGPlanes * (size_t)N * kp, 256);
+  L.p_off = L.b_off + align_up(sizeof(__nv_bfloat16) * kGPlanes * (size_t)N * kp, 256);
+  L.bytes = L.p_off + (L.splits > 1 ? align_up(sizeof(float) * L.splits * (size_t)M * N, 256) : 0);
   return L;
 }
 
@@ -298,15 +337,24 @@ extern "C" int tlgb_ws_gemm_tc(int M, int N, int K, const void* A, int64_t sam, 
   GemmArgs g{};
   g.M = M;
   g.N = N;
-  g.ksteps = (int)ceil_div(kp, (int64_t)kGK);
+  g.ksteps = L.ksteps;
+  g.kps = L.kps;
+  g.partial = L.splits > 1 ? reinterpret_cast<float*>(ws + L.p_off) : nullptr;
   g.C = static_cast<float*>(C);
   g.ldc = ldc;
   g.bias = static_cast<const float*>(bias);
   g.relu = relu;
   g.mask = static_cast<const float*>(mask);
   g.err = reinterpret_cast<int*>(ws);
-  dim3 grid((unsigned)ceil_div((int64_t)N, (int64_t)kGN), (unsigned)ceil_div((int64_t)M, (int64_t)kGM));
+  dim3 grid((unsigned)ceil_div((int64_t)N, (int64_t)kGN), (unsigned)ceil_div((int64_t)M, (int64_t)kGM),
+            (unsigned)L.splits);
   k_gemm_tc<<<grid, kGThreads, kGSmem, st>>>(ma, mb, g);
   TLGB_LAUNCH_CHECK();
+  if (L.splits > 1) {
+    const int64_t n_el = (int64_t)M * N;
+    k_gemm_reduce<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n_el, 256), sm_count() * 8)),
+                    256, 0, st>>>(g.partial, L.splits, M, N, g.C, ldc, g.bias, relu, g.mask);
+    TLGB_LAUNCH_CHECK();
+  }
   return TLGB_OK;
 }

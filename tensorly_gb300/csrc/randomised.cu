@@ -188,9 +188,8 @@ int rand_check(int dtype, int ndim, const int64_t* shape, int64_t rank, int64_t 
 }
 
 template <typename T>
-int rand_iteration(const T* X, int ndim, const int64_t* shape, int64_t R, T* const* factors,
-                   int64_t ns, const int64_t* indices, double* rec_error, void* ws,
-                   cudaStream_t st) {
+int rand_enqueue(const T* X, int ndim, const int64_t* shape, int64_t R, T* const* factors,
+                 int64_t ns, const int64_t* indices, void* ws, cudaStream_t st) {
   const int dtype = TypeCode<T>::value;
   const RandLayout L = rand_layout(dtype, ndim, shape, R, ns);
   char* base = static_cast<char*>(ws);
@@ -259,9 +258,18 @@ int rand_iteration(const T* X, int ndim, const int64_t* shape, int64_t R, T* con
   }
   const void* fp[kMaxModes];
   for (int k = 0; k < ndim; ++k) fp[k] = factors[k];
-  int rc = cp_full_run(dtype, ndim, shape, R, fp, nullptr, nullptr, nullptr, X, resid,
-                       base + L.rec, cp_full_ws_bytes(dtype, ndim, shape, R), st);
-  if (rc) return rc;
+  return cp_full_run(dtype, ndim, shape, R, fp, nullptr, nullptr, nullptr, X, resid,
+                     base + L.rec, cp_full_ws_bytes(dtype, ndim, shape, R), st);
+}
+
+// Waits for an enqueued iteration; its checks and the residual norm.
+int rand_finish(int dtype, int ndim, const int64_t* shape, int64_t R, int64_t ns,
+                double* rec_error, void* ws, cudaStream_t st) {
+  const RandLayout L = rand_layout(dtype, ndim, shape, R, ns);
+  char* base = static_cast<char*>(ws);
+  const AlsCtrl* ctrl = reinterpret_cast<const AlsCtrl*>(base + L.ctrl);
+  const double* resid = reinterpret_cast<const double*>(base + L.resid);
+  const int* bad = reinterpret_cast<const int*>(base + L.bad);
   struct { double resid; int bad; AlsCtrl ctrl; } h{};
   TLGB_CUDA_TRY(cudaMemcpyAsync(&h.resid, resid, sizeof(double), cudaMemcpyDeviceToHost, st));
   TLGB_CUDA_TRY(cudaMemcpyAsync(&h.bad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -290,12 +298,11 @@ extern "C" int tlgb_cp_randomised_workspace_size(int dtype, int ndim, const int6
   return TLGB_OK;
 }
 
-extern "C" int tlgb_cp_randomised_iteration(int dtype, const void* X, int ndim,
-                                            const int64_t* shape, int64_t rank,
-                                            void* const* factors, int64_t n_samples,
-                                            const int64_t* indices, double* rec_error,
-                                            void* workspace, size_t workspace_bytes,
-                                            void* stream) {
+extern "C" int tlgb_cp_randomised_launch(int dtype, const void* X, int ndim,
+                                         const int64_t* shape, int64_t rank,
+                                         void* const* factors, int64_t n_samples,
+                                         const int64_t* indices, void* workspace,
+                                         size_t workspace_bytes, void* stream) {
   clear_error();
   int rc = rand_check(dtype, ndim, shape, rank, n_samples);
   if (rc) return rc;
@@ -308,12 +315,38 @@ extern "C" int tlgb_cp_randomised_iteration(int dtype, const void* X, int ndim,
   if (rc) return rc;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (dtype == TLGB_F64)
-    return rand_iteration<double>(static_cast<const double*>(X), ndim, shape, rank,
-                                  reinterpret_cast<double* const*>(factors), n_samples, indices,
-                                  rec_error, workspace, st);
-  return rand_iteration<float>(static_cast<const float*>(X), ndim, shape, rank,
-                               reinterpret_cast<float* const*>(factors), n_samples, indices,
-                               rec_error, workspace, st);
+    return rand_enqueue<double>(static_cast<const double*>(X), ndim, shape, rank,
+                                reinterpret_cast<double* const*>(factors), n_samples, indices,
+                                workspace, st);
+  return rand_enqueue<float>(static_cast<const float*>(X), ndim, shape, rank,
+                             reinterpret_cast<float* const*>(factors), n_samples, indices,
+                             workspace, st);
+}
+
+extern "C" int tlgb_cp_randomised_iteration(int dtype, const void* X, int ndim,
+                                            const int64_t* shape, int64_t rank,
+                                            void* const* factors, int64_t n_samples,
+                                            const int64_t* indices, double* rec_error,
+                                            void* workspace, size_t workspace_bytes,
+                                            void* stream) {
+  int rc = tlgb_cp_randomised_launch(dtype, X, ndim, shape, rank, factors, n_samples, indices,
+                                     workspace, workspace_bytes, stream);
+  if (rc) return rc;
+  return rand_finish(dtype, ndim, shape, rank, n_samples, rec_error, workspace,
+                     static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int tlgb_cp_randomised_finish(int dtype, int ndim, const int64_t* shape,
+                                         int64_t rank, int64_t n_samples, void* workspace,
+                                         size_t workspace_bytes, double* rec_error,
+                                         void* stream) {
+  clear_error();
+  int rc = rand_check(dtype, ndim, shape, rank, n_samples);
+  if (rc) return rc;
+  if (!workspace || workspace_bytes < rand_layout(dtype, ndim, shape, rank, n_samples).bytes)
+    return set_error(TLGB_EWORKSPACE, "randomised_parafac: workspace too small");
+  return rand_finish(dtype, ndim, shape, rank, n_samples, rec_error, workspace,
+                     static_cast<cudaStream_t>(stream));
 }
 
 extern "C" int tlgb_sample_khatri_rao(int dtype, int n_mats, const void* const* mats,

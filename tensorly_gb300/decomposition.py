@@ -1018,10 +1018,14 @@ def randomised_parafac(tensor, rank, n_samples, n_iter_max=100, init="random",
     signature, stop rules and returns.
 
     Per iteration the host draws every mode's sample indices with NumPy's
-    RandomState in the reference's order; ``tlgb_cp_randomised_iteration``
-    then runs the mode updates (sampled Khatri-Rao rows, sampled unfolding,
-    the normal equations of the sampled least-squares problem) and the
-    reconstruction error ||X - [[A]]|| without forming the full tensor."""
+    RandomState in the reference's order; ``tlgb_cp_randomised_launch``
+    then enqueues the mode updates (sampled Khatri-Rao rows, sampled
+    unfolding, the normal equations of the sampled least-squares problem)
+    and the reconstruction error ||X - [[A]]|| without forming the full
+    tensor.  While the GPU runs them, the next iteration's indices are drawn
+    from a copy of the generator; ``tlgb_cp_randomised_finish`` returns the
+    error, and the copy's state becomes the generator's only if the loop
+    goes on, so the draws are the reference's whatever iteration stops."""
     x, placement = to_device(tensor)
     code = dtype_code(x)
     x = x.contiguous()
@@ -1049,17 +1053,39 @@ def randomised_parafac(tensor, rank, n_samples, n_iter_max=100, init="random",
     ws = workspace(nbytes.value, x.device)
     fptrs = (ctypes.c_void_p * n_dims)(*[f.data_ptr() for f in factors])
     rec = ctypes.c_double(0.0)
-    for iteration in range(n_iter_max):
+
+    def draw(gen):
         idx = np.empty((n_dims, n_dims - 1, n_samples), dtype=np.int64)
         for mode in range(n_dims):
             others = [k for k in range(n_dims) if k != mode]
             for q, k in enumerate(others):          # sample_khatri_rao(..., random_state=rng)
-                idx[mode, q] = rng.randint(0, x.shape[k], size=n_samples, dtype=int)
-        d_idx = torch.from_numpy(idx).to(x.device)
-        _lib.check(lib.tlgb_cp_randomised_iteration(code, x.data_ptr(), n_dims, shape, rank,
-                                                    fptrs, int(n_samples), d_idx.data_ptr(),
-                                                    ctypes.byref(rec), ptr(ws), ws.numel(),
-                                                    stream_of(x)))
+                idx[mode, q] = gen.randint(0, x.shape[k], size=n_samples, dtype=int)
+        return idx
+
+    def fork(gen):
+        twin = np.random.RandomState()
+        twin.set_state(gen.get_state())
+        return twin
+
+    idx_host = torch.empty((n_dims, n_dims - 1, n_samples), dtype=torch.int64).pin_memory()
+    d_idx = torch.empty(idx_host.shape, dtype=torch.int64, device=x.device)
+    ahead, ahead_idx = None, None
+    for iteration in range(n_iter_max):
+        if ahead is not None:                        # the loop goes on: keep the early draws
+            rng.set_state(ahead.get_state())
+            idx = ahead_idx
+        else:
+            idx = draw(rng)
+        idx_host.copy_(torch.from_numpy(idx))
+        d_idx.copy_(idx_host, non_blocking=True)
+        _lib.check(lib.tlgb_cp_randomised_launch(code, x.data_ptr(), n_dims, shape, rank, fptrs,
+                                                 int(n_samples), d_idx.data_ptr(), ptr(ws),
+                                                 ws.numel(), stream_of(x)))
+        ahead = fork(rng) if iteration + 1 < n_iter_max else None
+        ahead_idx = draw(ahead) if ahead is not None else None
+        _lib.check(lib.tlgb_cp_randomised_finish(code, n_dims, shape, rank, int(n_samples),
+                                                 ptr(ws), ws.numel(), ctypes.byref(rec),
+                                                 stream_of(x)))
         rec_error = rec.value / norm_tensor
         if callback is not None:
             if callback(cp_now(), rec_error) is True:
