@@ -223,7 +223,8 @@ typedef struct tlgb_cp_als_options {
                               (tensor cores on the exact 3-plane bf16 split of X and
                               the factor when rank <= 64, else the SIMT f32 kernel) */
   int check_every;         /* sweeps between host reads of the device stop flag (>= 1) */
-  int use_graph;           /* replay one captured sweep as a CUDA graph */
+  int use_graph;           /* 1: replay groups of captured sweeps as CUDA graphs; 0 (default):
+                              launch the sweeps directly, a group ahead of the host's reads */
   tlgb_sweep_callback callback;  /* per-sweep hook (parafac callback) or NULL */
   void* callback_user;
   /* Optional (NULL = off), host, TLGB_CP_ALS_SWEEP_KINDS x TLGB_MAX_MODES

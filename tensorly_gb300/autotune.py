@@ -114,13 +114,13 @@ def _set_key(key, value):
     _lib.check(_lib.lib().tlgb_set_tuning(key.encode(), int(value)))
 
 
-def _time_dense(x, rank, init, sweeps, reps):
+def _time_dense(x, rank, init, sweeps, reps, refine_sweeps):
     from .cp_tensor import CPTensor
     from .decomposition import parafac
 
     def run():
         parafac(x, rank, init=CPTensor((None, [f.clone() for f in init])), n_iter_max=sweeps,
-                tol=0, precision="bf16", refine_sweeps=0)
+                tol=0, precision="bf16", refine_sweeps=refine_sweeps)
     run()
     st = torch.cuda.current_stream()
     a = torch.cuda.Event(enable_timing=True)
@@ -133,14 +133,18 @@ def _time_dense(x, rank, init, sweeps, reps):
     return a.elapsed_time(b) / reps
 
 
-def tune_dense(x, rank, sweeps=12, reps=3, min_gain=0.01, verbose=False):
+def tune_dense(x, rank, sweeps=50, refine_sweeps=3, reps=2, min_gain=0.01, verbose=False):
     """Pick the tensor-core MTTKRP's inner-mode group size, ring depth and
     wave count for bf16 CP-ALS of the f32 CUDA tensor ``x`` at ``rank`` by a
     coordinate search over ``DENSE_SPACE`` (the defaults first); a value
     replaces the current one only if it is at least ``min_gain`` faster, so
-    timing noise does not move the choice.  Returns {key: value} and leaves
-    it set.  Cached per device, shape and rank."""
-    key = (torch.cuda.get_device_name(x.device), tuple(x.shape), int(rank))
+    timing noise does not move the choice.  Each candidate is timed on whole
+    ``parafac`` calls of ``sweeps`` sweeps, the last ``refine_sweeps`` of them
+    f32 closing sweeps (the tile choice also sets their three-plane plans),
+    so the mix is that of the run being tuned.  Returns {key: value} and
+    leaves it set.  Cached per device, shape, rank and sweep mix."""
+    key = (torch.cuda.get_device_name(x.device), tuple(x.shape), int(rank), int(sweeps),
+           int(refine_sweeps))
     if key in _dense_cache:
         for k, v in _dense_cache[key].items():
             _set_key(k, v)
@@ -151,7 +155,7 @@ def tune_dense(x, rank, sweeps=12, reps=3, min_gain=0.01, verbose=False):
     choice = dict(DENSE_DEFAULT)
     for k, v in choice.items():
         _set_key(k, v)
-    best_ms = _time_dense(x, rank, init, sweeps, reps)
+    best_ms = _time_dense(x, rank, init, sweeps, reps, refine_sweeps)
     if verbose:
         print(f"dense defaults {choice}: {best_ms:.3f} ms")
     for k, values in DENSE_SPACE:
@@ -160,7 +164,7 @@ def tune_dense(x, rank, sweeps=12, reps=3, min_gain=0.01, verbose=False):
                 continue
             _set_key(k, v)
             try:
-                ms = _time_dense(x, rank, init, sweeps, reps)
+                ms = _time_dense(x, rank, init, sweeps, reps, refine_sweeps)
             except NotImplementedError:     # the plan does not fit with this value
                 ms = float("inf")
             if verbose:

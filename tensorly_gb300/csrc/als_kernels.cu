@@ -133,10 +133,14 @@ __global__ void k_gram_partial(const T* __restrict__ A, int64_t I, int R, int64_
 // reduces those on or below the diagonal, so every load is coalesced; its 8
 // warps take every 8th partial, then the warps' sums are combined in a fixed
 // order.  df: the partials are (hi, lo) f32 planes, summed on the f32 pipe
-// (Neumaier for hi, plain for lo) with one conversion at the end.
+// (Neumaier for hi, plain for lo) with one conversion at the end; df == 2:
+// only the hi planes were written (the lite solve's f32 Gram).
+// G32 (optional): the entry's f32 (hi, lo) split as well, hi at G32[e] and lo
+// at G32[R^2 + e].
 // Returns the reduced entry in warp 0's lanes that own one (0 elsewhere).
 __device__ __forceinline__ double gram_reduce_block(const double* __restrict__ gpart, int nparts,
-                                                   int R, double* G, int df) {
+                                                   int R, double* G, int df,
+                                                   float* G32 = nullptr) {
   __shared__ double red[8][33];
   const int RR = R * R;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -145,16 +149,25 @@ __device__ __forceinline__ double gram_reduce_block(const double* __restrict__ g
   const bool mine = e < RR && s <= r;
   double part = 0.0;
   if (df) {
+    // sixteen partials of a warp in flight per batch (one L2 round trip each)
     float h = 0.f, c = 0.f, l = 0.f;
     if (mine) {
       const float* gp = reinterpret_cast<const float*>(gpart);
-#pragma unroll 4
-      for (int p = warp; p < nparts; p += 8) {
-        const float v = gp[(int64_t)p * 2 * RR + e];
-        l += gp[(int64_t)p * 2 * RR + RR + e];
-        const float t = h + v;
-        c += (fabsf(h) >= fabsf(v)) ? ((h - t) + v) : ((v - t) + h);
-        h = t;
+      for (int p0 = warp; p0 < nparts; p0 += 8 * 16) {
+        float v[16], lo[16];
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+          const int p = p0 + 8 * u;
+          v[u] = (p < nparts) ? gp[(int64_t)p * 2 * RR + e] : 0.f;
+          lo[u] = (p < nparts && df == 1) ? gp[(int64_t)p * 2 * RR + RR + e] : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+          l += lo[u];
+          const float t = h + v[u];
+          c += (fabsf(h) >= fabsf(v[u])) ? ((h - t) + v[u]) : ((v[u] - t) + h);
+          h = t;
+        }
       }
     }
     part = (double)h + (double)(c + l);
@@ -177,15 +190,24 @@ __device__ __forceinline__ double gram_reduce_block(const double* __restrict__ g
     for (int w = 0; w < 8; ++w) t += red[w][lane];
     G[e] = t;
     if (s < r) G[s * R + r] = t;
+    if (G32) {
+      const float h = (float)t, l = (float)(t - (double)h);
+      G32[e] = h;
+      G32[RR + e] = l;
+      if (s < r) {
+        G32[s * R + r] = h;
+        G32[RR + s * R + r] = l;
+      }
+    }
   }
   return t;
 }
 
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 4)   // <= 64 registers: fits beside an MTTKRP CTA
 k_gram_reduce(const double* __restrict__ gpart, int nparts, int R, double* G, const int* done,
-              int df) {
+              int df, float* G32) {
   if (done && *done) return;
-  gram_reduce_block(gpart, nparts, R, G, df);
+  gram_reduce_block(gpart, nparts, R, G, df, G32);
 }
 
 // ---------------------------------------------------------------- factorisation
@@ -205,108 +227,280 @@ __device__ void build_v(double* V, const double* G, int ndim, int mode, int R, c
 }
 
 // ---- fast path: f32 Gauss-Jordan inverse of V, matrix held in registers.
-// Thread (ti, tj) of a TI x TJ grid owns rows ti + TI*u and columns tj + TJ*v;
-// per pivot only row k and column k pass through shared memory.  No dynamic
-// shared memory and few threads, so the kernel can share an SM with the
-// tensor-core MTTKRP it runs beside.  Pivots of Gauss-Jordan are the Schur
-// complement pivots, so their spread bounds cond(V) from below; a spread
-// above kIrMaxPivotRatio (or a non-positive pivot) hands V to the f64 kernel.
+// Thread (ti, tj) of a TI x TJ grid owns rows ti + TI*u and columns tj + TJ*v
+// of the matrix padded to n = TI*NI = TJ*NJ (identity beyond R).  Pivots of
+// Gauss-Jordan are the Schur complement pivots, so their spread bounds
+// cond(V) from below; a spread above kIrMaxPivotRatio (or a non-positive
+// pivot) hands V to the f64 kernel.
+//
+// Blocked by kGjBlock pivots: one warp inverts the diagonal block D of the
+// current Schur complement with shuffles (no block barrier between its
+// pivots), then with the block column C and block row P (shared memory)
+// every thread applies the block step to the elements it owns:
+//   block rows: D^-1 P (and D^-1 in the block's columns);
+//   other rows: A - C (D^-1 P), and -C D^-1 in the block's columns.
+// Four barriers per block instead of two per pivot.
+//
+// V: in double-float on the f32 pipe from the Grams' f32 (hi, lo) planes when
+// they are given and the solve takes V's planes only (f32 factors with
+// R <= kSolveDfMaxRank), else in f64 (this GPU's f64 pipe is far slower, so
+// the f64 build is most of the kernel's time when it runs).
 constexpr float kIrMaxPivotRatio = 1e5f;
+constexpr int kGjBlock = 16;
+
+// (h, l) *= (bh, bl), double-float product (~2^-46 relative).
+__device__ __forceinline__ void df_mul(float& h, float& l, float bh, float bl) {
+  const float p = h * bh;
+  float e = fmaf(h, bh, -p);
+  e = fmaf(h, bl, e);
+  e = fmaf(l, bh, e);
+  const float t = p + e;
+  l = e - (t - p);
+  h = t;
+}
+// (h, l) += (bh, bl), double-float sum.
+__device__ __forceinline__ void df_add(float& h, float& l, float bh, float bl) {
+  const float t = h + bh;
+  const float bb = t - h;
+  float e = (h - (t - bb)) + (bh - bb);
+  e += l + bl;
+  const float u = t + e;
+  l = e - (u - t);
+  h = u;
+}
 
 template <typename T, int TI, int TJ, int NI, int NJ>
 __global__ void __launch_bounds__(TI * TJ)
-k_factorize_fast(const double* __restrict__ G, int ndim, int mode, int R,
-                 const T* __restrict__ w, double l2, double* __restrict__ vmat,
+k_factorize_fast(const double* __restrict__ G, const float* __restrict__ G32, int ndim, int mode,
+                 int R, const T* __restrict__ w, double l2, double* __restrict__ vmat,
                  float* __restrict__ w32, AlsCtrl* ctrl) {
+  constexpr int N = TI * NI;
+  constexpr int B = kGjBlock;
+  constexpr int NT = TI * TJ;
+  static_assert(TJ * NJ == N && N % B == 0, "padded order must be a multiple of the block");
   if (ctrl->done) return;
-  __shared__ float rowk[NJ * TJ], colk[NI * TI];
-  __shared__ double wsh[NI * TI];
-  const int ti = threadIdx.x / TJ, tj = threadIdx.x - (threadIdx.x / TJ) * TJ;
+  __shared__ __align__(16) float sC[N][B];   // block column of the current Schur complement
+  __shared__ __align__(16) float sP[B][N];   // block row
+  __shared__ __align__(16) float sT[B][N];   // D^-1 P (D^-1 itself in the block's columns)
+  __shared__ float sD[B][B];                 // D^-1
+  __shared__ double wsh[N];
+  __shared__ int s_ok;
+  const int tid = threadIdx.x;
+  const int ti = tid / TJ, tj = tid - (tid / TJ) * TJ;
   const int RR = R * R;
-  for (int t = threadIdx.x; t < R; t += TI * TJ) wsh[t] = w ? (double)w[t] : 1.0;
-  __syncthreads();
-  // V = (prod_{k != mode} G_k + l2 I) * w w^T in f64, a chunk of rows at a
-  // time with every Gram load of the chunk issued before any use (they come
-  // from L2; issued one by one they would serialise on its latency).
-  constexpr int UB = (32 / NJ) > 0 ? (32 / NJ) : 1;
+  const bool dfv = (sizeof(T) == 4) && G32 != nullptr && R <= kSolveDfMaxRank;
   float a[NI][NJ];
+  if (dfv) {
+    // V = (prod_{k != mode} G_k + l2 I) * w w^T in double-float; the planes of
+    // a row chunk are all loaded before the products that use them
+    const float l2h = (float)l2, l2l = (float)(l2 - (double)l2h);
+    constexpr int UB = (16 / NJ) > 0 ? (16 / NJ) : 1;
 #pragma unroll
-  for (int u0 = 0; u0 < NI; u0 += UB) {
-    double g[UB][NJ];
+    for (int u0 = 0; u0 < NI; u0 += UB) {
+      float vh[UB][NJ], vl[UB][NJ];
 #pragma unroll
-    for (int u = 0; u < UB; ++u)
+      for (int u = 0; u < UB; ++u)
 #pragma unroll
-      for (int v = 0; v < NJ; ++v) g[u][v] = 1.0;
-    for (int k = 0; k < ndim; ++k) {
-      if (k == mode) continue;
-      const double* Gk = G + (int64_t)k * RR;
+        for (int v = 0; v < NJ; ++v) { vh[u][v] = 1.f; vl[u][v] = 0.f; }
+      for (int k = 0; k < ndim; ++k) {
+        if (k == mode) continue;
+        const float* gh = G32 + (int64_t)k * 2 * RR;
+        float bh[UB][NJ], bl[UB][NJ];
+#pragma unroll
+        for (int u = 0; u < UB; ++u)
+#pragma unroll
+          for (int v = 0; v < NJ; ++v) {
+            const int i = ti + TI * (u0 + u), j = tj + TJ * v;
+            const bool in = u0 + u < NI && i < R && j < R;
+            bh[u][v] = in ? gh[i * R + j] : 1.f;
+            bl[u][v] = in ? gh[RR + i * R + j] : 0.f;
+          }
+#pragma unroll
+        for (int u = 0; u < UB; ++u)
+#pragma unroll
+          for (int v = 0; v < NJ; ++v) df_mul(vh[u][v], vl[u][v], bh[u][v], bl[u][v]);
+      }
 #pragma unroll
       for (int u = 0; u < UB; ++u)
 #pragma unroll
         for (int v = 0; v < NJ; ++v) {
+          if (u0 + u >= NI) continue;
           const int i = ti + TI * (u0 + u), j = tj + TJ * v;
-          if (u0 + u < NI && i < R && j < R) g[u][v] *= Gk[i * R + j];
+          float h = 0.f;
+          if (i < R && j < R) {
+            float l = vl[u][v];
+            h = vh[u][v];
+            if (i == j) df_add(h, l, l2h, l2l);
+            if (w) {
+              df_mul(h, l, (float)w[i], 0.f);
+              df_mul(h, l, (float)w[j], 0.f);
+            }
+            w32[RR + i * R + j] = h;
+            w32[2 * RR + i * R + j] = l;
+          }
+          a[u0 + u][v] = h;
         }
     }
-#pragma unroll
-    for (int u = 0; u < UB; ++u)
-#pragma unroll
-      for (int v = 0; v < NJ; ++v) {
-        if (u0 + u >= NI) continue;
-        const int i = ti + TI * (u0 + u), j = tj + TJ * v;
-        float val = 0.f;
-        if (i < R && j < R) {
-          double gv = g[u][v];
-          if (i == j) gv = gv + l2;
-          gv = (wsh[i] * gv) * wsh[j];
-          vmat[i * R + j] = gv;
-          val = (float)gv;
-          // f32 (hi, lo) planes of V after W in w32, for the double-float solve
-          w32[R * R + i * R + j] = val;
-          w32[2 * R * R + i * R + j] = (float)(gv - (double)val);
-        }
-        a[u0 + u][v] = val;
-      }
-  }
-  float pmin = 3.0e38f, pmax = 0.f;
-  bool ok = true;
-  for (int k = 0; k < R; ++k) {
-    const int ku = k / TI, kv = k / TJ;
-    if (k - ku * TI == ti) {
-#pragma unroll
-      for (int u = 0; u < NI; ++u)
-        if (u == ku)
-#pragma unroll
-          for (int v = 0; v < NJ; ++v) rowk[tj + TJ * v] = a[u][v];
-    }
-    if (k - kv * TJ == tj) {
-#pragma unroll
-      for (int v = 0; v < NJ; ++v)
-        if (v == kv)
-#pragma unroll
-          for (int u = 0; u < NI; ++u) colk[ti + TI * u] = a[u][v];
-    }
+  } else {
+    for (int t = tid; t < R; t += NT) wsh[t] = w ? (double)w[t] : 1.0;
     __syncthreads();
-    const float p = rowk[k];
-    if (!(p > 0.f)) { ok = false; break; }  // uniform: every thread read the same p
-    pmin = fminf(pmin, p);
-    pmax = fmaxf(pmax, p);
-    const float inv = __frcp_rn(p);
+    // V in f64, a chunk of rows at a time with every Gram load of the chunk
+    // issued before any use (they come from L2; issued one by one they would
+    // serialise on its latency)
+    constexpr int UB = (32 / NJ) > 0 ? (32 / NJ) : 1;
+#pragma unroll
+    for (int u0 = 0; u0 < NI; u0 += UB) {
+      double g[UB][NJ];
+#pragma unroll
+      for (int u = 0; u < UB; ++u)
+#pragma unroll
+        for (int v = 0; v < NJ; ++v) g[u][v] = 1.0;
+      for (int k = 0; k < ndim; ++k) {
+        if (k == mode) continue;
+        const double* Gk = G + (int64_t)k * RR;
+#pragma unroll
+        for (int u = 0; u < UB; ++u)
+#pragma unroll
+          for (int v = 0; v < NJ; ++v) {
+            const int i = ti + TI * (u0 + u), j = tj + TJ * v;
+            if (u0 + u < NI && i < R && j < R) g[u][v] *= Gk[i * R + j];
+          }
+      }
+#pragma unroll
+      for (int u = 0; u < UB; ++u)
+#pragma unroll
+        for (int v = 0; v < NJ; ++v) {
+          if (u0 + u >= NI) continue;
+          const int i = ti + TI * (u0 + u), j = tj + TJ * v;
+          float val = 0.f;
+          if (i < R && j < R) {
+            double gv = g[u][v];
+            if (i == j) gv = gv + l2;
+            gv = (wsh[i] * gv) * wsh[j];
+            vmat[i * R + j] = gv;
+            val = (float)gv;
+            // f32 (hi, lo) planes of V after W in w32, for the double-float solve
+            w32[RR + i * R + j] = val;
+            w32[2 * RR + i * R + j] = (float)(gv - (double)val);
+          }
+          a[u0 + u][v] = val;
+        }
+    }
+  }
+  // identity beyond R
+#pragma unroll
+  for (int u = 0; u < NI; ++u)
+#pragma unroll
+    for (int v = 0; v < NJ; ++v) {
+      const int i = ti + TI * u, j = tj + TJ * v;
+      if (i >= R || j >= R) a[u][v] = (i == j) ? 1.f : 0.f;
+    }
+  if (tid == 0) s_ok = 1;
+  float pmin = 3.0e38f, pmax = 0.f;   // warp 0
+  const int warp = tid >> 5, lane = tid & 31;
+  for (int k0 = 0; k0 < N; k0 += B) {
+    // the block column and row of the current Schur complement
 #pragma unroll
     for (int u = 0; u < NI; ++u) {
       const int i = ti + TI * u;
-      const float fi = colk[i] * inv;
 #pragma unroll
       for (int v = 0; v < NJ; ++v) {
         const int j = tj + TJ * v;
-        const float rj = rowk[j];
-        const float upd = fmaf(-fi, rj, a[u][v]);
-        a[u][v] = (i == k) ? ((j == k) ? inv : a[u][v] * inv) : ((j == k) ? -fi : upd);
+        if ((unsigned)(j - k0) < (unsigned)B) sC[i][j - k0] = a[u][v];
+        if ((unsigned)(i - k0) < (unsigned)B) sP[i - k0][j] = a[u][v];
       }
     }
     __syncthreads();
+    if (warp == 0) {
+      // D^-1 by scalar Gauss-Jordan: lane l holds row l & 15, columns
+      // (l >> 4) * 8 .. + 7; entry (x, y) lives in lane x + 16 * (y >> 3),
+      // register y & 7
+      const int r = lane & 15, c0 = (lane >> 4) * 8;
+      float d[8];
+#pragma unroll
+      for (int m = 0; m < 8; ++m) d[m] = sP[r][k0 + c0 + m];
+      bool ok = true;
+#pragma unroll
+      for (int k = 0; k < B; ++k) {
+        const int hi = (k >> 3) << 4;
+        const float dk = d[k & 7];
+        const float p = __shfl_sync(0xffffffffu, dk, k + hi);
+        const float ck = __shfl_sync(0xffffffffu, dk, r + hi);
+        float rk[8];
+#pragma unroll
+        for (int m = 0; m < 8; ++m) rk[m] = __shfl_sync(0xffffffffu, d[m], k + (lane & 16));
+        if (!(p > 0.f)) ok = false;   // the same p in every lane
+        if (k0 + k < R) {
+          pmin = fminf(pmin, p);
+          pmax = fmaxf(pmax, p);
+        }
+        const float inv = __frcp_rn(p);
+        const float fi = ck * inv;
+#pragma unroll
+        for (int m = 0; m < 8; ++m) {
+          const int col = c0 + m;
+          const float upd = fmaf(-fi, rk[m], d[m]);
+          d[m] = (r == k) ? ((col == k) ? inv : d[m] * inv) : ((col == k) ? -fi : upd);
+        }
+      }
+#pragma unroll
+      for (int m = 0; m < 8; ++m) sD[r][c0 + m] = d[m];
+      if (lane == 0 && !ok) s_ok = 0;
+    }
+    __syncthreads();
+    if (!s_ok) break;   // uniform
+    for (int e = tid; e < B * N; e += NT) {
+      const int m = e / N, j = e - (e / N) * N;
+      float t;
+      if ((unsigned)(j - k0) < (unsigned)B) {
+        t = sD[m][j - k0];
+      } else {
+        float t0 = 0.f, t1 = 0.f;
+#pragma unroll
+        for (int q = 0; q < B; q += 2) {
+          t0 = fmaf(sD[m][q], sP[q][j], t0);
+          t1 = fmaf(sD[m][q + 1], sP[q + 1][j], t1);
+        }
+        t = t0 + t1;
+      }
+      sT[m][j] = t;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < NI; ++u) {
+      const int i = ti + TI * u;
+      if ((unsigned)(i - k0) < (unsigned)B) continue;
+#pragma unroll
+      for (int v = 0; v < NJ; ++v) {
+        const int j = tj + TJ * v;
+        if ((unsigned)(j - k0) < (unsigned)B) a[u][v] = 0.f;
+      }
+    }
+#pragma unroll 4
+    for (int m = 0; m < B; ++m) {
+      float cv[NI], tv[NJ];
+#pragma unroll
+      for (int u = 0; u < NI; ++u) cv[u] = sC[ti + TI * u][m];
+#pragma unroll
+      for (int v = 0; v < NJ; ++v) tv[v] = sT[m][tj + TJ * v];
+#pragma unroll
+      for (int u = 0; u < NI; ++u)
+#pragma unroll
+        for (int v = 0; v < NJ; ++v) a[u][v] = fmaf(-cv[u], tv[v], a[u][v]);
+    }
+#pragma unroll
+    for (int u = 0; u < NI; ++u) {
+      const int i = ti + TI * u;
+      if ((unsigned)(i - k0) < (unsigned)B)
+#pragma unroll
+        for (int v = 0; v < NJ; ++v) a[u][v] = sT[i - k0][tj + TJ * v];
+    }
+    __syncthreads();   // sC, sP, sT are rewritten by the next block
   }
-  if (ok && pmax > kIrMaxPivotRatio * pmin) ok = false;
+  __shared__ float s_pr[2];
+  if (tid == 0) { s_pr[0] = pmin; s_pr[1] = pmax; }
+  __syncthreads();
+  const bool ok = s_ok && !(s_pr[1] > kIrMaxPivotRatio * s_pr[0]);
   if (ok) {
 #pragma unroll
     for (int u = 0; u < NI; ++u)
@@ -316,7 +510,7 @@ k_factorize_fast(const double* __restrict__ G, int ndim, int mode, int R,
         if (i < R && j < R) w32[i * R + j] = a[u][v];
       }
   }
-  if (threadIdx.x == 0) ctrl->fac_kind = ok ? 2 : 3;
+  if (tid == 0) ctrl->fac_kind = ok ? 2 : 3;
 }
 
 // ---- fallback: f64 Cholesky (fac_kind 0) or LU with partial pivoting
@@ -458,6 +652,21 @@ __device__ __forceinline__ double store_entry(T* A, __nv_bfloat16* A_bt, int64_t
   return xd;
 }
 
+// store_entry for f32 factors with the value already in f32 (the lite solve).
+__device__ __forceinline__ void store_entry_f32(float* A, __nv_bfloat16* A_bt, int64_t I, int R,
+                                                int64_t row, int r, float x) {
+  A[row * R + r] = x;
+  if (A_bt) {
+    const __nv_bfloat16 p0 = __float2bfloat16_rn(x);
+    const float r1 = x - __bfloat162float(p0);
+    const __nv_bfloat16 p1 = __float2bfloat16_rn(r1);
+    const int64_t plane = (int64_t)R * I, at = (int64_t)r * I + row;
+    A_bt[at] = p0;
+    A_bt[plane + at] = p1;
+    A_bt[2 * plane + at] = __float2bfloat16_rn(r1 - __bfloat162float(p1));
+  }
+}
+
 // gacc += sum over `nrows` rows of a a^T, lower triangle only; the entry
 // index advances without integer division.
 __device__ __forceinline__ void gram_update(double* gacc, const double* rows, int nrows, int R) {
@@ -528,8 +737,9 @@ __device__ __forceinline__ void gram_update_f32(float* g, const float* rows, int
 // Sum of the MTTKRP split partials of one entry.  f32 partials: compensated
 // f32 summation (Neumaier), whose error (~splits * 2^-48) is far below the
 // partials' own rounding, on the f32 pipe (the f64 pipe is ~70x slower here).
-__device__ __forceinline__ double sum_splits(const float* __restrict__ partial, int splits,
-                                             int64_t stride, int64_t off) {
+__device__ __forceinline__ void sum_splits_sc(const float* __restrict__ partial, int splits,
+                                              int64_t stride, int64_t off, float& s_out,
+                                              float& c_out) {
   float s = 0.f, c = 0.f;
   int p = 0;
   // eighteen loads in flight per batch: the partials come from L2 and a
@@ -562,6 +772,13 @@ __device__ __forceinline__ double sum_splits(const float* __restrict__ partial, 
     c += (fabsf(s) >= fabsf(x)) ? ((s - t) + x) : ((x - t) + s);
     s = t;
   }
+  s_out = s;
+  c_out = c;
+}
+__device__ __forceinline__ double sum_splits(const float* __restrict__ partial, int splits,
+                                             int64_t stride, int64_t off) {
+  float s, c;
+  sum_splits_sc(partial, splits, stride, off, s, c);
   return (double)s + (double)c;
 }
 
@@ -598,9 +815,10 @@ k_solve(const T* __restrict__ partial, int splits, int64_t I, int R_in,
         __nv_bfloat16* A_bt, double* gpart, double* ipart, AlsCtrl* ctrl, int64_t rpb,
         int mats_in_smem, int max_passes, int lite_in) {
   const int R = (RT > 0) ? RT : R_in;
-  griddep_wait();   // the MTTKRP partials (programmatic launch inside a sweep)
-  griddep_launch_dependents();
-  if (ctrl->done) return;
+  // Up to the first read of the partials, nothing here reads what the
+  // programmatic predecessor (the MTTKRP) writes: the factorisation's W and V
+  // and the control block's fac_kind were written by kernels that completed
+  // before this one was launched, so their staging overlaps the MTTKRP's tail.
   extern __shared__ double sm[];
   const int RR = R * R;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -673,11 +891,67 @@ k_solve(const T* __restrict__ partial, int splits, int64_t I, int R_in,
       for (int e = tid; e < 2 * RR; e += blockDim.x) gh[e] = 0.f;
     }
     __syncthreads();
+    griddep_wait();   // the MTTKRP partials (programmatic launch inside a sweep)
+    griddep_launch_dependents();
+    if (ctrl->done) {
+      asm volatile("cp.async.wait_all;\n" ::: "memory");   // no copy outlives the CTA
+      return;
+    }
     const int rr = tid / R, c = tid - (tid / R) * R;
     const bool act = tid < RB * R;
     for (int64_t base = row0; base < row1; base += RB) {
       const int64_t row = base + rr;
       const bool live = act && row < row1;
+      if constexpr (sizeof(T) == 4) {
+        if (lite) {
+          // The bf16 sweeps' solve on the f32 pipe alone (this GPU's f64 pipe
+          // is ~64x slower): m in f32, x = m W, and with max_passes > 0 one
+          // correction x += (m - x V_hi) W.  The MTTKRP it solves for is
+          // itself only accurate to ~1e-6.
+          float m = 0.f;
+          if (live) {
+            float sh, sc;
+            sum_splits_sc(partial, splits, IR, row * R + c, sh, sc);
+            m = sh + sc;
+          }
+          if (act) mbf[rr * R + c] = m;
+          asm volatile("cp.async.wait_all;\n" ::: "memory");   // this thread's copies of W, V
+          __syncthreads();
+          // four-chain dot products of a row vector in shared memory with a
+          // column of an R x R matrix in shared memory
+          auto dot_col = [&](const float* v, const float* M) -> float {
+            float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+            int k = 0;
+            for (; k + 3 < R; k += 4) {
+              a0 = fmaf(v[k], M[k * R + c], a0);
+              a1 = fmaf(v[k + 1], M[(k + 1) * R + c], a1);
+              a2 = fmaf(v[k + 2], M[(k + 2) * R + c], a2);
+              a3 = fmaf(v[k + 3], M[(k + 3) * R + c], a3);
+            }
+            for (; k < R; ++k) a0 = fmaf(v[k], M[k * R + c], a0);
+            return (a0 + a1) + (a2 + a3);
+          };
+          float x = act ? dot_col(mbf + rr * R, Wm) : 0.f;
+          if (max_passes > 0) {
+            if (act) xbh[rr * R + c] = x;
+            __syncthreads();
+            if (act) rbf[rr * R + c] = m - dot_col(xbh + rr * R, VmH);
+            __syncthreads();
+            if (act) x += dot_col(rbf + rr * R, Wm);
+          }
+          if (live) {
+            store_entry_f32(reinterpret_cast<float*>(A), A_bt, I, R, row, c, x);
+            ip += (double)(m * x);
+            gbf[rr * R + c] = x;
+          } else if (act) {
+            gbf[rr * R + c] = 0.f;
+          }
+          __syncthreads();
+          gram_update_f32(reinterpret_cast<float*>(gacc), gbf, RB, R);
+          __syncthreads();
+          continue;
+        }
+      }
       if (act) {
         const double mv = live ? sum_splits(partial, splits, IR, row * R + c) : 0.0;
         mb[rr * R + c] = mv;
@@ -765,12 +1039,13 @@ k_solve(const T* __restrict__ partial, int splits, int64_t I, int R_in,
             xbh[rr * R + c] = h;
             xbl[rr * R + c] = (float)(xn - (double)h);
           }
-          if (live) {  // non-negative doubles order like their bit patterns
+          if (live && pass + 1 < max_passes) {  // non-negative doubles order like their bits
             atomicMax(&s_dmax, (unsigned long long)__double_as_longlong(fabs(d)));
             atomicMax(&s_xmax, (unsigned long long)__double_as_longlong(fabs(xn)));
           }
         }
         __syncthreads();
+        if (pass + 1 == max_passes) break;   // no stop test after the last pass
         const bool stop = __longlong_as_double((long long)s_dmax) <=
                           kIrStop * __longlong_as_double((long long)s_xmax);
         __syncthreads();  // everyone has read the maxima before they are reset
@@ -792,6 +1067,9 @@ k_solve(const T* __restrict__ partial, int splits, int64_t I, int R_in,
     }
   } else {
     // ------------------------------------------------ substitution path
+    griddep_wait();
+    griddep_launch_dependents();
+    if (ctrl->done) return;
     double* rowbuf = gacc + RR;                    // kSolveWarps * R
     double* sfac = rowbuf + kSolveWarps * R;       // RR + R (optional)
     if (mats_in_smem)
@@ -874,9 +1152,9 @@ k_solve(const T* __restrict__ partial, int splits, int64_t I, int R_in,
   double* out = gpart + (int64_t)blockIdx.x * RR;
   if (df) {
     float* o = reinterpret_cast<float*>(out);
-    if (kind == 2) {
+    if (kind == 2) {   // the lite Gram has no lo plane (the reducer reads hi only)
       const float* g = reinterpret_cast<const float*>(gacc);
-      for (int e = tid; e < 2 * RR; e += blockDim.x) o[e] = g[e];
+      for (int e = tid; e < (lite ? RR : 2 * RR); e += blockDim.x) o[e] = g[e];
     } else {
       for (int e = tid; e < RR; e += blockDim.x) {
         const double g = gacc[e];
@@ -957,15 +1235,20 @@ __global__ void k_fit(const double* G, int ndim, int R, const T* w, const double
 // fpart[block]; the block that finishes last (a device-scope counter in the
 // control block, which it resets) sums fpart and the <M, A> partials in a
 // fixed order and records the error.  Deterministic whichever block is last.
+// At most 64 registers a thread (the second launch bound): a CTA then fits
+// beside a tensor-core MTTKRP CTA (192 threads x 253 registers), so on the
+// aux stream it does not wait for an idle SM.
 template <typename T>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 4)
 k_gram_reduce_fit(const double* __restrict__ gpart, int nparts, int R, double* G_all, int mode,
                   int ndim, int df, const T* w, const double* ipart, int nip, double* fpart,
-                  AlsCtrl* ctrl, double* errors, int n_iter_max, double tol, int crit) {
+                  AlsCtrl* ctrl, double* errors, int n_iter_max, double tol, int crit,
+                  float* G32_all) {
   griddep_wait();   // the solve's Gram and <M, A> partials
   if (ctrl->done) return;
   const int RR = R * R;
-  const double t = gram_reduce_block(gpart, nparts, R, G_all + (int64_t)mode * RR, df);
+  const double t = gram_reduce_block(gpart, nparts, R, G_all + (int64_t)mode * RR, df,
+                                     G32_all ? G32_all + (int64_t)mode * 2 * RR : nullptr);
   __shared__ int s_last;
   __shared__ double scratch[32];
   if (threadIdx.x < 32) {
@@ -1125,7 +1408,7 @@ int als_launch_sumsq(int dtype, const void* X, int64_t n, double* part, int nblo
 
 template <typename T>
 int als_launch_gram(const T* A, int64_t I, int R, double* gpart, int nparts_max, double* G,
-                    const int* done, cudaStream_t st) {
+                    const int* done, cudaStream_t st, float* G32) {
   int nparts = (int)std::min<int64_t>(nparts_max, std::max<int64_t>(1, ceil_div(I, 4)));
   const int64_t rpb = ceil_div(I, nparts);
   nparts = (int)ceil_div(I, rpb);
@@ -1141,22 +1424,22 @@ int als_launch_gram(const T* A, int64_t I, int R, double* gpart, int nparts_max,
   }
   k_gram_partial<T><<<nparts, threads, smem, st>>>(A, I, R, rpb, gpart, done);
   TLGB_LAUNCH_CHECK();
-  return als_launch_gram_reduce(gpart, nparts, R, G, done, 0, st);
+  return als_launch_gram_reduce(gpart, nparts, R, G, done, 0, st, G32);
 }
 
 int als_launch_gram_reduce(const double* gpart, int nparts, int R, double* G, const int* done,
-                           int df, cudaStream_t st) {
+                           int df, cudaStream_t st, float* G32) {
   const int RR = R * R;
-  k_gram_reduce<<<(int)ceil_div(RR, 32), 256, 0, st>>>(gpart, nparts, R, G, done, df);
+  k_gram_reduce<<<(int)ceil_div(RR, 32), 256, 0, st>>>(gpart, nparts, R, G, done, df, G32);
   TLGB_LAUNCH_CHECK();
   return TLGB_OK;
 }
 
 template <typename T, int TI, int TJ, int NI, int NJ>
-static void launch_fast(const double* G, int ndim, int mode, int R, const T* w, double l2,
-                        double* vmat, float* w32, AlsCtrl* ctrl, cudaStream_t st) {
-  k_factorize_fast<T, TI, TJ, NI, NJ><<<1, TI * TJ, 0, st>>>(G, ndim, mode, R, w, l2, vmat, w32,
-                                                             ctrl);
+static void launch_fast(const double* G, const float* G32, int ndim, int mode, int R, const T* w,
+                        double l2, double* vmat, float* w32, AlsCtrl* ctrl, cudaStream_t st) {
+  k_factorize_fast<T, TI, TJ, NI, NJ><<<1, TI * TJ, 0, st>>>(G, G32, ndim, mode, R, w, l2, vmat,
+                                                             w32, ctrl);
 }
 
 // Hands every factorisation to the f64 kernel (the "f64_factorize" tuning key).
@@ -1167,19 +1450,19 @@ __global__ void k_force_f64_factorize(AlsCtrl* ctrl) {
 template <typename T>
 int als_launch_factorize(const double* G, int ndim, int mode, int R, const T* weights,
                          double l2_reg, double* fac, int* perm, double* vmat, float* w32,
-                         AlsCtrl* ctrl, cudaStream_t st) {
+                         AlsCtrl* ctrl, cudaStream_t st, const float* G32) {
   int rc = als_prepare(TypeCode<T>::value);
   if (rc) return rc;
   if (tc_tuning().f64_factorize)
     k_force_f64_factorize<<<1, 32, 0, st>>>(ctrl);
   else if (R <= 32)
-    launch_fast<T, 8, 16, 4, 2>(G, ndim, mode, R, weights, l2_reg, vmat, w32, ctrl, st);
+    launch_fast<T, 8, 16, 4, 2>(G, G32, ndim, mode, R, weights, l2_reg, vmat, w32, ctrl, st);
   else if (R <= 64)
-    launch_fast<T, 16, 16, 4, 4>(G, ndim, mode, R, weights, l2_reg, vmat, w32, ctrl, st);
+    launch_fast<T, 16, 16, 4, 4>(G, G32, ndim, mode, R, weights, l2_reg, vmat, w32, ctrl, st);
   else if (R <= 96)
-    launch_fast<T, 16, 16, 6, 6>(G, ndim, mode, R, weights, l2_reg, vmat, w32, ctrl, st);
+    launch_fast<T, 16, 16, 6, 6>(G, G32, ndim, mode, R, weights, l2_reg, vmat, w32, ctrl, st);
   else
-    launch_fast<T, 16, 16, 10, 10>(G, ndim, mode, R, weights, l2_reg, vmat, w32, ctrl, st);
+    launch_fast<T, 16, 16, 10, 10>(G, G32, ndim, mode, R, weights, l2_reg, vmat, w32, ctrl, st);
   TLGB_LAUNCH_CHECK();
   k_factorize<T><<<1, 256, 0, st>>>(G, ndim, mode, R, weights, l2_reg, fac, perm, vmat, ctrl);
   TLGB_LAUNCH_CHECK();
@@ -1243,12 +1526,13 @@ template <typename T>
 int als_launch_gram_reduce_fit(const double* gpart, int nparts, int R, double* G_all, int mode,
                                int ndim, int df, const T* weights, const double* ipart, int nip,
                                double* fpart, AlsCtrl* ctrl, double* errors, int n_iter_max,
-                               double tol, int cvg_criterion, cudaStream_t st, bool pdl) {
+                               double tol, int cvg_criterion, cudaStream_t st, bool pdl,
+                               float* G32_all) {
   const int RR = R * R;
   TLGB_CUDA_TRY(launch_maybe_pdl(pdl, k_gram_reduce_fit<T>, dim3((unsigned)ceil_div(RR, 32)),
                                  dim3(256), 0, st, gpart, nparts, R, G_all, mode, ndim, df,
                                  weights, ipart, nip, fpart, ctrl, errors, n_iter_max, tol,
-                                 cvg_criterion));
+                                 cvg_criterion, G32_all));
   return TLGB_OK;
 }
 
@@ -1338,10 +1622,10 @@ int als_prepare(int dtype) {
 
 #define TLGB_INST(T)                                                                          \
   template int als_launch_gram<T>(const T*, int64_t, int, double*, int, double*, const int*,  \
-                                  cudaStream_t);                                             \
+                                  cudaStream_t, float*);                                     \
   template int als_launch_factorize<T>(const double*, int, int, int, const T*, double,       \
                                        double*, int*, double*, float*, AlsCtrl*,             \
-                                       cudaStream_t);                                        \
+                                       cudaStream_t, const float*);                          \
   template int als_launch_solve<T>(const T*, int, int64_t, int, const double*, const int*,   \
                                    const double*, const float*, T*, __nv_bfloat16*, double*, \
                                    double*, AlsCtrl*, int, int*, cudaStream_t, bool, bool);  \
@@ -1349,7 +1633,8 @@ int als_prepare(int dtype) {
                                  AlsCtrl*, double*, int, double, int, cudaStream_t);         \
   template int als_launch_gram_reduce_fit<T>(const double*, int, int, double*, int, int, int,  \
                                              const T*, const double*, int, double*, AlsCtrl*, \
-                                             double*, int, double, int, cudaStream_t, bool); \
+                                             double*, int, double, int, cudaStream_t, bool, \
+                                             float*);                                         \
   template int als_launch_normalize<T>(T* const*, const int64_t*, int, int, T*, const int*,  \
                                        cudaStream_t);
 TLGB_INST(float)

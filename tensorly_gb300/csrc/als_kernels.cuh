@@ -21,17 +21,23 @@ constexpr int kSolveWarps = 8;       // warps per solve CTA
 int als_launch_sumsq(int dtype, const void* X, int64_t n, double* part, int nblocks,
                      AlsCtrl* ctrl, cudaStream_t st);
 
+// G32 (optional, 2 R^2 floats): the Gram's f32 (hi, lo) planes, the operand
+// of the factorisation's double-float V (see als_launch_factorize).
 template <typename T>
 int als_launch_gram(const T* A, int64_t I, int R, double* gpart, int nparts_max, double* G,
-                    const int* done, cudaStream_t st);
+                    const int* done, cudaStream_t st, float* G32 = nullptr);
 
 // vmat (R*R f64) and w32 (R*R f32) receive V and its f32 inverse for the
 // refinement path; fac/perm the f64 Cholesky or LU fallback.
+// G32 (optional; ndim x 2 R^2 floats, the (hi, lo) planes of every Gram as
+// written by the Gram reductions): for f32 factors with R <= kSolveDfMaxRank,
+// V is then formed in double-float on the f32 pipe and vmat is not written
+// (the solve reads only w32's V planes there).
 template <typename T>
 int als_launch_factorize(const double* G, int ndim, int mode, int R, const T* weights,
                          double l2_reg, double* fac, int* perm, double* vmat,
                          float* w32 /* 3 R^2: W, then V's f32 hi and lo planes */,
-                         AlsCtrl* ctrl, cudaStream_t st);
+                         AlsCtrl* ctrl, cudaStream_t st, const float* G32 = nullptr);
 
 // Sums the MTTKRP partials of each row, solves with the factorisation, stores
 // the factor (and optionally its bf16 transpose), and writes per-CTA Gram and
@@ -52,9 +58,11 @@ int als_launch_solve(const T* partial, int splits, int64_t I, int R, const doubl
 constexpr int kIrMaxPasses = 4;
 
 // df: the partials are (hi, lo) f32 planes (written by k_solve for f32 factors
-// with rank <= kSolveDfMaxRank), else f64.
+// with rank <= kSolveDfMaxRank), 2: the hi planes only (a lite solve's Gram,
+// whose lo planes are zero; its substitution fallback's lo planes are
+// dropped), else f64.
 int als_launch_gram_reduce(const double* gpart, int nparts, int R, double* G, const int* done,
-                           int df, cudaStream_t st);
+                           int df, cudaStream_t st, float* G32 = nullptr);
 constexpr int kSolveDfMaxRank = 96;
 
 template <typename T>
@@ -69,7 +77,8 @@ template <typename T>
 int als_launch_gram_reduce_fit(const double* gpart, int nparts, int R, double* G_all, int mode,
                                int ndim, int df, const T* weights, const double* ipart, int nip,
                                double* fpart, AlsCtrl* ctrl, double* errors, int n_iter_max,
-                               double tol, int cvg_criterion, cudaStream_t st, bool pdl = false);
+                               double tol, int cvg_criterion, cudaStream_t st, bool pdl = false,
+                               float* G32_all = nullptr);
 
 template <typename T>
 int als_launch_normalize(T* const* factors, const int64_t* rows, int ndim, int R, T* weights,

@@ -22,6 +22,7 @@ struct AlsBuffers {
   AlsCtrl* ctrl;
   double* errors;
   double* G;
+  float* G32;                           // (hi, lo) f32 planes of every Gram (f32 factors)
   double* fac;
   int* perm;
   double* vmat;                         // V of the current mode (f64)
@@ -64,6 +65,7 @@ int layout(int dtype, const Shape& sh, int64_t R, const tlgb_cp_als_options& o,
   B->ctrl = c.take<AlsCtrl>(1);
   B->errors = c.take<double>(std::max(1, o.n_iter_max));
   B->G = c.take<double>((size_t)sh.ndim * RR);
+  B->G32 = (dtype == TLGB_F32) ? c.take<float>((size_t)sh.ndim * 2 * RR) : nullptr;
   B->fac = c.take<double>((size_t)RR + R);
   B->perm = c.take<int>(R);
   B->vmat = c.take<double>((size_t)RR);
@@ -173,7 +175,9 @@ struct Runner {
   Plans* P;
   AlsBuffers B;
   std::vector<int> modes;
-  int last_nb = 1;
+  // The last mode's Gram reduction and fit of the previous sweep when that
+  // sweep deferred it (mode < 0: none pending).
+  int fit_mode = -1, fit_nb = 0, fit_df = 0;
   // The factorisation of mode n's normal equations needs only the Grams, so
   // it runs on `aux` concurrently with mode n's MTTKRP (fork/join by events,
   // captured into the graph as parallel branches).
@@ -211,7 +215,17 @@ struct Runner {
   // the fit's cancellation amplifies an error in <M_last, A_last> by about
   // ||X||^2 / rec_error^2; the closing sweep's last MTTKRP feeds the reported
   // error, so it runs unbiased.
-  int sweep(int kind, cudaStream_t st) {
+  //
+  // defer_fit: the last mode's Gram reduction and the fit are left to the
+  // next sweep, which runs them on the aux stream in front of its first
+  // factorisation (their only consumer besides the stop test), so the next
+  // sweep's first MTTKRP follows the last solve directly.  The stop flag the
+  // fit raises is then seen one sweep late: every kernel of that next sweep
+  // that writes a factor or the Grams runs after the fit (its solves wait for
+  // the aux stream) and returns at once, so the factors stay those of the
+  // converged sweep.  Not used with normalize_factors (the normalisation
+  // rewrites the Grams and the weights the fit reads).
+  int sweep(int kind, cudaStream_t st, bool defer_fit = false) {
     const bool tc = kind == kSweepBf16;
     const int N = sh.ndim;
     const int RR = (int)(R * R);
@@ -230,21 +244,30 @@ struct Runner {
     // The Gram reduction of a mode other than the last runs on the aux
     // stream in front of the next mode's factorisation (the only consumer of
     // that Gram), so the next MTTKRP does not wait for it.
-    int pending_mode = -1, pending_nb = 0;
+    int pending_mode = -1, pending_nb = 0, pending_df = 0;
     for (size_t mi = 0; mi < modes.size(); ++mi) {
       const int mode = modes[mi];
       const bool last = (mi + 1 == modes.size());
       TLGB_CUDA_TRY(cudaEventRecord(ev_fork, st));
       TLGB_CUDA_TRY(cudaStreamWaitEvent(aux, ev_fork, 0));
       int rc;
+      if (fit_mode >= 0) {   // the previous sweep's deferred fit
+        rc = als_launch_gram_reduce_fit<T>(B.gpart, fit_nb, (int)R, B.G, fit_mode, N, fit_df,
+                                           weights, B.ipart, fit_nb, B.fpart, B.ctrl, B.errors,
+                                           o.n_iter_max, o.tol, o.cvg_criterion, aux, false,
+                                           B.G32);
+        if (rc) return rc;
+        fit_mode = -1;
+      }
       if (pending_mode >= 0) {
         rc = als_launch_gram_reduce(B.gpart, pending_nb, (int)R,
-                                    B.G + (size_t)pending_mode * RR, done, df, aux);
+                                    B.G + (size_t)pending_mode * RR, done, pending_df, aux,
+                                    B.G32 ? B.G32 + (size_t)pending_mode * 2 * RR : nullptr);
         if (rc) return rc;
         pending_mode = -1;
       }
       rc = als_launch_factorize<T>(B.G, N, mode, (int)R, weights, o.l2_reg, B.fac, B.perm,
-                                   B.vmat, B.w32, B.ctrl, aux);
+                                   B.vmat, B.w32, B.ctrl, aux, B.G32);
       if (rc) return rc;
       TLGB_CUDA_TRY(cudaEventRecord(ev_join, aux));
       if (ev_mt[0][mode]) TLGB_CUDA_TRY(cudaEventRecord(ev_mt[0][mode], st));
@@ -285,23 +308,29 @@ struct Runner {
       if (ev_mt[1][mode]) TLGB_CUDA_TRY(cudaEventRecord(ev_mt[1][mode], st));
       TLGB_CUDA_TRY(cudaStreamWaitEvent(st, ev_join, 0));
       int nb = 0;
+      // the bf16 sweeps' solve keeps its Gram in plain f32 (one plane)
+      const bool lite = tc && P->tc[mode].valid && !tc_tuning().full_solve;
+      const int gdf = (df && lite) ? 2 : df;
       rc = als_launch_solve<T>((const T*)partial, splits, sh.dim[mode], (int)R, B.fac, B.perm,
                                B.vmat, B.w32, factors[mode], B.fbt[mode], B.gpart,
                                last ? B.ipart : nullptr, B.ctrl,
                                // the bf16 MTTKRP is accurate to ~1e-6, so one plain-f32
                                // refinement pass (solve error ~cond * 6e-8) is enough there
-                               (tc && P->tc[mode].valid) ? 1 : kIrMaxPasses, &nb, st, pdl,
-                               tc && P->tc[mode].valid && !tc_tuning().full_solve);
+                               (tc && P->tc[mode].valid) ? 1 : kIrMaxPasses, &nb, st, pdl, lite);
       if (rc) return rc;
-      if (last) last_nb = nb;
-      if (last) {   // the last mode's Gram reduction also computes the fit (in order)
-        rc = als_launch_gram_reduce_fit<T>(B.gpart, nb, (int)R, B.G, mode, N, df, weights,
+      if (last && defer_fit && !o.normalize_factors && !tc_tuning().inline_fit) {
+        fit_mode = mode;
+        fit_nb = nb;
+        fit_df = gdf;
+      } else if (last) {   // the last mode's Gram reduction also computes the fit (in order)
+        rc = als_launch_gram_reduce_fit<T>(B.gpart, nb, (int)R, B.G, mode, N, gdf, weights,
                                            B.ipart, nb, B.fpart, B.ctrl, B.errors,
-                                           o.n_iter_max, o.tol, o.cvg_criterion, st, pdl);
+                                           o.n_iter_max, o.tol, o.cvg_criterion, st, pdl, B.G32);
         if (rc) return rc;
       } else {      // reduced on the aux stream before the next factorisation
         pending_mode = mode;
         pending_nb = nb;
+        pending_df = gdf;
       }
     }
     int rc = TLGB_OK;
@@ -324,7 +353,8 @@ struct Runner {
     for (int k = 0; k < sh.ndim; ++k) imax = std::max(imax, sh.dim[k]);
     for (int k = 0; k < sh.ndim; ++k) {
       int rc = als_launch_gram<T>(factors[k], sh.dim[k], (int)R, B.gpart, solve_blocks_for(imax),
-                                  B.G + (size_t)k * RR, done, st);
+                                  B.G + (size_t)k * RR, done, st,
+                                  B.G32 ? B.G32 + (size_t)k * 2 * RR : nullptr);
       if (rc) return rc;
     }
     return TLGB_OK;
@@ -375,6 +405,9 @@ class GraphGuard {
  public:
   cudaGraph_t g = nullptr;
   cudaGraphExec_t e = nullptr;
+  GraphGuard() = default;
+  GraphGuard(const GraphGuard&) = delete;
+  GraphGuard& operator=(const GraphGuard&) = delete;
   ~GraphGuard() {
     if (e) cudaGraphExecDestroy(e);
     if (g) cudaGraphDestroy(g);
@@ -472,8 +505,24 @@ int run(const T* X, const Shape& sh, int64_t R, T* const* factors, T* weights,
   StreamGuard cap;
   // Timing events recorded inside a graph cannot be read back, so timed runs
   // launch the sweeps directly (kernel durations are the same).
+  // Without graphs (the default), the sweeps are launched directly, a group
+  // ahead of the host's read of the control block (which then waits for the
+  // previous group only, on a side stream), so the GPU never waits for the
+  // host between groups and programmatic launch and the deferred fit bridge
+  // every sweep of a phase.  The host sees a converged run up to two groups
+  // late; the sweeps launched meanwhile return at once on the device's stop
+  // flag.  A callback (which sees every sweep) and the timing events read
+  // the control block after every group instead.
   const bool use_graph = o.use_graph && !o.mttkrp_ms;
+  const bool lookahead = !use_graph && !o.mttkrp_ms && !o.callback;
   if (use_graph) TLGB_CUDA_TRY(cudaStreamCreateWithFlags(&cap.s, cudaStreamNonBlocking));
+  StreamGuard peek;
+  EventGuard ev_grp[2];
+  if (lookahead) {
+    TLGB_CUDA_TRY(cudaStreamCreateWithFlags(&peek.s, cudaStreamNonBlocking));
+    for (int j = 0; j < 2; ++j)
+      TLGB_CUDA_TRY(cudaEventCreateWithFlags(&ev_grp[j].e, cudaEventDisableTiming));
+  }
 
   AlsCtrl hc{};
   int launched = 0;
@@ -485,28 +534,82 @@ int run(const T* X, const Shape& sh, int64_t R, T* const* factors, T* weights,
       // A converged bf16 phase still gets its refinement sweeps: clear the flag.
       TLGB_CUDA_TRY(cudaMemsetAsync(&run.B.ctrl->done, 0, sizeof(int), st));
     }
-    GraphGuard gg;
-    if (use_graph) {
+    // The sweeps run in groups of check_every (the last group of a phase may
+    // be shorter); the host reads the control block after each group.  A
+    // group is launched as CUDA graphs of up to gmax sweeps (one graph per
+    // length, captured when first needed), so programmatic launch and the
+    // deferred fit also bridge the sweeps inside a graph; a graph's last
+    // sweep runs its fit in line.
+    const int gsize = std::min(check_every, ph.sweeps);
+    const int gmax = tc_tuning().graph_sweeps > 0 ? std::min(tc_tuning().graph_sweeps, gsize)
+                                                  : gsize;
+    std::vector<GraphGuard> gg(gmax + 1);   // [n]: the graph of n sweeps
+    auto capture = [&](int n, GraphGuard& g) -> int {
       TLGB_CUDA_TRY(cudaStreamBeginCapture(cap.s, cudaStreamCaptureModeThreadLocal));
-      int rc2 = run.sweep(ph.kind, cap.s);
-      cudaGraph_t g = nullptr;
-      cudaError_t ce = cudaStreamEndCapture(cap.s, &g);
-      gg.g = g;
+      int rc2 = TLGB_OK;
+      for (int j = 0; j < n && !rc2; ++j) rc2 = run.sweep(ph.kind, cap.s, j + 1 < n);
+      cudaGraph_t graph = nullptr;
+      cudaError_t ce = cudaStreamEndCapture(cap.s, &graph);
+      g.g = graph;
       if (rc2) return rc2;
       if (ce != cudaSuccess)
         return set_error(TLGB_ECUDA, std::string("cp_als: graph capture: ") + cudaGetErrorString(ce));
-      TLGB_CUDA_TRY(cudaGraphInstantiate(&gg.e, gg.g, 0));
+      TLGB_CUDA_TRY(cudaGraphInstantiate(&g.e, g.g, 0));
+      return TLGB_OK;
+    };
+    if (use_graph) {
+      rc = capture(gmax, gg[gmax]);
+      if (rc) return rc;
     }
-    for (int s = 0; s < ph.sweeps; ++s) {
-      if (use_graph) {
-        TLGB_CUDA_TRY(cudaGraphLaunch(gg.e, st));
-      } else {
-        rc = run.sweep(ph.kind, st);
-        if (rc) return rc;
+    if (lookahead) {
+      int cur = 0;
+      bool have_prev = false;
+      for (int s = 0; s < ph.sweeps;) {
+        const int n = std::min(gsize, ph.sweeps - s);
+        for (int j = 0; j < n; ++j) {
+          // the phase's last sweep runs its fit in line: the next phase (or
+          // the final read) follows it in stream order
+          rc = run.sweep(ph.kind, st, s + j + 1 < ph.sweeps);
+          if (rc) return rc;
+        }
+        s += n;
+        launched += n;
+        TLGB_CUDA_TRY(cudaEventRecord(ev_grp[cur].e, st));
+        if (have_prev) {   // the control block as of the previous group
+          TLGB_CUDA_TRY(cudaStreamWaitEvent(peek.s, ev_grp[cur ^ 1].e, 0));
+          TLGB_CUDA_TRY(cudaMemcpyAsync(&hc, run.B.ctrl, sizeof(AlsCtrl), cudaMemcpyDeviceToHost,
+                                        peek.s));
+          TLGB_CUDA_TRY(cudaStreamSynchronize(peek.s));
+          // errors are reported after the final synchronisation below
+          if (hc.tc_err != 0 || hc.status != TLGB_OK || hc.done) break;
+        }
+        have_prev = true;
+        cur ^= 1;
       }
-      ++launched;
-      const bool end_of_phase = (s + 1 == ph.sweeps);
-      if (((s + 1) % check_every) == 0 || end_of_phase) {
+      if (hc.tc_err != 0 || hc.status != TLGB_OK) break;
+      continue;
+    }
+    for (int s = 0; s < ph.sweeps;) {
+      const int n = std::min(gsize, ph.sweeps - s);
+      for (int left = n; left > 0;) {
+        const int k = std::min(gmax, left);
+        if (use_graph) {
+          if (!gg[k].e) {
+            rc = capture(k, gg[k]);
+            if (rc) return rc;
+          }
+          TLGB_CUDA_TRY(cudaGraphLaunch(gg[k].e, st));
+        } else {
+          for (int j = 0; j < k; ++j) {
+            rc = run.sweep(ph.kind, st, j + 1 < k);
+            if (rc) return rc;
+          }
+        }
+        left -= k;
+      }
+      launched += n;
+      s += n;
+      {   // end of a group: read the control block
         TLGB_CUDA_TRY(cudaMemcpyAsync(&hc, run.B.ctrl, sizeof(AlsCtrl), cudaMemcpyDeviceToHost, st));
         TLGB_CUDA_TRY(cudaStreamSynchronize(st));
         // a timed-out MTTKRP leaves garbage partials behind it, so it is
@@ -570,7 +673,7 @@ extern "C" void tlgb_cp_als_default_options(tlgb_cp_als_options* o) {
   o->precision = TLGB_PREC_NATIVE;
   o->refine_sweeps = 3;
   o->check_every = 8;
-  o->use_graph = 1;
+  o->use_graph = 0;
   o->callback = nullptr;
   o->callback_user = nullptr;
 }

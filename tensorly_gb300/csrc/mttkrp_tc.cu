@@ -959,6 +959,8 @@ extern "C" int tlgb_set_tuning(const char* key, int value) {
   else if (k == "split_simt") tc_tuning().split_simt = value;
   else if (k == "full_solve") tc_tuning().full_solve = value;
   else if (k == "closing_planes") tc_tuning().closing_planes = value;
+  else if (k == "cp_graph_sweeps") tc_tuning().graph_sweeps = value;
+  else if (k == "cp_inline_fit") tc_tuning().inline_fit = value;
   else return batched_set_tuning(k, value);   // the batched CP-ALS variants
   return TLGB_OK;
 }

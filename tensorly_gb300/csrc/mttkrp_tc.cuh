@@ -47,6 +47,8 @@ struct TcTuning {
   int split_simt = 0;         // 1: non-negative / constrained CP keep the SIMT f32 MTTKRP
   int full_solve = 0;         // 1: bf16 CP-ALS sweeps solve with the double-float refinement
   int closing_planes = 0;     // 3: the closing sweeps also contract the third tensor plane
+  int graph_sweeps = 0;       // > 0: at most this many CP-ALS sweeps per CUDA graph
+  int inline_fit = 0;         // 1: every CP-ALS sweep runs its last mode's fit in line
 };
 TcTuning& tc_tuning();
 

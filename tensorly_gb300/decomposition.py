@@ -116,15 +116,16 @@ def parafac(tensor, rank, n_iter_max=100, init="svd", svd="truncated_svd",
             verbose=0, return_errors=False, sparsity=None, l2_reg=0, mask=None,
             cvg_criterion="abs_rec_error", fixed_modes=None, svd_mask_repeats=5,
             linesearch=False, callback=None, *, precision="native", refine_sweeps=3,
-            check_every=8, use_graph=True, mttkrp_times=None):
+            check_every=8, use_graph=False, mttkrp_times=None):
     """CP decomposition by ALS (tensorly/decomposition/_cp.py:230-543).
 
     Same signature, return types and stopping rule as the reference.  The
     keyword-only arguments select the GB300 execution: ``precision='bf16'``
     stores an f32 tensor in bf16 and runs the tensor-core MTTKRP for all but
     the last ``refine_sweeps`` sweeps, which run in f32; ``check_every`` is the
-    number of sweeps between host reads of the device-side stop flag;
-    ``use_graph`` replays one captured sweep as a CUDA graph.  If
+    number of sweeps between host reads of the device-side stop flag (the
+    sweeps are launched a group ahead of those reads); ``use_graph`` replays
+    groups of captured sweeps as CUDA graphs instead.  If
     ``mttkrp_times`` is a dict, it receives, per sweep kind that ran
     (``'native'``, ``'bf16'``, ``'f32_split'``, ``'closing'``), the list of
     per-mode MTTKRP durations (ms, CUDA events inside the sweep) of the last

@@ -71,7 +71,7 @@ def test_argument_validation_without_gpu(library):
                                           ctypes.byref(nbytes)) == _lib.TLGB_EINVAL
     opts = _lib.CpAlsOptions()
     lib.tlgb_cp_als_default_options(ctypes.byref(opts))
-    assert opts.n_iter_max == 100 and abs(opts.tol - 1e-8) < 1e-20 and opts.use_graph == 1
+    assert opts.n_iter_max == 100 and abs(opts.tol - 1e-8) < 1e-20 and opts.use_graph == 0
     opts.precision = _lib.TLGB_PREC_BF16
     rc = lib.tlgb_cp_als_workspace_size(_lib.TLGB_F64, 3, shape, 2, ctypes.byref(opts),
                                         ctypes.byref(nbytes))

@@ -222,12 +222,12 @@ def test_dense_autotuner_picks_valid_tiles_and_keeps_results(gb300):
     try:
         autotune.reset_dense()
         _, e0 = gb300.parafac(x, 16, init=gb300.CPTensor((None, [f.clone() for f in init])), **kw)
-        choice = autotune.tune_dense(x, 16, sweeps=3, reps=1)
+        choice = autotune.tune_dense(x, 16, sweeps=4, refine_sweeps=1, reps=1)
         space = dict(autotune.DENSE_SPACE)
         assert set(choice) == set(space)
         for k, v in choice.items():
             assert v in space[k]
-        assert autotune.tune_dense(x, 16) == choice          # cached
+        assert autotune.tune_dense(x, 16, sweeps=4, refine_sweeps=1) == choice   # cached
         _, e1 = gb300.parafac(x, 16, init=gb300.CPTensor((None, [f.clone() for f in init])), **kw)
         np.testing.assert_allclose(e1, e0, rtol=1e-5, atol=1e-7)
     finally:

@@ -309,3 +309,32 @@ def test_parafac_f32_odd_ranks_match_f64_oracle(gb300, shape, rank, precision):
     e = np.linalg.norm(x64 - oracle.cp_to_tensor((None, [host(t).astype(np.float64) for t in f]))) \
         / np.linalg.norm(x64)
     assert abs(e - e64) / e64 < 1e-3, (e, e64)
+
+
+@pytest.mark.parametrize("dtype,rank", [
+    (np.float64, 130), (np.float64, 100), (np.float64, 70), (np.float64, 40),
+    (np.float32, 90), (np.float32, 120), (np.float32, 50), (np.float32, 20)])
+def test_parafac_wide_ranks_match_oracle(gb300, dtype, rank):
+    """Every padded order of the blocked Gauss-Jordan inverse (32, 64, 96 and
+    160) and both builds of V (double-float from the Grams' f32 planes for
+    f32 factors up to rank 96, f64 otherwise), three sweeps from the same
+    initial factors as the f64 oracle: f64 errors to 1e-9 and factors to
+    1e-7, f32 errors to 2e-6 absolute and factors to 1e-3."""
+    rs = np.random.RandomState(rank)
+    shape = (24, 22, 20)
+    x = rs.rand(*shape).astype(dtype)
+    init = [rs.rand(d, rank).astype(dtype) for d in shape]
+    (_, f), errs = gb300.parafac(torch.as_tensor(x, device="cuda"), rank, n_iter_max=3, tol=0,
+                                 init=(None, [torch.as_tensor(a, device="cuda") for a in init]),
+                                 return_errors=True)
+    x64 = x.astype(np.float64)
+    _, of, oerrs = oracle.parafac_sweeps(x64, np.ones(rank), [a.astype(np.float64) for a in init],
+                                         3)
+    if dtype == np.float64:
+        np.testing.assert_allclose(errs, oerrs, rtol=1e-9)
+        for a, b in zip(f, of):
+            assert rel(host(a), b) < 1e-7
+    else:
+        np.testing.assert_allclose(errs, oerrs, rtol=0, atol=2e-6)
+        for a, b in zip(f, of):
+            assert rel(host(a), b) < 1e-3
