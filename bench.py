@@ -271,7 +271,7 @@ def run_gpu(args):
     init = [torch.from_numpy(f).to(dev) for f in init_np]
 
     kw = dict(n_iter_max=args.sweeps, tol=0, precision=args.precision,
-              refine_sweeps=args.refine, check_every=args.sweeps, return_errors=True)
+              refine_sweeps=args.refine, return_errors=True)
     tiles = None
     if args.precision == "bf16" and not args.no_tune:
         # tensor-core MTTKRP tile choices for this tensor (outside the timed region)

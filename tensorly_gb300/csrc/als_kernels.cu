@@ -269,6 +269,18 @@ __device__ __forceinline__ void df_add(float& h, float& l, float bh, float bl) {
   h = u;
 }
 
+// Stop test of the kernels that run after a deferred fit in stream order (the
+// solves, the factorisations, the fits): true when either flag is set; a
+// solve (promote) raises `done` from `done_pending` for the kernels after it.
+__device__ __forceinline__ bool als_stopped(AlsCtrl* ctrl, bool promote = false) {
+  if (ctrl->done) return true;
+  if (ctrl->done_pending) {
+    if (promote && blockIdx.x == 0 && threadIdx.x == 0) ctrl->done = 1;
+    return true;
+  }
+  return false;
+}
+
 template <typename T, int TI, int TJ, int NI, int NJ>
 __global__ void __launch_bounds__(TI * TJ)
 k_factorize_fast(const double* __restrict__ G, const float* __restrict__ G32, int ndim, int mode,
@@ -278,7 +290,7 @@ k_factorize_fast(const double* __restrict__ G, const float* __restrict__ G32, in
   constexpr int B = kGjBlock;
   constexpr int NT = TI * TJ;
   static_assert(TJ * NJ == N && N % B == 0, "padded order must be a multiple of the block");
-  if (ctrl->done) return;
+  if (als_stopped(ctrl)) return;
   __shared__ __align__(16) float sC[N][B];   // block column of the current Schur complement
   __shared__ __align__(16) float sP[B][N];   // block row
   __shared__ __align__(16) float sT[B][N];   // D^-1 P (D^-1 itself in the block's columns)
@@ -524,7 +536,7 @@ template <typename T>
 __global__ void __launch_bounds__(256)
 k_factorize(const double* G, int ndim, int mode, int R, const T* w, double l2, double* fac,
             int* perm, double* V, AlsCtrl* ctrl) {
-  if (ctrl->done || ctrl->fac_kind != 3) return;
+  if (als_stopped(ctrl) || ctrl->fac_kind != 3) return;
   __shared__ int s_fail;
   __shared__ int s_piv;
   const int RR = R * R;
@@ -742,8 +754,19 @@ __device__ __forceinline__ void sum_splits_sc(const float* __restrict__ partial,
                                               float& c_out) {
   float s = 0.f, c = 0.f;
   int p = 0;
-  // eighteen loads in flight per batch: the partials come from L2 and a
-  // batch costs one round trip (the bf16 sweeps' 36 tiles take two)
+  // up to 36 loads in flight per batch: the partials come from L2 and a
+  // batch costs one round trip (the bf16 sweeps' 36 tiles take one)
+  for (; p + 35 < splits; p += 36) {
+    float v[36];
+#pragma unroll
+    for (int u = 0; u < 36; ++u) v[u] = partial[(int64_t)(p + u) * stride + off];
+#pragma unroll
+    for (int u = 0; u < 36; ++u) {
+      const float t = s + v[u];
+      c += (fabsf(s) >= fabsf(v[u])) ? ((s - t) + v[u]) : ((v[u] - t) + s);
+      s = t;
+    }
+  }
   for (; p + 17 < splits; p += 18) {
     float v[18];
 #pragma unroll
@@ -893,7 +916,7 @@ k_solve(const T* __restrict__ partial, int splits, int64_t I, int R_in,
     __syncthreads();
     griddep_wait();   // the MTTKRP partials (programmatic launch inside a sweep)
     griddep_launch_dependents();
-    if (ctrl->done) {
+    if (als_stopped(ctrl, true)) {
       asm volatile("cp.async.wait_all;\n" ::: "memory");   // no copy outlives the CTA
       return;
     }
@@ -1069,7 +1092,7 @@ k_solve(const T* __restrict__ partial, int splits, int64_t I, int R_in,
     // ------------------------------------------------ substitution path
     griddep_wait();
     griddep_launch_dependents();
-    if (ctrl->done) return;
+    if (als_stopped(ctrl, true)) return;
     double* rowbuf = gacc + RR;                    // kSolveWarps * R
     double* sfac = rowbuf + kSolveWarps * R;       // RR + R (optional)
     if (mats_in_smem)
@@ -1209,7 +1232,7 @@ __device__ double sum_gram_product(const double* G, int ndim, int R, const T* w)
 template <typename T>
 __global__ void k_fit(const double* G, int ndim, int R, const T* w, const double* ipart, int nip,
                       AlsCtrl* ctrl, double* errors, int n_iter_max, double tol, int crit) {
-  if (ctrl->done) return;
+  if (als_stopped(ctrl)) return;
   __shared__ double scratch[32];
   double c = block_sum(sum_gram_product<T>(G, ndim, R, w), scratch);
   double ip = 0.0;
@@ -1243,9 +1266,9 @@ __global__ void __launch_bounds__(256, 4)
 k_gram_reduce_fit(const double* __restrict__ gpart, int nparts, int R, double* G_all, int mode,
                   int ndim, int df, const T* w, const double* ipart, int nip, double* fpart,
                   AlsCtrl* ctrl, double* errors, int n_iter_max, double tol, int crit,
-                  float* G32_all) {
+                  float* G32_all, int deferred) {
   griddep_wait();   // the solve's Gram and <M, A> partials
-  if (ctrl->done) return;
+  if (als_stopped(ctrl)) return;
   const int RR = R * R;
   const double t = gram_reduce_block(gpart, nparts, R, G_all + (int64_t)mode * RR, df,
                                      G32_all ? G32_all + (int64_t)mode * 2 * RR : nullptr);
@@ -1286,7 +1309,10 @@ k_gram_reduce_fit(const double* __restrict__ gpart, int nparts, int R, double* G
     if (tol > 0.0 && it >= 1) {
       const double dec = errors[it - 1] - err;
       const bool stop = (crit == 0) ? (fabs(dec) < tol) : (dec < tol);
-      if (stop) ctrl->done = 1;
+      if (stop) {   // deferred: beside the next sweep's first MTTKRP, which reads done
+        if (deferred) ctrl->done_pending = 1;
+        else ctrl->done = 1;
+      }
     }
     ctrl->iter = it + 1;
   }
@@ -1444,7 +1470,7 @@ static void launch_fast(const double* G, const float* G32, int ndim, int mode, i
 
 // Hands every factorisation to the f64 kernel (the "f64_factorize" tuning key).
 __global__ void k_force_f64_factorize(AlsCtrl* ctrl) {
-  if (!ctrl->done && threadIdx.x == 0) ctrl->fac_kind = 3;
+  if (!als_stopped(ctrl) && threadIdx.x == 0) ctrl->fac_kind = 3;
 }
 
 template <typename T>
@@ -1527,12 +1553,12 @@ int als_launch_gram_reduce_fit(const double* gpart, int nparts, int R, double* G
                                int ndim, int df, const T* weights, const double* ipart, int nip,
                                double* fpart, AlsCtrl* ctrl, double* errors, int n_iter_max,
                                double tol, int cvg_criterion, cudaStream_t st, bool pdl,
-                               float* G32_all) {
+                               float* G32_all, bool deferred) {
   const int RR = R * R;
   TLGB_CUDA_TRY(launch_maybe_pdl(pdl, k_gram_reduce_fit<T>, dim3((unsigned)ceil_div(RR, 32)),
                                  dim3(256), 0, st, gpart, nparts, R, G_all, mode, ndim, df,
                                  weights, ipart, nip, fpart, ctrl, errors, n_iter_max, tol,
-                                 cvg_criterion, G32_all));
+                                 cvg_criterion, G32_all, deferred ? 1 : 0));
   return TLGB_OK;
 }
 
@@ -1599,6 +1625,23 @@ static int als_prepare_typed() {
   TLGB_CUDA_TRY((set_carveout_fast<T, 16, 16, 4, 4>()));
   TLGB_CUDA_TRY((set_carveout_fast<T, 16, 16, 6, 6>()));
   TLGB_CUDA_TRY((set_carveout_fast<T, 16, 16, 10, 10>()));
+  // likewise the Gram reductions on the side stream, which share SMs with
+  // MTTKRP CTAs (they fit beside one in registers and shared memory), and
+  // the solves
+  TLGB_CUDA_TRY(cudaFuncSetAttribute(k_gram_reduce_fit<T>,
+                                     cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     cudaSharedmemCarveoutMaxShared));
+  TLGB_CUDA_TRY(cudaFuncSetAttribute(k_gram_reduce, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     cudaSharedmemCarveoutMaxShared));
+  TLGB_CUDA_TRY((cudaFuncSetAttribute(k_solve<T, 64>,
+                                      cudaFuncAttributePreferredSharedMemoryCarveout,
+                                      cudaSharedmemCarveoutMaxShared)));
+  TLGB_CUDA_TRY((cudaFuncSetAttribute(k_solve<T, 32>,
+                                      cudaFuncAttributePreferredSharedMemoryCarveout,
+                                      cudaSharedmemCarveoutMaxShared)));
+  TLGB_CUDA_TRY((cudaFuncSetAttribute(k_solve<T, 0>,
+                                      cudaFuncAttributePreferredSharedMemoryCarveout,
+                                      cudaSharedmemCarveoutMaxShared)));
   TLGB_CUDA_TRY(cudaFuncSetAttribute(
       k_gram_partial<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
       (int)(((size_t)kMaxAlsRank * kMaxAlsRank + kGramRows * kMaxAlsRank) * sizeof(double))));
@@ -1634,7 +1677,7 @@ int als_prepare(int dtype) {
   template int als_launch_gram_reduce_fit<T>(const double*, int, int, double*, int, int, int,  \
                                              const T*, const double*, int, double*, AlsCtrl*, \
                                              double*, int, double, int, cudaStream_t, bool, \
-                                             float*);                                         \
+                                             float*, bool);                                   \
   template int als_launch_normalize<T>(T* const*, const int64_t*, int, int, T*, const int*,  \
                                        cudaStream_t);
 TLGB_INST(float)

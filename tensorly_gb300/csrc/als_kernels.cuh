@@ -13,6 +13,11 @@ struct AlsCtrl {
   double norm_x2;
   int tc_err;    // TLGB_ETIMEOUT if a tensor-core pipeline wait expired
   int red_count; // blocks of the fused Gram reduction + fit that finished (reset by the last)
+  // Stop raised by a fit deferred to the side stream, which runs beside the
+  // next sweep's first MTTKRP (whose threads read `done`, so `done` may not
+  // change under it); the first solve after it, ordered after it, promotes
+  // it to `done`.
+  int done_pending;
 };
 
 constexpr int kMaxAlsRank = 160;     // f64 factorisation held in one CTA's shared memory
@@ -78,7 +83,7 @@ int als_launch_gram_reduce_fit(const double* gpart, int nparts, int R, double* G
                                int ndim, int df, const T* weights, const double* ipart, int nip,
                                double* fpart, AlsCtrl* ctrl, double* errors, int n_iter_max,
                                double tol, int cvg_criterion, cudaStream_t st, bool pdl = false,
-                               float* G32_all = nullptr);
+                               float* G32_all = nullptr, bool deferred = false);
 
 template <typename T>
 int als_launch_normalize(T* const* factors, const int64_t* rows, int ndim, int R, T* weights,

@@ -255,7 +255,7 @@ struct Runner {
         rc = als_launch_gram_reduce_fit<T>(B.gpart, fit_nb, (int)R, B.G, fit_mode, N, fit_df,
                                            weights, B.ipart, fit_nb, B.fpart, B.ctrl, B.errors,
                                            o.n_iter_max, o.tol, o.cvg_criterion, aux, false,
-                                           B.G32);
+                                           B.G32, true);
         if (rc) return rc;
         fit_mode = -1;
       }
@@ -533,6 +533,7 @@ int run(const T* X, const Shape& sh, int64_t R, T* const* factors, T* weights,
     if (pi > 0 && phases[pi - 1].kind == kSweepBf16) {
       // A converged bf16 phase still gets its refinement sweeps: clear the flag.
       TLGB_CUDA_TRY(cudaMemsetAsync(&run.B.ctrl->done, 0, sizeof(int), st));
+      TLGB_CUDA_TRY(cudaMemsetAsync(&run.B.ctrl->done_pending, 0, sizeof(int), st));
     }
     // The sweeps run in groups of check_every (the last group of a phase may
     // be shorter); the host reads the control block after each group.  A
@@ -581,7 +582,7 @@ int run(const T* X, const Shape& sh, int64_t R, T* const* factors, T* weights,
                                         peek.s));
           TLGB_CUDA_TRY(cudaStreamSynchronize(peek.s));
           // errors are reported after the final synchronisation below
-          if (hc.tc_err != 0 || hc.status != TLGB_OK || hc.done) break;
+          if (hc.tc_err != 0 || hc.status != TLGB_OK || hc.done || hc.done_pending) break;
         }
         have_prev = true;
         cur ^= 1;
@@ -628,7 +629,7 @@ int run(const T* X, const Shape& sh, int64_t R, T* const* factors, T* weights,
             if (ret != 0) { stopped = true; break; }
           }
         }
-        if (stopped || hc.done) break;  // callback asked to stop, or converged
+        if (stopped || hc.done || hc.done_pending) break;  // callback asked to stop, or converged
       }
     }
     if (o.mttkrp_ms) {  // durations of this phase's last sweep (the host synced above)
@@ -640,7 +641,7 @@ int run(const T* X, const Shape& sh, int64_t R, T* const* factors, T* weights,
       }
     }
     // only the bf16 phase hands a converged run on to further sweeps
-    if (hc.done && ph.kind != kSweepBf16) break;
+    if ((hc.done || hc.done_pending) && ph.kind != kSweepBf16) break;
   }
   TLGB_CUDA_TRY(cudaMemcpyAsync(&hc, run.B.ctrl, sizeof(AlsCtrl), cudaMemcpyDeviceToHost, st));
   TLGB_CUDA_TRY(cudaStreamSynchronize(st));

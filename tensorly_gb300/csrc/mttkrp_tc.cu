@@ -93,7 +93,7 @@ __host__ __device__ constexpr int tmem_stride(int nb) {
 //    x1 with NPL = 2, x2 with NPL = 1: every product x_i f_j with i + j <= 2.
 //    The dropped terms are below 2^-26 of |x||f|, under one f32 rounding.
 template <int RP, bool MN, int NPL>
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kThreads, RP <= 64 ? 2 : 1)   // RP <= 64: at most 168 registers
 mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmF,
                  const TcArgs a) {
   constexpr int NB = NPL * RP;             // MMA N (one RP-wide block per factor plane)
@@ -119,6 +119,7 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant_
   uint64_t* mdrain = bfull + 1;           // [1] MMA completion before teardown
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mdrain + 1);
   int* ep_ok = reinterpret_cast<int*>(tmem_slot + 1);         // [2] epilogue wait outcome
+  int* s_skip = reinterpret_cast<int*>(tmem_slot + 3);        // the epilogue's stop flag
   float* s_sm = reinterpret_cast<float*>(tmem_slot + 4);      // [2][RP]
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -271,7 +272,12 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant_
     } else {
       // ------------------------------------------------------------ epilogue
       griddep_wait();   // the scales read the factors; the partial tiles are rewritten
-      if (!(a.skip && *a.skip)) {
+      // one read of the stop flag for the four epilogue warps, which meet at
+      // named barriers below (the flag is stable while this kernel runs)
+      if (threadIdx.x == 64) *s_skip = (a.skip && *a.skip) ? 1 : 0;
+      asm volatile("bar.sync 1, 128;" ::: "memory");
+      const bool skip_ep = *s_skip != 0;
+      if (!skip_ep) {
         const int e = threadIdx.x - 64;            // 0..127
         const int q = warp & 3;                    // TMEM lane quarter of this warp
         const int row = 32 * q + lane;
@@ -318,19 +324,22 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant_
           tc_fence_after();
           const uint32_t lane_addr = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(buf * TS);
           if constexpr (RP >= 32) {
+            // 16 columns of every plane at a time: fewer live registers, so
+            // the kernel fits 168 a thread (two of its warps per SM
+            // sub-partition beside a small solve CTA)
 #pragma unroll
-            for (int c = 0; c < RP / 32; ++c) {
-              uint32_t pv[NPL][32];
+            for (int c = 0; c < RP / 16; ++c) {
+              uint32_t pv[NPL][16];
 #pragma unroll
               for (int pl = 0; pl < NPL; ++pl)
-                tmem_ld32_nowait(lane_addr + (uint32_t)(pl * RP + c * 32), pv[pl]);
+                tmem_ld16_nowait(lane_addr + (uint32_t)(pl * RP + c * 16), pv[pl]);
               tmem_wait_ld();
 #pragma unroll
-              for (int j = 0; j < 32; ++j) {
+              for (int j = 0; j < 16; ++j) {
                 float v = __uint_as_float(pv[NPL - 1][j]);   // smallest plane first
 #pragma unroll
                 for (int pl = NPL - 2; pl >= 0; --pl) v += __uint_as_float(pv[pl][j]);
-                acc[c * 32 + j] = fmaf(s_sm[buf * RP + c * 32 + j], v, acc[c * 32 + j]);
+                acc[c * 16 + j] = fmaf(s_sm[buf * RP + c * 16 + j], v, acc[c * 16 + j]);
               }
             }
           } else {
@@ -961,6 +970,7 @@ extern "C" int tlgb_set_tuning(const char* key, int value) {
   else if (k == "closing_planes") tc_tuning().closing_planes = value;
   else if (k == "cp_graph_sweeps") tc_tuning().graph_sweeps = value;
   else if (k == "cp_inline_fit") tc_tuning().inline_fit = value;
+
   else return batched_set_tuning(k, value);   // the batched CP-ALS variants
   return TLGB_OK;
 }
