@@ -136,9 +136,20 @@ int tlgb_mttkrp_bf16(const void* X, int ndim, const int64_t* shape, const void* 
  * "tc_test_starve" = 1 is for testing the timeout path: the tensor-core
  * MTTKRP issues no copies, its waits give up after 1 ms, and the workspace
  * status (tlgb_workspace_status) reads TLGB_ETIMEOUT;
+ * "split_simt" = 1 keeps the SIMT f32 MTTKRP in the non-negative and
+ * constrained CP loops (instead of the exact bf16 split on the tensor cores);
+ * "full_solve" = 1 gives the bf16 CP-ALS sweeps the double-float refinement
+ * solve of the closing sweeps; "closing_planes" = 3 makes the closing sweeps
+ * also contract the third bf16 plane of the f32 tensor;
+ * "cp_graph_sweeps" = n caps the sweeps of one CUDA graph (use_graph = 1);
+ * "cp_inline_fit" = 1 runs every sweep's last Gram reduction and fit on the
+ * main stream instead of deferring it to the side stream under the next
+ * sweep;
  * "batched_threads_small" / "_medium" / "_large" = threads per CTA (128, 256
  * or 512; 4, 2 or 1 CTAs per SM) of tlgb_cp_als_batched for the tensors
- * whose padded size fits 128-, 256-thread CTAs' shared memory, or neither.
+ * whose padded size fits 128-, 256-thread CTAs' shared memory, or neither;
+ * "batched_outer_tile_small" / "_medium" / "_large" = outer slices per
+ * MTTKRP work tile of those classes (0..64, 0: spread over the threads).
  * Process-wide; no counterpart in TensorLy.
  */
 int tlgb_set_tuning(const char* key, int value);

@@ -1427,6 +1427,10 @@ int als_launch_sumsq(int dtype, const void* X, int64_t n, double* part, int nblo
   else
     k_sumsq<double><<<nblocks, 256, 0, st>>>((const double*)X, n, part);
   TLGB_LAUNCH_CHECK();
+  return als_launch_sumsq_final(part, nblocks, ctrl, st);
+}
+
+int als_launch_sumsq_final(const double* part, int nblocks, AlsCtrl* ctrl, cudaStream_t st) {
   k_sumsq_final<<<1, 256, 0, st>>>(part, nblocks, ctrl);
   TLGB_LAUNCH_CHECK();
   return TLGB_OK;

@@ -25,6 +25,8 @@ constexpr int kSolveWarps = 8;       // warps per solve CTA
 
 int als_launch_sumsq(int dtype, const void* X, int64_t n, double* part, int nblocks,
                      AlsCtrl* ctrl, cudaStream_t st);
+// ||X||^2 into the control block from `nblocks` partial sums (fixed order).
+int als_launch_sumsq_final(const double* part, int nblocks, AlsCtrl* ctrl, cudaStream_t st);
 
 // G32 (optional, 2 R^2 floats): the Gram's f32 (hi, lo) planes, the operand
 // of the factorisation's double-float V (see als_launch_factorize).

@@ -462,17 +462,35 @@ int run(const T* X, const Shape& sh, int64_t R, T* const* factors, T* weights,
 
   // ---- set-up: control block, ||X||^2, Grams, bf16 operands
   TLGB_CUDA_TRY(cudaMemsetAsync(run.B.ctrl, 0, sizeof(AlsCtrl), st));
-  rc = als_launch_sumsq(TypeCode<T>::value, X, sh.numel, run.B.sumsq_part, kSumsqBlocks,
-                        run.B.ctrl, st);
-  if (rc) return rc;
-  rc = run.grams(nullptr, st);
-  if (rc) return rc;
   if (mixed) {
-    rc = P.refine_tc ? tc_launch_split3((const float*)X, sh.numel, run.B.xbf, run.B.xsplit[0],
-                                        run.B.xsplit[1], st)   // x2 only with three planes
-                     : tc_launch_to_bf16((const float*)X, sh.numel, run.B.xbf, st);
+    // The Grams and the factors' bf16 planes on the side stream, beside the
+    // pass over X that writes its bf16 planes (and, with the closing sweeps'
+    // split, ||X||^2 in the same pass).
+    TLGB_CUDA_TRY(cudaEventRecord(run.ev_fork, st));
+    TLGB_CUDA_TRY(cudaStreamWaitEvent(aux.s, run.ev_fork, 0));
+    rc = run.grams(nullptr, aux.s);
     if (rc) return rc;
-    rc = run.bf16_factors(st);
+    rc = run.bf16_factors(aux.s);
+    if (rc) return rc;
+    TLGB_CUDA_TRY(cudaEventRecord(run.ev_join, aux.s));
+    if (P.refine_tc) {   // x2 only with three planes
+      rc = tc_launch_split3_sumsq((const float*)X, sh.numel, run.B.xbf, run.B.xsplit[0],
+                                  run.B.xsplit[1], run.B.sumsq_part, kSumsqBlocks, st);
+      if (rc) return rc;
+      rc = als_launch_sumsq_final(run.B.sumsq_part, kSumsqBlocks, run.B.ctrl, st);
+    } else {
+      rc = als_launch_sumsq(TypeCode<T>::value, X, sh.numel, run.B.sumsq_part, kSumsqBlocks,
+                            run.B.ctrl, st);
+      if (rc) return rc;
+      rc = tc_launch_to_bf16((const float*)X, sh.numel, run.B.xbf, st);
+    }
+    if (rc) return rc;
+    TLGB_CUDA_TRY(cudaStreamWaitEvent(st, run.ev_join, 0));
+  } else {
+    rc = als_launch_sumsq(TypeCode<T>::value, X, sh.numel, run.B.sumsq_part, kSumsqBlocks,
+                          run.B.ctrl, st);
+    if (rc) return rc;
+    rc = run.grams(nullptr, st);
     if (rc) return rc;
   }
   if (o.callback) {

@@ -107,11 +107,21 @@ mttkrp_split_kernel(const MttkrpArgs<T> a) {
     s_o = o;
   };
 
-  auto load_step = [&](int64_t t) {
-    const int64_t o = t / a.KC;
-    const int64_t c0 = (t % a.KC) * BK;
-    const T* Xo = a.X + outer_offset(o);
+  // (outer slice, chunk) of the next step to load, advanced incrementally:
+  // the 64-bit divisions of the slice index run once per slice, not per step
+  int64_t ld_o = t_begin / a.KC;
+  int64_t ld_kc = t_begin - ld_o * a.KC;
+  int64_t ld_xoff = outer_offset(ld_o);
+  auto load_step = [&]() {
+    const int64_t o = ld_o;
+    const int64_t c0 = ld_kc * BK;
+    const T* Xo = a.X + ld_xoff;
     if (o != s_o) load_scales(o);
+    if (++ld_kc == a.KC) {
+      ld_kc = 0;
+      ++ld_o;
+      if (ld_o * a.KC < a.total_steps) ld_xoff = outer_offset(ld_o);
+    }
 #pragma unroll
     for (int v = 0; v < XV; ++v) {
       const int e = v * kThreads + tid;
@@ -211,13 +221,13 @@ mttkrp_split_kernel(const MttkrpArgs<T> a) {
   }
 
   if (t_begin < t_end) {
-    load_step(t_begin);
+    load_step();
     store_step(0);
     __syncthreads();
     int buf = 0;
     for (int64_t t = t_begin; t < t_end; ++t) {
       const bool has_next = (t + 1 < t_end);
-      if (has_next) load_step(t + 1);
+      if (has_next) load_step();
       const T* A = As + buf * BK * PADM;
       const T* B = Bs + buf * BK * PADN;
       // unrolled by 8: the fully unrolled step (BK x TM x TN FMAs) outgrows

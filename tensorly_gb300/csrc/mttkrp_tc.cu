@@ -420,11 +420,29 @@ __global__ void k_to_bf16(const float* __restrict__ X, int64_t n, __nv_bfloat16*
 // x0 = bf16(x), x1 = bf16(x - x0), x2 = bf16(x - x0 - x1).  The residuals are
 // exact in f32 and x2 holds the last <= 8 significant bits, so the sum is x
 // (for normal numbers).
-__global__ void k_split3_bf16(const float* __restrict__ X, int64_t n, __nv_bfloat16* __restrict__ y0,
-                              __nv_bfloat16* __restrict__ y1, __nv_bfloat16* __restrict__ y2) {
+// Neumaier step of the f32 sum of squares: x*x split exactly into hi + lo.
+__device__ __forceinline__ void sumsq_add(float x, float& s, float& c) {
+  const float hi = x * x;
+  const float lo = fmaf(x, x, -hi);
+  const float t = s + hi;
+  c += ((fabsf(s) >= hi) ? ((s - t) + hi) : ((hi - t) + s)) + lo;
+  s = t;
+}
+
+// part (optional, gridDim.x doubles): the block's share of ||X||^2, summed
+// as in the stand-alone sum-of-squares kernel, so the split's pass over X
+// also gives the norm.
+__global__ void __launch_bounds__(256)
+k_split3_bf16(const float* __restrict__ X, int64_t n, __nv_bfloat16* __restrict__ y0,
+              __nv_bfloat16* __restrict__ y1, __nv_bfloat16* __restrict__ y2, double* part) {
+  float s = 0.f, c = 0.f;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n / 2;
        i += (int64_t)gridDim.x * blockDim.x) {
     const float2 v = reinterpret_cast<const float2*>(X)[i];
+    if (part) {
+      sumsq_add(v.x, s, c);
+      sumsq_add(v.y, s, c);
+    }
     const __nv_bfloat162 a0 = __floats2bfloat162_rn(v.x, v.y);
     const float2 r1 = make_float2(v.x - __low2float(a0), v.y - __high2float(a0));
     const __nv_bfloat162 a1 = __floats2bfloat162_rn(r1.x, r1.y);
@@ -442,6 +460,20 @@ __global__ void k_split3_bf16(const float* __restrict__ X, int64_t n, __nv_bfloa
     y0[n - 1] = a0;
     y1[n - 1] = a1;
     if (y2) y2[n - 1] = __float2bfloat16_rn(r1 - __bfloat162float(a1));
+    if (part) sumsq_add(x, s, c);
+  }
+  if (part) {   // block total in a fixed order
+    __shared__ double red[8];
+    double t = (double)s + (double)c;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double b = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) b += red[w];
+      part[blockIdx.x] = b;
+    }
   }
 }
 
@@ -792,7 +824,14 @@ int tc_launch_split3(const float* X, int64_t n, __nv_bfloat16* x0, __nv_bfloat16
                      (reinterpret_cast<uintptr_t>(x1) % 4) == 0 &&
                      (reinterpret_cast<uintptr_t>(x2) % 4) == 0,   // x2 may be null
                  "split3: misaligned buffers");
-  k_split3_bf16<<<sm_count() * 8, 256, 0, st>>>(X, n, x0, x1, x2);
+  k_split3_bf16<<<sm_count() * 8, 256, 0, st>>>(X, n, x0, x1, x2, nullptr);
+  TLGB_LAUNCH_CHECK();
+  return TLGB_OK;
+}
+
+int tc_launch_split3_sumsq(const float* X, int64_t n, __nv_bfloat16* x0, __nv_bfloat16* x1,
+                           __nv_bfloat16* x2, double* part, int nparts, cudaStream_t st) {
+  k_split3_bf16<<<nparts, 256, 0, st>>>(X, n, x0, x1, x2, part);
   TLGB_LAUNCH_CHECK();
   return TLGB_OK;
 }

@@ -89,6 +89,10 @@ int tc_launch_to_bf16(const float* X, int64_t n, __nv_bfloat16* out, cudaStream_
 // the first two planes are written).
 int tc_launch_split3(const float* X, int64_t n, __nv_bfloat16* x0, __nv_bfloat16* x1,
                      __nv_bfloat16* x2, cudaStream_t st);
+// The same split, which also writes each of its `nparts` blocks' share of
+// ||X||^2 to part (f32 compensated sums, f64 block totals).
+int tc_launch_split3_sumsq(const float* X, int64_t n, __nv_bfloat16* x0, __nv_bfloat16* x1,
+                           __nv_bfloat16* x2, double* part, int nparts, cudaStream_t st);
 // out (planes x R x rows bf16, planes 2 or 3): the bf16 split of A^T,
 // plane 0 = bf16(A^T), plane k = bf16(A^T - planes before k).
 int tc_launch_factor_bf16t(const float* A, int64_t rows, int64_t R, int planes,
