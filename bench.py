@@ -540,14 +540,29 @@ def measure_batched(args, steps, warmup):
     # accuracy: final errors against per-tensor f64 oracle runs on a sample
     import oracle
     fin = final.cpu().numpy()
-    rel = []
+    # A sample tensor whose f64 run has not settled (its error still moving by
+    # more than 1e-6 relative over the last 10 sweeps) is reported apart, with
+    # the NumPy f32 run's own distance from f64 beside the batched kernel's:
+    # there f32 and f64 ALS take different paths whatever computes them.
+    rel, unsettled = [], []
     sample = sorted(set(np.linspace(0, n - 1, min(n, 16)).astype(int).tolist()))
     for t in sample:
         init = oracle.random_cp(xs[t].shape, ranks[t], random_state=seeds[t])[1]
         x64 = xs[t].astype(np.float64)
-        _, f64, _ = oracle.parafac_sweeps(x64, np.ones(ranks[t]), init, sweeps)
+        _, f64, e64s = oracle.parafac_sweeps(x64, np.ones(ranks[t]), init, sweeps)
         e64 = np.linalg.norm(x64 - oracle.cp_to_tensor((None, f64))) / np.linalg.norm(x64)
-        rel.append(abs(fin[t] - e64) / e64)
+        d = abs(fin[t] - e64) / e64
+        if len(e64s) > 10 and abs(e64s[-10] - e64s[-1]) > 1e-6 * e64s[-1]:
+            _, f32, _ = oracle.parafac_sweeps(xs[t].astype(np.float32),
+                                              np.ones(ranks[t], np.float32),
+                                              [i.astype(np.float32) for i in init], sweeps)
+            e32 = np.linalg.norm(x64 - oracle.cp_to_tensor(
+                (None, [f.astype(np.float64) for f in f32]))) / np.linalg.norm(x64)
+            unsettled.append({"tensor": int(t), "shape": list(xs[t].shape),
+                              "rank": int(ranks[t]), "batched_rel_diff": float(d),
+                              "numpy_f32_rel_diff": float(abs(e32 - e64) / e64)})
+        else:
+            rel.append(d)
     # end to end through the public API with host tensors
     e0 = time.perf_counter()
     tg.parafac_batched(xs, ranks, n_iter_max=sweeps, random_state=seeds)
@@ -578,11 +593,13 @@ def measure_batched(args, steps, warmup):
             "config": {"workload": f"{n} uneven 3-way tensors, dims 8-64, rank 4-16, "
                                    f"{sweeps} sweeps", "l2": "0.76 GB of tensors > L2",
                        "autotuned_threads": choice, "autotuned_outer_tiles": tiles},
-            "accuracy_vs_f64": {"max_rel_diff_final_error": float(max(rel)),
-                                "median": float(np.median(rel)),
+            "accuracy_vs_f64": {"max_rel_diff_final_error": float(max(rel)) if rel else None,
+                                "median": float(np.median(rel)) if rel else None,
                                 "within_1e-4": f"{sum(r < 1e-4 for r in rel)}/{len(rel)}",
                                 "sample": f"{len(sample)} tensors spread over the batch, "
-                                          "per-tensor f64 oracle runs from the same init"},
+                                          "per-tensor f64 oracle runs from the same init; "
+                                          "the settled ones above, the others below",
+                                "unsettled": unsettled},
             "mttkrp_tflops": flops / (ms / 1000.0) / 1e12,
             "fp32_pipe_frac_of_nominal": flops / (ms / 1000.0) / 1e12 / FP32_FFMA_PEAK_TFLOPS,
             "per_tensor_gpu": {"value": per_tensor, "unit": "decomps/s",
