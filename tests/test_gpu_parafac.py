@@ -78,6 +78,42 @@ def test_graph_and_check_every_do_not_change_results(gb300, golden):
         assert torch.equal(a, b) and torch.equal(a, c)
 
 
+@pytest.mark.parametrize("precision", ["native", "bf16"])
+def test_deferred_fit_and_lookahead_stop_like_one_sweep_at_a_time(gb300, precision):
+    """A converging run (tol > 0) launched a group ahead of the host, with the
+    last mode's fit deferred to the side stream (the defaults), stops at the
+    same sweep and returns the same bits as sweeps run one at a time with the
+    fit in line, and as graph replay; with small and large groups."""
+    from tensorly_gb300 import _lib
+    lib = _lib.lib()
+    rs = np.random.RandomState(11)
+    fs = [rs.rand(d, 6) for d in (48, 40, 32)]
+    x = torch.as_tensor(np.einsum("ir,jr,kr->ijk", *fs) + 0.01 * rs.randn(48, 40, 32),
+                        dtype=torch.float32, device="cuda")
+    init = [torch.as_tensor(rs.rand(d, 6), dtype=torch.float32, device="cuda")
+            for d in x.shape]
+    kw = dict(n_iter_max=60, tol=1e-7, precision=precision, return_errors=True)
+
+    def run(**extra):
+        (w, f), e = gb300.parafac(x, 6, init=gb300.CPTensor((None, [a.clone() for a in init])),
+                                  **kw, **extra)
+        return w, f, e
+
+    try:
+        lib.tlgb_set_tuning(b"cp_inline_fit", 1)
+        w0, f0, e0 = run(use_graph=False, check_every=1)
+    finally:
+        lib.tlgb_set_tuning(b"cp_inline_fit", 0)
+    assert len(e0) < 60, "the case must converge before n_iter_max"
+    for extra in (dict(), dict(check_every=3), dict(check_every=64),
+                  dict(use_graph=True, check_every=8)):
+        w1, f1, e1 = run(**extra)
+        assert e1 == e0, extra
+        assert torch.equal(w1, w0)
+        for a, b in zip(f1, f0):
+            assert torch.equal(a, b), extra
+
+
 def test_callback_semantics(gb300, golden):
     run = golden["runs"]["dense_cp_small"]
     seen = []
