@@ -886,7 +886,7 @@ k_solve(const T* __restrict__ partial, int splits, int64_t I, int R_in,
         // [W | V hi | V lo] as written by the factorisation, copied with
         // 16-byte loads that are all issued before the first store
         float* Ws = reinterpret_cast<float*>(Vs);
-        const int n = 3 * RR;
+        const int n = (lite ? 2 : 3) * RR;   // the lite residual reads V's hi plane only
         const int n4 = ((reinterpret_cast<uintptr_t>(w32) & 15) == 0) ? n / 4 : 0;
         // asynchronous 16-byte copies (cp.async): all in flight at once and
         // overlapped with the partial sums below; waited for before the first
@@ -909,9 +909,9 @@ k_solve(const T* __restrict__ partial, int splits, int64_t I, int R_in,
         Wm = Ws;
       }
     }
-    if (df) {
+    if (df) {   // the lite Gram accumulates the hi plane only
       float* gh = reinterpret_cast<float*>(gacc);
-      for (int e = tid; e < 2 * RR; e += blockDim.x) gh[e] = 0.f;
+      for (int e = tid; e < (lite ? RR : 2 * RR); e += blockDim.x) gh[e] = 0.f;
     }
     __syncthreads();
     griddep_wait();   // the MTTKRP partials (programmatic launch inside a sweep)
@@ -1175,9 +1175,14 @@ k_solve(const T* __restrict__ partial, int splits, int64_t I, int R_in,
   double* out = gpart + (int64_t)blockIdx.x * RR;
   if (df) {
     float* o = reinterpret_cast<float*>(out);
-    if (kind == 2) {   // the lite Gram has no lo plane (the reducer reads hi only)
+    if (kind == 2 && lite) {
+      // one plane, lower triangle: the entries the reducer reads (df == 2)
       const float* g = reinterpret_cast<const float*>(gacc);
-      for (int e = tid; e < (lite ? RR : 2 * RR); e += blockDim.x) o[e] = g[e];
+      for (int e = tid; e < RR; e += blockDim.x)
+        if (e - (e / R) * R <= e / R) o[e] = g[e];
+    } else if (kind == 2) {
+      const float* g = reinterpret_cast<const float*>(gacc);
+      for (int e = tid; e < 2 * RR; e += blockDim.x) o[e] = g[e];
     } else {
       for (int e = tid; e < RR; e += blockDim.x) {
         const double g = gacc[e];

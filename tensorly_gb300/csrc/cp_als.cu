@@ -347,6 +347,20 @@ struct Runner {
     return TLGB_OK;
   }
 
+  // A fit still deferred when a phase ends early (the host saw the stop flag
+  // and launched no further sweep) runs here, on the main stream before the
+  // next phase clears the flag: it then finds the flag set and records
+  // nothing, instead of running in the next phase on the partials of a
+  // sweep that did no work.
+  int flush_fit(cudaStream_t st) {
+    if (fit_mode < 0) return TLGB_OK;
+    const int mode = fit_mode;
+    fit_mode = -1;
+    return als_launch_gram_reduce_fit<T>(B.gpart, fit_nb, (int)R, B.G, mode, sh.ndim, fit_df,
+                                         weights, B.ipart, fit_nb, B.fpart, B.ctrl, B.errors,
+                                         o.n_iter_max, o.tol, o.cvg_criterion, st, false, B.G32);
+  }
+
   int grams(const int* done, cudaStream_t st) {
     const int RR = (int)(R * R);
     int64_t imax = 0;
@@ -605,6 +619,8 @@ int run(const T* X, const Shape& sh, int64_t R, T* const* factors, T* weights,
         have_prev = true;
         cur ^= 1;
       }
+      rc = run.flush_fit(st);
+      if (rc) return rc;
       if (hc.tc_err != 0 || hc.status != TLGB_OK) break;
       continue;
     }
@@ -650,6 +666,8 @@ int run(const T* X, const Shape& sh, int64_t R, T* const* factors, T* weights,
         if (stopped || hc.done || hc.done_pending) break;  // callback asked to stop, or converged
       }
     }
+    rc = run.flush_fit(st);
+    if (rc) return rc;
     if (o.mttkrp_ms) {  // durations of this phase's last sweep (the host synced above)
       for (int k : run.modes) {
         float ms = 0.f;

@@ -90,9 +90,11 @@ def test_deferred_fit_and_lookahead_stop_like_one_sweep_at_a_time(gb300, precisi
     fs = [rs.rand(d, 6) for d in (48, 40, 32)]
     x = torch.as_tensor(np.einsum("ir,jr,kr->ijk", *fs) + 0.01 * rs.randn(48, 40, 32),
                         dtype=torch.float32, device="cuda")
-    init = [torch.as_tensor(rs.rand(d, 6), dtype=torch.float32, device="cuda")
-            for d in x.shape]
-    kw = dict(n_iter_max=60, tol=1e-7, precision=precision, return_errors=True)
+    # a start near the generating factors: the error change falls below tol
+    # after about 14 sweeps (f64 oracle)
+    init = [torch.as_tensor(f * (1 + 0.3 * rs.randn(*f.shape)), dtype=torch.float32,
+                            device="cuda") for f in fs]
+    kw = dict(n_iter_max=60, tol=1e-5, precision=precision, return_errors=True)
 
     def run(**extra):
         (w, f), e = gb300.parafac(x, 6, init=gb300.CPTensor((None, [a.clone() for a in init])),
