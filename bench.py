@@ -208,24 +208,27 @@ def run_reference(args):
 
 # ----------------------------------------------------------------------------- GPU arm
 def launches_per_step(ndim, sweeps, refine, precision, rank=64):
-    """Kernel launches of one parafac call (library structure):
-    set-up: sum-of-squares (2) + one Gram per mode (2 each) [+ tensor split or
-    cast (1) + factor planes (ndim)];
-    per sweep and mode: fast + fallback factorisation (2), MTTKRP (1, or 3 for
-    the three-plane f32 split), solve (1), Gram reduce (1); then the fit (1).
-    The closing sweep runs its last mode's MTTKRP on the SIMT kernel."""
+    """Kernel launches of one parafac call (library structure; matches the
+    ncu launch list of a call):
+    set-up: the norm (2: partial sums + final) and one Gram per mode (2
+    each); in bf16 the tensor split also sums the norm (1 + 1) and the factor
+    planes add one launch per mode;
+    per sweep and mode: fast + fallback factorisation (2), MTTKRP (1; 2 in
+    the closing sweeps: x0 and x1 planes), solve (1), Gram reduction (1; the
+    last mode's also computes the fit).  The last closing sweep runs its last
+    mode's MTTKRP on the SIMT kernel (1)."""
     mode_cost = 5
     if precision != "bf16":
-        return 2 + 2 * ndim + sweeps * (mode_cost * ndim + 1)
-    setup = 2 + 2 * ndim + 1 + ndim
+        return 2 + 2 * ndim + sweeps * mode_cost * ndim
+    setup = 2 + 2 * ndim + ndim
     refine = min(refine, sweeps)
     bf16 = sweeps - refine
     if refine == 0:
-        return setup + bf16 * (mode_cost * ndim + 1)
-    split = 7 if rank <= 64 else mode_cost      # three MTTKRP launches per mode
-    n = setup + bf16 * (mode_cost * ndim + 1)
-    n += (refine - 1) * (split * ndim + 1)
-    n += split * (ndim - 1) + mode_cost + 1
+        return setup + bf16 * mode_cost * ndim
+    closing = mode_cost + 1                      # two MTTKRP launches per mode
+    n = setup + bf16 * mode_cost * ndim
+    n += (refine - 1) * closing * ndim
+    n += closing * (ndim - 1) + mode_cost
     return n
 
 
@@ -447,6 +450,8 @@ def run_gpu(args):
         line["batched"] = measure_batched(args, steps=3, warmup=3)
         torch.cuda.empty_cache()
         line["tucker_cp_128x4"] = measure_tucker(args, steps=3, warmup=3)
+        torch.cuda.empty_cache()
+        line["learned_warm_start"] = measure_learned(args, steps=3, warmup=3)
     print(json.dumps(line), flush=True)
 
 
@@ -631,12 +636,19 @@ def _learned_cpu_sample(seeds, n_sample, tol, max_sweeps):
 
 
 def run_learned(args):
-    import torch
-    import tensorly_gb300 as tg
-    from tensorly_gb300 import _lib, learned
     ws_n, rank, _ = dist_env()
     if rank != 0:
         return
+    line = measure_learned(args, args.steps, args.warmup)
+    print(json.dumps(line), flush=True)
+
+
+def measure_learned(args, steps, warmup):
+    """The C5 line (learned warm start on 10,000 held-out tensors), as a dict;
+    also a sub-object of the default run."""
+    import torch
+    import tensorly_gb300 as tg
+    from tensorly_gb300 import _lib, learned
     n = 10000
     tol, max_sweeps = 1e-6, 300
     seeds = np.arange(10 ** 6, 10 ** 6 + n)
@@ -655,8 +667,7 @@ def run_learned(args):
                                  "kind": "port", "sample": "8 tensors, parafac(init='svd', tol)"},
                 "e2e": {"value": v, "unit": "decomps/s", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}}
-        print(json.dumps(line), flush=True)
-        return
+        return line
     tg.build() if not os.path.exists(_lib.library_path()) else None
     dev = torch.device("cuda", torch.cuda.current_device())
     gen = learned.Generator(dev)
@@ -675,7 +686,7 @@ def run_learned(args):
         F, _, _ = learned.warm_start(net, X, gen.omega)
         return learned._als(X, F, max_sweeps, tol=tol)
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         step()
     fallback_any = bool(learned.warm_start(net, X, gen.omega)[1].any().item())
     torch.cuda.synchronize()
@@ -684,12 +695,12 @@ def run_learned(args):
     clocks = ClockSampler(dev.index)
     clocks.start()
     ev0.record(st)
-    for _ in range(args.steps):
+    for _ in range(steps):
         prob = step()
     ev1.record(st)
     torch.cuda.synchronize()
     clk = clocks.stop()
-    ms = ev0.elapsed_time(ev1) / args.steps
+    ms = ev0.elapsed_time(ev1) / steps
     # inference alone: sketch + network + lift for the whole batch
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -725,7 +736,7 @@ def run_learned(args):
                 "median_final_err": float(np.median(res["err_" + k]))}
 
     line = {"metric": LEARNED_METRIC, "value": n / (ms / 1000.0), "unit": "decomps/s",
-            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "n_gpus": 1, "steps": steps, "warmup": warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
             "config": {"workload": workload, "l2": "1.3 GB of tensors > L2",
@@ -744,8 +755,8 @@ def run_learned(args):
                     "d2h_bytes_per_step": int(fb.numel() * 4 + fe.numel() * 8)},
             # per step: sketch, 3 GEMMs + skip, loss/scale, lift, the batched ALS
             # kernel (+ gram3, eig and scale when a tensor falls back to the SVD start)
-            "clocks": clk, "gpu_launches": (8 + (3 if fallback_any else 0)) * args.steps}
-    print(json.dumps(line), flush=True)
+            "clocks": clk, "gpu_launches": (8 + (3 if fallback_any else 0)) * steps}
+    return line
 
 
 TUCKER_METRIC = "Tucker-HOOI iterations/s at 128^4 f32 rank 16^4 (init='svd' included)"
