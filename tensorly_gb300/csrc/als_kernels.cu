@@ -886,7 +886,8 @@ k_solve(const T* __restrict__ partial, int splits, int64_t I, int R_in,
         // [W | V hi | V lo] as written by the factorisation, copied with
         // 16-byte loads that are all issued before the first store
         float* Ws = reinterpret_cast<float*>(Vs);
-        const int n = (lite ? 2 : 3) * RR;   // the lite residual reads V's hi plane only
+        // the lite solve reads W (and, with a correction pass, V's hi plane)
+        const int n = (lite ? (max_passes > 0 ? 2 : 1) : 3) * RR;
         const int n4 = ((reinterpret_cast<uintptr_t>(w32) & 15) == 0) ? n / 4 : 0;
         // asynchronous 16-byte copies (cp.async): all in flight at once and
         // overlapped with the partial sums below; waited for before the first

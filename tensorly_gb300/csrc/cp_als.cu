@@ -314,9 +314,12 @@ struct Runner {
       rc = als_launch_solve<T>((const T*)partial, splits, sh.dim[mode], (int)R, B.fac, B.perm,
                                B.vmat, B.w32, factors[mode], B.fbt[mode], B.gpart,
                                last ? B.ipart : nullptr, B.ctrl,
-                               // the bf16 MTTKRP is accurate to ~1e-6, so one plain-f32
-                               // refinement pass (solve error ~cond * 6e-8) is enough there
-                               (tc && P->tc[mode].valid) ? 1 : kIrMaxPasses, &nb, st, pdl, lite);
+                               // the bf16 sweeps take x = m W (f32 inverse) with no
+                               // correction pass: their MTTKRP is itself only accurate
+                               // to ~1e-6, and the closing sweeps solve in double-float
+                               (tc && P->tc[mode].valid) ? (tc_tuning().lite_correction ? 1 : 0)
+                                                         : kIrMaxPasses,
+                               &nb, st, pdl, lite);
       if (rc) return rc;
       if (last && defer_fit && !o.normalize_factors && !tc_tuning().inline_fit) {
         fit_mode = mode;

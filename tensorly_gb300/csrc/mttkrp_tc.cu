@@ -1009,6 +1009,7 @@ extern "C" int tlgb_set_tuning(const char* key, int value) {
   else if (k == "closing_planes") tc_tuning().closing_planes = value;
   else if (k == "cp_graph_sweeps") tc_tuning().graph_sweeps = value;
   else if (k == "cp_inline_fit") tc_tuning().inline_fit = value;
+  else if (k == "cp_lite_correction") tc_tuning().lite_correction = value;
 
   else return batched_set_tuning(k, value);   // the batched CP-ALS variants
   return TLGB_OK;
