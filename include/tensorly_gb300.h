@@ -145,7 +145,8 @@ int tlgb_mttkrp_bf16(const void* X, int ndim, const int64_t* shape, const void* 
  * "cp_inline_fit" = 1 runs every sweep's last Gram reduction and fit on the
  * main stream instead of deferring it to the side stream under the next
  * sweep; "cp_lite_correction" = 1 adds one f32 correction pass to the bf16
- * sweeps' solve x = m V^-1;
+ * sweeps' solve x = m V^-1; "tc_l2_keep" = 1 loads the tensor-core MTTKRP's
+ * tensor tiles without the evict-first L2 policy;
  * "batched_threads_small" / "_medium" / "_large" = threads per CTA (128, 256
  * or 512; 4, 2 or 1 CTAs per SM) of tlgb_cp_als_batched for the tensors
  * whose padded size fits 128-, 256-thread CTAs' shared memory, or neither;

@@ -61,6 +61,7 @@ struct TcArgs {
   // Test of the timeout path (tuning key "tc_test_starve"): the producer
   // issues no copies, and the MMA and epilogue waits give up after 1 ms.
   int starve;
+  int l2_stream;   // tensor tiles loaded with an evict-first L2 policy
 };
 constexpr unsigned long long kStarveWaitNs = 1000000ull;  // 1 ms
 
@@ -177,12 +178,21 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant_
         int stage = 0;
         uint32_t phase = 0;
         int64_t i = 0;
+        const uint64_t pol = l2_policy_evict_first();
         auto issue = [&]() -> bool {   // the tensor tile of the next step
           if (!mbar_wait(&empty[stage], phase ^ 1u, a.err, failed)) return false;
           mbar_expect_tx(&full[stage], kStageBytes);
           unsigned char* dst = sA + stage * kStageBytes;
           const int cx = (kc0 + kc) * kChunk;
-          if (!MN) {
+          if (a.l2_stream) {
+            if (!MN) {
+              tma_load_4d_hint(dst, &tmX, &full[stage], cx, (int)m0, c2, c3, pol);
+            } else {
+              tma_load_4d_hint(dst, &tmX, &full[stage], (int)m0, cx, c2, c3, pol);
+              tma_load_4d_hint(dst + kStageBytes / 2, &tmX, &full[stage], (int)m0 + 64, cx, c2,
+                               c3, pol);
+            }
+          } else if (!MN) {
             tma_load_4d(dst, &tmX, &full[stage], cx, (int)m0, c2, c3);
           } else {
             tma_load_4d(dst, &tmX, &full[stage], (int)m0, cx, c2, c3);
@@ -768,6 +778,7 @@ int mttkrp_tc_launch_maps(const TcPlan& p, const TcMaps& maps, const float* cons
   a.err = err;
   a.skip = skip_flag;
   a.starve = tc_tuning().test_starve;
+  a.l2_stream = tc_tuning().l2_keep ? 0 : 1;
   if (p.npl == 2) {
     switch (p.n_pad) {
       case 16: return launch_mn<16, 2>(p, tx, tf, a, st);
@@ -1009,6 +1020,7 @@ extern "C" int tlgb_set_tuning(const char* key, int value) {
   else if (k == "closing_planes") tc_tuning().closing_planes = value;
   else if (k == "cp_graph_sweeps") tc_tuning().graph_sweeps = value;
   else if (k == "cp_inline_fit") tc_tuning().inline_fit = value;
+  else if (k == "tc_l2_keep") tc_tuning().l2_keep = value;
   else if (k == "cp_lite_correction") tc_tuning().lite_correction = value;
 
   else return batched_set_tuning(k, value);   // the batched CP-ALS variants

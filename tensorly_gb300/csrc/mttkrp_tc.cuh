@@ -49,6 +49,7 @@ struct TcTuning {
   int closing_planes = 0;     // 3: the closing sweeps also contract the third tensor plane
   int graph_sweeps = 0;       // > 0: at most this many CP-ALS sweeps per CUDA graph
   int inline_fit = 0;         // 1: every CP-ALS sweep runs its last mode's fit in line
+  int l2_keep = 0;            // 1: tensor tiles loaded without the evict-first L2 policy
   int lite_correction = 0;    // 1: the bf16 sweeps' solve adds one f32 correction pass to x = m W
 };
 TcTuning& tc_tuning();
