@@ -1,5 +1,6 @@
 // SIMT MTTKRP kernels (f32 / f64).  See mttkrp_simt.cuh for the formulation.
 #include "mttkrp_simt.cuh"
+#include "mttkrp_tc.cuh"   // tc_tuning
 
 namespace tlgb {
 
@@ -10,6 +11,23 @@ constexpr int kThreads = 128;  // 4 warps
 template <typename T> struct Vec;
 template <> struct Vec<float> { using type = float4; static constexpr int n = 4; };
 template <> struct Vec<double> { using type = double2; static constexpr int n = 2; };
+
+// A 16-byte read-only load of the streamed tensor with an evict-first L2
+// policy (it is read once per MTTKRP), so it does not push the factors and
+// the partial tiles out of L2; f64 keeps the plain load.
+__device__ __forceinline__ uint64_t l2_evict_first_policy() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ float4 ldg_stream(const float4* a, uint64_t pol) {
+  float4 v;
+  asm volatile("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+               : "l"(a), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ double2 ldg_stream(const double2* a, uint64_t) { return __ldg(a); }
 
 template <typename T, int N>
 __device__ __forceinline__ void ld_smem(const T* p, T (&v)[N]) {
@@ -107,6 +125,7 @@ mttkrp_split_kernel(const MttkrpArgs<T> a) {
     s_o = o;
   };
 
+  const uint64_t xpol = l2_evict_first_policy();
   // (outer slice, chunk) of the next step to load, advanced incrementally:
   // the 64-bit divisions of the slice index run once per slice, not per step
   int64_t ld_o = t_begin / a.KC;
@@ -137,7 +156,8 @@ mttkrp_split_kernel(const MttkrpArgs<T> a) {
         const bool inb = (m < a.I_out) && (c < a.C);
         if (inb) {
           using V = typename Vec<T>::type;
-          V x = __ldg(reinterpret_cast<const V*>(Xo + m * a.s_out + c * a.s_c));
+          const V* xp = reinterpret_cast<const V*>(Xo + m * a.s_out + c * a.s_c);
+          V x = a.l2_stream ? ldg_stream(xp, xpol) : __ldg(xp);
           if constexpr (VEC == 4) { xr[v][0] = x.x; xr[v][1] = x.y; xr[v][2] = x.z; xr[v][3] = x.w; }
           else { xr[v][0] = x.x; xr[v][1] = x.y; }
         } else {
@@ -405,6 +425,7 @@ int mttkrp_launch_partials(const MttkrpPlan& p, const T* X, const T* const* fact
   a.vec_f = ((reinterpret_cast<uintptr_t>(a.F) % 16) == 0) && (p.R % VEC == 0);
   a.partial = partial;
   a.skip_flag = skip_flag;
+  a.l2_stream = tc_tuning().l2_keep ? 0 : 1;
   switch (p.bn) {
     case 16: return launch_bn<T, 16>(a, p, stream);
     case 32: return launch_bn<T, 32>(a, p, stream);

@@ -36,6 +36,7 @@ struct MttkrpArgs {
   int vec_x, vec_f;              // 16-byte vector loads allowed
   T* partial;                    // [splits][I_out][R]
   const int* skip_flag;          // kernel returns at once if *skip_flag != 0 (may be null)
+  int l2_stream;                 // f32 tensor loads with an evict-first L2 policy
 };
 
 struct MttkrpPlan {
