@@ -25,6 +25,46 @@ int batched_set_tuning(const std::string& key, int value);
 // wrote (or writes anything an earlier kernel reads).  griddep_wait() is a
 // no-op in a kernel launched the ordinary way.  griddep_launch_dependents()
 // lets the next such kernel of the stream be scheduled early.
+// Read-only loads of data read once (a streamed tensor) with an
+// evict-first L2 policy, so they do not push data that is read again out of
+// L2 (factors, partial tiles, the next product's input).
+__device__ __forceinline__ uint64_t l2_evict_first_policy() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ float4 ldg_stream(const float4* a, uint64_t pol) {
+  float4 v;
+  asm volatile("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+               : "l"(a), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ float2 ldg_stream(const float2* a, uint64_t pol) {
+  float2 v;
+  asm volatile("ld.global.nc.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;"
+               : "=f"(v.x), "=f"(v.y)
+               : "l"(a), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ float ldg_stream(const float* a, uint64_t pol) {
+  float v;
+  asm volatile("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(a), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ double2 ldg_stream(const double2* a, uint64_t pol) {
+  double2 v;
+  asm volatile("ld.global.nc.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;"
+               : "=d"(v.x), "=d"(v.y)
+               : "l"(a), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ double ldg_stream(const double* a, uint64_t pol) {
+  double v;
+  asm volatile("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(a), "l"(pol));
+  return v;
+}
+
 __device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void griddep_launch_dependents() {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");

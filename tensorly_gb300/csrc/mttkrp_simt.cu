@@ -12,23 +12,6 @@ template <typename T> struct Vec;
 template <> struct Vec<float> { using type = float4; static constexpr int n = 4; };
 template <> struct Vec<double> { using type = double2; static constexpr int n = 2; };
 
-// A 16-byte read-only load of the streamed tensor with an evict-first L2
-// policy (it is read once per MTTKRP), so it does not push the factors and
-// the partial tiles out of L2; f64 keeps the plain load.
-__device__ __forceinline__ uint64_t l2_evict_first_policy() {
-  uint64_t p;
-  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
-  return p;
-}
-__device__ __forceinline__ float4 ldg_stream(const float4* a, uint64_t pol) {
-  float4 v;
-  asm volatile("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
-               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
-               : "l"(a), "l"(pol));
-  return v;
-}
-__device__ __forceinline__ double2 ldg_stream(const double2* a, uint64_t) { return __ldg(a); }
-
 template <typename T, int N>
 __device__ __forceinline__ void ld_smem(const T* p, T (&v)[N]) {
   // N consecutive elements from a 16-byte aligned shared address

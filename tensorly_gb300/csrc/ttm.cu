@@ -8,6 +8,7 @@
 // contraction runs along the contiguous dimension.  SIMT f32 / f64 tiles,
 // 16-byte vector loads along whichever dimension is contiguous.
 #include <type_traits>
+#include "mttkrp_tc.cuh"   // tc_tuning
 
 #include "linalg.cuh"
 
@@ -193,7 +194,7 @@ constexpr size_t kStreamSmemMax = 96 * 1024;   // W in shared memory: I * JP ele
 template <typename T, int JP, int V>
 __global__ void __launch_bounds__(kStreamThreads)
 ttm_stream_kernel(const T* __restrict__ X, const T* __restrict__ U, T* __restrict__ Y, int64_t L,
-                  int I, int64_t Tt, int J, int transpose) {
+                  int I, int64_t Tt, int J, int transpose, int l2_stream) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* Ws = reinterpret_cast<T*>(smem_raw);   // [I][JP]
   const int tid = threadIdx.x;
@@ -208,6 +209,7 @@ ttm_stream_kernel(const T* __restrict__ X, const T* __restrict__ U, T* __restric
   // threads over (l, t / V) jointly, so a short t range does not idle lanes
   const int64_t tv = Tt / V;
   const int64_t total = L * tv;
+  const uint64_t xpol = l2_evict_first_policy();   // X is streamed once
   for (int64_t g = (int64_t)blockIdx.x * kStreamThreads + tid; g < total;
        g += (int64_t)gridDim.x * kStreamThreads) {
     const int64_t l = g / tv;
@@ -223,7 +225,8 @@ ttm_stream_kernel(const T* __restrict__ X, const T* __restrict__ U, T* __restric
 #pragma unroll
       for (int u = 0; u < kRowBatch; ++u) {
         if (i0 + u < I) {
-          const Vec x = __ldg(reinterpret_cast<const Vec*>(xp + (int64_t)(i0 + u) * Tt));
+          const Vec* xa = reinterpret_cast<const Vec*>(xp + (int64_t)(i0 + u) * Tt);
+          const Vec x = l2_stream ? ldg_stream(xa, xpol) : __ldg(xa);
           const T* xv = reinterpret_cast<const T*>(&x);
 #pragma unroll
           for (int v = 0; v < V; ++v) xs[u][v] = xv[v];
@@ -273,7 +276,8 @@ int launch_stream(const T* X, const T* U, T* Y, int64_t L, int I, int64_t Tt, in
   }
   const int64_t tb = std::min<int64_t>(ceil_div(L * (Tt / V), kStreamThreads), 1ll << 30);
   dim3 grid((unsigned)tb);
-  ttm_stream_kernel<T, JP, V><<<grid, kStreamThreads, smem, st>>>(X, U, Y, L, I, Tt, J, transpose);
+  ttm_stream_kernel<T, JP, V><<<grid, kStreamThreads, smem, st>>>(X, U, Y, L, I, Tt, J, transpose,
+                                                                  tc_tuning().l2_keep ? 0 : 1);
   TLGB_LAUNCH_CHECK();
   return TLGB_OK;
 }
