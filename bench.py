@@ -234,8 +234,9 @@ def launches_per_step(ndim, sweeps, refine, precision, rank=64):
 
 # DRAM bytes (read + write) per launch of the dominant kernel at 512^3 rank 64,
 # from one-kernel ncu captures (dram__bytes_read.sum + dram__bytes_write.sum;
-# the bf16 figure from the tcgen05 MTTKRP with the default tiles).
-NCU_TRAFFIC = {"native": 537485312 + 13983488, "bf16": 268767232 + 3389184}
+# the bf16 figure from the tcgen05 MTTKRP with the default tiles, the native
+# one from the SIMT f32 MTTKRP, both at their current builds).
+NCU_TRAFFIC = {"native": 537303552 + 5170944, "bf16": 268758784 + 3906816}
 KERNEL = {"native": "mttkrp_split_kernel<float,64> + reduce (SIMT f32)",
           "bf16": "mttkrp_tc_kernel (tcgen05 bf16, TMA)"}
 
