@@ -446,30 +446,63 @@ __global__ void __launch_bounds__(256)
 k_split3_bf16(const float* __restrict__ X, int64_t n, __nv_bfloat16* __restrict__ y0,
               __nv_bfloat16* __restrict__ y1, __nv_bfloat16* __restrict__ y2, double* part) {
   float s = 0.f, c = 0.f;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n / 2;
+  // four elements an iteration (16-byte loads, 8-byte stores a plane) when
+  // every pointer allows it, else two
+  const bool v4 = ((reinterpret_cast<uintptr_t>(X) & 15) | (reinterpret_cast<uintptr_t>(y0) & 7) |
+                   (reinterpret_cast<uintptr_t>(y1) & 7) |
+                   (y2 ? (reinterpret_cast<uintptr_t>(y2) & 7) : 0)) == 0;
+  const int W = v4 ? 4 : 2;
+  const int64_t nv = n / W;
+  auto split2 = [&](float x, float y, __nv_bfloat162& a0, __nv_bfloat162& a1,
+                    __nv_bfloat162& a2) {
+    a0 = __floats2bfloat162_rn(x, y);
+    const float2 r1 = make_float2(x - __low2float(a0), y - __high2float(a0));
+    a1 = __floats2bfloat162_rn(r1.x, r1.y);
+    a2 = __floats2bfloat162_rn(r1.x - __low2float(a1), r1.y - __high2float(a1));
+  };
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nv;
        i += (int64_t)gridDim.x * blockDim.x) {
-    const float2 v = reinterpret_cast<const float2*>(X)[i];
-    if (part) {
-      sumsq_add(v.x, s, c);
-      sumsq_add(v.y, s, c);
+    if (v4) {
+      const float4 v = reinterpret_cast<const float4*>(X)[i];
+      if (part) {
+        sumsq_add(v.x, s, c);
+        sumsq_add(v.y, s, c);
+        sumsq_add(v.z, s, c);
+        sumsq_add(v.w, s, c);
+      }
+      __nv_bfloat162 p0, p1, p2, q0, q1, q2;
+      split2(v.x, v.y, p0, p1, p2);
+      split2(v.z, v.w, q0, q1, q2);
+      auto pack = [](__nv_bfloat162 lo, __nv_bfloat162 hi) {
+        return make_uint2(*reinterpret_cast<const unsigned*>(&lo),
+                          *reinterpret_cast<const unsigned*>(&hi));
+      };
+      reinterpret_cast<uint2*>(y0)[i] = pack(p0, q0);
+      reinterpret_cast<uint2*>(y1)[i] = pack(p1, q1);
+      if (y2) reinterpret_cast<uint2*>(y2)[i] = pack(p2, q2);   // the third plane is optional
+    } else {
+      const float2 v = reinterpret_cast<const float2*>(X)[i];
+      if (part) {
+        sumsq_add(v.x, s, c);
+        sumsq_add(v.y, s, c);
+      }
+      __nv_bfloat162 p0, p1, p2;
+      split2(v.x, v.y, p0, p1, p2);
+      reinterpret_cast<__nv_bfloat162*>(y0)[i] = p0;
+      reinterpret_cast<__nv_bfloat162*>(y1)[i] = p1;
+      if (y2) reinterpret_cast<__nv_bfloat162*>(y2)[i] = p2;
     }
-    const __nv_bfloat162 a0 = __floats2bfloat162_rn(v.x, v.y);
-    const float2 r1 = make_float2(v.x - __low2float(a0), v.y - __high2float(a0));
-    const __nv_bfloat162 a1 = __floats2bfloat162_rn(r1.x, r1.y);
-    reinterpret_cast<__nv_bfloat162*>(y0)[i] = a0;
-    reinterpret_cast<__nv_bfloat162*>(y1)[i] = a1;
-    if (y2)   // the third plane is optional
-      reinterpret_cast<__nv_bfloat162*>(y2)[i] =
-          __floats2bfloat162_rn(r1.x - __low2float(a1), r1.y - __high2float(a1));
   }
-  if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
-    const float x = X[n - 1];
+  // the last n mod W elements, one a thread of block 0
+  if (blockIdx.x == 0 && threadIdx.x < n - nv * W) {
+    const int64_t e = nv * W + threadIdx.x;
+    const float x = X[e];
     const __nv_bfloat16 a0 = __float2bfloat16_rn(x);
     const float r1 = x - __bfloat162float(a0);
     const __nv_bfloat16 a1 = __float2bfloat16_rn(r1);
-    y0[n - 1] = a0;
-    y1[n - 1] = a1;
-    if (y2) y2[n - 1] = __float2bfloat16_rn(r1 - __bfloat162float(a1));
+    y0[e] = a0;
+    y1[e] = a1;
+    if (y2) y2[e] = __float2bfloat16_rn(r1 - __bfloat162float(a1));
     if (part) sumsq_add(x, s, c);
   }
   if (part) {   // block total in a fixed order
