@@ -213,11 +213,12 @@ def launches_per_step(ndim, sweeps, refine, precision, rank=64):
     set-up: the norm (2: partial sums + final) and one Gram per mode (2
     each); in bf16 the tensor split also sums the norm (1 + 1) and the factor
     planes add one launch per mode;
-    per sweep and mode: fast + fallback factorisation (2), MTTKRP (1; 2 in
-    the closing sweeps: x0 and x1 planes), solve (1), Gram reduction (1; the
-    last mode's also computes the fit).  The last closing sweep runs its last
-    mode's MTTKRP on the SIMT kernel (1)."""
-    mode_cost = 5
+    per sweep and mode: the factorisation (1, with its f64 fallback in the
+    same launch), MTTKRP (1; 2 in the closing sweeps: x0 and x1 planes),
+    solve (1), Gram reduction (1; the last mode's also computes the fit).
+    The last closing sweep runs its last mode's MTTKRP on the SIMT kernel
+    (1)."""
+    mode_cost = 4
     if precision != "bf16":
         return 2 + 2 * ndim + sweeps * mode_cost * ndim
     setup = 2 + 2 * ndim + ndim

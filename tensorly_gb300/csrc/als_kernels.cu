@@ -269,6 +269,10 @@ __device__ __forceinline__ void df_add(float& h, float& l, float bh, float bl) {
   h = u;
 }
 
+template <typename T>
+__device__ void factorize_f64(const double* G, int ndim, int mode, int R, const T* w, double l2,
+                              double* fac, int* perm, double* V, AlsCtrl* ctrl);
+
 // Stop test of the kernels that run after a deferred fit in stream order (the
 // solves, the factorisations, the fits): true when either flag is set; a
 // solve (promote) raises `done` from `done_pending` for the kernels after it.
@@ -285,7 +289,7 @@ template <typename T, int TI, int TJ, int NI, int NJ>
 __global__ void __launch_bounds__(TI * TJ)
 k_factorize_fast(const double* __restrict__ G, const float* __restrict__ G32, int ndim, int mode,
                  int R, const T* __restrict__ w, double l2, double* __restrict__ vmat,
-                 float* __restrict__ w32, AlsCtrl* ctrl) {
+                 float* __restrict__ w32, AlsCtrl* ctrl, double* fac, int* perm) {
   constexpr int N = TI * NI;
   constexpr int B = kGjBlock;
   constexpr int NT = TI * TJ;
@@ -523,6 +527,10 @@ k_factorize_fast(const double* __restrict__ G, const float* __restrict__ G32, in
       }
   }
   if (tid == 0) ctrl->fac_kind = ok ? 2 : 3;
+  if (!ok) {   // uniform: the f64 Cholesky / LU in the same launch
+    __syncthreads();
+    factorize_f64<T>(G, ndim, mode, R, w, l2, fac, perm, vmat, ctrl);
+  }
 }
 
 // ---- fallback: f64 Cholesky (fac_kind 0) or LU with partial pivoting
@@ -533,9 +541,8 @@ k_factorize_fast(const double* __restrict__ G, const float* __restrict__ G32, in
 // from hosting a tensor-core MTTKRP CTA that runs concurrently on another
 // stream.
 template <typename T>
-__global__ void __launch_bounds__(256)
-k_factorize(const double* G, int ndim, int mode, int R, const T* w, double l2, double* fac,
-            int* perm, double* V, AlsCtrl* ctrl) {
+__device__ void factorize_f64(const double* G, int ndim, int mode, int R, const T* w, double l2,
+                              double* fac, int* perm, double* V, AlsCtrl* ctrl) {
   if (als_stopped(ctrl) || ctrl->fac_kind != 3) return;
   __shared__ int s_fail;
   __shared__ int s_piv;
@@ -620,6 +627,13 @@ k_factorize(const double* G, int ndim, int mode, int R, const T* w, double l2, d
     ctrl->fac_kind = 1;
     if (s_fail == 2) ctrl->status = TLGB_ESINGULAR;
   }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_factorize(const double* G, int ndim, int mode, int R, const T* w, double l2, double* fac,
+            int* perm, double* V, AlsCtrl* ctrl) {
+  factorize_f64<T>(G, ndim, mode, R, w, l2, fac, perm, V, ctrl);
 }
 
 // ---------------------------------------------------------------- solve
@@ -1473,9 +1487,10 @@ int als_launch_gram_reduce(const double* gpart, int nparts, int R, double* G, co
 
 template <typename T, int TI, int TJ, int NI, int NJ>
 static void launch_fast(const double* G, const float* G32, int ndim, int mode, int R, const T* w,
-                        double l2, double* vmat, float* w32, AlsCtrl* ctrl, cudaStream_t st) {
+                        double l2, double* vmat, float* w32, AlsCtrl* ctrl, double* fac, int* perm,
+                        cudaStream_t st) {
   k_factorize_fast<T, TI, TJ, NI, NJ><<<1, TI * TJ, 0, st>>>(G, G32, ndim, mode, R, w, l2, vmat,
-                                                             w32, ctrl);
+                                                             w32, ctrl, fac, perm);
 }
 
 // Hands every factorisation to the f64 kernel (the "f64_factorize" tuning key).
@@ -1492,16 +1507,22 @@ int als_launch_factorize(const double* G, int ndim, int mode, int R, const T* we
   if (tc_tuning().f64_factorize)
     k_force_f64_factorize<<<1, 32, 0, st>>>(ctrl);
   else if (R <= 32)
-    launch_fast<T, 8, 16, 4, 2>(G, G32, ndim, mode, R, weights, l2_reg, vmat, w32, ctrl, st);
+    launch_fast<T, 8, 16, 4, 2>(G, G32, ndim, mode, R, weights, l2_reg, vmat, w32, ctrl, fac,
+                                    perm, st);
   else if (R <= 64)
-    launch_fast<T, 16, 16, 4, 4>(G, G32, ndim, mode, R, weights, l2_reg, vmat, w32, ctrl, st);
+    launch_fast<T, 16, 16, 4, 4>(G, G32, ndim, mode, R, weights, l2_reg, vmat, w32, ctrl, fac,
+                                    perm, st);
   else if (R <= 96)
-    launch_fast<T, 16, 16, 6, 6>(G, G32, ndim, mode, R, weights, l2_reg, vmat, w32, ctrl, st);
+    launch_fast<T, 16, 16, 6, 6>(G, G32, ndim, mode, R, weights, l2_reg, vmat, w32, ctrl, fac,
+                                    perm, st);
   else
-    launch_fast<T, 16, 16, 10, 10>(G, G32, ndim, mode, R, weights, l2_reg, vmat, w32, ctrl, st);
+    launch_fast<T, 16, 16, 10, 10>(G, G32, ndim, mode, R, weights, l2_reg, vmat, w32, ctrl, fac,
+                                    perm, st);
   TLGB_LAUNCH_CHECK();
-  k_factorize<T><<<1, 256, 0, st>>>(G, ndim, mode, R, weights, l2_reg, fac, perm, vmat, ctrl);
-  TLGB_LAUNCH_CHECK();
+  if (tc_tuning().f64_factorize) {   // (the fast kernel otherwise falls back in its own launch)
+    k_factorize<T><<<1, 256, 0, st>>>(G, ndim, mode, R, weights, l2_reg, fac, perm, vmat, ctrl);
+    TLGB_LAUNCH_CHECK();
+  }
   return TLGB_OK;
 }
 
