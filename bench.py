@@ -46,7 +46,7 @@ def parse():
     p.add_argument("--size", type=int, default=512)
     p.add_argument("--rank", type=int, default=64)
     p.add_argument("--sweeps", type=int, default=50)
-    p.add_argument("--refine", type=int, default=3)
+    p.add_argument("--refine", type=int, default=1)
     p.add_argument("--cpu-sweeps", type=int, default=40)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--workload", default="dense",
@@ -281,7 +281,7 @@ def run_gpu(args):
     if args.precision == "bf16" and not args.no_tune:
         # tensor-core MTTKRP tile choices for this tensor (outside the timed region)
         from tensorly_gb300 import autotune
-        tiles = autotune.tune_dense(x, args.rank)
+        tiles = autotune.tune_dense(x, args.rank, sweeps=args.sweeps, refine_sweeps=args.refine)
 
     def step(times=None):
         return tg.parafac(x, args.rank, init=tg.CPTensor((None, init)), mttkrp_times=times, **kw)

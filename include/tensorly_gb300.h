@@ -234,7 +234,7 @@ typedef struct tlgb_cp_als_options {
   int precision;           /* TLGB_PREC_NATIVE or TLGB_PREC_BF16 (f32 tensors only) */
   int refine_sweeps;       /* TLGB_PREC_BF16: closing sweeps with an f32-accurate MTTKRP
                               (tensor cores on the exact 3-plane bf16 split of X and
-                              the factor when rank <= 64, else the SIMT f32 kernel) */
+                              the factor when rank <= 64, else the SIMT f32 kernel); 1 by default */
   int check_every;         /* sweeps between host reads of the device stop flag (>= 1) */
   int use_graph;           /* 1: replay groups of captured sweeps as CUDA graphs; 0 (default):
                               launch the sweeps directly, a group ahead of the host's reads */

@@ -133,7 +133,7 @@ def _time_dense(x, rank, init, sweeps, reps, refine_sweeps):
     return a.elapsed_time(b) / reps
 
 
-def tune_dense(x, rank, sweeps=50, refine_sweeps=3, reps=2, min_gain=0.01, verbose=False):
+def tune_dense(x, rank, sweeps=50, refine_sweeps=1, reps=2, min_gain=0.01, verbose=False):
     """Pick the tensor-core MTTKRP's inner-mode group size, ring depth and
     wave count for bf16 CP-ALS of the f32 CUDA tensor ``x`` at ``rank`` by a
     coordinate search over ``DENSE_SPACE`` (the defaults first); a value

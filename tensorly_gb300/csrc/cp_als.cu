@@ -711,7 +711,7 @@ extern "C" void tlgb_cp_als_default_options(tlgb_cp_als_options* o) {
   o->normalize_factors = 0;
   o->fixed_modes = 0;
   o->precision = TLGB_PREC_NATIVE;
-  o->refine_sweeps = 3;
+  o->refine_sweeps = 1;
   o->check_every = 8;
   o->use_graph = 0;
   o->callback = nullptr;

@@ -115,7 +115,7 @@ def parafac(tensor, rank, n_iter_max=100, init="svd", svd="truncated_svd",
             normalize_factors=False, orthogonalise=False, tol=1e-8, random_state=None,
             verbose=0, return_errors=False, sparsity=None, l2_reg=0, mask=None,
             cvg_criterion="abs_rec_error", fixed_modes=None, svd_mask_repeats=5,
-            linesearch=False, callback=None, *, precision="native", refine_sweeps=3,
+            linesearch=False, callback=None, *, precision="native", refine_sweeps=1,
             check_every=8, use_graph=False, mttkrp_times=None):
     """CP decomposition by ALS (tensorly/decomposition/_cp.py:230-543).
 

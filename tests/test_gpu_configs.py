@@ -75,23 +75,30 @@ def test_c2_f64_two_sweeps_match_oracle(gb300, c2):
 
 
 def test_c2_bf16_50_sweeps_reach_f64_fit(gb300, c2):
+    """The 512^3 rank-64 workload, 50 sweeps from the same start: bf16 sweeps
+    with one closing f32 sweep (the default) and with three reach the f64
+    run's final error and factors."""
     x, init = c2
     xt = torch.from_numpy(x).cuda()
     it = [torch.from_numpy(a).cuda() for a in init]
-    (w, f), errs = gb300.parafac(xt, 64, init=gb300.CPTensor((None, it)), n_iter_max=50, tol=0,
-                                 precision="bf16", refine_sweeps=3, return_errors=True)
+    runs = {}
+    for refine in (1, 3):
+        runs[refine] = gb300.parafac(xt, 64, init=gb300.CPTensor((None, [a.clone() for a in it])),
+                                     n_iter_max=50, tol=0, precision="bf16",
+                                     refine_sweeps=refine, return_errors=True)
     x64 = xt.double()
     del xt
     (w64, f64), errs64 = gb300.parafac(x64, 64, init=gb300.CPTensor((None, [a.double() for a in it])),
                                        n_iter_max=50, tol=0, return_errors=True)
     del x64
-    assert len(errs) == len(errs64) == 50
-    d = abs(errs[-1] - errs64[-1]) / errs64[-1]
-    cong = congruence([a.double().cpu().numpy() for a in f], [a.cpu().numpy() for a in f64])
-    print(f"512^3 R64 bf16+3 f32 closing sweeps: final error {errs[-1]:.10f}, f64 "
-          f"{errs64[-1]:.10f}, relative difference {d:.2e}, congruence {cong:.6f}")
-    assert d < 1e-4
-    assert cong > 0.999
+    for refine, ((w, f), errs) in runs.items():
+        assert len(errs) == len(errs64) == 50
+        d = abs(errs[-1] - errs64[-1]) / errs64[-1]
+        cong = congruence([a.double().cpu().numpy() for a in f], [a.cpu().numpy() for a in f64])
+        print(f"512^3 R64 bf16 + {refine} f32 closing sweep(s): final error {errs[-1]:.10f}, f64 "
+              f"{errs64[-1]:.10f}, relative difference {d:.2e}, congruence {cong:.7f}")
+        assert d < 1e-4
+        assert cong > 0.999
 
 
 @pytest.fixture(scope="module")
