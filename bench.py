@@ -9,7 +9,8 @@ L2 flush is needed between steps.
 
 Arms:
   default            tensorly_gb300 on the GPU (precision bf16 = tensor-core
-                     MTTKRP + 3 closing f32 sweeps, or --precision native)
+                     MTTKRP + 1 closing f32 sweep, --refine N for N, or
+                     --precision native)
   --impl reference   the NumPy restatement of TensorLy's CPU path (oracle/)
                      on the host cores, a bounded sample of sweeps per step
 
